@@ -1,0 +1,367 @@
+"""Benchmark of the GB300 MPPI engine: MPPI iterations/s and sample-steps/s on one GPU.
+
+A step is one MPPI iteration (sample -> rollout -> weights -> update) over every instance of the workload.
+* value — sample-steps/s of device-resident solves (inputs already in HBM; mppi_enqueue_solve), timed with CUDA events
+  on the engine's stream; max over ranks; whole-job aggregate.
+* e2e   — the same metric through the public computeControl call with host buffers: the H2D copy of the initial
+  states and nominal controls, the device work, the D2H copy of the result and the host post-processing are inside
+  the timed region every step.
+* roofline — the dominant kernel's algorithmic bytes per launch / its CUDA-event duration, against the measured HBM
+  copy bandwidth.
+* cpu_baseline — the CPU oracle (a restatement of the reference's host rollout + weight + update path) on a bounded
+  sample of the same workload, all host threads.
+
+Multi-GPU: the path does not shard across GPUs; ``--gpus N`` under torchrun runs N independent replicas (weak scaling).
+``--impl reference`` times the reference's CPU path (the oracle port) and prints its own line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+METRIC = "MPPI sample-steps/s (iters/s x sum_i K_i*T_i) on 1 GB300"
+UNIT = "sample-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batched_di", choices=["batched_di", "cartpole", "bicycle",
+                                                                 "batched_di_gaussian"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        if shutil.which("nvidia-smi") is None:
+            return
+        self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                     stderr=subprocess.DEVNULL, text=True)
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names[1:], parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(name, seed, stream):
+    from mppi_generic_vendor_gb300 import workloads as W
+
+    if name == "batched_di":
+        return W.batched_di(seed=seed, colored=True, stream=stream)
+    if name == "batched_di_gaussian":
+        return W.batched_di(seed=seed, colored=False, stream=stream)
+    if name == "cartpole":
+        return W.cartpole(seed=seed, stream=stream)
+    return W.bicycle(seed=seed, stream=stream)
+
+
+def algorithmic_bytes(wl, colored: bool):
+    """Minimum HBM bytes per launch of each kernel (control samples are 4 B each, costs / weights 4 B per sample)."""
+    n = wl.control_floats
+    k = int(wl.K.sum())
+    spec = int(np.sum(wl.K.astype(np.int64) * (wl.T + 1))) * wl.control_dim * 2 if colored else 0
+    sampler = 4 * n  # write the constrained samples (Philox noise is generated in registers)
+    rollout = 4 * n + 4 * k  # read the samples, write the costs
+    update = 4 * n + 8 * k  # read the samples and costs, write the weights
+    del spec
+    return {"sampler": sampler, "rollout": rollout, "update": update}
+
+
+# ------------------------------------------------------------------------------------------------ CPU baseline
+def cpu_baseline(name, seed, budget_s):
+    """Time the CPU oracle (host rollout + weights + update, all threads) on a bounded sample of the workload."""
+    import oracle
+    from mppi_generic_vendor_gb300 import _abi as A
+    from mppi_generic_vendor_gb300 import workloads as W
+
+    threads = oracle.threads_default()
+    rng = np.random.default_rng(seed)
+    done_steps, elapsed, iters, inst_done = 0, 0.0, 0, 0
+    if name in ("batched_di", "batched_di_gaussian"):
+        colored = name == "batched_di"
+        Ks, Ts, costs, x0 = W.batched_di_params(seed)
+        cp = A.default_controller_params()
+        cp.dt, cp.lambda_, cp.num_iters = 0.02, 1.0, 1
+        sp = A.default_sampling_params()
+        sp.std_dev[0] = sp.std_dev[1] = 0.5
+        cc = A.default_constraints()
+        for i in range(2):
+            cc.lower[i], cc.upper[i] = -1.0, 1.0
+        dyn = A.DoubleIntegratorParams(0.0)
+        i = 0
+        while elapsed < budget_s and i < len(Ks):
+            K, T = int(Ks[i]), int(Ts[i])
+            t0 = time.perf_counter()
+            if colored:
+                spec = rng.standard_normal(K * 2 * (T + 1) * 2).astype(np.float32)
+                eps = oracle.colored_noise(spec, K, T, 2, [1.0, 1.0], decay=0.97, offset_t=1, threads=threads)
+            else:
+                eps = rng.standard_normal(K * T * 2).astype(np.float32)
+            oracle.compute_control(A.MODEL_DOUBLE_INTEGRATOR, dyn, costs[i].getParams(), cp, sp, cc, K, T, 2, 4,
+                                   x0[4 * i:4 * i + 4], eps, np.zeros((T, 2), np.float32), threads=threads)
+            elapsed += time.perf_counter() - t0
+            done_steps += K * T
+            i += 1
+        inst_done = i
+        sample = f"{inst_done} of 256 instances (sum K*T = {done_steps}), one iteration each"
+    else:
+        wl_k, wl_t = (2048, 100) if name == "cartpole" else (16384, 100)
+        if name == "cartpole":
+            model, S, Cd = A.MODEL_CARTPOLE, 4, 1
+            dyn, cost = A.CartpoleParams(1, 1, 1, 9.81), A.CartpoleCostParams(10, 1, 100, 1, 0)
+            cmap = None
+            lam, std = 1.0, (1.0,)
+            lo, hi = [(-5.0, 5.0)], None
+            x0 = np.array([0.0, 0.0, 1.0, 0.0], np.float32)
+        else:
+            model, S, Cd = A.MODEL_BICYCLE_COSTMAP, 4, 2
+            dyn, cost = A.BicycleParams(2.5), A.CostmapCostParams(1.0, 8.0, 1.0, 0.0, 0.0)
+            cmap = (W.gaussian_bump_costmap(seed), 0.1, (0.0, 0.0))
+            lam, std = 2.0, (1.0, 0.3)
+            lo = [(-3.0, 3.0), (-1.0, 1.0)]
+            x0 = np.array([25.0, 25.0, 0.3, 4.0], np.float32)
+        cp = A.default_controller_params()
+        cp.dt, cp.lambda_, cp.num_iters = 0.02, lam, 1
+        sp = A.default_sampling_params()
+        for i, s in enumerate(std):
+            sp.std_dev[i] = s
+        cc = A.default_constraints()
+        for i, (a, b) in enumerate(lo):
+            cc.lower[i], cc.upper[i] = a, b
+        u = np.zeros((wl_t, Cd), np.float32)
+        while elapsed < budget_s and iters < 200:
+            eps = rng.standard_normal(wl_k * wl_t * Cd).astype(np.float32)
+            t0 = time.perf_counter()
+            r = oracle.compute_control(model, dyn, cost, cp, sp, cc, wl_k, wl_t, Cd, S, x0, eps, u, costmap=cmap,
+                                       threads=threads)
+            elapsed += time.perf_counter() - t0
+            u = r["control"]
+            done_steps += wl_k * wl_t
+            iters += 1
+        sample = f"{iters} MPPI iterations of K={wl_k}, T={wl_t}"
+    return {"value": done_steps / elapsed, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+            "seconds": round(elapsed, 3)}
+
+
+# ------------------------------------------------------------------------------------------------ GPU arm
+def run_gpu(args, ws, rank, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from mppi_generic_vendor_gb300 import build as B
+
+    B.build()
+    stream = torch.cuda.Stream()
+    wl = build_workload(args.workload, seed=0, stream=stream.cuda_stream)
+    ctrl = wl.controller
+    colored = args.workload == "batched_di"
+    x0 = wl.x0
+    # ---------------- device-resident throughput
+    ctrl.computeControl(x0, 1)  # uploads x0 and the nominal controls, builds the graphs
+    ctrl.enqueueSolve(1, max(args.warmup, 3))
+    ctrl.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        ctrl.enqueueSolve(1, args.steps)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    steps_per_iter = wl.sample_steps_per_iter
+    iters = args.steps * wl.num_iters
+    value = ws * steps_per_iter * iters / (ms / 1e3)
+    iters_per_s = iters / (ms / 1e3)
+    kernels = ctrl.kernelsPerCompute()
+    # ---------------- per-kernel timing and roofline
+    kms = ctrl.timeKernels(1, reps=max(3, min(10, args.steps)))
+    names = ["sampler", "rollout", "update"]
+    abytes = algorithmic_bytes(wl, colored)
+    dom = int(np.argmax(kms))
+    peak, peak_kind = measured_peaks()
+    achieved = abytes[names[dom]] / (kms[dom] * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "dram_traffic.json"
+    if tfile.exists():
+        try:
+            tj = json.loads(tfile.read_text())
+            ent = tj.get(wl.name, {}).get(names[dom])
+            if ent:
+                traffic = float(ent["bytes_per_unit"]) * (wl.control_floats if ent["unit"] == "control_float"
+                                                          else steps_per_iter)
+        except Exception:
+            traffic = None
+    # ---------------- end to end through computeControl with host buffers
+    for _ in range(max(args.warmup, 3)):
+        ctrl.computeControlFlat(x0, 1)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctrl.computeControlFlat(x0, 1)
+        u = ctrl.control_flat()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = ws * steps_per_iter * iters / e2e_s
+    n_inst = wl.controller.num_instances
+    h2d = 4 * (n_inst * wl.state_dim + int(np.sum(wl.T)) * wl.control_dim)
+    d2h = 4 * int(np.sum(wl.T)) * wl.control_dim + 8 * n_inst + 24 * n_inst + u.nbytes
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded; shapes of the benchmark configuration)",
+        "config": {"workload": wl.name, **wl.description, "num_iters": wl.num_iters,
+                   "sample_steps_per_iter": steps_per_iter,
+                   "l2": ("inputs larger than L2 (samples buffer %.0f MB)" % (wl.control_floats * 4 / 1e6))
+                   if wl.control_floats * 4 > 129e6 else
+                   "working set %.1f MB fits in L2; device-resident value is L2-warm" % (wl.control_floats * 4 / 1e6),
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "iters_per_s": iters_per_s,
+        "kernel_ms": {n: float(v) for n, v in zip(names, kms)},
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes": abytes[names[dom]]},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "iters_per_s": ws * iters / e2e_s},
+        "gpu_launches": kernels * args.steps,
+    }
+    if clk:
+        line["clocks"] = clk
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.workload, 0, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctrl.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_baseline(args.workload, 0, per_step)
+    vals = []
+    t0 = time.perf_counter()
+    last = None
+    for _ in range(args.steps):
+        last = cpu_baseline(args.workload, 0, per_step)
+        vals.append(last["value"])
+    total = time.perf_counter() - t0
+    v = float(np.mean(vals))
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; shapes of the benchmark configuration)",
+            "config": {"workload": args.workload}, "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": "port",
+                             "sample": last["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,336 @@
+/*
+ * mppi_gb.h — C ABI of the GB300-native MPPI engine (libmppi_gb.so).
+ *
+ * The engine stands in for MPPI-Generic's plain MPPI path: a VanillaMPPIController built from a Dynamics plugin,
+ * a Cost plugin and a Gaussian or colored-noise SamplingDistribution.  Every entry point below names the reference
+ * interface it replaces (paths relative to the MPPI-Generic source tree).
+ *
+ * Conventions
+ *  - Every function returns an mppi_status; none calls exit() or throws across the ABI (the reference exits the
+ *    process from HANDLE_ERROR, include/mppi/utils/gpu_err_chk.cuh:32-40).  mppi_last_error_string() explains the
+ *    most recent failure on the calling thread.
+ *  - Plain pointers and sizes only.  "host" pointers are ordinary CPU memory; "device" pointers are CUDA global
+ *    memory on the current device.  Streams are passed as void* (a cudaStream_t).
+ *  - Control sequences are float[T][C] (time-major, control innermost), which is the memory order of the reference's
+ *    column-major Eigen control_trajectory (C x MAX_T).  Control samples are float[K][T][C] per instance, the
+ *    reference's control_samples_d_ layout (sampling_distribution.cu:108-116).
+ *  - A handle owns all of its device memory and is not thread-safe: use one handle per thread.
+ *  - A handle holds num_instances independent controllers (each with its own K, T, plugin parameters, nominal
+ *    control and state).  num_instances == 1 is the reference's single VanillaMPPIController.  Arrays that take
+ *    "all instances" are the concatenation over instances in index order.
+ */
+#ifndef MPPI_GB_H
+#define MPPI_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPPI_GB_ABI_VERSION 1
+#define MPPI_MAX_STATE_DIM 8
+#define MPPI_MAX_CONTROL_DIM 4
+#define MPPI_MAX_OBSTACLES 8
+
+typedef enum mppi_status
+{
+  MPPI_OK = 0,
+  MPPI_EINVAL = 1,      /* bad argument, size or parameter (reference: precondition exit(), mppi_common.cu:1302-1313) */
+  MPPI_ECUDA = 2,       /* a CUDA runtime call failed (reference: HANDLE_ERROR exit) */
+  MPPI_ENAN = 3,        /* non-finite input state, noise or baseline cost */
+  MPPI_ETIMEOUT = 4,    /* a bounded device-side wait gave up */
+  MPPI_ENOMEM = 5,      /* device or host allocation failed */
+  MPPI_EUNSUPPORTED = 6 /* model / sampler combination not built */
+} mppi_status;
+
+/* Concrete plugin pairs (Dynamics + Cost) compiled into the library. */
+typedef enum mppi_model
+{
+  MPPI_MODEL_CARTPOLE = 1,            /* CartpoleDynamics (cartpole_dynamics.cu:87-105) + swing-up cost */
+  MPPI_MODEL_DOUBLE_INTEGRATOR = 2,   /* DoubleIntegratorDynamics (di_dynamics.cu:46-53) + goal/obstacle cost */
+  MPPI_MODEL_BICYCLE_COSTMAP = 3,     /* kinematic bicycle + bilinear costmap + speed cost (no reference model) */
+  MPPI_MODEL_BICYCLE_SLIP = 4,        /* 7-state dynamic bicycle with linear tyres (no reference model) */
+  MPPI_MODEL_BICYCLE_SLIP_MLP = 5     /* same cost, dynamics from the learned MLP surrogate */
+} mppi_model;
+
+typedef enum mppi_sampler_kind
+{
+  MPPI_SAMPLER_GAUSSIAN = 0,      /* GaussianDistributionImpl (gaussian.cuh:98) */
+  MPPI_SAMPLER_COLORED_NOISE = 1  /* ColoredNoiseDistributionImpl (colored_noise.cuh:79) */
+} mppi_sampler_kind;
+
+/* ControllerParams (include/mppi/controllers/controller.cuh:46-68).  Block dimensions are chosen by the engine. */
+typedef struct mppi_controller_params
+{
+  float dt;
+  float lambda;
+  float alpha;
+  int num_timesteps; /* T; per-instance values for batches are passed separately */
+  int num_iters;     /* optimisation iterations per computeControl */
+  uint64_t seed;     /* Philox key */
+  float slide_control_scale[MPPI_MAX_CONTROL_DIM];
+} mppi_controller_params;
+
+/* GaussianParamsImpl (gaussian.cuh:21-61) and ColoredNoiseParamsImpl (colored_noise.cuh:44-73). */
+typedef struct mppi_sampling_params
+{
+  int kind; /* mppi_sampler_kind */
+  float std_dev[MPPI_MAX_CONTROL_DIM];
+  float control_cost_coeff[MPPI_MAX_CONTROL_DIM];
+  float pure_noise_trajectories_percentage; /* default 0.01 */
+  float std_dev_decay;                      /* default 1.0 */
+  float exponents[MPPI_MAX_CONTROL_DIM];    /* colored noise: PSD ~ 1/f^exponent */
+  float offset_decay_rate;                  /* colored noise, default 0.97 */
+  float fmin;                               /* colored noise low-frequency cutoff, default 0 */
+} mppi_sampling_params;
+
+/* Dynamics::control_rngs_, control_deadband_, zero_control_ (dynamics.cuh:508; dynamics.cu:107-126). */
+typedef struct mppi_control_constraints
+{
+  float lower[MPPI_MAX_CONTROL_DIM];
+  float upper[MPPI_MAX_CONTROL_DIM];
+  float deadband[MPPI_MAX_CONTROL_DIM];
+  float zero_control[MPPI_MAX_CONTROL_DIM];
+} mppi_control_constraints;
+
+/* ---- plugin parameter blocks ------------------------------------------------------------------------------------ */
+
+/* CartpoleDynamicsParams (cartpole_dynamics.cuh); gravity is the reference's gravity_ = 9.81 constant. */
+typedef struct mppi_cartpole_params
+{
+  float cart_mass;
+  float pole_mass;
+  float pole_length;
+  float gravity;
+} mppi_cartpole_params;
+
+/* Swing-up cost: x_coeff*x^2 + x_dot_coeff*xdot^2 + cos_coeff*(1+cos theta)^2 + theta_dot_coeff*thetadot^2,
+ * terminal cost = terminal_coeff * (same expression).  Same API as CartpoleQuadraticCost
+ * (cartpole_quadratic_cost.cu:20-43). */
+typedef struct mppi_cartpole_cost_params
+{
+  float x_coeff;
+  float x_dot_coeff;
+  float cos_coeff;
+  float theta_dot_coeff;
+  float terminal_coeff;
+} mppi_cartpole_cost_params;
+
+/* DoubleIntegratorDynamics has no parameters on the MPPI path (di_dynamics.cu:46-53). */
+typedef struct mppi_double_integrator_params
+{
+  float reserved;
+} mppi_double_integrator_params;
+
+/* Quadratic-to-goal cost (QuadraticCostImpl, quadratic_cost.cu:35-48) plus obstacle_cost when the position lies
+ * strictly inside any circle (composed like DoubleIntegratorCircleCost, double_integrator_circle_cost.cu:8-32). */
+typedef struct mppi_di_obstacle_cost_params
+{
+  float goal[4];
+  float coeff[4];
+  float terminal_coeff;
+  int num_obstacles;
+  float obstacle_x[MPPI_MAX_OBSTACLES];
+  float obstacle_y[MPPI_MAX_OBSTACLES];
+  float obstacle_radius[MPPI_MAX_OBSTACLES];
+  float obstacle_cost;
+} mppi_di_obstacle_cost_params;
+
+/* Kinematic bicycle: state (x, y, yaw, v), control (accel, steer).  Closest reference: DubinsDynamics
+ * (dubins.cu:60-65). */
+typedef struct mppi_bicycle_params
+{
+  float wheelbase;
+} mppi_bicycle_params;
+
+/* Costmap cost: map_coeff * bilinear(map, x, y) + speed_coeff * (v - speed_target)^2.  The map itself is uploaded with
+ * mppi_set_costmap().  Replaces the TwoDTextureHelper query (two_d_texture_helper.cu:66-72, CPU twin :151). */
+typedef struct mppi_costmap_cost_params
+{
+  float map_coeff;
+  float speed_target;
+  float speed_coeff;
+  float steer_coeff;
+  float terminal_coeff;
+} mppi_costmap_cost_params;
+
+/* Dynamic bicycle with linear tyres: state (x, y, yaw, vx, vy, yaw_rate, steer), control (throttle, steer_cmd). */
+typedef struct mppi_bicycle_slip_params
+{
+  float mass;
+  float yaw_inertia;
+  float lf;
+  float lr;
+  float cornering_stiffness;
+  float max_drive_force;
+  float drag;
+  float max_steer;
+  float steer_time_constant;
+  float min_vx;
+} mppi_bicycle_slip_params;
+
+/* ---- controller handle (Controller / VanillaMPPIController, controller.cuh:70-1058, mppi_controller.cuh:14-78) --- */
+
+typedef struct mppi_handle mppi_handle;
+
+/* Version and build information. */
+int mppi_abi_version(void);
+/* Dims of a model: writes STATE_DIM, CONTROL_DIM, OUTPUT_DIM (Dynamics::STATE_DIM etc., dynamics.cuh:75-77). */
+mppi_status mppi_model_dims(int model, int* state_dim, int* control_dim, int* output_dim);
+/* Size in bytes of the dynamics / cost parameter blocks a model expects. */
+mppi_status mppi_model_param_sizes(int model, size_t* dyn_bytes, size_t* cost_bytes);
+/* Reference defaults: ControllerParams, GaussianParamsImpl/ColoredNoiseParamsImpl, and unbounded constraints. */
+void mppi_default_controller_params(mppi_controller_params* p);
+void mppi_default_sampling_params(mppi_sampling_params* p);
+void mppi_default_constraints(mppi_control_constraints* c);
+
+/* Message describing the last failure on this thread ("" if none). */
+const char* mppi_last_error_string(void);
+
+/*
+ * Create a controller holding num_instances independent MPPI problems.
+ * Replaces the VanillaMPPIController constructor (mppi_controller.cu:16-29 -> Controller::Controller,
+ * controller.cuh:111-153).  num_rollouts[i] / num_timesteps[i] give K_i and T_i; dyn_params and cost_params point to
+ * num_instances consecutive parameter blocks of dyn_bytes / cost_bytes each (sizes from mppi_model_param_sizes).
+ * init_control (may be NULL = zeros) holds the concatenated initial control sequences.  stream may be NULL, in which
+ * case the handle creates its own non-blocking stream.
+ */
+mppi_status mppi_create(int model, int num_instances, const int* num_rollouts, const int* num_timesteps,
+                        const mppi_controller_params* params, const mppi_sampling_params* sampling,
+                        const mppi_control_constraints* constraints, const void* dyn_params, size_t dyn_bytes,
+                        const void* cost_params, size_t cost_bytes, const float* init_control, void* stream,
+                        mppi_handle** out);
+/* Frees every device and host resource (Controller::~Controller -> freeCudaMem, controller.cuh:196-218). */
+mppi_status mppi_destroy(mppi_handle* h);
+
+/* Number of instances, and K / T of instance i. */
+mppi_status mppi_get_instance_dims(const mppi_handle* h, int instance, int* num_rollouts, int* num_timesteps);
+
+/*
+ * One MPC solve for every instance: num_iters x (sample -> rollout -> weights -> update), then the host-side
+ * Savitzky-Golay smoothing, nominal state rollout and control clamp.  x0 is host float[num_instances][STATE_DIM].
+ * Replaces VanillaMPPIController::computeControl(state, optimization_stride) (mppi_controller.cu:152-237).
+ */
+mppi_status mppi_compute_control(mppi_handle* h, const float* x0, int optimization_stride);
+
+/* Nominal control sequences, host float[sum_i T_i * C].  Controller::getControlSeq (controller.cuh:425-428). */
+mppi_status mppi_get_control_seq(mppi_handle* h, float* out);
+/* Overwrite the nominal control sequences (ControllerParams::init_control_traj_ / setParams, controller.cuh:857-876). */
+mppi_status mppi_set_control_seq(mppi_handle* h, const float* in);
+/* Shift every instance's sequence by steps (Controller::slideControlSequence, controller.cuh:370-376, 609-636). */
+mppi_status mppi_slide_control_sequence(mppi_handle* h, int steps);
+/* Nominal state trajectories, host float[sum_i T_i * STATE_DIM] (Controller::getTargetStateSeq, controller.cuh:433). */
+mppi_status mppi_get_state_seq(mppi_handle* h, float* out);
+/* Baseline (min cost) and normaliser (sum of exp weights) of the last iteration, host float[2 * num_instances]
+ * as (baseline, normaliser) pairs (Controller::getBaselineCost / getNormalizerCost, controller.cuh:526-533).
+ * The normaliser is accumulated in double on the device; normalizer_fp64 (may be NULL) receives it unrounded. */
+mppi_status mppi_get_baseline_normalizer(mppi_handle* h, float* out, double* normalizer_fp64);
+/* Per-sample trajectory costs before the weight transform, host float[sum_i K_i]. */
+mppi_status mppi_get_sample_costs(mppi_handle* h, float* out);
+/* Per-sample unnormalised weights exp(-(c - baseline)/lambda), host float[sum_i K_i].  This is what the reference's
+ * Controller::getSampledCostSeq returns after an iteration (controller.cuh:449-452; the array is transformed in
+ * place by fullGPUcomputeWeights, mppi_common.cu:1067-1089). */
+mppi_status mppi_get_sample_weights(mppi_handle* h, float* out);
+/* Control samples of the last iteration after the constraints were applied, host float[sum_i K_i*T_i*C].
+ * SamplingDistribution::getControlSample (sampling_distribution.cuh:234-236). */
+mppi_status mppi_get_control_samples(mppi_handle* h, float* out);
+/* Free-energy statistics of instance i (MPPIFreeEnergyStatistics, controller.cuh:22-38; computeFreeEnergy,
+ * mppi_common.cu:1101-1117): out[0..5] = mean, variance, modified variance, normaliser percent, increase,
+ * previous baseline. */
+mppi_status mppi_get_free_energy(mppi_handle* h, int instance, float* out6);
+
+/* Replace the model parameters of every instance (Dynamics::setParams / Cost::setParams). */
+mppi_status mppi_set_dynamics_params(mppi_handle* h, const void* dyn_params, size_t dyn_bytes);
+mppi_status mppi_set_cost_params(mppi_handle* h, const void* cost_params, size_t cost_bytes);
+/* Replace the sampling parameters (Controller::setSamplingParams, controller.cuh:852). */
+mppi_status mppi_set_sampling_params(mppi_handle* h, const mppi_sampling_params* sampling);
+/* Set lambda / alpha / num_iters / dt / slide scale (Controller::setParams, controller.cuh:857-876). */
+mppi_status mppi_set_controller_params(mppi_handle* h, const mppi_controller_params* params);
+
+/* Costmap for MPPI_MODEL_BICYCLE_COSTMAP / BICYCLE_SLIP*: row-major float[height][width], cell (0,0) centred at
+ * (origin_x + resolution/2, origin_y + resolution/2).  All instances share one map. */
+mppi_status mppi_set_costmap(mppi_handle* h, const float* map, int width, int height, float resolution,
+                             float origin_x, float origin_y);
+
+/* Surrogate weights for MPPI_MODEL_BICYCLE_SLIP_MLP: 9->64->64->5 tanh MLP, fp32 row-major W1[64][9], b1[64],
+ * W2[64][64], b2[64], W3[5][64], b3[5] (FNNHelper layout, fnn_helper.cu:353-382), plus input / output scaling.
+ * precision 0 = bf16 weights, 1 = fp8 e4m3 with one scale per layer. */
+mppi_status mppi_set_mlp(mppi_handle* h, const float* params, size_t num_params, int precision);
+
+/*
+ * Parity hook: use the given standard-normal noise for every subsequent iteration instead of Philox noise.
+ * Gaussian: host float[sum_i K_i*T_i*C], the epsilon that curandGenerateNormal writes before setGaussianControls
+ * (gaussian.cu:375-431).  Colored noise: host float[sum_i K_i*C*(T_i+1)*2], the complex spectrum before
+ * configureFrequencyNoise (colored_noise.cu:343).  noise == NULL clears the injection.
+ */
+mppi_status mppi_inject_noise(mppi_handle* h, const float* noise, size_t count);
+
+/* Run only the sampler of iteration iteration_num (SamplingDistribution::generateSamples, gaussian.cu:375-431 /
+ * colored_noise.cu:285-392); the result is readable with mppi_get_control_samples. */
+mppi_status mppi_generate_samples(mppi_handle* h, int optimization_stride, int iteration_num);
+
+/* 1 = record each computeControl as a CUDA graph and replay it (default), 0 = plain stream launches. */
+mppi_status mppi_set_graph_mode(mppi_handle* h, int enable);
+/* Choose launch shapes by timing candidates on the device; cache_path (may be NULL) is a JSON file that stores and
+ * restores the choice per (model, instance shape) key. */
+mppi_status mppi_autotune(mppi_handle* h, const char* cache_path);
+/* The launch shape in use: samples per rollout CTA, time chunk, samples per reduction CTA. */
+mppi_status mppi_get_launch_config(const mppi_handle* h, int* rollout_samples_per_cta, int* rollout_time_chunk,
+                                   int* reduction_samples_per_cta);
+mppi_status mppi_set_launch_config(mppi_handle* h, int rollout_samples_per_cta, int rollout_time_chunk,
+                                   int reduction_samples_per_cta);
+/* Number of kernels one computeControl launches (for launch accounting). */
+mppi_status mppi_kernels_per_compute(const mppi_handle* h, int* count);
+/* Enqueue `count` device-resident solves (num_iters x sample/rollout/update each, as one replayed CUDA graph) on the
+ * handle's stream without copying anything to or from the host and without synchronising: the initial states and
+ * nominal controls already on the device are reused and the nominal controls keep evolving on the device.  This is
+ * the steady-state GPU path of computeControl without its host round trip. */
+mppi_status mppi_enqueue_solve(mppi_handle* h, int optimization_stride, int count);
+/* Wait for the handle's stream. */
+mppi_status mppi_synchronize(mppi_handle* h);
+/* Average device time in ms of one launch of each kernel (ms_out[0] sampler, [1] rollout, [2] weights+update),
+ * measured with CUDA events on the handle's stream over `reps` iterations. */
+mppi_status mppi_time_kernels(mppi_handle* h, int optimization_stride, int reps, float* ms_out3);
+/* The stream the handle enqueues on (a cudaStream_t). */
+void* mppi_get_stream(const mppi_handle* h);
+
+/* ---- kernel-level entry points (mppi::kernels launchers, include/mppi/core/mppi_common.cuh:206-258) ----------- */
+
+/* baseline = min, w = exp(-(c - baseline) * lambda_inv) in place, normaliser = sum w; out2[2*s] = baseline,
+ * out2[2*s+1] = normaliser for each of num_systems arrays of num_rollouts costs (device pointers).
+ * Replaces launchWeightTransformKernel (mppi_common.cu:1483-1506).  Scratch is allocated per call. */
+mppi_status mppi_kernel_weight_transform(float* costs_d, float* out2_d, float lambda_inv, int num_rollouts,
+                                         int num_systems, void* stream);
+/* new_u[t][c] = sum_k (w_k / normaliser) u_k[t][c], normaliser read from baseline_norm_d[2*index+1] (device).
+ * Replaces launchWeightedReductionKernel, device-normaliser variant (mppi_common.cu:1438-1454).  Scratch is
+ * allocated per call. */
+mppi_status mppi_kernel_weighted_reduction(const float* weights_d, const float* controls_d, float* new_u_d,
+                                           const float* baseline_norm_d, int index, int num_timesteps,
+                                           int num_rollouts, int control_dim, void* stream);
+/* Rollout of K samples from x0 with the given (already constrained) controls, writing per-sample costs (device).
+ * Replaces launchRolloutKernel (mppi_common.cu:1335-1361).  mean_d (float[T*C]) feeds the likelihood-ratio term. */
+mppi_status mppi_kernel_rollout(int model, const void* dyn_params, size_t dyn_bytes, const void* cost_params,
+                                size_t cost_bytes, const mppi_sampling_params* sampling, const float* x0_d,
+                                const float* controls_d, const float* mean_d, float* costs_d, int num_rollouts,
+                                int num_timesteps, float dt, float lambda, float alpha, void* stream);
+/* In-place rewrite of standard-normal noise into control samples with constraints applied (setGaussianControls,
+ * gaussian.cu:17-277, followed by Dynamics::enforceConstraints, dynamics.cu:107-126). */
+mppi_status mppi_kernel_gaussian_controls(float* samples_d, const float* mean_d, const float* std_dev_h,
+                                          const mppi_control_constraints* constraints, int num_rollouts,
+                                          int num_timesteps, int control_dim, int optimization_stride,
+                                          float std_dev_decay_pow, float pure_noise_percentage, void* stream);
+/* Philox4x32-10 standard normals (Box-Muller) for n floats at counter offset, device output. */
+mppi_status mppi_kernel_philox_normal(float* out_d, size_t n, uint64_t seed, uint64_t offset, void* stream);
+/* Raw Philox4x32-10 blocks: out[4*i..4*i+3] = philox(ctr = {ctr0 + i, ctr1, ctr2, ctr3}, key), device output. */
+mppi_status mppi_kernel_philox_raw(uint32_t* out_d, size_t nblocks, const uint32_t ctr[4], const uint32_t key[2],
+                                   void* stream);
+/* The engine's single-precision sine/cosine evaluated on n inputs (device), for bit-level parity checks. */
+mppi_status mppi_kernel_sincos(const float* x_d, float* sin_d, float* cos_d, size_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPPI_GB_H */

@@ -1,0 +1,14 @@
+"""GB300-native MPPI engine with MPPI-Generic's plugin / controller interface.
+
+The compute path is libmppi_gb.so (hand-written sm_103a CUDA behind the C ABI in include/mppi_gb.h); this package is
+the host-side mirror of the reference's interface.  Build the library with ``python -m mppi_generic_vendor_gb300.build``.
+"""
+from . import _abi
+from ._abi import MPPIError
+from .controller import (BatchedMPPIController, BicycleDynamics, BicycleSlipDynamics, CartpoleDynamics,
+                         CartpoleSwingupCost, ColoredNoiseDistribution, CostmapCost, DoubleIntegratorDynamics,
+                         DoubleIntegratorObstacleCost, GaussianDistribution, VanillaMPPIController)
+
+__all__ = ["MPPIError", "BatchedMPPIController", "VanillaMPPIController", "CartpoleDynamics", "CartpoleSwingupCost",
+           "DoubleIntegratorDynamics", "DoubleIntegratorObstacleCost", "BicycleDynamics", "BicycleSlipDynamics",
+           "CostmapCost", "GaussianDistribution", "ColoredNoiseDistribution", "_abi"]

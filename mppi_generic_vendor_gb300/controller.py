@@ -1,0 +1,416 @@
+"""Host-side mirror of MPPI-Generic's plugin and controller interface over the C ABI.
+
+Names, argument meanings and shapes follow the reference so that code written against it reads the same:
+
+* plugins — ``CartpoleDynamics``, ``DoubleIntegratorDynamics``, ``BicycleDynamics``, ``BicycleSlipDynamics``
+  (Dynamics, include/mppi/dynamics/dynamics.cuh:68), the matching costs (Cost, cost_functions/cost.cuh:34) and
+  ``GaussianDistribution`` / ``ColoredNoiseDistribution`` (sampling_distributions/gaussian/gaussian.cuh:98,
+  colored_noise/colored_noise.cuh:79);
+* ``VanillaMPPIController`` (controllers/MPPI/mppi_controller.cuh:14) with ``computeControl``, ``getControlSeq``,
+  ``slideControlSequence``, ``getBaselineCost``, ``getNormalizerCost``, ``getSampledCostSeq``,
+  ``getTargetStateSeq``, ``setParams`` / ``getParams``;
+* ``BatchedMPPIController``: many independent controllers of one plugin pair, solved together on the GPU.
+
+Control and state sequences are returned as (C, T) / (S, T) arrays, the shape of the reference's column-major Eigen
+trajectories.  All compute runs in libmppi_gb.so; nothing here computes MPPI on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi as A
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+# ------------------------------------------------------------------------------------------------------ plugins
+class _Plugin:
+    model_id: int = 0
+
+    def __init__(self, params):
+        self.params_ = params
+
+    def getParams(self):
+        return self.params_
+
+    def setParams(self, params):
+        self.params_ = params
+
+
+class CartpoleDynamics(_Plugin):
+    """CartpoleDynamics(cart_mass, pole_mass, pole_length) (dynamics/cartpole/cartpole_dynamics.cu:4-8)."""
+
+    model_id = A.MODEL_CARTPOLE
+    STATE_DIM, CONTROL_DIM, OUTPUT_DIM = 4, 1, 4
+
+    def __init__(self, cart_mass=1.0, pole_mass=1.0, pole_length=1.0, gravity=9.81):
+        super().__init__(A.CartpoleParams(cart_mass, pole_mass, pole_length, gravity))
+        self.control_rngs = [(-np.finfo(np.float32).max, np.finfo(np.float32).max)]
+
+    def setControlRanges(self, ranges):
+        self.control_rngs = [tuple(r) for r in ranges]
+
+
+class CartpoleSwingupCost(_Plugin):
+    """x_coeff x^2 + x_dot_coeff xdot^2 + cos_coeff (1 + cos theta)^2 + theta_dot_coeff thetadot^2."""
+
+    def __init__(self, x_coeff=10.0, x_dot_coeff=1.0, cos_coeff=100.0, theta_dot_coeff=1.0, terminal_coeff=0.0):
+        super().__init__(A.CartpoleCostParams(x_coeff, x_dot_coeff, cos_coeff, theta_dot_coeff, terminal_coeff))
+
+
+class DoubleIntegratorDynamics(_Plugin):
+    """DoubleIntegratorDynamics (dynamics/double_integrator/di_dynamics.cu:46-53)."""
+
+    model_id = A.MODEL_DOUBLE_INTEGRATOR
+    STATE_DIM, CONTROL_DIM, OUTPUT_DIM = 4, 2, 4
+
+    def __init__(self):
+        super().__init__(A.DoubleIntegratorParams(0.0))
+        self.control_rngs = [(-np.finfo(np.float32).max, np.finfo(np.float32).max)] * 2
+
+    def setControlRanges(self, ranges):
+        self.control_rngs = [tuple(r) for r in ranges]
+
+
+class DoubleIntegratorObstacleCost(_Plugin):
+    """Weighted squared error to a goal state plus obstacle_cost inside any of up to 8 circles."""
+
+    def __init__(self, goal=(0, 0, 0, 0), coeff=(1, 1, 0.1, 0.1), terminal_coeff=0.0, obstacles=(),
+                 obstacle_cost=1000.0):
+        p = A.DIObstacleCostParams()
+        p.goal[:] = [float(v) for v in goal]
+        p.coeff[:] = [float(v) for v in coeff]
+        p.terminal_coeff = terminal_coeff
+        obstacles = list(obstacles)
+        if len(obstacles) > A.MPPI_MAX_OBSTACLES:
+            raise ValueError(f"at most {A.MPPI_MAX_OBSTACLES} obstacles")
+        p.num_obstacles = len(obstacles)
+        for j, (x, y, r) in enumerate(obstacles):
+            p.obstacle_x[j], p.obstacle_y[j], p.obstacle_radius[j] = x, y, r
+        p.obstacle_cost = obstacle_cost
+        super().__init__(p)
+
+
+class BicycleDynamics(_Plugin):
+    """Kinematic bicycle: state (x, y, yaw, v), control (accel, steer)."""
+
+    model_id = A.MODEL_BICYCLE_COSTMAP
+    STATE_DIM, CONTROL_DIM, OUTPUT_DIM = 4, 2, 4
+
+    def __init__(self, wheelbase=2.5):
+        super().__init__(A.BicycleParams(wheelbase))
+        self.control_rngs = [(-3.0, 3.0), (-1.0, 1.0)]
+
+    def setControlRanges(self, ranges):
+        self.control_rngs = [tuple(r) for r in ranges]
+
+
+class BicycleSlipDynamics(_Plugin):
+    """Dynamic bicycle with linear tyres: state (x, y, yaw, vx, vy, yaw_rate, steer), control (throttle, steer_cmd)."""
+
+    model_id = A.MODEL_BICYCLE_SLIP
+    STATE_DIM, CONTROL_DIM, OUTPUT_DIM = 7, 2, 7
+
+    def __init__(self, mass=1500.0, yaw_inertia=2500.0, lf=1.2, lr=1.3, cornering_stiffness=8e4,
+                 max_drive_force=4000.0, drag=50.0, max_steer=0.5, steer_time_constant=0.1, min_vx=1.0):
+        super().__init__(A.BicycleSlipParams(mass, yaw_inertia, lf, lr, cornering_stiffness, max_drive_force, drag,
+                                             max_steer, steer_time_constant, min_vx))
+        self.control_rngs = [(-1.0, 1.0), (-1.0, 1.0)]
+
+    def setControlRanges(self, ranges):
+        self.control_rngs = [tuple(r) for r in ranges]
+
+
+class CostmapCost(_Plugin):
+    """map_coeff * bilinear(costmap, x, y) + speed_coeff (v - speed_target)^2 + steer_coeff steer^2."""
+
+    def __init__(self, map_coeff=1.0, speed_target=8.0, speed_coeff=1.0, steer_coeff=0.0, terminal_coeff=0.0,
+                 costmap=None, resolution=0.1, origin=(0.0, 0.0)):
+        super().__init__(A.CostmapCostParams(map_coeff, speed_target, speed_coeff, steer_coeff, terminal_coeff))
+        self.costmap = None if costmap is None else np.ascontiguousarray(costmap, dtype=np.float32)
+        self.resolution = float(resolution)
+        self.origin = (float(origin[0]), float(origin[1]))
+
+
+@dataclass
+class GaussianDistribution:
+    """GaussianDistributionImpl parameters (sampling_distributions/gaussian/gaussian.cuh:21-61)."""
+
+    std_dev: tuple = (1.0,)
+    control_cost_coeff: tuple = (0.0,)
+    pure_noise_trajectories_percentage: float = 0.01
+    std_dev_decay: float = 1.0
+    kind: int = field(default=A.SAMPLER_GAUSSIAN, init=False)
+
+    def to_c(self) -> A.SamplingParams:
+        p = A.default_sampling_params()
+        p.kind = self.kind
+        for i, v in enumerate(self.std_dev):
+            p.std_dev[i] = v
+        for i, v in enumerate(self.control_cost_coeff):
+            p.control_cost_coeff[i] = v
+        p.pure_noise_trajectories_percentage = self.pure_noise_trajectories_percentage
+        p.std_dev_decay = self.std_dev_decay
+        return p
+
+
+@dataclass
+class ColoredNoiseDistribution(GaussianDistribution):
+    """ColoredNoiseDistributionImpl parameters (sampling_distributions/colored_noise/colored_noise.cuh:44-73)."""
+
+    exponents: tuple = (1.0,)
+    offset_decay_rate: float = 0.97
+    fmin: float = 0.0
+
+    def __post_init__(self):
+        self.kind = A.SAMPLER_COLORED_NOISE
+
+    def to_c(self) -> A.SamplingParams:
+        p = super().to_c()
+        for i, v in enumerate(self.exponents):
+            p.exponents[i] = v
+        p.offset_decay_rate = self.offset_decay_rate
+        p.fmin = self.fmin
+        return p
+
+
+# ------------------------------------------------------------------------------------------------ controllers
+class BatchedMPPIController:
+    """Many independent VanillaMPPIControllers of one plugin pair, solved by one set of GPU launches.
+
+    ``dynamics`` / ``costs`` are one plugin object each or a list with one per instance; ``num_rollouts`` and
+    ``num_timesteps`` are per-instance sequences.  ``stream`` is a cudaStream_t as an int (0 = own stream).
+    """
+
+    def __init__(self, dynamics, costs, sampler, num_rollouts, num_timesteps, dt=0.02, max_iter=1, lambda_=1.0,
+                 alpha=0.0, seed=0, init_control_traj=None, stream=0, slide_control_scale=None):
+        self.num_instances = len(num_rollouts)
+        dyn_list = dynamics if isinstance(dynamics, (list, tuple)) else [dynamics] * self.num_instances
+        cost_list = costs if isinstance(costs, (list, tuple)) else [costs] * self.num_instances
+        if len(dyn_list) != self.num_instances or len(cost_list) != self.num_instances:
+            raise ValueError("one dynamics and one cost object per instance")
+        self.model_ = dyn_list[0]
+        self.cost_ = cost_list[0]
+        self.sampler_ = sampler
+        self.model_id = self.model_.model_id
+        self.S, self.Cdim = self.model_.STATE_DIM, self.model_.CONTROL_DIM
+        self.K = np.asarray(num_rollouts, dtype=np.int32)
+        self.T = np.asarray(num_timesteps, dtype=np.int32)
+        dyn_t, cost_t = A.MODEL_PARAM_TYPES[self.model_id]
+        self._dyn_arr = (dyn_t * self.num_instances)(*[d.getParams() for d in dyn_list])
+        self._cost_arr = (cost_t * self.num_instances)(*[c.getParams() for c in cost_list])
+        cp = A.default_controller_params()
+        cp.dt, cp.lambda_, cp.alpha, cp.num_iters, cp.seed = dt, lambda_, alpha, max_iter, seed
+        cp.num_timesteps = int(self.T.max())
+        if slide_control_scale is not None:
+            for i, v in enumerate(slide_control_scale):
+                cp.slide_control_scale[i] = v
+        self.params_ = cp
+        cc = A.default_constraints()
+        for i, (lo, hi) in enumerate(self.model_.control_rngs):
+            cc.lower[i], cc.upper[i] = lo, hi
+        self.constraints_ = cc
+        self._t_off = np.concatenate([[0], np.cumsum(self.T * self.Cdim)]).astype(np.int64)
+        self._s_off = np.concatenate([[0], np.cumsum(self.T * self.S)]).astype(np.int64)
+        self._k_off = np.concatenate([[0], np.cumsum(self.K)]).astype(np.int64)
+        init = None
+        if init_control_traj is not None:
+            init = np.ascontiguousarray(np.asarray(init_control_traj, dtype=np.float32).reshape(-1))
+            if init.size != self._t_off[-1]:
+                raise ValueError(f"init_control_traj must hold {self._t_off[-1]} floats")
+        h = C.c_void_p()
+        sp = sampler.to_c()
+        A.call("mppi_create", self.model_id, self.num_instances, self.K.ctypes.data_as(C.POINTER(C.c_int)),
+               self.T.ctypes.data_as(C.POINTER(C.c_int)), C.byref(cp), C.byref(sp), C.byref(cc),
+               C.cast(self._dyn_arr, C.c_void_p), C.sizeof(dyn_t), C.cast(self._cost_arr, C.c_void_p),
+               C.sizeof(cost_t), None if init is None else _fptr(init), C.c_void_p(stream or None), C.byref(h))
+        self._h = h
+        cm = getattr(self.cost_, "costmap", None)
+        if cm is not None:
+            self.setCostmap(cm, self.cost_.resolution, self.cost_.origin)
+
+    # ---- lifecycle
+    def close(self):
+        if getattr(self, "_h", None):
+            A.lib().mppi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- the hot path
+    def computeControl(self, state, optimization_stride=1):
+        """VanillaMPPIController::computeControl (controllers/MPPI/mppi_controller.cu:152-237) for all instances."""
+        x0 = np.ascontiguousarray(np.asarray(state, dtype=np.float32).reshape(-1))
+        if x0.size != self.num_instances * self.S:
+            raise ValueError(f"state must hold {self.num_instances * self.S} floats")
+        A.call("mppi_compute_control", self._h, _fptr(x0), int(optimization_stride))
+
+    def computeControlFlat(self, x0: np.ndarray, optimization_stride=1):
+        """computeControl without reshaping or copying (x0 must be contiguous float32)."""
+        A.call("mppi_compute_control", self._h, _fptr(x0), int(optimization_stride))
+
+    # ---- accessors (flat, all instances)
+    def control_flat(self) -> np.ndarray:
+        out = np.empty(int(self._t_off[-1]), dtype=np.float32)
+        A.call("mppi_get_control_seq", self._h, _fptr(out))
+        return out
+
+    def getControlSeqs(self):
+        flat = self.control_flat()
+        return [flat[self._t_off[i]:self._t_off[i + 1]].reshape(int(self.T[i]), self.Cdim).T.copy()
+                for i in range(self.num_instances)]
+
+    def setControlSeqs(self, seqs):
+        flat = np.concatenate([np.asarray(s, dtype=np.float32).T.reshape(-1) for s in seqs])
+        flat = np.ascontiguousarray(flat)
+        A.call("mppi_set_control_seq", self._h, _fptr(flat))
+
+    def slideControlSequence(self, steps):
+        """Controller::slideControlSequence (controllers/controller.cuh:370-376)."""
+        A.call("mppi_slide_control_sequence", self._h, int(steps))
+
+    def getTargetStateSeqs(self):
+        out = np.empty(int(self._s_off[-1]), dtype=np.float32)
+        A.call("mppi_get_state_seq", self._h, _fptr(out))
+        return [out[self._s_off[i]:self._s_off[i + 1]].reshape(int(self.T[i]), self.S).T.copy()
+                for i in range(self.num_instances)]
+
+    def baseline_normalizer(self):
+        out = np.empty(2 * self.num_instances, dtype=np.float32)
+        n64 = np.empty(self.num_instances, dtype=np.float64)
+        A.call("mppi_get_baseline_normalizer", self._h, _fptr(out), n64.ctypes.data_as(C.POINTER(C.c_double)))
+        return out.reshape(-1, 2), n64
+
+    def getBaselineCost(self, ind=0):
+        return float(self.baseline_normalizer()[0][ind, 0])
+
+    def getNormalizerCost(self, ind=0):
+        return float(self.baseline_normalizer()[0][ind, 1])
+
+    def sample_costs(self) -> np.ndarray:
+        out = np.empty(int(self._k_off[-1]), dtype=np.float32)
+        A.call("mppi_get_sample_costs", self._h, _fptr(out))
+        return out
+
+    def sample_weights(self) -> np.ndarray:
+        out = np.empty(int(self._k_off[-1]), dtype=np.float32)
+        A.call("mppi_get_sample_weights", self._h, _fptr(out))
+        return out
+
+    def control_samples(self) -> np.ndarray:
+        n = int(np.sum(self.K.astype(np.int64) * self.T * self.Cdim))
+        out = np.empty(n, dtype=np.float32)
+        A.call("mppi_get_control_samples", self._h, _fptr(out))
+        return out
+
+    def getFreeEnergyStatistics(self, ind=0):
+        out = np.empty(6, dtype=np.float32)
+        A.call("mppi_get_free_energy", self._h, int(ind), _fptr(out))
+        keys = ("freeEnergyMean", "freeEnergyVariance", "freeEnergyModifiedVariance", "normalizerPercent",
+                "increase", "previousBaseline")
+        return dict(zip(keys, map(float, out)))
+
+    # ---- parameters
+    def getParams(self):
+        return self.params_
+
+    def setParams(self, params: A.ControllerParams):
+        A.call("mppi_set_controller_params", self._h, C.byref(params))
+        self.params_ = params
+
+    def setSamplingParams(self, sampler):
+        sp = sampler.to_c()
+        A.call("mppi_set_sampling_params", self._h, C.byref(sp))
+        self.sampler_ = sampler
+
+    def setCostmap(self, costmap, resolution=0.1, origin=(0.0, 0.0)):
+        m = np.ascontiguousarray(costmap, dtype=np.float32)
+        A.call("mppi_set_costmap", self._h, _fptr(m), int(m.shape[1]), int(m.shape[0]), float(resolution),
+               float(origin[0]), float(origin[1]))
+
+    def injectNoise(self, noise):
+        """Parity hook: use this standard-normal noise (all instances, samples layout) instead of Philox noise."""
+        if noise is None:
+            A.call("mppi_inject_noise", self._h, None, 0)
+            return
+        n = np.ascontiguousarray(np.asarray(noise, dtype=np.float32).reshape(-1))
+        A.call("mppi_inject_noise", self._h, _fptr(n), n.size)
+        self._injected = n
+
+    def generateSamples(self, optimization_stride=1, iteration_num=0):
+        A.call("mppi_generate_samples", self._h, int(optimization_stride), int(iteration_num))
+
+    def setGraphMode(self, enable: bool):
+        A.call("mppi_set_graph_mode", self._h, int(bool(enable)))
+
+    def autotune(self, cache_path=None):
+        A.call("mppi_autotune", self._h, None if cache_path is None else str(cache_path).encode())
+
+    def launchConfig(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        A.call("mppi_get_launch_config", self._h, C.byref(a), C.byref(b), C.byref(c))
+        return a.value, b.value, c.value
+
+    def setLaunchConfig(self, rollout_samples_per_cta, reduction_samples_per_cta):
+        A.call("mppi_set_launch_config", self._h, int(rollout_samples_per_cta), 0, int(reduction_samples_per_cta))
+
+    def kernelsPerCompute(self) -> int:
+        n = C.c_int()
+        A.call("mppi_kernels_per_compute", self._h, C.byref(n))
+        return n.value
+
+    def enqueueSolve(self, optimization_stride=1, count=1):
+        """Device-resident solves with no host round trip (see mppi_enqueue_solve)."""
+        A.call("mppi_enqueue_solve", self._h, int(optimization_stride), int(count))
+
+    def synchronize(self):
+        A.call("mppi_synchronize", self._h)
+
+    def timeKernels(self, optimization_stride=1, reps=10):
+        """Average device ms per launch of (sampler, rollout, weights+update)."""
+        out = np.zeros(3, dtype=np.float32)
+        A.call("mppi_time_kernels", self._h, int(optimization_stride), int(reps), _fptr(out))
+        return out
+
+    def stream(self) -> int:
+        return A.lib().mppi_get_stream(self._h) or 0
+
+
+class VanillaMPPIController(BatchedMPPIController):
+    """VanillaMPPIController(model, cost, fb_controller, sampler, dt, max_iter, lambda, alpha, num_timesteps,
+    init_control_traj, stream) (controllers/MPPI/mppi_controller.cu:16-29), one instance with NUM_ROLLOUTS samples."""
+
+    def __init__(self, model, cost, fb_controller, sampler, dt, max_iter, lambda_, alpha, num_timesteps,
+                 num_rollouts, init_control_traj=None, stream=0, seed=0, slide_control_scale=None):
+        del fb_controller  # feedback controllers are not part of the plain MPPI path
+        init = None
+        if init_control_traj is not None:
+            init = np.asarray(init_control_traj, dtype=np.float32).reshape(model.CONTROL_DIM, num_timesteps).T
+        super().__init__(model, cost, sampler, [num_rollouts], [num_timesteps], dt=dt, max_iter=max_iter,
+                         lambda_=lambda_, alpha=alpha, seed=seed, init_control_traj=init, stream=stream,
+                         slide_control_scale=slide_control_scale)
+
+    def getControlSeq(self) -> np.ndarray:
+        return self.getControlSeqs()[0]
+
+    def setControlSeq(self, seq):
+        self.setControlSeqs([seq])
+
+    def getTargetStateSeq(self) -> np.ndarray:
+        return self.getTargetStateSeqs()[0]
+
+    def getSampledCostSeq(self) -> np.ndarray:
+        """The exp-weights the reference's trajectory_costs_ holds after an iteration (controller.cuh:449-452)."""
+        return self.sample_weights()
+
+    def getNormalizerPercent(self) -> float:
+        return self.getNormalizerCost() / float(self.K[0])

@@ -1,0 +1,1021 @@
+// mg_engine.cuh — host side of the engine: the Controller / VanillaMPPIController re-designed for one GB300.
+//
+// Engine<Model> holds num_instances independent MPPI problems of one plugin pair.  One computeControl enqueues, for
+// every optimisation iteration, three kernels that each cover all instances (sample, rollout, weights+update); the
+// whole sequence, including the H2D copy of the initial states and nominal controls and the D2H copy of the results,
+// is recorded once as a CUDA graph per optimisation stride and replayed.  The host then applies the reference's
+// post-processing per instance: Savitzky-Golay smoothing, nominal state rollout and control clamp
+// (VanillaMPPIController::computeControl, mppi_controller.cu:152-237).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "mg_common.cuh"
+#include "mg_kernels.cuh"
+
+namespace mg
+{
+struct CreateArgs
+{
+  int model;
+  int num_instances;
+  const int* K;
+  const int* T;
+  mppi_controller_params cp;
+  mppi_sampling_params sp;
+  mppi_control_constraints cc;
+  const void* dyn;
+  size_t dyn_bytes;
+  const void* cost;
+  size_t cost_bytes;
+  const float* init_control;
+  cudaStream_t stream;
+};
+
+class EngineBase
+{
+public:
+  virtual ~EngineBase() {}
+  virtual int model() const = 0;
+  virtual int state_dim() const = 0;
+  virtual int control_dim() const = 0;
+  virtual int num_instances() const = 0;
+  virtual void dims(int i, int* K, int* T) const = 0;
+  virtual mppi_status compute_control(const float* x0, int stride) = 0;
+  virtual mppi_status get_control_seq(float* out) = 0;
+  virtual mppi_status set_control_seq(const float* in) = 0;
+  virtual mppi_status slide_control_sequence(int steps) = 0;
+  virtual mppi_status get_state_seq(float* out) = 0;
+  virtual mppi_status get_baseline_normalizer(float* out, double* norm64) = 0;
+  virtual mppi_status get_sample_costs(float* out) = 0;
+  virtual mppi_status get_sample_weights(float* out) = 0;
+  virtual mppi_status get_control_samples(float* out) = 0;
+  virtual mppi_status get_free_energy(int i, float* out6) = 0;
+  virtual mppi_status set_dynamics_params(const void* p, size_t bytes) = 0;
+  virtual mppi_status set_cost_params(const void* p, size_t bytes) = 0;
+  virtual mppi_status set_sampling_params(const mppi_sampling_params* sp) = 0;
+  virtual mppi_status set_controller_params(const mppi_controller_params* cp) = 0;
+  virtual mppi_status set_costmap(const float* map, int w, int h, float res, float ox, float oy) = 0;
+  virtual mppi_status inject_noise(const float* noise, size_t count) = 0;
+  virtual mppi_status generate_samples(int stride, int iter) = 0;
+  virtual mppi_status set_graph_mode(int enable) = 0;
+  virtual mppi_status get_launch_config(int* ns, int* tch, int* kc) const = 0;
+  virtual mppi_status set_launch_config(int ns, int tch, int kc) = 0;
+  virtual mppi_status autotune(const char* cache_path) = 0;
+  virtual int kernels_per_compute() const = 0;
+  virtual cudaStream_t stream() const = 0;
+  virtual mppi_status enqueue_device_solves(int stride, int count) = 0;
+  virtual mppi_status time_kernels(int stride, int reps, float* ms3) = 0;
+};
+
+// Factories, one per model translation unit.
+mppi_status create_cartpole_engine(const CreateArgs& a, EngineBase** out);
+mppi_status create_double_integrator_engine(const CreateArgs& a, EngineBase** out);
+mppi_status create_bicycle_costmap_engine(const CreateArgs& a, EngineBase** out);
+mppi_status create_bicycle_slip_engine(const CreateArgs& a, EngineBase** out);
+
+// Kernel-level rollout entry points, one per model translation unit.
+mppi_status standalone_rollout_cartpole(const void* dyn, const void* cost, const mppi_sampling_params* sp,
+                                        const float* x0_d, const float* controls_d, const float* mean_d,
+                                        float* costs_d, int K, int T, float dt, float lambda, float alpha,
+                                        cudaStream_t s);
+mppi_status standalone_rollout_double_integrator(const void* dyn, const void* cost, const mppi_sampling_params* sp,
+                                                 const float* x0_d, const float* controls_d, const float* mean_d,
+                                                 float* costs_d, int K, int T, float dt, float lambda, float alpha,
+                                                 cudaStream_t s);
+
+// Rollout CTA sizes the engine instantiates; the time chunk follows from the 48 KB static shared-memory budget.
+template <int NS, int C>
+struct RolloutShape
+{
+  static constexpr int TCH = (NS * (32 * C + 4) * 4 <= 48 * 1024) ? 32 : 16;
+};
+
+inline SampleShared make_sample_shared(const mppi_sampling_params& sp, const mppi_control_constraints& cc)
+{
+  SampleShared sh;
+  for (int i = 0; i < kMaxC; ++i)
+  {
+    sh.std_dev[i] = sp.std_dev[i];
+    sh.control_cost_coeff[i] = sp.control_cost_coeff[i];
+    sh.lower[i] = cc.lower[i];
+    sh.upper[i] = cc.upper[i];
+    sh.deadband[i] = cc.deadband[i];
+    sh.zero[i] = cc.zero_control[i];
+  }
+  sh.pure_pct = sp.pure_noise_trajectories_percentage;
+  return sh;
+}
+
+// Controller::smoothControlTrajectoryHelper (controller.cuh:573-607).
+inline void smooth_control(float* u, int T, int C)
+{
+  const float coef[5] = { -3.0f / 35.0f, 12.0f / 35.0f, 17.0f / 35.0f, 12.0f / 35.0f, -3.0f / 35.0f };
+  std::vector<float> buf((size_t)(T + 4) * C);
+  for (int c = 0; c < C; ++c)
+  {
+    buf[c] = u[c];
+    buf[C + c] = u[c];
+    for (int t = 0; t < T; ++t) buf[(size_t)(t + 2) * C + c] = u[(size_t)t * C + c];
+    buf[(size_t)(T + 2) * C + c] = u[(size_t)(T - 1) * C + c];
+    buf[(size_t)(T + 3) * C + c] = u[(size_t)(T - 1) * C + c];
+  }
+  for (int t = 1; t < T; ++t)
+    for (int c = 0; c < C; ++c)
+    {
+      float acc = 0.0f;
+      for (int j = 0; j < 5; ++j) acc += coef[j] * buf[(size_t)(t + j) * C + c];
+      u[(size_t)t * C + c] = acc;
+    }
+}
+
+template <class Model>
+class Engine : public EngineBase
+{
+public:
+  static constexpr int S = Model::STATE_DIM;
+  static constexpr int C = Model::CONTROL_DIM;
+  using DynParams = typename Model::DynParams;
+  using CostParams = typename Model::CostParams;
+
+  ~Engine() override
+  {
+    if (stream_) cudaStreamSynchronize(stream_);
+    invalidate_graphs();
+    if (own_stream_ && stream_) cudaStreamDestroy(stream_);
+  }
+
+  static mppi_status create(const CreateArgs& a, EngineBase** out)
+  {
+    MG_CHECK(a.num_instances >= 1, "num_instances must be >= 1 (got %d)", a.num_instances);
+    MG_CHECK(a.K && a.T, "num_rollouts and num_timesteps arrays are required");
+    MG_CHECK(a.dyn_bytes == sizeof(DynParams), "dynamics parameter block is %zu bytes, model expects %zu",
+             a.dyn_bytes, sizeof(DynParams));
+    MG_CHECK(a.cost_bytes == sizeof(CostParams), "cost parameter block is %zu bytes, model expects %zu",
+             a.cost_bytes, sizeof(CostParams));
+    MG_CHECK(a.dyn && a.cost, "parameter blocks must not be NULL");
+    std::unique_ptr<Engine> e(new Engine());
+    MG_TRY(e->init(a));
+    *out = e.release();
+    return MPPI_OK;
+  }
+
+  int model() const override { return Model::kModelId; }
+  int state_dim() const override { return S; }
+  int control_dim() const override { return C; }
+  int num_instances() const override { return I_; }
+  void dims(int i, int* K, int* T) const override
+  {
+    if (K) *K = K_[i];
+    if (T) *T = T_[i];
+  }
+  cudaStream_t stream() const override { return stream_; }
+  int kernels_per_compute() const override { return 3 * cp_.num_iters; }
+
+  // ------------------------------------------------------------------------------------------------ computeControl
+  mppi_status compute_control(const float* x0, int stride) override
+  {
+    MG_CHECK(x0 != nullptr, "x0 must not be NULL");
+    MG_CHECK(stride >= 0, "optimization_stride must be >= 0");
+    MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
+    for (int i = 0; i < I_ * S; ++i)
+      if (!std::isfinite(x0[i]))
+      {
+        set_error("initial state has a non-finite entry at index %d", i);
+        return MPPI_ENAN;
+      }
+    for (int i = 0; i < I_; ++i) prev_baseline_[i] = baseline_norm_[2 * i];
+    memcpy(x0_h_.p, x0, sizeof(float) * I_ * S);
+    memcpy(mean_h_.p, control_.data(), sizeof(float) * control_.size());
+    if (graph_mode_)
+    {
+      cudaGraphExec_t exec = nullptr;
+      MG_TRY(get_graph(stride, &exec));
+      MG_CUDA(cudaGraphLaunch(exec, stream_));
+    }
+    else
+    {
+      MG_TRY(enqueue_solve(stride));
+    }
+    MG_CUDA(cudaStreamSynchronize(stream_));
+    return finish_solve(x0);
+  }
+
+  mppi_status get_control_seq(float* out) override
+  {
+    MG_CHECK(out, "out must not be NULL");
+    memcpy(out, control_.data(), sizeof(float) * control_.size());
+    return MPPI_OK;
+  }
+  mppi_status set_control_seq(const float* in) override
+  {
+    MG_CHECK(in, "in must not be NULL");
+    memcpy(control_.data(), in, sizeof(float) * control_.size());
+    return MPPI_OK;
+  }
+  // Controller::slideControlSequence -> saveControlHistoryHelper + slideControlSequenceHelper (controller.cuh:370-376,
+  // 609-636).  The history only feeds smoothing variants the reference no longer uses, but it is kept for parity.
+  mppi_status slide_control_sequence(int steps) override
+  {
+    MG_CHECK(steps >= 0, "steps must be >= 0");
+    for (int i = 0; i < I_; ++i)
+    {
+      float* u = control_.data() + t_off_[i];
+      const int T = T_[i];
+      float* hist = history_.data() + (size_t)i * 2 * C;
+      if (steps == 1)
+      {
+        for (int c = 0; c < C; ++c)
+        {
+          hist[c] = hist[C + c];
+          hist[C + c] = last_pre_smooth_[(size_t)i * C + c];
+        }
+      }
+      else if (steps >= 2)
+      {
+        for (int c = 0; c < C; ++c)
+        {
+          hist[c] = u[(size_t)std::min(steps - 2, T - 1) * C + c];
+          hist[C + c] = u[(size_t)std::min(steps - 1, T - 1) * C + c];
+        }
+      }
+      for (int t = 0; t < T; ++t)
+      {
+        const int ind = std::min(t + steps, T - 1);
+        for (int c = 0; c < C; ++c)
+        {
+          float v = u[(size_t)ind * C + c];
+          if (t + steps > T - 1)
+            v = (v - cc_.zero_control[c]) * cp_.slide_control_scale[c] + cc_.zero_control[c];
+          u[(size_t)t * C + c] = v;
+        }
+      }
+    }
+    return MPPI_OK;
+  }
+  mppi_status get_state_seq(float* out) override
+  {
+    MG_CHECK(out, "out must not be NULL");
+    memcpy(out, state_seq_.data(), sizeof(float) * state_seq_.size());
+    return MPPI_OK;
+  }
+  mppi_status get_baseline_normalizer(float* out, double* norm64) override
+  {
+    if (out) memcpy(out, baseline_norm_.data(), sizeof(float) * 2 * I_);
+    if (norm64)
+      for (int i = 0; i < I_; ++i) norm64[i] = stats_[3 * i];
+    return MPPI_OK;
+  }
+  mppi_status get_sample_costs(float* out) override { return copy_per_sample(costs_d_.p, out); }
+  mppi_status get_sample_weights(float* out) override { return copy_per_sample(weights_d_.p, out); }
+  mppi_status get_control_samples(float* out) override
+  {
+    MG_CHECK(out, "out must not be NULL");
+    MG_CUDA(cudaStreamSynchronize(stream_));
+    size_t o = 0;
+    for (int i = 0; i < I_; ++i)
+    {
+      const size_t n = (size_t)K_[i] * T_[i] * C;
+      MG_CUDA(cudaMemcpy(out + o, samples_d_.p + u_off_[i], n * sizeof(float), cudaMemcpyDeviceToHost));
+      o += n;
+    }
+    return MPPI_OK;
+  }
+  // computeFreeEnergy (mppi_common.cu:1101-1117) from the device sums of w and w^2.
+  mppi_status get_free_energy(int i, float* out6) override
+  {
+    MG_CHECK(i >= 0 && i < I_, "instance %d out of range", i);
+    MG_CHECK(out6, "out must not be NULL");
+    const float lambda = cp_.lambda;
+    const int K = K_[i];
+    const float norm = (float)(stats_[3 * i] / K);
+    const float var = (float)stats_[3 * i + 1];
+    const float baseline = baseline_norm_[2 * i];
+    const float fe = -lambda * logf(norm) + baseline;
+    const float fe_var = lambda * (var / K - norm * norm);
+    const float weird = fe_var / (norm * sqrtf(1.0f * K));
+    out6[0] = fe;
+    out6[1] = fe_var;
+    out6[2] = lambda * (weird + 0.5f * weird * weird);
+    out6[3] = baseline_norm_[2 * i + 1] / (float)K;
+    out6[4] = baseline - prev_baseline_[i];
+    out6[5] = prev_baseline_[i];
+    return MPPI_OK;
+  }
+
+  mppi_status set_dynamics_params(const void* p, size_t bytes) override
+  {
+    MG_CHECK(p && bytes == sizeof(DynParams), "dynamics parameter block must be %zu bytes", sizeof(DynParams));
+    memcpy(dyn_.data(), p, sizeof(DynParams) * I_);
+    MG_CUDA(cudaMemcpyAsync(dyn_d_.p, dyn_.data(), sizeof(DynParams) * I_, cudaMemcpyHostToDevice, stream_));
+    MG_CUDA(cudaStreamSynchronize(stream_));
+    return MPPI_OK;
+  }
+  mppi_status set_cost_params(const void* p, size_t bytes) override
+  {
+    MG_CHECK(p && bytes == sizeof(CostParams), "cost parameter block must be %zu bytes", sizeof(CostParams));
+    memcpy(cost_.data(), p, sizeof(CostParams) * I_);
+    MG_CUDA(cudaMemcpyAsync(cost_d_.p, cost_.data(), sizeof(CostParams) * I_, cudaMemcpyHostToDevice, stream_));
+    MG_CUDA(cudaStreamSynchronize(stream_));
+    return MPPI_OK;
+  }
+  mppi_status set_sampling_params(const mppi_sampling_params* sp) override
+  {
+    MG_CHECK(sp, "sampling params must not be NULL");
+    MG_TRY(check_sampling(*sp));
+    sp_ = *sp;
+    invalidate_graphs();
+    return MPPI_OK;
+  }
+  mppi_status set_controller_params(const mppi_controller_params* cp) override
+  {
+    MG_CHECK(cp, "controller params must not be NULL");
+    MG_CHECK(cp->num_iters >= 1, "num_iters must be >= 1");
+    MG_CHECK(cp->lambda > 0.0f && std::isfinite(cp->lambda), "lambda must be positive");
+    MG_CHECK(std::isfinite(cp->dt), "dt must be finite");
+    cp_ = *cp;
+    invalidate_graphs();
+    return MPPI_OK;
+  }
+  mppi_status set_costmap(const float* map, int w, int h, float res, float ox, float oy) override
+  {
+    MG_CHECK(map && w >= 2 && h >= 2 && res > 0.0f, "costmap needs data, width/height >= 2 and resolution > 0");
+    MG_TRY(costmap_d_.alloc((size_t)w * h));
+    MG_CUDA(cudaMemcpy(costmap_d_.p, map, sizeof(float) * w * h, cudaMemcpyHostToDevice));
+    aux_.map = CostmapView{ costmap_d_.p, w, h, 1.0f / res, res, ox, oy };
+    invalidate_graphs();
+    return MPPI_OK;
+  }
+
+  mppi_status inject_noise(const float* noise, size_t count) override
+  {
+    if (!noise)
+    {
+      injected_d_.reset();
+      invalidate_graphs();
+      return MPPI_OK;
+    }
+    MG_CHECK(sp_.kind == MPPI_SAMPLER_GAUSSIAN, "noise injection for this sampler is not built");
+    size_t need = 0;
+    for (int i = 0; i < I_; ++i) need += (size_t)K_[i] * T_[i] * C;
+    MG_CHECK(count == need, "injected noise has %zu floats, expected %zu", count, need);
+    for (size_t j = 0; j < count; ++j)
+      if (!std::isfinite(noise[j]))
+      {
+        set_error("injected noise has a non-finite entry at index %zu", j);
+        return MPPI_ENAN;
+      }
+    MG_TRY(injected_d_.alloc(samples_d_.n));
+    size_t o = 0;
+    for (int i = 0; i < I_; ++i)
+    {
+      const size_t n = (size_t)K_[i] * T_[i] * C;
+      MG_CUDA(cudaMemcpy(injected_d_.p + u_off_[i], noise + o, n * sizeof(float), cudaMemcpyHostToDevice));
+      o += n;
+    }
+    invalidate_graphs();
+    return MPPI_OK;
+  }
+
+  mppi_status generate_samples(int stride, int iter) override
+  {
+    MG_CHECK(stride >= 0 && iter >= 0, "stride and iteration must be >= 0");
+    memcpy(mean_h_.p, control_.data(), sizeof(float) * control_.size());
+    MG_CUDA(cudaMemcpyAsync(mean_d_.p, mean_h_.p, sizeof(float) * control_.size(), cudaMemcpyHostToDevice, stream_));
+    MG_TRY(launch_sampler(stride, iter));
+    bump_counter_kernel<<<1, 1, 0, stream_>>>(counters_d_.p + 3);
+    MG_CUDA(cudaGetLastError());
+    MG_CUDA(cudaStreamSynchronize(stream_));
+    return MPPI_OK;
+  }
+
+  mppi_status set_graph_mode(int enable) override
+  {
+    graph_mode_ = enable != 0;
+    return MPPI_OK;
+  }
+  mppi_status get_launch_config(int* ns, int* tch, int* kc) const override
+  {
+    if (ns) *ns = ns_;
+    if (tch) *tch = tch_for(ns_);
+    if (kc) *kc = kc_;
+    return MPPI_OK;
+  }
+  mppi_status set_launch_config(int ns, int tch, int kc) override
+  {
+    MG_CHECK(ns == 32 || ns == 64 || ns == 128 || ns == 256, "rollout samples per CTA must be 32, 64, 128 or 256");
+    MG_CHECK(kc >= 32 && kc <= 256 && (kc % 32) == 0, "reduction samples per CTA must be a multiple of 32 in [32, 256]");
+    (void)tch;
+    ns_ = ns;
+    kc_ = kc;
+    MG_TRY(build_work_lists());
+    invalidate_graphs();
+    return MPPI_OK;
+  }
+  mppi_status autotune(const char* cache_path) override;
+
+  mppi_status enqueue_device_solves(int stride, int count) override
+  {
+    MG_CHECK(stride >= 0 && count >= 0, "stride and count must be >= 0");
+    MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
+    auto it = device_graphs_.find(stride);
+    cudaGraphExec_t exec = nullptr;
+    if (it == device_graphs_.end())
+    {
+      cudaGraph_t g = nullptr;
+      MG_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+      mppi_status st = enqueue_kernels(stride);
+      cudaError_t ce = cudaStreamEndCapture(stream_, &g);
+      if (st != MPPI_OK)
+      {
+        if (g) cudaGraphDestroy(g);
+        return st;
+      }
+      MG_CUDA(ce);
+      ce = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      MG_CUDA(ce);
+      device_graphs_[stride] = exec;
+    }
+    else
+    {
+      exec = it->second;
+    }
+    for (int i = 0; i < count; ++i) MG_CUDA(cudaGraphLaunch(exec, stream_));
+    return MPPI_OK;
+  }
+
+  mppi_status time_kernels(int stride, int reps, float* ms3) override
+  {
+    MG_CHECK(ms3 && reps >= 1, "need an output array and reps >= 1");
+    MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
+    cudaEvent_t ev[4];
+    for (auto& e : ev) MG_CUDA(cudaEventCreate(&e));
+    float tot[3] = { 0, 0, 0 };
+    for (int r = 0; r < reps + 1; ++r)
+    {
+      MG_CUDA(cudaEventRecord(ev[0], stream_));
+      MG_TRY(launch_sampler(stride, 0));
+      MG_CUDA(cudaEventRecord(ev[1], stream_));
+      MG_TRY(launch_rollout());
+      MG_CUDA(cudaEventRecord(ev[2], stream_));
+      MG_TRY(launch_weights());
+      MG_CUDA(cudaEventRecord(ev[3], stream_));
+      MG_CUDA(cudaEventSynchronize(ev[3]));
+      if (r == 0) continue;  // warm-up
+      for (int k = 0; k < 3; ++k)
+      {
+        float ms = 0.0f;
+        MG_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+        tot[k] += ms;
+      }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < 3; ++k) ms3[k] = tot[k] / reps;
+    return MPPI_OK;
+  }
+
+private:
+  Engine() = default;
+
+  static int tch_for(int ns)
+  {
+    switch (ns)
+    {
+      case 32: return RolloutShape<32, C>::TCH;
+      case 64: return RolloutShape<64, C>::TCH;
+      case 128: return RolloutShape<128, C>::TCH;
+      default: return RolloutShape<256, C>::TCH;
+    }
+  }
+
+  mppi_status check_sampling(const mppi_sampling_params& sp)
+  {
+    MG_CHECK(sp.kind == MPPI_SAMPLER_GAUSSIAN || sp.kind == MPPI_SAMPLER_COLORED_NOISE, "unknown sampler kind %d",
+             sp.kind);
+    MG_CHECK(sp.kind == MPPI_SAMPLER_GAUSSIAN, "the colored-noise sampler is not built for this model");
+    for (int c = 0; c < C; ++c)
+      MG_CHECK(std::isfinite(sp.std_dev[c]) && sp.std_dev[c] >= 0.0f, "std_dev[%d] must be finite and >= 0", c);
+    MG_CHECK(sp.pure_noise_trajectories_percentage >= 0.0f && sp.pure_noise_trajectories_percentage <= 1.0f,
+             "pure_noise_trajectories_percentage must be in [0, 1]");
+    return MPPI_OK;
+  }
+
+  mppi_status init(const CreateArgs& a)
+  {
+    I_ = a.num_instances;
+    cp_ = a.cp;
+    cc_ = a.cc;
+    MG_CHECK(cp_.num_iters >= 1, "num_iters must be >= 1");
+    MG_CHECK(cp_.lambda > 0.0f && std::isfinite(cp_.lambda), "lambda must be positive");
+    MG_CHECK(std::isfinite(cp_.dt), "dt must be finite");
+    MG_TRY(check_sampling(a.sp));
+    sp_ = a.sp;
+    K_.assign(a.K, a.K + I_);
+    T_.assign(a.T, a.T + I_);
+    long long total_u = 0;
+    int total_k = 0, total_t = 0;
+    for (int i = 0; i < I_; ++i)
+    {
+      MG_CHECK(K_[i] >= 1, "num_rollouts[%d] must be >= 1 (got %d)", i, K_[i]);
+      MG_CHECK(T_[i] >= 1, "num_timesteps[%d] must be >= 1 (got %d)", i, T_[i]);
+      MG_CHECK((long long)K_[i] * T_[i] * C < (1LL << 31), "instance %d is too large", i);
+      k_off_.push_back(total_k);
+      t_off_.push_back(total_t);
+      u_off_.push_back(total_u);
+      total_k += K_[i];
+      total_t += T_[i] * C;
+      total_u += ((long long)K_[i] * T_[i] * C + 3) / 4 * 4;
+    }
+    total_k_ = total_k;
+    dyn_.assign((const DynParams*)a.dyn, (const DynParams*)a.dyn + I_);
+    cost_.assign((const CostParams*)a.cost, (const CostParams*)a.cost + I_);
+    control_.assign((size_t)total_t, 0.0f);
+    if (a.init_control) memcpy(control_.data(), a.init_control, sizeof(float) * total_t);
+    size_t total_s = 0;
+    for (int i = 0; i < I_; ++i) total_s += (size_t)T_[i] * S;
+    state_seq_.assign(total_s, 0.0f);
+    history_.assign((size_t)I_ * 2 * C, 0.0f);
+    last_pre_smooth_.assign((size_t)I_ * C, 0.0f);
+    baseline_norm_.assign((size_t)2 * I_, 0.0f);
+    stats_.assign((size_t)3 * I_, 0.0);
+    prev_baseline_.assign(I_, 0.0f);
+    memset(&aux_, 0, sizeof(aux_));
+
+    if (a.stream)
+    {
+      stream_ = a.stream;
+    }
+    else
+    {
+      MG_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+      own_stream_ = true;
+    }
+    int dev = 0;
+    MG_CUDA(cudaGetDevice(&dev));
+    MG_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
+
+    MG_TRY(samples_d_.alloc((size_t)total_u));
+    MG_CUDA(cudaMemset(samples_d_.p, 0, sizeof(float) * samples_d_.n));
+    MG_TRY(costs_d_.alloc(total_k));
+    MG_TRY(weights_d_.alloc(total_k));
+    MG_CUDA(cudaMemset(costs_d_.p, 0, sizeof(float) * total_k));
+    MG_CUDA(cudaMemset(weights_d_.p, 0, sizeof(float) * total_k));
+    MG_TRY(mean_d_.alloc(total_t));
+    MG_TRY(x0_d_.alloc((size_t)I_ * S));
+    MG_TRY(dyn_d_.alloc(I_));
+    MG_TRY(cost_d_.alloc(I_));
+    MG_CUDA(cudaMemcpy(dyn_d_.p, dyn_.data(), sizeof(DynParams) * I_, cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(cost_d_.p, cost_.data(), sizeof(CostParams) * I_, cudaMemcpyHostToDevice));
+    MG_TRY(baseline_bits_d_.alloc(I_));
+    MG_TRY(arrive_d_.alloc(I_));
+    MG_TRY(counters_d_.alloc(8));
+    MG_TRY(bn_d_.alloc((size_t)2 * I_));
+    MG_TRY(stats_d_.alloc((size_t)3 * I_));
+    MG_CUDA(cudaMemset(arrive_d_.p, 0, sizeof(unsigned int) * I_));
+    MG_CUDA(cudaMemset(counters_d_.p, 0, sizeof(unsigned int) * 8));
+    fill_u32_kernel<<<1, 256, 0, stream_>>>(baseline_bits_d_.p, kOrderedPosInf, I_);
+    MG_CUDA(cudaGetLastError());
+    MG_TRY(x0_h_.alloc((size_t)I_ * S));
+    MG_TRY(mean_h_.alloc(total_t));
+    MG_TRY(out_mean_h_.alloc(total_t));
+    MG_TRY(out_bn_h_.alloc((size_t)2 * I_));
+    MG_TRY(out_stats_h_.alloc((size_t)3 * I_));
+    MG_TRY(build_work_lists());
+    MG_CUDA(cudaStreamSynchronize(stream_));
+    return MPPI_OK;
+  }
+
+  // Work lists: rollout tiles ordered by decreasing horizon (the cost of a tile is proportional to T), sampler items,
+  // and weight/update chunks with the offsets of their partial rows.
+  mppi_status build_work_lists()
+  {
+    std::vector<InstDesc> inst(I_);
+    std::vector<int2> tiles, swork;
+    std::vector<int4> chunks;
+    std::vector<long long> part_off;
+    std::vector<int> chunk0(I_);
+    long long poff = 0;
+    for (int i = 0; i < I_; ++i)
+    {
+      InstDesc& d = inst[i];
+      d.K = K_[i];
+      d.T = T_[i];
+      d.k_off = k_off_[i];
+      d.t_off = t_off_[i];
+      d.u_off = u_off_[i];
+      d.spec_off = 0;
+      d.x_off = i * S;
+      d.num_chunks = (K_[i] + kc_ - 1) / kc_;
+      chunk0[i] = (int)chunks.size();
+      for (int c = 0; c < d.num_chunks; ++c)
+      {
+        chunks.push_back(make_int4(i, c * kc_, std::min(K_[i], (c + 1) * kc_), c));
+        part_off.push_back(poff);
+        poff += (long long)T_[i] * C;
+      }
+      const long long nq = ((long long)K_[i] * T_[i] * C + 3) / 4;
+      for (long long q = 0; q < nq; q += kSampleQuadsPerItem) swork.push_back(make_int2(i, (int)q));
+    }
+    std::vector<int> order(I_);
+    for (int i = 0; i < I_; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return T_[x] > T_[y]; });
+    for (int i : order)
+      for (int k0 = 0; k0 < K_[i]; k0 += ns_) tiles.push_back(make_int2(i, k0));
+    num_tiles_ = (int)tiles.size();
+    num_chunks_ = (int)chunks.size();
+    num_swork_ = (int)swork.size();
+    MG_TRY(inst_d_.alloc(I_));
+    MG_TRY(tiles_d_.alloc(tiles.size()));
+    MG_TRY(swork_d_.alloc(swork.size()));
+    MG_TRY(chunks_d_.alloc(chunks.size()));
+    MG_TRY(part_off_d_.alloc(part_off.size()));
+    MG_TRY(chunk0_d_.alloc(I_));
+    MG_TRY(partials_d_.alloc((size_t)std::max<long long>(poff, 1)));
+    MG_TRY(part_w_d_.alloc(2 * chunks.size()));
+    MG_CUDA(cudaMemcpy(inst_d_.p, inst.data(), sizeof(InstDesc) * I_, cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(tiles_d_.p, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(swork_d_.p, swork.data(), sizeof(int2) * swork.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(chunks_d_.p, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(part_off_d_.p, part_off.data(), sizeof(long long) * part_off.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(chunk0_d_.p, chunk0.data(), sizeof(int) * I_, cudaMemcpyHostToDevice));
+    // persistent rollout grid: every SM filled to its occupancy limit, never more CTAs than tiles
+    int per_sm = 1;
+    MG_TRY(rollout_occupancy(&per_sm));
+    rollout_grid_ = std::max(1, std::min(num_tiles_, per_sm * num_sms_));
+    return MPPI_OK;
+  }
+
+  template <int NS>
+  mppi_status occupancy_ns(int* per_sm)
+  {
+    constexpr int TCH = RolloutShape<NS, C>::TCH;
+    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, rollout_kernel<Model, NS, TCH>, NS, 0));
+    if (*per_sm < 1) *per_sm = 1;
+    return MPPI_OK;
+  }
+  mppi_status rollout_occupancy(int* per_sm)
+  {
+    switch (ns_)
+    {
+      case 32: return occupancy_ns<32>(per_sm);
+      case 64: return occupancy_ns<64>(per_sm);
+      case 128: return occupancy_ns<128>(per_sm);
+      default: return occupancy_ns<256>(per_sm);
+    }
+  }
+
+  mppi_status launch_sampler(int stride, int iter)
+  {
+    SampleArgs a;
+    a.inst = inst_d_.p;
+    a.work = swork_d_.p;
+    a.num_work = num_swork_;
+    a.quads_per_item = kSampleQuadsPerItem;
+    a.samples = samples_d_.p;
+    a.mean = mean_d_.p;
+    a.injected = injected_d_.p;
+    a.noise_counter = counters_d_.p + 3;
+    a.seed_lo = (uint32_t)cp_.seed;
+    a.seed_hi = (uint32_t)(cp_.seed >> 32);
+    a.stride = stride;
+    a.decay_pow = powf(sp_.std_dev_decay, (float)iter);
+    a.sh = make_sample_shared(sp_, cc_);
+    const int grid = std::min(num_swork_, 8 * num_sms_);
+    gaussian_sample_kernel<C><<<grid, 256, 0, stream_>>>(a);
+    MG_CUDA(cudaGetLastError());
+    return MPPI_OK;
+  }
+
+  template <int NS>
+  void launch_rollout_ns(const RolloutArgs<Model>& a)
+  {
+    constexpr int TCH = RolloutShape<NS, C>::TCH;
+    rollout_kernel<Model, NS, TCH><<<rollout_grid_, NS, 0, stream_>>>(a);
+  }
+  mppi_status launch_rollout()
+  {
+    RolloutArgs<Model> a;
+    a.inst = inst_d_.p;
+    a.tiles = tiles_d_.p;
+    a.num_tiles = num_tiles_;
+    a.dyn = dyn_d_.p;
+    a.cost = cost_d_.p;
+    a.aux = aux_;
+    a.x0 = x0_d_.p;
+    a.samples = samples_d_.p;
+    a.mean = mean_d_.p;
+    a.costs = costs_d_.p;
+    a.baseline_bits = baseline_bits_d_.p;
+    a.tile_counter = counters_d_.p;
+    a.dt = cp_.dt;
+    a.lambda = cp_.lambda;
+    a.alpha = cp_.alpha;
+    a.use_likelihood = 0;
+    for (int c = 0; c < C; ++c)
+      if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
+    a.sh = make_sample_shared(sp_, cc_);
+    switch (ns_)
+    {
+      case 32: launch_rollout_ns<32>(a); break;
+      case 64: launch_rollout_ns<64>(a); break;
+      case 128: launch_rollout_ns<128>(a); break;
+      default: launch_rollout_ns<256>(a); break;
+    }
+    MG_CUDA(cudaGetLastError());
+    return MPPI_OK;
+  }
+
+  mppi_status launch_weights()
+  {
+    WeightsArgs a;
+    a.inst = inst_d_.p;
+    a.chunks = chunks_d_.p;
+    a.part_off = part_off_d_.p;
+    a.inst_chunk0 = chunk0_d_.p;
+    a.num_chunks = num_chunks_;
+    a.num_instances = I_;
+    a.costs = costs_d_.p;
+    a.weights = weights_d_.p;
+    a.samples = samples_d_.p;
+    a.partials = partials_d_.p;
+    a.part_w = part_w_d_.p;
+    a.baseline_bits = baseline_bits_d_.p;
+    a.arrive = arrive_d_.p;
+    a.inst_done = counters_d_.p + 2;
+    a.noise_counter = counters_d_.p + 3;
+    a.mean_out = mean_d_.p;
+    a.baseline_norm = bn_d_.p;
+    a.stats = stats_d_.p;
+    a.lambda_inv = 1.0f / cp_.lambda;
+    a.weights_given = 0;
+    a.given_norm = nullptr;
+    weights_update_kernel<C><<<num_chunks_, 256, 0, stream_>>>(a);
+    MG_CUDA(cudaGetLastError());
+    return MPPI_OK;
+  }
+
+  // num_iters x (sample, rollout, weights+update), in stream order.
+  mppi_status enqueue_kernels(int stride)
+  {
+    for (int it = 0; it < cp_.num_iters; ++it)
+    {
+      MG_TRY(launch_sampler(stride, it));
+      MG_TRY(launch_rollout());
+      MG_TRY(launch_weights());
+    }
+    return MPPI_OK;
+  }
+
+  // The device work of one computeControl, in stream order.
+  mppi_status enqueue_solve(int stride)
+  {
+    const size_t tc = control_.size();
+    MG_CUDA(cudaMemcpyAsync(x0_d_.p, x0_h_.p, sizeof(float) * I_ * S, cudaMemcpyHostToDevice, stream_));
+    MG_CUDA(cudaMemcpyAsync(mean_d_.p, mean_h_.p, sizeof(float) * tc, cudaMemcpyHostToDevice, stream_));
+    MG_TRY(enqueue_kernels(stride));
+    MG_CUDA(cudaMemcpyAsync(out_mean_h_.p, mean_d_.p, sizeof(float) * tc, cudaMemcpyDeviceToHost, stream_));
+    MG_CUDA(cudaMemcpyAsync(out_bn_h_.p, bn_d_.p, sizeof(float) * 2 * I_, cudaMemcpyDeviceToHost, stream_));
+    MG_CUDA(cudaMemcpyAsync(out_stats_h_.p, stats_d_.p, sizeof(double) * 3 * I_, cudaMemcpyDeviceToHost, stream_));
+    return MPPI_OK;
+  }
+
+  mppi_status get_graph(int stride, cudaGraphExec_t* exec)
+  {
+    auto it = graphs_.find(stride);
+    if (it != graphs_.end())
+    {
+      *exec = it->second;
+      return MPPI_OK;
+    }
+    cudaGraph_t g = nullptr;
+    MG_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    mppi_status st = enqueue_solve(stride);
+    cudaError_t ce = cudaStreamEndCapture(stream_, &g);
+    if (st != MPPI_OK)
+    {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (ce != cudaSuccess)
+    {
+      set_error("cudaStreamEndCapture failed: %s", cudaGetErrorString(ce));
+      return MPPI_ECUDA;
+    }
+    cudaGraphExec_t e = nullptr;
+    ce = cudaGraphInstantiate(&e, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess)
+    {
+      set_error("cudaGraphInstantiate failed: %s", cudaGetErrorString(ce));
+      return MPPI_ECUDA;
+    }
+    graphs_[stride] = e;
+    *exec = e;
+    return MPPI_OK;
+  }
+
+  void invalidate_graphs()
+  {
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+    for (auto& kv : device_graphs_) cudaGraphExecDestroy(kv.second);
+    device_graphs_.clear();
+  }
+
+  // Host post-processing of computeControl (mppi_controller.cu:208-227).
+  mppi_status finish_solve(const float* x0)
+  {
+    memcpy(control_.data(), out_mean_h_.p, sizeof(float) * control_.size());
+    memcpy(baseline_norm_.data(), out_bn_h_.p, sizeof(float) * 2 * I_);
+    memcpy(stats_.data(), out_stats_h_.p, sizeof(double) * 3 * I_);
+    bool bad = false;
+    for (int i = 0; i < I_; ++i)
+    {
+      if (!std::isfinite(baseline_norm_[2 * i]) || !(stats_[3 * i] > 0.0)) bad = true;
+      float* u = control_.data() + t_off_[i];
+      const int T = T_[i];
+      for (int c = 0; c < C; ++c) last_pre_smooth_[(size_t)i * C + c] = u[c];
+      smooth_control(u, T, C);
+      // computeOutputTrajectoryHelper (controller.cuh:664-684): x0 then T-1 constrained steps
+      float* xs = state_seq_.data();
+      for (int j = 0; j < i; ++j) xs += (size_t)T_[j] * S;
+      float x[S], xn[S], uc[C];
+      for (int s = 0; s < S; ++s) x[s] = xs[s] = x0[(size_t)i * S + s];
+      for (int t = 0; t < T - 1; ++t)
+      {
+        for (int c = 0; c < C; ++c)
+          uc[c] = enforce_constraint(u[(size_t)t * C + c], cc_.lower[c], cc_.upper[c], cc_.deadband[c],
+                                     cc_.zero_control[c]);
+        euler_step<Model>(dyn_[i], x, uc, xn, cp_.dt);
+        for (int s = 0; s < S; ++s) x[s] = xs[(size_t)(t + 1) * S + s] = xn[s];
+      }
+      for (int t = 0; t < T; ++t)
+        for (int c = 0; c < C; ++c)
+          u[(size_t)t * C + c] = enforce_constraint(u[(size_t)t * C + c], cc_.lower[c], cc_.upper[c],
+                                                    cc_.deadband[c], cc_.zero_control[c]);
+    }
+    if (bad)
+    {
+      set_error("a sampled cost or the normaliser is not finite (NaN state or noise?)");
+      return MPPI_ENAN;
+    }
+    return MPPI_OK;
+  }
+
+  mppi_status copy_per_sample(const float* src_d, float* out)
+  {
+    MG_CHECK(out, "out must not be NULL");
+    MG_CUDA(cudaStreamSynchronize(stream_));
+    MG_CUDA(cudaMemcpy(out, src_d, sizeof(float) * total_k_, cudaMemcpyDeviceToHost));
+    return MPPI_OK;
+  }
+
+  static constexpr int kSampleQuadsPerItem = 2048;
+
+  int I_ = 0;
+  std::vector<int> K_, T_, k_off_, t_off_;
+  std::vector<long long> u_off_;
+  int total_k_ = 0;
+  mppi_controller_params cp_{};
+  mppi_sampling_params sp_{};
+  mppi_control_constraints cc_{};
+  std::vector<DynParams> dyn_;
+  std::vector<CostParams> cost_;
+  ModelAux aux_{};
+  std::vector<float> control_, state_seq_, history_, last_pre_smooth_, baseline_norm_, prev_baseline_;
+  std::vector<double> stats_;
+
+  cudaStream_t stream_ = nullptr;
+  bool own_stream_ = false;
+  int num_sms_ = 1;
+  bool graph_mode_ = true;
+  std::map<int, cudaGraphExec_t> graphs_, device_graphs_;
+
+  int ns_ = 128;  // rollout samples per CTA
+  int kc_ = 128;  // weight/update samples per CTA
+  int num_tiles_ = 0, num_chunks_ = 0, num_swork_ = 0, rollout_grid_ = 1;
+
+  DevBuf<float> samples_d_, costs_d_, weights_d_, mean_d_, x0_d_, partials_d_, bn_d_, injected_d_, costmap_d_;
+  DevBuf<double> part_w_d_, stats_d_;
+  DevBuf<DynParams> dyn_d_;
+  DevBuf<CostParams> cost_d_;
+  DevBuf<unsigned int> baseline_bits_d_, arrive_d_, counters_d_;
+  DevBuf<InstDesc> inst_d_;
+  DevBuf<int2> tiles_d_, swork_d_;
+  DevBuf<int4> chunks_d_;
+  DevBuf<long long> part_off_d_;
+  DevBuf<int> chunk0_d_;
+  PinnedBuf<float> x0_h_, mean_h_, out_mean_h_, out_bn_h_;
+  PinnedBuf<double> out_stats_h_;
+};
+
+// Autotuner: times one full solve (non-graph) per candidate launch shape with CUDA events and keeps the fastest.
+// Candidates: rollout samples per CTA {32, 64, 128, 256} x update samples per CTA {64, 128, 256}.  The cache is a
+// small JSON object {"<key>": [ns, kc], ...} keyed by the model id and the instance shapes.
+mppi_status autotune_impl(EngineBase* e, const char* cache_path, const std::string& key,
+                          mppi_status (*time_one)(EngineBase*, float*));
+
+template <class Model>
+mppi_status Engine<Model>::autotune(const char* cache_path)
+{
+  std::string key = "m" + std::to_string(Model::kModelId) + "_i" + std::to_string(I_);
+  unsigned long long h = 1469598103934665603ULL;
+  for (int i = 0; i < I_; ++i)
+  {
+    h = (h ^ (unsigned long long)K_[i]) * 1099511628211ULL;
+    h = (h ^ (unsigned long long)T_[i]) * 1099511628211ULL;
+  }
+  key += "_" + std::to_string(h);
+  auto time_one = [](EngineBase* base, float* ms) -> mppi_status {
+    Engine* self = static_cast<Engine*>(base);
+    std::vector<float> x0((size_t)self->I_ * S, 0.0f);
+    memcpy(self->x0_h_.p, x0.data(), sizeof(float) * x0.size());
+    memcpy(self->mean_h_.p, self->control_.data(), sizeof(float) * self->control_.size());
+    cudaEvent_t e0, e1;
+    MG_CUDA(cudaEventCreate(&e0));
+    MG_CUDA(cudaEventCreate(&e1));
+    MG_TRY(self->enqueue_solve(1));  // warm-up
+    MG_CUDA(cudaEventRecord(e0, self->stream_));
+    for (int r = 0; r < 3; ++r) MG_TRY(self->enqueue_solve(1));
+    MG_CUDA(cudaEventRecord(e1, self->stream_));
+    MG_CUDA(cudaEventSynchronize(e1));
+    MG_CUDA(cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return MPPI_OK;
+  };
+  return autotune_impl(this, cache_path, key, time_one);
+}
+
+// Kernel-level rollout of one instance (launchRolloutKernel, mppi_common.cu:1335-1361): temporary descriptors and
+// counters are allocated on the stream and freed after the launch.
+template <class Model>
+mppi_status standalone_rollout(const void* dyn, const void* cost, const mppi_sampling_params* sp, const float* x0_d,
+                               const float* controls_d, const float* mean_d, float* costs_d, int K, int T, float dt,
+                               float lambda, float alpha, cudaStream_t s)
+{
+  constexpr int C = Model::CONTROL_DIM;
+  constexpr int NS = 128;
+  constexpr int TCH = RolloutShape<NS, C>::TCH;
+  MG_CHECK(K >= 1 && T >= 1, "K and T must be >= 1");
+  MG_CHECK(((uintptr_t)controls_d & 15) == 0, "controls must be 16-byte aligned");
+  InstDesc d{};
+  d.K = K;
+  d.T = T;
+  d.num_chunks = 1;
+  std::vector<int2> tiles;
+  for (int k0 = 0; k0 < K; k0 += NS) tiles.push_back(make_int2(0, k0));
+  DevBuf<InstDesc> inst_d;
+  DevBuf<int2> tiles_d;
+  DevBuf<typename Model::DynParams> dyn_d;
+  DevBuf<typename Model::CostParams> cost_d;
+  DevBuf<unsigned int> cnt_d;
+  MG_TRY(inst_d.alloc(1));
+  MG_TRY(tiles_d.alloc(tiles.size()));
+  MG_TRY(dyn_d.alloc(1));
+  MG_TRY(cost_d.alloc(1));
+  MG_TRY(cnt_d.alloc(4));
+  MG_CUDA(cudaMemcpyAsync(inst_d.p, &d, sizeof(d), cudaMemcpyHostToDevice, s));
+  MG_CUDA(cudaMemcpyAsync(tiles_d.p, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice, s));
+  MG_CUDA(cudaMemcpyAsync(dyn_d.p, dyn, sizeof(typename Model::DynParams), cudaMemcpyHostToDevice, s));
+  MG_CUDA(cudaMemcpyAsync(cost_d.p, cost, sizeof(typename Model::CostParams), cudaMemcpyHostToDevice, s));
+  MG_CUDA(cudaMemsetAsync(cnt_d.p, 0, sizeof(unsigned int) * 4, s));
+  fill_u32_kernel<<<1, 32, 0, s>>>(cnt_d.p + 2, kOrderedPosInf, 1);
+  RolloutArgs<Model> a;
+  a.inst = inst_d.p;
+  a.tiles = tiles_d.p;
+  a.num_tiles = (int)tiles.size();
+  a.dyn = dyn_d.p;
+  a.cost = cost_d.p;
+  memset(&a.aux, 0, sizeof(a.aux));
+  a.x0 = x0_d;
+  a.samples = controls_d;
+  a.mean = mean_d;
+  a.costs = costs_d;
+  a.baseline_bits = cnt_d.p + 2;
+  a.tile_counter = cnt_d.p;
+  a.dt = dt;
+  a.lambda = lambda;
+  a.alpha = alpha;
+  a.use_likelihood = 0;
+  for (int c = 0; c < C; ++c)
+    if (sp->control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
+  mppi_control_constraints cc;
+  mppi_default_constraints(&cc);
+  a.sh = make_sample_shared(*sp, cc);
+  rollout_kernel<Model, NS, TCH><<<(int)tiles.size(), NS, 0, s>>>(a);
+  MG_CUDA(cudaGetLastError());
+  MG_CUDA(cudaStreamSynchronize(s));
+  return MPPI_OK;
+}
+
+}  // namespace mg

@@ -1,0 +1,539 @@
+// mg_kernels.cuh — the MPPI iteration as three batched kernels: sample, rollout, weights+update.
+//
+// All kernels take a table of instances (independent controllers with their own K, T, parameters and nominal
+// control) and a work list, so one launch serves any number of uneven instances.  Data layout in HBM:
+//   samples   float[sum_i pad4(K_i*T_i*C)]   instance i at u_off, element ((k*T_i + t)*C + c)   ([D=1][K][T][C] of
+//             the reference, sampling_distribution.cu:108-116)
+//   costs     float[sum_i K_i]               instance i at k_off
+//   weights   float[sum_i K_i]
+//   mean      float[sum_i T_i*C]             instance i at t_off (the nominal control / importance sampler)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mg_math.cuh"
+#include "mg_models.cuh"
+
+namespace mg
+{
+constexpr int kMaxC = MPPI_MAX_CONTROL_DIM;
+constexpr int kMaxS = MPPI_MAX_STATE_DIM;
+
+struct InstDesc
+{
+  int K, T;
+  int k_off;         // into costs / weights
+  int t_off;         // into mean (floats)
+  long long u_off;   // into samples (floats, multiple of 4)
+  long long spec_off;  // into the colored-noise spectrum (floats)
+  int x_off;         // into x0 (floats)
+  int num_chunks;    // weight/update chunks of this instance
+};
+
+// Uniform (per handle) sampling + constraint parameters.
+struct SampleShared
+{
+  float std_dev[kMaxC];
+  float control_cost_coeff[kMaxC];
+  float lower[kMaxC], upper[kMaxC], deadband[kMaxC], zero[kMaxC];
+  float pure_pct;
+};
+
+// Ordered-integer encoding of a float so unsigned atomicMin orders like the float (NaN counts as +inf).
+__device__ __forceinline__ unsigned int float_to_ordered(float f)
+{
+  if (f != f) f = __int_as_float(0x7f800000);
+  const unsigned int b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float ordered_to_float(unsigned int o)
+{
+  const unsigned int b = (o & 0x80000000u) ? (o & 0x7fffffffu) : ~o;
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(b);
+#else
+  float f;
+  memcpy(&f, &b, 4);
+  return f;
+#endif
+}
+constexpr unsigned int kOrderedPosInf = 0xff800000u;
+
+// ============================================================================================== 1. Gaussian sampler
+// setGaussianControls (gaussian.cu:17-277) fused with the noise generation it consumes (curandGenerateNormal,
+// gaussian.cu:375-395) and with Dynamics::enforceConstraints (dynamics.cu:107-126).  Each thread writes whole float4
+// quads; the Philox block index of a quad is its quad index inside the instance, the Philox stream is the instance,
+// and the Philox counter is the handle's iteration counter (read from device memory, so a captured graph advances
+// it without host involvement).
+struct SampleArgs
+{
+  const InstDesc* inst;
+  const int2* work;  // (instance, first quad)
+  int num_work;
+  int quads_per_item;
+  float* samples;
+  const float* mean;
+  const float* injected;  // standard-normal noise in samples layout, or nullptr for Philox
+  const unsigned int* noise_counter;
+  uint32_t seed_lo, seed_hi;
+  int stride;
+  float decay_pow;
+  SampleShared sh;
+};
+
+template <int C>
+__global__ void __launch_bounds__(256) gaussian_sample_kernel(const __grid_constant__ SampleArgs a)
+{
+  for (int item = blockIdx.x; item < a.num_work; item += gridDim.x)
+  {
+    const int2 w = a.work[item];
+    const InstDesc d = a.inst[w.x];
+    const long long n = (long long)d.K * d.T * C;
+    const long long nq = (n + 3) / 4;
+    const int TC = d.T * C;
+    const float pure_threshold = (1.0f - a.sh.pure_pct) * (float)d.K;
+    const uint32_t counter = a.noise_counter ? *a.noise_counter : 0u;
+    const long long q_end = min((long long)w.y + a.quads_per_item, nq);
+    for (long long q = (long long)w.y + threadIdx.x; q < q_end; q += blockDim.x)
+    {
+      float4 z;
+      if (a.injected)
+      {
+        const float* src = a.injected + d.u_off + 4 * q;
+        if (4 * q + 3 < n)
+        {
+          z = *reinterpret_cast<const float4*>(src);
+        }
+        else
+        {  // tail quad: never read past the caller's buffer
+          z.x = src[0];
+          z.y = (4 * q + 1 < n) ? src[1] : 0.0f;
+          z.z = (4 * q + 2 < n) ? src[2] : 0.0f;
+          z.w = 0.0f;
+        }
+      }
+      else
+      {
+        z = philox_normal4((uint64_t)q, (uint32_t)w.x, counter, a.seed_lo, a.seed_hi);
+      }
+      float zz[4] = { z.x, z.y, z.z, z.w };
+      float out[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        const long long e = 4 * q + j;
+        const int k = (int)(e / TC);
+        const int rem = (int)(e - (long long)k * TC);
+        const int t = rem / C;
+        const int c = rem - t * C;
+        const float m = (e < n) ? a.mean[d.t_off + rem] : 0.0f;
+        const float sd = a.decay_pow * a.sh.std_dev[c];
+        float u;
+        if (k == 0 || t < a.stride)
+          u = m;
+        else if ((float)k >= pure_threshold)
+          u = sd * zz[j];
+        else
+          u = fmaf(sd, zz[j], m);
+        out[j] = enforce_constraint(u, a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c], a.sh.zero[c]);
+      }
+      float* dst = a.samples + d.u_off + 4 * q;
+      if (4 * q + 3 < n)
+      {
+        *reinterpret_cast<float4*>(dst) = make_float4(out[0], out[1], out[2], out[3]);
+      }
+      else
+      {
+        for (int j = 0; j < 4; ++j)
+          if (4 * q + j < n) dst[j] = out[j];
+      }
+    }
+  }
+}
+
+// ============================================================================================== 2. rollout
+// rolloutKernel (mppi_common.cu:35-153) restructured for the GB300: one thread per sample with its state in
+// registers; the CTA stages a time chunk of its samples' controls in shared memory with coalesced 16-byte loads
+// (rows padded by 4 floats so the per-thread 16-byte reads are bank-conflict free); running cost accumulates in FP32
+// in reference order; cost = running / T + terminal / T (computeAndSaveCost, mppi_common.cu:879-889).  The CTA also
+// folds its samples into the instance's minimum cost with one atomicMin, which the weight kernel consumes as the
+// baseline.  The kernel is persistent: CTAs pull (instance, first sample) tiles from a work list ordered by
+// decreasing cost through an atomic counter; the last CTA to finish resets the counters for the next launch.
+template <class Model>
+struct RolloutArgs
+{
+  const InstDesc* inst;
+  const int2* tiles;  // (instance, first sample)
+  int num_tiles;
+  const typename Model::DynParams* dyn;
+  const typename Model::CostParams* cost;
+  ModelAux aux;
+  const float* x0;
+  const float* samples;
+  const float* mean;
+  float* costs;
+  unsigned int* baseline_bits;  // per instance, ordered-int min
+  unsigned int* tile_counter;   // [0] = next tile, [1] = finished CTAs
+  float dt, lambda, alpha;
+  int use_likelihood;
+  SampleShared sh;
+};
+
+template <class Model, int NS, int TCH>
+__global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ RolloutArgs<Model> a)
+{
+  constexpr int S = Model::STATE_DIM;
+  constexpr int C = Model::CONTROL_DIM;
+  constexpr int ROW = TCH * C + 4;  // floats per staged sample row
+  static_assert((TCH * C) % 4 == 0, "time chunk must hold whole float4s");
+  __shared__ __align__(16) float stage[NS * ROW];
+  __shared__ int s_tile;
+  __shared__ unsigned int s_min;
+
+  const int tid = threadIdx.x;
+  for (;;)
+  {
+    if (tid == 0)
+    {
+      s_tile = (int)atomicAdd(&a.tile_counter[0], 1u);
+      s_min = kOrderedPosInf;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= a.num_tiles) break;
+    const int2 w = a.tiles[tile];
+    const InstDesc d = a.inst[w.x];
+    const int k = w.y + tid;
+    const bool active = k < d.K;
+    const int rows = min(NS, d.K - w.y);
+    const typename Model::DynParams dp = a.dyn[w.x];
+    const typename Model::CostParams& cp = a.cost[w.x];
+
+    float x[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i) x[i] = a.x0[d.x_off + i];
+    float running = 0.0f;
+    const bool aligned = ((d.T * C) & 3) == 0;
+    const float* base = a.samples + d.u_off + (long long)w.y * d.T * C;
+
+    for (int t0 = 0; t0 < d.T; t0 += TCH)
+    {
+      const int nt = min(TCH, d.T - t0);
+      // ---- stage controls [rows][t0, t0+nt) into shared memory
+      if (aligned && (nt * C) % 4 == 0)
+      {
+        const int q_per_row = nt * C / 4;
+        const int total_q = rows * q_per_row;
+        for (int i = tid; i < total_q; i += NS)
+        {
+          const int r = i / q_per_row;
+          const int qq = i - r * q_per_row;
+          const float4 v = __ldg(reinterpret_cast<const float4*>(base + (long long)r * d.T * C + t0 * C) + qq);
+          *reinterpret_cast<float4*>(&stage[r * ROW + 4 * qq]) = v;
+        }
+      }
+      else
+      {
+        const int per_row = nt * C;
+        const int total = rows * per_row;
+        for (int i = tid; i < total; i += NS)
+        {
+          const int r = i / per_row;
+          const int j = i - r * per_row;
+          stage[r * ROW + j] = __ldg(base + (long long)r * d.T * C + t0 * C + j);
+        }
+      }
+      __syncthreads();
+      if (active)
+      {
+        const float* urow = &stage[tid * ROW];
+        auto do_step = [&](const float* u, int t) {
+          float xn[S];
+          euler_step<Model>(dp, x, u, xn, a.dt);
+          float step_cost = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
+          if (a.use_likelihood)
+          {
+            // GaussianDistributionImpl::computeLikelihoodRatioCost (gaussian.cu:490-574)
+            const bool zero_mean = (float)k >= (1.0f - a.sh.pure_pct) * (float)d.K;
+            float lc = 0.0f;
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+            {
+              const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + c];
+              const float sd = a.sh.std_dev[c];
+              lc += a.sh.control_cost_coeff[c] * m * (m - 2.0f * u[c]) / (sd * sd);
+            }
+            step_cost += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
+          }
+          running += step_cost;
+#pragma unroll
+          for (int i = 0; i < S; ++i) x[i] = xn[i];
+        };
+        int tt = 0;
+        if constexpr (4 % C == 0)
+        {
+          // one 16-byte shared-memory read feeds 4/C steps
+          constexpr int G = 4 / C;
+          for (; tt + G <= nt; tt += G)
+          {
+            const float4 v = *reinterpret_cast<const float4*>(urow + tt * C);
+            const float uu[4] = { v.x, v.y, v.z, v.w };
+#pragma unroll
+            for (int g = 0; g < G; ++g) do_step(uu + g * C, t0 + tt + g);
+          }
+        }
+        for (; tt < nt; ++tt)
+        {
+          float u[C];
+#pragma unroll
+          for (int c = 0; c < C; ++c) u[c] = urow[tt * C + c];
+          do_step(u, t0 + tt);
+        }
+      }
+      __syncthreads();
+    }
+    unsigned int o = kOrderedPosInf;
+    if (active)
+    {
+      const float tf = (float)d.T;
+      const float cost = running / tf + Model::terminalCost(cp, a.aux, x) / tf;
+      a.costs[d.k_off + k] = cost;
+      o = float_to_ordered(cost);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) o = min(o, __shfl_xor_sync(0xffffffffu, o, off));
+    if ((tid & 31) == 0) atomicMin(&s_min, o);
+    __syncthreads();
+    if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+  }
+  // last CTA out resets the work counters for the next launch
+  if (tid == 0)
+  {
+    __threadfence();
+    const unsigned int done = atomicAdd(&a.tile_counter[1], 1u);
+    if (done == gridDim.x - 1)
+    {
+      a.tile_counter[0] = 0u;
+      a.tile_counter[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// ============================================================================================== 3. weights + update
+// fullGPUcomputeWeights (mppi_common.cu:1067-1089) and weightedReductionKernelDeviceNorm (mppi_common.cu:746-773) in
+// one multi-CTA kernel.  Each CTA owns a chunk of one instance's samples: it computes w_k = exp(-(c_k - b)/lambda)
+// with the baseline subtraction in FP64, accumulates the chunk's sum of weights (FP64) and the chunk's weighted
+// control sums sum_k w_k u_k[t][c] (FP32, one column per thread, coalesced rows), and writes them as partials.  The
+// last CTA of an instance (arrival counter; no waiting) adds the partials in chunk order — a fixed order, so the
+// result is deterministic — divides by the normaliser and writes the new nominal control, baseline and normaliser,
+// then resets the instance's counters.  The last instance to finish advances the noise counter.
+struct WeightsArgs
+{
+  const InstDesc* inst;
+  const int4* chunks;  // (instance, k_begin, k_end, chunk index within instance)
+  const long long* part_off;  // per chunk: offset of its partial row in `partials` (floats)
+  const int* inst_chunk0;     // per instance: global index of its first chunk
+  int num_chunks;
+  int num_instances;
+  const float* costs;
+  float* weights;
+  const float* samples;
+  float* partials;
+  double* part_w;   // per chunk: sum w, sum w^2
+  unsigned int* baseline_bits;
+  unsigned int* arrive;  // per instance
+  unsigned int* inst_done;  // [0]
+  unsigned int* noise_counter;
+  float* mean_out;
+  float* baseline_norm;  // per instance (baseline, normaliser)
+  double* stats;         // per instance: normaliser, sum w^2, baseline
+  float lambda_inv;
+  int weights_given;        // 1: read w from `weights` instead of computing it from `costs`
+  const float* given_norm;  // non-null: divide by given_norm[0] (a device float) instead of the summed weights
+};
+
+template <int C>
+__global__ void __launch_bounds__(256) weights_update_kernel(const __grid_constant__ WeightsArgs a)
+{
+  constexpr int MAXK = 256;  // samples per chunk held in shared memory
+  __shared__ float s_w[MAXK];
+  __shared__ double s_red[2][8];
+  __shared__ unsigned int s_last;
+
+  const int tid = threadIdx.x;
+  const int4 ch = a.chunks[blockIdx.x];
+  const InstDesc d = a.inst[ch.x];
+  const int kb = ch.y, ke = ch.z, nk = ke - kb;
+  const float b = ordered_to_float(a.baseline_bits[ch.x]);
+  const double bd = (double)b;
+  const double linv = (double)a.lambda_inv;
+
+  // weights of this chunk
+  double sw = 0.0, sw2 = 0.0;
+  for (int i = tid; i < nk; i += blockDim.x)
+  {
+    float wk;
+    if (a.weights_given)
+    {
+      wk = a.weights[d.k_off + kb + i];
+    }
+    else
+    {
+      const float c = a.costs[d.k_off + kb + i];
+      const double diff = (double)c - bd;
+      wk = expf((float)(-diff * linv));
+      a.weights[d.k_off + kb + i] = wk;
+    }
+    s_w[i] = wk;
+    sw += (double)wk;
+    sw2 += (double)wk * (double)wk;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+  {
+    sw += __shfl_xor_sync(0xffffffffu, sw, off);
+    sw2 += __shfl_xor_sync(0xffffffffu, sw2, off);
+  }
+  if ((tid & 31) == 0)
+  {
+    s_red[0][tid >> 5] = sw;
+    s_red[1][tid >> 5] = sw2;
+  }
+  __syncthreads();
+
+  // weighted control sums: thread j owns columns j, j + blockDim, ...
+  const int TC = a.samples ? d.T * C : 0;
+  const float* ubase = a.samples + d.u_off + (long long)kb * TC;
+  float* prow = a.partials + a.part_off[blockIdx.x];
+  for (int j = tid; j < TC; j += blockDim.x)
+  {
+    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc3 = 0.0f;
+    int i = 0;
+    for (; i + 4 <= nk; i += 4)
+    {
+      acc0 = fmaf(s_w[i], __ldg(ubase + (long long)i * TC + j), acc0);
+      acc1 = fmaf(s_w[i + 1], __ldg(ubase + (long long)(i + 1) * TC + j), acc1);
+      acc2 = fmaf(s_w[i + 2], __ldg(ubase + (long long)(i + 2) * TC + j), acc2);
+      acc3 = fmaf(s_w[i + 3], __ldg(ubase + (long long)(i + 3) * TC + j), acc3);
+    }
+    for (; i < nk; ++i) acc0 = fmaf(s_w[i], __ldg(ubase + (long long)i * TC + j), acc0);
+    prow[j] = (acc0 + acc1) + (acc2 + acc3);
+  }
+  if (tid == 0)
+  {
+    double t0 = 0.0, t1 = 0.0;
+    for (int wi = 0; wi < (int)(blockDim.x >> 5); ++wi)
+    {
+      t0 += s_red[0][wi];
+      t1 += s_red[1][wi];
+    }
+    a.part_w[2 * blockIdx.x] = t0;
+    a.part_w[2 * blockIdx.x + 1] = t1;
+  }
+
+  // arrival: the last chunk of the instance finalises
+  __threadfence();
+  __syncthreads();
+  if (tid == 0)
+  {
+    const unsigned int prev = atomicAdd(&a.arrive[ch.x], 1u);
+    s_last = (prev == (unsigned int)(d.num_chunks - 1)) ? 1u : 0u;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+
+  const int c0 = a.inst_chunk0[ch.x];
+  double eta = 0.0, w2 = 0.0;
+  for (int c = 0; c < d.num_chunks; ++c)
+  {
+    eta += __ldcg(&a.part_w[2 * (c0 + c)]);
+    w2 += __ldcg(&a.part_w[2 * (c0 + c) + 1]);
+  }
+  const double div = a.given_norm ? (double)a.given_norm[0] : eta;
+  for (int j = tid; j < TC; j += blockDim.x)
+  {
+    double s = 0.0;
+    for (int c = 0; c < d.num_chunks; ++c) s += (double)__ldcg(a.partials + a.part_off[c0 + c] + j);
+    a.mean_out[d.t_off + j] = (float)(s / div);
+  }
+  if (tid == 0)
+  {
+    a.baseline_norm[2 * ch.x] = b;
+    a.baseline_norm[2 * ch.x + 1] = (float)eta;
+    a.stats[3 * ch.x] = eta;
+    a.stats[3 * ch.x + 1] = w2;
+    a.stats[3 * ch.x + 2] = bd;
+    a.arrive[ch.x] = 0u;
+    a.baseline_bits[ch.x] = kOrderedPosInf;
+    __threadfence();
+    const unsigned int fin = atomicAdd(a.inst_done, 1u);
+    if (fin == (unsigned int)(a.num_instances - 1))
+    {
+      *a.inst_done = 0u;
+      if (a.noise_counter) *a.noise_counter += 1u;
+      __threadfence();
+    }
+  }
+}
+
+// Per-system minimum of costs into ordered-int slots (the baseline pass of fullGPUcomputeWeights,
+// computeBaselineCost, mppi_common.cu:938-992), for the kernel-level weight-transform entry point.
+static __global__ void min_cost_kernel(const float* costs, int num_rollouts, int num_systems, unsigned int* out_bits)
+{
+  const int sys = blockIdx.y;
+  if (sys >= num_systems) return;
+  unsigned int o = kOrderedPosInf;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < num_rollouts; k += gridDim.x * blockDim.x)
+    o = min(o, float_to_ordered(costs[(size_t)sys * num_rollouts + k]));
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) o = min(o, __shfl_xor_sync(0xffffffffu, o, off));
+  if ((threadIdx.x & 31) == 0) atomicMin(&out_bits[sys], o);
+}
+
+static __global__ void fill_u32_kernel(unsigned int* p, unsigned int v, int n)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
+}
+
+static __global__ void bump_counter_kernel(unsigned int* p) { *p += 1u; }
+
+// ============================================================================================== test entry kernels
+static __global__ void philox_normal_kernel(float* out, size_t n, uint32_t k0, uint32_t k1, uint64_t offset)
+{
+  const size_t nq = (n + 3) / 4;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nq; q += (size_t)gridDim.x * blockDim.x)
+  {
+    const uint64_t blk = offset + q;
+    const u32x4 r = philox4x32_10(u32x4{ (uint32_t)blk, (uint32_t)(blk >> 32), 0u, 0u }, k0, k1);
+    float z[4];
+    box_muller(r.x, r.y, &z[0], &z[1]);
+    box_muller(r.z, r.w, &z[2], &z[3]);
+    for (int j = 0; j < 4; ++j)
+      if (4 * q + j < n) out[4 * q + j] = z[j];
+  }
+}
+
+static __global__ void philox_raw_kernel(uint32_t* out, size_t nblocks, u32x4 ctr, uint32_t k0, uint32_t k1)
+{
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nblocks; i += (size_t)gridDim.x * blockDim.x)
+  {
+    u32x4 c = ctr;
+    c.x += (uint32_t)i;
+    const u32x4 r = philox4x32_10(c, k0, k1);
+    out[4 * i] = r.x;
+    out[4 * i + 1] = r.y;
+    out[4 * i + 2] = r.z;
+    out[4 * i + 3] = r.w;
+  }
+}
+
+static __global__ void sincos_kernel(const float* x, float* s, float* c, size_t n)
+{
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    sincos_f(x[i], &s[i], &c[i]);
+}
+
+}  // namespace mg

@@ -1,0 +1,258 @@
+// mg_models.cuh — Dynamics + Cost plugins compiled into the engine.
+//
+// Each model type mirrors the reference's plugin contract: compile-time STATE_DIM / CONTROL_DIM / OUTPUT_DIM
+// (dynamics.cuh:75-77), computeDynamics(x, u, xdot) (dynamics.cuh:369), Euler step (dynamics.cu:128-152),
+// computeStateCost(y, t) + computeControlCost(u, t) (cost.cuh:146, 205) and terminalCost(y) (cost.cuh:161).  The
+// functions are __host__ __device__ so the host side reuses them for the nominal state trajectory
+// (Controller::computeOutputTrajectoryHelper, controller.cuh:664-684), as the reference's plugins carry host twins.
+//
+// Control constraints are the generic per-control clamp + deadband of Dynamics::enforceConstraints and depend only on
+// the control, so the engine applies them once when the samples are written (the reference applies them inside the
+// rollout and writes the constrained control back, mppi_common.cu:117-124; both leave the same values in the sample
+// buffer and feed the same controls to the dynamics).
+#pragma once
+
+#include "../../include/mppi_gb.h"
+#include "mg_math.cuh"
+
+namespace mg
+{
+// Read-only view of a row-major costmap; cell (0, 0) is centred at origin + resolution / 2.
+struct CostmapView
+{
+  const float* data;
+  int width, height;
+  float inv_resolution;  // unused by the lookup (kept for callers); the lookup divides by resolution
+  float resolution, origin_x, origin_y;
+};
+
+// Bilinear lookup with clamp-to-edge addressing, in the order of the reference's CPU texture twin
+// (TwoDTextureHelper::queryTextureCPU, two_d_texture_helper.cu:151-235).  The reference's GPU path uses the texture
+// unit (tex2D, two_d_texture_helper.cu:66-72), whose interpolation weights are 9-bit fixed point; the engine
+// interpolates in FP32 on both sides.
+MG_HD float costmap_bilinear(const CostmapView& m, float x, float y)
+{
+  float px = (x - m.origin_x) / m.resolution - 0.5f;
+  float py = (y - m.origin_y) / m.resolution - 0.5f;
+  px = fminf(fmaxf(px, 0.0f), (float)(m.width - 1));
+  py = fminf(fmaxf(py, 0.0f), (float)(m.height - 1));
+  int x0 = (int)floorf(px);
+  int y0 = (int)floorf(py);
+  x0 = x0 < m.width - 2 ? x0 : m.width - 2;
+  y0 = y0 < m.height - 2 ? y0 : m.height - 2;
+  const float fx = px - (float)x0;
+  const float fy = py - (float)y0;
+  const float* row0 = m.data + (size_t)y0 * m.width;
+  const float* row1 = row0 + m.width;
+#if defined(__CUDA_ARCH__)
+  const float q00 = __ldg(row0 + x0), q01 = __ldg(row0 + x0 + 1);
+  const float q10 = __ldg(row1 + x0), q11 = __ldg(row1 + x0 + 1);
+#else
+  const float q00 = row0[x0], q01 = row0[x0 + 1];
+  const float q10 = row1[x0], q11 = row1[x0 + 1];
+#endif
+  const float top = q00 * (1.0f - fx) + q01 * fx;
+  const float bot = q10 * (1.0f - fx) + q11 * fx;
+  return top * (1.0f - fy) + bot * fy;
+}
+
+// Shared (per-launch) data that some costs need besides their parameter block.
+struct ModelAux
+{
+  CostmapView map;
+};
+
+// --------------------------------------------------------------------------------------------------------- cartpole
+// CartpoleDynamics (cartpole_dynamics.cu:87-105) with the swing-up running cost
+// x_coeff*x^2 + x_dot_coeff*xdot^2 + cos_coeff*(1 + cos theta)^2 + theta_dot_coeff*thetadot^2.
+struct CartpoleModel
+{
+  static constexpr int STATE_DIM = 4, CONTROL_DIM = 1, OUTPUT_DIM = 4;
+  static constexpr int kModelId = MPPI_MODEL_CARTPOLE;
+  static constexpr bool kNeedsCostmap = false;
+  static constexpr int kFlopsPerStep = 60;  // counted from the source below (sin/cos polynomial included)
+  using DynParams = mppi_cartpole_params;
+  using CostParams = mppi_cartpole_cost_params;
+
+  static MG_HD void computeDynamics(const DynParams& p, const float* x, const float* u, float* xd)
+  {
+    const float th = normalize_angle(x[2]);
+    float s, c;
+    sincos_f(th, &s, &c);
+    const float td = x[3], f = u[0];
+    const float mc = p.cart_mass, mp = p.pole_mass, lp = p.pole_length, g = p.gravity;
+    xd[0] = x[1];
+    xd[1] = (f + mp * s * (lp * (td * td) + g * c)) / (mc + mp * (s * s));
+    xd[2] = td;
+    xd[3] = (-f * c - mp * lp * (td * td) * c * s - (mc + mp) * g * s) / (lp * (mc + mp * (s * s)));
+  }
+  static MG_HD float computeStateCost(const CostParams& q, const ModelAux&, const float* y, int)
+  {
+    const float th = normalize_angle(y[2]);
+    float s, c;
+    sincos_f(th, &s, &c);
+    const float a = 1.0f + c;
+    return q.x_coeff * (y[0] * y[0]) + q.x_dot_coeff * (y[1] * y[1]) + q.cos_coeff * (a * a) +
+           q.theta_dot_coeff * (y[3] * y[3]);
+  }
+  static MG_HD float computeControlCost(const CostParams&, const float*, int) { return 0.0f; }
+  static MG_HD float terminalCost(const CostParams& q, const ModelAux& aux, const float* y)
+  {
+    return computeStateCost(q, aux, y, 0) * q.terminal_coeff;
+  }
+};
+
+// -------------------------------------------------------------------------------------------- double integrator
+// DoubleIntegratorDynamics (di_dynamics.cu:46-53); cost = QuadraticCostImpl-style weighted squared error to the goal
+// (quadratic_cost.cu:35-48) + obstacle_cost if strictly inside any circle (composed like
+// DoubleIntegratorCircleCost, double_integrator_circle_cost.cu:8-32).
+struct DoubleIntegratorModel
+{
+  static constexpr int STATE_DIM = 4, CONTROL_DIM = 2, OUTPUT_DIM = 4;
+  static constexpr int kModelId = MPPI_MODEL_DOUBLE_INTEGRATOR;
+  static constexpr bool kNeedsCostmap = false;
+  static constexpr int kFlopsPerStep = 8 + 11 + 8 * 6;
+  using DynParams = mppi_double_integrator_params;
+  using CostParams = mppi_di_obstacle_cost_params;
+
+  static MG_HD void computeDynamics(const DynParams&, const float* x, const float* u, float* xd)
+  {
+    xd[0] = x[2];
+    xd[1] = x[3];
+    xd[2] = u[0];
+    xd[3] = u[1];
+  }
+  static MG_HD float quad(const CostParams& q, const float* y)
+  {
+    const float d0 = y[0] - q.goal[0], d1 = y[1] - q.goal[1], d2 = y[2] - q.goal[2], d3 = y[3] - q.goal[3];
+    return q.coeff[0] * (d0 * d0) + q.coeff[1] * (d1 * d1) + q.coeff[2] * (d2 * d2) + q.coeff[3] * (d3 * d3);
+  }
+  static MG_HD float computeStateCost(const CostParams& q, const ModelAux&, const float* y, int)
+  {
+    float cost = quad(q, y);
+    bool inside = false;
+    for (int j = 0; j < q.num_obstacles; ++j)
+    {
+      const float ox = y[0] - q.obstacle_x[j];
+      const float oy = y[1] - q.obstacle_y[j];
+      const float r = q.obstacle_radius[j];
+      inside = inside || (ox * ox + oy * oy < r * r);
+    }
+    if (inside) cost = cost + q.obstacle_cost;
+    return cost;
+  }
+  static MG_HD float computeControlCost(const CostParams&, const float*, int) { return 0.0f; }
+  static MG_HD float terminalCost(const CostParams& q, const ModelAux&, const float* y)
+  {
+    return quad(q, y) * q.terminal_coeff;
+  }
+};
+
+// --------------------------------------------------------------------------------------------- kinematic bicycle
+// State (x, y, yaw, v), control (accel, steer).  xdot = v cos yaw, ydot = v sin yaw, yawdot = v tan(steer) / L,
+// vdot = accel (closest reference model: DubinsDynamics, dubins.cu:60-65).  Cost: costmap + speed tracking + steer
+// effort.
+struct BicycleCostmapModel
+{
+  static constexpr int STATE_DIM = 4, CONTROL_DIM = 2, OUTPUT_DIM = 4;
+  static constexpr int kModelId = MPPI_MODEL_BICYCLE_COSTMAP;
+  static constexpr bool kNeedsCostmap = true;
+  static constexpr int kFlopsPerStep = 2 * 22 + 12 + 25;
+  using DynParams = mppi_bicycle_params;
+  using CostParams = mppi_costmap_cost_params;
+
+  static MG_HD void computeDynamics(const DynParams& p, const float* x, const float* u, float* xd)
+  {
+    float sy, cy, sd, cd;
+    sincos_f(x[2], &sy, &cy);
+    sincos_f(u[1], &sd, &cd);
+    xd[0] = x[3] * cy;
+    xd[1] = x[3] * sy;
+    xd[2] = x[3] * (sd / cd) / p.wheelbase;
+    xd[3] = u[0];
+  }
+  static MG_HD float speedMapCost(const CostParams& q, const ModelAux& aux, const float* y)
+  {
+    const float dv = y[3] - q.speed_target;
+    return q.map_coeff * costmap_bilinear(aux.map, y[0], y[1]) + q.speed_coeff * (dv * dv);
+  }
+  static MG_HD float computeStateCost(const CostParams& q, const ModelAux& aux, const float* y, int)
+  {
+    return speedMapCost(q, aux, y);
+  }
+  static MG_HD float computeControlCost(const CostParams& q, const float* u, int) { return q.steer_coeff * (u[1] * u[1]); }
+  static MG_HD float terminalCost(const CostParams& q, const ModelAux& aux, const float* y)
+  {
+    return speedMapCost(q, aux, y) * q.terminal_coeff;
+  }
+};
+
+// ------------------------------------------------------------------------------------------ dynamic bicycle (slip)
+// State (x, y, yaw, vx, vy, yaw_rate, steer), control (throttle, steer_cmd); linear tyres with one cornering stiffness,
+// first-order steering actuator.  Kinematic rows follow NeuralNetModel::computeKinematics (ar_nn_model.cu:119-124).
+struct BicycleSlipModel
+{
+  static constexpr int STATE_DIM = 7, CONTROL_DIM = 2, OUTPUT_DIM = 7;
+  static constexpr int kModelId = MPPI_MODEL_BICYCLE_SLIP;
+  static constexpr bool kNeedsCostmap = true;
+  static constexpr int kFlopsPerStep = 3 * 22 + 45 + 25;
+  using DynParams = mppi_bicycle_slip_params;
+  using CostParams = mppi_costmap_cost_params;
+
+  static MG_HD void computeKinematics(const float* x, float* xd)
+  {
+    float sy, cy;
+    sincos_f(x[2], &sy, &cy);
+    xd[0] = x[3] * cy - x[4] * sy;
+    xd[1] = x[3] * sy + x[4] * cy;
+    xd[2] = x[5];
+  }
+  static MG_HD void computeDynamics(const DynParams& p, const float* x, const float* u, float* xd)
+  {
+    float sy, cy;
+    sincos_f(x[2], &sy, &cy);
+    const float vx = x[3], vy = x[4], r = x[5], d = x[6];
+    const float vxs = fmaxf(vx, p.min_vx);
+    const float af = d - (vy + p.lf * r) / vxs;
+    const float ar = -(vy - p.lr * r) / vxs;
+    const float fyf = p.cornering_stiffness * af;
+    const float fyr = p.cornering_stiffness * ar;
+    float sd, cd;
+    sincos_f(d, &sd, &cd);
+    const float fx = p.max_drive_force * u[0] - p.drag * vx;
+    xd[0] = vx * cy - vy * sy;
+    xd[1] = vx * sy + vy * cy;
+    xd[2] = r;
+    xd[3] = (fx - fyf * sd) / p.mass + vy * r;
+    xd[4] = (fyr + fyf * cd) / p.mass - vx * r;
+    xd[5] = (p.lf * fyf * cd - p.lr * fyr) / p.yaw_inertia;
+    xd[6] = (u[1] * p.max_steer - d) / p.steer_time_constant;
+  }
+  static MG_HD float speedMapCost(const CostParams& q, const ModelAux& aux, const float* y)
+  {
+    const float dv = y[3] - q.speed_target;
+    return q.map_coeff * costmap_bilinear(aux.map, y[0], y[1]) + q.speed_coeff * (dv * dv);
+  }
+  static MG_HD float computeStateCost(const CostParams& q, const ModelAux& aux, const float* y, int)
+  {
+    return speedMapCost(q, aux, y);
+  }
+  static MG_HD float computeControlCost(const CostParams& q, const float* u, int) { return q.steer_coeff * (u[1] * u[1]); }
+  static MG_HD float terminalCost(const CostParams& q, const ModelAux& aux, const float* y)
+  {
+    return speedMapCost(q, aux, y) * q.terminal_coeff;
+  }
+};
+
+// Euler step shared by every model (Dynamics::step -> updateState, dynamics.cu:128-152): x' = x + xdot * dt as one
+// fused multiply-add (the form the reference's device code compiles to).
+template <class Model>
+MG_HD void euler_step(const typename Model::DynParams& p, const float* x, const float* u, float* x_next, float dt)
+{
+  float xd[Model::STATE_DIM];
+  Model::computeDynamics(p, x, u, xd);
+#pragma unroll
+  for (int i = 0; i < Model::STATE_DIM; ++i) x_next[i] = fmaf(xd[i], dt, x[i]);
+}
+
+}  // namespace mg

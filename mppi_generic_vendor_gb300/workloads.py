@@ -1,0 +1,116 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+* ``cartpole``   — plain MPPI, cartpole, K=2048, T=100, sigma 1.0, lambda 1.0, force clamped to +-5 N, dt 0.02,
+  x0 with theta ~ U(-pi, pi) and the other states ~ U(-0.1, 0.1), receding horizon.
+* ``batched_di`` — 256 double-integrator instances, K ~ U{512, 1024, 2048, 4096, 8192}, T ~ U{32, 64, 128},
+  controls clamped to +-1, colored noise with exponents (1, 1) and sigma 0.5, goal + 8 circular obstacles
+  (centres U(-5, 5)^2, radii U(0.3, 1.0), cost 1000 inside).
+* ``bicycle``    — kinematic bicycle on a 512x512 costmap (0.1 m cells) built from 32 Gaussian bumps
+  (amplitude U(0, 10), sigma U(0.5, 3) m), speed target 8 m/s, K=16384, T=100, sigma (1.0, 0.3), lambda 2.0.
+
+There is no public dataset behind these configurations; every input is drawn from a recorded seed.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .controller import (BatchedMPPIController, BicycleDynamics, CartpoleDynamics, CartpoleSwingupCost,
+                         ColoredNoiseDistribution, CostmapCost, DoubleIntegratorDynamics,
+                         DoubleIntegratorObstacleCost, GaussianDistribution, VanillaMPPIController)
+
+
+@dataclass
+class Workload:
+    name: str
+    controller: BatchedMPPIController
+    x0: np.ndarray            # float32 [num_instances * S]
+    K: np.ndarray
+    T: np.ndarray
+    state_dim: int
+    control_dim: int
+    num_iters: int
+    description: dict = field(default_factory=dict)
+
+    @property
+    def sample_steps_per_iter(self) -> int:
+        return int(np.sum(self.K.astype(np.int64) * self.T))
+
+    @property
+    def control_floats(self) -> int:
+        return int(np.sum(self.K.astype(np.int64) * self.T)) * self.control_dim
+
+
+def cartpole(seed: int = 0, K: int = 2048, T: int = 100, stream: int = 0) -> Workload:
+    rng = np.random.default_rng(seed)
+    dyn = CartpoleDynamics(1.0, 1.0, 1.0, 9.81)
+    dyn.setControlRanges([(-5.0, 5.0)])
+    cost = CartpoleSwingupCost(10.0, 1.0, 100.0, 1.0, 0.0)
+    ctrl = VanillaMPPIController(dyn, cost, None, GaussianDistribution(std_dev=(1.0,)), 0.02, 1, 1.0, 0.0, T, K,
+                                 stream=stream, seed=seed)
+    x0 = np.array([rng.uniform(-0.1, 0.1), rng.uniform(-0.1, 0.1), rng.uniform(-np.pi, np.pi),
+                   rng.uniform(-0.1, 0.1)], dtype=np.float32)
+    return Workload("cartpole_K2048_T100", ctrl, x0, np.array([K]), np.array([T]), 4, 1, 1,
+                    dict(model="cartpole", K=K, T=T, sigma=1.0, lam=1.0, dt=0.02, seed=seed))
+
+
+def batched_di_params(seed: int = 0, num_instances: int = 256):
+    rng = np.random.default_rng(seed)
+    Ks = rng.choice([512, 1024, 2048, 4096, 8192], size=num_instances)
+    Ts = rng.choice([32, 64, 128], size=num_instances)
+    costs, x0 = [], []
+    for _ in range(num_instances):
+        obs = [(rng.uniform(-5, 5), rng.uniform(-5, 5), rng.uniform(0.3, 1.0)) for _ in range(8)]
+        goal = (rng.uniform(-4, 4), rng.uniform(-4, 4), 0.0, 0.0)
+        costs.append(DoubleIntegratorObstacleCost(goal=goal, coeff=(1.0, 1.0, 0.1, 0.1), terminal_coeff=10.0,
+                                                  obstacles=obs, obstacle_cost=1000.0))
+        x0.append(np.array([rng.uniform(-5, 5), rng.uniform(-5, 5), 0.0, 0.0], dtype=np.float32))
+    return Ks.astype(np.int32), Ts.astype(np.int32), costs, np.concatenate(x0)
+
+
+def batched_di(seed: int = 0, num_instances: int = 256, colored: bool = True, stream: int = 0) -> Workload:
+    Ks, Ts, costs, x0 = batched_di_params(seed, num_instances)
+    dyn = DoubleIntegratorDynamics()
+    dyn.setControlRanges([(-1.0, 1.0), (-1.0, 1.0)])
+    if colored:
+        sampler = ColoredNoiseDistribution(std_dev=(0.5, 0.5), exponents=(1.0, 1.0))
+    else:
+        sampler = GaussianDistribution(std_dev=(0.5, 0.5))
+    ctrl = BatchedMPPIController(dyn, costs, sampler, Ks, Ts, dt=0.02, max_iter=1, lambda_=1.0, seed=seed,
+                                 stream=stream)
+    name = f"batched_di_{num_instances}x_colored" if colored else f"batched_di_{num_instances}x_gaussian"
+    return Workload(name, ctrl, x0, Ks, Ts, 4, 2, 1,
+                    dict(model="double_integrator", instances=num_instances, sum_K=int(Ks.sum()),
+                         noise="colored beta=(1,1)" if colored else "gaussian", sigma=0.5, seed=seed))
+
+
+def gaussian_bump_costmap(seed: int = 0, size: int = 512, resolution: float = 0.1, bumps: int = 32) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    extent = size * resolution
+    c = (np.arange(size) + 0.5) * resolution
+    X, Y = np.meshgrid(c, c)
+    m = np.zeros((size, size), dtype=np.float64)
+    for _ in range(bumps):
+        a = rng.uniform(0, 10)
+        s = rng.uniform(0.5, 3.0)
+        cx, cy = rng.uniform(0, extent, 2)
+        m += a * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * s * s))
+    return m.astype(np.float32)
+
+
+def bicycle(seed: int = 0, K: int = 16384, T: int = 100, stream: int = 0) -> Workload:
+    rng = np.random.default_rng(seed + 1)
+    cmap = gaussian_bump_costmap(seed)
+    dyn = BicycleDynamics(2.5)
+    dyn.setControlRanges([(-3.0, 3.0), (-1.0, 1.0)])
+    cost = CostmapCost(map_coeff=1.0, speed_target=8.0, speed_coeff=1.0, steer_coeff=0.0, terminal_coeff=0.0,
+                       costmap=cmap, resolution=0.1, origin=(0.0, 0.0))
+    ctrl = VanillaMPPIController(dyn, cost, None, GaussianDistribution(std_dev=(1.0, 0.3)), 0.02, 1, 2.0, 0.0, T, K,
+                                 stream=stream, seed=seed)
+    x0 = np.array([rng.uniform(5, 45), rng.uniform(5, 45), rng.uniform(-np.pi, np.pi), 4.0], dtype=np.float32)
+    return Workload("bicycle_costmap_K16384_T100", ctrl, x0, np.array([K]), np.array([T]), 4, 2, 1,
+                    dict(model="bicycle_costmap", K=K, T=T, map="512x512@0.1m, 32 bumps", lam=2.0, seed=seed))
+
+
+BUILDERS = {"cartpole": cartpole, "batched_di": batched_di, "bicycle": bicycle}

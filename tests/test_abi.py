@@ -1,0 +1,94 @@
+"""The C-ABI library loads, exports every symbol include/mppi_gb.h declares, and rejects bad arguments on the host
+before touching the GPU (the reference exits the process instead: gpu_err_chk.cuh:32-40, mppi_common.cu:1302-1313)."""
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+from mppi_generic_vendor_gb300 import _abi as A
+
+
+def declared_functions():
+    text = A.HEADER_PATH.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mppi_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_symbols_exported_and_bound():
+    lib = A.lib()
+    names = declared_functions()
+    assert len(names) > 30
+    bound = {n for n, _, _ in A.SIGNATURES}
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in mppi_gb.h but not exported"
+        assert n in bound, f"{n} has no ctypes signature"
+    assert lib.mppi_abi_version() == 1
+
+
+@pytest.mark.parametrize("model", [A.MODEL_CARTPOLE, A.MODEL_DOUBLE_INTEGRATOR, A.MODEL_BICYCLE_COSTMAP,
+                                   A.MODEL_BICYCLE_SLIP, A.MODEL_BICYCLE_SLIP_MLP])
+def test_param_block_sizes_match_header(model):
+    d, c = C.c_size_t(), C.c_size_t()
+    A.call("mppi_model_param_sizes", model, C.byref(d), C.byref(c))
+    dt, ct = A.MODEL_PARAM_TYPES[model]
+    assert d.value == C.sizeof(dt) and c.value == C.sizeof(ct)
+    s, cd, o = C.c_int(), C.c_int(), C.c_int()
+    A.call("mppi_model_dims", model, C.byref(s), C.byref(cd), C.byref(o))
+    assert s.value in (4, 7) and cd.value in (1, 2) and o.value == s.value
+
+
+def test_reference_defaults():
+    sp = A.default_sampling_params()
+    # GaussianParamsImpl defaults (gaussian.cuh:21-41); ColoredNoiseParamsImpl (colored_noise.cuh:44-50)
+    assert list(sp.std_dev) == [1.0] * 4 and list(sp.control_cost_coeff) == [0.0] * 4
+    assert sp.pure_noise_trajectories_percentage == np.float32(0.01) and sp.std_dev_decay == 1.0
+    assert sp.offset_decay_rate == np.float32(0.97) and sp.fmin == 0.0
+    cc = A.default_constraints()  # setDefaultControlRanges (dynamics.cu:19-26)
+    assert cc.lower[0] == -np.finfo(np.float32).max and cc.upper[0] == np.finfo(np.float32).max
+    cp = A.default_controller_params()  # ControllerParams (controller.cuh:46-68)
+    assert cp.lambda_ == 1.0 and cp.alpha == 0.0 and cp.num_iters == 1
+
+
+def _create(model=A.MODEL_CARTPOLE, K=(64,), T=(16,), dyn_bytes=None, **over):
+    cp = A.default_controller_params()
+    sp = A.default_sampling_params()
+    for k, v in over.items():
+        setattr(cp if hasattr(cp, k) else sp, k, v)
+    dt, ct = A.MODEL_PARAM_TYPES.get(model, A.MODEL_PARAM_TYPES[A.MODEL_CARTPOLE])
+    n = len(K)
+    dyn = (dt * n)()
+    cost = (ct * n)()
+    Ka = (C.c_int * n)(*K)
+    Ta = (C.c_int * n)(*T)
+    h = C.c_void_p()
+    st = A.lib().mppi_create(model, n, Ka, Ta, C.byref(cp), C.byref(sp), None, C.cast(dyn, C.c_void_p),
+                             dyn_bytes or C.sizeof(dt), C.cast(cost, C.c_void_p), C.sizeof(ct), None,
+                             None, C.byref(h))
+    return st, h
+
+
+@pytest.mark.parametrize("kwargs", [dict(K=(0,)), dict(T=(0,)), dict(num_iters=0), dict(lambda_=0.0),
+                                    dict(lambda_=-1.0), dict(dyn_bytes=3), dict(model=99),
+                                    dict(pure_noise_trajectories_percentage=2.0), dict(kind=7)])
+def test_create_rejects_bad_arguments_without_gpu(kwargs):
+    st, h = _create(**kwargs)
+    assert st == 1, A.STATUS_NAMES.get(st)
+    assert not h.value
+    assert A.lib().mppi_last_error_string()
+
+
+def test_calls_on_null_handle_fail_cleanly():
+    lib = A.lib()
+    out = np.zeros(4, np.float32)
+    assert lib.mppi_compute_control(None, out.ctypes.data_as(C.POINTER(C.c_float)), 1) == 1
+    assert lib.mppi_get_control_seq(None, out.ctypes.data_as(C.POINTER(C.c_float))) == 1
+    assert lib.mppi_destroy(None) == 0
+    assert b"invalid handle" in lib.mppi_last_error_string()
+
+
+def test_kernel_entries_reject_null_pointers_without_gpu():
+    lib = A.lib()
+    assert lib.mppi_kernel_weight_transform(None, None, 1.0, 16, 1, None) == 1
+    assert lib.mppi_kernel_weighted_reduction(None, None, None, None, 0, 4, 4, 1, None) == 1
+    assert lib.mppi_kernel_philox_normal(None, 4, 0, 0, None) == 1

@@ -1,0 +1,243 @@
+"""Controller-level parity of the engine against the oracle's computeControl, given the same injected standard-normal
+noise (the parity definition of the port), plus the reference's controller behaviours: batching of uneven instances,
+graph replay, receding horizon, NaN rejection, sampler statistics, free-energy statistics, autotune cache."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from mppi_generic_vendor_gb300 import (BatchedMPPIController, CartpoleDynamics, CartpoleSwingupCost,
+                                       DoubleIntegratorDynamics, DoubleIntegratorObstacleCost, GaussianDistribution,
+                                       MPPIError, VanillaMPPIController)
+from mppi_generic_vendor_gb300 import _abi as A
+
+pytestmark = pytest.mark.gpu
+
+
+def cartpole_controller(K=2048, T=100, iters=1, std=1.0, lam=1.0, seed=0):
+    dyn = CartpoleDynamics(1.0, 1.0, 1.0)
+    dyn.setControlRanges([(-5.0, 5.0)])
+    cost = CartpoleSwingupCost(10.0, 1.0, 100.0, 1.0, 0.0)
+    sampler = GaussianDistribution(std_dev=(std,))
+    ctrl = VanillaMPPIController(dyn, cost, None, sampler, 0.02, iters, lam, 0.0, T, K, seed=seed)
+    return ctrl, dyn, cost
+
+
+def di_cost(rng):
+    obs = [(rng.uniform(-5, 5), rng.uniform(-5, 5), rng.uniform(0.3, 1.0)) for _ in range(8)]
+    goal = (rng.uniform(-4, 4), rng.uniform(-4, 4), 0.0, 0.0)
+    return DoubleIntegratorObstacleCost(goal=goal, coeff=(1.0, 1.0, 0.1, 0.1), terminal_coeff=10.0, obstacles=obs,
+                                        obstacle_cost=1000.0)
+
+
+def oracle_solve(ctrl, i, x0, eps, control_tc, stride=1, dyn=None, cost=None):
+    cp = ctrl.getParams()
+    sp = ctrl.sampler_.to_c()
+    K, T = int(ctrl.K[i]), int(ctrl.T[i])
+    d = ctrl._dyn_arr[i] if dyn is None else dyn
+    c = ctrl._cost_arr[i] if cost is None else cost
+    return oracle.compute_control(ctrl.model_id, d, c, cp, sp, ctrl.constraints_, K, T, ctrl.Cdim, ctrl.S, x0, eps,
+                                  control_tc, stride=stride)
+
+
+def check_control(got_tc, ref, tol=1e-5):
+    # the update is a weighted sum; compare relative to the sample-control scale
+    scale = max(1.0, float(np.abs(ref["samples"]).max()))
+    err = np.abs(got_tc - ref["control"]).max()
+    assert err <= tol * scale, (err, scale)
+
+
+@pytest.mark.parametrize("iters", [1, 3])
+def test_cartpole_compute_control_parity(iters):
+    K, T = 2048, 100
+    ctrl, dyn, cost = cartpole_controller(K, T, iters)
+    rng = np.random.default_rng(2024)
+    eps = rng.standard_normal(K * T).astype(np.float32)
+    x0 = np.array([0.05, -0.02, rng.uniform(-np.pi, np.pi), 0.03], dtype=np.float32)
+    u_init = rng.uniform(-1, 1, (T, 1)).astype(np.float32)
+    ctrl.setControlSeqs([u_init.T])
+    ctrl.injectNoise(eps)
+    ctrl.computeControl(x0, 1)
+    ref = oracle_solve(ctrl, 0, x0, eps, u_init)
+    got_costs = ctrl.sample_costs()
+    if iters == 1:
+        # same inputs: per-sample costs and constrained samples are bit-identical, the baseline is exact
+        assert np.array_equal(got_costs.view(np.uint32), ref["costs"].view(np.uint32))
+        assert np.array_equal(ctrl.control_samples().view(np.uint32), ref["samples"].view(np.uint32))
+        assert ctrl.getBaselineCost() == ref["baseline"]
+        w = ctrl.sample_weights()
+        big = ref["weights"] > 1e-30
+        assert np.all(np.abs(w[big] - ref["weights"][big]) <= 1e-5 * ref["weights"][big])
+        bn, n64 = ctrl.baseline_normalizer()
+        assert abs(n64[0] - ref["normalizer"]) <= 1e-5 * ref["normalizer"]
+        check_control(ctrl.getControlSeq().T, ref)
+    else:
+        # later iterations start from an update that differs by float rounding; costs stay within 1e-5 relative
+        assert np.median(np.abs(got_costs - ref["costs"]) / np.abs(ref["costs"])) < 1e-5
+        check_control(ctrl.getControlSeq().T, ref, tol=1e-3)
+    st = ctrl.getTargetStateSeq().T
+    assert np.allclose(st, ref["state_seq"], rtol=1e-4, atol=1e-4)
+    ctrl.close()
+
+
+def test_double_integrator_batched_parity():
+    rng = np.random.default_rng(99)
+    Ks = [512, 1024, 2048, 777, 4096, 100]
+    Ts = [32, 64, 128, 50, 32, 17]
+    costs = [di_cost(rng) for _ in Ks]
+    dyn = DoubleIntegratorDynamics()
+    dyn.setControlRanges([(-1.0, 1.0), (-1.0, 1.0)])
+    ctrl = BatchedMPPIController(dyn, costs, GaussianDistribution(std_dev=(0.5, 0.5)), Ks, Ts, dt=0.02,
+                                 max_iter=1, lambda_=1.0)
+    eps = [rng.standard_normal(K * T * 2).astype(np.float32) for K, T in zip(Ks, Ts)]
+    x0 = [rng.uniform(-5, 5, 4).astype(np.float32) for _ in Ks]
+    init = [rng.uniform(-0.5, 0.5, (T, 2)).astype(np.float32) for T in Ts]
+    ctrl.setControlSeqs([u.T for u in init])
+    ctrl.injectNoise(np.concatenate(eps))
+    ctrl.computeControl(np.concatenate(x0), 1)
+    got_costs = ctrl.sample_costs()
+    got_u = ctrl.getControlSeqs()
+    bn, _ = ctrl.baseline_normalizer()
+    koff = np.concatenate([[0], np.cumsum(Ks)])
+    for i in range(len(Ks)):
+        ref = oracle_solve(ctrl, i, x0[i], eps[i], init[i])
+        gc = got_costs[koff[i]:koff[i + 1]]
+        assert np.array_equal(gc.view(np.uint32), ref["costs"].view(np.uint32)), i
+        assert bn[i, 0] == ref["baseline"]
+        check_control(got_u[i].T, ref)
+    ctrl.close()
+
+
+def test_graph_replay_matches_stream_launches():
+    K, T = 1024, 64
+    outs = []
+    for graph in (True, False):
+        ctrl, _, _ = cartpole_controller(K, T, iters=2, seed=7)
+        ctrl.setGraphMode(graph)
+        x0 = np.array([0.0, 0.0, 0.3, 0.0], np.float32)
+        for _ in range(3):
+            ctrl.computeControl(x0, 1)
+            ctrl.slideControlSequence(1)
+        outs.append((ctrl.getControlSeq().copy(), ctrl.sample_costs().copy()))
+        ctrl.close()
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_philox_noise_changes_every_call_and_is_reproducible():
+    a, _, _ = cartpole_controller(256, 32, seed=3)
+    b, _, _ = cartpole_controller(256, 32, seed=3)
+    x0 = np.array([0.0, 0.0, 1.0, 0.0], np.float32)
+    a.computeControl(x0)
+    s1 = a.control_samples().copy()
+    a.computeControl(x0)
+    s2 = a.control_samples().copy()
+    b.computeControl(x0)
+    assert not np.array_equal(s1, s2)
+    assert np.array_equal(s1, b.control_samples())
+    a.close()
+    b.close()
+
+
+def test_cartpole_swing_up_receding_horizon():
+    # vanilla_mppi_test.cu:79-136 style integration test: swing the pole up (theta = pi) with receding horizon
+    ctrl, dyn, _ = cartpole_controller(2048, 100, iters=1, std=1.0, lam=1.0, seed=1)
+    p = dyn.getParams()
+    x = np.array([0.0, 0.0, 0.0, 0.0], np.float64)
+
+    def f(x, u):
+        s, c = math.sin(x[2]), math.cos(x[2])
+        mc, mp, l, g = p.cart_mass, p.pole_mass, p.pole_length, p.gravity
+        xdd = (u + mp * s * (l * x[3] ** 2 + g * c)) / (mc + mp * s * s)
+        tdd = (-u * c - mp * l * x[3] ** 2 * c * s - (mc + mp) * g * s) / (l * (mc + mp * s * s))
+        return np.array([x[1], xdd, x[3], tdd])
+
+    upright = 0
+    for step in range(500):
+        ctrl.computeControl(x.astype(np.float32), 1)
+        u = float(ctrl.getControlSeq()[0, 0])
+        x = x + 0.02 * f(x, u)
+        ctrl.slideControlSequence(1)
+        if 1.0 + math.cos(x[2]) < 0.05:
+            upright += 1
+    assert upright > 100, upright
+    ctrl.close()
+
+
+def test_nan_state_is_rejected_and_handle_survives():
+    ctrl, _, _ = cartpole_controller(256, 32)
+    with pytest.raises(MPPIError) as e:
+        ctrl.computeControl(np.array([0.0, np.nan, 0.0, 0.0], np.float32))
+    assert e.value.status == 3
+    ctrl.computeControl(np.zeros(4, np.float32))
+    assert np.isfinite(ctrl.getBaselineCost())
+    with pytest.raises(MPPIError):
+        ctrl.injectNoise(np.full(256 * 32, np.nan, np.float32))
+    ctrl.close()
+
+
+def bins_ok(z):
+    for j in range(3):
+        rule = 0.5 * (math.erf((j + 1) / math.sqrt(2.0)) - math.erf(-(j + 1) / math.sqrt(2.0)))
+        frac = float(np.mean(np.abs(z) < j + 1))
+        assert abs(frac - rule) / rule < 1e-3, (j, frac, rule)
+
+
+@pytest.mark.parametrize("pure", [0.0, 1.0])
+def test_generate_samples_are_gaussian(pure):
+    # gaussian_noise_tests.cu:114-245 (CheckSamplesAreGaussian / CheckZeroMeanSamplesAreGaussian)
+    K, T = 8192, 128
+    dyn = DoubleIntegratorDynamics()
+    rng = np.random.default_rng(0)
+    ctrl = BatchedMPPIController(dyn, di_cost(rng), GaussianDistribution(std_dev=(2.3, 2.3),
+                                                                          pure_noise_trajectories_percentage=pure),
+                                 [K], [T], seed=42)
+    mean = rng.uniform(-1, 1, (T, 2)).astype(np.float32)
+    ctrl.setControlSeqs([mean.T])
+    ctrl.generateSamples(0, 0)
+    s = ctrl.control_samples().reshape(K, T, 2)
+    m = 0.0 if pure == 1.0 else mean[None]
+    z = ((s - m) / 2.3)[1:]  # sample 0 is the mean
+    bins_ok(z.reshape(-1).astype(np.float64))
+    ctrl.close()
+
+
+def test_free_energy_statistics():
+    K, T = 1024, 50
+    ctrl, _, _ = cartpole_controller(K, T)
+    ctrl.computeControl(np.array([0, 0, 2.0, 0], np.float32))
+    w = ctrl.sample_weights().astype(np.float64)
+    fe = ctrl.getFreeEnergyStatistics()
+    lam = 1.0
+    norm = w.sum() / K
+    assert math.isclose(fe["freeEnergyMean"], -lam * math.log(norm) + ctrl.getBaselineCost(), rel_tol=1e-5)
+    assert math.isclose(fe["normalizerPercent"], ctrl.getNormalizerCost() / K, rel_tol=1e-6)
+    ctrl.close()
+
+
+def test_autotune_cache_roundtrip(tmp_path):
+    cache = tmp_path / "tune.json"
+    a, _, _ = cartpole_controller(1024, 32)
+    a.autotune(cache)
+    cfg = a.launchConfig()
+    assert cache.exists() and '"m1_i1_' in cache.read_text()
+    b, _, _ = cartpole_controller(1024, 32)
+    b.autotune(cache)
+    assert b.launchConfig() == cfg
+    # results do not depend on the launch shape
+    x0 = np.array([0, 0, 1.0, 0], np.float32)
+    rng = np.random.default_rng(4)
+    eps = rng.standard_normal(1024 * 32).astype(np.float32)
+    outs = []
+    for ns, kc in [(32, 64), (256, 256)]:
+        c, _, _ = cartpole_controller(1024, 32)
+        c.setLaunchConfig(ns, kc)
+        c.injectNoise(eps)
+        c.computeControl(x0)
+        outs.append((c.sample_costs(), c.getControlSeq()))
+        c.close()
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.allclose(outs[0][1], outs[1][1], rtol=0, atol=1e-6)
+    a.close()
+    b.close()

@@ -1,0 +1,129 @@
+"""Pins of the CPU oracle against the reference's own known answers (no GPU).
+
+The oracle is the checker for every GPU parity test, so it is itself checked here against: the Philox4x32-10
+known-answer vectors of its published definition, the smoothing / slide / equilibrium known answers of the
+reference's tests, the normexp and weighted-reduction recipes of the reference's kernel tests, and the reference's
+NumPy colored-noise generator run with the same normals.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from mppi_generic_vendor_gb300 import _abi as A
+
+
+def ulp(x):
+    return np.spacing(np.abs(np.float32(x))).astype(np.float64)
+
+
+def test_philox_known_answers():
+    # Random123 kat_vectors for philox4x32_10 (Salmon et al., SC 2011)
+    assert oracle.philox4x32_10([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert oracle.philox4x32_10([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6,
+                                                                          0x6D5451FD]
+    assert oracle.philox4x32_10([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == [
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_sincos_accuracy():
+    rng = np.random.default_rng(3)
+    x = np.concatenate([np.linspace(-np.pi, np.pi, 200001), rng.uniform(-200, 200, 200000),
+                        rng.uniform(-2e4, 2e4, 20000)]).astype(np.float32)
+    s, c = oracle.sincosf(x)
+    xs = x.astype(np.float64)
+    es = np.abs(s - np.sin(xs)) / np.maximum(ulp(np.sin(xs)), 2.0 ** -149)
+    ec = np.abs(c - np.cos(xs)) / np.maximum(ulp(np.cos(xs)), 2.0 ** -149)
+    # absolute error bound near the zeros, 2-ulp bound elsewhere
+    ok_s = (es <= 2.0) | (np.abs(s - np.sin(xs)) < 2e-9)
+    ok_c = (ec <= 2.0) | (np.abs(c - np.cos(xs)) < 2e-9)
+    assert ok_s.all() and ok_c.all(), (es.max(), ec.max())
+
+
+def test_normalize_angle_matches_reference_formula():
+    for a in [-10.0, -3.2, -np.pi, -1.0, 0.0, 0.5, np.pi, 3.5, 7.0, 100.0]:
+        a32 = np.float32(a)
+        r = np.fmod(np.float32(a32 + np.float32(np.pi)), np.float32(2 * np.pi))
+        ref = r + np.float32(np.pi) if r <= 0 else r - np.float32(np.pi)
+        assert np.float32(oracle.normalize_angle(a32)) == np.float32(ref)
+
+
+def test_smoothing_known_answer():
+    # controller_generic_tests.cu:214-237: u[0] kept; with T = 2, u(:,1) = 61/35
+    u = np.array([[1.0], [2.0]], dtype=np.float32)
+    out = oracle.smooth(u[:1])
+    assert out[0, 0] == 1.0
+    out = oracle.smooth(u)
+    assert out[0, 0] == 1.0
+    assert abs(out[1, 0] - 61.0 / 35.0) <= 4 * ulp(61.0 / 35.0)
+
+
+def test_slide_known_answer():
+    # controller_generic_tests.cu:239-282 (slide_control_scale = 0, zero control = 0)
+    T, Cd = 100, 3
+    u = np.repeat(np.arange(T, dtype=np.float32)[:, None], Cd, axis=1)
+    z = np.zeros(Cd, np.float32)
+    u1 = oracle.slide(u, 1, z, z)
+    for i in range(T):
+        expect = 0.0 if i + 1 > T - 1 else min(i + 1, T - 1)
+        assert (u1[i] == expect).all()
+    u2 = oracle.slide(u1, 10, z, z)
+    for i in range(T):
+        expect = 0.0 if i + 10 > T - 2 else min(i + 11, T - 1)
+        assert (u2[i] == expect).all()
+
+
+def test_cartpole_equilibrium():
+    # cartpole_dynamics_tests.cu:24-45
+    dyn = A.CartpoleParams(1.0, 1.0, 1.0, 9.81)
+    cost = A.CartpoleCostParams(10, 1, 100, 1, 0)
+    for fp64 in (True, False):
+        xd = oracle.dynamics_deriv(A.MODEL_CARTPOLE, dyn, cost, np.zeros(4), np.zeros(1), fp64=fp64)
+        assert np.abs(xd).max() < 1e-4
+
+
+def test_normexp_known_answers(golden):
+    k = golden["kats"]
+    _, b, _ = oracle.weights(k["baseline_costs"], lambda_inv=1.0)
+    assert np.float32(b) == k["baseline_known"][0]
+    w, b, n = oracle.weights(k["expnorm_costs"], lambda_inv=np.float32(0.3))
+    known = k["expnorm_known"]
+    assert np.all(np.abs(w - known) <= 4 * ulp(known))
+    assert abs(n - float(np.sum(known.astype(np.float64)))) < 1e-9 * n
+
+
+def test_weighted_reduction_known_answer(golden):
+    k = golden["kats"]
+    out, absout = oracle.weighted_mean(k["wr_weights"], k["wr_normalizer"][0], k["wr_controls"], 1024, 100, 4)
+    assert np.allclose(out, k["wr_known"], rtol=1e-12, atol=0)
+
+
+def colored_case(golden, case):
+    g = golden["colored"]
+    T = int(g[f"c{case}_T"])
+    zr, zi = g[f"c{case}_zr"], g[f"c{case}_zi"]
+    spec = np.stack([zr, zi], axis=-1)  # [batch][F][2]
+    return T, float(g[f"c{case}_beta"]), float(g[f"c{case}_fmin"]), spec, g[f"c{case}_y"]
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_colored_noise_matches_reference_script(golden, case):
+    T, beta, fmin, spec, y = colored_case(golden, case)
+    batch = spec.shape[0]
+    eps = oracle.colored_noise(spec, batch, T, 1, [beta], fmin=fmin, decay=0.0, offset_t=0)
+    ref = y[:, :T]
+    err = np.abs(eps.reshape(batch, T) - ref)
+    assert err.max() <= 2e-5 * max(1.0, np.abs(ref).max()), err.max()
+
+
+def test_colored_scales_follow_fftfreq_cutoff():
+    # colored_noise.cu:294-333: frequencies below max(fmin, 1/N) take the cutoff's scale
+    s, sigma = oracle.colored_scales(4, 1, [2.0], fmin=0.0)
+    f = np.arange(5) / 8.0
+    f[0] = f[1]
+    ref = f ** -1.0
+    assert np.allclose(s[:, 0], ref, rtol=1e-6)
+    w = ref[1:].copy()
+    w[-1] *= 0.5
+    assert math.isclose(sigma[0], 2 * np.sqrt(np.sum(w ** 2)) / 8, rel_tol=1e-6)

@@ -265,7 +265,7 @@ def run_gpu(args, ws, rank, local):
     iters_per_s = iters / (ms / 1e3)
     kernels = ctrl.kernelsPerCompute()
     # ---------------- per-kernel timing and roofline
-    kms = ctrl.timeKernels(1, reps=max(3, min(10, args.steps)))
+    kms = [float(v) for v in ctrl.timeKernels(1, reps=max(3, min(10, args.steps)))]
     names = ["sampler", "rollout", "update"]
     abytes = algorithmic_bytes(wl, colored)
     dom = int(np.argmax(kms))

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "mg_common.cuh"
+#include "mg_colored.cuh"
 #include "mg_kernels.cuh"
 
 namespace mg
@@ -331,7 +332,9 @@ public:
   {
     MG_CHECK(sp, "sampling params must not be NULL");
     MG_TRY(check_sampling(*sp));
+    if (sp->kind != sp_.kind) injected_d_.reset();
     sp_ = *sp;
+    MG_TRY(build_colored_tables());
     invalidate_graphs();
     return MPPI_OK;
   }
@@ -363,9 +366,10 @@ public:
       invalidate_graphs();
       return MPPI_OK;
     }
-    MG_CHECK(sp_.kind == MPPI_SAMPLER_GAUSSIAN, "noise injection for this sampler is not built");
+    const bool colored = sp_.kind == MPPI_SAMPLER_COLORED_NOISE;
     size_t need = 0;
-    for (int i = 0; i < I_; ++i) need += (size_t)K_[i] * T_[i] * C;
+    for (int i = 0; i < I_; ++i)
+      need += colored ? (size_t)K_[i] * C * (T_[i] + 1) * 2 : (size_t)K_[i] * T_[i] * C;
     MG_CHECK(count == need, "injected noise has %zu floats, expected %zu", count, need);
     for (size_t j = 0; j < count; ++j)
       if (!std::isfinite(noise[j]))
@@ -373,13 +377,22 @@ public:
         set_error("injected noise has a non-finite entry at index %zu", j);
         return MPPI_ENAN;
       }
-    MG_TRY(injected_d_.alloc(samples_d_.n));
-    size_t o = 0;
-    for (int i = 0; i < I_; ++i)
+    if (colored)
     {
-      const size_t n = (size_t)K_[i] * T_[i] * C;
-      MG_CUDA(cudaMemcpy(injected_d_.p + u_off_[i], noise + o, n * sizeof(float), cudaMemcpyHostToDevice));
-      o += n;
+      // spectrum layout [K][C][F][2] per instance, instances concatenated (spec_off)
+      MG_TRY(injected_d_.alloc(count));
+      MG_CUDA(cudaMemcpy(injected_d_.p, noise, count * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    else
+    {
+      MG_TRY(injected_d_.alloc(samples_d_.n));
+      size_t o = 0;
+      for (int i = 0; i < I_; ++i)
+      {
+        const size_t n = (size_t)K_[i] * T_[i] * C;
+        MG_CUDA(cudaMemcpy(injected_d_.p + u_off_[i], noise + o, n * sizeof(float), cudaMemcpyHostToDevice));
+        o += n;
+      }
     }
     invalidate_graphs();
     return MPPI_OK;
@@ -501,11 +514,17 @@ private:
   {
     MG_CHECK(sp.kind == MPPI_SAMPLER_GAUSSIAN || sp.kind == MPPI_SAMPLER_COLORED_NOISE, "unknown sampler kind %d",
              sp.kind);
-    MG_CHECK(sp.kind == MPPI_SAMPLER_GAUSSIAN, "the colored-noise sampler is not built for this model");
     for (int c = 0; c < C; ++c)
       MG_CHECK(std::isfinite(sp.std_dev[c]) && sp.std_dev[c] >= 0.0f, "std_dev[%d] must be finite and >= 0", c);
     MG_CHECK(sp.pure_noise_trajectories_percentage >= 0.0f && sp.pure_noise_trajectories_percentage <= 1.0f,
              "pure_noise_trajectories_percentage must be in [0, 1]");
+    if (sp.kind == MPPI_SAMPLER_COLORED_NOISE)
+    {
+      for (int c = 0; c < C; ++c) MG_CHECK(std::isfinite(sp.exponents[c]), "exponents[%d] must be finite", c);
+      MG_CHECK(std::isfinite(sp.offset_decay_rate) && std::isfinite(sp.fmin), "offset_decay_rate and fmin must be finite");
+      for (int T : T_)
+        MG_CHECK(T <= kColoredMaxT, "the colored-noise sampler supports num_timesteps <= %d (got %d)", kColoredMaxT, T);
+    }
     return MPPI_OK;
   }
 
@@ -517,10 +536,10 @@ private:
     MG_CHECK(cp_.num_iters >= 1, "num_iters must be >= 1");
     MG_CHECK(cp_.lambda > 0.0f && std::isfinite(cp_.lambda), "lambda must be positive");
     MG_CHECK(std::isfinite(cp_.dt), "dt must be finite");
-    MG_TRY(check_sampling(a.sp));
-    sp_ = a.sp;
     K_.assign(a.K, a.K + I_);
     T_.assign(a.T, a.T + I_);
+    MG_TRY(check_sampling(a.sp));
+    sp_ = a.sp;
     long long total_u = 0;
     int total_k = 0, total_t = 0;
     for (int i = 0; i < I_; ++i)
@@ -590,7 +609,86 @@ private:
     MG_TRY(out_bn_h_.alloc((size_t)2 * I_));
     MG_TRY(out_stats_h_.alloc((size_t)3 * I_));
     MG_TRY(build_work_lists());
+    MG_TRY(build_colored_tables());
     MG_CUDA(cudaStreamSynchronize(stream_));
+    return MPPI_OK;
+  }
+
+  // Per-T tables for the colored-noise sampler (see mg_colored.cuh): twiddles e^{2 pi i j / 2T} in double rounded to
+  // float; frequency scales and sigma in float in the order of the reference's host code (colored_noise.cu:294-333);
+  // decay^t with powf as rearrangeNoise does (colored_noise.cu:44).
+  mppi_status build_colored_tables()
+  {
+    if (sp_.kind != MPPI_SAMPLER_COLORED_NOISE) return MPPI_OK;
+    std::vector<float> tab;
+    std::map<int, std::pair<int, int4>> by_t;
+    std::vector<int> tab_off(I_);
+    std::vector<int4> parts(I_);
+    auto align4 = [&]() {
+      while (tab.size() % 4) tab.push_back(0.0f);
+    };
+    for (int i = 0; i < I_; ++i)
+    {
+      const int T = T_[i];
+      auto it = by_t.find(T);
+      if (it == by_t.end())
+      {
+        const int N = 2 * T, F = T + 1;
+        const int base = (int)tab.size();
+        for (int j = 0; j < N; ++j)
+        {
+          tab.push_back((float)std::cos(2.0 * M_PI * j / N));
+          tab.push_back((float)std::sin(2.0 * M_PI * j / N));
+        }
+        align4();
+        // fftfreq (colored_noise.cuh:24-34) and the cutoff / scale loop (colored_noise.cu:294-317)
+        std::vector<float> freq(F), scale((size_t)F * C, 0.0f);
+        for (int j = 0; j < F; ++j) freq[j] = j / (1.0f * N);
+        const float cutoff = fmaxf(sp_.fmin, 1.0f / N);
+        int smaller = 0;
+        for (int f = 0; f < F; ++f)
+        {
+          if (freq[f] < cutoff)
+            smaller++;
+          else if (smaller < F)
+            for (int j = 0; j < smaller; ++j)
+            {
+              freq[j] = freq[smaller];
+              for (int c = 0; c < C; ++c) scale[(size_t)j * C + c] = powf(freq[smaller], -sp_.exponents[c] / 2.0f);
+            }
+          for (int c = 0; c < C; ++c) scale[(size_t)f * C + c] = powf(freq[f], -sp_.exponents[c] / 2.0f);
+        }
+        int4 p;
+        p.x = (int)tab.size() - base;
+        tab.insert(tab.end(), scale.begin(), scale.end());
+        align4();
+        p.y = (int)tab.size() - base;
+        for (int c = 0; c < C; ++c)  // sigma (colored_noise.cu:320-328)
+        {
+          float s = 0.0f;
+          for (int j = 1; j < F - 1; ++j) s += scale[(size_t)j * C + c] * scale[(size_t)j * C + c];
+          const float last = scale[(size_t)(F - 1) * C + c] * ((1.0f + (N % 2)) / 2.0f);
+          s += last * last;
+          tab.push_back(2.0f * sqrtf(s) / N);
+        }
+        align4();
+        p.z = (int)tab.size() - base;
+        for (int t = 0; t < T; ++t)
+          tab.push_back(sp_.offset_decay_rate == 0.0f ? 0.0f : powf(sp_.offset_decay_rate, (float)t));
+        align4();
+        p.w = 0;
+        it = by_t.emplace(T, std::make_pair(base, p)).first;
+      }
+      tab_off[i] = it->second.first;
+      parts[i] = it->second.second;
+    }
+    MG_TRY(ctab_d_.alloc(tab.size()));
+    MG_TRY(ctab_off_d_.alloc(I_));
+    MG_TRY(ctab_parts_d_.alloc(I_));
+    MG_CUDA(cudaMemcpy(ctab_d_.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(ctab_off_d_.p, tab_off.data(), sizeof(int) * I_, cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(ctab_parts_d_.p, parts.data(), sizeof(int4) * I_, cudaMemcpyHostToDevice));
+    max_t_ = *std::max_element(T_.begin(), T_.end());
     return MPPI_OK;
   }
 
@@ -599,11 +697,11 @@ private:
   mppi_status build_work_lists()
   {
     std::vector<InstDesc> inst(I_);
-    std::vector<int2> tiles, swork;
+    std::vector<int2> tiles, swork, cwork;
     std::vector<int4> chunks;
     std::vector<long long> part_off;
     std::vector<int> chunk0(I_);
-    long long poff = 0;
+    long long poff = 0, spec = 0;
     for (int i = 0; i < I_; ++i)
     {
       InstDesc& d = inst[i];
@@ -612,8 +710,10 @@ private:
       d.k_off = k_off_[i];
       d.t_off = t_off_[i];
       d.u_off = u_off_[i];
-      d.spec_off = 0;
+      d.spec_off = spec;
+      spec += (long long)K_[i] * C * (T_[i] + 1) * 2;
       d.x_off = i * S;
+      for (int k0 = 0; k0 < K_[i]; k0 += kColoredSamplesPerCta) cwork.push_back(make_int2(i, k0));
       d.num_chunks = (K_[i] + kc_ - 1) / kc_;
       chunk0[i] = (int)chunks.size();
       for (int c = 0; c < d.num_chunks; ++c)
@@ -633,9 +733,12 @@ private:
     num_tiles_ = (int)tiles.size();
     num_chunks_ = (int)chunks.size();
     num_swork_ = (int)swork.size();
+    num_cwork_ = (int)cwork.size();
     MG_TRY(inst_d_.alloc(I_));
     MG_TRY(tiles_d_.alloc(tiles.size()));
     MG_TRY(swork_d_.alloc(swork.size()));
+    MG_TRY(cwork_d_.alloc(cwork.size()));
+    MG_CUDA(cudaMemcpy(cwork_d_.p, cwork.data(), sizeof(int2) * cwork.size(), cudaMemcpyHostToDevice));
     MG_TRY(chunks_d_.alloc(chunks.size()));
     MG_TRY(part_off_d_.alloc(part_off.size()));
     MG_TRY(chunk0_d_.alloc(I_));
@@ -689,8 +792,43 @@ private:
     a.stride = stride;
     a.decay_pow = powf(sp_.std_dev_decay, (float)iter);
     a.sh = make_sample_shared(sp_, cc_);
+    if (sp_.kind == MPPI_SAMPLER_COLORED_NOISE) return launch_colored(a);
     const int grid = std::min(num_swork_, 8 * num_sms_);
     gaussian_sample_kernel<C><<<grid, 256, 0, stream_>>>(a);
+    MG_CUDA(cudaGetLastError());
+    return MPPI_OK;
+  }
+
+  mppi_status launch_colored(const SampleArgs& s)
+  {
+    constexpr int SPB = kColoredSamplesPerCta;
+    for (int T : T_)
+      MG_CHECK(s.stride < 2 * T, "optimization_stride (%d) must be below 2 * num_timesteps for colored noise",
+               s.stride);
+    ColoredArgs a;
+    a.inst = inst_d_.p;
+    a.work = cwork_d_.p;
+    a.num_work = num_cwork_;
+    a.samples_per_item = SPB;
+    a.tables = ctab_d_.p;
+    a.tab_off = ctab_off_d_.p;
+    a.tab_parts = ctab_parts_d_.p;
+    a.samples = samples_d_.p;
+    a.mean = mean_d_.p;
+    a.injected_spec = injected_d_.p;
+    a.noise_counter = s.noise_counter;
+    a.seed_lo = s.seed_lo;
+    a.seed_hi = s.seed_hi;
+    a.stride = s.stride;
+    a.decay_pow = s.decay_pow;
+    a.sh = s.sh;
+    const size_t smem = colored_smem_bytes<C, SPB>(max_t_);
+    auto kern = colored_sample_kernel<C, SPB>;
+    if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 1;
+    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * SPB * C, smem));
+    const int grid = std::max(1, std::min(num_cwork_, std::max(per_sm, 1) * num_sms_));
+    kern<<<grid, 32 * SPB * C, smem, stream_>>>(a);
     MG_CUDA(cudaGetLastError());
     return MPPI_OK;
   }
@@ -910,7 +1048,12 @@ private:
   DevBuf<CostParams> cost_d_;
   DevBuf<unsigned int> baseline_bits_d_, arrive_d_, counters_d_;
   DevBuf<InstDesc> inst_d_;
-  DevBuf<int2> tiles_d_, swork_d_;
+  DevBuf<int2> tiles_d_, swork_d_, cwork_d_;
+  DevBuf<float> ctab_d_;
+  DevBuf<int> ctab_off_d_;
+  DevBuf<int4> ctab_parts_d_;
+  int num_cwork_ = 0, max_t_ = 1;
+  static constexpr int kColoredSamplesPerCta = 8 / C > 0 ? 8 / C : 1;
   DevBuf<int4> chunks_d_;
   DevBuf<long long> part_off_d_;
   DevBuf<int> chunk0_d_;

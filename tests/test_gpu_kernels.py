@@ -138,8 +138,8 @@ def test_gaussian_controls_bit_identical(Cd, stride, decay, pure):
     cc = A.default_constraints()
     for i in range(Cd):
         cc.lower[i], cc.upper[i], cc.deadband[i] = -1.5, 1.2, 0.05 * i
-    s = dev(eps)
-    A.call("mppi_kernel_gaussian_controls", ptr(s), ptr(dev(mean)), std.ctypes.data_as(C.POINTER(C.c_float)),
+    s, mean_d = dev(eps), dev(mean)  # keep the device buffers alive until the kernel has run
+    A.call("mppi_kernel_gaussian_controls", ptr(s), ptr(mean_d), std.ctypes.data_as(C.POINTER(C.c_float)),
            C.byref(cc), K, T, Cd, stride, decay, pure, stream())
     ref = oracle.gaussian_rewrite(eps, mean, std, K, T, Cd, stride, decay, pure)
     ref = oracle.enforce_constraints(ref, Cd, cc)
@@ -182,8 +182,9 @@ def test_rollout_costs_bit_identical(model, K, T, Cd, cc_coeff):
         sp.control_cost_coeff[i] = cc_coeff
     cc = A.default_constraints()
     costs = empty(K)
+    x0_d, u_d, mean_d = dev(x0), dev(u), dev(mean)  # keep the device buffers alive until the kernel has run
     A.call("mppi_kernel_rollout", model, C.byref(dyn), C.sizeof(dyn), C.byref(cost), C.sizeof(cost), C.byref(sp),
-           ptr(dev(x0)), ptr(dev(u)), ptr(dev(mean)), ptr(costs), K, T, 0.02, 1.0, 0.0, stream())
+           ptr(x0_d), ptr(u_d), ptr(mean_d), ptr(costs), K, T, 0.02, 1.0, 0.0, stream())
     got = host(costs)
     ref, _, _ = oracle.rollout(model, dyn, cost, x0, u, mean, sp, cc, 1.0, 0.0, K, T, 0.02)
     assert np.array_equal(got.view(np.uint32), ref.astype(np.float32).view(np.uint32))

@@ -614,9 +614,12 @@ private:
     return MPPI_OK;
   }
 
-  // Per-T tables for the colored-noise sampler (see mg_colored.cuh): twiddles e^{2 pi i j / 2T} in double rounded to
-  // float; frequency scales and sigma in float in the order of the reference's host code (colored_noise.cu:294-333);
-  // decay^t with powf as rearrangeNoise does (colored_noise.cu:44).
+  // Per-T tables for the colored-noise sampler (mg_colored.cu).  Twiddles are computed in double and rounded to float:
+  //   T = 32 R (R = 1, 2, 4, 8): packing twiddles e^{2 pi i k / 2T} (k < T), then the register-stage twiddles
+  //     [log2 R][R][32] and the lane-stage twiddles [5][32] of the T-point decimation-in-frequency inverse FFT;
+  //   other T: the full table e^{2 pi i j / 2T}, j < 2T, for the direct transform.
+  // Frequency scales and sigma are computed in float in the order of the reference's host code
+  // (colored_noise.cu:294-333); decay^t with powf as rearrangeNoise does (colored_noise.cu:44).
   mppi_status build_colored_tables()
   {
     if (sp_.kind != MPPI_SAMPLER_COLORED_NOISE) return MPPI_OK;
@@ -627,6 +630,10 @@ private:
     auto align4 = [&]() {
       while (tab.size() % 4) tab.push_back(0.0f);
     };
+    auto push_tw = [&](double num, double den) {
+      tab.push_back((float)std::cos(2.0 * M_PI * num / den));
+      tab.push_back((float)std::sin(2.0 * M_PI * num / den));
+    };
     for (int i = 0; i < I_; ++i)
     {
       const int T = T_[i];
@@ -635,10 +642,28 @@ private:
       {
         const int N = 2 * T, F = T + 1;
         const int base = (int)tab.size();
-        for (int j = 0; j < N; ++j)
+        const bool pow2 = (T == 32 || T == 64 || T == 128 || T == 256);
+        int lane_off = 0;
+        if (pow2)
         {
-          tab.push_back((float)std::cos(2.0 * M_PI * j / N));
-          tab.push_back((float)std::sin(2.0 * M_PI * j / N));
+          const int R = T / 32;
+          for (int k = 0; k < T; ++k) push_tw(k, N);
+          int s = 0;
+          for (int hr = R / 2; hr >= 1; hr >>= 1, ++s)
+            for (int r = 0; r < R; ++r)
+              for (int lane = 0; lane < 32; ++lane)
+                push_tw((r & hr) == 0 ? lane + 32 * (r % (2 * hr)) : 0, 64.0 * hr);
+          lane_off = (int)tab.size() - base;
+          for (int st = 0; st < 5; ++st)
+          {
+            const int half = 16 >> st;
+            for (int lane = 0; lane < 32; ++lane)
+              push_tw((lane & half) ? (lane % (2 * half)) - half : 0, 2.0 * half);
+          }
+        }
+        else
+        {
+          for (int j = 0; j < N; ++j) push_tw(j, N);
         }
         align4();
         // fftfreq (colored_noise.cuh:24-34) and the cutoff / scale loop (colored_noise.cu:294-317)
@@ -676,7 +701,7 @@ private:
         for (int t = 0; t < T; ++t)
           tab.push_back(sp_.offset_decay_rate == 0.0f ? 0.0f : powf(sp_.offset_decay_rate, (float)t));
         align4();
-        p.w = 0;
+        p.w = lane_off;
         it = by_t.emplace(T, std::make_pair(base, p)).first;
       }
       tab_off[i] = it->second.first;
@@ -801,7 +826,6 @@ private:
 
   mppi_status launch_colored(const SampleArgs& s)
   {
-    constexpr int SPB = kColoredSamplesPerCta;
     for (int T : T_)
       MG_CHECK(s.stride < 2 * T, "optimization_stride (%d) must be below 2 * num_timesteps for colored noise",
                s.stride);
@@ -809,7 +833,6 @@ private:
     a.inst = inst_d_.p;
     a.work = cwork_d_.p;
     a.num_work = num_cwork_;
-    a.samples_per_item = SPB;
     a.tables = ctab_d_.p;
     a.tab_off = ctab_off_d_.p;
     a.tab_parts = ctab_parts_d_.p;
@@ -822,15 +845,7 @@ private:
     a.stride = s.stride;
     a.decay_pow = s.decay_pow;
     a.sh = s.sh;
-    const size_t smem = colored_smem_bytes<C, SPB>(max_t_);
-    auto kern = colored_sample_kernel<C, SPB>;
-    if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 1;
-    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * SPB * C, smem));
-    const int grid = std::max(1, std::min(num_cwork_, std::max(per_sm, 1) * num_sms_));
-    kern<<<grid, 32 * SPB * C, smem, stream_>>>(a);
-    MG_CUDA(cudaGetLastError());
-    return MPPI_OK;
+    return launch_colored_sampler<C>(a, max_t_, num_sms_, stream_);
   }
 
   template <int NS>
@@ -1053,7 +1068,7 @@ private:
   DevBuf<int> ctab_off_d_;
   DevBuf<int4> ctab_parts_d_;
   int num_cwork_ = 0, max_t_ = 1;
-  static constexpr int kColoredSamplesPerCta = 8 / C > 0 ? 8 / C : 1;
+  static constexpr int kColoredSamplesPerCta = ColoredShape<C>::SPB;
   DevBuf<int4> chunks_d_;
   DevBuf<long long> part_off_d_;
   DevBuf<int> chunk0_d_;

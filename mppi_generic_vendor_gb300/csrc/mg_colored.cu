@@ -233,12 +233,16 @@ __device__ __forceinline__ void row_transform_direct(const ColoredArgs& a, const
   __syncwarp();
 }
 
-template <int C, int SPB>
-__global__ void __launch_bounds__(32 * SPB * C) colored_sample_kernel(const __grid_constant__ ColoredArgs a)
+// One launch per horizon class: R = T / 32 for T = 32, 64, 128, 256, R = 0 for the direct transform.  Specialising
+// the kernel on R keeps the register footprint of a single transform size.
+template <int C, int SPB, int R>
+__global__ void __launch_bounds__(32 * SPB * C, (R >= 8 || R == 0) ? 2 : 3)
+    colored_sample_kernel(const __grid_constant__ ColoredArgs a)
 {
   extern __shared__ __align__(16) float smem[];
-  float2* Xall = reinterpret_cast<float2*>(smem);                               // [warps][kColoredMaxT + 2]
-  float* tile = reinterpret_cast<float*>(Xall + SPB * C * (kColoredMaxT + 2));  // [SPB][T][C]
+  // direct transform only: per-warp spectrum buffers [warps][kColoredMaxT + 2]; then the output tile [SPB][T][C]
+  float2* Xall = reinterpret_cast<float2*>(smem);
+  float* tile = reinterpret_cast<float*>(Xall + (R == 0 ? SPB * C * (kColoredMaxT + 2) : 0));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t counter = a.noise_counter ? *a.noise_counter : 0u;
 
@@ -255,17 +259,11 @@ __global__ void __launch_bounds__(32 * SPB * C) colored_sample_kernel(const __gr
     {
       const long long row = (long long)(w.y + s_local) * C + c;
       float* tile_row = tile + s_local * T * C + c;
-      switch (T)
-      {
-        case 32: row_transform_pow2<C, 1>(a, d, w.x, row, c, lane, tab, parts, tile_row, counter); break;
-        case 64: row_transform_pow2<C, 2>(a, d, w.x, row, c, lane, tab, parts, tile_row, counter); break;
-        case 128: row_transform_pow2<C, 4>(a, d, w.x, row, c, lane, tab, parts, tile_row, counter); break;
-        case 256: row_transform_pow2<C, 8>(a, d, w.x, row, c, lane, tab, parts, tile_row, counter); break;
-        default:
-          row_transform_direct<C>(a, d, w.x, row, c, lane, tab, parts, tile_row, Xall + warp * (kColoredMaxT + 2),
-                                  counter);
-          break;
-      }
+      if constexpr (R > 0)
+        row_transform_pow2<C, R>(a, d, w.x, row, c, lane, tab, parts, tile_row, counter);
+      else
+        row_transform_direct<C>(a, d, w.x, row, c, lane, tab, parts, tile_row, Xall + warp * (kColoredMaxT + 2),
+                                counter);
     }
     __syncthreads();
     // ---- Gaussian rewrite + constraints, coalesced store of nsamp whole samples ([K][T][C] rows are contiguous)
@@ -321,13 +319,15 @@ __global__ void __launch_bounds__(32 * SPB * C) colored_sample_kernel(const __gr
 }
 }  // namespace
 
-template <int C>
-mppi_status launch_colored_sampler(const ColoredArgs& a, int max_t, int num_sms, cudaStream_t s)
+template <int C, int R>
+static mppi_status launch_class(const ColoredArgs& a, int max_t, int num_sms, cudaStream_t s)
 {
   constexpr int SPB = ColoredShape<C>::SPB;
   constexpr int THREADS = ColoredShape<C>::THREADS;
-  const size_t smem = sizeof(float2) * (size_t)SPB * C * (kColoredMaxT + 2) + sizeof(float) * (size_t)SPB * max_t * C;
-  auto kern = colored_sample_kernel<C, SPB>;
+  const size_t xbuf = (R == 0) ? sizeof(float2) * (size_t)SPB * C * (kColoredMaxT + 2) : 0;
+  const int tmax = (R == 0) ? max_t : 32 * R;
+  const size_t smem = xbuf + sizeof(float) * (size_t)SPB * tmax * C;
+  auto kern = colored_sample_kernel<C, SPB, R>;
   if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 1;
   MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem));
@@ -337,9 +337,33 @@ mppi_status launch_colored_sampler(const ColoredArgs& a, int max_t, int num_sms,
   return MPPI_OK;
 }
 
-template mppi_status launch_colored_sampler<1>(const ColoredArgs&, int, int, cudaStream_t);
-template mppi_status launch_colored_sampler<2>(const ColoredArgs&, int, int, cudaStream_t);
-template mppi_status launch_colored_sampler<3>(const ColoredArgs&, int, int, cudaStream_t);
-template mppi_status launch_colored_sampler<4>(const ColoredArgs&, int, int, cudaStream_t);
+template <int C>
+mppi_status launch_colored_sampler(const ColoredArgs& a, const int* class_begin, int max_t, int num_sms,
+                                   cudaStream_t s)
+{
+  // class k (R = 0, 1, 2, 4, 8) owns work items [class_begin[k], class_begin[k + 1])
+  for (int k = 0; k < 5; ++k)
+  {
+    const int n = class_begin[k + 1] - class_begin[k];
+    if (n <= 0) continue;
+    ColoredArgs b = a;
+    b.work = a.work + class_begin[k];
+    b.num_work = n;
+    switch (k)
+    {
+      case 0: MG_TRY((launch_class<C, 0>(b, max_t, num_sms, s))); break;
+      case 1: MG_TRY((launch_class<C, 1>(b, max_t, num_sms, s))); break;
+      case 2: MG_TRY((launch_class<C, 2>(b, max_t, num_sms, s))); break;
+      case 3: MG_TRY((launch_class<C, 4>(b, max_t, num_sms, s))); break;
+      default: MG_TRY((launch_class<C, 8>(b, max_t, num_sms, s))); break;
+    }
+  }
+  return MPPI_OK;
+}
+
+template mppi_status launch_colored_sampler<1>(const ColoredArgs&, const int*, int, int, cudaStream_t);
+template mppi_status launch_colored_sampler<2>(const ColoredArgs&, const int*, int, int, cudaStream_t);
+template mppi_status launch_colored_sampler<3>(const ColoredArgs&, const int*, int, int, cudaStream_t);
+template mppi_status launch_colored_sampler<4>(const ColoredArgs&, const int*, int, int, cudaStream_t);
 
 }  // namespace mg

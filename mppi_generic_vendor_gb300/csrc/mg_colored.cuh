@@ -43,8 +43,23 @@ struct ColoredShape
   static constexpr int THREADS = 32 * SPB * C;
 };
 
-// Launch the colored sampler over every instance of `a` (defined in mg_colored.cu for C = 1..4).
+// Horizon class of an instance: 0 = direct transform, 1..4 = register FFT with T = 32, 64, 128, 256.
+inline int colored_class(int T)
+{
+  switch (T)
+  {
+    case 32: return 1;
+    case 64: return 2;
+    case 128: return 3;
+    case 256: return 4;
+    default: return 0;
+  }
+}
+
+// Launch the colored sampler over every instance of `a`: the work list is grouped by horizon class, class k owning
+// items [class_begin[k], class_begin[k + 1]); one launch per non-empty class (defined in mg_colored.cu, C = 1..4).
 template <int C>
-mppi_status launch_colored_sampler(const ColoredArgs& a, int max_t, int num_sms, cudaStream_t s);
+mppi_status launch_colored_sampler(const ColoredArgs& a, const int* class_begin, int max_t, int num_sms,
+                                   cudaStream_t s);
 
 }  // namespace mg

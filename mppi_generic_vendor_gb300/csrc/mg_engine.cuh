@@ -179,7 +179,16 @@ public:
     if (T) *T = T_[i];
   }
   cudaStream_t stream() const override { return stream_; }
-  int kernels_per_compute() const override { return 3 * cp_.num_iters; }
+  int kernels_per_compute() const override
+  {
+    int sampler = 1;
+    if (sp_.kind == MPPI_SAMPLER_COLORED_NOISE)
+    {
+      sampler = 0;
+      for (int k = 0; k < 5; ++k) sampler += class_begin_[k + 1] > class_begin_[k] ? 1 : 0;
+    }
+    return (sampler + 2) * cp_.num_iters;
+  }
 
   // ------------------------------------------------------------------------------------------------ computeControl
   mppi_status compute_control(const float* x0, int stride) override
@@ -555,6 +564,9 @@ private:
       total_u += ((long long)K_[i] * T_[i] * C + 3) / 4 * 4;
     }
     total_k_ = total_k;
+    use_bulk_ = true;
+    for (int i = 0; i < I_; ++i)
+      if (((long long)T_[i] * C) % 4 != 0) use_bulk_ = false;
     dyn_.assign((const DynParams*)a.dyn, (const DynParams*)a.dyn + I_);
     cost_.assign((const CostParams*)a.cost, (const CostParams*)a.cost + I_);
     control_.assign((size_t)total_t, 0.0f);
@@ -608,6 +620,7 @@ private:
     MG_TRY(out_mean_h_.alloc(total_t));
     MG_TRY(out_bn_h_.alloc((size_t)2 * I_));
     MG_TRY(out_stats_h_.alloc((size_t)3 * I_));
+    MG_TRY(status_h_.alloc(1));
     MG_TRY(build_work_lists());
     MG_TRY(build_colored_tables());
     MG_CUDA(cudaStreamSynchronize(stream_));
@@ -722,7 +735,7 @@ private:
   mppi_status build_work_lists()
   {
     std::vector<InstDesc> inst(I_);
-    std::vector<int2> tiles, swork, cwork;
+    std::vector<int2> tiles, swork, cwork, cwork_cls[5];
     std::vector<int4> chunks;
     std::vector<long long> part_off;
     std::vector<int> chunk0(I_);
@@ -738,7 +751,8 @@ private:
       d.spec_off = spec;
       spec += (long long)K_[i] * C * (T_[i] + 1) * 2;
       d.x_off = i * S;
-      for (int k0 = 0; k0 < K_[i]; k0 += kColoredSamplesPerCta) cwork.push_back(make_int2(i, k0));
+      for (int k0 = 0; k0 < K_[i]; k0 += kColoredSamplesPerCta)
+        cwork_cls[colored_class(T_[i])].push_back(make_int2(i, k0));
       d.num_chunks = (K_[i] + kc_ - 1) / kc_;
       chunk0[i] = (int)chunks.size();
       for (int c = 0; c < d.num_chunks; ++c)
@@ -758,6 +772,12 @@ private:
     num_tiles_ = (int)tiles.size();
     num_chunks_ = (int)chunks.size();
     num_swork_ = (int)swork.size();
+    class_begin_[0] = 0;
+    for (int k = 0; k < 5; ++k)
+    {
+      cwork.insert(cwork.end(), cwork_cls[k].begin(), cwork_cls[k].end());
+      class_begin_[k + 1] = (int)cwork.size();
+    }
     num_cwork_ = (int)cwork.size();
     MG_TRY(inst_d_.alloc(I_));
     MG_TRY(tiles_d_.alloc(tiles.size()));
@@ -785,8 +805,17 @@ private:
   template <int NS>
   mppi_status occupancy_ns(int* per_sm)
   {
-    constexpr int TCH = RolloutShape<NS, C>::TCH;
-    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, rollout_kernel<Model, NS, TCH>, NS, 0));
+    if (use_bulk_)
+    {
+      using B = BulkRolloutShape<NS, C>;
+      MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, rollout_kernel_bulk<Model, NS, B::TCH>, NS,
+                                                            B::SMEM));
+    }
+    else
+    {
+      constexpr int TCH = RolloutShape<NS, C>::TCH;
+      MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, rollout_kernel<Model, NS, TCH>, NS, 0));
+    }
     if (*per_sm < 1) *per_sm = 1;
     return MPPI_OK;
   }
@@ -845,14 +874,22 @@ private:
     a.stride = s.stride;
     a.decay_pow = s.decay_pow;
     a.sh = s.sh;
-    return launch_colored_sampler<C>(a, max_t_, num_sms_, stream_);
+    return launch_colored_sampler<C>(a, class_begin_, max_t_, num_sms_, stream_);
   }
 
   template <int NS>
   void launch_rollout_ns(const RolloutArgs<Model>& a)
   {
-    constexpr int TCH = RolloutShape<NS, C>::TCH;
-    rollout_kernel<Model, NS, TCH><<<rollout_grid_, NS, 0, stream_>>>(a);
+    if (use_bulk_)
+    {
+      using B = BulkRolloutShape<NS, C>;
+      rollout_kernel_bulk<Model, NS, B::TCH><<<rollout_grid_, NS, B::SMEM, stream_>>>(a);
+    }
+    else
+    {
+      constexpr int TCH = RolloutShape<NS, C>::TCH;
+      rollout_kernel<Model, NS, TCH><<<rollout_grid_, NS, 0, stream_>>>(a);
+    }
   }
   mppi_status launch_rollout()
   {
@@ -869,6 +906,7 @@ private:
     a.costs = costs_d_.p;
     a.baseline_bits = baseline_bits_d_.p;
     a.tile_counter = counters_d_.p;
+    a.status = counters_d_.p + 4;
     a.dt = cp_.dt;
     a.lambda = cp_.lambda;
     a.alpha = cp_.alpha;
@@ -938,6 +976,7 @@ private:
     MG_CUDA(cudaMemcpyAsync(out_mean_h_.p, mean_d_.p, sizeof(float) * tc, cudaMemcpyDeviceToHost, stream_));
     MG_CUDA(cudaMemcpyAsync(out_bn_h_.p, bn_d_.p, sizeof(float) * 2 * I_, cudaMemcpyDeviceToHost, stream_));
     MG_CUDA(cudaMemcpyAsync(out_stats_h_.p, stats_d_.p, sizeof(double) * 3 * I_, cudaMemcpyDeviceToHost, stream_));
+    MG_CUDA(cudaMemcpyAsync(status_h_.p, counters_d_.p + 4, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_));
     return MPPI_OK;
   }
 
@@ -987,6 +1026,14 @@ private:
   // Host post-processing of computeControl (mppi_controller.cu:208-227).
   mppi_status finish_solve(const float* x0)
   {
+    if (status_h_.p[0] != 0u)
+    {
+      status_h_.p[0] = 0u;
+      MG_CUDA(cudaMemsetAsync(counters_d_.p + 4, 0, sizeof(unsigned int), stream_));
+      MG_CUDA(cudaStreamSynchronize(stream_));
+      set_error("a bounded wait for staged control data gave up inside the rollout kernel");
+      return MPPI_ETIMEOUT;
+    }
     memcpy(control_.data(), out_mean_h_.p, sizeof(float) * control_.size());
     memcpy(baseline_norm_.data(), out_bn_h_.p, sizeof(float) * 2 * I_);
     memcpy(stats_.data(), out_stats_h_.p, sizeof(double) * 3 * I_);
@@ -1068,12 +1115,15 @@ private:
   DevBuf<int> ctab_off_d_;
   DevBuf<int4> ctab_parts_d_;
   int num_cwork_ = 0, max_t_ = 1;
+  int class_begin_[6] = { 0, 0, 0, 0, 0, 0 };
   static constexpr int kColoredSamplesPerCta = ColoredShape<C>::SPB;
   DevBuf<int4> chunks_d_;
   DevBuf<long long> part_off_d_;
   DevBuf<int> chunk0_d_;
   PinnedBuf<float> x0_h_, mean_h_, out_mean_h_, out_bn_h_;
   PinnedBuf<double> out_stats_h_;
+  PinnedBuf<unsigned int> status_h_;
+  bool use_bulk_ = false;  // every instance has T*C % 4 == 0: stage controls with the bulk-copy engine
 };
 
 // Autotuner: times one full solve (non-graph) per candidate launch shape with CUDA events and keeps the fastest.
@@ -1161,6 +1211,7 @@ mppi_status standalone_rollout(const void* dyn, const void* cost, const mppi_sam
   a.costs = costs_d;
   a.baseline_bits = cnt_d.p + 2;
   a.tile_counter = cnt_d.p;
+  a.status = cnt_d.p + 3;
   a.dt = dt;
   a.lambda = lambda;
   a.alpha = alpha;

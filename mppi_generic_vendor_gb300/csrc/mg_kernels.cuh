@@ -14,6 +14,7 @@
 
 #include "mg_math.cuh"
 #include "mg_models.cuh"
+#include "mg_ptx.cuh"
 
 namespace mg
 {
@@ -175,10 +176,65 @@ struct RolloutArgs
   float* costs;
   unsigned int* baseline_bits;  // per instance, ordered-int min
   unsigned int* tile_counter;   // [0] = next tile, [1] = finished CTAs
+  unsigned int* status;         // set non-zero if a bounded wait gave up
   float dt, lambda, alpha;
   int use_likelihood;
   SampleShared sh;
 };
+
+// Steps t0 .. t0+nt-1 of sample k from its staged control row: Euler step, running cost on the stepped output plus
+// the likelihood-ratio term, accumulated in reference order (mppi_common.cu:105-144).
+template <class Model>
+__device__ __forceinline__ void rollout_chunk(const RolloutArgs<Model>& a, const InstDesc& d,
+                                              const typename Model::DynParams& dp,
+                                              const typename Model::CostParams& cp, int k, const float* urow, int t0,
+                                              int nt, float* x, float& running)
+{
+  constexpr int S = Model::STATE_DIM;
+  constexpr int C = Model::CONTROL_DIM;
+  auto do_step = [&](const float* u, int t) {
+    float xn[S];
+    euler_step<Model>(dp, x, u, xn, a.dt);
+    float step_cost = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
+    if (a.use_likelihood)
+    {
+      // GaussianDistributionImpl::computeLikelihoodRatioCost (gaussian.cu:490-574)
+      const bool zero_mean = (float)k >= (1.0f - a.sh.pure_pct) * (float)d.K;
+      float lc = 0.0f;
+#pragma unroll
+      for (int c = 0; c < C; ++c)
+      {
+        const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + c];
+        const float sd = a.sh.std_dev[c];
+        lc += a.sh.control_cost_coeff[c] * m * (m - 2.0f * u[c]) / (sd * sd);
+      }
+      step_cost += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
+    }
+    running += step_cost;
+#pragma unroll
+    for (int i = 0; i < S; ++i) x[i] = xn[i];
+  };
+  int tt = 0;
+  if constexpr (4 % C == 0)
+  {
+    // one 16-byte shared-memory read feeds 4/C steps
+    constexpr int G = 4 / C;
+    for (; tt + G <= nt; tt += G)
+    {
+      const float4 v = *reinterpret_cast<const float4*>(urow + tt * C);
+      const float uu[4] = { v.x, v.y, v.z, v.w };
+#pragma unroll
+      for (int g = 0; g < G; ++g) do_step(uu + g * C, t0 + tt + g);
+    }
+  }
+  for (; tt < nt; ++tt)
+  {
+    float u[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) u[c] = urow[tt * C + c];
+    do_step(u, t0 + tt);
+  }
+}
 
 template <class Model, int NS, int TCH>
 __global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ RolloutArgs<Model> a)
@@ -245,52 +301,7 @@ __global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ Rol
         }
       }
       __syncthreads();
-      if (active)
-      {
-        const float* urow = &stage[tid * ROW];
-        auto do_step = [&](const float* u, int t) {
-          float xn[S];
-          euler_step<Model>(dp, x, u, xn, a.dt);
-          float step_cost = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
-          if (a.use_likelihood)
-          {
-            // GaussianDistributionImpl::computeLikelihoodRatioCost (gaussian.cu:490-574)
-            const bool zero_mean = (float)k >= (1.0f - a.sh.pure_pct) * (float)d.K;
-            float lc = 0.0f;
-#pragma unroll
-            for (int c = 0; c < C; ++c)
-            {
-              const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + c];
-              const float sd = a.sh.std_dev[c];
-              lc += a.sh.control_cost_coeff[c] * m * (m - 2.0f * u[c]) / (sd * sd);
-            }
-            step_cost += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
-          }
-          running += step_cost;
-#pragma unroll
-          for (int i = 0; i < S; ++i) x[i] = xn[i];
-        };
-        int tt = 0;
-        if constexpr (4 % C == 0)
-        {
-          // one 16-byte shared-memory read feeds 4/C steps
-          constexpr int G = 4 / C;
-          for (; tt + G <= nt; tt += G)
-          {
-            const float4 v = *reinterpret_cast<const float4*>(urow + tt * C);
-            const float uu[4] = { v.x, v.y, v.z, v.w };
-#pragma unroll
-            for (int g = 0; g < G; ++g) do_step(uu + g * C, t0 + tt + g);
-          }
-        }
-        for (; tt < nt; ++tt)
-        {
-          float u[C];
-#pragma unroll
-          for (int c = 0; c < C; ++c) u[c] = urow[tt * C + c];
-          do_step(u, t0 + tt);
-        }
-      }
+      if (active) rollout_chunk<Model>(a, d, dp, cp, k, &stage[tid * ROW], t0, nt, x, running);
       __syncthreads();
     }
     unsigned int o = kOrderedPosInf;
@@ -308,6 +319,130 @@ __global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ Rol
     if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
   }
   // last CTA out resets the work counters for the next launch
+  if (tid == 0)
+  {
+    __threadfence();
+    const unsigned int done = atomicAdd(&a.tile_counter[1], 1u);
+    if (done == gridDim.x - 1)
+    {
+      a.tile_counter[0] = 0u;
+      a.tile_counter[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// Rollout with the controls staged by the bulk-copy engine.  Each thread owns one row of a double-buffered stage and
+// copies its own sample's next time chunk with one cp.async.bulk while it integrates the current one; completion is
+// tracked by one mbarrier per warp and buffer (32 arrivals, expect-tx bytes).  No shared data crosses threads inside
+// the time loop, so warps run decoupled.  Every wait is bounded: a wait that gives up sets *status and the CTA stops.
+// Requires T*C % 4 == 0 for every instance (16-byte aligned rows and chunks).
+constexpr uint32_t kMaxBarrierSpins = 1u << 22;
+
+template <int NS, int C>
+struct BulkRolloutShape
+{
+  static constexpr int TCH = (2 * NS * (32 * C + 4) * 4 <= 48 * 1024) ? 32 : (2 * NS * (16 * C + 4) * 4 <= 48 * 1024) ? 16 : 8;
+  static constexpr int ROW = TCH * C + 4;
+  static constexpr size_t SMEM = 2 * (size_t)NS * ROW * sizeof(float);
+};
+
+template <class Model, int NS, int TCH>
+__global__ void __launch_bounds__(NS) rollout_kernel_bulk(const __grid_constant__ RolloutArgs<Model> a)
+{
+  constexpr int S = Model::STATE_DIM;
+  constexpr int C = Model::CONTROL_DIM;
+  constexpr int ROW = TCH * C + 4;
+  constexpr int WARPS = NS / 32;
+  static_assert((TCH * C) % 4 == 0 && NS % 32 == 0, "chunk rows must be whole 16-byte units");
+  extern __shared__ __align__(16) float stage[];  // [2][NS][ROW]
+  __shared__ __align__(8) uint64_t mbar[2][WARPS];
+  __shared__ int s_tile;
+  __shared__ unsigned int s_min;
+  __shared__ int s_fail;  // CTA-uniform stop flag (read only after a barrier)
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (tid < 2 * WARPS) mbar_init(&mbar[tid / WARPS][tid % WARPS], 32);
+  if (tid == 0) s_fail = 0;
+  fence_mbarrier_init();
+  __syncthreads();
+  uint32_t parity = 0u;  // bit b = phase parity of buffer b
+  int uses = 0;  // buffer of chunk j of the current tile is (uses + j) & 1
+  bool failed = false;
+
+  for (;;)
+  {
+    if (tid == 0)
+    {
+      s_tile = (int)atomicAdd(&a.tile_counter[0], 1u);
+      s_min = kOrderedPosInf;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= a.num_tiles || s_fail) break;
+    const int2 w = a.tiles[tile];
+    const InstDesc d = a.inst[w.x];
+    const int k = w.y + tid;
+    const bool active = k < d.K;
+    const typename Model::DynParams dp = a.dyn[w.x];
+    const typename Model::CostParams& cp = a.cost[w.x];
+    const float* my_row = a.samples + d.u_off + (long long)k * d.T * C;
+    float* const my_stage0 = stage + tid * ROW;  // buffer b row: my_stage0 + b * NS * ROW
+
+    float x[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i) x[i] = a.x0[d.x_off + i];
+    float running = 0.0f;
+    const int nchunks = (d.T + TCH - 1) / TCH;
+    auto issue = [&](int j) {
+      const int b = (uses + j) & 1;
+      const int t0 = j * TCH;
+      const uint32_t bytes = (uint32_t)(min(TCH, d.T - t0) * C * 4);
+      if (active)
+      {
+        fence_proxy_async_smem();  // this thread's earlier reads of its row precede the async overwrite
+        mbar_arrive_expect_tx(&mbar[b][warp], bytes);
+        bulk_copy_g2s(my_stage0 + b * NS * ROW, my_row + t0 * C, bytes, &mbar[b][warp]);
+      }
+      else
+      {
+        mbar_arrive(&mbar[b][warp]);
+      }
+    };
+    issue(0);
+    for (int j = 0; j < nchunks; ++j)
+    {
+      const int b = (uses + j) & 1;
+      if (j + 1 < nchunks) issue(j + 1);
+      if (!mbar_wait_bounded(&mbar[b][warp], (parity >> b) & 1u, kMaxBarrierSpins))
+      {
+        failed = true;
+        s_fail = 1;
+        atomicOr(a.status, 1u);
+        // give the copy in flight one more bounded chance to land before the CTA leaves
+        mbar_wait_bounded(&mbar[b][warp], (parity >> b) & 1u, kMaxBarrierSpins);
+        if (j + 1 < nchunks) mbar_wait_bounded(&mbar[b ^ 1][warp], (parity >> (b ^ 1)) & 1u, kMaxBarrierSpins);
+        break;
+      }
+      parity ^= (1u << b);
+      const int t0 = j * TCH;
+      if (active) rollout_chunk<Model>(a, d, dp, cp, k, my_stage0 + b * NS * ROW, t0, min(TCH, d.T - t0), x, running);
+    }
+    uses += nchunks;
+    unsigned int o = kOrderedPosInf;
+    if (active && !failed)
+    {
+      const float tf = (float)d.T;
+      const float cost = running / tf + Model::terminalCost(cp, a.aux, x) / tf;
+      a.costs[d.k_off + k] = cost;
+      o = float_to_ordered(cost);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) o = min(o, __shfl_xor_sync(0xffffffffu, o, off));
+    if ((tid & 31) == 0) atomicMin(&s_min, o);
+    __syncthreads();
+    if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+  }
   if (tid == 0)
   {
     __threadfence();
@@ -407,19 +542,51 @@ __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_consta
   const int TC = a.samples ? d.T * C : 0;
   const float* ubase = a.samples + d.u_off + (long long)kb * TC;
   float* prow = a.partials + a.part_off[blockIdx.x];
-  for (int j = tid; j < TC; j += blockDim.x)
+  if (TC > 0 && TC <= (int)blockDim.x)
   {
-    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc3 = 0.0f;
-    int i = 0;
-    for (; i + 4 <= nk; i += 4)
+    // G groups of TC threads; group g sums samples g, g + G, ... of the chunk for column j, then the groups are
+    // combined in group order (a fixed order, so the result does not depend on scheduling)
+    __shared__ float s_part[256];
+    const int G = blockDim.x / TC;
+    const int g = tid / TC, j = tid - g * TC;
+    float acc = 0.0f;
+    if (g < G)
     {
-      acc0 = fmaf(s_w[i], __ldg(ubase + (long long)i * TC + j), acc0);
-      acc1 = fmaf(s_w[i + 1], __ldg(ubase + (long long)(i + 1) * TC + j), acc1);
-      acc2 = fmaf(s_w[i + 2], __ldg(ubase + (long long)(i + 2) * TC + j), acc2);
-      acc3 = fmaf(s_w[i + 3], __ldg(ubase + (long long)(i + 3) * TC + j), acc3);
+      float acc0 = 0.0f, acc1 = 0.0f;
+      int i = g;
+      for (; i + G < nk; i += 2 * G)
+      {
+        acc0 = fmaf(s_w[i], __ldg(ubase + (long long)i * TC + j), acc0);
+        acc1 = fmaf(s_w[i + G], __ldg(ubase + (long long)(i + G) * TC + j), acc1);
+      }
+      if (i < nk) acc0 = fmaf(s_w[i], __ldg(ubase + (long long)i * TC + j), acc0);
+      acc = acc0 + acc1;
+      s_part[tid] = acc;
     }
-    for (; i < nk; ++i) acc0 = fmaf(s_w[i], __ldg(ubase + (long long)i * TC + j), acc0);
-    prow[j] = (acc0 + acc1) + (acc2 + acc3);
+    __syncthreads();
+    if (tid < TC)
+    {
+      float s = s_part[tid];
+      for (int gg = 1; gg < G; ++gg) s += s_part[gg * TC + tid];
+      prow[tid] = s;
+    }
+  }
+  else
+  {
+    for (int j = tid; j < TC; j += blockDim.x)
+    {
+      float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc3 = 0.0f;
+      int i = 0;
+      for (; i + 4 <= nk; i += 4)
+      {
+        acc0 = fmaf(s_w[i], __ldg(ubase + (long long)i * TC + j), acc0);
+        acc1 = fmaf(s_w[i + 1], __ldg(ubase + (long long)(i + 1) * TC + j), acc1);
+        acc2 = fmaf(s_w[i + 2], __ldg(ubase + (long long)(i + 2) * TC + j), acc2);
+        acc3 = fmaf(s_w[i + 3], __ldg(ubase + (long long)(i + 3) * TC + j), acc3);
+      }
+      for (; i < nk; ++i) acc0 = fmaf(s_w[i], __ldg(ubase + (long long)i * TC + j), acc0);
+      prow[j] = (acc0 + acc1) + (acc2 + acc3);
+    }
   }
   if (tid == 0)
   {

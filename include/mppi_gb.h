@@ -296,6 +296,43 @@ mppi_status mppi_time_kernels(mppi_handle* h, int optimization_stride, int reps,
 /* The stream the handle enqueues on (a cudaStream_t). */
 void* mppi_get_stream(const mppi_handle* h);
 
+/* ---- learned dynamics surrogate (no reference counterpart; the reference only runs pre-trained networks,
+ *      FNNHelper / NeuralNetModel, fnn_helper.cu:418-495, ar_nn_model.cu:127-156) ---------------------------------- */
+
+/* 9 -> 64 -> 64 -> 5 tanh MLP: inputs (x, y, yaw, vx, vy, yaw_rate, steer, throttle, steer_cmd) normalised as
+ * (v - in_mean) / in_std; outputs d/dt (yaw, vx, vy, yaw_rate, steer) as out * out_std + out_mean.  A parameter
+ * vector is W1[64][9], b1[64], W2[64][64], b2[64], W3[5][64], b3[5], in_mean[9], in_std[9], out_mean[5],
+ * out_std[5] (MPPI_MLP_PARAMS floats). */
+#define MPPI_MLP_WEIGHTS 5125
+#define MPPI_MLP_PARAMS 5153
+
+typedef struct mppi_surrogate_config
+{
+  int num_transitions;               /* training set size (default 1 << 20) */
+  float state_lower[7];              /* box the training states are drawn from, uniformly */
+  float state_upper[7];
+  uint64_t seed;
+} mppi_surrogate_config;
+
+typedef struct mppi_surrogate mppi_surrogate;
+
+void mppi_default_surrogate_config(mppi_surrogate_config* cfg);
+mppi_status mppi_surrogate_create(const mppi_bicycle_slip_params* dyn, const mppi_surrogate_config* cfg, void* stream,
+                                  mppi_surrogate** out);
+mppi_status mppi_surrogate_destroy(mppi_surrogate* s);
+/* Draw the training transitions on the GPU from the analytic model and fix the input / output normalisation. */
+mppi_status mppi_surrogate_generate(mppi_surrogate* s);
+/* `steps` Adam steps on random mini-batches of `batch` transitions, learning rate decaying geometrically from lr to
+ * lr_final; loss_out (may be NULL) receives the mini-batch loss of every step. */
+mppi_status mppi_surrogate_train(mppi_surrogate* s, int steps, int batch, float lr, float lr_final, float* loss_out);
+/* Loss and parameter gradient on a given normalised batch (host X[B][9], Y[B][5]) with the training kernels. */
+mppi_status mppi_surrogate_gradient(mppi_surrogate* s, const float* X, const float* Y, int batch, float* grad_out,
+                                    float* loss_out);
+/* Root-mean-square error per output, in physical units, on n fresh transitions of the analytic model. */
+mppi_status mppi_surrogate_validate(mppi_surrogate* s, int n, float* rmse5);
+mppi_status mppi_surrogate_get_params(mppi_surrogate* s, float* out);
+mppi_status mppi_surrogate_set_params(mppi_surrogate* s, const float* in);
+
 /* ---- kernel-level entry points (mppi::kernels launchers, include/mppi/core/mppi_common.cuh:206-258) ----------- */
 
 /* baseline = min, w = exp(-(c - baseline) * lambda_inv) in place, normaliser = sum w; out2[2*s] = baseline,

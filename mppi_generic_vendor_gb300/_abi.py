@@ -144,6 +144,28 @@ SIGNATURES = [
     ("mppi_kernel_sincos", C.c_int, [_P, _P, _P, C.c_size_t, _P]),
 ]
 
+MLP_WEIGHTS = 5125
+MLP_PARAMS = 5153
+
+
+class SurrogateConfig(C.Structure):
+    _fields_ = [("num_transitions", C.c_int), ("state_lower", C.c_float * 7), ("state_upper", C.c_float * 7),
+                ("seed", C.c_uint64)]
+
+
+SIGNATURES += [
+    ("mppi_default_surrogate_config", None, [C.POINTER(SurrogateConfig)]),
+    ("mppi_surrogate_create", C.c_int, [C.POINTER(BicycleSlipParams), C.POINTER(SurrogateConfig), _P,
+                                        C.POINTER(_P)]),
+    ("mppi_surrogate_destroy", C.c_int, [_P]),
+    ("mppi_surrogate_generate", C.c_int, [_P]),
+    ("mppi_surrogate_train", C.c_int, [_P, C.c_int, C.c_int, C.c_float, C.c_float, _FP]),
+    ("mppi_surrogate_gradient", C.c_int, [_P, _FP, _FP, C.c_int, _FP, _FP]),
+    ("mppi_surrogate_validate", C.c_int, [_P, C.c_int, _FP]),
+    ("mppi_surrogate_get_params", C.c_int, [_P, _FP]),
+    ("mppi_surrogate_set_params", C.c_int, [_P, _FP]),
+]
+
 PKG_DIR = Path(__file__).resolve().parent
 LIB_PATH = PKG_DIR / "_build" / "libmppi_gb.so"
 HEADER_PATH = PKG_DIR.parent / "include" / "mppi_gb.h"

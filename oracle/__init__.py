@@ -232,3 +232,37 @@ def compute_control(model, dyn, cost, cparams, sampling, constraints, K, T, Cdim
         raise ValueError(f"oracle has no model {model}")
     return dict(control=control.reshape(T, Cdim), costs=costs, weights=w, samples=samples, baseline=b.value,
                 normalizer=n.value, state_seq=state.reshape(T, S))
+
+
+# ------------------------------------------------------------------------------------------------ MLP surrogate
+def _mlp_sigs():
+    L = lib()
+    L.orc_mlp_num_params.restype = C.c_int
+    L.orc_mlp_forward.argtypes = [_FP, _FP, C.c_int, _DP]
+    L.orc_mlp_loss_grad.restype = C.c_double
+    L.orc_mlp_loss_grad.argtypes = [_DP, _FP, _FP, C.c_int, _DP]
+    return L
+
+
+def mlp_num_params() -> int:
+    return _mlp_sigs().orc_mlp_num_params()
+
+
+def mlp_forward(params, X):
+    L = _mlp_sigs()
+    p = _f32(params)
+    X = _f32(X).reshape(-1, 9)
+    Y = np.empty((X.shape[0], 5), dtype=np.float64)
+    L.orc_mlp_forward(_fp(p), _fp(X), X.shape[0], Y.ctypes.data_as(_DP))
+    return Y
+
+
+def mlp_loss_grad(params, X, Y):
+    """MSE loss and its gradient in FP64 by hand back-propagation (params in float64)."""
+    L = _mlp_sigs()
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    X = _f32(X).reshape(-1, 9)
+    Y = _f32(Y).reshape(-1, 5)
+    g = np.empty_like(p)
+    loss = L.orc_mlp_loss_grad(p.ctypes.data_as(_DP), _fp(X), _fp(Y), X.shape[0], g.ctypes.data_as(_DP))
+    return loss, g

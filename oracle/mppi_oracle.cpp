@@ -653,10 +653,106 @@ static void colored_noise(const float* spectrum /*[K][C][F][2]*/, int K, int T, 
   for (auto& th : pool) th.join();
 }
 
+// ------------------------------------------------------------------------------------------------ MLP surrogate
+// 9 -> 64 -> 64 -> 5 tanh MLP with a linear output layer (FNNHelper::forward, fnn_helper.cu:353-382; the last layer
+// applies no non-linearity, :368-379).  Parameters are one flat vector: W1[64][9], b1[64], W2[64][64], b2[64],
+// W3[5][64], b3[5] (row-major, output index first, as FNNHelper's theta_ layout).
+constexpr int kIn = 9, kHid = 64, kOut = 5;
+constexpr int kW1 = 0, kB1 = kW1 + kHid * kIn, kW2 = kB1 + kHid, kB2 = kW2 + kHid * kHid, kW3 = kB2 + kHid,
+              kB3 = kW3 + kOut * kHid, kNumParams = kB3 + kOut;
+
+template <class R>
+static void mlp_forward(const R* p, const R* x, R* h1, R* h2, R* y)
+{
+  for (int j = 0; j < kHid; ++j)
+  {
+    R z = p[kB1 + j];
+    for (int i = 0; i < kIn; ++i) z += p[kW1 + j * kIn + i] * x[i];
+    h1[j] = std::tanh(z);
+  }
+  for (int j = 0; j < kHid; ++j)
+  {
+    R z = p[kB2 + j];
+    for (int i = 0; i < kHid; ++i) z += p[kW2 + j * kHid + i] * h1[i];
+    h2[j] = std::tanh(z);
+  }
+  for (int j = 0; j < kOut; ++j)
+  {
+    R z = p[kB3 + j];
+    for (int i = 0; i < kHid; ++i) z += p[kW3 + j * kHid + i] * h2[i];
+    y[j] = z;
+  }
+}
+
+// Mean squared error over B samples and 5 outputs and its gradient by hand back-propagation (FP64).
+static double mlp_loss_grad(const double* p, const float* X, const float* Y, int B, double* g)
+{
+  std::fill(g, g + kNumParams, 0.0);
+  double loss = 0.0;
+  const double scale = 2.0 / ((double)B * kOut);
+  for (int b = 0; b < B; ++b)
+  {
+    double x[kIn], h1[kHid], h2[kHid], y[kOut], dy[kOut], dh2[kHid], dh1[kHid];
+    for (int i = 0; i < kIn; ++i) x[i] = X[(size_t)b * kIn + i];
+    mlp_forward<double>(p, x, h1, h2, y);
+    for (int j = 0; j < kOut; ++j)
+    {
+      const double e = y[j] - (double)Y[(size_t)b * kOut + j];
+      loss += e * e;
+      dy[j] = scale * e;
+      g[kB3 + j] += dy[j];
+      for (int i = 0; i < kHid; ++i) g[kW3 + j * kHid + i] += dy[j] * h2[i];
+    }
+    for (int i = 0; i < kHid; ++i)
+    {
+      double s = 0.0;
+      for (int j = 0; j < kOut; ++j) s += dy[j] * p[kW3 + j * kHid + i];
+      dh2[i] = s * (1.0 - h2[i] * h2[i]);
+    }
+    for (int j = 0; j < kHid; ++j)
+    {
+      g[kB2 + j] += dh2[j];
+      for (int i = 0; i < kHid; ++i) g[kW2 + j * kHid + i] += dh2[j] * h1[i];
+    }
+    for (int i = 0; i < kHid; ++i)
+    {
+      double s = 0.0;
+      for (int j = 0; j < kHid; ++j) s += dh2[j] * p[kW2 + j * kHid + i];
+      dh1[i] = s * (1.0 - h1[i] * h1[i]);
+    }
+    for (int j = 0; j < kHid; ++j)
+    {
+      g[kB1 + j] += dh1[j];
+      for (int i = 0; i < kIn; ++i) g[kW1 + j * kIn + i] += dh1[j] * x[i];
+    }
+  }
+  return loss / ((double)B * kOut);
+}
+
 }  // namespace orc
 
 // ================================================================================================= C interface
 extern "C" {
+
+int orc_mlp_num_params(void) { return orc::kNumParams; }
+
+// Forward pass of B samples (X float[B][9], Y float[B][5]) in FP64 with FP32 parameters.
+void orc_mlp_forward(const float* params, const float* X, int B, double* Y)
+{
+  std::vector<double> p(params, params + orc::kNumParams);
+  for (int b = 0; b < B; ++b)
+  {
+    double x[orc::kIn], h1[orc::kHid], h2[orc::kHid];
+    for (int i = 0; i < orc::kIn; ++i) x[i] = X[(size_t)b * orc::kIn + i];
+    orc::mlp_forward<double>(p.data(), x, h1, h2, Y + (size_t)b * orc::kOut);
+  }
+}
+
+// MSE loss and its parameter gradient (hand back-propagation, FP64).
+double orc_mlp_loss_grad(const double* params, const float* X, const float* Y, int B, double* grad)
+{
+  return orc::mlp_loss_grad(params, X, Y, B, grad);
+}
 
 void orc_sincosf(const float* x, float* s, float* c, size_t n)
 {

@@ -346,6 +346,16 @@ mppi_status mppi_kernel_weight_transform(float* costs_d, float* out2_d, float la
 mppi_status mppi_kernel_weighted_reduction(const float* weights_d, const float* controls_d, float* new_u_d,
                                            const float* baseline_norm_d, int index, int num_timesteps,
                                            int num_rollouts, int control_dim, void* stream);
+/* Same result as mppi_kernel_weighted_reduction for callers that may not allocate memory (a control loop with a
+ * frozen memory map, a process whose GPU memory belongs to another allocator, a build that forbids allocation after
+ * start-up).  No counterpart in the reference.  The scratch is one 4 MiB array inside the library's device image,
+ * kept by every GPU that loads the library until exit; the first call on a device looks up its address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.  Limits: num_rollouts <= 65536 and
+ * num_timesteps * control_dim <= 1024, else MPPI_EINVAL.  Calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller. */
+mppi_status mppi_kernel_weighted_reduction_noalloc(const float* weights_d, const float* controls_d, float* new_u_d,
+                                                   const float* baseline_norm_d, int index, int num_timesteps,
+                                                   int num_rollouts, int control_dim, void* stream);
 /* Rollout of K samples from x0 with the given (already constrained) controls, writing per-sample costs (device).
  * Replaces launchRolloutKernel (mppi_common.cu:1335-1361).  mean_d (float[T*C]) feeds the likelihood-ratio term. */
 mppi_status mppi_kernel_rollout(int model, const void* dyn_params, size_t dyn_bytes, const void* cost_params,

@@ -135,6 +135,7 @@ SIGNATURES = [
     ("mppi_get_stream", C.c_void_p, [_P]),
     ("mppi_kernel_weight_transform", C.c_int, [_P, _P, C.c_float, C.c_int, C.c_int, _P]),
     ("mppi_kernel_weighted_reduction", C.c_int, [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    ("mppi_kernel_weighted_reduction_noalloc", C.c_int, [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
     ("mppi_kernel_rollout", C.c_int, [C.c_int, _P, C.c_size_t, _P, C.c_size_t, C.POINTER(SamplingParams), _P, _P,
                                       _P, _P, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, _P]),
     ("mppi_kernel_gaussian_controls", C.c_int, [_P, _P, _FP, C.POINTER(ControlConstraints), C.c_int, C.c_int,

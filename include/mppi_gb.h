@@ -333,6 +333,11 @@ mppi_status mppi_surrogate_validate(mppi_surrogate* s, int n, float* rmse5);
 mppi_status mppi_surrogate_get_params(mppi_surrogate* s, float* out);
 mppi_status mppi_surrogate_set_params(mppi_surrogate* s, const float* in);
 
+/* Surrogate forward pass on the tensor cores (BF16 operands, FP32 accumulation) for `batch` rows of physical inputs
+ * X_d[batch][9], writing physical outputs Y_d[batch][5] (device pointers); params is the host parameter vector.
+ * The evaluation FNNHelper::forward performs per sample (fnn_helper.cu:418-495), as one GEMM chain per 128 rows. */
+mppi_status mppi_kernel_mlp_forward(const float* params, const float* X_d, float* Y_d, int batch, void* stream);
+
 /* ---- kernel-level entry points (mppi::kernels launchers, include/mppi/core/mppi_common.cuh:206-258) ----------- */
 
 /* baseline = min, w = exp(-(c - baseline) * lambda_inv) in place, normaliser = sum w; out2[2*s] = baseline,

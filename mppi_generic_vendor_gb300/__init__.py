@@ -5,10 +5,12 @@ the host-side mirror of the reference's interface.  Build the library with ``pyt
 """
 from . import _abi
 from ._abi import MPPIError
-from .controller import (BatchedMPPIController, BicycleDynamics, BicycleSlipDynamics, CartpoleDynamics,
+from .controller import (BatchedMPPIController, BicycleDynamics, BicycleSlipDynamics, BicycleSlipMLPDynamics,
+                         CartpoleDynamics,
                          CartpoleSwingupCost, ColoredNoiseDistribution, CostmapCost, DoubleIntegratorDynamics,
                          DoubleIntegratorObstacleCost, GaussianDistribution, VanillaMPPIController)
 
 __all__ = ["MPPIError", "BatchedMPPIController", "VanillaMPPIController", "CartpoleDynamics", "CartpoleSwingupCost",
            "DoubleIntegratorDynamics", "DoubleIntegratorObstacleCost", "BicycleDynamics", "BicycleSlipDynamics",
+           "BicycleSlipMLPDynamics",
            "CostmapCost", "GaussianDistribution", "ColoredNoiseDistribution", "_abi"]

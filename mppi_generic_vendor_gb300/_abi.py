@@ -165,6 +165,7 @@ SIGNATURES += [
     ("mppi_surrogate_validate", C.c_int, [_P, C.c_int, _FP]),
     ("mppi_surrogate_get_params", C.c_int, [_P, _FP]),
     ("mppi_surrogate_set_params", C.c_int, [_P, _FP]),
+    ("mppi_kernel_mlp_forward", C.c_int, [_FP, _P, _P, C.c_int, _P]),
 ]
 
 PKG_DIR = Path(__file__).resolve().parent

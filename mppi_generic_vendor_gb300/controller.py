@@ -126,6 +126,37 @@ class BicycleSlipDynamics(_Plugin):
         self.control_rngs = [tuple(r) for r in ranges]
 
 
+class BicycleSlipMLPDynamics(BicycleSlipDynamics):
+    """Dynamic bicycle whose five non-kinematic derivatives come from the learned 9-64-64-5 surrogate
+    (NeuralNetModel, include/mppi/dynamics/autorally/ar_nn_model.cuh:133-145).  The network is evaluated on the
+    tensor cores with BF16 (``precision="bf16"``) or FP8 E4M3 (``"fp8"``) weights and FP32 accumulation.  The
+    ``BicycleSlipDynamics`` parameters are kept for the analytic judge and the host twin."""
+
+    model_id = A.MODEL_BICYCLE_SLIP_MLP
+    PRECISIONS = {"bf16": 0, "fp8": 1}
+
+    def __init__(self, params=None, precision="bf16", **slip_kwargs):
+        super().__init__(**slip_kwargs)
+        if precision not in self.PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(self.PRECISIONS)}")
+        self.precision = precision
+        self.mlp_params = None
+        if params is not None:
+            self.updateModel(params)
+
+    def updateModel(self, params):
+        """Network + normalisation parameters, MPPI_MLP_PARAMS floats (``Surrogate.params()``)."""
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(-1))
+        if p.size != A.MLP_PARAMS:
+            raise ValueError(f"surrogate parameter vector must hold {A.MLP_PARAMS} floats")
+        self.mlp_params = p
+
+    def loadParams(self, path):
+        """Parameters saved by ``Surrogate.save`` (npz)."""
+        with np.load(path) as f:
+            self.updateModel(f["params"])
+
+
 class CostmapCost(_Plugin):
     """map_coeff * bilinear(costmap, x, y) + speed_coeff (v - speed_target)^2 + steer_coeff steer^2."""
 
@@ -233,6 +264,9 @@ class BatchedMPPIController:
         cm = getattr(self.cost_, "costmap", None)
         if cm is not None:
             self.setCostmap(cm, self.cost_.resolution, self.cost_.origin)
+        mlp = getattr(self.model_, "mlp_params", None)
+        if mlp is not None:
+            self.setMLP(mlp, self.model_.precision)
 
     # ---- lifecycle
     def close(self):
@@ -336,6 +370,12 @@ class BatchedMPPIController:
         m = np.ascontiguousarray(costmap, dtype=np.float32)
         A.call("mppi_set_costmap", self._h, _fptr(m), int(m.shape[1]), int(m.shape[0]), float(resolution),
                float(origin[0]), float(origin[1]))
+
+    def setMLP(self, params, precision="bf16"):
+        """Load surrogate weights (MPPI_MLP_PARAMS floats) into the MLP dynamics; precision "bf16" or "fp8"."""
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(-1))
+        prec = BicycleSlipMLPDynamics.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        A.call("mppi_set_mlp", self._h, _fptr(p), p.size, prec)
 
     def injectNoise(self, noise):
         """Parity hook: use this standard-normal noise (all instances, samples layout) instead of Philox noise."""

@@ -273,7 +273,7 @@ mppi_status mppi_create(int model, int num_instances, const int* num_rollouts, c
     case MPPI_MODEL_DOUBLE_INTEGRATOR: st = create_double_integrator_engine(a, &e); break;
     case MPPI_MODEL_BICYCLE_COSTMAP: st = create_bicycle_costmap_engine(a, &e); break;
     case MPPI_MODEL_BICYCLE_SLIP: st = create_bicycle_slip_engine(a, &e); break;
-    case MPPI_MODEL_BICYCLE_SLIP_MLP: set_error("the MLP surrogate model is not built in this library"); return MPPI_EUNSUPPORTED;
+    case MPPI_MODEL_BICYCLE_SLIP_MLP: st = create_bicycle_slip_mlp_engine(a, &e); break;
     default: set_error("unknown model id %d", model); return MPPI_EINVAL;
   }
   if (st != MPPI_OK) return st;
@@ -379,11 +379,7 @@ mppi_status mppi_set_costmap(mppi_handle* h, const float* map, int width, int he
 mppi_status mppi_set_mlp(mppi_handle* h, const float* params, size_t num_params, int precision)
 {
   HANDLE_OK(h);
-  (void)params;
-  (void)num_params;
-  (void)precision;
-  set_error("this handle's model has no learned surrogate");
-  return MPPI_EUNSUPPORTED;
+  return h->engine->set_mlp(params, num_params, precision);
 }
 mppi_status mppi_inject_noise(mppi_handle* h, const float* noise, size_t count)
 {

@@ -13,3 +13,11 @@ mppi_status create_bicycle_slip_engine(const CreateArgs& a, EngineBase** out)
   return Engine<BicycleSlipModel>::create(a, out);
 }
 }  // namespace mg
+
+namespace mg
+{
+mppi_status create_bicycle_slip_mlp_engine(const CreateArgs& a, EngineBase** out)
+{
+  return Engine<BicycleSlipMLPModel>::create(a, out);
+}
+}  // namespace mg

@@ -21,6 +21,7 @@
 #include "mg_common.cuh"
 #include "mg_colored.cuh"
 #include "mg_kernels.cuh"
+#include "mg_mlp.cuh"
 
 namespace mg
 {
@@ -75,6 +76,7 @@ public:
   virtual cudaStream_t stream() const = 0;
   virtual mppi_status enqueue_device_solves(int stride, int count) = 0;
   virtual mppi_status time_kernels(int stride, int reps, float* ms3) = 0;
+  virtual mppi_status set_mlp(const float* params, size_t n, int precision) = 0;
 };
 
 // Factories, one per model translation unit.
@@ -82,6 +84,7 @@ mppi_status create_cartpole_engine(const CreateArgs& a, EngineBase** out);
 mppi_status create_double_integrator_engine(const CreateArgs& a, EngineBase** out);
 mppi_status create_bicycle_costmap_engine(const CreateArgs& a, EngineBase** out);
 mppi_status create_bicycle_slip_engine(const CreateArgs& a, EngineBase** out);
+mppi_status create_bicycle_slip_mlp_engine(const CreateArgs& a, EngineBase** out);
 
 // Kernel-level rollout entry points, one per model translation unit.
 mppi_status standalone_rollout_cartpole(const void* dyn, const void* cost, const mppi_sampling_params* sp,
@@ -196,6 +199,7 @@ public:
     MG_CHECK(x0 != nullptr, "x0 must not be NULL");
     MG_CHECK(stride >= 0, "optimization_stride must be >= 0");
     MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
+    MG_CHECK(!Model::kMlp || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
     for (int i = 0; i < I_ * S; ++i)
       if (!std::isfinite(x0[i]))
       {
@@ -434,6 +438,7 @@ public:
   mppi_status set_launch_config(int ns, int tch, int kc) override
   {
     MG_CHECK(ns == 32 || ns == 64 || ns == 128 || ns == 256, "rollout samples per CTA must be 32, 64, 128 or 256");
+    if (Model::kMlp) ns = 128;  // the tensor-core rollout owns 128-sample tiles
     MG_CHECK(kc >= 32 && kc <= 256 && (kc % 32) == 0, "reduction samples per CTA must be a multiple of 32 in [32, 256]");
     (void)tch;
     ns_ = ns;
@@ -444,10 +449,31 @@ public:
   }
   mppi_status autotune(const char* cache_path) override;
 
+  // Surrogate weights for the MLP model (ignored by analytic models): host FP32 copy for the nominal trajectory,
+  // device FP32 copy the rollout kernel converts to BF16 tensor-core operands.
+  mppi_status set_mlp(const float* params, size_t n, int precision) override
+  {
+    if (!Model::kMlp)
+    {
+      set_error("this handle's model has no learned surrogate");
+      return MPPI_EUNSUPPORTED;
+    }
+    MG_CHECK(params && n == (size_t)MPPI_MLP_PARAMS, "the MLP parameter vector holds %d floats", MPPI_MLP_PARAMS);
+    MG_CHECK(precision == 0, "MLP precision %d is not built (0 = bf16)", precision);
+    for (size_t i = 0; i < n; ++i) MG_CHECK(std::isfinite(params[i]), "MLP parameter %zu is not finite", i);
+    for (int i = 0; i < kMlpIn; ++i) MG_CHECK(params[kMlpInStd + i] > 0.0f, "MLP input scale %d must be positive", i);
+    mlp_host_.assign(params, params + n);
+    MG_TRY(mlp_d_.alloc(n));
+    MG_CUDA(cudaMemcpy(mlp_d_.p, params, sizeof(float) * n, cudaMemcpyHostToDevice));
+    invalidate_graphs();
+    return MPPI_OK;
+  }
+
   mppi_status enqueue_device_solves(int stride, int count) override
   {
     MG_CHECK(stride >= 0 && count >= 0, "stride and count must be >= 0");
     MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
+    MG_CHECK(!Model::kMlp || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
     auto it = device_graphs_.find(stride);
     cudaGraphExec_t exec = nullptr;
     if (it == device_graphs_.end())
@@ -479,6 +505,7 @@ public:
   {
     MG_CHECK(ms3 && reps >= 1, "need an output array and reps >= 1");
     MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
+    MG_CHECK(!Model::kMlp || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
     cudaEvent_t ev[4];
     for (auto& e : ev) MG_CUDA(cudaEventCreate(&e));
     float tot[3] = { 0, 0, 0 };
@@ -914,6 +941,7 @@ private:
     for (int c = 0; c < C; ++c)
       if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
     a.sh = make_sample_shared(sp_, cc_);
+    if constexpr (Model::kMlp) return launch_mlp_rollout(a, mlp_d_.p, num_sms_, stream_);
     switch (ns_)
     {
       case 32: launch_rollout_ns<32>(a); break;
@@ -1055,7 +1083,16 @@ private:
         for (int c = 0; c < C; ++c)
           uc[c] = enforce_constraint(u[(size_t)t * C + c], cc_.lower[c], cc_.upper[c], cc_.deadband[c],
                                      cc_.zero_control[c]);
-        euler_step<Model>(dyn_[i], x, uc, xn, cp_.dt);
+        if constexpr (Model::kMlp)
+        {
+          float xd[S];
+          mlp_host_dynamics(mlp_host_.data(), x, uc, xd);
+          for (int s = 0; s < S; ++s) xn[s] = fmaf(xd[s], cp_.dt, x[s]);
+        }
+        else
+        {
+          euler_step<Model>(dyn_[i], x, uc, xn, cp_.dt);
+        }
         for (int s = 0; s < S; ++s) x[s] = xs[(size_t)(t + 1) * S + s] = xn[s];
       }
       for (int t = 0; t < T; ++t)
@@ -1123,6 +1160,8 @@ private:
   PinnedBuf<float> x0_h_, mean_h_, out_mean_h_, out_bn_h_;
   PinnedBuf<double> out_stats_h_;
   PinnedBuf<unsigned int> status_h_;
+  std::vector<float> mlp_host_;  // surrogate parameters (MLP models only)
+  DevBuf<float> mlp_d_;
   bool use_bulk_ = false;  // every instance has T*C % 4 == 0: stage controls with the bulk-copy engine
 };
 

@@ -70,6 +70,7 @@ struct CartpoleModel
   static constexpr int STATE_DIM = 4, CONTROL_DIM = 1, OUTPUT_DIM = 4;
   static constexpr int kModelId = MPPI_MODEL_CARTPOLE;
   static constexpr bool kNeedsCostmap = false;
+  static constexpr bool kMlp = false;
   static constexpr int kFlopsPerStep = 60;  // counted from the source below (sin/cos polynomial included)
   using DynParams = mppi_cartpole_params;
   using CostParams = mppi_cartpole_cost_params;
@@ -111,6 +112,7 @@ struct DoubleIntegratorModel
   static constexpr int STATE_DIM = 4, CONTROL_DIM = 2, OUTPUT_DIM = 4;
   static constexpr int kModelId = MPPI_MODEL_DOUBLE_INTEGRATOR;
   static constexpr bool kNeedsCostmap = false;
+  static constexpr bool kMlp = false;
   static constexpr int kFlopsPerStep = 8 + 11 + 8 * 6;
   using DynParams = mppi_double_integrator_params;
   using CostParams = mppi_di_obstacle_cost_params;
@@ -157,6 +159,7 @@ struct BicycleCostmapModel
   static constexpr int STATE_DIM = 4, CONTROL_DIM = 2, OUTPUT_DIM = 4;
   static constexpr int kModelId = MPPI_MODEL_BICYCLE_COSTMAP;
   static constexpr bool kNeedsCostmap = true;
+  static constexpr bool kMlp = false;
   static constexpr int kFlopsPerStep = 2 * 22 + 12 + 25;
   using DynParams = mppi_bicycle_params;
   using CostParams = mppi_costmap_cost_params;
@@ -195,6 +198,7 @@ struct BicycleSlipModel
   static constexpr int STATE_DIM = 7, CONTROL_DIM = 2, OUTPUT_DIM = 7;
   static constexpr int kModelId = MPPI_MODEL_BICYCLE_SLIP;
   static constexpr bool kNeedsCostmap = true;
+  static constexpr bool kMlp = false;
   static constexpr int kFlopsPerStep = 3 * 22 + 45 + 25;
   using DynParams = mppi_bicycle_slip_params;
   using CostParams = mppi_costmap_cost_params;
@@ -242,6 +246,14 @@ struct BicycleSlipModel
   {
     return speedMapCost(q, aux, y) * q.terminal_coeff;
   }
+};
+
+// Learned-surrogate variant of the dynamic bicycle: same state, controls, parameters and cost; the (yaw, vx, vy,
+// yaw_rate, steer) derivatives come from the MLP (evaluated on the tensor cores by the engine's MLP rollout kernel).
+struct BicycleSlipMLPModel : BicycleSlipModel
+{
+  static constexpr int kModelId = MPPI_MODEL_BICYCLE_SLIP_MLP;
+  static constexpr bool kMlp = true;
 };
 
 // Euler step shared by every model (Dynamics::step -> updateState, dynamics.cu:128-152): x' = x + xdot * dt as one

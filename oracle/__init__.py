@@ -266,3 +266,14 @@ def mlp_loss_grad(params, X, Y):
     g = np.empty_like(p)
     loss = L.orc_mlp_loss_grad(p.ctypes.data_as(_DP), _fp(X), _fp(Y), X.shape[0], g.ctypes.data_as(_DP))
     return loss, g
+
+
+def set_mlp(params):
+    """Surrogate parameters (network + normalisation, 5153 floats) for the MLP bicycle model
+    (model id 5) in rollout / compute_control / dynamics_deriv."""
+    p = _f32(params).reshape(-1)
+    if p.size != 5153:
+        raise ValueError("surrogate parameter vector must hold 5153 floats")
+    L = lib()
+    L.orc_set_mlp.argtypes = [_FP]
+    L.orc_set_mlp(_fp(p))

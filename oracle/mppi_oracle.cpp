@@ -397,6 +397,67 @@ static void rollout_range(const Model& m, const float* x0, float* controls, bool
   }
 }
 
+// 9 -> 64 -> 64 -> 5 tanh MLP with a linear output layer (FNNHelper::forward, fnn_helper.cu:353-382; the last layer
+// applies no non-linearity, :368-379).  Parameters are one flat vector: W1[64][9], b1[64], W2[64][64], b2[64],
+// W3[5][64], b3[5] (row-major, output index first, as FNNHelper's theta_ layout).
+constexpr int kIn = 9, kHid = 64, kOut = 5;
+constexpr int kW1 = 0, kB1 = kW1 + kHid * kIn, kW2 = kB1 + kHid, kB2 = kW2 + kHid * kHid, kW3 = kB2 + kHid,
+              kB3 = kW3 + kOut * kHid, kNumParams = kB3 + kOut;
+
+template <class R>
+static void mlp_forward(const R* p, const R* x, R* h1, R* h2, R* y)
+{
+  for (int j = 0; j < kHid; ++j)
+  {
+    R z = p[kB1 + j];
+    for (int i = 0; i < kIn; ++i) z += p[kW1 + j * kIn + i] * x[i];
+    h1[j] = std::tanh(z);
+  }
+  for (int j = 0; j < kHid; ++j)
+  {
+    R z = p[kB2 + j];
+    for (int i = 0; i < kHid; ++i) z += p[kW2 + j * kHid + i] * h1[i];
+    h2[j] = std::tanh(z);
+  }
+  for (int j = 0; j < kOut; ++j)
+  {
+    R z = p[kB3 + j];
+    for (int i = 0; i < kHid; ++i) z += p[kW3 + j * kHid + i] * h2[i];
+    y[j] = z;
+  }
+}
+
+// Surrogate parameters of the MLP bicycle model (set with orc_set_mlp): the network above followed by the input and
+// output normalisation (in_mean[9], in_std[9], out_mean[5], out_std[5]), 5153 floats, kept in both precisions.
+constexpr int kInMean = kNumParams, kInStd = kInMean + kIn, kOutMean = kInStd + kIn, kOutStd = kOutMean + kOut,
+              kSurrogateParams = kOutStd + kOut;
+static std::vector<double> g_mlp_d;
+static std::vector<float> g_mlp_f;
+template <class R> static const R* mlp_params();
+template <> const double* mlp_params<double>() { return g_mlp_d.data(); }
+template <> const float* mlp_params<float>() { return g_mlp_f.data(); }
+
+template <class R>
+struct BicycleSlipMLP : BicycleSlip<R>
+{
+  // Kinematic rows as NeuralNetModel::computeKinematics (ar_nn_model.cu:119-124); the other five derivatives come
+  // from the network on the normalised (state, control) row (NeuralNetModel::computeDynamics, ar_nn_model.cu:127-156)
+  // evaluated in precision R with exact tanh.
+  void deriv(const R* x, const R* u, R* xd) const
+  {
+    const R* P = mlp_params<R>();
+    R sy, cy;
+    M<R>::sincos(x[2], &sy, &cy);
+    xd[0] = x[3] * cy - x[4] * sy;
+    xd[1] = x[3] * sy + x[4] * cy;
+    R in[kIn], h1[kHid], h2[kHid], y[kOut];
+    for (int i = 0; i < 7; ++i) in[i] = (x[i] - P[kInMean + i]) / P[kInStd + i];
+    for (int i = 0; i < 2; ++i) in[7 + i] = (u[i] - P[kInMean + 7 + i]) / P[kInStd + 7 + i];
+    mlp_forward<R>(P, in, h1, h2, y);
+    for (int j = 0; j < kOut; ++j) xd[2 + j] = y[j] * P[kOutStd + j] + P[kOutMean + j];
+  }
+};
+
 struct ModelBlob
 {
   int model;
@@ -434,6 +495,13 @@ static void with_model(const ModelBlob& b, F&& f)
       f(m);
       break;
     }
+    case MPPI_MODEL_BICYCLE_SLIP_MLP:
+    {
+      BicycleSlipMLP<R> m{ { *(const mppi_bicycle_slip_params*)b.dyn, *(const mppi_costmap_cost_params*)b.cost,
+                             b.map } };
+      f(m);
+      break;
+    }
     default: break;
   }
 }
@@ -446,6 +514,7 @@ static int model_state_dim(int model)
     case MPPI_MODEL_DOUBLE_INTEGRATOR: return 4;
     case MPPI_MODEL_BICYCLE_COSTMAP: return 4;
     case MPPI_MODEL_BICYCLE_SLIP: return 7;
+    case MPPI_MODEL_BICYCLE_SLIP_MLP: return g_mlp_d.empty() ? 0 : 7;
     default: return 0;
   }
 }
@@ -457,6 +526,7 @@ static int model_control_dim(int model)
     case MPPI_MODEL_DOUBLE_INTEGRATOR: return 2;
     case MPPI_MODEL_BICYCLE_COSTMAP: return 2;
     case MPPI_MODEL_BICYCLE_SLIP: return 2;
+    case MPPI_MODEL_BICYCLE_SLIP_MLP: return 2;
     default: return 0;
   }
 }
@@ -654,36 +724,6 @@ static void colored_noise(const float* spectrum /*[K][C][F][2]*/, int K, int T, 
 }
 
 // ------------------------------------------------------------------------------------------------ MLP surrogate
-// 9 -> 64 -> 64 -> 5 tanh MLP with a linear output layer (FNNHelper::forward, fnn_helper.cu:353-382; the last layer
-// applies no non-linearity, :368-379).  Parameters are one flat vector: W1[64][9], b1[64], W2[64][64], b2[64],
-// W3[5][64], b3[5] (row-major, output index first, as FNNHelper's theta_ layout).
-constexpr int kIn = 9, kHid = 64, kOut = 5;
-constexpr int kW1 = 0, kB1 = kW1 + kHid * kIn, kW2 = kB1 + kHid, kB2 = kW2 + kHid * kHid, kW3 = kB2 + kHid,
-              kB3 = kW3 + kOut * kHid, kNumParams = kB3 + kOut;
-
-template <class R>
-static void mlp_forward(const R* p, const R* x, R* h1, R* h2, R* y)
-{
-  for (int j = 0; j < kHid; ++j)
-  {
-    R z = p[kB1 + j];
-    for (int i = 0; i < kIn; ++i) z += p[kW1 + j * kIn + i] * x[i];
-    h1[j] = std::tanh(z);
-  }
-  for (int j = 0; j < kHid; ++j)
-  {
-    R z = p[kB2 + j];
-    for (int i = 0; i < kHid; ++i) z += p[kW2 + j * kHid + i] * h1[i];
-    h2[j] = std::tanh(z);
-  }
-  for (int j = 0; j < kOut; ++j)
-  {
-    R z = p[kB3 + j];
-    for (int i = 0; i < kHid; ++i) z += p[kW3 + j * kHid + i] * h2[i];
-    y[j] = z;
-  }
-}
-
 // Mean squared error over B samples and 5 outputs and its gradient by hand back-propagation (FP64).
 static double mlp_loss_grad(const double* p, const float* X, const float* Y, int B, double* g)
 {
@@ -735,6 +775,13 @@ static double mlp_loss_grad(const double* p, const float* X, const float* Y, int
 extern "C" {
 
 int orc_mlp_num_params(void) { return orc::kNumParams; }
+
+// Surrogate parameters (network + normalisation, 5153 floats) used by the MLP bicycle model.
+void orc_set_mlp(const float* params)
+{
+  orc::g_mlp_f.assign(params, params + orc::kSurrogateParams);
+  orc::g_mlp_d.assign(params, params + orc::kSurrogateParams);
+}
 
 // Forward pass of B samples (X float[B][9], Y float[B][5]) in FP64 with FP32 parameters.
 void orc_mlp_forward(const float* params, const float* X, int B, double* Y)

@@ -256,8 +256,20 @@ mppi_status mppi_set_costmap(mppi_handle* h, const float* map, int width, int he
 
 /* Surrogate weights for MPPI_MODEL_BICYCLE_SLIP_MLP: 9->64->64->5 tanh MLP, fp32 row-major W1[64][9], b1[64],
  * W2[64][64], b2[64], W3[5][64], b3[5] (FNNHelper layout, fnn_helper.cu:353-382), plus input / output scaling.
- * precision 0 = bf16 weights, 1 = fp8 e4m3 with one scale per layer. */
+ * precision 0 = bf16 weights on the tensor cores, 1 = fp8 e4m3 weights with one scale per layer on the tensor cores
+ * (both FP32 accumulation), 2 = plain FP32 on the CUDA cores (one thread per sample, as FNNHelper evaluates it). */
 mppi_status mppi_set_mlp(mppi_handle* h, const float* params, size_t num_params, int precision);
+
+/* Analytic judge of the surrogate rollout (MPPI_MODEL_BICYCLE_SLIP_MLP only): after the surrogate rollout the
+ * ceil(fraction * K_i) lowest-cost samples of every instance are re-rolled with the analytic dynamic bicycle in FP32;
+ * their costs become analytic - mean(analytic - surrogate) and the baseline is recomputed.  fraction 0 disables it;
+ * the default is 0.01.  No counterpart in the reference, whose NeuralNetModel rollouts are not checked. */
+mppi_status mppi_set_judge(mppi_handle* h, float fraction);
+/* Per instance after the last computeControl: out[2*i] = mean(analytic - surrogate) cost over the judged samples,
+ * out[2*i+1] = mean |analytic - surrogate| / |analytic|.  Zeros when the judge is off. */
+mppi_status mppi_get_judge_stats(mppi_handle* h, float* out);
+/* Fallback: roll out the analytic model instead of the surrogate (1) or the surrogate again (0). */
+mppi_status mppi_use_analytic_dynamics(mppi_handle* h, int enable);
 
 /*
  * Parity hook: use the given standard-normal noise for every subsequent iteration instead of Philox noise.
@@ -334,9 +346,15 @@ mppi_status mppi_surrogate_get_params(mppi_surrogate* s, float* out);
 mppi_status mppi_surrogate_set_params(mppi_surrogate* s, const float* in);
 
 /* Surrogate forward pass on the tensor cores (BF16 operands, FP32 accumulation) for `batch` rows of physical inputs
- * X_d[batch][9], writing physical outputs Y_d[batch][5] (device pointers); params is the host parameter vector.
- * The evaluation FNNHelper::forward performs per sample (fnn_helper.cu:418-495), as one GEMM chain per 128 rows. */
-mppi_status mppi_kernel_mlp_forward(const float* params, const float* X_d, float* Y_d, int batch, void* stream);
+ * X_d[batch][9], writing physical outputs Y_d[batch][5] (device pointers); params is the host parameter vector and
+ * precision selects BF16 (0) or FP8 E4M3 weights with one scale per layer (1).  The evaluation FNNHelper::forward
+ * performs per sample (fnn_helper.cu:418-495), as one GEMM chain per 128 rows. */
+mppi_status mppi_kernel_mlp_forward(const float* params, int precision, const float* X_d, float* Y_d, int batch,
+                                    void* stream);
+/* The weights the tensor cores see for a precision: out[MPPI_MLP_PARAMS] is params with every weight replaced by its
+ * quantised value q (BF16 rounding happens on the device; FP8: the E4M3 value of W / scale), layer_scales[3] (may be
+ * NULL) the per-layer scales (1 for BF16).  W is represented as q * scale. */
+mppi_status mppi_mlp_quantize(const float* params, int precision, float* out, float* layer_scales);
 
 /* ---- kernel-level entry points (mppi::kernels launchers, include/mppi/core/mppi_common.cuh:206-258) ----------- */
 

@@ -122,6 +122,9 @@ SIGNATURES = [
     ("mppi_set_controller_params", C.c_int, [_P, C.POINTER(ControllerParams)]),
     ("mppi_set_costmap", C.c_int, [_P, _FP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float]),
     ("mppi_set_mlp", C.c_int, [_P, _FP, C.c_size_t, C.c_int]),
+    ("mppi_set_judge", C.c_int, [_P, C.c_float]),
+    ("mppi_get_judge_stats", C.c_int, [_P, _FP]),
+    ("mppi_use_analytic_dynamics", C.c_int, [_P, C.c_int]),
     ("mppi_inject_noise", C.c_int, [_P, _FP, C.c_size_t]),
     ("mppi_generate_samples", C.c_int, [_P, C.c_int, C.c_int]),
     ("mppi_set_graph_mode", C.c_int, [_P, C.c_int]),
@@ -165,7 +168,8 @@ SIGNATURES += [
     ("mppi_surrogate_validate", C.c_int, [_P, C.c_int, _FP]),
     ("mppi_surrogate_get_params", C.c_int, [_P, _FP]),
     ("mppi_surrogate_set_params", C.c_int, [_P, _FP]),
-    ("mppi_kernel_mlp_forward", C.c_int, [_FP, _P, _P, C.c_int, _P]),
+    ("mppi_kernel_mlp_forward", C.c_int, [_FP, C.c_int, _P, _P, C.c_int, _P]),
+    ("mppi_mlp_quantize", C.c_int, [_FP, C.c_int, _FP, _FP]),
 ]
 
 PKG_DIR = Path(__file__).resolve().parent

@@ -129,11 +129,12 @@ class BicycleSlipDynamics(_Plugin):
 class BicycleSlipMLPDynamics(BicycleSlipDynamics):
     """Dynamic bicycle whose five non-kinematic derivatives come from the learned 9-64-64-5 surrogate
     (NeuralNetModel, include/mppi/dynamics/autorally/ar_nn_model.cuh:133-145).  The network is evaluated on the
-    tensor cores with BF16 (``precision="bf16"``) or FP8 E4M3 (``"fp8"``) weights and FP32 accumulation.  The
+    tensor cores with BF16 (``precision="bf16"``) or FP8 E4M3 (``"fp8"``) weights and FP32 accumulation, or in plain
+    FP32 on the CUDA cores (``"fp32"``, one thread per sample as the reference's FNNHelper).  The
     ``BicycleSlipDynamics`` parameters are kept for the analytic judge and the host twin."""
 
     model_id = A.MODEL_BICYCLE_SLIP_MLP
-    PRECISIONS = {"bf16": 0, "fp8": 1}
+    PRECISIONS = {"bf16": 0, "fp8": 1, "fp32": 2}
 
     def __init__(self, params=None, precision="bf16", **slip_kwargs):
         super().__init__(**slip_kwargs)
@@ -376,6 +377,20 @@ class BatchedMPPIController:
         p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(-1))
         prec = BicycleSlipMLPDynamics.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         A.call("mppi_set_mlp", self._h, _fptr(p), p.size, prec)
+
+    def setJudge(self, fraction=0.01):
+        """Re-roll the ceil(fraction * K) lowest-cost surrogate samples with the analytic model (0 disables)."""
+        A.call("mppi_set_judge", self._h, float(fraction))
+
+    def judgeStats(self):
+        """Per instance (mean(analytic - surrogate) cost, mean relative |analytic - surrogate|) over judged samples."""
+        out = np.empty(2 * self.num_instances, dtype=np.float32)
+        A.call("mppi_get_judge_stats", self._h, _fptr(out))
+        return out.reshape(-1, 2)
+
+    def useAnalyticDynamics(self, enable=True):
+        """Fallback of the surrogate model: roll out the analytic dynamics instead of the network."""
+        A.call("mppi_use_analytic_dynamics", self._h, int(bool(enable)))
 
     def injectNoise(self, noise):
         """Parity hook: use this standard-normal noise (all instances, samples layout) instead of Philox noise."""

@@ -381,6 +381,21 @@ mppi_status mppi_set_mlp(mppi_handle* h, const float* params, size_t num_params,
   HANDLE_OK(h);
   return h->engine->set_mlp(params, num_params, precision);
 }
+mppi_status mppi_set_judge(mppi_handle* h, float fraction)
+{
+  HANDLE_OK(h);
+  return h->engine->set_judge(fraction);
+}
+mppi_status mppi_get_judge_stats(mppi_handle* h, float* out)
+{
+  HANDLE_OK(h);
+  return h->engine->get_judge_stats(out);
+}
+mppi_status mppi_use_analytic_dynamics(mppi_handle* h, int enable)
+{
+  HANDLE_OK(h);
+  return h->engine->use_analytic(enable);
+}
 mppi_status mppi_inject_noise(mppi_handle* h, const float* noise, size_t count)
 {
   HANDLE_OK(h);

@@ -77,6 +77,9 @@ public:
   virtual mppi_status enqueue_device_solves(int stride, int count) = 0;
   virtual mppi_status time_kernels(int stride, int reps, float* ms3) = 0;
   virtual mppi_status set_mlp(const float* params, size_t n, int precision) = 0;
+  virtual mppi_status set_judge(float fraction) = 0;
+  virtual mppi_status get_judge_stats(float* out) = 0;
+  virtual mppi_status use_analytic(int enable) = 0;
 };
 
 // Factories, one per model translation unit.
@@ -190,7 +193,8 @@ public:
       sampler = 0;
       for (int k = 0; k < 5; ++k) sampler += class_begin_[k + 1] > class_begin_[k] ? 1 : 0;
     }
-    return (sampler + 2) * cp_.num_iters;
+    const int judge = (Model::kMlp && !use_analytic_ && judge_total_ > 0) ? 3 : 0;
+    return (sampler + 2 + judge) * cp_.num_iters;
   }
 
   // ------------------------------------------------------------------------------------------------ computeControl
@@ -199,7 +203,7 @@ public:
     MG_CHECK(x0 != nullptr, "x0 must not be NULL");
     MG_CHECK(stride >= 0, "optimization_stride must be >= 0");
     MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
-    MG_CHECK(!Model::kMlp || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
+    MG_CHECK(!Model::kMlp || use_analytic_ || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
     for (int i = 0; i < I_ * S; ++i)
       if (!std::isfinite(x0[i]))
       {
@@ -459,12 +463,46 @@ public:
       return MPPI_EUNSUPPORTED;
     }
     MG_CHECK(params && n == (size_t)MPPI_MLP_PARAMS, "the MLP parameter vector holds %d floats", MPPI_MLP_PARAMS);
-    MG_CHECK(precision == 0, "MLP precision %d is not built (0 = bf16)", precision);
+    MG_CHECK(precision >= 0 && precision <= 2, "MLP precision must be 0 (bf16), 1 (fp8 e4m3) or 2 (fp32)");
     for (size_t i = 0; i < n; ++i) MG_CHECK(std::isfinite(params[i]), "MLP parameter %zu is not finite", i);
     for (int i = 0; i < kMlpIn; ++i) MG_CHECK(params[kMlpInStd + i] > 0.0f, "MLP input scale %d must be positive", i);
-    mlp_host_.assign(params, params + n);
-    MG_TRY(mlp_d_.alloc(n));
-    MG_CUDA(cudaMemcpy(mlp_d_.p, params, sizeof(float) * n, cudaMemcpyHostToDevice));
+    std::vector<float> dev(kMlpDevParams);
+    mlp_host_.resize(kMlpNumParams);
+    mlp_prepare(params, precision, dev.data(), mlp_host_.data());
+    mlp_precision_ = precision;
+    MG_TRY(mlp_d_.alloc(kMlpDevParams));
+    MG_CUDA(cudaMemcpy(mlp_d_.p, dev.data(), sizeof(float) * kMlpDevParams, cudaMemcpyHostToDevice));
+    invalidate_graphs();
+    return MPPI_OK;
+  }
+
+  mppi_status set_judge(float fraction) override
+  {
+    MG_CHECK(Model::kMlp, "the analytic judge applies to the surrogate model only");
+    MG_CHECK(std::isfinite(fraction) && fraction >= 0.0f && fraction <= 1.0f, "judge fraction must be in [0, 1]");
+    judge_frac_ = fraction;
+    MG_TRY(build_judge_lists());
+    invalidate_graphs();
+    return MPPI_OK;
+  }
+
+  mppi_status get_judge_stats(float* out) override
+  {
+    MG_CHECK(out, "out must not be NULL");
+    if (!Model::kMlp || judge_total_ == 0 || use_analytic_)
+    {
+      std::fill(out, out + 2 * I_, 0.0f);
+      return MPPI_OK;
+    }
+    MG_CUDA(cudaStreamSynchronize(stream_));
+    MG_CUDA(cudaMemcpy(out, judge_stats_d_.p, sizeof(float) * 2 * I_, cudaMemcpyDeviceToHost));
+    return MPPI_OK;
+  }
+
+  mppi_status use_analytic(int enable) override
+  {
+    MG_CHECK(Model::kMlp, "only the surrogate model has an analytic fallback");
+    use_analytic_ = enable != 0;
     invalidate_graphs();
     return MPPI_OK;
   }
@@ -473,7 +511,7 @@ public:
   {
     MG_CHECK(stride >= 0 && count >= 0, "stride and count must be >= 0");
     MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
-    MG_CHECK(!Model::kMlp || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
+    MG_CHECK(!Model::kMlp || use_analytic_ || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
     auto it = device_graphs_.find(stride);
     cudaGraphExec_t exec = nullptr;
     if (it == device_graphs_.end())
@@ -505,7 +543,7 @@ public:
   {
     MG_CHECK(ms3 && reps >= 1, "need an output array and reps >= 1");
     MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
-    MG_CHECK(!Model::kMlp || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
+    MG_CHECK(!Model::kMlp || use_analytic_ || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
     cudaEvent_t ev[4];
     for (auto& e : ev) MG_CUDA(cudaEventCreate(&e));
     float tot[3] = { 0, 0, 0 };
@@ -650,6 +688,7 @@ private:
     MG_TRY(status_h_.alloc(1));
     MG_TRY(build_work_lists());
     MG_TRY(build_colored_tables());
+    MG_TRY(build_judge_lists());
     MG_CUDA(cudaStreamSynchronize(stream_));
     return MPPI_OK;
   }
@@ -941,7 +980,23 @@ private:
     for (int c = 0; c < C; ++c)
       if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
     a.sh = make_sample_shared(sp_, cc_);
-    if constexpr (Model::kMlp) return launch_mlp_rollout(a, mlp_d_.p, num_sms_, stream_);
+    if constexpr (Model::kMlp)
+      if (!use_analytic_)
+      {
+        MG_TRY(launch_mlp_rollout(a, mlp_d_.p, mlp_precision_, num_sms_, stream_));
+        if (judge_total_ == 0) return MPPI_OK;
+        JudgeArgs j;
+        j.r = a;
+        j.num_instances = I_;
+        j.sel_off = judge_off_d_.p;
+        j.sel_inst = judge_inst_d_.p;
+        j.sel = judge_sel_d_.p;
+        j.judged_cost = judge_cost_d_.p;
+        j.unjudged_min = judge_min_d_.p;
+        j.stats = judge_stats_d_.p;
+        j.total = judge_total_;
+        return launch_judge(j, stream_);
+      }
     switch (ns_)
     {
       case 32: launch_rollout_ns<32>(a); break;
@@ -1083,7 +1138,7 @@ private:
         for (int c = 0; c < C; ++c)
           uc[c] = enforce_constraint(u[(size_t)t * C + c], cc_.lower[c], cc_.upper[c], cc_.deadband[c],
                                      cc_.zero_control[c]);
-        if constexpr (Model::kMlp)
+        if (Model::kMlp && !use_analytic_)
         {
           float xd[S];
           mlp_host_dynamics(mlp_host_.data(), x, uc, xd);
@@ -1160,8 +1215,41 @@ private:
   PinnedBuf<float> x0_h_, mean_h_, out_mean_h_, out_bn_h_;
   PinnedBuf<double> out_stats_h_;
   PinnedBuf<unsigned int> status_h_;
-  std::vector<float> mlp_host_;  // surrogate parameters (MLP models only)
+  std::vector<float> mlp_host_;  // surrogate parameters as the tensor cores see them (MLP models only)
   DevBuf<float> mlp_d_;
+  int mlp_precision_ = 0;      // 0 bf16 / 1 fp8 tensor cores, 2 fp32 CUDA cores
+  bool use_analytic_ = false;  // MLP models: roll out the analytic model instead
+  float judge_frac_ = 0.01f;   // MLP models: fraction of samples re-rolled by the analytic judge
+  int judge_total_ = 0;
+  DevBuf<int> judge_off_d_, judge_inst_d_, judge_sel_d_;
+  DevBuf<float> judge_cost_d_, judge_stats_d_;
+  DevBuf<unsigned int> judge_min_d_;
+
+  // Judged slots per instance: ceil(judge_frac_ * K_i), capped at K_i.
+  mppi_status build_judge_lists()
+  {
+    judge_total_ = 0;
+    if (!Model::kMlp || judge_frac_ <= 0.0f) return MPPI_OK;
+    std::vector<int> off(I_ + 1, 0), inst;
+    for (int i = 0; i < I_; ++i)
+    {
+      const int m = std::min(K_[i], (int)std::ceil((double)judge_frac_ * K_[i]));
+      off[i + 1] = off[i] + m;
+      inst.insert(inst.end(), m, i);
+    }
+    judge_total_ = off[I_];
+    MG_TRY(judge_off_d_.alloc(I_ + 1));
+    MG_TRY(judge_inst_d_.alloc(std::max(1, judge_total_)));
+    MG_TRY(judge_sel_d_.alloc(std::max(1, judge_total_)));
+    MG_TRY(judge_cost_d_.alloc(std::max(1, judge_total_)));
+    MG_TRY(judge_stats_d_.alloc(2 * I_));
+    MG_TRY(judge_min_d_.alloc(I_));
+    MG_CUDA(cudaMemcpy(judge_off_d_.p, off.data(), sizeof(int) * (I_ + 1), cudaMemcpyHostToDevice));
+    if (judge_total_)
+      MG_CUDA(cudaMemcpy(judge_inst_d_.p, inst.data(), sizeof(int) * judge_total_, cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemset(judge_stats_d_.p, 0, sizeof(float) * 2 * I_));
+    return MPPI_OK;
+  }
   bool use_bulk_ = false;  // every instance has T*C % 4 == 0: stage controls with the bulk-copy engine
 };
 

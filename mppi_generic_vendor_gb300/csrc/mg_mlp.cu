@@ -3,6 +3,7 @@
 // tile, FP32 accumulation in TMEM; see mg_mlp.cuh).
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "mg_common.cuh"
 #include "mg_mlp.cuh"
@@ -11,9 +12,11 @@ namespace mg
 {
 namespace
 {
-// Every CTA of the MLP kernels allocates MlpSmem::TMEM_COLS = 256 TMEM columns; requesting at least this much
-// shared memory keeps two CTAs per SM at most, so allocation never waits on another CTA's columns.
-constexpr size_t kMlpMinSmem = 100 * 1024;
+// Every CTA of the MLP kernels allocates MlpSmem::TMEM_COLS = 64 TMEM columns and holds MlpSmem::TOTAL bytes of
+// dynamic shared memory (+ alignment slack).  At most 6 such CTAs fit an SM's 228 KB of shared memory, 384 of its 512
+// columns, so an allocation never waits on another CTA's columns.
+constexpr size_t kMlpSmem = MlpSmem::TOTAL + 1024;
+constexpr int kMlpMaxCtasPerSm = 512 / MlpSmem::TMEM_COLS;
 
 __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, const float* X, float* Y, int B,
                                                           unsigned int* status)
@@ -59,10 +62,51 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, c
   if (warp == 0) tmem_dealloc(taddr, MlpSmem::TMEM_COLS);
 }
 
+// Plain FP32 surrogate evaluation on the CUDA cores, one thread per sample, as FNNHelper::forward evaluates it
+// (fnn_helper.cu:418-495): weights in shared memory (read as broadcasts), activations in registers.  Products and
+// sums are separate FP32 operations in FNNHelper's order, so the result differs from an FP32 host evaluation only by
+// the last-place rounding of tanhf.
+__device__ __forceinline__ void mlp_thread_forward(const float* P, const float* xin, float* y)
+{
+  float h1[kMlpHid];
+#pragma unroll
+  for (int j = 0; j < kMlpHid; ++j)
+  {
+    float z = P[kMlpB1 + j];
+#pragma unroll
+    for (int i = 0; i < kMlpIn; ++i) z = z + P[kMlpW1 + j * kMlpIn + i] * xin[i];
+    h1[j] = tanhf(z);
+  }
+  // hidden unit j of layer 2 is folded into the outputs as soon as it is known: each output still sums its 64
+  // terms in index order, starting from its bias
+#pragma unroll
+  for (int o = 0; o < kMlpOut; ++o) y[o] = P[kMlpB3 + o];
+#pragma unroll 2
+  for (int j = 0; j < kMlpHid; ++j)
+  {
+    float z = P[kMlpB2 + j];
+    const float4* w = reinterpret_cast<const float4*>(P + kMlpW2 + j * kMlpHid);
+#pragma unroll
+    for (int i = 0; i < kMlpHid / 4; ++i)
+    {
+      const float4 v = w[i];
+      z = z + v.x * h1[4 * i];
+      z = z + v.y * h1[4 * i + 1];
+      z = z + v.z * h1[4 * i + 2];
+      z = z + v.w * h1[4 * i + 3];
+    }
+    const float h2 = tanhf(z);
+#pragma unroll
+    for (int o = 0; o < kMlpOut; ++o) y[o] = y[o] + P[kMlpW3 + o * kMlpHid + j] * h2;
+  }
+}
+
 // Surrogate rollout: BicycleSlipModel with the (yaw, vx, vy, yaw_rate, steer) derivatives from the MLP and the
-// x / y rows analytic (NeuralNetModel::computeKinematics, ar_nn_model.cu:119-124).  One persistent CTA per SM slot
-// walks 128-sample tiles; the Euler step, the costmap cost and the likelihood term follow rolloutKernel
-// (mppi_common.cu:105-152) exactly as the analytic rollout does.
+// x / y rows analytic (NeuralNetModel::computeKinematics, ar_nn_model.cu:119-124).  Persistent CTAs walk 128-sample
+// tiles; the Euler step, the costmap cost and the likelihood term follow rolloutKernel (mppi_common.cu:105-152)
+// exactly as the analytic rollout does.  kTensor: the network runs on the tensor cores (mlp_tile_forward, BF16 or
+// FP8 weights); otherwise in plain FP32 on the CUDA cores (mlp_thread_forward).
+template <bool kTensor>
 __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant__ RolloutArgs<BicycleSlipMLPModel> a,
                                                           const float* mlp)
 {
@@ -74,23 +118,32 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
   __shared__ int s_tile;
   __shared__ unsigned int s_min;
   const int tid = threadIdx.x, warp = tid >> 5;
-  if (warp == 0)
+  float* pf = reinterpret_cast<float*>(sm);  // FP32 path: the device parameter vector
+  if constexpr (kTensor)
   {
-    tmem_alloc(&s_tmem, MlpSmem::TMEM_COLS);
-    tmem_relinquish();
+    if (warp == 0)
+    {
+      tmem_alloc(&s_tmem, MlpSmem::TMEM_COLS);
+      tmem_relinquish();
+    }
+    if (tid == 0)
+    {
+      mbar_init(&mbar, 1);
+      fence_mbarrier_init();
+    }
+    mlp_load_weights(sm, mlp);
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
   }
-  if (tid == 0)
+  else
   {
-    mbar_init(&mbar, 1);
-    fence_mbarrier_init();
+    for (int e = tid; e < kMlpDevParams; e += blockDim.x) pf[e] = mlp[e];
+    __syncthreads();
   }
-  mlp_load_weights(sm, mlp);
-  tc_fence_before_sync();
-  __syncthreads();
-  tc_fence_after_sync();
-  const uint32_t taddr = s_tmem;
+  const uint32_t taddr = kTensor ? s_tmem : 0u;
   uint32_t phase = 0;
-  const float* nrm = reinterpret_cast<const float*>(sm + MlpSmem::NORM);
+  const float* nrm = kTensor ? reinterpret_cast<const float*>(sm + MlpSmem::NORM) : pf + kMlpInMean;
   bool ok = true;
   for (;;)
   {
@@ -122,8 +175,15 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
       for (int i = 0; i < S; ++i) xin[i] = (x[i] - nrm[i]) / nrm[9 + i];
       xin[7] = (u[0] - nrm[7]) / nrm[16];
       xin[8] = (u[1] - nrm[8]) / nrm[17];
-      ok = mlp_tile_forward(sm, taddr, &mbar, phase, xin, y);
-      if (!ok) break;
+      if constexpr (kTensor)
+      {
+        ok = mlp_tile_forward(sm, taddr, &mbar, phase, xin, y);
+        if (!ok) break;
+      }
+      else
+      {
+        mlp_thread_forward(pf, xin, y);
+      }
       float xd[S];
       float sy, cy;
       sincos_f(x[2], &sy, &cy);
@@ -174,9 +234,12 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
     __syncthreads();
     if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
   }
-  tc_fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tmem_dealloc(taddr, MlpSmem::TMEM_COLS);
+  if constexpr (kTensor)
+  {
+    tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(taddr, MlpSmem::TMEM_COLS);
+  }
   if (tid == 0)
   {
     __threadfence();
@@ -189,35 +252,311 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
     }
   }
 }
+
+// Exclusive prefix count of `flag` over the CTA in thread order (ballot + popc per warp, one warp scans the warp
+// totals); *total receives the CTA's count.  s_warp holds 64 ints.  Every thread of the CTA must call it.
+__device__ __forceinline__ int block_excl_count(bool flag, int* s_warp, int* total)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned int b = __ballot_sync(0xffffffffu, flag);
+  const int in_warp = __popc(b & ((1u << lane) - 1u));
+  if (lane == 0) s_warp[warp] = __popc(b);
+  __syncthreads();
+  if (warp == 0)
+  {
+    int v = lane < nw ? s_warp[lane] : 0;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1)
+    {
+      const int n = __shfl_up_sync(0xffffffffu, v, off);
+      if (lane >= off) v += n;
+    }
+    s_warp[32 + lane] = v;  // inclusive
+  }
+  __syncthreads();
+  const int before = warp ? s_warp[32 + warp - 1] : 0;
+  *total = s_warp[32 + nw - 1];
+  __syncthreads();
+  return before + in_warp;
+}
+
+__device__ __forceinline__ unsigned int block_min_u32(unsigned int v, unsigned int* s_min)
+{
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, off));
+  if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned int m = kOrderedPosInf;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = min(m, s_min[w]);
+  return m;
+}
+
+// One CTA per instance: radix selection (4 passes of 8 bits over the ordered-int costs) of the M-th smallest key,
+// then an index-ordered compaction of the keys below it plus the first ties, so the judged set and its order are
+// deterministic.  Also records the minimum over the samples that are not judged.
+__global__ void __launch_bounds__(1024) judge_select_kernel(const __grid_constant__ JudgeArgs a)
+{
+  __shared__ unsigned int hist[256];
+  __shared__ int s_warp[64];
+  __shared__ unsigned int s_min[32];
+  __shared__ unsigned int s_bin, s_need;
+  const int i = blockIdx.x, tid = threadIdx.x;
+  const int base = a.sel_off[i], M = a.sel_off[i + 1] - base;
+  const InstDesc d = a.r.inst[i];
+  const float* c = a.r.costs + d.k_off;
+  if (M <= 0)
+  {
+    if (tid == 0) a.unjudged_min[i] = a.r.baseline_bits[i];
+    return;
+  }
+  unsigned int prefix = 0u, mask = 0u, need = (unsigned int)M;
+  for (int shift = 24; shift >= 0; shift -= 8)
+  {
+    for (int b = tid; b < 256; b += blockDim.x) hist[b] = 0u;
+    __syncthreads();
+    for (int k = tid; k < d.K; k += blockDim.x)
+    {
+      const unsigned int key = float_to_ordered(c[k]);
+      if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    if (tid == 0)
+    {
+      unsigned int cum = 0u, b = 0u;
+      for (; b < 255u; ++b)
+      {
+        if (cum + hist[b] >= need) break;
+        cum += hist[b];
+      }
+      s_bin = b;
+      s_need = need - cum;
+    }
+    __syncthreads();
+    prefix |= s_bin << shift;
+    mask |= 255u << shift;
+    need = s_need;
+    __syncthreads();
+  }
+  const unsigned int thr = prefix;
+  const int need_eq = (int)need;
+  int n_eq = 0, n_sel = 0;
+  unsigned int my_min = kOrderedPosInf;
+  for (int k0 = 0; k0 < d.K; k0 += blockDim.x)
+  {
+    const int k = k0 + tid;
+    const bool valid = k < d.K;
+    const unsigned int key = valid ? float_to_ordered(c[k]) : 0u;
+    const bool eq = valid && key == thr;
+    int tot;
+    const int r_eq = n_eq + block_excl_count(eq, s_warp, &tot);
+    n_eq += tot;
+    const bool sel = valid && (key < thr || (eq && r_eq < need_eq));
+    const int pos = n_sel + block_excl_count(sel, s_warp, &tot);
+    n_sel += tot;
+    if (sel && pos < M) a.sel[base + pos] = k;
+    if (valid && !sel) my_min = min(my_min, key);
+  }
+  const unsigned int m = block_min_u32(my_min, s_min);
+  if (tid == 0) a.unjudged_min[i] = m;
+}
+
+// One thread per judged sample: the analytic FP32 rollout of that sample, step for step as the analytic rollout
+// kernel (Euler step, running cost on the stepped state, likelihood-ratio term, terminal cost).
+__global__ void __launch_bounds__(128) judge_rollout_kernel(const __grid_constant__ JudgeArgs a)
+{
+  using Model = BicycleSlipModel;
+  constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.total) return;
+  const int i = a.sel_inst[j], k = a.sel[j];
+  const InstDesc d = a.r.inst[i];
+  const typename Model::DynParams& dp = a.r.dyn[i];
+  const typename Model::CostParams& cp = a.r.cost[i];
+  const float* urow = a.r.samples + d.u_off + (long long)k * d.T * C;
+  float x[S];
+#pragma unroll
+  for (int s = 0; s < S; ++s) x[s] = a.r.x0[d.x_off + s];
+  float running = 0.0f;
+  const bool zero_mean = (float)k >= (1.0f - a.r.sh.pure_pct) * (float)d.K;
+  for (int t = 0; t < d.T; ++t)
+  {
+    const float2 uv = __ldg(reinterpret_cast<const float2*>(urow + t * C));
+    const float u[2] = { uv.x, uv.y };
+    float xn[S];
+    euler_step<Model>(dp, x, u, xn, a.r.dt);
+    float step_cost = Model::computeStateCost(cp, a.r.aux, xn, t) + Model::computeControlCost(cp, u, t);
+    if (a.r.use_likelihood)
+    {
+      float lc = 0.0f;
+#pragma unroll
+      for (int c = 0; c < C; ++c)
+      {
+        const float m = zero_mean ? 0.0f : a.r.mean[d.t_off + t * C + c];
+        const float sd = a.r.sh.std_dev[c];
+        lc += a.r.sh.control_cost_coeff[c] * m * (m - 2.0f * u[c]) / (sd * sd);
+      }
+      step_cost += 0.5f * a.r.lambda * (1.0f - a.r.alpha) * lc;
+    }
+    running += step_cost;
+#pragma unroll
+    for (int s = 0; s < S; ++s) x[s] = xn[s];
+  }
+  const float tf = (float)d.T;
+  a.judged_cost[j] = running / tf + Model::terminalCost(cp, a.r.aux, x) / tf;
+}
+
+// One CTA per instance: mean judge correction (fixed-order FP64 reduction), corrected costs written back, baseline
+// recomputed over judged and unjudged samples.
+__global__ void __launch_bounds__(256) judge_finalize_kernel(const __grid_constant__ JudgeArgs a)
+{
+  __shared__ double s_red[2][8];
+  __shared__ unsigned int s_min[8];
+  const int i = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int base = a.sel_off[i], M = a.sel_off[i + 1] - base;
+  if (M <= 0) return;
+  float* c = a.r.costs + a.r.inst[i].k_off;
+  double sd = 0.0, sr = 0.0;
+  for (int j = tid; j < M; j += blockDim.x)
+  {
+    const double nw = a.judged_cost[base + j], old = c[a.sel[base + j]];
+    sd += nw - old;
+    sr += fabs(nw - old) / fmax(fabs(nw), 1e-30);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+  {
+    sd += __shfl_xor_sync(0xffffffffu, sd, off);
+    sr += __shfl_xor_sync(0xffffffffu, sr, off);
+  }
+  if (lane == 0)
+  {
+    s_red[0][warp] = sd;
+    s_red[1][warp] = sr;
+  }
+  __syncthreads();
+  double tsd = 0.0, tsr = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+  {
+    tsd += s_red[0][w];
+    tsr += s_red[1][w];
+  }
+  const double shift = tsd / M;
+  unsigned int mn = kOrderedPosInf;
+  for (int j = tid; j < M; j += blockDim.x)
+  {
+    const float v = (float)((double)a.judged_cost[base + j] - shift);
+    c[a.sel[base + j]] = v;
+    mn = min(mn, float_to_ordered(v));
+  }
+  const unsigned int m = block_min_u32(mn, s_min);
+  if (tid == 0)
+  {
+    a.r.baseline_bits[i] = min(m, a.unjudged_min[i]);
+    a.stats[2 * i] = (float)shift;
+    a.stats[2 * i + 1] = (float)(tsr / M);
+  }
+}
 }  // namespace
 
-mppi_status launch_mlp_rollout(const RolloutArgs<BicycleSlipMLPModel>& a, const float* mlp_d, int num_sms,
-                               cudaStream_t s)
+mppi_status launch_mlp_rollout(const RolloutArgs<BicycleSlipMLPModel>& a, const float* mlp_d, int precision,
+                               int num_sms, cudaStream_t s)
 {
-  const size_t smem = kMlpMinSmem;
-  MG_CUDA(cudaFuncSetAttribute(rollout_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int grid = std::max(1, std::min(a.num_tiles, 2 * num_sms));
-  rollout_mlp_kernel<<<grid, 128, smem, s>>>(a, mlp_d);
+  const bool tensor = precision != 2;
+  auto kern = tensor ? rollout_mlp_kernel<true> : rollout_mlp_kernel<false>;
+  const size_t smem = tensor ? kMlpSmem : sizeof(float) * kMlpDevParams;
+  MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 1;
+  MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem));
+  per_sm = std::max(1, tensor ? std::min(per_sm, kMlpMaxCtasPerSm) : per_sm);
+  const int grid = std::max(1, std::min(a.num_tiles, per_sm * num_sms));
+  kern<<<grid, 128, smem, s>>>(a, mlp_d);
   MG_CUDA(cudaGetLastError());
   return MPPI_OK;
 }
 
+
+mppi_status launch_judge(const JudgeArgs& a, cudaStream_t s)
+{
+  if (a.total <= 0) return MPPI_OK;
+  judge_select_kernel<<<a.num_instances, 1024, 0, s>>>(a);
+  MG_CUDA(cudaGetLastError());
+  judge_rollout_kernel<<<(a.total + 127) / 128, 128, 0, s>>>(a);
+  MG_CUDA(cudaGetLastError());
+  judge_finalize_kernel<<<a.num_instances, 256, 0, s>>>(a);
+  MG_CUDA(cudaGetLastError());
+  return MPPI_OK;
+}
+
+float e4m3_round(float x)
+{
+  const float a = std::fabs(x);
+  if (a == 0.0f) return x;
+  if (a >= 448.0f) return std::copysign(448.0f, x);
+  int e = 0;
+  std::frexp(a, &e);               // a in [2^(e-1), 2^e)
+  const int E = std::max(e - 1, -6);  // below 2^-6 the spacing stays that of the subnormals, 2^-9
+  const float quantum = std::ldexp(1.0f, E - 3);
+  const float q = std::min(std::nearbyint(a / quantum) * quantum, 448.0f);
+  return std::copysign(q, x);
+}
+
+void mlp_prepare(const float* params, int precision, float* dev_out, float* effective_out)
+{
+  std::copy(params, params + kMlpNumParams, dev_out);
+  std::copy(params, params + kMlpNumParams, effective_out);
+  const int w_off[3] = { kMlpW1, kMlpW2, kMlpW3 };
+  const int w_len[3] = { kMlpHid * kMlpIn, kMlpHid * kMlpHid, kMlpOut * kMlpHid };
+  for (int l = 0; l < 3; ++l)
+  {
+    float scale = 1.0f;
+    if (precision == 1)
+    {
+      float amax = 0.0f;
+      for (int e = 0; e < w_len[l]; ++e) amax = std::max(amax, std::fabs(params[w_off[l] + e]));
+      if (amax > 0.0f) scale = amax / 448.0f;
+      for (int e = 0; e < w_len[l]; ++e)
+      {
+        const float q = e4m3_round(params[w_off[l] + e] / scale);
+        dev_out[w_off[l] + e] = q;
+        effective_out[w_off[l] + e] = q * scale;
+      }
+    }
+    dev_out[kMlpScale + l] = scale;
+  }
+}
 }  // namespace mg
 
 using namespace mg;
 
 extern "C" {
 
-mppi_status mppi_kernel_mlp_forward(const float* params, const float* X_d, float* Y_d, int batch, void* stream)
+mppi_status mppi_mlp_quantize(const float* params, int precision, float* out, float* layer_scales)
+{
+  clear_error();
+  MG_CHECK(params && out, "pointers must not be NULL");
+  MG_CHECK(precision >= 0 && precision <= 2, "precision must be 0 (bf16), 1 (fp8 e4m3) or 2 (fp32)");
+  for (int i = 0; i < MPPI_MLP_PARAMS; ++i) MG_CHECK(std::isfinite(params[i]), "parameter %d is not finite", i);
+  std::vector<float> dev(kMlpDevParams), eff(kMlpNumParams);
+  mlp_prepare(params, precision, dev.data(), eff.data());
+  std::copy(dev.begin(), dev.begin() + kMlpNumParams, out);
+  if (layer_scales) std::copy(dev.begin() + kMlpScale, dev.end(), layer_scales);
+  return MPPI_OK;
+}
+
+mppi_status mppi_kernel_mlp_forward(const float* params, int precision, const float* X_d, float* Y_d, int batch,
+                                    void* stream)
 {
   clear_error();
   MG_CHECK(params && X_d && Y_d, "pointers must not be NULL");
   MG_CHECK(batch >= 1, "batch must be >= 1");
+  MG_CHECK(precision == 0 || precision == 1, "the tensor-core forward takes precision 0 (bf16) or 1 (fp8 e4m3)");
   for (int i = 0; i < MPPI_MLP_PARAMS; ++i) MG_CHECK(std::isfinite(params[i]), "parameter %d is not finite", i);
   for (int i = 0; i < kMlpIn; ++i) MG_CHECK(params[kMlpInStd + i] > 0.0f, "input scale %d must be positive", i);
+  std::vector<float> dev(kMlpDevParams), eff(kMlpNumParams);
+  mlp_prepare(params, precision, dev.data(), eff.data());
   cudaStream_t s = (cudaStream_t)stream;
   void* buf = nullptr;
-  const size_t bytes = sizeof(float) * MPPI_MLP_PARAMS + 256;
+  const size_t bytes = sizeof(float) * kMlpDevParams + 256;
   cudaError_t e = cudaMallocAsync(&buf, bytes, s);
   if (e != cudaSuccess)
   {
@@ -225,18 +564,19 @@ mppi_status mppi_kernel_mlp_forward(const float* params, const float* X_d, float
     return MPPI_ENOMEM;
   }
   float* p_d = (float*)buf;
-  unsigned int* status = (unsigned int*)((char*)buf + sizeof(float) * MPPI_MLP_PARAMS + 128);
+  unsigned int* status = (unsigned int*)((char*)buf + sizeof(float) * kMlpDevParams + 128);
   mppi_status st = MPPI_OK;
   do
   {
-    if ((e = cudaMemcpyAsync(p_d, params, sizeof(float) * MPPI_MLP_PARAMS, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    if ((e = cudaMemcpyAsync(p_d, dev.data(), sizeof(float) * kMlpDevParams, cudaMemcpyHostToDevice, s)) !=
+        cudaSuccess)
       break;
     if ((e = cudaMemsetAsync(status, 0, sizeof(unsigned int), s)) != cudaSuccess) break;
     if ((e = cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kMlpMinSmem)) != cudaSuccess)
+                                  (int)kMlpSmem)) != cudaSuccess)
       break;
     const int tiles = (batch + 127) / 128;
-    mlp_forward_kernel<<<std::min(tiles, 1024), 128, kMlpMinSmem, s>>>(p_d, X_d, Y_d, batch, status);
+    mlp_forward_kernel<<<std::min(tiles, 8192), 128, kMlpSmem, s>>>(p_d, X_d, Y_d, batch, status);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     unsigned int h = 0;
     if ((e = cudaMemcpyAsync(&h, status, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;

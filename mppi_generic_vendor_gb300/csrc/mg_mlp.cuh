@@ -21,6 +21,9 @@ constexpr int kMlpW1 = 0, kMlpB1 = kMlpW1 + kMlpHid * kMlpIn, kMlpW2 = kMlpB1 + 
               kMlpInMean = kMlpB3 + kMlpOut, kMlpInStd = kMlpInMean + kMlpIn, kMlpOutMean = kMlpInStd + kMlpIn,
               kMlpOutStd = kMlpOutMean + kMlpOut, kMlpNumParams = kMlpOutStd + kMlpOut;
 static_assert(kMlpNumParams == MPPI_MLP_PARAMS, "MLP parameter layout");
+// Device copy: the parameter vector followed by one scale per layer.  BF16 weights carry scale 1; FP8 weights hold
+// E4M3 values q with W = q * scale, the scale applied to the FP32 accumulator in the epilogue.
+constexpr int kMlpScale = kMlpNumParams, kMlpDevParams = kMlpScale + 3;
 
 // Shared-memory map of one MLP tile (bytes from a 1024-byte aligned base).
 struct MlpSmem
@@ -31,9 +34,11 @@ struct MlpSmem
   static constexpr int A1 = 12288;      // 128 x 16 bf16
   static constexpr int A2 = 16384;      // 128 x 64 bf16 (hidden 1, then hidden 2)
   static constexpr int BIAS = 32768;    // fp32 b1[64] b2[64] b3[16]
-  static constexpr int NORM = 33792;    // fp32 in_mean[9] in_std[9] out_mean[5] out_std[5] (+ pad)
+  static constexpr int NORM = 33792;    // fp32 in_mean[9] in_std[9] out_mean[5] out_std[5] layer_scale[3]
   static constexpr int TOTAL = 34048;
-  static constexpr uint32_t TMEM_COLS = 256;  // D1 at 0, D2 at 64, D3 at 128
+  // One 64-column accumulator serves all three layers: each layer's result is read back into shared memory before
+  // the next layer's MMA is issued.
+  static constexpr uint32_t TMEM_COLS = 64;
 };
 
 // Byte offset of element (row, k) in the K-major core-matrix layout of a tile whose K extent is KD.
@@ -48,7 +53,8 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
   return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// Load the FP32 parameter vector (FNNHelper row-major layout) into BF16 operand tiles and FP32 biases.
+// Load the device parameter vector (FNNHelper row-major layout + layer scales) into BF16 operand tiles and FP32
+// biases.  E4M3 values are exact in BF16, so FP8 weights reach the tensor cores unrounded.
 __device__ __forceinline__ void mlp_load_weights(unsigned char* sm, const float* params)
 {
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -74,7 +80,7 @@ __device__ __forceinline__ void mlp_load_weights(unsigned char* sm, const float*
   for (int e = tid; e < 144; e += nt)
     bias[e] = e < 64 ? params[kMlpB1 + e] : e < 128 ? params[kMlpB2 + e - 64] : (e - 128 < kMlpOut ? params[kMlpB3 + e - 128] : 0.0f);
   float* nrm = reinterpret_cast<float*>(sm + MlpSmem::NORM);
-  for (int e = tid; e < 28; e += nt) nrm[e] = params[kMlpInMean + e];
+  for (int e = tid; e < 31; e += nt) nrm[e] = params[kMlpInMean + e];  // normalisation + layer scales
 }
 
 // One forward pass of the tile.  Thread i provides its normalised input row xin[9] and receives yout[5]
@@ -86,6 +92,8 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
   const uint32_t sbase = smem_u32(sm);
   const float* bias = reinterpret_cast<const float*>(sm + MlpSmem::BIAS);
+  const float* lscale = reinterpret_cast<const float*>(sm + MlpSmem::NORM) + 28;
+  const float s1 = lscale[0], s2 = lscale[1], s3 = lscale[2];
   constexpr uint32_t kId64 = umma_idesc_bf16_f32(128, 64);
   constexpr uint32_t kId16 = umma_idesc_bf16_f32(128, 16);
 
@@ -126,10 +134,10 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
       uint4 c;
       const float* b = bias + 16 * q + 8 * h;
       const float* x = v + 8 * h;
-      c.x = pack_bf16(tanh_fast(x[0] + b[0]), tanh_fast(x[1] + b[1]));
-      c.y = pack_bf16(tanh_fast(x[2] + b[2]), tanh_fast(x[3] + b[3]));
-      c.z = pack_bf16(tanh_fast(x[4] + b[4]), tanh_fast(x[5] + b[5]));
-      c.w = pack_bf16(tanh_fast(x[6] + b[6]), tanh_fast(x[7] + b[7]));
+      c.x = pack_bf16(tanh_fast(fmaf(x[0], s1, b[0])), tanh_fast(fmaf(x[1], s1, b[1])));
+      c.y = pack_bf16(tanh_fast(fmaf(x[2], s1, b[2])), tanh_fast(fmaf(x[3], s1, b[3])));
+      c.z = pack_bf16(tanh_fast(fmaf(x[4], s1, b[4])), tanh_fast(fmaf(x[5], s1, b[5])));
+      c.w = pack_bf16(tanh_fast(fmaf(x[6], s1, b[6])), tanh_fast(fmaf(x[7], s1, b[7])));
       *reinterpret_cast<uint4*>(sm + MlpSmem::A2 + core_off(m, 16 * q + 8 * h, 64)) = c;
     }
   }
@@ -142,7 +150,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
     tc_fence_after_sync();
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-      umma_bf16(taddr + 64, umma_smem_desc(sbase + MlpSmem::A2 + 256 * k, 128, 1024),
+      umma_bf16(taddr, umma_smem_desc(sbase + MlpSmem::A2 + 256 * k, 128, 1024),
                 umma_smem_desc(sbase + MlpSmem::W2 + 256 * k, 128, 1024), kId64, k > 0 ? 1u : 0u);
     umma_commit(mbar);
   }
@@ -153,7 +161,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   for (int q = 0; q < 4; ++q)
   {
     float v[16];
-    tmem_ld16(taddr + lane_base + 64 + 16 * q, v);
+    tmem_ld16(taddr + lane_base + 16 * q, v);
     tmem_ld_wait();
 #pragma unroll
     for (int h = 0; h < 2; ++h)
@@ -161,10 +169,10 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
       uint4 c;
       const float* b = bias + 64 + 16 * q + 8 * h;
       const float* x = v + 8 * h;
-      c.x = pack_bf16(tanh_fast(x[0] + b[0]), tanh_fast(x[1] + b[1]));
-      c.y = pack_bf16(tanh_fast(x[2] + b[2]), tanh_fast(x[3] + b[3]));
-      c.z = pack_bf16(tanh_fast(x[4] + b[4]), tanh_fast(x[5] + b[5]));
-      c.w = pack_bf16(tanh_fast(x[6] + b[6]), tanh_fast(x[7] + b[7]));
+      c.x = pack_bf16(tanh_fast(fmaf(x[0], s2, b[0])), tanh_fast(fmaf(x[1], s2, b[1])));
+      c.y = pack_bf16(tanh_fast(fmaf(x[2], s2, b[2])), tanh_fast(fmaf(x[3], s2, b[3])));
+      c.z = pack_bf16(tanh_fast(fmaf(x[4], s2, b[4])), tanh_fast(fmaf(x[5], s2, b[5])));
+      c.w = pack_bf16(tanh_fast(fmaf(x[6], s2, b[6])), tanh_fast(fmaf(x[7], s2, b[7])));
       *reinterpret_cast<uint4*>(sm + MlpSmem::A2 + core_off(m, 16 * q + 8 * h, 64)) = c;
     }
   }
@@ -177,7 +185,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
     tc_fence_after_sync();
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-      umma_bf16(taddr + 128, umma_smem_desc(sbase + MlpSmem::A2 + 256 * k, 128, 1024),
+      umma_bf16(taddr, umma_smem_desc(sbase + MlpSmem::A2 + 256 * k, 128, 1024),
                 umma_smem_desc(sbase + MlpSmem::W3 + 256 * k, 128, 1024), kId16, k > 0 ? 1u : 0u);
     umma_commit(mbar);
   }
@@ -186,18 +194,45 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   tc_fence_after_sync();
   {
     float v[16];
-    tmem_ld16(taddr + lane_base + 128, v);
+    tmem_ld16(taddr + lane_base, v);
     tmem_ld_wait();
 #pragma unroll
-    for (int j = 0; j < kMlpOut; ++j) yout[j] = v[j] + bias[128 + j];
+    for (int j = 0; j < kMlpOut; ++j) yout[j] = fmaf(v[j], s3, bias[128 + j]);
   }
   tc_fence_before_sync();
   return true;
 }
 
 // Rollout of the MLP bicycle model over every instance (defined in mg_mlp.cu).
-mppi_status launch_mlp_rollout(const RolloutArgs<BicycleSlipMLPModel>& a, const float* mlp_d, int num_sms,
-                               cudaStream_t s);
+// precision 0 / 1: tensor cores with BF16 / FP8 weights; 2: plain FP32 on the CUDA cores.
+mppi_status launch_mlp_rollout(const RolloutArgs<BicycleSlipMLPModel>& a, const float* mlp_d, int precision,
+                               int num_sms, cudaStream_t s);
+
+// Analytic judge of the surrogate rollout.  Per instance the M lowest surrogate costs (M = ceil(fraction * K), the
+// samples that carry the weight) are re-rolled with the analytic BicycleSlipModel in FP32.  Their costs become
+// analytic - mean(analytic - surrogate), which ranks them by the exact model while keeping one cost scale with the
+// samples that were not re-rolled (a per-instance shift leaves the MPPI weights unchanged), and the baseline is
+// recomputed over the corrected costs.
+struct JudgeArgs
+{
+  RolloutArgs<BicycleSlipMLPModel> r;  // instances, parameters, samples, costs and baseline of the rollout
+  int num_instances;
+  const int* sel_off;           // I + 1 entries: instance i owns judged slots sel_off[i] .. sel_off[i+1]-1
+  const int* sel_inst;          // per judged slot: its instance
+  int* sel;                     // per judged slot: sample index within the instance (ascending)
+  float* judged_cost;           // per judged slot: analytic cost
+  unsigned int* unjudged_min;   // per instance: ordered-int min over the samples that were not re-rolled
+  float* stats;                 // per instance: mean(analytic - surrogate), mean |analytic - surrogate| / |analytic|
+  int total;                    // judged slots over all instances
+};
+mppi_status launch_judge(const JudgeArgs& a, cudaStream_t s);
+
+// Device parameter vector (kMlpDevParams floats) for precision 0 (BF16 weights, scales 1), 1 (FP8 E4M3 weights
+// with one scale per layer, scale = max |W| / 448) or 2 (FP32, unchanged), and the FP32 parameters those weights
+// represent (q * scale), used by the host twin.
+void mlp_prepare(const float* params, int precision, float* dev_out, float* effective_out);
+// Round to the nearest E4M3 value (ties to even, saturating at +-448).
+float e4m3_round(float x);
 
 // Host twin of the surrogate dynamics in FP32 (exact tanh), used for the nominal state trajectory of a controller
 // (Controller::computeOutputTrajectoryHelper, controller.cuh:664-684).

@@ -7,6 +7,11 @@
   (centres U(-5, 5)^2, radii U(0.3, 1.0), cost 1000 inside).
 * ``bicycle``    — kinematic bicycle on a 512x512 costmap (0.1 m cells) built from 32 Gaussian bumps
   (amplitude U(0, 10), sigma U(0.5, 3) m), speed target 8 m/s, K=16384, T=100, sigma (1.0, 0.3), lambda 2.0.
+* ``slip_mlp``   — the 7-state dynamic bicycle through the learned 9-64-64-5 surrogate (trained on the GPU on 2^20
+  transitions of the analytic model), BF16 weights, K=16384, T=100, analytic judge on the top 1% of samples, the
+  costmap of ``bicycle``, sigma (0.5, 0.5), lambda 2.0.
+* ``batched_slip_mlp`` — 128 surrogate instances with K ~ U[2048, 16384] and T ~ U{50, 100, 200}, FP8 E4M3 weights
+  with one scale per layer, one shared costmap as in ``bicycle``.
 
 There is no public dataset behind these configurations; every input is drawn from a recorded seed.
 """
@@ -16,7 +21,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .controller import (BatchedMPPIController, BicycleDynamics, CartpoleDynamics, CartpoleSwingupCost,
+from .controller import (BatchedMPPIController, BicycleDynamics, BicycleSlipMLPDynamics, CartpoleDynamics,
+                         CartpoleSwingupCost,
                          ColoredNoiseDistribution, CostmapCost, DoubleIntegratorDynamics,
                          DoubleIntegratorObstacleCost, GaussianDistribution, VanillaMPPIController)
 
@@ -113,4 +119,61 @@ def bicycle(seed: int = 0, K: int = 16384, T: int = 100, stream: int = 0) -> Wor
                     dict(model="bicycle_costmap", K=K, T=T, map="512x512@0.1m, 32 bumps", lam=2.0, seed=seed))
 
 
-BUILDERS = {"cartpole": cartpole, "batched_di": batched_di, "bicycle": bicycle}
+def train_surrogate(seed: int = 7, num_transitions: int = 1 << 20, steps: int = 10000, batch: int = 8192,
+                    stream: int = 0) -> np.ndarray:
+    """Surrogate parameters trained on the GPU by the engine's own kernels (a second or so on one GB300)."""
+    from .surrogate import Surrogate
+
+    s = Surrogate(num_transitions=num_transitions, seed=seed, stream=stream)
+    try:
+        s.generate()
+        s.train(steps=steps, batch=batch, lr=3e-3, lr_final=1e-4)
+        return s.params()
+    finally:
+        s.close()
+
+
+def _slip_cost(cmap):
+    return CostmapCost(map_coeff=1.0, speed_target=8.0, speed_coeff=1.0, steer_coeff=0.5, terminal_coeff=2.0,
+                       costmap=cmap, resolution=0.1, origin=(0.0, 0.0))
+
+
+def _slip_x0(rng):
+    return np.array([rng.uniform(5, 45), rng.uniform(5, 45), rng.uniform(-np.pi, np.pi), rng.uniform(4, 8), 0.0, 0.0,
+                     0.0], dtype=np.float32)
+
+
+def slip_mlp(seed: int = 0, K: int = 16384, T: int = 100, precision: str = "bf16", params=None, judge: float = 0.01,
+             stream: int = 0) -> Workload:
+    rng = np.random.default_rng(seed + 3)
+    if params is None:
+        params = train_surrogate(stream=stream)
+    dyn = BicycleSlipMLPDynamics(params, precision=precision)
+    ctrl = VanillaMPPIController(dyn, _slip_cost(gaussian_bump_costmap(seed)), None,
+                                 GaussianDistribution(std_dev=(0.5, 0.5)), 0.02, 1, 2.0, 0.0, T, K, stream=stream,
+                                 seed=seed)
+    ctrl.setJudge(judge)
+    return Workload(f"slip_mlp_{precision}_K{K}_T{T}", ctrl, _slip_x0(rng), np.array([K]), np.array([T]), 7, 2, 1,
+                    dict(model="bicycle_slip_mlp", precision=precision, K=K, T=T, judge=judge,
+                         map="512x512@0.1m, 32 bumps", lam=2.0, seed=seed))
+
+
+def batched_slip_mlp(seed: int = 0, num_instances: int = 128, precision: str = "fp8", params=None,
+                     judge: float = 0.01, stream: int = 0) -> Workload:
+    rng = np.random.default_rng(seed + 5)
+    if params is None:
+        params = train_surrogate(stream=stream)
+    Ks = rng.integers(2048, 16385, size=num_instances).astype(np.int32)
+    Ts = rng.choice([50, 100, 200], size=num_instances).astype(np.int32)
+    x0 = np.concatenate([_slip_x0(rng) for _ in range(num_instances)])
+    dyn = BicycleSlipMLPDynamics(params, precision=precision)
+    ctrl = BatchedMPPIController(dyn, _slip_cost(gaussian_bump_costmap(seed)), GaussianDistribution(std_dev=(0.5, 0.5)),
+                                 Ks, Ts, dt=0.02, max_iter=1, lambda_=2.0, seed=seed, stream=stream)
+    ctrl.setJudge(judge)
+    return Workload(f"batched_slip_mlp_{num_instances}x_{precision}", ctrl, x0, Ks, Ts, 7, 2, 1,
+                    dict(model="bicycle_slip_mlp", precision=precision, instances=num_instances, sum_K=int(Ks.sum()),
+                         T="U{50,100,200}", judge=judge, map="512x512@0.1m, 32 bumps (shared)", lam=2.0, seed=seed))
+
+
+BUILDERS = {"cartpole": cartpole, "batched_di": batched_di, "bicycle": bicycle, "slip_mlp": slip_mlp,
+            "batched_slip_mlp": batched_slip_mlp}

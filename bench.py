@@ -43,7 +43,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched_di", choices=["batched_di", "cartpole", "bicycle",
-                                                                 "batched_di_gaussian"])
+                                                                 "batched_di_gaussian", "slip_mlp",
+                                                                 "batched_slip_mlp"])
+    ap.add_argument("--precision", default=None, choices=["bf16", "fp8", "fp32"],
+                    help="surrogate workloads: weight precision (default bf16 for slip_mlp, fp8 for batched_slip_mlp)")
     ap.add_argument("--instances", type=int, default=256, help="batched workloads: number of instances")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -57,12 +60,17 @@ def dist_env():
     return ws, rank, local
 
 
-def measured_peaks():
+def measured_peaks(kind="hbm"):
+    """(peak, provenance): HBM copy GB/s, or burst bf16 TFLOP/s for a tensor-core kernel."""
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        return (float(d["hbm_gbs"]) if kind == "hbm" else float(d["bf16_tflops"])), "measured"
+    return (6800.0 if kind == "hbm" else 1900.0), "fallback"
+
+
+# FLOPs of one surrogate evaluation (9 -> 64 -> 64 -> 5; multiply-adds counted as 2), per sample-step
+MLP_FLOPS = 2 * (9 * 64 + 64 * 64 + 64 * 5)
 
 
 class ClockSampler:
@@ -120,9 +128,14 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_workload(name, seed, stream, instances=256):
+def build_workload(name, seed, stream, instances=256, precision=None, params=None):
     from mppi_generic_vendor_gb300 import workloads as W
 
+    if name == "slip_mlp":
+        return W.slip_mlp(seed=seed, precision=precision or "bf16", params=params, stream=stream)
+    if name == "batched_slip_mlp":
+        return W.batched_slip_mlp(seed=seed, num_instances=instances if instances != 256 else 128,
+                                  precision=precision or "fp8", params=params, stream=stream)
     if name == "batched_di":
         return W.batched_di(seed=seed, num_instances=instances, colored=True, stream=stream)
     if name == "batched_di_gaussian":
@@ -142,6 +155,87 @@ def algorithmic_bytes(wl, colored: bool):
     update = 4 * n + 8 * k  # read the samples and costs, write the weights
     del spec
     return {"sampler": sampler, "rollout": rollout, "update": update}
+
+
+_SURROGATE = {}
+
+
+def surrogate_params():
+    """Surrogate weights for the surrogate workloads, trained once per process on the GPU by the engine's own kernels
+    (the CPU baseline of the reference arm, which has no GPU, falls back to a fixed seeded initialisation)."""
+    if "p" not in _SURROGATE:
+        try:
+            if _SURROGATE.get("cpu_only"):
+                raise RuntimeError("no GPU on this arm")
+            from mppi_generic_vendor_gb300 import workloads as W
+
+            _SURROGATE["p"] = W.train_surrogate()
+        except Exception:
+            rng = np.random.default_rng(7)
+            p = np.zeros(5153, np.float32)
+            p[:576] = rng.normal(0, 1 / 3, 576)
+            p[640:4736] = rng.normal(0, 1 / 8, 4096)
+            p[4800:5120] = rng.normal(0, 1 / 8, 320)
+            p[5134:5143] = [15.0, 15.0, 1.8, 4.0, 1.2, 0.9, 0.3, 0.6, 0.6]
+            p[5125:5134] = [25.6, 25.6, 0.0, 8.0, 0.0, 0.0, 0.0, 0.0, 0.0]
+            p[5148:5153] = 1.0
+            _SURROGATE["p"] = p
+    return _SURROGATE["p"]
+
+
+def surrogate_extras(args, wl, stream):
+    """Surrogate workloads: the plain GPU form (the same instances, analytic model in FP32, one controller per
+    instance solved one after another) timed on the same GPU, and the final-cost error of each instance's nominal
+    control sequence under the surrogate against the FP64 analytic rollout."""
+    import oracle
+    from mppi_generic_vendor_gb300 import BicycleSlipDynamics, GaussianDistribution, VanillaMPPIController
+    from mppi_generic_vendor_gb300 import _abi as A
+    from mppi_generic_vendor_gb300 import workloads as W
+
+    ctrl = wl.controller
+    n = ctrl.num_instances
+    x0 = wl.x0.reshape(n, 7)
+    cmap = W.gaussian_bump_costmap(0)
+    # plain GPU form
+    plain = [VanillaMPPIController(BicycleSlipDynamics(), W._slip_cost(cmap), None,
+                                   GaussianDistribution(std_dev=(0.5, 0.5)), 0.02, 1, 2.0, 0.0, int(wl.T[i]),
+                                   int(wl.K[i]), seed=i, stream=stream) for i in range(n)]
+    for c, x in zip(plain, x0):
+        c.computeControl(x, 1)
+    reps = max(2, min(5, args.steps))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        for c, x in zip(plain, x0):
+            c.computeControl(x, 1)
+    plain_s = (time.perf_counter() - t0) / reps
+    for c in plain:
+        c.close()
+    # final-cost error: sample 0 of an iteration is the nominal sequence (noise-free); judge off for this read-out
+    ctrl.setJudge(0.0)
+    ctrl.computeControl(wl.x0, 1)
+    costs = ctrl.sample_costs()
+    samples = ctrl.control_samples()
+    ctrl.setJudge(0.01)
+    errs = []
+    u_off = 0
+    sp = GaussianDistribution(std_dev=(0.5, 0.5)).to_c()
+    for i in range(n):
+        K, T = int(wl.K[i]), int(wl.T[i])
+        u0 = samples[u_off:u_off + T * 2].reshape(T, 2)
+        u_off += K * T * 2
+        if i >= 16:
+            continue
+        c64, _, _ = oracle.rollout(A.MODEL_BICYCLE_SLIP, BicycleSlipDynamics().getParams(), ctrl._cost_arr[i],
+                                   x0[i], u0, u0, sp, ctrl.constraints_, 2.0, 0.0, 1, T, 0.02,
+                                   costmap=(cmap, 0.1, (0.0, 0.0)), fp64=True, state_dim=7)
+        k0 = int(np.sum(wl.K[:i]))
+        errs.append(abs(float(costs[k0]) - float(c64[0])) / abs(float(c64[0])))
+    return {"plain_gpu": {"form": "analytic model, FP32, one controller per instance, solved in turn",
+                          "iters_per_s": 1.0 / plain_s,
+                          "sample_steps_per_s": wl.sample_steps_per_iter / plain_s},
+            "final_cost_error": {"vs": "FP64 analytic rollout of each instance's nominal control sequence",
+                                 "instances": len(errs), "median": float(np.median(errs)),
+                                 "max": float(np.max(errs))}}
 
 
 # ------------------------------------------------------------------------------------------------ CPU baseline
@@ -182,6 +276,38 @@ def cpu_baseline(name, seed, budget_s):
             i += 1
         inst_done = i
         sample = f"{inst_done} of 256 instances (sum K*T = {done_steps}), one iteration each"
+    elif name in ("slip_mlp", "batched_slip_mlp"):
+        # the surrogate model in FP32 on the host (the oracle's restatement of the GPU rollout), same shapes
+        params = surrogate_params()
+        oracle.set_mlp(params)
+        if name == "slip_mlp":
+            shapes = [(16384, 100)]
+        else:
+            r = np.random.default_rng(seed + 5)
+            shapes = list(zip(r.integers(2048, 16385, size=128).tolist(), r.choice([50, 100, 200], size=128).tolist()))
+        cmap = (W.gaussian_bump_costmap(seed), 0.1, (0.0, 0.0))
+        cp = A.default_controller_params()
+        cp.dt, cp.lambda_, cp.num_iters = 0.02, 2.0, 1
+        sp = A.default_sampling_params()
+        sp.std_dev[0] = sp.std_dev[1] = 0.5
+        cc = A.default_constraints()
+        for i in range(2):
+            cc.lower[i], cc.upper[i] = -1.0, 1.0
+        dyn = A.BicycleSlipParams(1500.0, 2500.0, 1.2, 1.3, 8e4, 4000.0, 50.0, 0.5, 0.1, 1.0)
+        cost = A.CostmapCostParams(1.0, 8.0, 1.0, 0.5, 2.0)
+        x0 = np.array([25.0, 25.0, 0.3, 6.0, 0.0, 0.0, 0.0], np.float32)
+        i = 0
+        while elapsed < budget_s and iters < 200:
+            K, T = shapes[i % len(shapes)]
+            eps = rng.standard_normal(K * T * 2).astype(np.float32)
+            t0 = time.perf_counter()
+            oracle.compute_control(A.MODEL_BICYCLE_SLIP_MLP, dyn, cost, cp, sp, cc, K, T, 2, 7, x0, eps,
+                                   np.zeros((T, 2), np.float32), costmap=cmap, threads=threads)
+            elapsed += time.perf_counter() - t0
+            done_steps += K * T
+            iters += 1
+            i += 1
+        sample = f"{iters} MPPI iterations of the FP32 surrogate model ({'K=16384, T=100' if name == 'slip_mlp' else 'the first instances of the 128'})"
     else:
         wl_k, wl_t = (2048, 100) if name == "cartpole" else (16384, 100)
         if name == "cartpole":
@@ -235,7 +361,9 @@ def run_gpu(args, ws, rank, local):
 
     B.build()
     stream = torch.cuda.Stream()
-    wl = build_workload(args.workload, seed=0, stream=stream.cuda_stream, instances=args.instances)
+    surrogate = args.workload in ("slip_mlp", "batched_slip_mlp")
+    wl = build_workload(args.workload, seed=0, stream=stream.cuda_stream, instances=args.instances,
+                        precision=args.precision, params=surrogate_params() if surrogate else None)
     ctrl = wl.controller
     colored = args.workload == "batched_di"
     x0 = wl.x0
@@ -273,6 +401,11 @@ def run_gpu(args, ws, rank, local):
     dom = int(np.argmax(kms))
     peak, peak_kind = measured_peaks()
     achieved = abytes[names[dom]] / (kms[dom] * 1e-3) / 1e9
+    if surrogate:
+        # the surrogate rollout is a chain of tensor-core GEMMs: FLOPs against the bf16 peak
+        dom = 1
+        peak, peak_kind = measured_peaks("tensor")
+        achieved = MLP_FLOPS * steps_per_iter / (kms[1] * 1e-3) / 1e12
     traffic = None
     tfile = ROOT / "profiles" / "dram_traffic.json"
     if tfile.exists():
@@ -314,15 +447,22 @@ def run_gpu(args, ws, rank, local):
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "iters_per_s": iters_per_s,
         "kernel_ms": {n: float(v) for n, v in zip(names, kms)},
-        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes": abytes[names[dom]]},
+        "roofline": ({"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                      "algorithmic_bytes": abytes[names[dom]]} if not surrogate else
+                     {"bound": "tensor", "kernel": "rollout (surrogate + judge)", "achieved": achieved, "peak": peak,
+                      "unit": "TFLOP/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                      "algorithmic_flops": MLP_FLOPS * steps_per_iter}),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "iters_per_s": ws * iters / e2e_s},
         "gpu_launches": kernels * args.steps,
     }
     if clk:
         line["clocks"] = clk
+    if surrogate:
+        line["dtype"] = {"bf16": "bf16 weights, f32 accumulate/state", "fp8": "fp8-e4m3 weights, f32 accumulate/state",
+                         "fp32": "f32"}[wl.description["precision"]]
+        line.update(surrogate_extras(args, wl, stream.cuda_stream))
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, 0, args.cpu_seconds)
     if rank == 0:
@@ -335,6 +475,7 @@ def run_gpu(args, ws, rank, local):
 def run_reference(args, ws, rank):
     if rank != 0:
         return
+    _SURROGATE["cpu_only"] = True
     per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
     for _ in range(args.warmup):
         cpu_baseline(args.workload, 0, per_step)

@@ -330,7 +330,7 @@ static mppi_status launch_class(const ColoredArgs& a, int max_t, int num_sms, cu
   auto kern = colored_sample_kernel<C, SPB, R>;
   if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 1;
-  MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem));
+  MG_CUDA(resident_ctas_per_sm(kern, THREADS, smem, &per_sm));
   const int grid = std::max(1, std::min(a.num_work, std::max(per_sm, 1) * num_sms));
   kern<<<grid, THREADS, smem, s>>>(a);
   MG_CUDA(cudaGetLastError());

@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstddef>
 #include <cstdio>
@@ -112,5 +113,38 @@ struct PinnedBuf
     return MPPI_OK;
   }
 };
+
+// CTAs of `kern` that can be resident on one SM with `threads` threads and `dyn_smem` bytes of dynamic shared memory.
+// The kernel's shared-memory carveout preference is set to the maximum first, so the L1 / shared split leaves room
+// for that many; the count is the smaller of the register, shared-memory, thread and CTA-slot limits (the larger of
+// that and the runtime's occupancy answer).
+template <class Kernel>
+inline cudaError_t resident_ctas_per_sm(Kernel kern, int threads, size_t dyn_smem, int* out)
+{
+  *out = 1;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  if ((e = cudaFuncGetAttributes(&fa, kern)) != cudaSuccess) return e;
+  int dev = 0, smem_sm = 0, resv = 0, regs_sm = 0, thr_sm = 0, blk_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  cudaDeviceGetAttribute(&blk_sm, cudaDevAttrMaxBlocksPerMultiprocessor, dev);
+  const int warps = (threads + 31) / 32;
+  const int regs_warp = ((fa.numRegs * 32 + 255) / 256) * 256;  // allocation granule: 256 registers per warp
+  int n = blk_sm > 0 ? blk_sm : 32;
+  if (regs_warp > 0) n = std::min(n, regs_sm / (regs_warp * warps));
+  n = std::min(n, thr_sm / (warps * 32));
+  const size_t smem_blk = fa.sharedSizeBytes + dyn_smem + (size_t)resv;
+  if (smem_blk > 0) n = std::min(n, (int)((size_t)smem_sm / smem_blk));
+  int api = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&api, kern, threads, dyn_smem)) != cudaSuccess) return e;
+  *out = std::max(1, std::max(n, api));
+  return cudaSuccess;
+}
 
 }  // namespace mg

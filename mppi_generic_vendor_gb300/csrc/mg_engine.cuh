@@ -282,8 +282,40 @@ public:
   mppi_status get_state_seq(float* out) override
   {
     MG_CHECK(out, "out must not be NULL");
+    if (traj_dirty_) compute_state_seq();
     memcpy(out, state_seq_.data(), sizeof(float) * state_seq_.size());
     return MPPI_OK;
+  }
+
+  // computeOutputTrajectoryHelper (controller.cuh:664-684): x0, then T-1 steps under the constrained nominal controls
+  // of the last solve, with the model's host twin (the surrogate in FP32 for the MLP model).
+  void compute_state_seq()
+  {
+    float* xs = state_seq_.data();
+    for (int i = 0; i < I_; ++i)
+    {
+      const int T = T_[i];
+      const float* u = traj_u_.data() + t_off_[i];
+      float x[S], xn[S];
+      for (int s = 0; s < S; ++s) x[s] = xs[s] = traj_x0_[(size_t)i * S + s];
+      for (int t = 0; t < T - 1; ++t)
+      {
+        const float* uc = u + (size_t)t * C;
+        if (Model::kMlp && !use_analytic_)
+        {
+          float xd[S];
+          mlp_host_dynamics(mlp_host_.data(), x, uc, xd);
+          for (int s = 0; s < S; ++s) xn[s] = fmaf(xd[s], cp_.dt, x[s]);
+        }
+        else
+        {
+          euler_step<Model>(dyn_[i], x, uc, xn, cp_.dt);
+        }
+        for (int s = 0; s < S; ++s) x[s] = xs[(size_t)(t + 1) * S + s] = xn[s];
+      }
+      xs += (size_t)T * S;
+    }
+    traj_dirty_ = false;
   }
   mppi_status get_baseline_normalizer(float* out, double* norm64) override
   {
@@ -874,13 +906,12 @@ private:
     if (use_bulk_)
     {
       using B = BulkRolloutShape<NS, C>;
-      MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, rollout_kernel_bulk<Model, NS, B::TCH>, NS,
-                                                            B::SMEM));
+      MG_CUDA(resident_ctas_per_sm(rollout_kernel_bulk<Model, NS, B::TCH>, NS, B::SMEM, per_sm));
     }
     else
     {
       constexpr int TCH = RolloutShape<NS, C>::TCH;
-      MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, rollout_kernel<Model, NS, TCH>, NS, 0));
+      MG_CUDA(resident_ctas_per_sm(rollout_kernel<Model, NS, TCH>, NS, 0, per_sm));
     }
     if (*per_sm < 1) *per_sm = 1;
     return MPPI_OK;
@@ -1128,33 +1159,15 @@ private:
       const int T = T_[i];
       for (int c = 0; c < C; ++c) last_pre_smooth_[(size_t)i * C + c] = u[c];
       smooth_control(u, T, C);
-      // computeOutputTrajectoryHelper (controller.cuh:664-684): x0 then T-1 constrained steps
-      float* xs = state_seq_.data();
-      for (int j = 0; j < i; ++j) xs += (size_t)T_[j] * S;
-      float x[S], xn[S], uc[C];
-      for (int s = 0; s < S; ++s) x[s] = xs[s] = x0[(size_t)i * S + s];
-      for (int t = 0; t < T - 1; ++t)
-      {
-        for (int c = 0; c < C; ++c)
-          uc[c] = enforce_constraint(u[(size_t)t * C + c], cc_.lower[c], cc_.upper[c], cc_.deadband[c],
-                                     cc_.zero_control[c]);
-        if (Model::kMlp && !use_analytic_)
-        {
-          float xd[S];
-          mlp_host_dynamics(mlp_host_.data(), x, uc, xd);
-          for (int s = 0; s < S; ++s) xn[s] = fmaf(xd[s], cp_.dt, x[s]);
-        }
-        else
-        {
-          euler_step<Model>(dyn_[i], x, uc, xn, cp_.dt);
-        }
-        for (int s = 0; s < S; ++s) x[s] = xs[(size_t)(t + 1) * S + s] = xn[s];
-      }
       for (int t = 0; t < T; ++t)
         for (int c = 0; c < C; ++c)
           u[(size_t)t * C + c] = enforce_constraint(u[(size_t)t * C + c], cc_.lower[c], cc_.upper[c],
                                                     cc_.deadband[c], cc_.zero_control[c]);
     }
+    // the nominal state trajectory is rolled out when it is first read (get_state_seq), from these snapshots
+    traj_u_ = control_;
+    traj_x0_.assign(x0, x0 + (size_t)I_ * S);
+    traj_dirty_ = true;
     if (bad)
     {
       set_error("a sampled cost or the normaliser is not finite (NaN state or noise?)");
@@ -1184,6 +1197,8 @@ private:
   std::vector<CostParams> cost_;
   ModelAux aux_{};
   std::vector<float> control_, state_seq_, history_, last_pre_smooth_, baseline_norm_, prev_baseline_;
+  std::vector<float> traj_u_, traj_x0_;  // constrained nominal controls and x0 of the last solve
+  bool traj_dirty_ = false;
   std::vector<double> stats_;
 
   cudaStream_t stream_ = nullptr;

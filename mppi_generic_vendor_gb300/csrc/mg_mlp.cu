@@ -24,6 +24,7 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, c
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t s_tmem;
+  __shared__ int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0)
   {
@@ -32,6 +33,7 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, c
   }
   if (tid == 0)
   {
+    s_fail = 0;
     mbar_init(&mbar, 1);
     fence_mbarrier_init();
   }
@@ -47,18 +49,15 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, c
     const int row = tile * 128 + tid;
     float x[kMlpIn], y[kMlpOut];
 #pragma unroll
-    for (int i = 0; i < kMlpIn; ++i) x[i] = row < B ? (X[(size_t)row * kMlpIn + i] - nrm[i]) / nrm[9 + i] : 0.0f;
-    if (!mlp_tile_forward(sm, taddr, &mbar, phase, x, y))
-    {
-      if (tid == 0) atomicOr(status, 1u);
-      break;
-    }
+    for (int i = 0; i < kMlpIn; ++i) x[i] = row < B ? (X[(size_t)row * kMlpIn + i] - nrm[i]) * nrm[32 + i] : 0.0f;
+    if (!mlp_tile_forward(sm, taddr, &mbar, phase, &s_fail, x, y)) break;
     if (row < B)
 #pragma unroll
       for (int j = 0; j < kMlpOut; ++j) Y[(size_t)row * kMlpOut + j] = y[j] * nrm[23 + j] + nrm[18 + j];
   }
   tc_fence_before_sync();
   __syncthreads();
+  if (tid == 0 && s_fail) atomicOr(status, 1u);
   if (warp == 0) tmem_dealloc(taddr, MlpSmem::TMEM_COLS);
 }
 
@@ -117,6 +116,7 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
   __shared__ uint32_t s_tmem;
   __shared__ int s_tile;
   __shared__ unsigned int s_min;
+  __shared__ int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5;
   float* pf = reinterpret_cast<float*>(sm);  // FP32 path: the device parameter vector
   if constexpr (kTensor)
@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
     }
     if (tid == 0)
     {
+      s_fail = 0;
       mbar_init(&mbar, 1);
       fence_mbarrier_init();
     }
@@ -171,17 +172,22 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
       const float u[2] = { u_next.x, u_next.y };
       if (active && t + 1 < d.T) u_next = __ldg(reinterpret_cast<const float2*>(urow + (t + 1) * C));
       float xin[kMlpIn], y[kMlpOut];
-#pragma unroll
-      for (int i = 0; i < S; ++i) xin[i] = (x[i] - nrm[i]) / nrm[9 + i];
-      xin[7] = (u[0] - nrm[7]) / nrm[16];
-      xin[8] = (u[1] - nrm[8]) / nrm[17];
       if constexpr (kTensor)
       {
-        ok = mlp_tile_forward(sm, taddr, &mbar, phase, xin, y);
+        // the inputs are rounded to BF16 next, so a multiply by the stored reciprocal stands in for the division
+#pragma unroll
+        for (int i = 0; i < S; ++i) xin[i] = (x[i] - nrm[i]) * nrm[32 + i];
+        xin[7] = (u[0] - nrm[7]) * nrm[32 + 7];
+        xin[8] = (u[1] - nrm[8]) * nrm[32 + 8];
+        ok = mlp_tile_forward(sm, taddr, &mbar, phase, &s_fail, xin, y);
         if (!ok) break;
       }
       else
       {
+#pragma unroll
+        for (int i = 0; i < S; ++i) xin[i] = (x[i] - nrm[i]) / nrm[9 + i];
+        xin[7] = (u[0] - nrm[7]) / nrm[16];
+        xin[8] = (u[1] - nrm[8]) / nrm[17];
         mlp_thread_forward(pf, xin, y);
       }
       float xd[S];
@@ -233,6 +239,11 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
     if ((tid & 31) == 0) atomicMin(&s_min, o);
     __syncthreads();
     if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+    if (kTensor && *reinterpret_cast<volatile int*>(&s_fail))  // CTA-uniform: set before the barrier above
+    {
+      if (tid == 0) atomicOr(a.status, 1u);
+      break;
+    }
   }
   if constexpr (kTensor)
   {
@@ -314,10 +325,15 @@ __global__ void __launch_bounds__(1024) judge_select_kernel(const __grid_constan
   {
     for (int b = tid; b < 256; b += blockDim.x) hist[b] = 0u;
     __syncthreads();
-    for (int k = tid; k < d.K; k += blockDim.x)
+    // the costs share their leading bits, so most lanes of a warp hit the same bin: one atomic per distinct bin
+    // and warp (__match_any_sync) instead of one per lane
+    for (int k0 = 0; k0 < d.K; k0 += blockDim.x)
     {
-      const unsigned int key = float_to_ordered(c[k]);
-      if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+      const int k = k0 + tid;
+      const unsigned int key = k < d.K ? float_to_ordered(c[k]) : 0u;
+      const unsigned int bin = (k < d.K && (key & mask) == prefix) ? ((key >> shift) & 255u) : 256u;
+      const unsigned int same = __match_any_sync(0xffffffffu, bin);
+      if (bin < 256u && (threadIdx.x & 31) == (unsigned int)(__ffs(same) - 1)) atomicAdd(&hist[bin], __popc(same));
     }
     __syncthreads();
     if (tid == 0)
@@ -466,7 +482,7 @@ mppi_status launch_mlp_rollout(const RolloutArgs<BicycleSlipMLPModel>& a, const 
   const size_t smem = tensor ? kMlpSmem : sizeof(float) * kMlpDevParams;
   MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 1;
-  MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem));
+  MG_CUDA(resident_ctas_per_sm(kern, 128, smem, &per_sm));
   per_sm = std::max(1, tensor ? std::min(per_sm, kMlpMaxCtasPerSm) : per_sm);
   const int grid = std::max(1, std::min(a.num_tiles, per_sm * num_sms));
   kern<<<grid, 128, smem, s>>>(a, mlp_d);

@@ -34,7 +34,8 @@ struct MlpSmem
   static constexpr int A1 = 12288;      // 128 x 16 bf16
   static constexpr int A2 = 16384;      // 128 x 64 bf16 (hidden 1, then hidden 2)
   static constexpr int BIAS = 32768;    // fp32 b1[64] b2[64] b3[16]
-  static constexpr int NORM = 33792;    // fp32 in_mean[9] in_std[9] out_mean[5] out_std[5] layer_scale[3]
+  static constexpr int NORM = 33792;    // fp32 in_mean[9] in_std[9] out_mean[5] out_std[5] layer_scale[3] pad
+                                        //      1/in_std[9] (from float 32)
   static constexpr int TOTAL = 34048;
   // One 64-column accumulator serves all three layers: each layer's result is read back into shared memory before
   // the next layer's MMA is issued.
@@ -81,12 +82,15 @@ __device__ __forceinline__ void mlp_load_weights(unsigned char* sm, const float*
     bias[e] = e < 64 ? params[kMlpB1 + e] : e < 128 ? params[kMlpB2 + e - 64] : (e - 128 < kMlpOut ? params[kMlpB3 + e - 128] : 0.0f);
   float* nrm = reinterpret_cast<float*>(sm + MlpSmem::NORM);
   for (int e = tid; e < 31; e += nt) nrm[e] = params[kMlpInMean + e];  // normalisation + layer scales
+  for (int e = tid; e < kMlpIn; e += nt) nrm[32 + e] = 1.0f / params[kMlpInStd + e];  // input scale reciprocals
 }
 
 // One forward pass of the tile.  Thread i provides its normalised input row xin[9] and receives yout[5]
-// (normalised outputs).  Returns false if a bounded wait gave up (the caller stops and frees TMEM).
+// (normalised outputs).  A bounded wait that gives up sets *fail (shared); every thread reads the flag after the
+// next CTA barrier, so the pass returns false on all threads together (the caller stops and frees TMEM).  A failure
+// in the last layer surfaces at the caller's next barrier.
 __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t taddr, uint64_t* mbar, uint32_t& phase,
-                                                 const float* xin, float* yout)
+                                                 volatile int* fail, const float* xin, float* yout)
 {
   const int m = threadIdx.x, warp = m >> 5;
   const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
@@ -112,6 +116,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   fence_proxy_async_smem();
   tc_fence_before_sync();
   __syncthreads();
+  if (*fail) return false;  // CTA-uniform: read after the barrier
   if (m == 0)
   {
     tc_fence_after_sync();
@@ -119,7 +124,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
               kId64, 0u);
     umma_commit(mbar);
   }
-  if (__syncthreads_or(!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins) ? 1 : 0)) return false;  // CTA-uniform
+  if (!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins)) *fail = 1;
   phase ^= 1u;
   tc_fence_after_sync();
 #pragma unroll
@@ -145,6 +150,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   fence_proxy_async_smem();
   tc_fence_before_sync();
   __syncthreads();
+  if (*fail) return false;  // CTA-uniform: read after the barrier
   if (m == 0)
   {
     tc_fence_after_sync();
@@ -154,7 +160,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
                 umma_smem_desc(sbase + MlpSmem::W2 + 256 * k, 128, 1024), kId64, k > 0 ? 1u : 0u);
     umma_commit(mbar);
   }
-  if (__syncthreads_or(!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins) ? 1 : 0)) return false;  // CTA-uniform
+  if (!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins)) *fail = 1;
   phase ^= 1u;
   tc_fence_after_sync();
 #pragma unroll
@@ -180,6 +186,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   fence_proxy_async_smem();
   tc_fence_before_sync();
   __syncthreads();
+  if (*fail) return false;  // CTA-uniform: read after the barrier
   if (m == 0)
   {
     tc_fence_after_sync();
@@ -189,7 +196,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
                 umma_smem_desc(sbase + MlpSmem::W3 + 256 * k, 128, 1024), kId16, k > 0 ? 1u : 0u);
     umma_commit(mbar);
   }
-  if (__syncthreads_or(!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins) ? 1 : 0)) return false;  // CTA-uniform
+  if (!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins)) *fail = 1;
   phase ^= 1u;
   tc_fence_after_sync();
   {

@@ -493,6 +493,14 @@ public:
       host_params[oInMean + j] = (float)(0.5 * (lo + hi));
       host_params[oInStd + j] = hi > lo ? (float)((hi - lo) / std::sqrt(12.0)) : 1.0f;
     }
+    // The body-frame derivatives do not depend on position or heading: those inputs get mean 0 and scale 1e30, so
+    // they reach the network as (numerically) zero and a rollout that leaves the training box in x / y / yaw never
+    // makes the network extrapolate.
+    for (int j = 0; j < 3; ++j)
+    {
+      host_params[oInMean + j] = 0.0f;
+      host_params[oInStd + j] = 1e30f;
+    }
     for (int j = 7; j < kIn; ++j)
     {
       host_params[oInMean + j] = 0.0f;

@@ -84,12 +84,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Hardware tanh approximation (MUFU), adequate for activations that are rounded to BF16 afterwards.
+// tanh.approx.f32: the hardware tanh (MUFU), maximum relative error about 2^-11, below the BF16 rounding that
+// follows it.
 __device__ __forceinline__ float tanh_fast(float x)
 {
   float y;
   asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
+
 
 }  // namespace mg

@@ -293,6 +293,76 @@ def test_surrogate_drift_from_fp64_analytic(trained):
     ctrl.close()
 
 
+@pytest.fixture(scope="module")
+def well_trained():
+    """2^20 transitions, 10^4 Adam steps (about half a second on one GB300)."""
+    s = Surrogate(num_transitions=1 << 20, seed=5)
+    s.generate()
+    s.train(steps=10000, batch=8192, lr=3e-3, lr_final=1e-4)
+    p = s.params()
+    s.close()
+    return p
+
+
+def _final_cost(dyn, cmap, x0, judge=None, iters=10, K=4096, T=100):
+    """FP64 analytic cost of the control sequence an MPPI controller with `dyn` settles on after `iters` iterations."""
+    sampler = GaussianDistribution(std_dev=(0.5, 0.5))
+    ctrl = VanillaMPPIController(dyn, slip_cost(cmap), None, sampler, 0.02, 1, 2.0, 0.0, T, K, seed=3)
+    if judge is not None:
+        ctrl.setJudge(judge)
+    for _ in range(iters):
+        ctrl.computeControl(x0, 1)
+    u = ctrl.getControlSeq().T.copy()
+    c64, _, _ = oracle.rollout(A.MODEL_BICYCLE_SLIP, BicycleSlipDynamics().getParams(), ctrl._cost_arr[0], x0, u, u,
+                               sampler.to_c(), ctrl.constraints_, 2.0, 0.0, 1, T, 0.02,
+                               costmap=(cmap, 0.1, (0.0, 0.0)), fp64=True, state_dim=7)
+    ctrl.close()
+    return float(c64[0])
+
+
+def test_final_trajectory_cost_within_one_percent(well_trained):
+    """MPPI on the BF16 surrogate (with the analytic judge) settles on controls whose exact FP64 cost is at most 1%
+    above what MPPI on the analytic model itself settles on, from the same seed (lower is allowed: ten MPPI
+    iterations do not reach the optimum, so either controller may end slightly ahead)."""
+    cmap = gaussian_bump_costmap(6, size=128)
+    x0 = np.array([20.0, 20.0, -0.4, 7.0, 0.0, 0.0, 0.0], np.float32)
+    j_analytic = _final_cost(BicycleSlipDynamics(), cmap, x0)
+    j_surrogate = _final_cost(BicycleSlipMLPDynamics(well_trained, precision="bf16"), cmap, x0, judge=0.01)
+    assert j_surrogate <= 1.01 * j_analytic, (j_surrogate, j_analytic)
+
+
+def test_trained_network_gain_over_nominal_model():
+    """What the learned model gains: the plant's true parameters differ from the nominal first-principles model an
+    engineer would write down (mass, tyre stiffness and drive force off by 20-40%).  Without the network, MPPI rolls
+    out that nominal model; with it, MPPI rolls out a surrogate trained on the plant's own transitions.  On the same
+    control samples the surrogate predicts the plant's sample costs at least twice as accurately as the nominal
+    model does."""
+    plant = BicycleSlipDynamics(mass=1500.0, cornering_stiffness=8e4, max_drive_force=4000.0)
+    nominal = BicycleSlipDynamics(mass=1200.0, cornering_stiffness=5e4, max_drive_force=5000.0)
+    s = Surrogate(dynamics=plant, num_transitions=1 << 20, seed=21)
+    s.generate()
+    s.train(steps=10000, batch=8192, lr=3e-3, lr_final=1e-4)
+    params = s.params()
+    s.close()
+    K, T, seed = 2048, 60, 12
+    cmap = gaussian_bump_costmap(seed, size=128)
+    x0 = np.array([20.0, 20.0, -0.4, 7.0, 0.0, 0.0, 0.0], np.float32)
+    rng = np.random.default_rng(seed)
+    eps = rng.standard_normal(K * T * 2).astype(np.float32)
+    init = np.zeros((T, 2), np.float32)
+    errs = {}
+    for name, dyn in [("surrogate", BicycleSlipMLPDynamics(params)), ("nominal", nominal)]:
+        ctrl = _slip_controller(dyn, cmap, K, T, eps, init, judge=0.0 if name == "surrogate" else None)
+        ctrl.computeControl(x0, 1)
+        pred = ctrl.sample_costs()
+        truth, _, _ = oracle.rollout(A.MODEL_BICYCLE_SLIP, plant.getParams(), ctrl._cost_arr[0], x0,
+                                     ctrl.control_samples(), init, ctrl.sampler_.to_c(), ctrl.constraints_, 2.0, 0.0,
+                                     K, T, 0.02, costmap=(cmap, 0.1, (0.0, 0.0)), fp64=True, state_dim=7)
+        errs[name] = float(np.median(np.abs(pred - truth) / np.abs(truth)))
+        ctrl.close()
+    assert errs["surrogate"] < 0.5 * errs["nominal"], errs
+
+
 def test_mlp_model_requires_weights():
     cmap = gaussian_bump_costmap(1, size=64)
     ctrl = VanillaMPPIController(BicycleSlipMLPDynamics(), slip_cost(cmap), None,

@@ -347,6 +347,25 @@ def cpu_baseline(name, seed, budget_s):
             "seconds": round(elapsed, 3)}
 
 
+# ------------------------------------------------------------------------------------------------ replicas
+def max_over_ranks(value: float, dist=None) -> float:
+    """The maximum of a per-rank number over all ranks (identity without a process group)."""
+    if dist is None or not dist.is_initialized():
+        return float(value)
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, seconds_max: float, world_size: int) -> float:
+    """Aggregate throughput of independent replicas: every rank processed `units_per_rank`, the job took the
+    slowest rank's time."""
+    return world_size * units_per_rank / seconds_max
+
+
 # ------------------------------------------------------------------------------------------------ GPU arm
 def run_gpu(args, ws, rank, local):
     import torch
@@ -385,13 +404,10 @@ def run_gpu(args, ws, rank, local):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     steps_per_iter = wl.sample_steps_per_iter
     iters = args.steps * wl.num_iters
-    value = ws * steps_per_iter * iters / (ms / 1e3)
+    value = whole_job_rate(steps_per_iter * iters, ms / 1e3, ws)
     iters_per_s = iters / (ms / 1e3)
     kernels = ctrl.kernelsPerCompute()
     # ---------------- per-kernel timing and roofline
@@ -426,12 +442,8 @@ def run_gpu(args, ws, rank, local):
     for _ in range(args.steps):
         ctrl.computeControlFlat(x0, 1)
         u = ctrl.control_flat()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = ws * steps_per_iter * iters / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e = whole_job_rate(steps_per_iter * iters, e2e_s, ws)
     n_inst = wl.controller.num_instances
     h2d = 4 * (n_inst * wl.state_dim + int(np.sum(wl.T)) * wl.control_dim)
     d2h = 4 * int(np.sum(wl.T)) * wl.control_dim + 8 * n_inst + 24 * n_inst + u.nbytes

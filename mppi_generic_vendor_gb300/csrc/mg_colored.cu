@@ -48,7 +48,7 @@ __device__ __forceinline__ void row_transform_pow2(const ColoredArgs& a, const I
   const float2* tw_lane = reinterpret_cast<const float2*>(tab + parts.w);  // [5][32]
   const float* scale = tab + parts.x;
   const float* decay_t = tab + parts.z;
-  const float div = tab[parts.y + c] * 2.0f * (float)M;
+  const float inv_div = 1.0f / (tab[parts.y + c] * 2.0f * (float)M);
 
   float2 z[R];
   float nyq = 0.0f;
@@ -142,21 +142,36 @@ __device__ __forceinline__ void row_transform_pow2(const ColoredArgs& a, const I
       }
     }
   }
+  // Branch-free butterflies: the lower lane of a pair forms z + p, the upper p - z (a sign flip inside one fma), and
+  // both multiply by their table twiddle, which is exactly 1 for lower lanes.  The output positions kept below all
+  // sit on even lanes unless the offset sample lies in the second half (stride >= T), so the last stage is a plain
+  // sum there.
+  const bool need_odd = a.stride >= M;
 #pragma unroll
   for (int st = 0; st < 5; ++st)
   {
     const int half = 16 >> st;
-    const bool upper = (lane & half) != 0;
-    const float2 w = __ldg(tw_lane + st * 32 + lane);
-#pragma unroll
-    for (int r = 0; r < R; ++r)
+    const float sgn = (lane & half) ? -1.0f : 1.0f;
+    if (st < 4 || need_odd)
     {
-      const float px = __shfl_xor_sync(FULL, z[r].x, half);
-      const float py = __shfl_xor_sync(FULL, z[r].y, half);
-      if (!upper)
+      const float2 w = __ldg(tw_lane + st * 32 + lane);
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+      {
+        const float px = __shfl_xor_sync(FULL, z[r].x, half);
+        const float py = __shfl_xor_sync(FULL, z[r].y, half);
+        z[r] = cmul(make_float2(fmaf(z[r].x, sgn, px), fmaf(z[r].y, sgn, py)), w);
+      }
+    }
+    else
+    {
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+      {
+        const float px = __shfl_xor_sync(FULL, z[r].x, half);
+        const float py = __shfl_xor_sync(FULL, z[r].y, half);
         z[r] = make_float2(z[r].x + px, z[r].y + py);
-      else
-        z[r] = cmul(make_float2(px - z[r].x, py - z[r].y), w);
+      }
     }
   }
 
@@ -175,8 +190,8 @@ __device__ __forceinline__ void row_transform_pow2(const ColoredArgs& a, const I
     if (m < M / 2)
     {
       const int t0 = 2 * m;
-      tile_row[t0 * C] = (z[r].x - x_off * __ldg(decay_t + t0)) / div;
-      tile_row[(t0 + 1) * C] = (z[r].y - x_off * __ldg(decay_t + t0 + 1)) / div;
+      tile_row[t0 * C] = (z[r].x - x_off * __ldg(decay_t + t0)) * inv_div;
+      tile_row[(t0 + 1) * C] = (z[r].y - x_off * __ldg(decay_t + t0 + 1)) * inv_div;
     }
   }
 }

@@ -194,6 +194,7 @@ public:
       for (int k = 0; k < 5; ++k) sampler += class_begin_[k + 1] > class_begin_[k] ? 1 : 0;
     }
     const int judge = (Model::kMlp && !use_analytic_ && judge_total_ > 0) ? 3 : 0;
+    if (fused()) sampler = 0;
     return (sampler + 2 + judge) * cp_.num_iters;
   }
 
@@ -381,8 +382,10 @@ public:
   {
     MG_CHECK(sp, "sampling params must not be NULL");
     MG_TRY(check_sampling(*sp));
-    if (sp->kind != sp_.kind) injected_d_.reset();
+    const bool kind_changed = sp->kind != sp_.kind;
+    if (kind_changed) injected_d_.reset();
     sp_ = *sp;
+    if (kind_changed) MG_TRY(build_work_lists());  // the rollout kernel (fused or not) and its grid follow the kind
     MG_TRY(build_colored_tables());
     invalidate_graphs();
     return MPPI_OK;
@@ -582,9 +585,9 @@ public:
     for (int r = 0; r < reps + 1; ++r)
     {
       MG_CUDA(cudaEventRecord(ev[0], stream_));
-      MG_TRY(launch_sampler(stride, 0));
+      if (!fused()) MG_TRY(launch_sampler(stride, 0));
       MG_CUDA(cudaEventRecord(ev[1], stream_));
-      MG_TRY(launch_rollout());
+      MG_TRY(launch_rollout(stride, 0));
       MG_CUDA(cudaEventRecord(ev[2], stream_));
       MG_TRY(launch_weights());
       MG_CUDA(cudaEventRecord(ev[3], stream_));
@@ -903,6 +906,12 @@ private:
   template <int NS>
   mppi_status occupancy_ns(int* per_sm)
   {
+    if constexpr ((4 % C) == 0)
+      if (fused())
+      {
+        MG_CUDA(resident_ctas_per_sm(rollout_fused_kernel<Model, NS>, NS, 0, per_sm));
+        return MPPI_OK;
+      }
     if (use_bulk_)
     {
       using B = BulkRolloutShape<NS, C>;
@@ -988,7 +997,14 @@ private:
       rollout_kernel<Model, NS, TCH><<<rollout_grid_, NS, 0, stream_>>>(a);
     }
   }
-  mppi_status launch_rollout()
+  // Gaussian noise is generated inside the rollout (rollout_fused_kernel) when every row holds whole quads of steps;
+  // the standalone sampler then runs only for mppi_generate_samples.
+  bool fused() const
+  {
+    return !Model::kMlp && sp_.kind == MPPI_SAMPLER_GAUSSIAN && (4 % C) == 0 && use_bulk_;
+  }
+
+  mppi_status launch_rollout(int stride, int iter)
   {
     RolloutArgs<Model> a;
     a.inst = inst_d_.p;
@@ -1011,6 +1027,27 @@ private:
     for (int c = 0; c < C; ++c)
       if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
     a.sh = make_sample_shared(sp_, cc_);
+    if constexpr ((4 % C) == 0)
+      if (fused())
+      {
+        FusedNoise f;
+        f.samples = samples_d_.p;
+        f.injected = injected_d_.p;
+        f.noise_counter = counters_d_.p + 3;
+        f.seed_lo = (uint32_t)cp_.seed;
+        f.seed_hi = (uint32_t)(cp_.seed >> 32);
+        f.stride = stride;
+        f.decay_pow = powf(sp_.std_dev_decay, (float)iter);
+        switch (ns_)
+        {
+          case 32: rollout_fused_kernel<Model, 32><<<rollout_grid_, 32, 0, stream_>>>(a, f); break;
+          case 64: rollout_fused_kernel<Model, 64><<<rollout_grid_, 64, 0, stream_>>>(a, f); break;
+          case 128: rollout_fused_kernel<Model, 128><<<rollout_grid_, 128, 0, stream_>>>(a, f); break;
+          default: rollout_fused_kernel<Model, 256><<<rollout_grid_, 256, 0, stream_>>>(a, f); break;
+        }
+        MG_CUDA(cudaGetLastError());
+        return MPPI_OK;
+      }
     if constexpr (Model::kMlp)
       if (!use_analytic_)
       {
@@ -1073,8 +1110,8 @@ private:
   {
     for (int it = 0; it < cp_.num_iters; ++it)
     {
-      MG_TRY(launch_sampler(stride, it));
-      MG_TRY(launch_rollout());
+      if (!fused()) MG_TRY(launch_sampler(stride, it));
+      MG_TRY(launch_rollout(stride, it));
       MG_TRY(launch_weights());
     }
     return MPPI_OK;

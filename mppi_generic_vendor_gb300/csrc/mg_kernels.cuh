@@ -182,38 +182,47 @@ struct RolloutArgs
   SampleShared sh;
 };
 
-// Steps t0 .. t0+nt-1 of sample k from its staged control row: Euler step, running cost on the stepped output plus
-// the likelihood-ratio term, accumulated in reference order (mppi_common.cu:105-144).
+// One step t of sample k under control u: Euler step, running cost on the stepped output plus the likelihood-ratio
+// term, accumulated in reference order (mppi_common.cu:105-144).
+template <class Model>
+__device__ __forceinline__ void rollout_step(const RolloutArgs<Model>& a, const InstDesc& d,
+                                             const typename Model::DynParams& dp,
+                                             const typename Model::CostParams& cp, int k, const float* u, int t,
+                                             float* x, float& running)
+{
+  constexpr int S = Model::STATE_DIM;
+  constexpr int C = Model::CONTROL_DIM;
+  float xn[S];
+  euler_step<Model>(dp, x, u, xn, a.dt);
+  float step_cost = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
+  if (a.use_likelihood)
+  {
+    // GaussianDistributionImpl::computeLikelihoodRatioCost (gaussian.cu:490-574)
+    const bool zero_mean = (float)k >= (1.0f - a.sh.pure_pct) * (float)d.K;
+    float lc = 0.0f;
+#pragma unroll
+    for (int c = 0; c < C; ++c)
+    {
+      const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + c];
+      const float sd = a.sh.std_dev[c];
+      lc += a.sh.control_cost_coeff[c] * m * (m - 2.0f * u[c]) / (sd * sd);
+    }
+    step_cost += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
+  }
+  running += step_cost;
+#pragma unroll
+  for (int i = 0; i < S; ++i) x[i] = xn[i];
+}
+
+// Steps t0 .. t0+nt-1 of sample k from its staged control row.
 template <class Model>
 __device__ __forceinline__ void rollout_chunk(const RolloutArgs<Model>& a, const InstDesc& d,
                                               const typename Model::DynParams& dp,
                                               const typename Model::CostParams& cp, int k, const float* urow, int t0,
                                               int nt, float* x, float& running)
 {
-  constexpr int S = Model::STATE_DIM;
   constexpr int C = Model::CONTROL_DIM;
-  auto do_step = [&](const float* u, int t) {
-    float xn[S];
-    euler_step<Model>(dp, x, u, xn, a.dt);
-    float step_cost = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
-    if (a.use_likelihood)
-    {
-      // GaussianDistributionImpl::computeLikelihoodRatioCost (gaussian.cu:490-574)
-      const bool zero_mean = (float)k >= (1.0f - a.sh.pure_pct) * (float)d.K;
-      float lc = 0.0f;
-#pragma unroll
-      for (int c = 0; c < C; ++c)
-      {
-        const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + c];
-        const float sd = a.sh.std_dev[c];
-        lc += a.sh.control_cost_coeff[c] * m * (m - 2.0f * u[c]) / (sd * sd);
-      }
-      step_cost += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
-    }
-    running += step_cost;
-#pragma unroll
-    for (int i = 0; i < S; ++i) x[i] = xn[i];
-  };
+  auto do_step = [&](const float* u, int t) { rollout_step<Model>(a, d, dp, cp, k, u, t, x, running); };
   int tt = 0;
   if constexpr (4 % C == 0)
   {
@@ -264,7 +273,7 @@ __global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ Rol
     const bool active = k < d.K;
     const int rows = min(NS, d.K - w.y);
     const typename Model::DynParams dp = a.dyn[w.x];
-    const typename Model::CostParams& cp = a.cost[w.x];
+    const typename Model::CostParams cp = a.cost[w.x];  // by value: loop-invariant for the whole tile
 
     float x[S];
 #pragma unroll
@@ -332,6 +341,118 @@ __global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ Rol
   }
 }
 
+// Gaussian sampling fused into the rollout (every instance has T*C % 4 == 0 and C divides 4).  Thread k draws the
+// Philox quads of its own sample row (the same quad index, stream and counter as gaussian_sample_kernel, so the
+// samples are bit-identical to the two-kernel path), applies setGaussianControls and the constraints, stores each
+// quad once with a 16-byte store (the update kernel reads them) and integrates the 4/C steps it holds.  Nothing is
+// read back from HBM; the next quad's Philox rounds are independent of the dynamics chain, so they fill its latency.
+struct FusedNoise
+{
+  float* samples;         // written: the constrained control samples
+  const float* injected;  // standard-normal noise in samples layout, or nullptr for Philox
+  const unsigned int* noise_counter;
+  uint32_t seed_lo, seed_hi;
+  int stride;
+  float decay_pow;
+};
+
+template <class Model, int NS>
+__global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant__ RolloutArgs<Model> a,
+                                                           const __grid_constant__ FusedNoise f)
+{
+  constexpr int S = Model::STATE_DIM;
+  constexpr int C = Model::CONTROL_DIM;
+  static_assert(4 % C == 0, "a quad must hold whole steps");
+  constexpr int G = 4 / C;
+  __shared__ int s_tile;
+  __shared__ unsigned int s_min;
+  const int tid = threadIdx.x;
+  const uint32_t counter = f.noise_counter ? *f.noise_counter : 0u;
+  for (;;)
+  {
+    if (tid == 0)
+    {
+      s_tile = (int)atomicAdd(&a.tile_counter[0], 1u);
+      s_min = kOrderedPosInf;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= a.num_tiles) break;
+    const int2 w = a.tiles[tile];
+    const InstDesc d = a.inst[w.x];
+    const int k = w.y + tid;
+    const bool active = k < d.K;
+    const typename Model::DynParams dp = a.dyn[w.x];
+    const typename Model::CostParams cp = a.cost[w.x];
+    float x[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i) x[i] = a.x0[d.x_off + i];
+    float running = 0.0f;
+    if (active)
+    {
+      const int nq = d.T * C / 4;
+      const long long q0 = (long long)k * nq;
+      const float pure_threshold = (1.0f - a.sh.pure_pct) * (float)d.K;
+      float* dst = f.samples + d.u_off + 4 * q0;
+      auto noise = [&](long long q) {
+        return f.injected ? *reinterpret_cast<const float4*>(f.injected + d.u_off + 4 * q)
+                          : philox_normal4((uint64_t)q, (uint32_t)w.x, counter, f.seed_lo, f.seed_hi);
+      };
+      float4 zn = noise(q0);
+      for (int qi = 0; qi < nq; ++qi)
+      {
+        const float4 z = zn;
+        if (qi + 1 < nq) zn = noise(q0 + qi + 1);
+        const float zz[4] = { z.x, z.y, z.z, z.w };
+        float out[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+        {
+          const int rem = 4 * qi + j;
+          const int t = rem / C, c = rem - t * C;
+          const float m = a.mean[d.t_off + rem];
+          const float sd = f.decay_pow * a.sh.std_dev[c];
+          float u;
+          if (k == 0 || t < f.stride)
+            u = m;
+          else if ((float)k >= pure_threshold)
+            u = sd * zz[j];
+          else
+            u = fmaf(sd, zz[j], m);
+          out[j] = enforce_constraint(u, a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c], a.sh.zero[c]);
+        }
+        *reinterpret_cast<float4*>(dst + 4 * qi) = make_float4(out[0], out[1], out[2], out[3]);
+#pragma unroll
+        for (int g = 0; g < G; ++g) rollout_step<Model>(a, d, dp, cp, k, out + g * C, qi * G + g, x, running);
+      }
+    }
+    unsigned int o = kOrderedPosInf;
+    if (active)
+    {
+      const float tf = (float)d.T;
+      const float cost = running / tf + Model::terminalCost(cp, a.aux, x) / tf;
+      a.costs[d.k_off + k] = cost;
+      o = float_to_ordered(cost);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) o = min(o, __shfl_xor_sync(0xffffffffu, o, off));
+    if ((tid & 31) == 0) atomicMin(&s_min, o);
+    __syncthreads();
+    if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+  }
+  if (tid == 0)
+  {
+    __threadfence();
+    const unsigned int done = atomicAdd(&a.tile_counter[1], 1u);
+    if (done == gridDim.x - 1)
+    {
+      a.tile_counter[0] = 0u;
+      a.tile_counter[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
 // Rollout with the controls staged by the bulk-copy engine.  Each thread owns one row of a double-buffered stage and
 // copies its own sample's next time chunk with one cp.async.bulk while it integrates the current one; completion is
 // tracked by one mbarrier per warp and buffer (32 arrivals, expect-tx bytes).  No shared data crosses threads inside
@@ -385,7 +506,7 @@ __global__ void __launch_bounds__(NS) rollout_kernel_bulk(const __grid_constant_
     const int k = w.y + tid;
     const bool active = k < d.K;
     const typename Model::DynParams dp = a.dyn[w.x];
-    const typename Model::CostParams& cp = a.cost[w.x];
+    const typename Model::CostParams cp = a.cost[w.x];  // by value: loop-invariant for the whole tile
     const float* my_row = a.samples + d.u_off + (long long)k * d.T * C;
     float* const my_stage0 = stage + tid * ROW;  // buffer b row: my_stage0 + b * NS * ROW
 
@@ -542,7 +663,56 @@ __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_consta
   const int TC = a.samples ? d.T * C : 0;
   const float* ubase = a.samples + d.u_off + (long long)kb * TC;
   float* prow = a.partials + a.part_off[blockIdx.x];
-  if (TC > 0 && TC <= (int)blockDim.x)
+  const bool vec4 = TC > 0 && (TC & 3) == 0 && TC / 4 <= (int)blockDim.x &&
+                    ((reinterpret_cast<uintptr_t>(ubase) | reinterpret_cast<uintptr_t>(prow)) & 15) == 0;
+  if (vec4)
+  {
+    // 16-byte loads, four samples in flight per thread: G groups of Q = TC / 4 threads, thread (g, j) sums float4
+    // column j over samples g, g + G, ... in four interleaved accumulators, then the groups are combined in group
+    // order (a fixed order, so the result does not depend on scheduling)
+    __shared__ float4 s_part4[256];
+    const int Q = TC >> 2;
+    const int G = blockDim.x / Q;
+    const int g = tid / Q, j = tid - g * Q;
+    const float4* ub = reinterpret_cast<const float4*>(ubase);
+    auto fma4 = [](float w, const float4& v, float4& acc) {
+      acc.x = fmaf(w, v.x, acc.x);
+      acc.y = fmaf(w, v.y, acc.y);
+      acc.z = fmaf(w, v.z, acc.z);
+      acc.w = fmaf(w, v.w, acc.w);
+    };
+    if (g < G)
+    {
+      float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
+      int i = g;
+      for (; i + 3 * G < nk; i += 4 * G)
+      {
+        const float4 v0 = __ldg(ub + (long long)i * Q + j);
+        const float4 v1 = __ldg(ub + (long long)(i + G) * Q + j);
+        const float4 v2 = __ldg(ub + (long long)(i + 2 * G) * Q + j);
+        const float4 v3 = __ldg(ub + (long long)(i + 3 * G) * Q + j);
+        fma4(s_w[i], v0, a0);
+        fma4(s_w[i + G], v1, a1);
+        fma4(s_w[i + 2 * G], v2, a2);
+        fma4(s_w[i + 3 * G], v3, a3);
+      }
+      for (; i < nk; i += G) fma4(s_w[i], __ldg(ub + (long long)i * Q + j), a0);
+      s_part4[tid] = make_float4((a0.x + a1.x) + (a2.x + a3.x), (a0.y + a1.y) + (a2.y + a3.y),
+                                 (a0.z + a1.z) + (a2.z + a3.z), (a0.w + a1.w) + (a2.w + a3.w));
+    }
+    __syncthreads();
+    if (tid < Q)
+    {
+      float4 s = s_part4[tid];
+      for (int gg = 1; gg < G; ++gg)
+      {
+        const float4 v = s_part4[gg * Q + tid];
+        s = make_float4(s.x + v.x, s.y + v.y, s.z + v.z, s.w + v.w);
+      }
+      reinterpret_cast<float4*>(prow)[tid] = s;
+    }
+  }
+  else if (TC > 0 && TC <= (int)blockDim.x)
   {
     // G groups of TC threads; group g sums samples g, g + G, ... of the chunk for column j, then the groups are
     // combined in group order (a fixed order, so the result does not depend on scheduling)

@@ -133,12 +133,14 @@ struct DoubleIntegratorModel
   {
     float cost = quad(q, y);
     bool inside = false;
-    for (int j = 0; j < q.num_obstacles; ++j)
+    // fixed trip count with a guard, so the obstacle table can live in registers for a whole rollout
+#pragma unroll
+    for (int j = 0; j < MPPI_MAX_OBSTACLES; ++j)
     {
       const float ox = y[0] - q.obstacle_x[j];
       const float oy = y[1] - q.obstacle_y[j];
       const float r = q.obstacle_radius[j];
-      inside = inside || (ox * ox + oy * oy < r * r);
+      inside = inside || (j < q.num_obstacles && ox * ox + oy * oy < r * r);
     }
     if (inside) cost = cost + q.obstacle_cost;
     return cost;

@@ -33,7 +33,13 @@ __device__ __forceinline__ float4 row_normals(uint32_t lane_block, long long row
   return z;
 }
 
-// Register-resident row transform for T = 32 R.  Writes eps[t] (t < T) to tile_row[t * C].
+// Output tile layout: sample row s at s * tile_row_floats(T), element (t, c) at t * C + c + (t >> 3).  The pad of one
+// float per 8 steps spreads the bit-reversed stores of the register transform (lanes 8 or 4 steps apart) over the
+// shared-memory banks.
+__host__ __device__ __forceinline__ int tile_pos(int t, int c, int C) { return t * C + c + (t >> 3); }
+__host__ __device__ __forceinline__ int tile_row_floats(int T, int C) { return T * C + (T >> 3) + 1; }
+
+// Register-resident row transform for T = 32 R.  Writes eps[t] (t < T) to tile_row[tile_pos(t, 0, C)].
 template <int C, int R>
 __device__ __forceinline__ void row_transform_pow2(const ColoredArgs& a, const InstDesc& d, int inst, long long row,
                                                    int c, int lane, const float* tab, const int4 parts,
@@ -190,8 +196,8 @@ __device__ __forceinline__ void row_transform_pow2(const ColoredArgs& a, const I
     if (m < M / 2)
     {
       const int t0 = 2 * m;
-      tile_row[t0 * C] = (z[r].x - x_off * __ldg(decay_t + t0)) * inv_div;
-      tile_row[(t0 + 1) * C] = (z[r].y - x_off * __ldg(decay_t + t0 + 1)) * inv_div;
+      tile_row[tile_pos(t0, 0, C)] = (z[r].x - x_off * __ldg(decay_t + t0)) * inv_div;
+      tile_row[tile_pos(t0 + 1, 0, C)] = (z[r].y - x_off * __ldg(decay_t + t0 + 1)) * inv_div;
     }
   }
 }
@@ -244,7 +250,7 @@ __device__ __forceinline__ void row_transform_direct(const ColoredArgs& a, const
     return acc;
   };
   const float x_off = eval(a.stride);
-  for (int t = lane; t < T; t += 32) tile_row[t * C] = (eval(t) - x_off * __ldg(decay_t + t)) / div;
+  for (int t = lane; t < T; t += 32) tile_row[tile_pos(t, 0, C)] = (eval(t) - x_off * __ldg(decay_t + t)) / div;
   __syncwarp();
 }
 
@@ -273,7 +279,7 @@ __global__ void __launch_bounds__(32 * SPB * C, (R >= 8 || R == 0) ? 2 : 3)
     if (s_local < nsamp)
     {
       const long long row = (long long)(w.y + s_local) * C + c;
-      float* tile_row = tile + s_local * T * C + c;
+      float* tile_row = tile + s_local * tile_row_floats(T, C) + c;
       if constexpr (R > 0)
         row_transform_pow2<C, R>(a, d, w.x, row, c, lane, tab, parts, tile_row, counter);
       else
@@ -296,7 +302,7 @@ __global__ void __launch_bounds__(32 * SPB * C, (R >= 8 || R == 0) ? 2 : 3)
       for (int sl = threadIdx.x / TC; sl < nsamp; sl += per_pass)
       {
         const int kk = w.y + sl;
-        const float eps = tile[sl * TC + rem];
+        const float eps = tile[sl * tile_row_floats(T, C) + rem + (t >> 3)];
         float u;
         if (kk == 0 || t < a.stride)
           u = m;
@@ -318,7 +324,7 @@ __global__ void __launch_bounds__(32 * SPB * C, (R >= 8 || R == 0) ? 2 : 3)
         const int kk = w.y + sl;
         const float m = a.mean[d.t_off + rem];
         const float sd = a.decay_pow * a.sh.std_dev[cc];
-        const float eps = tile[e];
+        const float eps = tile[sl * tile_row_floats(T, C) + rem + (t >> 3)];
         float u;
         if (kk == 0 || t < a.stride)
           u = m;
@@ -341,7 +347,7 @@ static mppi_status launch_class(const ColoredArgs& a, int max_t, int num_sms, cu
   constexpr int THREADS = ColoredShape<C>::THREADS;
   const size_t xbuf = (R == 0) ? sizeof(float2) * (size_t)SPB * C * (kColoredMaxT + 2) : 0;
   const int tmax = (R == 0) ? max_t : 32 * R;
-  const size_t smem = xbuf + sizeof(float) * (size_t)SPB * tmax * C;
+  const size_t smem = xbuf + sizeof(float) * (size_t)SPB * tile_row_floats(tmax, C);
   auto kern = colored_sample_kernel<C, SPB, R>;
   if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 1;

@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "mg_math.cuh"
 #include "mg_models.cuh"
 #include "mg_ptx.cuh"
@@ -184,8 +186,10 @@ struct RolloutArgs
 
 // One step t of sample k under control u: Euler step, running cost on the stepped output plus the likelihood-ratio
 // term, accumulated in reference order (mppi_common.cu:105-144).
-template <class Model>
-__device__ __forceinline__ void rollout_step(const RolloutArgs<Model>& a, const InstDesc& d,
+// kLik: the likelihood-ratio term is on (control_cost_coeff != 0).  It is a template flag so the step has no
+// branch and consecutive steps form one basic block the scheduler can interleave.
+template <class Model, bool kLik, class Args>
+__device__ __forceinline__ void rollout_step(const Args& a, const InstDesc& d,
                                              const typename Model::DynParams& dp,
                                              const typename Model::CostParams& cp, int k, const float* u, int t,
                                              float* x, float& running)
@@ -195,7 +199,7 @@ __device__ __forceinline__ void rollout_step(const RolloutArgs<Model>& a, const 
   float xn[S];
   euler_step<Model>(dp, x, u, xn, a.dt);
   float step_cost = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
-  if (a.use_likelihood)
+  if constexpr (kLik)
   {
     // GaussianDistributionImpl::computeLikelihoodRatioCost (gaussian.cu:490-574)
     const bool zero_mean = (float)k >= (1.0f - a.sh.pure_pct) * (float)d.K;
@@ -215,14 +219,14 @@ __device__ __forceinline__ void rollout_step(const RolloutArgs<Model>& a, const 
 }
 
 // Steps t0 .. t0+nt-1 of sample k from its staged control row.
-template <class Model>
+template <class Model, bool kLik>
 __device__ __forceinline__ void rollout_chunk(const RolloutArgs<Model>& a, const InstDesc& d,
                                               const typename Model::DynParams& dp,
                                               const typename Model::CostParams& cp, int k, const float* urow, int t0,
                                               int nt, float* x, float& running)
 {
   constexpr int C = Model::CONTROL_DIM;
-  auto do_step = [&](const float* u, int t) { rollout_step<Model>(a, d, dp, cp, k, u, t, x, running); };
+  auto do_step = [&](const float* u, int t) { rollout_step<Model, kLik>(a, d, dp, cp, k, u, t, x, running); };
   int tt = 0;
   if constexpr (4 % C == 0)
   {
@@ -310,7 +314,13 @@ __global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ Rol
         }
       }
       __syncthreads();
-      if (active) rollout_chunk<Model>(a, d, dp, cp, k, &stage[tid * ROW], t0, nt, x, running);
+      if (active)
+      {
+        if (a.use_likelihood)
+          rollout_chunk<Model, true>(a, d, dp, cp, k, &stage[tid * ROW], t0, nt, x, running);
+        else
+          rollout_chunk<Model, false>(a, d, dp, cp, k, &stage[tid * ROW], t0, nt, x, running);
+      }
       __syncthreads();
     }
     unsigned int o = kOrderedPosInf;
@@ -398,33 +408,40 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
         return f.injected ? *reinterpret_cast<const float4*>(f.injected + d.u_off + 4 * q)
                           : philox_normal4((uint64_t)q, (uint32_t)w.x, counter, f.seed_lo, f.seed_hi);
       };
-      float4 zn = noise(q0);
-      for (int qi = 0; qi < nq; ++qi)
-      {
-        const float4 z = zn;
-        if (qi + 1 < nq) zn = noise(q0 + qi + 1);
-        const float zz[4] = { z.x, z.y, z.z, z.w };
-        float out[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
+      auto run = [&](auto lik) {
+        float4 zn = noise(q0);
+        for (int qi = 0; qi < nq; ++qi)
         {
-          const int rem = 4 * qi + j;
-          const int t = rem / C, c = rem - t * C;
-          const float m = a.mean[d.t_off + rem];
-          const float sd = f.decay_pow * a.sh.std_dev[c];
-          float u;
-          if (k == 0 || t < f.stride)
-            u = m;
-          else if ((float)k >= pure_threshold)
-            u = sd * zz[j];
-          else
-            u = fmaf(sd, zz[j], m);
-          out[j] = enforce_constraint(u, a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c], a.sh.zero[c]);
-        }
-        *reinterpret_cast<float4*>(dst + 4 * qi) = make_float4(out[0], out[1], out[2], out[3]);
+          const float4 z = zn;
+          if (qi + 1 < nq) zn = noise(q0 + qi + 1);
+          const float zz[4] = { z.x, z.y, z.z, z.w };
+          float out[4];
 #pragma unroll
-        for (int g = 0; g < G; ++g) rollout_step<Model>(a, d, dp, cp, k, out + g * C, qi * G + g, x, running);
-      }
+          for (int j = 0; j < 4; ++j)
+          {
+            const int rem = 4 * qi + j;
+            const int t = rem / C, c = rem - t * C;
+            const float m = a.mean[d.t_off + rem];
+            const float sd = f.decay_pow * a.sh.std_dev[c];
+            float u;
+            if (k == 0 || t < f.stride)
+              u = m;
+            else if ((float)k >= pure_threshold)
+              u = sd * zz[j];
+            else
+              u = fmaf(sd, zz[j], m);
+            out[j] = enforce_constraint(u, a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c], a.sh.zero[c]);
+          }
+          *reinterpret_cast<float4*>(dst + 4 * qi) = make_float4(out[0], out[1], out[2], out[3]);
+#pragma unroll
+          for (int g = 0; g < G; ++g)
+            rollout_step<Model, decltype(lik)::value>(a, d, dp, cp, k, out + g * C, qi * G + g, x, running);
+        }
+      };
+      if (a.use_likelihood)
+        run(std::true_type{});
+      else
+        run(std::false_type{});
     }
     unsigned int o = kOrderedPosInf;
     if (active)
@@ -547,7 +564,14 @@ __global__ void __launch_bounds__(NS) rollout_kernel_bulk(const __grid_constant_
       }
       parity ^= (1u << b);
       const int t0 = j * TCH;
-      if (active) rollout_chunk<Model>(a, d, dp, cp, k, my_stage0 + b * NS * ROW, t0, min(TCH, d.T - t0), x, running);
+      if (active)
+      {
+        if (a.use_likelihood)
+          rollout_chunk<Model, true>(a, d, dp, cp, k, my_stage0 + b * NS * ROW, t0, min(TCH, d.T - t0), x, running);
+        else
+          rollout_chunk<Model, false>(a, d, dp, cp, k, my_stage0 + b * NS * ROW, t0, min(TCH, d.T - t0), x,
+                                      running);
+      }
     }
     uses += nchunks;
     unsigned int o = kOrderedPosInf;

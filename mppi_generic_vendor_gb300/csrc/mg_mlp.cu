@@ -393,30 +393,20 @@ __global__ void __launch_bounds__(128) judge_rollout_kernel(const __grid_constan
 #pragma unroll
   for (int s = 0; s < S; ++s) x[s] = a.r.x0[d.x_off + s];
   float running = 0.0f;
-  const bool zero_mean = (float)k >= (1.0f - a.r.sh.pure_pct) * (float)d.K;
-  for (int t = 0; t < d.T; ++t)
-  {
-    const float2 uv = __ldg(reinterpret_cast<const float2*>(urow + t * C));
-    const float u[2] = { uv.x, uv.y };
-    float xn[S];
-    euler_step<Model>(dp, x, u, xn, a.r.dt);
-    float step_cost = Model::computeStateCost(cp, a.r.aux, xn, t) + Model::computeControlCost(cp, u, t);
-    if (a.r.use_likelihood)
+  // the same step as the analytic rollout kernels; unrolled so the costmap loads of one step overlap the next
+  auto run = [&](auto lik) {
+#pragma unroll 4
+    for (int t = 0; t < d.T; ++t)
     {
-      float lc = 0.0f;
-#pragma unroll
-      for (int c = 0; c < C; ++c)
-      {
-        const float m = zero_mean ? 0.0f : a.r.mean[d.t_off + t * C + c];
-        const float sd = a.r.sh.std_dev[c];
-        lc += a.r.sh.control_cost_coeff[c] * m * (m - 2.0f * u[c]) / (sd * sd);
-      }
-      step_cost += 0.5f * a.r.lambda * (1.0f - a.r.alpha) * lc;
+      const float2 uv = __ldg(reinterpret_cast<const float2*>(urow + t * C));
+      const float u[2] = { uv.x, uv.y };
+      rollout_step<Model, decltype(lik)::value>(a.r, d, dp, cp, k, u, t, x, running);
     }
-    running += step_cost;
-#pragma unroll
-    for (int s = 0; s < S; ++s) x[s] = xn[s];
-  }
+  };
+  if (a.r.use_likelihood)
+    run(std::true_type{});
+  else
+    run(std::false_type{});
   const float tf = (float)d.T;
   a.judged_cost[j] = running / tf + Model::terminalCost(cp, a.r.aux, x) / tf;
 }

@@ -477,7 +477,7 @@ public:
   mppi_status set_launch_config(int ns, int tch, int kc) override
   {
     MG_CHECK(ns == 32 || ns == 64 || ns == 128 || ns == 256, "rollout samples per CTA must be 32, 64, 128 or 256");
-    if (Model::kMlp) ns = 128;  // the tensor-core rollout owns 128-sample tiles
+    if (Model::kMlp) ns = kMlpSamplesPerCta;  // the surrogate rollout's work items are fixed
     MG_CHECK(kc >= 32 && kc <= 256 && (kc % 32) == 0, "reduction samples per CTA must be a multiple of 32 in [32, 256]");
     (void)tch;
     ns_ = ns;
@@ -721,6 +721,7 @@ private:
     MG_TRY(out_bn_h_.alloc((size_t)2 * I_));
     MG_TRY(out_stats_h_.alloc((size_t)3 * I_));
     MG_TRY(status_h_.alloc(1));
+    if (Model::kMlp) ns_ = kMlpSamplesPerCta;
     MG_TRY(build_work_lists());
     MG_TRY(build_colored_tables());
     MG_TRY(build_judge_lists());
@@ -999,9 +1000,19 @@ private:
   }
   // Gaussian noise is generated inside the rollout (rollout_fused_kernel) when every row holds whole quads of steps;
   // the standalone sampler then runs only for mppi_generate_samples.
-  bool fused() const
+  bool fused() const { return sp_.kind == MPPI_SAMPLER_GAUSSIAN && (4 % C) == 0 && use_bulk_; }
+
+  FusedNoise fused_noise_args(int stride, int iter) const
   {
-    return !Model::kMlp && sp_.kind == MPPI_SAMPLER_GAUSSIAN && (4 % C) == 0 && use_bulk_;
+    FusedNoise f;
+    f.samples = samples_d_.p;
+    f.injected = injected_d_.p;
+    f.noise_counter = counters_d_.p + 3;
+    f.seed_lo = (uint32_t)cp_.seed;
+    f.seed_hi = (uint32_t)(cp_.seed >> 32);
+    f.stride = stride;
+    f.decay_pow = powf(sp_.std_dev_decay, (float)iter);
+    return f;
   }
 
   mppi_status launch_rollout(int stride, int iter)
@@ -1027,31 +1038,11 @@ private:
     for (int c = 0; c < C; ++c)
       if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
     a.sh = make_sample_shared(sp_, cc_);
-    if constexpr ((4 % C) == 0)
-      if (fused())
-      {
-        FusedNoise f;
-        f.samples = samples_d_.p;
-        f.injected = injected_d_.p;
-        f.noise_counter = counters_d_.p + 3;
-        f.seed_lo = (uint32_t)cp_.seed;
-        f.seed_hi = (uint32_t)(cp_.seed >> 32);
-        f.stride = stride;
-        f.decay_pow = powf(sp_.std_dev_decay, (float)iter);
-        switch (ns_)
-        {
-          case 32: rollout_fused_kernel<Model, 32><<<rollout_grid_, 32, 0, stream_>>>(a, f); break;
-          case 64: rollout_fused_kernel<Model, 64><<<rollout_grid_, 64, 0, stream_>>>(a, f); break;
-          case 128: rollout_fused_kernel<Model, 128><<<rollout_grid_, 128, 0, stream_>>>(a, f); break;
-          default: rollout_fused_kernel<Model, 256><<<rollout_grid_, 256, 0, stream_>>>(a, f); break;
-        }
-        MG_CUDA(cudaGetLastError());
-        return MPPI_OK;
-      }
     if constexpr (Model::kMlp)
       if (!use_analytic_)
       {
-        MG_TRY(launch_mlp_rollout(a, mlp_d_.p, mlp_precision_, num_sms_, stream_));
+        const FusedNoise fn = fused_noise_args(stride, iter);
+        MG_TRY(launch_mlp_rollout(a, mlp_d_.p, mlp_precision_, fused() ? &fn : nullptr, num_sms_, stream_));
         if (judge_total_ == 0) return MPPI_OK;
         JudgeArgs j;
         j.r = a;
@@ -1064,6 +1055,20 @@ private:
         j.stats = judge_stats_d_.p;
         j.total = judge_total_;
         return launch_judge(j, stream_);
+      }
+    if constexpr ((4 % C) == 0)
+      if (fused())
+      {
+        const FusedNoise f = fused_noise_args(stride, iter);
+        switch (ns_)
+        {
+          case 32: rollout_fused_kernel<Model, 32><<<rollout_grid_, 32, 0, stream_>>>(a, f); break;
+          case 64: rollout_fused_kernel<Model, 64><<<rollout_grid_, 64, 0, stream_>>>(a, f); break;
+          case 128: rollout_fused_kernel<Model, 128><<<rollout_grid_, 128, 0, stream_>>>(a, f); break;
+          default: rollout_fused_kernel<Model, 256><<<rollout_grid_, 256, 0, stream_>>>(a, f); break;
+        }
+        MG_CUDA(cudaGetLastError());
+        return MPPI_OK;
       }
     switch (ns_)
     {

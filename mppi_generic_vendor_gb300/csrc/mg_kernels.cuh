@@ -366,6 +366,41 @@ struct FusedNoise
   float decay_pow;
 };
 
+// setGaussianControls + constraints for the quad of elements rem0 .. rem0+3 of sample k's row (rem = t*C + c), as
+// gaussian_sample_kernel computes them.
+template <int C>
+__device__ __forceinline__ float4 gaussian_quad(const SampleShared& sh, const float* mean_inst, float decay_pow,
+                                                int stride, int k, float pure_threshold, int rem0, float4 z)
+{
+  const float zz[4] = { z.x, z.y, z.z, z.w };
+  float out[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+  {
+    const int rem = rem0 + j;
+    const int t = rem / C, c = rem - t * C;
+    const float m = mean_inst[rem];
+    const float sd = decay_pow * sh.std_dev[c];
+    float u;
+    if (k == 0 || t < stride)
+      u = m;
+    else if ((float)k >= pure_threshold)
+      u = sd * zz[j];
+    else
+      u = fmaf(sd, zz[j], m);
+    out[j] = enforce_constraint(u, sh.lower[c], sh.upper[c], sh.deadband[c], sh.zero[c]);
+  }
+  return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// The four normals of Philox quad q of instance inst (or the injected ones).
+__device__ __forceinline__ float4 fused_noise(const FusedNoise& f, const InstDesc& d, int inst, uint32_t counter,
+                                              long long q)
+{
+  return f.injected ? *reinterpret_cast<const float4*>(f.injected + d.u_off + 4 * q)
+                    : philox_normal4((uint64_t)q, (uint32_t)inst, counter, f.seed_lo, f.seed_hi);
+}
+
 template <class Model, int NS>
 __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant__ RolloutArgs<Model> a,
                                                            const __grid_constant__ FusedNoise f)
@@ -404,35 +439,15 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
       const long long q0 = (long long)k * nq;
       const float pure_threshold = (1.0f - a.sh.pure_pct) * (float)d.K;
       float* dst = f.samples + d.u_off + 4 * q0;
-      auto noise = [&](long long q) {
-        return f.injected ? *reinterpret_cast<const float4*>(f.injected + d.u_off + 4 * q)
-                          : philox_normal4((uint64_t)q, (uint32_t)w.x, counter, f.seed_lo, f.seed_hi);
-      };
       auto run = [&](auto lik) {
-        float4 zn = noise(q0);
+        float4 zn = fused_noise(f, d, w.x, counter, q0);
         for (int qi = 0; qi < nq; ++qi)
         {
           const float4 z = zn;
-          if (qi + 1 < nq) zn = noise(q0 + qi + 1);
-          const float zz[4] = { z.x, z.y, z.z, z.w };
-          float out[4];
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-          {
-            const int rem = 4 * qi + j;
-            const int t = rem / C, c = rem - t * C;
-            const float m = a.mean[d.t_off + rem];
-            const float sd = f.decay_pow * a.sh.std_dev[c];
-            float u;
-            if (k == 0 || t < f.stride)
-              u = m;
-            else if ((float)k >= pure_threshold)
-              u = sd * zz[j];
-            else
-              u = fmaf(sd, zz[j], m);
-            out[j] = enforce_constraint(u, a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c], a.sh.zero[c]);
-          }
-          *reinterpret_cast<float4*>(dst + 4 * qi) = make_float4(out[0], out[1], out[2], out[3]);
+          if (qi + 1 < nq) zn = fused_noise(f, d, w.x, counter, q0 + qi + 1);
+          const float4 o = gaussian_quad<C>(a.sh, a.mean + d.t_off, f.decay_pow, f.stride, k, pure_threshold, 4 * qi, z);
+          *reinterpret_cast<float4*>(dst + 4 * qi) = o;
+          const float out[4] = { o.x, o.y, o.z, o.w };
 #pragma unroll
           for (int g = 0; g < G; ++g)
             rollout_step<Model, decltype(lik)::value>(a, d, dp, cp, k, out + g * C, qi * G + g, x, running);

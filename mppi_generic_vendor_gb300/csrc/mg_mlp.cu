@@ -1,6 +1,6 @@
 // mg_mlp.cu — tensor-core evaluation of the surrogate MLP: a standalone forward entry point and the rollout kernel of
 // the MLP bicycle model (the per-timestep inference over all samples is one BF16 tcgen05 GEMM chain per 128-sample
-// tile, FP32 accumulation in TMEM; see mg_mlp.cuh).
+// tile, FP32 accumulation in TMEM; see mg_mlp.cuh).  The rollout's work items hold kMlpTiles tiles of one instance.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -12,11 +12,13 @@ namespace mg
 {
 namespace
 {
-// Every CTA of the MLP kernels allocates MlpSmem::TMEM_COLS = 64 TMEM columns and holds MlpSmem::TOTAL bytes of
-// dynamic shared memory (+ alignment slack).  At most 6 such CTAs fit an SM's 228 KB of shared memory, 384 of its 512
-// columns, so an allocation never waits on another CTA's columns.
-constexpr size_t kMlpSmem = MlpSmem::TOTAL + 1024;
-constexpr int kMlpMaxCtasPerSm = 512 / MlpSmem::TMEM_COLS;
+// The standalone forward runs one 128-row tile per CTA (64 TMEM columns, MlpSmem::total(1) bytes of shared memory:
+// at most 7 CTAs per SM, 448 columns).  The rollout runs kMlpTiles tiles per CTA (128 columns; its shared-memory
+// request is rounded up so at most 4 CTAs share an SM, 512 columns).  Either way the columns of co-resident CTAs fit
+// the SM's 512, so an allocation never waits for another CTA.
+constexpr size_t kMlpFwdSmem = MlpSmem::total(1) + 1024;
+constexpr size_t kMlpRolloutSmem = 56 * 1024;
+static_assert(MlpSmem::total(kMlpTiles) + 1024 <= (int)kMlpRolloutSmem, "rollout tile buffers");
 
 __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, const float* X, float* Y, int B,
                                                           unsigned int* status)
@@ -28,7 +30,7 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, c
   const int tid = threadIdx.x, warp = tid >> 5;
   if (warp == 0)
   {
-    tmem_alloc(&s_tmem, MlpSmem::TMEM_COLS);
+    tmem_alloc(&s_tmem, MlpSmem::tmem_cols(1));
     tmem_relinquish();
   }
   if (tid == 0)
@@ -47,18 +49,18 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, c
   for (int tile = blockIdx.x; tile * 128 < B; tile += gridDim.x)
   {
     const int row = tile * 128 + tid;
-    float x[kMlpIn], y[kMlpOut];
+    float x[1][kMlpIn], y[1][kMlpOut];
 #pragma unroll
-    for (int i = 0; i < kMlpIn; ++i) x[i] = row < B ? (X[(size_t)row * kMlpIn + i] - nrm[i]) * nrm[32 + i] : 0.0f;
-    if (!mlp_tile_forward(sm, taddr, &mbar, phase, &s_fail, x, y)) break;
+    for (int i = 0; i < kMlpIn; ++i) x[0][i] = row < B ? (X[(size_t)row * kMlpIn + i] - nrm[i]) * nrm[32 + i] : 0.0f;
+    if (!mlp_tile_forward<1>(sm, taddr, &mbar, phase, &s_fail, x, y)) break;
     if (row < B)
 #pragma unroll
-      for (int j = 0; j < kMlpOut; ++j) Y[(size_t)row * kMlpOut + j] = y[j] * nrm[23 + j] + nrm[18 + j];
+      for (int j = 0; j < kMlpOut; ++j) Y[(size_t)row * kMlpOut + j] = y[0][j] * nrm[23 + j] + nrm[18 + j];
   }
   tc_fence_before_sync();
   __syncthreads();
   if (tid == 0 && s_fail) atomicOr(status, 1u);
-  if (warp == 0) tmem_dealloc(taddr, MlpSmem::TMEM_COLS);
+  if (warp == 0) tmem_dealloc(taddr, MlpSmem::tmem_cols(1));
 }
 
 // Plain FP32 surrogate evaluation on the CUDA cores, one thread per sample, as FNNHelper::forward evaluates it
@@ -101,16 +103,21 @@ __device__ __forceinline__ void mlp_thread_forward(const float* P, const float* 
 }
 
 // Surrogate rollout: BicycleSlipModel with the (yaw, vx, vy, yaw_rate, steer) derivatives from the MLP and the
-// x / y rows analytic (NeuralNetModel::computeKinematics, ar_nn_model.cu:119-124).  Persistent CTAs walk 128-sample
-// tiles; the Euler step, the costmap cost and the likelihood term follow rolloutKernel (mppi_common.cu:105-152)
-// exactly as the analytic rollout does.  kTensor: the network runs on the tensor cores (mlp_tile_forward, BF16 or
-// FP8 weights); otherwise in plain FP32 on the CUDA cores (mlp_thread_forward).
-template <bool kTensor>
-__global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant__ RolloutArgs<BicycleSlipMLPModel> a,
-                                                          const float* mlp)
+// x / y rows analytic (NeuralNetModel::computeKinematics, ar_nn_model.cu:119-124).  Persistent CTAs of 128 threads
+// walk work items of 128 * kMlpTiles samples of one instance; thread i owns row i of every tile (samples
+// first + i + 128 n).  The Euler step, the costmap cost and the likelihood term follow rolloutKernel
+// (mppi_common.cu:105-152) exactly as the analytic rollout does.  kTensor: the network runs on the tensor cores
+// (mlp_tile_forward, BF16 or FP8 weights, one MMA round trip per layer for all tiles of the CTA); otherwise in plain
+// FP32 on the CUDA cores (mlp_thread_forward).
+template <bool kTensor, bool kFused>
+__global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
+    const __grid_constant__ RolloutArgs<BicycleSlipMLPModel> a, const float* mlp, const __grid_constant__ FusedNoise f)
 {
   using Model = BicycleSlipMLPModel;
-  constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM;
+  // tensor cores: 128 threads, each owning row i of kMlpTiles tiles; CUDA cores: one thread per sample
+  constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM, NT = kTensor ? kMlpTiles : 1;
+  static_assert(C == 2, "a fused noise quad holds two steps");
+  const uint32_t counter = (kFused && f.noise_counter) ? *f.noise_counter : 0u;
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t s_tmem;
@@ -123,7 +130,7 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
   {
     if (warp == 0)
     {
-      tmem_alloc(&s_tmem, MlpSmem::TMEM_COLS);
+      tmem_alloc(&s_tmem, MlpSmem::tmem_cols(NT));
       tmem_relinquish();
     }
     if (tid == 0)
@@ -158,68 +165,111 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
     if (tile >= a.num_tiles) break;
     const int2 w = a.tiles[tile];
     const InstDesc d = a.inst[w.x];
-    const int k = w.y + tid;
-    const bool active = k < d.K;
-    const typename Model::CostParams& cp = a.cost[w.x];
-    const float* urow = a.samples + d.u_off + (long long)(active ? k : w.y) * d.T * C;
-    float x[S];
+    const typename Model::CostParams cp = a.cost[w.x];
+    int k[NT];
+    bool active[NT];
+    const float* urow[NT];
+    float x[NT][S], running[NT];
+    float2 u_next[NT];
+    float4 uq[NT];  // kFused: the quad (steps t, t+1) generated for each row
+    const float pure_threshold = (1.0f - a.sh.pure_pct) * (float)d.K;
+    const long long nq_row = d.T * C / 4;
 #pragma unroll
-    for (int i = 0; i < S; ++i) x[i] = a.x0[d.x_off + i];
-    float running = 0.0f;
-    float2 u_next = active ? __ldg(reinterpret_cast<const float2*>(urow)) : make_float2(0.0f, 0.0f);
+    for (int n = 0; n < NT; ++n)
+    {
+      k[n] = w.y + tid + 128 * n;  // NT == 1 on the CUDA cores, where tid spans the whole work item
+      active[n] = k[n] < d.K;
+      urow[n] = a.samples + d.u_off + (long long)(active[n] ? k[n] : w.y) * d.T * C;
+#pragma unroll
+      for (int i = 0; i < S; ++i) x[n][i] = a.x0[d.x_off + i];
+      running[n] = 0.0f;
+      uq[n] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      u_next[n] = (!kFused && active[n]) ? __ldg(reinterpret_cast<const float2*>(urow[n])) : make_float2(0.0f, 0.0f);
+    }
     for (int t = 0; t < d.T && ok; ++t)
     {
-      const float u[2] = { u_next.x, u_next.y };
-      if (active && t + 1 < d.T) u_next = __ldg(reinterpret_cast<const float2*>(urow + (t + 1) * C));
-      float xin[kMlpIn], y[kMlpOut];
+      float u[NT][2], xin[NT][kMlpIn], y[NT][kMlpOut];
+#pragma unroll
+      for (int n = 0; n < NT; ++n)
+      {
+        if constexpr (kFused)
+        {
+          // Gaussian sampling fused in, quad by quad, exactly as gaussian_sample_kernel would have written it
+          if ((t & 1) == 0 && active[n])
+          {
+            const long long q = (long long)k[n] * nq_row + (t >> 1);
+            uq[n] = gaussian_quad<C>(a.sh, a.mean + d.t_off, f.decay_pow, f.stride, k[n], pure_threshold, t * C,
+                                     fused_noise(f, d, w.x, counter, q));
+            *reinterpret_cast<float4*>(f.samples + d.u_off + 4 * q) = uq[n];
+          }
+          u[n][0] = (t & 1) ? uq[n].z : uq[n].x;
+          u[n][1] = (t & 1) ? uq[n].w : uq[n].y;
+        }
+        else
+        {
+          u[n][0] = u_next[n].x;
+          u[n][1] = u_next[n].y;
+          if (active[n] && t + 1 < d.T) u_next[n] = __ldg(reinterpret_cast<const float2*>(urow[n] + (t + 1) * C));
+        }
+        if constexpr (kTensor)
+        {
+          // the inputs are rounded to BF16 next, so a multiply by the stored reciprocal stands in for the division
+#pragma unroll
+          for (int i = 0; i < S; ++i) xin[n][i] = (x[n][i] - nrm[i]) * nrm[32 + i];
+          xin[n][7] = (u[n][0] - nrm[7]) * nrm[32 + 7];
+          xin[n][8] = (u[n][1] - nrm[8]) * nrm[32 + 8];
+        }
+        else
+        {
+#pragma unroll
+          for (int i = 0; i < S; ++i) xin[n][i] = (x[n][i] - nrm[i]) / nrm[9 + i];
+          xin[n][7] = (u[n][0] - nrm[7]) / nrm[16];
+          xin[n][8] = (u[n][1] - nrm[8]) / nrm[17];
+        }
+      }
       if constexpr (kTensor)
       {
-        // the inputs are rounded to BF16 next, so a multiply by the stored reciprocal stands in for the division
-#pragma unroll
-        for (int i = 0; i < S; ++i) xin[i] = (x[i] - nrm[i]) * nrm[32 + i];
-        xin[7] = (u[0] - nrm[7]) * nrm[32 + 7];
-        xin[8] = (u[1] - nrm[8]) * nrm[32 + 8];
-        ok = mlp_tile_forward(sm, taddr, &mbar, phase, &s_fail, xin, y);
+        ok = mlp_tile_forward<NT>(sm, taddr, &mbar, phase, &s_fail, xin, y);
         if (!ok) break;
       }
       else
       {
-#pragma unroll
-        for (int i = 0; i < S; ++i) xin[i] = (x[i] - nrm[i]) / nrm[9 + i];
-        xin[7] = (u[0] - nrm[7]) / nrm[16];
-        xin[8] = (u[1] - nrm[8]) / nrm[17];
-        mlp_thread_forward(pf, xin, y);
+        mlp_thread_forward(pf, xin[0], y[0]);
       }
-      float xd[S];
-      float sy, cy;
-      sincos_f(x[2], &sy, &cy);
-      xd[0] = x[3] * cy - x[4] * sy;
-      xd[1] = x[3] * sy + x[4] * cy;
 #pragma unroll
-      for (int j = 0; j < kMlpOut; ++j) xd[2 + j] = y[j] * nrm[23 + j] + nrm[18 + j];
-      float xn[S];
-#pragma unroll
-      for (int i = 0; i < S; ++i) xn[i] = fmaf(xd[i], a.dt, x[i]);
-      if (active)
+      for (int n = 0; n < NT; ++n)
       {
-        float step_cost = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
-        if (a.use_likelihood)
+        float xd[S];
+        float sy, cy;
+        sincos_f(x[n][2], &sy, &cy);
+        xd[0] = x[n][3] * cy - x[n][4] * sy;
+        xd[1] = x[n][3] * sy + x[n][4] * cy;
+#pragma unroll
+        for (int j = 0; j < kMlpOut; ++j) xd[2 + j] = y[n][j] * nrm[23 + j] + nrm[18 + j];
+        float xn[S];
+#pragma unroll
+        for (int i = 0; i < S; ++i) xn[i] = fmaf(xd[i], a.dt, x[n][i]);
+        if (active[n])
         {
-          const bool zero_mean = (float)k >= (1.0f - a.sh.pure_pct) * (float)d.K;
-          float lc = 0.0f;
-#pragma unroll
-          for (int c = 0; c < C; ++c)
+          float step_cost = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u[n], t);
+          if (a.use_likelihood)
           {
-            const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + c];
-            const float sd = a.sh.std_dev[c];
-            lc += a.sh.control_cost_coeff[c] * m * (m - 2.0f * u[c]) / (sd * sd);
-          }
-          step_cost += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
-        }
-        running += step_cost;
-      }
+            const bool zero_mean = (float)k[n] >= (1.0f - a.sh.pure_pct) * (float)d.K;
+            float lc = 0.0f;
 #pragma unroll
-      for (int i = 0; i < S; ++i) x[i] = xn[i];
+            for (int c = 0; c < C; ++c)
+            {
+              const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + c];
+              const float sd = a.sh.std_dev[c];
+              lc += a.sh.control_cost_coeff[c] * m * (m - 2.0f * u[n][c]) / (sd * sd);
+            }
+            step_cost += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
+          }
+          running[n] += step_cost;
+        }
+#pragma unroll
+        for (int i = 0; i < S; ++i) x[n][i] = xn[i];
+      }
     }
     if (!ok)
     {
@@ -227,13 +277,15 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
       break;
     }
     unsigned int o = kOrderedPosInf;
-    if (active)
-    {
-      const float tf = (float)d.T;
-      const float cost = running / tf + Model::terminalCost(cp, a.aux, x) / tf;
-      a.costs[d.k_off + k] = cost;
-      o = float_to_ordered(cost);
-    }
+#pragma unroll
+    for (int n = 0; n < NT; ++n)
+      if (active[n])
+      {
+        const float tf = (float)d.T;
+        const float cost = running[n] / tf + Model::terminalCost(cp, a.aux, x[n]) / tf;
+        a.costs[d.k_off + k[n]] = cost;
+        o = min(o, float_to_ordered(cost));
+      }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) o = min(o, __shfl_xor_sync(0xffffffffu, o, off));
     if ((tid & 31) == 0) atomicMin(&s_min, o);
@@ -249,7 +301,7 @@ __global__ void __launch_bounds__(128) rollout_mlp_kernel(const __grid_constant_
   {
     tc_fence_before_sync();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(taddr, MlpSmem::TMEM_COLS);
+    if (warp == 0) tmem_dealloc(taddr, MlpSmem::tmem_cols(NT));
   }
   if (tid == 0)
   {
@@ -465,17 +517,20 @@ __global__ void __launch_bounds__(256) judge_finalize_kernel(const __grid_consta
 }  // namespace
 
 mppi_status launch_mlp_rollout(const RolloutArgs<BicycleSlipMLPModel>& a, const float* mlp_d, int precision,
-                               int num_sms, cudaStream_t s)
+                               const FusedNoise* fused, int num_sms, cudaStream_t s)
 {
   const bool tensor = precision != 2;
-  auto kern = tensor ? rollout_mlp_kernel<true> : rollout_mlp_kernel<false>;
-  const size_t smem = tensor ? kMlpSmem : sizeof(float) * kMlpDevParams;
+  auto kern = tensor ? (fused ? rollout_mlp_kernel<true, true> : rollout_mlp_kernel<true, false>)
+                     : (fused ? rollout_mlp_kernel<false, true> : rollout_mlp_kernel<false, false>);
+  FusedNoise f{};
+  if (fused) f = *fused;
+  const size_t smem = tensor ? kMlpRolloutSmem : sizeof(float) * kMlpDevParams;
   MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 1;
-  MG_CUDA(resident_ctas_per_sm(kern, 128, smem, &per_sm));
-  per_sm = std::max(1, tensor ? std::min(per_sm, kMlpMaxCtasPerSm) : per_sm);
+  MG_CUDA(resident_ctas_per_sm(kern, tensor ? 128 : kMlpSamplesPerCta, smem, &per_sm));
+  per_sm = std::max(1, tensor ? std::min(per_sm, (int)(512 / MlpSmem::tmem_cols(kMlpTiles))) : per_sm);
   const int grid = std::max(1, std::min(a.num_tiles, per_sm * num_sms));
-  kern<<<grid, 128, smem, s>>>(a, mlp_d);
+  kern<<<grid, tensor ? 128 : kMlpSamplesPerCta, smem, s>>>(a, mlp_d, f);
   MG_CUDA(cudaGetLastError());
   return MPPI_OK;
 }
@@ -579,10 +634,10 @@ mppi_status mppi_kernel_mlp_forward(const float* params, int precision, const fl
       break;
     if ((e = cudaMemsetAsync(status, 0, sizeof(unsigned int), s)) != cudaSuccess) break;
     if ((e = cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kMlpSmem)) != cudaSuccess)
+                                  (int)kMlpFwdSmem)) != cudaSuccess)
       break;
     const int tiles = (batch + 127) / 128;
-    mlp_forward_kernel<<<std::min(tiles, 8192), 128, kMlpSmem, s>>>(p_d, X_d, Y_d, batch, status);
+    mlp_forward_kernel<<<std::min(tiles, 8192), 128, kMlpFwdSmem, s>>>(p_d, X_d, Y_d, batch, status);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     unsigned int h = 0;
     if ((e = cudaMemcpyAsync(&h, status, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;

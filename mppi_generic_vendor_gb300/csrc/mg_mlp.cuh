@@ -25,21 +25,30 @@ static_assert(kMlpNumParams == MPPI_MLP_PARAMS, "MLP parameter layout");
 // E4M3 values q with W = q * scale, the scale applied to the FP32 accumulator in the epilogue.
 constexpr int kMlpScale = kMlpNumParams, kMlpDevParams = kMlpScale + 3;
 
-// Shared-memory map of one MLP tile (bytes from a 1024-byte aligned base).
+// Tiles of 128 samples per CTA of the surrogate rollout; its work items hold kMlpSamplesPerCta samples of one
+// instance.
+constexpr int kMlpTiles = 2;
+constexpr int kMlpSamplesPerCta = 128 * kMlpTiles;
+
+// Shared-memory map of an MLP CTA that evaluates NT tiles of 128 rows (bytes from a 1024-byte aligned base).  Each
+// tile owns one 128 x 64 BF16 activation buffer: the 128 x 16 input rows of layer 1 sit in its first 4 KB (dead once
+// the layer-1 MMA has completed), then hidden 1, then hidden 2 overwrite it, each after the MMA that read the previous
+// contents has completed.
 struct MlpSmem
 {
   static constexpr int W1 = 0;          // 64 x 16 bf16
   static constexpr int W2 = 2048;       // 64 x 64 bf16
   static constexpr int W3 = 10240;      // 16 x 64 bf16
-  static constexpr int A1 = 12288;      // 128 x 16 bf16
-  static constexpr int A2 = 16384;      // 128 x 64 bf16 (hidden 1, then hidden 2)
-  static constexpr int BIAS = 32768;    // fp32 b1[64] b2[64] b3[16]
-  static constexpr int NORM = 33792;    // fp32 in_mean[9] in_std[9] out_mean[5] out_std[5] layer_scale[3] pad
+  static constexpr int BIAS = 12288;    // fp32 b1[64] b2[64] b3[16]
+  static constexpr int NORM = 13312;    // fp32 in_mean[9] in_std[9] out_mean[5] out_std[5] layer_scale[3] pad
                                         //      1/in_std[9] (from float 32)
-  static constexpr int TOTAL = 34048;
-  // One 64-column accumulator serves all three layers: each layer's result is read back into shared memory before
-  // the next layer's MMA is issued.
-  static constexpr uint32_t TMEM_COLS = 64;
+  static constexpr int ACT = 14336;     // NT x (128 x 64 bf16)
+  static constexpr int ACT_BYTES = 16384;
+  __host__ __device__ static constexpr int total(int nt) { return ACT + nt * ACT_BYTES; }
+  // One 64-column accumulator per tile serves all three layers: each layer's result is read back into shared memory
+  // before the next layer's MMA is issued.
+  static constexpr uint32_t TILE_COLS = 64;
+  __host__ __device__ static constexpr uint32_t tmem_cols(int nt) { return nt == 1 ? 64u : nt == 2 ? 128u : 256u; }
 };
 
 // Byte offset of element (row, k) in the K-major core-matrix layout of a tile whose K extent is KD.
@@ -85,12 +94,15 @@ __device__ __forceinline__ void mlp_load_weights(unsigned char* sm, const float*
   for (int e = tid; e < kMlpIn; e += nt) nrm[32 + e] = 1.0f / params[kMlpInStd + e];  // input scale reciprocals
 }
 
-// One forward pass of the tile.  Thread i provides its normalised input row xin[9] and receives yout[5]
-// (normalised outputs).  A bounded wait that gives up sets *fail (shared); every thread reads the flag after the
-// next CTA barrier, so the pass returns false on all threads together (the caller stops and frees TMEM).  A failure
-// in the last layer surfaces at the caller's next barrier.
+// One forward pass of NT tiles.  Thread i provides the normalised input rows xin[n][9] of rows i of tiles n and
+// receives yout[n][5] (normalised outputs).  Per layer every tile's MMAs are issued by thread 0 and committed to one
+// mbarrier, so the CTA pays one round trip per layer for all of its tiles.  A bounded wait that gives up sets *fail
+// (shared); every thread reads the flag after the next CTA barrier, so the pass returns false on all threads together
+// (the caller stops and frees TMEM).  A failure in the last layer surfaces at the caller's next barrier.
+template <int NT>
 __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t taddr, uint64_t* mbar, uint32_t& phase,
-                                                 volatile int* fail, const float* xin, float* yout)
+                                                 volatile int* fail, const float (*xin)[kMlpIn],
+                                                 float (*yout)[kMlpOut])
 {
   const int m = threadIdx.x, warp = m >> 5;
   const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
@@ -101,17 +113,21 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   constexpr uint32_t kId64 = umma_idesc_bf16_f32(128, 64);
   constexpr uint32_t kId16 = umma_idesc_bf16_f32(128, 16);
 
-  // ---- layer 1
+  // ---- layer 1: inputs padded from 9 to 16 columns
+#pragma unroll
+  for (int n = 0; n < NT; ++n)
   {
+    const float* x = xin[n];
     uint4 c0, c1;
-    c0.x = pack_bf16(xin[0], xin[1]);
-    c0.y = pack_bf16(xin[2], xin[3]);
-    c0.z = pack_bf16(xin[4], xin[5]);
-    c0.w = pack_bf16(xin[6], xin[7]);
-    c1.x = pack_bf16(xin[8], 0.0f);
+    c0.x = pack_bf16(x[0], x[1]);
+    c0.y = pack_bf16(x[2], x[3]);
+    c0.z = pack_bf16(x[4], x[5]);
+    c0.w = pack_bf16(x[6], x[7]);
+    c1.x = pack_bf16(x[8], 0.0f);
     c1.y = c1.z = c1.w = 0u;
-    *reinterpret_cast<uint4*>(sm + MlpSmem::A1 + core_off(m, 0, 16)) = c0;
-    *reinterpret_cast<uint4*>(sm + MlpSmem::A1 + core_off(m, 8, 16)) = c1;
+    unsigned char* a1 = sm + MlpSmem::ACT + n * MlpSmem::ACT_BYTES;
+    *reinterpret_cast<uint4*>(a1 + core_off(m, 0, 16)) = c0;
+    *reinterpret_cast<uint4*>(a1 + core_off(m, 8, 16)) = c1;
   }
   fence_proxy_async_smem();
   tc_fence_before_sync();
@@ -120,100 +136,88 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   if (m == 0)
   {
     tc_fence_after_sync();
-    umma_bf16(taddr + 0, umma_smem_desc(sbase + MlpSmem::A1, 128, 256), umma_smem_desc(sbase + MlpSmem::W1, 128, 256),
-              kId64, 0u);
+#pragma unroll
+    for (int n = 0; n < NT; ++n)
+      umma_bf16(taddr + n * MlpSmem::TILE_COLS,
+                umma_smem_desc(sbase + MlpSmem::ACT + n * MlpSmem::ACT_BYTES, 128, 256),
+                umma_smem_desc(sbase + MlpSmem::W1, 128, 256), kId64, 0u);
     umma_commit(mbar);
   }
   if (!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins)) *fail = 1;
   phase ^= 1u;
   tc_fence_after_sync();
+
+  // ---- hidden layers 1 and 2: bias + tanh epilogue into the tile's activation buffer, then the next GEMM
 #pragma unroll
-  for (int q = 0; q < 4; ++q)
+  for (int layer = 0; layer < 2; ++layer)
   {
-    float v[16];
-    tmem_ld16(taddr + lane_base + 16 * q, v);
-    tmem_ld_wait();
+    const float sc = layer == 0 ? s1 : s2;
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
+    for (int n = 0; n < NT; ++n)
     {
-      uint4 c;
-      const float* b = bias + 16 * q + 8 * h;
-      const float* x = v + 8 * h;
-      c.x = pack_bf16(tanh_fast(fmaf(x[0], s1, b[0])), tanh_fast(fmaf(x[1], s1, b[1])));
-      c.y = pack_bf16(tanh_fast(fmaf(x[2], s1, b[2])), tanh_fast(fmaf(x[3], s1, b[3])));
-      c.z = pack_bf16(tanh_fast(fmaf(x[4], s1, b[4])), tanh_fast(fmaf(x[5], s1, b[5])));
-      c.w = pack_bf16(tanh_fast(fmaf(x[6], s1, b[6])), tanh_fast(fmaf(x[7], s1, b[7])));
-      *reinterpret_cast<uint4*>(sm + MlpSmem::A2 + core_off(m, 16 * q + 8 * h, 64)) = c;
+      unsigned char* act = sm + MlpSmem::ACT + n * MlpSmem::ACT_BYTES;
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+      {
+        float v[16];
+        tmem_ld16(taddr + n * MlpSmem::TILE_COLS + lane_base + 16 * q, v);
+        tmem_ld_wait();
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+        {
+          uint4 c;
+          const float* b = bias + 64 * layer + 16 * q + 8 * h;
+          const float* x = v + 8 * h;
+          c.x = pack_bf16(tanh_fast(fmaf(x[0], sc, b[0])), tanh_fast(fmaf(x[1], sc, b[1])));
+          c.y = pack_bf16(tanh_fast(fmaf(x[2], sc, b[2])), tanh_fast(fmaf(x[3], sc, b[3])));
+          c.z = pack_bf16(tanh_fast(fmaf(x[4], sc, b[4])), tanh_fast(fmaf(x[5], sc, b[5])));
+          c.w = pack_bf16(tanh_fast(fmaf(x[6], sc, b[6])), tanh_fast(fmaf(x[7], sc, b[7])));
+          *reinterpret_cast<uint4*>(act + core_off(m, 16 * q + 8 * h, 64)) = c;
+        }
+      }
     }
-  }
-  // ---- layer 2
-  fence_proxy_async_smem();
-  tc_fence_before_sync();
-  __syncthreads();
-  if (*fail) return false;  // CTA-uniform: read after the barrier
-  if (m == 0)
-  {
-    tc_fence_after_sync();
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      umma_bf16(taddr, umma_smem_desc(sbase + MlpSmem::A2 + 256 * k, 128, 1024),
-                umma_smem_desc(sbase + MlpSmem::W2 + 256 * k, 128, 1024), kId64, k > 0 ? 1u : 0u);
-    umma_commit(mbar);
-  }
-  if (!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins)) *fail = 1;
-  phase ^= 1u;
-  tc_fence_after_sync();
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-  {
-    float v[16];
-    tmem_ld16(taddr + lane_base + 16 * q, v);
-    tmem_ld_wait();
-#pragma unroll
-    for (int h = 0; h < 2; ++h)
+    fence_proxy_async_smem();
+    tc_fence_before_sync();
+    __syncthreads();
+    if (*fail) return false;  // CTA-uniform: read after the barrier
+    if (m == 0)
     {
-      uint4 c;
-      const float* b = bias + 64 + 16 * q + 8 * h;
-      const float* x = v + 8 * h;
-      c.x = pack_bf16(tanh_fast(fmaf(x[0], s2, b[0])), tanh_fast(fmaf(x[1], s2, b[1])));
-      c.y = pack_bf16(tanh_fast(fmaf(x[2], s2, b[2])), tanh_fast(fmaf(x[3], s2, b[3])));
-      c.z = pack_bf16(tanh_fast(fmaf(x[4], s2, b[4])), tanh_fast(fmaf(x[5], s2, b[5])));
-      c.w = pack_bf16(tanh_fast(fmaf(x[6], s2, b[6])), tanh_fast(fmaf(x[7], s2, b[7])));
-      *reinterpret_cast<uint4*>(sm + MlpSmem::A2 + core_off(m, 16 * q + 8 * h, 64)) = c;
-    }
-  }
-  // ---- layer 3 (linear)
-  fence_proxy_async_smem();
-  tc_fence_before_sync();
-  __syncthreads();
-  if (*fail) return false;  // CTA-uniform: read after the barrier
-  if (m == 0)
-  {
-    tc_fence_after_sync();
+      tc_fence_after_sync();
+      const uint32_t wb = sbase + (layer == 0 ? MlpSmem::W2 : MlpSmem::W3);
+      const uint32_t id = layer == 0 ? kId64 : kId16;
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-      umma_bf16(taddr, umma_smem_desc(sbase + MlpSmem::A2 + 256 * k, 128, 1024),
-                umma_smem_desc(sbase + MlpSmem::W3 + 256 * k, 128, 1024), kId16, k > 0 ? 1u : 0u);
-    umma_commit(mbar);
+      for (int n = 0; n < NT; ++n)
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          umma_bf16(taddr + n * MlpSmem::TILE_COLS,
+                    umma_smem_desc(sbase + MlpSmem::ACT + n * MlpSmem::ACT_BYTES + 256 * k, 128, 1024),
+                    umma_smem_desc(wb + 256 * k, 128, 1024), id, k > 0 ? 1u : 0u);
+      umma_commit(mbar);
+    }
+    if (!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins)) *fail = 1;
+    phase ^= 1u;
+    tc_fence_after_sync();
   }
-  if (!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins)) *fail = 1;
-  phase ^= 1u;
-  tc_fence_after_sync();
+
+  // ---- linear output layer
+#pragma unroll
+  for (int n = 0; n < NT; ++n)
   {
     float v[16];
-    tmem_ld16(taddr + lane_base, v);
+    tmem_ld16(taddr + n * MlpSmem::TILE_COLS + lane_base, v);
     tmem_ld_wait();
 #pragma unroll
-    for (int j = 0; j < kMlpOut; ++j) yout[j] = fmaf(v[j], s3, bias[128 + j]);
+    for (int j = 0; j < kMlpOut; ++j) yout[n][j] = fmaf(v[j], s3, bias[128 + j]);
   }
   tc_fence_before_sync();
   return true;
 }
 
 // Rollout of the MLP bicycle model over every instance (defined in mg_mlp.cu).
-// precision 0 / 1: tensor cores with BF16 / FP8 weights; 2: plain FP32 on the CUDA cores.
+// precision 0 / 1: tensor cores with BF16 / FP8 weights; 2: plain FP32 on the CUDA cores.  fused (may be null):
+// generate the Gaussian control samples inside the rollout (every instance has T*C % 4 == 0).
 mppi_status launch_mlp_rollout(const RolloutArgs<BicycleSlipMLPModel>& a, const float* mlp_d, int precision,
-                               int num_sms, cudaStream_t s);
+                               const FusedNoise* fused, int num_sms, cudaStream_t s);
 
 // Analytic judge of the surrogate rollout.  Per instance the M lowest surrogate costs (M = ceil(fraction * K), the
 // samples that carry the weight) are re-rolled with the analytic BicycleSlipModel in FP32.  Their costs become

@@ -12,13 +12,12 @@ namespace mg
 {
 namespace
 {
-// The standalone forward runs one 128-row tile per CTA (64 TMEM columns, MlpSmem::total(1) bytes of shared memory:
-// at most 7 CTAs per SM, 448 columns).  The rollout runs kMlpTiles tiles per CTA (128 columns; its shared-memory
-// request is rounded up so at most 4 CTAs share an SM, 512 columns).  Either way the columns of co-resident CTAs fit
-// the SM's 512, so an allocation never waits for another CTA.
+// A CTA of NT tiles holds MlpSmem::total(NT) bytes of shared memory (+ alignment slack) and MlpSmem::tmem_cols(NT)
+// TMEM columns: 31 KB and 64 columns for one tile (at most 7 CTAs per SM, 448 columns), 49 KB and 128 columns for two
+// (at most 4, 512 columns).  The columns of co-resident CTAs therefore fit the SM's 512, so an allocation never waits
+// for another CTA.
 constexpr size_t kMlpFwdSmem = MlpSmem::total(1) + 1024;
-constexpr size_t kMlpRolloutSmem = 56 * 1024;
-static_assert(MlpSmem::total(kMlpTiles) + 1024 <= (int)kMlpRolloutSmem, "rollout tile buffers");
+constexpr size_t kMlpRolloutSmem = MlpSmem::total(kMlpTiles) + 1024;
 
 __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, const float* X, float* Y, int B,
                                                           unsigned int* status)

@@ -26,8 +26,9 @@ static_assert(kMlpNumParams == MPPI_MLP_PARAMS, "MLP parameter layout");
 constexpr int kMlpScale = kMlpNumParams, kMlpDevParams = kMlpScale + 3;
 
 // Tiles of 128 samples per CTA of the surrogate rollout; its work items hold kMlpSamplesPerCta samples of one
-// instance.
-constexpr int kMlpTiles = 2;
+// instance.  One tile per CTA measured fastest: two tiles per CTA halve the MMA round trips per tile but double the
+// epilogue work between barriers and cut the resident CTAs per SM from 7 to 4, which cost more than they saved.
+constexpr int kMlpTiles = 1;
 constexpr int kMlpSamplesPerCta = 128 * kMlpTiles;
 
 // Shared-memory map of an MLP CTA that evaluates NT tiles of 128 rows (bytes from a 1024-byte aligned base).  Each

@@ -184,38 +184,78 @@ struct RolloutArgs
   SampleShared sh;
 };
 
-// One step t of sample k under control u: Euler step, running cost on the stepped output plus the likelihood-ratio
-// term, accumulated in reference order (mppi_common.cu:105-144).
-// kLik: the likelihood-ratio term is on (control_cost_coeff != 0).  It is a template flag so the step has no
-// branch and consecutive steps form one basic block the scheduler can interleave.
+// The running cost of step t (state cost on the stepped output y, control cost, likelihood-ratio term), in the
+// reference's arithmetic (mppi_common.cu:105-144).  kLik: the likelihood-ratio term is on (control_cost_coeff != 0);
+// a template flag, so a step has no branch.
 template <class Model, bool kLik, class Args>
-__device__ __forceinline__ void rollout_step(const Args& a, const InstDesc& d,
-                                             const typename Model::DynParams& dp,
-                                             const typename Model::CostParams& cp, int k, const float* u, int t,
-                                             float* x, float& running)
+__device__ __forceinline__ float step_cost(const Args& a, const InstDesc& d, const typename Model::CostParams& cp,
+                                           int k, const float* u, int t, const float* y)
 {
-  constexpr int S = Model::STATE_DIM;
   constexpr int C = Model::CONTROL_DIM;
-  float xn[S];
-  euler_step<Model>(dp, x, u, xn, a.dt);
-  float step_cost = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
+  float c = Model::computeStateCost(cp, a.aux, y, t) + Model::computeControlCost(cp, u, t);
   if constexpr (kLik)
   {
     // GaussianDistributionImpl::computeLikelihoodRatioCost (gaussian.cu:490-574)
     const bool zero_mean = (float)k >= (1.0f - a.sh.pure_pct) * (float)d.K;
     float lc = 0.0f;
 #pragma unroll
-    for (int c = 0; c < C; ++c)
+    for (int i = 0; i < C; ++i)
     {
-      const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + c];
-      const float sd = a.sh.std_dev[c];
-      lc += a.sh.control_cost_coeff[c] * m * (m - 2.0f * u[c]) / (sd * sd);
+      const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + i];
+      const float sd = a.sh.std_dev[i];
+      lc += a.sh.control_cost_coeff[i] * m * (m - 2.0f * u[i]) / (sd * sd);
     }
-    step_cost += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
+    c += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
   }
-  running += step_cost;
+  return c;
+}
+
+// A step's running cost is evaluated one step late, after the next step's dynamics: both depend only on the same
+// state, so the scheduler overlaps the cost's loads (costmap texels) and arithmetic with the dynamics chain.  The
+// costs still enter the running sum in step order.  `t < 0`: nothing pending.
+template <class Model>
+struct PendingCost
+{
+  float y[Model::STATE_DIM];
+  float u[Model::CONTROL_DIM];
+  int t;
+  __device__ __forceinline__ void reset(const float* x0)
+  {
 #pragma unroll
-  for (int i = 0; i < S; ++i) x[i] = xn[i];
+    for (int i = 0; i < Model::STATE_DIM; ++i) y[i] = x0[i];
+#pragma unroll
+    for (int i = 0; i < Model::CONTROL_DIM; ++i) u[i] = 0.0f;
+    t = -1;
+  }
+};
+
+// One step t of sample k under control u: Euler step, then the running cost of the previous step.
+template <class Model, bool kLik, class Args>
+__device__ __forceinline__ void rollout_step(const Args& a, const InstDesc& d,
+                                             const typename Model::DynParams& dp,
+                                             const typename Model::CostParams& cp, int k, const float* u, int t,
+                                             float* x, float& running, PendingCost<Model>& pc)
+{
+  constexpr int S = Model::STATE_DIM;
+  constexpr int C = Model::CONTROL_DIM;
+  float xn[S];
+  euler_step<Model>(dp, x, u, xn, a.dt);
+  const float c = step_cost<Model, kLik>(a, d, cp, k, pc.u, pc.t < 0 ? 0 : pc.t, pc.y);
+  running += pc.t >= 0 ? c : 0.0f;  // adding +0 leaves the (non-negative zero) initial sum unchanged
+#pragma unroll
+  for (int i = 0; i < S; ++i) pc.y[i] = x[i] = xn[i];
+#pragma unroll
+  for (int i = 0; i < C; ++i) pc.u[i] = u[i];
+  pc.t = t;
+}
+
+// Adds the last pending step cost.
+template <class Model, bool kLik, class Args>
+__device__ __forceinline__ void rollout_flush(const Args& a, const InstDesc& d, const typename Model::CostParams& cp,
+                                              int k, float& running, PendingCost<Model>& pc)
+{
+  if (pc.t >= 0) running += step_cost<Model, kLik>(a, d, cp, k, pc.u, pc.t, pc.y);
+  pc.t = -1;
 }
 
 // Steps t0 .. t0+nt-1 of sample k from its staged control row.
@@ -223,10 +263,10 @@ template <class Model, bool kLik>
 __device__ __forceinline__ void rollout_chunk(const RolloutArgs<Model>& a, const InstDesc& d,
                                               const typename Model::DynParams& dp,
                                               const typename Model::CostParams& cp, int k, const float* urow, int t0,
-                                              int nt, float* x, float& running)
+                                              int nt, float* x, float& running, PendingCost<Model>& pc)
 {
   constexpr int C = Model::CONTROL_DIM;
-  auto do_step = [&](const float* u, int t) { rollout_step<Model, kLik>(a, d, dp, cp, k, u, t, x, running); };
+  auto do_step = [&](const float* u, int t) { rollout_step<Model, kLik>(a, d, dp, cp, k, u, t, x, running, pc); };
   int tt = 0;
   if constexpr (4 % C == 0)
   {
@@ -283,6 +323,8 @@ __global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ Rol
 #pragma unroll
     for (int i = 0; i < S; ++i) x[i] = a.x0[d.x_off + i];
     float running = 0.0f;
+    PendingCost<Model> pc;
+    pc.reset(x);
     const bool aligned = ((d.T * C) & 3) == 0;
     const float* base = a.samples + d.u_off + (long long)w.y * d.T * C;
 
@@ -317,15 +359,19 @@ __global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ Rol
       if (active)
       {
         if (a.use_likelihood)
-          rollout_chunk<Model, true>(a, d, dp, cp, k, &stage[tid * ROW], t0, nt, x, running);
+          rollout_chunk<Model, true>(a, d, dp, cp, k, &stage[tid * ROW], t0, nt, x, running, pc);
         else
-          rollout_chunk<Model, false>(a, d, dp, cp, k, &stage[tid * ROW], t0, nt, x, running);
+          rollout_chunk<Model, false>(a, d, dp, cp, k, &stage[tid * ROW], t0, nt, x, running, pc);
       }
       __syncthreads();
     }
     unsigned int o = kOrderedPosInf;
     if (active)
     {
+      if (a.use_likelihood)
+        rollout_flush<Model, true>(a, d, cp, k, running, pc);
+      else
+        rollout_flush<Model, false>(a, d, cp, k, running, pc);
       const float tf = (float)d.T;
       const float cost = running / tf + Model::terminalCost(cp, a.aux, x) / tf;
       a.costs[d.k_off + k] = cost;
@@ -433,6 +479,8 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
 #pragma unroll
     for (int i = 0; i < S; ++i) x[i] = a.x0[d.x_off + i];
     float running = 0.0f;
+    PendingCost<Model> pc;
+    pc.reset(x);
     if (active)
     {
       const int nq = d.T * C / 4;
@@ -450,7 +498,7 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
           const float out[4] = { o.x, o.y, o.z, o.w };
 #pragma unroll
           for (int g = 0; g < G; ++g)
-            rollout_step<Model, decltype(lik)::value>(a, d, dp, cp, k, out + g * C, qi * G + g, x, running);
+            rollout_step<Model, decltype(lik)::value>(a, d, dp, cp, k, out + g * C, qi * G + g, x, running, pc);
         }
       };
       if (a.use_likelihood)
@@ -461,6 +509,10 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
     unsigned int o = kOrderedPosInf;
     if (active)
     {
+      if (a.use_likelihood)
+        rollout_flush<Model, true>(a, d, cp, k, running, pc);
+      else
+        rollout_flush<Model, false>(a, d, cp, k, running, pc);
       const float tf = (float)d.T;
       const float cost = running / tf + Model::terminalCost(cp, a.aux, x) / tf;
       a.costs[d.k_off + k] = cost;
@@ -546,6 +598,8 @@ __global__ void __launch_bounds__(NS) rollout_kernel_bulk(const __grid_constant_
 #pragma unroll
     for (int i = 0; i < S; ++i) x[i] = a.x0[d.x_off + i];
     float running = 0.0f;
+    PendingCost<Model> pc;
+    pc.reset(x);
     const int nchunks = (d.T + TCH - 1) / TCH;
     auto issue = [&](int j) {
       const int b = (uses + j) & 1;
@@ -582,16 +636,21 @@ __global__ void __launch_bounds__(NS) rollout_kernel_bulk(const __grid_constant_
       if (active)
       {
         if (a.use_likelihood)
-          rollout_chunk<Model, true>(a, d, dp, cp, k, my_stage0 + b * NS * ROW, t0, min(TCH, d.T - t0), x, running);
+          rollout_chunk<Model, true>(a, d, dp, cp, k, my_stage0 + b * NS * ROW, t0, min(TCH, d.T - t0), x, running,
+                                     pc);
         else
           rollout_chunk<Model, false>(a, d, dp, cp, k, my_stage0 + b * NS * ROW, t0, min(TCH, d.T - t0), x,
-                                      running);
+                                      running, pc);
       }
     }
     uses += nchunks;
     unsigned int o = kOrderedPosInf;
     if (active && !failed)
     {
+      if (a.use_likelihood)
+        rollout_flush<Model, true>(a, d, cp, k, running, pc);
+      else
+        rollout_flush<Model, false>(a, d, cp, k, running, pc);
       const float tf = (float)d.T;
       const float cost = running / tf + Model::terminalCost(cp, a.aux, x) / tf;
       a.costs[d.k_off + k] = cost;

@@ -185,12 +185,36 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
       uq[n] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       u_next[n] = (!kFused && active[n]) ? __ldg(reinterpret_cast<const float2*>(urow[n])) : make_float2(0.0f, 0.0f);
     }
+    // Step t's running cost is added at step t + 1: its costmap texels are gathered before step t + 1's network
+    // pass, which hides their latency, and blended after it.  The sum keeps step order.
+    auto step_cost_tx = [&](int n, const Texels& tx, const float* yv, const float* uv, int tt) {
+      float c = Model::stateCostFromTexels(cp, tx, yv) + Model::computeControlCost(cp, uv, tt);
+      if (a.use_likelihood)
+      {
+        const bool zero_mean = (float)k[n] >= (1.0f - a.sh.pure_pct) * (float)d.K;
+        float lc = 0.0f;
+#pragma unroll
+        for (int c2 = 0; c2 < C; ++c2)
+        {
+          const float m = zero_mean ? 0.0f : a.mean[d.t_off + tt * C + c2];
+          const float sd = a.sh.std_dev[c2];
+          lc += a.sh.control_cost_coeff[c2] * m * (m - 2.0f * uv[c2]) / (sd * sd);
+        }
+        c += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
+      }
+      return c;
+    };
+    float up[NT][2];
+#pragma unroll
+    for (int n = 0; n < NT; ++n) up[n][0] = up[n][1] = 0.0f;
     for (int t = 0; t < d.T && ok; ++t)
     {
       float u[NT][2], xin[NT][kMlpIn], y[NT][kMlpOut];
+      Texels tx[NT];
 #pragma unroll
       for (int n = 0; n < NT; ++n)
       {
+        tx[n] = costmap_gather(a.aux.map, x[n][0], x[n][1]);  // the state step t - 1 produced
         if constexpr (kFused)
         {
           // Gaussian sampling fused in, quad by quad, exactly as gaussian_sample_kernel would have written it
@@ -238,6 +262,9 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
 #pragma unroll
       for (int n = 0; n < NT; ++n)
       {
+        if (t > 0 && active[n]) running[n] += step_cost_tx(n, tx[n], x[n], up[n], t - 1);
+        up[n][0] = u[n][0];
+        up[n][1] = u[n][1];
         float xd[S];
         float sy, cy;
         sincos_f(x[n][2], &sy, &cy);
@@ -248,28 +275,15 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
         float xn[S];
 #pragma unroll
         for (int i = 0; i < S; ++i) xn[i] = fmaf(xd[i], a.dt, x[n][i]);
-        if (active[n])
-        {
-          float step_cost = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u[n], t);
-          if (a.use_likelihood)
-          {
-            const bool zero_mean = (float)k[n] >= (1.0f - a.sh.pure_pct) * (float)d.K;
-            float lc = 0.0f;
-#pragma unroll
-            for (int c = 0; c < C; ++c)
-            {
-              const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + c];
-              const float sd = a.sh.std_dev[c];
-              lc += a.sh.control_cost_coeff[c] * m * (m - 2.0f * u[n][c]) / (sd * sd);
-            }
-            step_cost += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
-          }
-          running[n] += step_cost;
-        }
 #pragma unroll
         for (int i = 0; i < S; ++i) x[n][i] = xn[i];
       }
     }
+    if (ok)
+#pragma unroll
+      for (int n = 0; n < NT; ++n)
+        if (active[n] && d.T > 0)
+          running[n] += step_cost_tx(n, costmap_gather(a.aux.map, x[n][0], x[n][1]), x[n], up[n], d.T - 1);
     if (!ok)
     {
       if (tid == 0) atomicOr(a.status, 1u);
@@ -444,15 +458,18 @@ __global__ void __launch_bounds__(128) judge_rollout_kernel(const __grid_constan
 #pragma unroll
   for (int s = 0; s < S; ++s) x[s] = a.r.x0[d.x_off + s];
   float running = 0.0f;
-  // the same step as the analytic rollout kernels; unrolled so the costmap loads of one step overlap the next
+  PendingCost<Model> pc;
+  pc.reset(x);
+  // the same step as the analytic rollout kernels
   auto run = [&](auto lik) {
 #pragma unroll 4
     for (int t = 0; t < d.T; ++t)
     {
       const float2 uv = __ldg(reinterpret_cast<const float2*>(urow + t * C));
       const float u[2] = { uv.x, uv.y };
-      rollout_step<Model, decltype(lik)::value>(a.r, d, dp, cp, k, u, t, x, running);
+      rollout_step<Model, decltype(lik)::value>(a.r, d, dp, cp, k, u, t, x, running, pc);
     }
+    rollout_flush<Model, decltype(lik)::value>(a.r, d, cp, k, running, pc);
   };
   if (a.r.use_likelihood)
     run(std::true_type{});

@@ -30,7 +30,14 @@ struct CostmapView
 // (TwoDTextureHelper::queryTextureCPU, two_d_texture_helper.cu:151-235).  The reference's GPU path uses the texture
 // unit (tex2D, two_d_texture_helper.cu:66-72), whose interpolation weights are 9-bit fixed point; the engine
 // interpolates in FP32 on both sides.
-MG_HD float costmap_bilinear(const CostmapView& m, float x, float y)
+struct Texels
+{
+  float q00, q01, q10, q11, fx, fy;
+};
+
+// The four texels and the interpolation fractions of point (x, y); split from the blend so a rollout can issue the
+// loads well before it needs the value.
+MG_HD Texels costmap_gather(const CostmapView& m, float x, float y)
 {
   float px = (x - m.origin_x) / m.resolution - 0.5f;
   float py = (y - m.origin_y) / m.resolution - 0.5f;
@@ -40,21 +47,33 @@ MG_HD float costmap_bilinear(const CostmapView& m, float x, float y)
   int y0 = (int)floorf(py);
   x0 = x0 < m.width - 2 ? x0 : m.width - 2;
   y0 = y0 < m.height - 2 ? y0 : m.height - 2;
-  const float fx = px - (float)x0;
-  const float fy = py - (float)y0;
+  Texels t;
+  t.fx = px - (float)x0;
+  t.fy = py - (float)y0;
   const float* row0 = m.data + (size_t)y0 * m.width;
   const float* row1 = row0 + m.width;
 #if defined(__CUDA_ARCH__)
-  const float q00 = __ldg(row0 + x0), q01 = __ldg(row0 + x0 + 1);
-  const float q10 = __ldg(row1 + x0), q11 = __ldg(row1 + x0 + 1);
+  t.q00 = __ldg(row0 + x0);
+  t.q01 = __ldg(row0 + x0 + 1);
+  t.q10 = __ldg(row1 + x0);
+  t.q11 = __ldg(row1 + x0 + 1);
 #else
-  const float q00 = row0[x0], q01 = row0[x0 + 1];
-  const float q10 = row1[x0], q11 = row1[x0 + 1];
+  t.q00 = row0[x0];
+  t.q01 = row0[x0 + 1];
+  t.q10 = row1[x0];
+  t.q11 = row1[x0 + 1];
 #endif
-  const float top = q00 * (1.0f - fx) + q01 * fx;
-  const float bot = q10 * (1.0f - fx) + q11 * fx;
-  return top * (1.0f - fy) + bot * fy;
+  return t;
 }
+
+MG_HD float costmap_blend(const Texels& t)
+{
+  const float top = t.q00 * (1.0f - t.fx) + t.q01 * t.fx;
+  const float bot = t.q10 * (1.0f - t.fx) + t.q11 * t.fx;
+  return top * (1.0f - t.fy) + bot * t.fy;
+}
+
+MG_HD float costmap_bilinear(const CostmapView& m, float x, float y) { return costmap_blend(costmap_gather(m, x, y)); }
 
 // Shared (per-launch) data that some costs need besides their parameter block.
 struct ModelAux
@@ -236,8 +255,13 @@ struct BicycleSlipModel
   }
   static MG_HD float speedMapCost(const CostParams& q, const ModelAux& aux, const float* y)
   {
+    return stateCostFromTexels(q, costmap_gather(aux.map, y[0], y[1]), y);
+  }
+  // The state cost from texels gathered earlier (costmap_gather at y[0], y[1]): the same arithmetic as speedMapCost.
+  static MG_HD float stateCostFromTexels(const CostParams& q, const Texels& tx, const float* y)
+  {
     const float dv = y[3] - q.speed_target;
-    return q.map_coeff * costmap_bilinear(aux.map, y[0], y[1]) + q.speed_coeff * (dv * dv);
+    return q.map_coeff * costmap_blend(tx) + q.speed_coeff * (dv * dv);
   }
   static MG_HD float computeStateCost(const CostParams& q, const ModelAux& aux, const float* y, int)
   {

@@ -123,6 +123,8 @@ SIGNATURES = [
     ("mppi_set_costmap", C.c_int, [_P, _FP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float]),
     ("mppi_set_mlp", C.c_int, [_P, _FP, C.c_size_t, C.c_int]),
     ("mppi_set_judge", C.c_int, [_P, C.c_float]),
+    ("mppi_set_rollout_mode", C.c_int, [_P, C.c_int]),
+    ("mppi_get_rollout_mode", C.c_int, [_P, _IP, _IP]),
     ("mppi_get_judge_stats", C.c_int, [_P, _FP]),
     ("mppi_use_analytic_dynamics", C.c_int, [_P, C.c_int]),
     ("mppi_inject_noise", C.c_int, [_P, _FP, C.c_size_t]),

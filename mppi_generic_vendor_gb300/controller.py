@@ -410,6 +410,16 @@ class BatchedMPPIController:
     def autotune(self, cache_path=None):
         A.call("mppi_autotune", self._h, None if cache_path is None else str(cache_path).encode())
 
+    def setRolloutMode(self, mode):
+        """0 = fused rollout kernel, 1 = split dynamics / cost kernels (small problems); costs are bit-identical."""
+        A.call("mppi_set_rollout_mode", self._h, int(mode))
+
+    def rolloutMode(self):
+        """(current mode, bitmask of available modes)."""
+        m, av = C.c_int(), C.c_int()
+        A.call("mppi_get_rollout_mode", self._h, C.byref(m), C.byref(av))
+        return m.value, av.value
+
     def launchConfig(self):
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         A.call("mppi_get_launch_config", self._h, C.byref(a), C.byref(b), C.byref(c))

@@ -29,8 +29,8 @@ void set_error(const char* fmt, ...)
 
 void clear_error() { g_last_error.clear(); }
 
-// Minimal reader/writer for the autotune cache: a flat JSON object of "key": [ns, kc] entries.
-static bool cache_lookup(const char* path, const std::string& key, int* ns, int* kc)
+// Minimal reader/writer for the autotune cache: a flat JSON object of "key": [ns, kc, rollout_mode] entries.
+static bool cache_lookup(const char* path, const std::string& key, int* ns, int* kc, int* mode)
 {
   if (!path) return false;
   std::ifstream f(path);
@@ -43,10 +43,11 @@ static bool cache_lookup(const char* path, const std::string& key, int* ns, int*
   if (p == std::string::npos) return false;
   p = s.find('[', p);
   if (p == std::string::npos) return false;
-  return sscanf(s.c_str() + p, "[%d,%d]", ns, kc) == 2 || sscanf(s.c_str() + p, "[%d, %d]", ns, kc) == 2;
+  *mode = 0;
+  return sscanf(s.c_str() + p, "[%d, %d, %d]", ns, kc, mode) >= 2 || sscanf(s.c_str() + p, "[%d,%d,%d]", ns, kc, mode) >= 2;
 }
 
-static void cache_store(const char* path, const std::string& key, int ns, int kc)
+static void cache_store(const char* path, const std::string& key, int ns, int kc, int mode)
 {
   if (!path) return;
   std::string body;
@@ -78,33 +79,44 @@ static void cache_store(const char* path, const std::string& key, int ns, int kc
   std::ofstream f(path);
   f << "{";
   if (!inner.empty()) f << inner << ", ";
-  f << pat << ": [" << ns << ", " << kc << "]}\n";
+  f << pat << ": [" << ns << ", " << kc << ", " << mode << "]}\n";
 }
 
 mppi_status autotune_impl(EngineBase* e, const char* cache_path, const std::string& key,
                           mppi_status (*time_one)(EngineBase*, float*))
 {
-  int ns = 0, kc = 0;
-  if (cache_lookup(cache_path, key, &ns, &kc)) return e->set_launch_config(ns, 0, kc);
+  int ns = 0, kc = 0, mode = 0;
+  if (cache_lookup(cache_path, key, &ns, &kc, &mode))
+  {
+    MG_TRY(e->set_launch_config(ns, 0, kc));
+    return e->set_rollout_mode((e->rollout_modes() >> mode) & 1 ? mode : 0);
+  }
   const int ns_c[4] = { 32, 64, 128, 256 };
   const int kc_c[3] = { 64, 128, 256 };
   float best = FLT_MAX;
-  int best_ns = 128, best_kc = 128;
-  for (int a : ns_c)
-    for (int b : kc_c)
-    {
-      MG_TRY(e->set_launch_config(a, 0, b));
-      float ms = 0.0f;
-      MG_TRY(time_one(e, &ms));
-      if (ms < best)
+  int best_ns = 128, best_kc = 128, best_mode = 0;
+  for (int m = 0; m < 2; ++m)
+  {
+    if (!((e->rollout_modes() >> m) & 1)) continue;
+    MG_TRY(e->set_rollout_mode(m));
+    for (int a : ns_c)
+      for (int b : kc_c)
       {
-        best = ms;
-        best_ns = a;
-        best_kc = b;
+        MG_TRY(e->set_launch_config(a, 0, b));
+        float ms = 0.0f;
+        MG_TRY(time_one(e, &ms));
+        if (ms < best)
+        {
+          best = ms;
+          best_ns = a;
+          best_kc = b;
+          best_mode = m;
+        }
       }
-    }
+  }
+  MG_TRY(e->set_rollout_mode(best_mode));
   MG_TRY(e->set_launch_config(best_ns, 0, best_kc));
-  cache_store(cache_path, key, best_ns, best_kc);
+  cache_store(cache_path, key, best_ns, best_kc, best_mode);
   return MPPI_OK;
 }
 
@@ -415,6 +427,18 @@ mppi_status mppi_autotune(mppi_handle* h, const char* cache_path)
 {
   HANDLE_OK(h);
   return h->engine->autotune(cache_path);
+}
+mppi_status mppi_set_rollout_mode(mppi_handle* h, int mode)
+{
+  HANDLE_OK(h);
+  return h->engine->set_rollout_mode(mode);
+}
+mppi_status mppi_get_rollout_mode(const mppi_handle* h, int* mode, int* available)
+{
+  HANDLE_OK(h);
+  if (mode) *mode = h->engine->rollout_mode();
+  if (available) *available = h->engine->rollout_modes();
+  return MPPI_OK;
 }
 mppi_status mppi_get_launch_config(const mppi_handle* h, int* rollout_samples_per_cta, int* rollout_time_chunk,
                                    int* reduction_samples_per_cta)

@@ -70,6 +70,10 @@ public:
   virtual mppi_status generate_samples(int stride, int iter) = 0;
   virtual mppi_status set_graph_mode(int enable) = 0;
   virtual mppi_status get_launch_config(int* ns, int* tch, int* kc) const = 0;
+  // Rollout mode: 0 = one fused kernel, 1 = split dynamics / cost kernels; rollout_modes() is the bitmask available.
+  virtual mppi_status set_rollout_mode(int mode) = 0;
+  virtual int rollout_mode() const = 0;
+  virtual int rollout_modes() const = 0;
   virtual mppi_status set_launch_config(int ns, int tch, int kc) = 0;
   virtual mppi_status autotune(const char* cache_path) = 0;
   virtual int kernels_per_compute() const = 0;
@@ -195,6 +199,7 @@ public:
     }
     const int judge = (Model::kMlp && !use_analytic_ && judge_total_ > 0) ? 3 : 0;
     if (fused()) sampler = 0;
+    if (fused() && split_) sampler = 1;  // the cost kernel
     return (sampler + 2 + judge) * cp_.num_iters;
   }
 
@@ -467,6 +472,26 @@ public:
     graph_mode_ = enable != 0;
     return MPPI_OK;
   }
+  // The split rollout needs the fused Gaussian sampler (whole quads per row), an analytic model, and room for the
+  // stepped states of every sample (at most 256 MB).
+  bool split_available() const
+  {
+    if (!fused() || (Model::kMlp && !use_analytic_)) return false;
+    return (double)total_u_ / C * S * sizeof(float) <= 256.0 * 1024 * 1024;
+  }
+  int rollout_modes() const override { return 1 | (split_available() ? 2 : 0); }
+  int rollout_mode() const override { return split_ ? 1 : 0; }
+  mppi_status set_rollout_mode(int mode) override
+  {
+    MG_CHECK(mode == 0 || mode == 1, "rollout mode must be 0 (fused) or 1 (split dynamics / cost)");
+    MG_CHECK(mode == 0 || split_available(),
+             "the split rollout needs Gaussian sampling, T*C %% 4 == 0, an analytic model and <= 256 MB of states");
+    if (mode == 1 && !states_d_.p) MG_TRY(states_d_.alloc((size_t)total_u_ / C * S));
+    split_ = mode == 1;
+    MG_TRY(build_work_lists());  // the rollout grid follows the kernel's occupancy
+    invalidate_graphs();
+    return MPPI_OK;
+  }
   mppi_status get_launch_config(int* ns, int* tch, int* kc) const override
   {
     if (ns) *ns = ns_;
@@ -695,6 +720,7 @@ private:
     MG_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
 
     MG_TRY(samples_d_.alloc((size_t)total_u));
+    total_u_ = total_u;
     MG_CUDA(cudaMemset(samples_d_.p, 0, sizeof(float) * samples_d_.n));
     MG_TRY(costs_d_.alloc(total_k));
     MG_TRY(weights_d_.alloc(total_k));
@@ -910,7 +936,10 @@ private:
     if constexpr ((4 % C) == 0)
       if (fused())
       {
-        MG_CUDA(resident_ctas_per_sm(rollout_fused_kernel<Model, NS>, NS, 0, per_sm));
+        if (split_)
+          MG_CUDA(resident_ctas_per_sm(rollout_dyn_kernel<Model, NS>, NS, 0, per_sm));
+        else
+          MG_CUDA(resident_ctas_per_sm(rollout_fused_kernel<Model, NS>, NS, 0, per_sm));
         return MPPI_OK;
       }
     if (use_bulk_)
@@ -1015,6 +1044,21 @@ private:
     return f;
   }
 
+  template <int NS>
+  mppi_status launch_cost_kernel(const RolloutArgs<Model>& a)
+  {
+    constexpr int WARPS = 4;
+    auto kern = rollout_cost_kernel<Model, NS, WARPS>;
+    const size_t smem = sizeof(float) * WARPS * (size_t)max_t_;
+    if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 1;
+    MG_CUDA(resident_ctas_per_sm(kern, WARPS * 32, smem, &per_sm));
+    const int grid = std::max(1, std::min(num_tiles_, per_sm * num_sms_));
+    kern<<<grid, WARPS * 32, smem, stream_>>>(a, states_d_.p);
+    MG_CUDA(cudaGetLastError());
+    return MPPI_OK;
+  }
+
   mppi_status launch_rollout(int stride, int iter)
   {
     RolloutArgs<Model> a;
@@ -1037,6 +1081,7 @@ private:
     a.use_likelihood = 0;
     for (int c = 0; c < C; ++c)
       if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
+    a.max_t = max_t_;
     a.sh = make_sample_shared(sp_, cc_);
     if constexpr (Model::kMlp)
       if (!use_analytic_)
@@ -1055,6 +1100,27 @@ private:
         j.stats = judge_stats_d_.p;
         j.total = judge_total_;
         return launch_judge(j, stream_);
+      }
+    if constexpr ((4 % C) == 0)
+      if (fused() && split_)
+      {
+        const FusedNoise f = fused_noise_args(stride, iter);
+        switch (ns_)
+        {
+          case 32: rollout_dyn_kernel<Model, 32><<<rollout_grid_, 32, 0, stream_>>>(a, f, states_d_.p); break;
+          case 64: rollout_dyn_kernel<Model, 64><<<rollout_grid_, 64, 0, stream_>>>(a, f, states_d_.p); break;
+          case 128: rollout_dyn_kernel<Model, 128><<<rollout_grid_, 128, 0, stream_>>>(a, f, states_d_.p); break;
+          default: rollout_dyn_kernel<Model, 256><<<rollout_grid_, 256, 0, stream_>>>(a, f, states_d_.p); break;
+        }
+        MG_CUDA(cudaGetLastError());
+        switch (ns_)
+        {
+          case 32: MG_TRY(launch_cost_kernel<32>(a)); break;
+          case 64: MG_TRY(launch_cost_kernel<64>(a)); break;
+          case 128: MG_TRY(launch_cost_kernel<128>(a)); break;
+          default: MG_TRY(launch_cost_kernel<256>(a)); break;
+        }
+        return MPPI_OK;
       }
     if constexpr ((4 % C) == 0)
       if (fused())
@@ -1274,6 +1340,9 @@ private:
   PinnedBuf<unsigned int> status_h_;
   std::vector<float> mlp_host_;  // surrogate parameters as the tensor cores see them (MLP models only)
   DevBuf<float> mlp_d_;
+  long long total_u_ = 0;      // control-sample floats over all instances
+  bool split_ = false;         // split dynamics / cost rollout (rollout mode 1)
+  DevBuf<float> states_d_;     // split rollout: stepped states [instance][k][t][S]
   int mlp_precision_ = 0;      // 0 bf16 / 1 fp8 tensor cores, 2 fp32 CUDA cores
   bool use_analytic_ = false;  // MLP models: roll out the analytic model instead
   float judge_frac_ = 0.01f;   // MLP models: fraction of samples re-rolled by the analytic judge

@@ -181,6 +181,7 @@ struct RolloutArgs
   unsigned int* status;         // set non-zero if a bounded wait gave up
   float dt, lambda, alpha;
   int use_likelihood;
+  int max_t;  // longest horizon of the handle
   SampleShared sh;
 };
 
@@ -521,6 +522,150 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) o = min(o, __shfl_xor_sync(0xffffffffu, o, off));
     if ((tid & 31) == 0) atomicMin(&s_min, o);
+    __syncthreads();
+    if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+  }
+  if (tid == 0)
+  {
+    __threadfence();
+    const unsigned int done = atomicAdd(&a.tile_counter[1], 1u);
+    if (done == gridDim.x - 1)
+    {
+      a.tile_counter[0] = 0u;
+      a.tile_counter[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// Split rollout for problems too small to fill the GPU with one thread per sample (the reference also keeps a split
+// dynamics / cost rollout, rolloutDynamicsKernel + rolloutCostKernel, mppi_common.cu:155-369, and picks the faster by
+// timing).  Kernel 1 runs only the dynamics chain (with the Gaussian sampling fused in) and stores every stepped state
+// in states[instance][k][t][S] (instance offset u_off / C * S, exact because every row holds whole quads).  Kernel 2
+// evaluates the running costs of all (k, t) in parallel, one warp per sample, and one lane adds them in step order,
+// so the per-sample costs are bit-identical to the fused kernels'.
+template <class Model, int NS>
+__global__ void __launch_bounds__(NS) rollout_dyn_kernel(const __grid_constant__ RolloutArgs<Model> a,
+                                                         const __grid_constant__ FusedNoise f, float* states)
+{
+  constexpr int S = Model::STATE_DIM;
+  constexpr int C = Model::CONTROL_DIM;
+  static_assert(4 % C == 0, "a quad must hold whole steps");
+  constexpr int G = 4 / C;
+  __shared__ int s_tile;
+  const int tid = threadIdx.x;
+  const uint32_t counter = f.noise_counter ? *f.noise_counter : 0u;
+  for (;;)
+  {
+    if (tid == 0) s_tile = (int)atomicAdd(&a.tile_counter[0], 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    __syncthreads();
+    if (tile >= a.num_tiles) break;
+    const int2 w = a.tiles[tile];
+    const InstDesc d = a.inst[w.x];
+    const int k = w.y + tid;
+    if (k < d.K)
+    {
+      const typename Model::DynParams dp = a.dyn[w.x];
+      float x[S];
+#pragma unroll
+      for (int i = 0; i < S; ++i) x[i] = a.x0[d.x_off + i];
+      const int nq = d.T * C / 4;
+      const long long q0 = (long long)k * nq;
+      const float pure_threshold = (1.0f - a.sh.pure_pct) * (float)d.K;
+      float* dst = f.samples + d.u_off + 4 * q0;
+      float* ys = states + d.u_off / C * S + (long long)k * d.T * S;
+      float4 zn = fused_noise(f, d, w.x, counter, q0);
+      for (int qi = 0; qi < nq; ++qi)
+      {
+        const float4 z = zn;
+        if (qi + 1 < nq) zn = fused_noise(f, d, w.x, counter, q0 + qi + 1);
+        const float4 o = gaussian_quad<C>(a.sh, a.mean + d.t_off, f.decay_pow, f.stride, k, pure_threshold, 4 * qi, z);
+        *reinterpret_cast<float4*>(dst + 4 * qi) = o;
+        const float out[4] = { o.x, o.y, o.z, o.w };
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+        {
+          float xn[S];
+          euler_step<Model>(dp, x, out + g * C, xn, a.dt);
+          float* yt = ys + (long long)(qi * G + g) * S;
+#pragma unroll
+          for (int i = 0; i < S; ++i) yt[i] = x[i] = xn[i];
+        }
+      }
+    }
+  }
+  if (tid == 0)
+  {
+    __threadfence();
+    const unsigned int done = atomicAdd(&a.tile_counter[1], 1u);
+    if (done == gridDim.x - 1)
+    {
+      a.tile_counter[0] = 0u;
+      a.tile_counter[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
+template <class Model, int NS, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) rollout_cost_kernel(const __grid_constant__ RolloutArgs<Model> a,
+                                                                  const float* states)
+{
+  constexpr int S = Model::STATE_DIM;
+  constexpr int C = Model::CONTROL_DIM;
+  extern __shared__ float s_cost[];  // [WARPS][T_max]
+  __shared__ int s_tile;
+  __shared__ unsigned int s_min;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (;;)
+  {
+    if (tid == 0)
+    {
+      s_tile = (int)atomicAdd(&a.tile_counter[0], 1u);
+      s_min = kOrderedPosInf;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= a.num_tiles) break;
+    const int2 w = a.tiles[tile];
+    const InstDesc d = a.inst[w.x];
+    const typename Model::CostParams cp = a.cost[w.x];
+    float* my = s_cost + warp * a.max_t;
+    unsigned int o = kOrderedPosInf;
+    const int rows = min(NS, d.K - w.y);
+    for (int r = warp; r < rows; r += WARPS)
+    {
+      const int k = w.y + r;
+      const float* ys = states + d.u_off / C * S + (long long)k * d.T * S;
+      const float* us = a.samples + d.u_off + (long long)k * d.T * C;
+      for (int t = lane; t < d.T; t += 32)
+      {
+        float y[S], u[C];
+#pragma unroll
+        for (int i = 0; i < S; ++i) y[i] = ys[(long long)t * S + i];
+#pragma unroll
+        for (int i = 0; i < C; ++i) u[i] = us[t * C + i];
+        my[t] = a.use_likelihood ? step_cost<Model, true>(a, d, cp, k, u, t, y)
+                                 : step_cost<Model, false>(a, d, cp, k, u, t, y);
+      }
+      __syncwarp();
+      if (lane == 0)
+      {
+        float running = 0.0f;
+        for (int t = 0; t < d.T; ++t) running += my[t];
+        float yT[S];
+#pragma unroll
+        for (int i = 0; i < S; ++i) yT[i] = ys[(long long)(d.T - 1) * S + i];
+        const float tf = (float)d.T;
+        const float cost = running / tf + Model::terminalCost(cp, a.aux, yT) / tf;
+        a.costs[d.k_off + k] = cost;
+        o = min(o, float_to_ordered(cost));
+      }
+      __syncwarp();
+    }
+    if (lane == 0) atomicMin(&s_min, o);
     __syncthreads();
     if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
   }

@@ -241,3 +241,45 @@ def test_autotune_cache_roundtrip(tmp_path):
     assert np.allclose(outs[0][1], outs[1][1], rtol=0, atol=1e-6)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("lik", [False, True])
+def test_split_rollout_bit_identical_to_fused(lik):
+    """Rollout mode 1 (dynamics chain, then all (k, t) costs in parallel) gives the fused kernel's costs bit for bit,
+    with and without the likelihood-ratio term, over several iterations of Philox noise."""
+    outs = []
+    for mode in (0, 1):
+        dyn = CartpoleDynamics(1.0, 1.0, 1.0)
+        dyn.setControlRanges([(-5.0, 5.0)])
+        sampler = GaussianDistribution(std_dev=(1.0,), control_cost_coeff=(1.0,) if lik else (0.0,))
+        ctrl = VanillaMPPIController(dyn, CartpoleSwingupCost(10.0, 1.0, 100.0, 1.0, 0.0), None, sampler, 0.02, 3, 1.0,
+                                     0.0, 100, 2048, seed=5)
+        m, avail = ctrl.rolloutMode()
+        assert m == 0 and avail == 3
+        ctrl.setRolloutMode(mode)
+        assert ctrl.rolloutMode()[0] == mode
+        x0 = np.array([0.0, 0.0, 2.0, 0.0], np.float32)
+        ctrl.computeControl(x0, 1)
+        ctrl.computeControl(x0, 1)
+        outs.append((ctrl.sample_costs(), ctrl.getControlSeq(), ctrl.control_samples(), ctrl.kernelsPerCompute()))
+        ctrl.close()
+    (c0, u0, s0, n0), (c1, u1, s1, n1) = outs
+    assert np.array_equal(s0, s1)
+    assert np.array_equal(c0.view(np.uint32), c1.view(np.uint32))
+    assert np.array_equal(u0, u1)
+    assert n1 == n0 + 3  # one more kernel per iteration
+
+
+def test_split_rollout_unavailable_for_colored_noise():
+    rng = np.random.default_rng(0)
+    ctrl = BatchedMPPIController(DoubleIntegratorDynamics(), [di_cost(rng)], A_colored(), [512], [32])
+    assert ctrl.rolloutMode() == (0, 1)
+    with pytest.raises(MPPIError):
+        ctrl.setRolloutMode(1)
+    ctrl.close()
+
+
+def A_colored():
+    from mppi_generic_vendor_gb300 import ColoredNoiseDistribution
+
+    return ColoredNoiseDistribution(std_dev=(0.5, 0.5), exponents=(1.0, 1.0))

@@ -747,6 +747,7 @@ private:
     MG_TRY(out_bn_h_.alloc((size_t)2 * I_));
     MG_TRY(out_stats_h_.alloc((size_t)3 * I_));
     MG_TRY(status_h_.alloc(1));
+    max_t_ = *std::max_element(T_.begin(), T_.end());  // sizes per-launch shared buffers (split cost kernel)
     if (Model::kMlp) ns_ = kMlpSamplesPerCta;
     MG_TRY(build_work_lists());
     MG_TRY(build_colored_tables());
@@ -854,7 +855,6 @@ private:
     MG_CUDA(cudaMemcpy(ctab_d_.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice));
     MG_CUDA(cudaMemcpy(ctab_off_d_.p, tab_off.data(), sizeof(int) * I_, cudaMemcpyHostToDevice));
     MG_CUDA(cudaMemcpy(ctab_parts_d_.p, parts.data(), sizeof(int4) * I_, cudaMemcpyHostToDevice));
-    max_t_ = *std::max_element(T_.begin(), T_.end());
     return MPPI_OK;
   }
 
@@ -1049,6 +1049,8 @@ private:
   {
     constexpr int WARPS = 4;
     auto kern = rollout_cost_kernel<Model, NS, WARPS>;
+    // one row of max_t_ step costs per warp; every instance's T is at most max_t_ (set at create)
+    MG_CHECK(max_t_ >= *std::max_element(T_.begin(), T_.end()), "internal: horizon bound not set");
     const size_t smem = sizeof(float) * WARPS * (size_t)max_t_;
     if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 1;

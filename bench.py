@@ -461,8 +461,9 @@ def run_gpu(args, ws, rank, local):
                    "working set %.1f MB fits in L2; device-resident value is L2-warm" % (wl.control_floats * 4 / 1e6),
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "iters_per_s": iters_per_s,
-        "launch_config": dict(zip(["rollout_samples_per_cta", "rollout_time_chunk", "reduction_samples_per_cta"],
-                                  ctrl.launchConfig())),
+        "launch_config": {**dict(zip(["rollout_samples_per_cta", "rollout_time_chunk", "reduction_samples_per_cta"],
+                                     ctrl.launchConfig())),
+                          "rollout_mode": ["fused", "split"][ctrl.rolloutMode()[0]]},
         "kernel_ms": {n: float(v) for n, v in zip(names, kms)},
         "roofline": ({"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                       "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,

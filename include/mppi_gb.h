@@ -288,12 +288,13 @@ mppi_status mppi_set_graph_mode(mppi_handle* h, int enable);
 /* Choose launch shapes by timing candidates on the device; cache_path (may be NULL) is a JSON file that stores and
  * restores the choice per (model, instance shape) key. */
 mppi_status mppi_autotune(mppi_handle* h, const char* cache_path);
-/* Rollout mode: 0 = one fused kernel per iteration (sampling, dynamics and costs), 1 = split dynamics / cost
- * kernels (the dynamics chain alone, then all (k, t) costs in parallel; for problems too small to fill the GPU with
- * one thread per sample, as the reference's rolloutDynamicsKernel + rolloutCostKernel, mppi_common.cu:155-369).
- * Both give bit-identical costs.  available (may be NULL) receives the bitmask of modes this handle supports; mode
- * 1 needs Gaussian sampling, T * C % 4 == 0, an analytic model and at most 256 MB of stepped states.  mppi_autotune
- * times both. */
+/* Rollout mode: 0 = one fused kernel per iteration (sampling, dynamics and costs, one thread per sample), 1 = split
+ * dynamics / cost kernels (the dynamics chain alone, then all (k, t) costs in parallel, as the reference's
+ * rolloutDynamicsKernel + rolloutCostKernel, mppi_common.cu:155-369), 2 = cooperative (four lanes per sample share
+ * the sampling and cost work off the dynamics chain).  Modes 1 and 2 are for problems too small to fill the GPU
+ * with one thread per sample; all give bit-identical costs.  available (may be NULL) receives the bitmask of modes
+ * this handle supports (bit m = mode m); modes 1 and 2 need Gaussian sampling, T * C % 4 == 0 and an analytic
+ * model, mode 1 also at most 256 MB of stepped states.  mppi_autotune times every available mode. */
 mppi_status mppi_set_rollout_mode(mppi_handle* h, int mode);
 mppi_status mppi_get_rollout_mode(const mppi_handle* h, int* mode, int* available);
 /* The launch shape in use: samples per rollout CTA, time chunk, samples per reduction CTA. */

@@ -479,14 +479,22 @@ public:
     if (!fused() || (Model::kMlp && !use_analytic_)) return false;
     return (double)total_u_ / C * S * sizeof(float) <= 256.0 * 1024 * 1024;
   }
-  int rollout_modes() const override { return 1 | (split_available() ? 2 : 0); }
-  int rollout_mode() const override { return split_ ? 1 : 0; }
+  // The cooperative rollout (four lanes per sample) needs the fused Gaussian sampler and an analytic model.
+  bool coop_available() const { return fused() && !(Model::kMlp && !use_analytic_); }
+  int rollout_modes() const override
+  {
+    return 1 | (split_available() ? 2 : 0) | (coop_available() ? 4 : 0);
+  }
+  int rollout_mode() const override { return rollout_mode_; }
   mppi_status set_rollout_mode(int mode) override
   {
-    MG_CHECK(mode == 0 || mode == 1, "rollout mode must be 0 (fused) or 1 (split dynamics / cost)");
-    MG_CHECK(mode == 0 || split_available(),
+    MG_CHECK(mode >= 0 && mode <= 2, "rollout mode must be 0 (fused), 1 (split dynamics / cost) or 2 (cooperative)");
+    MG_CHECK(mode != 1 || split_available(),
              "the split rollout needs Gaussian sampling, T*C %% 4 == 0, an analytic model and <= 256 MB of states");
+    MG_CHECK(mode != 2 || coop_available(), "the cooperative rollout needs Gaussian sampling, T*C %% 4 == 0 and an "
+             "analytic model");
     if (mode == 1 && !states_d_.p) MG_TRY(states_d_.alloc((size_t)total_u_ / C * S));
+    rollout_mode_ = mode;
     split_ = mode == 1;
     MG_TRY(build_work_lists());  // the rollout grid follows the kernel's occupancy
     invalidate_graphs();
@@ -938,6 +946,8 @@ private:
       {
         if (split_)
           MG_CUDA(resident_ctas_per_sm(rollout_dyn_kernel<Model, NS>, NS, 0, per_sm));
+        else if (rollout_mode_ == 2)
+          MG_CUDA(resident_ctas_per_sm(rollout_coop_kernel<Model, NS>, 4 * NS, 0, per_sm));
         else
           MG_CUDA(resident_ctas_per_sm(rollout_fused_kernel<Model, NS>, NS, 0, per_sm));
         return MPPI_OK;
@@ -1122,6 +1132,20 @@ private:
           case 128: MG_TRY(launch_cost_kernel<128>(a)); break;
           default: MG_TRY(launch_cost_kernel<256>(a)); break;
         }
+        return MPPI_OK;
+      }
+    if constexpr ((4 % C) == 0)
+      if (fused() && rollout_mode_ == 2)
+      {
+        const FusedNoise f = fused_noise_args(stride, iter);
+        switch (ns_)
+        {
+          case 32: rollout_coop_kernel<Model, 32><<<rollout_grid_, 128, 0, stream_>>>(a, f); break;
+          case 64: rollout_coop_kernel<Model, 64><<<rollout_grid_, 256, 0, stream_>>>(a, f); break;
+          case 128: rollout_coop_kernel<Model, 128><<<rollout_grid_, 512, 0, stream_>>>(a, f); break;
+          default: rollout_coop_kernel<Model, 256><<<rollout_grid_, 1024, 0, stream_>>>(a, f); break;
+        }
+        MG_CUDA(cudaGetLastError());
         return MPPI_OK;
       }
     if constexpr ((4 % C) == 0)
@@ -1344,6 +1368,7 @@ private:
   DevBuf<float> mlp_d_;
   long long total_u_ = 0;      // control-sample floats over all instances
   bool split_ = false;         // split dynamics / cost rollout (rollout mode 1)
+  int rollout_mode_ = 0;       // 0 fused, 1 split, 2 cooperative (four lanes per sample)
   DevBuf<float> states_d_;     // split rollout: stepped states [instance][k][t][S]
   int mlp_precision_ = 0;      // 0 bf16 / 1 fp8 tensor cores, 2 fp32 CUDA cores
   bool use_analytic_ = false;  // MLP models: roll out the analytic model instead

@@ -538,6 +538,132 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
   }
 }
 
+// Cooperative rollout for problems too small to fill the GPU with one thread per sample (rollout mode 2): four
+// lanes per sample.  All four integrate the dynamics chain (the same values, one issue per step), while the work
+// off the chain is dealt out: lane j draws and rewrites Philox quad 4i + j of its row (one quad per four), keeps the
+// states its quad's steps produce, and after each group of four quads evaluates the running costs of those steps;
+// the costs are then gathered by shuffles and added in step order.  Samples and costs are bit-identical to
+// rollout_fused_kernel's.
+template <class Model, int NS>
+__global__ void __launch_bounds__(4 * NS) rollout_coop_kernel(const __grid_constant__ RolloutArgs<Model> a,
+                                                              const __grid_constant__ FusedNoise f)
+{
+  constexpr int S = Model::STATE_DIM;
+  constexpr int C = Model::CONTROL_DIM;
+  static_assert(4 % C == 0, "a quad must hold whole steps");
+  constexpr int G = 4 / C;  // steps per quad
+  constexpr int L = 4;      // lanes per sample
+  __shared__ int s_tile;
+  __shared__ unsigned int s_min;
+  const int tid = threadIdx.x, j = tid & (L - 1);
+  const uint32_t counter = f.noise_counter ? *f.noise_counter : 0u;
+  for (;;)
+  {
+    if (tid == 0)
+    {
+      s_tile = (int)atomicAdd(&a.tile_counter[0], 1u);
+      s_min = kOrderedPosInf;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= a.num_tiles) break;
+    const int2 w = a.tiles[tile];
+    const InstDesc d = a.inst[w.x];
+    const int k = w.y + tid / L;
+    const bool active = k < d.K;
+    const typename Model::DynParams dp = a.dyn[w.x];
+    const typename Model::CostParams cp = a.cost[w.x];
+    float x[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i) x[i] = a.x0[d.x_off + i];
+    float running = 0.0f;
+    const int nq = d.T * C / 4;  // quads per row (uniform over the CTA: one instance per tile)
+    const long long q0 = (long long)(active ? k : w.y) * nq;
+    const float pure_threshold = (1.0f - a.sh.pure_pct) * (float)d.K;
+    float* dst = f.samples + d.u_off + 4 * q0;
+    auto group = [&](auto lik) {
+      for (int gi = 0; gi * L < nq; ++gi)
+      {
+        const int q = gi * L + j;  // this lane's quad
+        float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (q < nq && active)
+        {
+          o = gaussian_quad<C>(a.sh, a.mean + d.t_off, f.decay_pow, f.stride, k, pure_threshold, 4 * q,
+                               fused_noise(f, d, w.x, counter, q0 + q));
+          *reinterpret_cast<float4*>(dst + 4 * q) = o;
+        }
+        const int nquads = min(L, nq - gi * L);
+        float my_y[G][S];
+#pragma unroll
+        for (int jj = 0; jj < L; ++jj)
+        {
+          if (jj >= nquads) break;  // uniform over the CTA
+          const float v[4] = { __shfl_sync(0xffffffffu, o.x, jj, L), __shfl_sync(0xffffffffu, o.y, jj, L),
+                               __shfl_sync(0xffffffffu, o.z, jj, L), __shfl_sync(0xffffffffu, o.w, jj, L) };
+#pragma unroll
+          for (int g = 0; g < G; ++g)
+          {
+            float xn[S];
+            euler_step<Model>(dp, x, v + g * C, xn, a.dt);
+#pragma unroll
+            for (int i = 0; i < S; ++i)
+            {
+              if (jj == j) my_y[g][i] = xn[i];
+              x[i] = xn[i];
+            }
+          }
+        }
+        // the running costs of this lane's steps, then all of the group's in step order
+        float c[G];
+        const float ov[4] = { o.x, o.y, o.z, o.w };
+#pragma unroll
+        for (int g = 0; g < G; ++g) c[g] = 0.0f;
+        if (q < nq)  // a lane past the row's last quad has no steps (and must not read the mean past T)
+        {
+#pragma unroll
+          for (int g = 0; g < G; ++g)
+            c[g] = step_cost<Model, decltype(lik)::value>(a, d, cp, k, ov + g * C, q * G + g, my_y[g]);
+        }
+#pragma unroll
+        for (int jj = 0; jj < L; ++jj)
+        {
+          if (jj >= nquads) break;
+#pragma unroll
+          for (int g = 0; g < G; ++g) running += __shfl_sync(0xffffffffu, c[g], jj, L);
+        }
+      }
+    };
+    if (a.use_likelihood)
+      group(std::true_type{});
+    else
+      group(std::false_type{});
+    unsigned int o = kOrderedPosInf;
+    if (active)
+    {
+      const float tf = (float)d.T;
+      const float cost = running / tf + Model::terminalCost(cp, a.aux, x) / tf;
+      if (j == 0) a.costs[d.k_off + k] = cost;
+      o = float_to_ordered(cost);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) o = min(o, __shfl_xor_sync(0xffffffffu, o, off));
+    if ((tid & 31) == 0) atomicMin(&s_min, o);
+    __syncthreads();
+    if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+  }
+  if (tid == 0)
+  {
+    __threadfence();
+    const unsigned int done = atomicAdd(&a.tile_counter[1], 1u);
+    if (done == gridDim.x - 1)
+    {
+      a.tile_counter[0] = 0u;
+      a.tile_counter[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
 // Split rollout for problems too small to fill the GPU with one thread per sample (the reference also keeps a split
 // dynamics / cost rollout, rolloutDynamicsKernel + rolloutCostKernel, mppi_common.cu:155-369, and picks the faster by
 // timing).  Kernel 1 runs only the dynamics chain (with the Gaussian sampling fused in) and stores every stepped state

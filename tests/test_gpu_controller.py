@@ -245,17 +245,18 @@ def test_autotune_cache_roundtrip(tmp_path):
 
 @pytest.mark.parametrize("lik", [False, True])
 def test_split_rollout_bit_identical_to_fused(lik):
-    """Rollout mode 1 (dynamics chain, then all (k, t) costs in parallel) gives the fused kernel's costs bit for bit,
-    with and without the likelihood-ratio term, over several iterations of Philox noise."""
+    """Rollout modes 1 (dynamics chain, then all (k, t) costs in parallel) and 2 (four lanes per sample) give the
+    fused kernel's samples and costs bit for bit, with and without the likelihood-ratio term, over several
+    iterations of Philox noise (T = 100 is not a multiple of the cooperative kernel's 16-step groups)."""
     outs = []
-    for mode in (0, 1):
+    for mode in (0, 1, 2):
         dyn = CartpoleDynamics(1.0, 1.0, 1.0)
         dyn.setControlRanges([(-5.0, 5.0)])
         sampler = GaussianDistribution(std_dev=(1.0,), control_cost_coeff=(1.0,) if lik else (0.0,))
         ctrl = VanillaMPPIController(dyn, CartpoleSwingupCost(10.0, 1.0, 100.0, 1.0, 0.0), None, sampler, 0.02, 3, 1.0,
                                      0.0, 100, 2048, seed=5)
         m, avail = ctrl.rolloutMode()
-        assert m == 0 and avail == 3
+        assert m == 0 and avail == 7
         ctrl.setRolloutMode(mode)
         assert ctrl.rolloutMode()[0] == mode
         x0 = np.array([0.0, 0.0, 2.0, 0.0], np.float32)
@@ -263,11 +264,13 @@ def test_split_rollout_bit_identical_to_fused(lik):
         ctrl.computeControl(x0, 1)
         outs.append((ctrl.sample_costs(), ctrl.getControlSeq(), ctrl.control_samples(), ctrl.kernelsPerCompute()))
         ctrl.close()
-    (c0, u0, s0, n0), (c1, u1, s1, n1) = outs
-    assert np.array_equal(s0, s1)
-    assert np.array_equal(c0.view(np.uint32), c1.view(np.uint32))
-    assert np.array_equal(u0, u1)
+    (c0, u0, s0, n0), (c1, u1, s1, n1), (c2, u2, s2, n2) = outs
+    for c, u, smp in ((c1, u1, s1), (c2, u2, s2)):
+        assert np.array_equal(s0, smp)
+        assert np.array_equal(c0.view(np.uint32), c.view(np.uint32))
+        assert np.array_equal(u0, u)
     assert n1 == n0 + 3  # one more kernel per iteration
+    assert n2 == n0
 
 
 def test_split_rollout_unavailable_for_colored_noise():

@@ -1151,18 +1151,24 @@ __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_consta
   if (!s_last) return;
   __threadfence();
 
+  // The instance's chunks are consecutive: partial rows TC floats apart from the first chunk's, and the (sum w,
+  // sum w^2) pairs adjacent.  Loads are issued eight chunks ahead of the (in-order) additions.
   const int c0 = a.inst_chunk0[ch.x];
+  const double* pw = a.part_w + 2 * c0;
   double eta = 0.0, w2 = 0.0;
+#pragma unroll 8
   for (int c = 0; c < d.num_chunks; ++c)
   {
-    eta += __ldcg(&a.part_w[2 * (c0 + c)]);
-    w2 += __ldcg(&a.part_w[2 * (c0 + c) + 1]);
+    eta += __ldcg(pw + 2 * c);
+    w2 += __ldcg(pw + 2 * c + 1);
   }
   const double div = a.given_norm ? (double)a.given_norm[0] : eta;
+  const float* p0 = a.partials + a.part_off[c0];
   for (int j = tid; j < TC; j += blockDim.x)
   {
     double s = 0.0;
-    for (int c = 0; c < d.num_chunks; ++c) s += (double)__ldcg(a.partials + a.part_off[c0 + c] + j);
+#pragma unroll 8
+    for (int c = 0; c < d.num_chunks; ++c) s += (double)__ldcg(p0 + (long long)c * TC + j);
     a.mean_out[d.t_off + j] = (float)(s / div);
   }
   if (tid == 0)

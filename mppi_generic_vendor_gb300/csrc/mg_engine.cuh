@@ -331,7 +331,18 @@ public:
     return MPPI_OK;
   }
   mppi_status get_sample_costs(float* out) override { return copy_per_sample(costs_d_.p, out); }
-  mppi_status get_sample_weights(float* out) override { return copy_per_sample(weights_d_.p, out); }
+  mppi_status get_sample_weights(float* out) override
+  {
+    if (weights_stale_)
+    {
+      // the tiles reduced without materialising the weights: derive them from the costs and the baselines
+      weights_from_costs_kernel<<<dim3(std::max(1, std::min(64, (max_k_ + 255) / 256)), I_), 256, 0, stream_>>>(
+          inst_d_.p, costs_d_.p, bn_d_.p, 1.0f / cp_.lambda, weights_d_.p);
+      MG_CUDA(cudaGetLastError());
+      weights_stale_ = false;
+    }
+    return copy_per_sample(weights_d_.p, out);
+  }
   mppi_status get_control_samples(float* out) override
   {
     MG_CHECK(out, "out must not be NULL");
@@ -903,9 +914,33 @@ private:
     std::vector<int> order(I_);
     for (int i = 0; i < I_; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return T_[x] > T_[y]; });
+    std::vector<int> inst_tile0(I_, 0);
+    std::vector<long long> tile_poff;
+    long long tpoff = 0;
+    max_tiles_per_inst_ = 1;
+    max_k_ = 1;
     for (int i : order)
-      for (int k0 = 0; k0 < K_[i]; k0 += ns_) tiles.push_back(make_int2(i, k0));
+    {
+      inst_tile0[i] = (int)tiles.size();
+      max_tiles_per_inst_ = std::max(max_tiles_per_inst_, (K_[i] + ns_ - 1) / ns_);
+      max_k_ = std::max(max_k_, K_[i]);
+      for (int k0 = 0; k0 < K_[i]; k0 += ns_)
+      {
+        tiles.push_back(make_int2(i, k0));
+        tile_poff.push_back(tpoff);  // an instance's tile rows are consecutive, T*C floats apart
+        tpoff += (long long)T_[i] * C;
+      }
+    }
     num_tiles_ = (int)tiles.size();
+    MG_CHECK(sizeof(double) * (size_t)max_tiles_per_inst_ <= 200 * 1024,
+             "too many rollout tiles in one instance (%d); raise the samples per CTA", max_tiles_per_inst_);
+    MG_TRY(tile_part_d_.alloc((size_t)std::max<long long>(tpoff, 1)));
+    MG_TRY(tile_poff_d_.alloc(tile_poff.size()));
+    MG_TRY(tile_sums_d_.alloc(2 * tile_poff.size()));
+    MG_TRY(tile_min_d_.alloc(tile_poff.size()));
+    MG_TRY(inst_tile0_d_.alloc(I_));
+    MG_CUDA(cudaMemcpy(tile_poff_d_.p, tile_poff.data(), sizeof(long long) * tile_poff.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(inst_tile0_d_.p, inst_tile0.data(), sizeof(int) * I_, cudaMemcpyHostToDevice));
     num_chunks_ = (int)chunks.size();
     num_swork_ = (int)swork.size();
     class_begin_[0] = 0;
@@ -1073,7 +1108,7 @@ private:
 
   mppi_status launch_rollout(int stride, int iter)
   {
-    RolloutArgs<Model> a;
+    RolloutArgs<Model> a{};
     a.inst = inst_d_.p;
     a.tiles = tiles_d_.p;
     a.num_tiles = num_tiles_;
@@ -1095,6 +1130,14 @@ private:
       if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
     a.max_t = max_t_;
     a.sh = make_sample_shared(sp_, cc_);
+    if (tile_reduce_active())
+    {
+      a.tr.partials = tile_part_d_.p;
+      a.tr.poff = tile_poff_d_.p;
+      a.tr.sums = tile_sums_d_.p;
+      a.tr.tmin = tile_min_d_.p;
+      a.tr.lambda_inv = 1.0f / cp_.lambda;
+    }
     if constexpr (Model::kMlp)
       if (!use_analytic_)
       {
@@ -1173,8 +1216,40 @@ private:
     return MPPI_OK;
   }
 
+  // The rollout tiles reduce the samples themselves (TileReduce) unless the surrogate's judge rewrites costs after
+  // the rollout or the split rollout is in use; then weights_update_kernel reads the samples again.
+  bool tile_reduce_active() const { return !(Model::kMlp && !use_analytic_) && rollout_mode_ != 1; }
+
   mppi_status launch_weights()
   {
+    if (tile_reduce_active())
+    {
+      FinalizeArgs f;
+      f.inst = inst_d_.p;
+      f.num_instances = I_;
+      f.inst_tile0 = inst_tile0_d_.p;
+      f.tile_samples = ns_;
+      f.tr.partials = tile_part_d_.p;
+      f.tr.poff = tile_poff_d_.p;
+      f.tr.sums = tile_sums_d_.p;
+      f.tr.tmin = tile_min_d_.p;
+      f.tr.lambda_inv = 1.0f / cp_.lambda;
+      f.baseline_bits = baseline_bits_d_.p;
+      f.inst_done = counters_d_.p + 2;
+      f.noise_counter = counters_d_.p + 3;
+      f.mean_out = mean_d_.p;
+      f.baseline_norm = bn_d_.p;
+      f.stats = stats_d_.p;
+      f.C = C;
+      const size_t smem = sizeof(double) * (size_t)max_tiles_per_inst_;
+      if (smem > 48 * 1024)
+        MG_CUDA(cudaFuncSetAttribute(tile_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      tile_finalize_kernel<<<I_, 256, smem, stream_>>>(f);
+      MG_CUDA(cudaGetLastError());
+      weights_stale_ = true;
+      return MPPI_OK;
+    }
+    weights_stale_ = false;
     WeightsArgs a;
     a.inst = inst_d_.p;
     a.chunks = chunks_d_.p;
@@ -1369,6 +1444,14 @@ private:
   long long total_u_ = 0;      // control-sample floats over all instances
   bool split_ = false;         // split dynamics / cost rollout (rollout mode 1)
   int rollout_mode_ = 0;       // 0 fused, 1 split, 2 cooperative (four lanes per sample)
+  // tile reduction (TileReduce): per tile partial rows, (sum w, sum w^2), minimum; first tile of each instance
+  DevBuf<float> tile_part_d_;
+  DevBuf<long long> tile_poff_d_;
+  DevBuf<double> tile_sums_d_;
+  DevBuf<unsigned int> tile_min_d_;
+  DevBuf<int> inst_tile0_d_;
+  int max_tiles_per_inst_ = 1, max_k_ = 1;
+  bool weights_stale_ = false;  // weights_d_ not yet derived from the last costs
   DevBuf<float> states_d_;     // split rollout: stepped states [instance][k][t][S]
   int mlp_precision_ = 0;      // 0 bf16 / 1 fp8 tensor cores, 2 fp32 CUDA cores
   bool use_analytic_ = false;  // MLP models: roll out the analytic model instead
@@ -1478,7 +1561,7 @@ mppi_status standalone_rollout(const void* dyn, const void* cost, const mppi_sam
   MG_CUDA(cudaMemcpyAsync(cost_d.p, cost, sizeof(typename Model::CostParams), cudaMemcpyHostToDevice, s));
   MG_CUDA(cudaMemsetAsync(cnt_d.p, 0, sizeof(unsigned int) * 4, s));
   fill_u32_kernel<<<1, 32, 0, s>>>(cnt_d.p + 2, kOrderedPosInf, 1);
-  RolloutArgs<Model> a;
+  RolloutArgs<Model> a{};
   a.inst = inst_d.p;
   a.tiles = tiles_d.p;
   a.num_tiles = (int)tiles.size();

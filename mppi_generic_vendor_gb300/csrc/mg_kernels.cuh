@@ -163,6 +163,20 @@ __global__ void __launch_bounds__(256) gaussian_sample_kernel(const __grid_const
 // folds its samples into the instance's minimum cost with one atomicMin, which the weight kernel consumes as the
 // baseline.  The kernel is persistent: CTAs pull (instance, first sample) tiles from a work list ordered by
 // decreasing cost through an atomic counter; the last CTA to finish resets the counters for the next launch.
+// Weighted reduction done at the end of each rollout tile (the update kernel then only combines tiles): with the
+// tile's own minimum cost b_l as baseline, w = expf(-(c - b_l) / lambda) (the arithmetic of the weight transform),
+// the tile's partial sums S_l[t][c] = sum_k w_k u_k[t][c] (FP32, samples in index order) and sum w, sum w^2 (FP64).
+// tile_finalize_kernel rescales each tile by exp(-(b_l - b) / lambda) with the instance's minimum b, which is the
+// same weighted mean up to rounding, without reading the control samples from HBM a second time.
+struct TileReduce
+{
+  float* partials;          // per work tile: T*C floats at poff[tile]; null: weights_update_kernel reduces instead
+  const long long* poff;
+  double* sums;             // per work tile: sum w, sum w^2 (tile baseline)
+  unsigned int* tmin;       // per work tile: ordered-int minimum cost
+  float lambda_inv;
+};
+
 template <class Model>
 struct RolloutArgs
 {
@@ -183,7 +197,72 @@ struct RolloutArgs
   int use_likelihood;
   int max_t;  // longest horizon of the handle
   SampleShared sh;
+  TileReduce tr;
 };
+
+// The tile epilogue (all threads of the CTA; the tile's costs are in a.costs and its minimum in tile_min).  s_w holds
+// one float per sample of the tile, s_red 64 doubles.
+template <int C, class Args>
+__device__ __forceinline__ void tile_reduce(const Args& a, const InstDesc& d, int tile, int first, int rows,
+                                            unsigned int tile_min, float* s_w, double* s_red)
+{
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const double bl = (double)ordered_to_float(tile_min);
+  const double linv = (double)a.tr.lambda_inv;
+  double sw = 0.0, sw2 = 0.0;
+  for (int k = tid; k < rows; k += nt)
+  {
+    const float c = __ldcg(a.costs + d.k_off + first + k);
+    const float w = expf((float)(-((double)c - bl) * linv));
+    s_w[k] = w;
+    sw += (double)w;
+    sw2 += (double)w * (double)w;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+  {
+    sw += __shfl_xor_sync(0xffffffffu, sw, off);
+    sw2 += __shfl_xor_sync(0xffffffffu, sw2, off);
+  }
+  if (lane == 0)
+  {
+    s_red[warp] = sw;
+    s_red[32 + warp] = sw2;
+  }
+  __syncthreads();
+  const int TC = d.T * C;
+  const float* u = a.samples + d.u_off + (long long)first * TC;  // written earlier in this launch or by the sampler
+  float* out = a.tr.partials + a.tr.poff[tile];
+  for (int j = tid; j < TC; j += nt)
+  {
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    int k = 0;
+    for (; k + 4 <= rows; k += 4)
+    {
+      const float v0 = __ldcg(u + (long long)k * TC + j), v1 = __ldcg(u + (long long)(k + 1) * TC + j);
+      const float v2 = __ldcg(u + (long long)(k + 2) * TC + j), v3 = __ldcg(u + (long long)(k + 3) * TC + j);
+      a0 = fmaf(s_w[k], v0, a0);
+      a1 = fmaf(s_w[k + 1], v1, a1);
+      a2 = fmaf(s_w[k + 2], v2, a2);
+      a3 = fmaf(s_w[k + 3], v3, a3);
+    }
+    for (; k < rows; ++k) a0 = fmaf(s_w[k], __ldcg(u + (long long)k * TC + j), a0);
+    out[j] = (a0 + a1) + (a2 + a3);
+  }
+  if (tid == 0)
+  {
+    double t0 = 0.0, t1 = 0.0;
+    for (int wi = 0; wi < (nt + 31) / 32; ++wi)
+    {
+      t0 += s_red[wi];
+      t1 += s_red[32 + wi];
+    }
+    a.tr.sums[2 * tile] = t0;
+    a.tr.sums[2 * tile + 1] = t1;
+    a.tr.tmin[tile] = tile_min;
+  }
+  __syncthreads();
+}
 
 // The running cost of step t (state cost on the stepped output y, control cost, likelihood-ratio term), in the
 // reference's arithmetic (mppi_common.cu:105-144).  kLik: the likelihood-ratio term is on (control_cost_coeff != 0);
@@ -300,6 +379,8 @@ __global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ Rol
   __shared__ __align__(16) float stage[NS * ROW];
   __shared__ int s_tile;
   __shared__ unsigned int s_min;
+  __shared__ float s_tw[NS];  // tile_reduce: the tile's weights
+  __shared__ double s_tred[64];
 
   const int tid = threadIdx.x;
   for (;;)
@@ -383,6 +464,7 @@ __global__ void __launch_bounds__(NS) rollout_kernel(const __grid_constant__ Rol
     if ((tid & 31) == 0) atomicMin(&s_min, o);
     __syncthreads();
     if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+    if (a.tr.partials) tile_reduce<C>(a, d, tile, w.y, rows, s_min, s_tw, s_tred);
   }
   // last CTA out resets the work counters for the next launch
   if (tid == 0)
@@ -458,6 +540,8 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
   constexpr int G = 4 / C;
   __shared__ int s_tile;
   __shared__ unsigned int s_min;
+  __shared__ float s_tw[NS];  // tile_reduce: the tile's weights
+  __shared__ double s_tred[64];
   const int tid = threadIdx.x;
   const uint32_t counter = f.noise_counter ? *f.noise_counter : 0u;
   for (;;)
@@ -524,6 +608,7 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
     if ((tid & 31) == 0) atomicMin(&s_min, o);
     __syncthreads();
     if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+    if (a.tr.partials) tile_reduce<C>(a, d, tile, w.y, min(NS, d.K - w.y), s_min, s_tw, s_tred);
   }
   if (tid == 0)
   {
@@ -555,6 +640,8 @@ __global__ void __launch_bounds__(4 * NS) rollout_coop_kernel(const __grid_const
   constexpr int L = 4;      // lanes per sample
   __shared__ int s_tile;
   __shared__ unsigned int s_min;
+  __shared__ float s_tw[NS];  // tile_reduce: the tile's weights
+  __shared__ double s_tred[64];
   const int tid = threadIdx.x, j = tid & (L - 1);
   const uint32_t counter = f.noise_counter ? *f.noise_counter : 0u;
   for (;;)
@@ -650,6 +737,7 @@ __global__ void __launch_bounds__(4 * NS) rollout_coop_kernel(const __grid_const
     if ((tid & 31) == 0) atomicMin(&s_min, o);
     __syncthreads();
     if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+    if (a.tr.partials) tile_reduce<C>(a, d, tile, w.y, min(NS, d.K - w.y), s_min, s_tw, s_tred);
   }
   if (tid == 0)
   {
@@ -835,6 +923,8 @@ __global__ void __launch_bounds__(NS) rollout_kernel_bulk(const __grid_constant_
   __shared__ __align__(8) uint64_t mbar[2][WARPS];
   __shared__ int s_tile;
   __shared__ unsigned int s_min;
+  __shared__ float s_tw[NS];  // tile_reduce: the tile's weights
+  __shared__ double s_tred[64];
   __shared__ int s_fail;  // CTA-uniform stop flag (read only after a barrier)
 
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -932,6 +1022,7 @@ __global__ void __launch_bounds__(NS) rollout_kernel_bulk(const __grid_constant_
     if ((tid & 31) == 0) atomicMin(&s_min, o);
     __syncthreads();
     if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+    if (a.tr.partials) tile_reduce<C>(a, d, tile, w.y, min(NS, d.K - w.y), s_min, s_tw, s_tred);
   }
   if (tid == 0)
   {
@@ -1189,6 +1280,105 @@ __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_consta
       __threadfence();
     }
   }
+}
+
+// Combines the rollout tiles' partial reductions (TileReduce) into each instance's new mean, one CTA per instance:
+// tile l is rescaled by r_l = exp(-(b_l - b) / lambda) (FP64), b the instance's minimum cost; eta = sum_l r_l sum_w_l,
+// mean[j] = sum_l r_l S_l[j] / eta, summed in tile order.  Then the same bookkeeping as weights_update_kernel's
+// last block.  Dynamic shared memory: one double per tile of the largest instance.
+struct FinalizeArgs
+{
+  const InstDesc* inst;
+  int num_instances;
+  const int* inst_tile0;  // per instance: its first tile (an instance's tiles are consecutive)
+  int tile_samples;
+  TileReduce tr;
+  unsigned int* baseline_bits;
+  unsigned int* inst_done;
+  unsigned int* noise_counter;
+  float* mean_out;
+  float* baseline_norm;
+  double* stats;
+  int C;
+};
+
+static __global__ void __launch_bounds__(256) tile_finalize_kernel(const __grid_constant__ FinalizeArgs a)
+{
+  extern __shared__ double s_r[];
+  __shared__ double s_red[2][8];
+  const int i = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const InstDesc d = a.inst[i];
+  const int nt = (d.K + a.tile_samples - 1) / a.tile_samples;
+  const int t0 = a.inst_tile0[i];
+  const float b = ordered_to_float(a.baseline_bits[i]);
+  const double bd = (double)b;
+  const double linv = (double)a.tr.lambda_inv;
+  double eta = 0.0, w2 = 0.0;
+  for (int l = tid; l < nt; l += blockDim.x)
+  {
+    const double r = exp(-((double)ordered_to_float(a.tr.tmin[t0 + l]) - bd) * linv);
+    s_r[l] = r;
+    eta += r * __ldcg(a.tr.sums + 2 * (t0 + l));
+    w2 += r * r * __ldcg(a.tr.sums + 2 * (t0 + l) + 1);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+  {
+    eta += __shfl_xor_sync(0xffffffffu, eta, off);
+    w2 += __shfl_xor_sync(0xffffffffu, w2, off);
+  }
+  if (lane == 0)
+  {
+    s_red[0][warp] = eta;
+    s_red[1][warp] = w2;
+  }
+  __syncthreads();
+  eta = 0.0;
+  w2 = 0.0;
+  for (int wi = 0; wi < (int)(blockDim.x >> 5); ++wi)
+  {
+    eta += s_red[0][wi];
+    w2 += s_red[1][wi];
+  }
+  const int TC = d.T * a.C;
+  const float* p0 = a.tr.partials + a.tr.poff[t0];
+  for (int j = tid; j < TC; j += blockDim.x)
+  {
+    double s = 0.0;
+#pragma unroll 8
+    for (int l = 0; l < nt; ++l) s += s_r[l] * (double)__ldcg(p0 + (long long)l * TC + j);
+    a.mean_out[d.t_off + j] = (float)(s / eta);
+  }
+  if (tid == 0)
+  {
+    a.baseline_norm[2 * i] = b;
+    a.baseline_norm[2 * i + 1] = (float)eta;
+    a.stats[3 * i] = eta;
+    a.stats[3 * i + 1] = w2;
+    a.stats[3 * i + 2] = bd;
+    a.baseline_bits[i] = kOrderedPosInf;
+    __threadfence();
+    const unsigned int fin = atomicAdd(a.inst_done, 1u);
+    if (fin == (unsigned int)(a.num_instances - 1))
+    {
+      *a.inst_done = 0u;
+      if (a.noise_counter) *a.noise_counter += 1u;
+      __threadfence();
+    }
+  }
+}
+
+// Weights w = expf(-(c - b) / lambda) of every sample from its cost and its instance's baseline (baseline_norm), as
+// weights_update_kernel computes them; used to serve mppi_get_sample_weights when the tiles did the reduction.
+static __global__ void weights_from_costs_kernel(const InstDesc* inst, const float* costs, const float* baseline_norm,
+                                                 float lambda_inv, float* weights)
+{
+  const int i = blockIdx.y;
+  const InstDesc d = inst[i];
+  const double bd = (double)baseline_norm[2 * i];
+  const double linv = (double)lambda_inv;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.K; k += gridDim.x * blockDim.x)
+    weights[d.k_off + k] = expf((float)(-((double)costs[d.k_off + k] - bd) * linv));
 }
 
 // Per-system minimum of costs into ordered-int slots (the baseline pass of fullGPUcomputeWeights,

@@ -1216,9 +1216,9 @@ private:
     return MPPI_OK;
   }
 
-  // The rollout tiles reduce the samples themselves (TileReduce) unless the surrogate's judge rewrites costs after
-  // the rollout or the split rollout is in use; then weights_update_kernel reads the samples again.
-  bool tile_reduce_active() const { return !(Model::kMlp && !use_analytic_) && rollout_mode_ != 1; }
+  // The rollout tiles reduce the samples themselves (TileReduce) unless the surrogate rollout is in use (its judge
+  // rewrites costs after the rollout); then weights_update_kernel reads the samples again.
+  bool tile_reduce_active() const { return !(Model::kMlp && !use_analytic_); }
 
   mppi_status launch_weights()
   {

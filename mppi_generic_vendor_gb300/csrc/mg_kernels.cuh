@@ -832,6 +832,8 @@ __global__ void __launch_bounds__(WARPS * 32) rollout_cost_kernel(const __grid_c
   extern __shared__ float s_cost[];  // [WARPS][T_max]
   __shared__ int s_tile;
   __shared__ unsigned int s_min;
+  __shared__ float s_tw[NS];  // tile_reduce: the tile's weights
+  __shared__ double s_tred[64];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (;;)
   {
@@ -882,6 +884,7 @@ __global__ void __launch_bounds__(WARPS * 32) rollout_cost_kernel(const __grid_c
     if (lane == 0) atomicMin(&s_min, o);
     __syncthreads();
     if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
+    if (a.tr.partials) tile_reduce<C>(a, d, tile, w.y, rows, s_min, s_tw, s_tred);
   }
   if (tid == 0)
   {

@@ -126,28 +126,6 @@ inline SampleShared make_sample_shared(const mppi_sampling_params& sp, const mpp
   return sh;
 }
 
-// Controller::smoothControlTrajectoryHelper (controller.cuh:573-607).
-inline void smooth_control(float* u, int T, int C)
-{
-  const float coef[5] = { -3.0f / 35.0f, 12.0f / 35.0f, 17.0f / 35.0f, 12.0f / 35.0f, -3.0f / 35.0f };
-  std::vector<float> buf((size_t)(T + 4) * C);
-  for (int c = 0; c < C; ++c)
-  {
-    buf[c] = u[c];
-    buf[C + c] = u[c];
-    for (int t = 0; t < T; ++t) buf[(size_t)(t + 2) * C + c] = u[(size_t)t * C + c];
-    buf[(size_t)(T + 2) * C + c] = u[(size_t)(T - 1) * C + c];
-    buf[(size_t)(T + 3) * C + c] = u[(size_t)(T - 1) * C + c];
-  }
-  for (int t = 1; t < T; ++t)
-    for (int c = 0; c < C; ++c)
-    {
-      float acc = 0.0f;
-      for (int j = 0; j < 5; ++j) acc += coef[j] * buf[(size_t)(t + j) * C + c];
-      u[(size_t)t * C + c] = acc;
-    }
-}
-
 template <class Model>
 class Engine : public EngineBase
 {
@@ -200,7 +178,7 @@ public:
     const int judge = (Model::kMlp && !use_analytic_ && judge_total_ > 0) ? 3 : 0;
     if (fused()) sampler = 0;
     if (fused() && split_) sampler = 1;  // the cost kernel
-    return (sampler + 2 + judge) * cp_.num_iters;
+    return (sampler + 2 + judge) * cp_.num_iters + 1;  // + the smoothing / constraint kernel
   }
 
   // ------------------------------------------------------------------------------------------------ computeControl
@@ -766,6 +744,8 @@ private:
     MG_TRY(out_bn_h_.alloc((size_t)2 * I_));
     MG_TRY(out_stats_h_.alloc((size_t)3 * I_));
     MG_TRY(status_h_.alloc(1));
+    MG_TRY(first_d_.alloc((size_t)I_ * C));
+    MG_TRY(first_h_.alloc((size_t)I_ * C));
     max_t_ = *std::max_element(T_.begin(), T_.end());  // sizes per-launch shared buffers (split cost kernel)
     if (Model::kMlp) ns_ = kMlpSamplesPerCta;
     MG_TRY(build_work_lists());
@@ -1286,6 +1266,10 @@ private:
       MG_TRY(launch_rollout(stride, it));
       MG_TRY(launch_weights());
     }
+    // smoothing + constraints of the new nominal sequences (the host post-processing of computeControl)
+    finish_controls_kernel<C><<<I_, 256, sizeof(float) * (size_t)(max_t_ + 4) * C, stream_>>>(
+        inst_d_.p, mean_d_.p, first_d_.p, make_sample_shared(sp_, cc_));
+    MG_CUDA(cudaGetLastError());
     return MPPI_OK;
   }
 
@@ -1300,6 +1284,7 @@ private:
     MG_CUDA(cudaMemcpyAsync(out_bn_h_.p, bn_d_.p, sizeof(float) * 2 * I_, cudaMemcpyDeviceToHost, stream_));
     MG_CUDA(cudaMemcpyAsync(out_stats_h_.p, stats_d_.p, sizeof(double) * 3 * I_, cudaMemcpyDeviceToHost, stream_));
     MG_CUDA(cudaMemcpyAsync(status_h_.p, counters_d_.p + 4, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_));
+    MG_CUDA(cudaMemcpyAsync(first_h_.p, first_d_.p, sizeof(float) * I_ * C, cudaMemcpyDeviceToHost, stream_));
     return MPPI_OK;
   }
 
@@ -1360,19 +1345,11 @@ private:
     memcpy(control_.data(), out_mean_h_.p, sizeof(float) * control_.size());
     memcpy(baseline_norm_.data(), out_bn_h_.p, sizeof(float) * 2 * I_);
     memcpy(stats_.data(), out_stats_h_.p, sizeof(double) * 3 * I_);
+    // control_ arrives smoothed and constrained (finish_controls_kernel); first_h_ holds the unclamped first controls
+    memcpy(last_pre_smooth_.data(), first_h_.p, sizeof(float) * I_ * C);
     bool bad = false;
     for (int i = 0; i < I_; ++i)
-    {
       if (!std::isfinite(baseline_norm_[2 * i]) || !(stats_[3 * i] > 0.0)) bad = true;
-      float* u = control_.data() + t_off_[i];
-      const int T = T_[i];
-      for (int c = 0; c < C; ++c) last_pre_smooth_[(size_t)i * C + c] = u[c];
-      smooth_control(u, T, C);
-      for (int t = 0; t < T; ++t)
-        for (int c = 0; c < C; ++c)
-          u[(size_t)t * C + c] = enforce_constraint(u[(size_t)t * C + c], cc_.lower[c], cc_.upper[c],
-                                                    cc_.deadband[c], cc_.zero_control[c]);
-    }
     // the nominal state trajectory is rolled out when it is first read (get_state_seq), from these snapshots
     traj_u_ = control_;
     traj_x0_.assign(x0, x0 + (size_t)I_ * S);
@@ -1439,6 +1416,8 @@ private:
   PinnedBuf<float> x0_h_, mean_h_, out_mean_h_, out_bn_h_;
   PinnedBuf<double> out_stats_h_;
   PinnedBuf<unsigned int> status_h_;
+  DevBuf<float> first_d_;    // per instance: unclamped first control of the last solve (slide history)
+  PinnedBuf<float> first_h_;
   std::vector<float> mlp_host_;  // surrogate parameters as the tensor cores see them (MLP models only)
   DevBuf<float> mlp_d_;
   long long total_u_ = 0;      // control-sample floats over all instances

@@ -1384,6 +1384,47 @@ static __global__ void weights_from_costs_kernel(const InstDesc* inst, const flo
     weights[d.k_off + k] = expf((float)(-((double)costs[d.k_off + k] - bd) * linv));
 }
 
+// Controller::smoothControlTrajectoryHelper (controller.cuh:573-607) and the final constraint pass, on the device:
+// one CTA per instance smooths its new mean in place with the 5-tap Savitzky-Golay filter [-3, 12, 17, 12, -3] / 35
+// (edges replicated, the first control kept; each tap product rounded to FP32 and added in tap order), clamps it,
+// and records the unclamped first control (the slide history).  Dynamic shared memory: (T_max + 4) * C floats.
+template <int C>
+__global__ void __launch_bounds__(256) finish_controls_kernel(const InstDesc* inst, float* mean, float* first_out,
+                                                              const __grid_constant__ SampleShared sh)
+{
+  extern __shared__ float buf[];
+  const int i = blockIdx.x, tid = threadIdx.x;
+  const InstDesc d = inst[i];
+  const int T = d.T;
+  float* u = mean + d.t_off;
+  for (int e = tid; e < (T + 4) * C; e += blockDim.x)
+  {
+    const int tt = e / C, c = e - tt * C;
+    const int src = min(max(tt - 2, 0), T - 1);
+    buf[e] = u[src * C + c];
+  }
+  __syncthreads();
+  const float coef[5] = { -3.0f / 35.0f, 12.0f / 35.0f, 17.0f / 35.0f, 12.0f / 35.0f, -3.0f / 35.0f };
+  for (int e = tid; e < T * C; e += blockDim.x)
+  {
+    const int t = e / C, c = e - t * C;
+    float v;
+    if (t == 0)
+    {
+      v = buf[2 * C + c];
+      first_out[i * C + c] = v;
+    }
+    else
+    {
+      float acc = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 5; ++j) acc += coef[j] * buf[(t + j) * C + c];
+      v = acc;
+    }
+    u[e] = enforce_constraint(v, sh.lower[c], sh.upper[c], sh.deadband[c], sh.zero[c]);
+  }
+}
+
 // Per-system minimum of costs into ordered-int slots (the baseline pass of fullGPUcomputeWeights,
 // computeBaselineCost, mppi_common.cu:938-992), for the kernel-level weight-transform entry point.
 static __global__ void min_cost_kernel(const float* costs, int num_rollouts, int num_systems, unsigned int* out_bits)

@@ -55,15 +55,25 @@ struct DevBuf
 {
   T* p = nullptr;
   size_t n = 0;
+  bool owned = true;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { reset(); }
   void reset()
   {
-    if (p) cudaFree(p);
+    if (p && owned) cudaFree(p);
     p = nullptr;
     n = 0;
+    owned = true;
+  }
+  // Point at count elements inside a block another buffer owns.
+  void view(T* ptr, size_t count)
+  {
+    reset();
+    p = ptr;
+    n = count;
+    owned = false;
   }
   mppi_status alloc(size_t count)
   {
@@ -87,15 +97,25 @@ struct PinnedBuf
 {
   T* p = nullptr;
   size_t n = 0;
+  bool owned = true;
   PinnedBuf() = default;
   PinnedBuf(const PinnedBuf&) = delete;
   PinnedBuf& operator=(const PinnedBuf&) = delete;
   ~PinnedBuf() { reset(); }
   void reset()
   {
-    if (p) cudaFreeHost(p);
+    if (p && owned) cudaFreeHost(p);
     p = nullptr;
     n = 0;
+    owned = true;
+  }
+  // Point at count elements inside a block another buffer owns.
+  void view(T* ptr, size_t count)
+  {
+    reset();
+    p = ptr;
+    n = count;
+    owned = false;
   }
   mppi_status alloc(size_t count)
   {

@@ -723,8 +723,39 @@ private:
     MG_TRY(weights_d_.alloc(total_k));
     MG_CUDA(cudaMemset(costs_d_.p, 0, sizeof(float) * total_k));
     MG_CUDA(cudaMemset(weights_d_.p, 0, sizeof(float) * total_k));
-    MG_TRY(mean_d_.alloc(total_t));
-    MG_TRY(x0_d_.alloc((size_t)I_ * S));
+    // Per-solve I/O in one block so a solve needs one host-to-device and one device-to-host copy:
+    //   [x0 | mean] is copied in, [mean | first | baseline,normaliser | status | stats] is copied out.
+    {
+      auto up16 = [](size_t b) { return (b + 15) / 16 * 16; };
+      const size_t o_x0 = 0, o_mean = o_x0 + sizeof(float) * I_ * S;
+      const size_t o_first = o_mean + sizeof(float) * total_t;
+      const size_t o_bn = o_first + sizeof(float) * I_ * C;
+      const size_t o_status = o_bn + sizeof(float) * 2 * I_;
+      const size_t o_stats = up16(o_status + sizeof(unsigned int));
+      const size_t o_end = o_stats + sizeof(double) * 3 * I_;
+      io_in_bytes_ = o_mean + sizeof(float) * total_t;
+      io_out_off_ = o_mean;
+      io_out_bytes_ = o_end - o_mean;
+      MG_TRY(io_d_.alloc(o_end));
+      MG_CUDA(cudaMemset(io_d_.p, 0, o_end));
+      MG_TRY(io_in_h_.alloc(io_in_bytes_));
+      MG_TRY(io_out_h_.alloc(io_out_bytes_));
+      unsigned char* d = io_d_.p;
+      x0_d_.view(reinterpret_cast<float*>(d + o_x0), (size_t)I_ * S);
+      mean_d_.view(reinterpret_cast<float*>(d + o_mean), total_t);
+      first_d_.view(reinterpret_cast<float*>(d + o_first), (size_t)I_ * C);
+      bn_d_.view(reinterpret_cast<float*>(d + o_bn), (size_t)2 * I_);
+      status_d_ = reinterpret_cast<unsigned int*>(d + o_status);
+      stats_d_.view(reinterpret_cast<double*>(d + o_stats), (size_t)3 * I_);
+      x0_h_.view(reinterpret_cast<float*>(io_in_h_.p + o_x0), (size_t)I_ * S);
+      mean_h_.view(reinterpret_cast<float*>(io_in_h_.p + o_mean), total_t);
+      unsigned char* h = io_out_h_.p - o_mean;  // same offsets as the device block
+      out_mean_h_.view(reinterpret_cast<float*>(h + o_mean), total_t);
+      first_h_.view(reinterpret_cast<float*>(h + o_first), (size_t)I_ * C);
+      out_bn_h_.view(reinterpret_cast<float*>(h + o_bn), (size_t)2 * I_);
+      status_h_.view(reinterpret_cast<unsigned int*>(h + o_status), 1);
+      out_stats_h_.view(reinterpret_cast<double*>(h + o_stats), (size_t)3 * I_);
+    }
     MG_TRY(dyn_d_.alloc(I_));
     MG_TRY(cost_d_.alloc(I_));
     MG_CUDA(cudaMemcpy(dyn_d_.p, dyn_.data(), sizeof(DynParams) * I_, cudaMemcpyHostToDevice));
@@ -732,20 +763,10 @@ private:
     MG_TRY(baseline_bits_d_.alloc(I_));
     MG_TRY(arrive_d_.alloc(I_));
     MG_TRY(counters_d_.alloc(8));
-    MG_TRY(bn_d_.alloc((size_t)2 * I_));
-    MG_TRY(stats_d_.alloc((size_t)3 * I_));
     MG_CUDA(cudaMemset(arrive_d_.p, 0, sizeof(unsigned int) * I_));
     MG_CUDA(cudaMemset(counters_d_.p, 0, sizeof(unsigned int) * 8));
     fill_u32_kernel<<<1, 256, 0, stream_>>>(baseline_bits_d_.p, kOrderedPosInf, I_);
     MG_CUDA(cudaGetLastError());
-    MG_TRY(x0_h_.alloc((size_t)I_ * S));
-    MG_TRY(mean_h_.alloc(total_t));
-    MG_TRY(out_mean_h_.alloc(total_t));
-    MG_TRY(out_bn_h_.alloc((size_t)2 * I_));
-    MG_TRY(out_stats_h_.alloc((size_t)3 * I_));
-    MG_TRY(status_h_.alloc(1));
-    MG_TRY(first_d_.alloc((size_t)I_ * C));
-    MG_TRY(first_h_.alloc((size_t)I_ * C));
     max_t_ = *std::max_element(T_.begin(), T_.end());  // sizes per-launch shared buffers (split cost kernel)
     if (Model::kMlp) ns_ = kMlpSamplesPerCta;
     MG_TRY(build_work_lists());
@@ -1101,7 +1122,7 @@ private:
     a.costs = costs_d_.p;
     a.baseline_bits = baseline_bits_d_.p;
     a.tile_counter = counters_d_.p;
-    a.status = counters_d_.p + 4;
+    a.status = status_d_;
     a.dt = cp_.dt;
     a.lambda = cp_.lambda;
     a.alpha = cp_.alpha;
@@ -1277,14 +1298,10 @@ private:
   mppi_status enqueue_solve(int stride)
   {
     const size_t tc = control_.size();
-    MG_CUDA(cudaMemcpyAsync(x0_d_.p, x0_h_.p, sizeof(float) * I_ * S, cudaMemcpyHostToDevice, stream_));
-    MG_CUDA(cudaMemcpyAsync(mean_d_.p, mean_h_.p, sizeof(float) * tc, cudaMemcpyHostToDevice, stream_));
+    (void)tc;
+    MG_CUDA(cudaMemcpyAsync(io_d_.p, io_in_h_.p, io_in_bytes_, cudaMemcpyHostToDevice, stream_));
     MG_TRY(enqueue_kernels(stride));
-    MG_CUDA(cudaMemcpyAsync(out_mean_h_.p, mean_d_.p, sizeof(float) * tc, cudaMemcpyDeviceToHost, stream_));
-    MG_CUDA(cudaMemcpyAsync(out_bn_h_.p, bn_d_.p, sizeof(float) * 2 * I_, cudaMemcpyDeviceToHost, stream_));
-    MG_CUDA(cudaMemcpyAsync(out_stats_h_.p, stats_d_.p, sizeof(double) * 3 * I_, cudaMemcpyDeviceToHost, stream_));
-    MG_CUDA(cudaMemcpyAsync(status_h_.p, counters_d_.p + 4, sizeof(unsigned int), cudaMemcpyDeviceToHost, stream_));
-    MG_CUDA(cudaMemcpyAsync(first_h_.p, first_d_.p, sizeof(float) * I_ * C, cudaMemcpyDeviceToHost, stream_));
+    MG_CUDA(cudaMemcpyAsync(io_out_h_.p, io_d_.p + io_out_off_, io_out_bytes_, cudaMemcpyDeviceToHost, stream_));
     return MPPI_OK;
   }
 
@@ -1337,7 +1354,7 @@ private:
     if (status_h_.p[0] != 0u)
     {
       status_h_.p[0] = 0u;
-      MG_CUDA(cudaMemsetAsync(counters_d_.p + 4, 0, sizeof(unsigned int), stream_));
+      MG_CUDA(cudaMemsetAsync(status_d_, 0, sizeof(unsigned int), stream_));
       MG_CUDA(cudaStreamSynchronize(stream_));
       set_error("a bounded wait for staged control data gave up inside the rollout kernel");
       return MPPI_ETIMEOUT;
@@ -1418,6 +1435,12 @@ private:
   PinnedBuf<unsigned int> status_h_;
   DevBuf<float> first_d_;    // per instance: unclamped first control of the last solve (slide history)
   PinnedBuf<float> first_h_;
+  // one block per direction for the per-solve copies; x0_d_, mean_d_, first_d_, bn_d_, stats_d_ and the host
+  // staging buffers are views into them
+  DevBuf<unsigned char> io_d_;
+  PinnedBuf<unsigned char> io_in_h_, io_out_h_;
+  size_t io_in_bytes_ = 0, io_out_off_ = 0, io_out_bytes_ = 0;
+  unsigned int* status_d_ = nullptr;  // set non-zero by a kernel whose bounded wait gave up
   std::vector<float> mlp_host_;  // surrogate parameters as the tensor cores see them (MLP models only)
   DevBuf<float> mlp_d_;
   long long total_u_ = 0;      // control-sample floats over all instances

@@ -286,3 +286,60 @@ def A_colored():
     from mppi_generic_vendor_gb300 import ColoredNoiseDistribution
 
     return ColoredNoiseDistribution(std_dev=(0.5, 0.5), exponents=(1.0, 1.0))
+
+
+def test_cooperative_rollout_bit_identical_for_two_controls():
+    """Mode 2 with C = 2 (a quad holds two steps) on the kinematic bicycle: samples, costs and the update equal
+    mode 0's bit for bit; the weights served after the tile reduction equal the oracle's within 1e-5."""
+    from mppi_generic_vendor_gb300 import BicycleDynamics, CostmapCost
+    from mppi_generic_vendor_gb300.workloads import gaussian_bump_costmap
+
+    cmap = gaussian_bump_costmap(3, size=128)
+    K, T = 3000, 50
+    rng = np.random.default_rng(31)
+    eps = rng.standard_normal(K * T * 2).astype(np.float32)
+    init = rng.uniform(-0.3, 0.3, (T, 2)).astype(np.float32)
+    x0 = np.array([6.0, 5.0, 0.4, 4.0], np.float32)
+    outs = []
+    for mode in (0, 2):
+        cost = CostmapCost(map_coeff=1.0, speed_target=8.0, speed_coeff=1.0, steer_coeff=0.5, terminal_coeff=2.0,
+                           costmap=cmap, resolution=0.1, origin=(0.0, 0.0))
+        ctrl = VanillaMPPIController(BicycleDynamics(2.5), cost, None, GaussianDistribution(std_dev=(1.0, 0.3)), 0.02,
+                                     1, 2.0, 0.0, T, K)
+        ctrl.setRolloutMode(mode)
+        ctrl.setControlSeq(init.T)
+        ctrl.injectNoise(eps)
+        ctrl.computeControl(x0, 1)
+        outs.append((ctrl.sample_costs(), ctrl.getControlSeq(), ctrl.sample_weights(), ctrl.control_samples()))
+        ref = oracle.compute_control(ctrl.model_id, ctrl._dyn_arr[0], ctrl._cost_arr[0], ctrl.getParams(),
+                                     ctrl.sampler_.to_c(), ctrl.constraints_, K, T, 2, 4, x0, eps, init,
+                                     costmap=(cmap, 0.1, (0.0, 0.0)))
+        w = outs[-1][2]
+        big = ref["weights"] > 1e-30
+        assert np.all(np.abs(w[big] - ref["weights"][big]) <= 1e-5 * ref["weights"][big])
+        check_control(outs[-1][1].T, ref)
+        ctrl.close()
+    (c0, u0, w0, s0), (c2, u2, w2, s2) = outs
+    assert np.array_equal(s0, s2)
+    assert np.array_equal(c0.view(np.uint32), c2.view(np.uint32))
+    assert np.array_equal(u0, u2)
+    assert np.array_equal(w0, w2)
+
+
+def test_device_only_solves_match_compute_control():
+    """enqueueSolve runs the same device work as computeControl, smoothing and constraints included: n device-only
+    solves from the same start leave the nominal sequence computeControl produces after n calls."""
+    outs = []
+    for device_only in (False, True):
+        ctrl, _, _ = cartpole_controller(1024, 64, iters=1, seed=11)
+        x0 = np.array([0.0, 0.0, 0.5, 0.0], np.float32)
+        ctrl.computeControl(x0, 1)  # uploads x0 and the nominal sequence
+        if device_only:
+            ctrl.enqueueSolve(1, 3)
+            ctrl.synchronize()
+        else:
+            for _ in range(3):
+                ctrl.computeControl(x0, 1)
+        outs.append(ctrl.sample_costs())
+        ctrl.close()
+    assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))

@@ -463,7 +463,7 @@ def run_gpu(args, ws, rank, local):
         "iters_per_s": iters_per_s,
         "launch_config": {**dict(zip(["rollout_samples_per_cta", "rollout_time_chunk", "reduction_samples_per_cta"],
                                      ctrl.launchConfig())),
-                          "rollout_mode": ["fused", "split", "cooperative"][ctrl.rolloutMode()[0]]},
+                          "rollout_mode": ["fused", "split", "cooperative", "sampled"][ctrl.rolloutMode()[0]]},
         "kernel_ms": {n: float(v) for n, v in zip(names, kms)},
         "roofline": ({"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                       "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,

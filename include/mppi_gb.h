@@ -291,10 +291,12 @@ mppi_status mppi_autotune(mppi_handle* h, const char* cache_path);
 /* Rollout mode: 0 = one fused kernel per iteration (sampling, dynamics and costs, one thread per sample), 1 = split
  * dynamics / cost kernels (the dynamics chain alone, then all (k, t) costs in parallel, as the reference's
  * rolloutDynamicsKernel + rolloutCostKernel, mppi_common.cu:155-369), 2 = cooperative (four lanes per sample share
- * the sampling and cost work off the dynamics chain).  Modes 1 and 2 are for problems too small to fill the GPU
- * with one thread per sample; all give bit-identical costs.  available (may be NULL) receives the bitmask of modes
- * this handle supports (bit m = mode m); modes 1 and 2 need Gaussian sampling, T * C % 4 == 0 and an analytic
- * model, mode 1 also at most 256 MB of stepped states.  mppi_autotune times every available mode. */
+ * the sampling and cost work off the dynamics chain), 3 = the Gaussian sampler as its own kernel, then the rollout
+ * on the staged samples (the reference's order: generateSamples, then the rollout kernel).  Modes 1 and 2 are for
+ * problems too small to fill the GPU with one thread per sample; all give bit-identical samples and costs.
+ * available (may be NULL) receives the bitmask of modes this handle supports (bit m = mode m); modes 1 to 3 need
+ * Gaussian sampling, T * C % 4 == 0 and an analytic model, mode 1 also at most 256 MB of stepped states.
+ * mppi_autotune times every available mode. */
 mppi_status mppi_set_rollout_mode(mppi_handle* h, int mode);
 mppi_status mppi_get_rollout_mode(const mppi_handle* h, int* mode, int* available);
 /* The launch shape in use: samples per rollout CTA, time chunk, samples per reduction CTA. */

@@ -411,8 +411,9 @@ class BatchedMPPIController:
         A.call("mppi_autotune", self._h, None if cache_path is None else str(cache_path).encode())
 
     def setRolloutMode(self, mode):
-        """0 = fused rollout kernel, 1 = split dynamics / cost kernels, 2 = cooperative (four lanes per sample);
-        modes 1 and 2 are for small problems; costs are bit-identical."""
+        """0 = fused rollout kernel, 1 = split dynamics / cost kernels, 2 = cooperative (four lanes per sample),
+        3 = sampler kernel then the staged rollout; modes 1 and 2 are for small problems; samples and costs are
+        bit-identical."""
         A.call("mppi_set_rollout_mode", self._h, int(mode))
 
     def rolloutMode(self):

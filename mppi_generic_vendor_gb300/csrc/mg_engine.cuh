@@ -176,6 +176,7 @@ public:
       for (int k = 0; k < 5; ++k) sampler += class_begin_[k + 1] > class_begin_[k] ? 1 : 0;
     }
     const int judge = (Model::kMlp && !use_analytic_ && judge_total_ > 0) ? 3 : 0;
+    if (tail_finalize()) return cp_.num_iters;  // one fused rollout per iteration, nothing else
     if (fused()) sampler = 0;
     if (fused() && split_) sampler = 1;  // the cost kernel
     return (sampler + 2 + judge) * cp_.num_iters + 1;  // + the smoothing / constraint kernel
@@ -465,23 +466,28 @@ public:
   // stepped states of every sample (at most 256 MB).
   bool split_available() const
   {
-    if (!fused() || (Model::kMlp && !use_analytic_)) return false;
+    if (!fusable() || (Model::kMlp && !use_analytic_)) return false;
     return (double)total_u_ / C * S * sizeof(float) <= 256.0 * 1024 * 1024;
   }
   // The cooperative rollout (four lanes per sample) needs the fused Gaussian sampler and an analytic model.
-  bool coop_available() const { return fused() && !(Model::kMlp && !use_analytic_); }
+  bool coop_available() const { return fusable() && !(Model::kMlp && !use_analytic_); }
+  // Mode 3 runs the Gaussian sampler as its own kernel and the staged rollout on the written samples.
+  bool unfused_available() const { return fusable() && !(Model::kMlp && !use_analytic_); }
   int rollout_modes() const override
   {
-    return 1 | (split_available() ? 2 : 0) | (coop_available() ? 4 : 0);
+    return 1 | (split_available() ? 2 : 0) | (coop_available() ? 4 : 0) | (unfused_available() ? 8 : 0);
   }
   int rollout_mode() const override { return rollout_mode_; }
   mppi_status set_rollout_mode(int mode) override
   {
-    MG_CHECK(mode >= 0 && mode <= 2, "rollout mode must be 0 (fused), 1 (split dynamics / cost) or 2 (cooperative)");
+    MG_CHECK(mode >= 0 && mode <= 3, "rollout mode must be 0 (fused), 1 (split dynamics / cost), 2 (cooperative) or "
+             "3 (sampler kernel, then the staged rollout)");
     MG_CHECK(mode != 1 || split_available(),
              "the split rollout needs Gaussian sampling, T*C %% 4 == 0, an analytic model and <= 256 MB of states");
     MG_CHECK(mode != 2 || coop_available(), "the cooperative rollout needs Gaussian sampling, T*C %% 4 == 0 and an "
              "analytic model");
+    MG_CHECK(mode != 3 || unfused_available(), "rollout mode 3 needs Gaussian sampling, T*C %% 4 == 0 and an analytic "
+             "model");
     if (mode == 1 && !states_d_.p) MG_TRY(states_d_.alloc((size_t)total_u_ / C * S));
     rollout_mode_ = mode;
     split_ = mode == 1;
@@ -560,6 +566,7 @@ public:
   {
     MG_CHECK(Model::kMlp, "only the surrogate model has an analytic fallback");
     use_analytic_ = enable != 0;
+    MG_TRY(build_work_lists());  // the rollout kernel, and so its grid, changes
     invalidate_graphs();
     return MPPI_OK;
   }
@@ -580,6 +587,7 @@ public:
       if (st != MPPI_OK)
       {
         if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();  // the invalidated capture's error stays with this call
         return st;
       }
       MG_CUDA(ce);
@@ -727,7 +735,8 @@ private:
     //   [x0 | mean] is copied in, [mean | first | baseline,normaliser | status | stats] is copied out.
     {
       auto up16 = [](size_t b) { return (b + 15) / 16 * 16; };
-      const size_t o_x0 = 0, o_mean = o_x0 + sizeof(float) * I_ * S;
+      // the mean row starts on a 16-byte boundary: the fused samplers read it as float4 (odd S leaves a gap)
+      const size_t o_x0 = 0, o_mean = up16(o_x0 + sizeof(float) * I_ * S);
       const size_t o_first = o_mean + sizeof(float) * total_t;
       const size_t o_bn = o_first + sizeof(float) * I_ * C;
       const size_t o_status = o_bn + sizeof(float) * 2 * I_;
@@ -740,9 +749,11 @@ private:
       MG_CUDA(cudaMemset(io_d_.p, 0, o_end));
       MG_TRY(io_in_h_.alloc(io_in_bytes_));
       MG_TRY(io_out_h_.alloc(io_out_bytes_));
+      memset(io_in_h_.p, 0, io_in_bytes_);
       unsigned char* d = io_d_.p;
       x0_d_.view(reinterpret_cast<float*>(d + o_x0), (size_t)I_ * S);
       mean_d_.view(reinterpret_cast<float*>(d + o_mean), total_t);
+      MG_CHECK((reinterpret_cast<uintptr_t>(mean_d_.p) & 15) == 0, "internal: the mean row must be 16-byte aligned");
       first_d_.view(reinterpret_cast<float*>(d + o_first), (size_t)I_ * C);
       bn_d_.view(reinterpret_cast<float*>(d + o_bn), (size_t)2 * I_);
       status_d_ = reinterpret_cast<unsigned int*>(d + o_status);
@@ -769,6 +780,13 @@ private:
     MG_CUDA(cudaGetLastError());
     max_t_ = *std::max_element(T_.begin(), T_.end());  // sizes per-launch shared buffers (split cost kernel)
     if (Model::kMlp) ns_ = kMlpSamplesPerCta;
+    if constexpr ((4 % C) == 0)
+    {
+      MG_TRY(allow_fused_stage<32>());
+      MG_TRY(allow_fused_stage<64>());
+      MG_TRY(allow_fused_stage<128>());
+      MG_TRY(allow_fused_stage<256>());
+    }
     MG_TRY(build_work_lists());
     MG_TRY(build_colored_tables());
     MG_TRY(build_judge_lists());
@@ -940,6 +958,8 @@ private:
     MG_TRY(tile_sums_d_.alloc(2 * tile_poff.size()));
     MG_TRY(tile_min_d_.alloc(tile_poff.size()));
     MG_TRY(inst_tile0_d_.alloc(I_));
+    MG_TRY(inst_tiles_done_d_.alloc(I_));
+    MG_CUDA(cudaMemset(inst_tiles_done_d_.p, 0, sizeof(unsigned int) * I_));
     MG_CUDA(cudaMemcpy(tile_poff_d_.p, tile_poff.data(), sizeof(long long) * tile_poff.size(), cudaMemcpyHostToDevice));
     MG_CUDA(cudaMemcpy(inst_tile0_d_.p, inst_tile0.data(), sizeof(int) * I_, cudaMemcpyHostToDevice));
     num_chunks_ = (int)chunks.size();
@@ -974,6 +994,83 @@ private:
     return MPPI_OK;
   }
 
+  // Dynamic shared memory of the fused rollout: the tile's controls, staged for the tile reduction (0: the reduction
+  // reads them back from L2 instead, for horizons too long to stage).
+  template <int NS>
+  size_t fused_stage_bytes_max() const
+  {
+    const size_t b = sizeof(float) * (size_t)max_t_ * C * (NS + 1);
+    return b <= 200 * 1024 ? b : 0;
+  }
+  template <int NS>
+  size_t fused_stage_bytes() const
+  {
+    return tile_reduce_active() ? fused_stage_bytes_max<NS>() : 0;
+  }
+  // The fused rollout's dynamic shared memory: the staged controls, reused by the CTA that finalizes an instance
+  // for the per-tile rescale factors and for the smoothing buffer.
+  template <int NS>
+  size_t fused_dyn_bytes(bool stage) const
+  {
+    const int max_k = *std::max_element(K_.begin(), K_.end());
+    const size_t tiles = sizeof(float) * (size_t)((max_k + NS - 1) / NS);
+    const size_t smooth = sizeof(float) * (size_t)(max_t_ + 4) * C;
+    return std::max(stage ? fused_stage_bytes_max<NS>() : (size_t)0, std::max(tiles, smooth));
+  }
+  // Opts the fused rollout into its shared-memory size once, at creation (never during graph capture).
+  template <int NS>
+  mppi_status allow_fused_stage()
+  {
+    const size_t b = fused_dyn_bytes<NS>(true);
+    if (b > 48 * 1024)
+      MG_CUDA(cudaFuncSetAttribute(rollout_fused_kernel<Model, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)b));
+    return MPPI_OK;
+  }
+
+  // The fused rollout (mode 0) with tile reduction also combines each instance and, in the last iteration, smooths
+  // it: no finalize or smoothing kernel follows it.
+  bool tail_finalize() const { return tile_reduce_active() && fused() && !split_ && rollout_mode_ == 0; }
+
+  FinalizeArgs finalize_args() const
+  {
+    FinalizeArgs f{};
+    f.inst = inst_d_.p;
+    f.num_instances = I_;
+    f.inst_tile0 = inst_tile0_d_.p;
+    f.tile_samples = ns_;
+    f.tr.partials = tile_part_d_.p;
+    f.tr.poff = tile_poff_d_.p;
+    f.tr.sums = tile_sums_d_.p;
+    f.tr.tmin = tile_min_d_.p;
+    f.tr.lambda_inv = 1.0f / cp_.lambda;
+    f.baseline_bits = baseline_bits_d_.p;
+    f.inst_done = counters_d_.p + 2;
+    f.noise_counter = counters_d_.p + 3;
+    f.mean_out = mean_d_.p;
+    f.baseline_norm = bn_d_.p;
+    f.stats = stats_d_.p;
+    f.C = C;
+    f.inst_tiles_done = inst_tiles_done_d_.p;
+    f.first_out = first_d_.p;
+    f.finish = 0;
+    return f;
+  }
+
+  template <int NS>
+  void launch_fused(RolloutArgs<Model> a, const FusedNoise& f, int iter)
+  {
+    const size_t stage = fused_stage_bytes<NS>();
+    a.tr.u_stride = stage ? NS + 1 : 0;
+    if (tail_finalize())
+    {
+      a.tail = 1;
+      a.fin = finalize_args();
+      a.fin.finish = iter == cp_.num_iters - 1;
+    }
+    rollout_fused_kernel<Model, NS><<<rollout_grid_, NS, fused_dyn_bytes<NS>(stage != 0), stream_>>>(a, f);
+  }
+
   template <int NS>
   mppi_status occupancy_ns(int* per_sm)
   {
@@ -985,7 +1082,8 @@ private:
         else if (rollout_mode_ == 2)
           MG_CUDA(resident_ctas_per_sm(rollout_coop_kernel<Model, NS>, 4 * NS, 0, per_sm));
         else
-          MG_CUDA(resident_ctas_per_sm(rollout_fused_kernel<Model, NS>, NS, 0, per_sm));
+          MG_CUDA(resident_ctas_per_sm(rollout_fused_kernel<Model, NS>, NS,
+                                       fused_dyn_bytes<NS>(fused_stage_bytes<NS>() != 0), per_sm));
         return MPPI_OK;
       }
     if (use_bulk_)
@@ -1075,7 +1173,10 @@ private:
   }
   // Gaussian noise is generated inside the rollout (rollout_fused_kernel) when every row holds whole quads of steps;
   // the standalone sampler then runs only for mppi_generate_samples.
-  bool fused() const { return sp_.kind == MPPI_SAMPLER_GAUSSIAN && (4 % C) == 0 && use_bulk_; }
+  // Gaussian sampling can run inside the rollout kernels (every row holds whole control quads) ...
+  bool fusable() const { return sp_.kind == MPPI_SAMPLER_GAUSSIAN && (4 % C) == 0 && use_bulk_; }
+  // ... and does, unless rollout mode 3 asks for the separate sampler kernel.
+  bool fused() const { return fusable() && rollout_mode_ != 3; }
 
   FusedNoise fused_noise_args(int stride, int iter) const
   {
@@ -1198,10 +1299,10 @@ private:
         const FusedNoise f = fused_noise_args(stride, iter);
         switch (ns_)
         {
-          case 32: rollout_fused_kernel<Model, 32><<<rollout_grid_, 32, 0, stream_>>>(a, f); break;
-          case 64: rollout_fused_kernel<Model, 64><<<rollout_grid_, 64, 0, stream_>>>(a, f); break;
-          case 128: rollout_fused_kernel<Model, 128><<<rollout_grid_, 128, 0, stream_>>>(a, f); break;
-          default: rollout_fused_kernel<Model, 256><<<rollout_grid_, 256, 0, stream_>>>(a, f); break;
+          case 32: launch_fused<32>(a, f, iter); break;
+          case 64: launch_fused<64>(a, f, iter); break;
+          case 128: launch_fused<128>(a, f, iter); break;
+          default: launch_fused<256>(a, f, iter); break;
         }
         MG_CUDA(cudaGetLastError());
         return MPPI_OK;
@@ -1223,26 +1324,15 @@ private:
 
   mppi_status launch_weights()
   {
+    if (tail_finalize())  // the fused rollout combined the instances itself
+    {
+      weights_stale_ = true;
+      return MPPI_OK;
+    }
     if (tile_reduce_active())
     {
-      FinalizeArgs f;
-      f.inst = inst_d_.p;
-      f.num_instances = I_;
-      f.inst_tile0 = inst_tile0_d_.p;
-      f.tile_samples = ns_;
-      f.tr.partials = tile_part_d_.p;
-      f.tr.poff = tile_poff_d_.p;
-      f.tr.sums = tile_sums_d_.p;
-      f.tr.tmin = tile_min_d_.p;
-      f.tr.lambda_inv = 1.0f / cp_.lambda;
-      f.baseline_bits = baseline_bits_d_.p;
-      f.inst_done = counters_d_.p + 2;
-      f.noise_counter = counters_d_.p + 3;
-      f.mean_out = mean_d_.p;
-      f.baseline_norm = bn_d_.p;
-      f.stats = stats_d_.p;
-      f.C = C;
-      const size_t smem = sizeof(double) * (size_t)max_tiles_per_inst_;
+      const FinalizeArgs f = finalize_args();
+      const size_t smem = sizeof(float) * (size_t)max_tiles_per_inst_;
       if (smem > 48 * 1024)
         MG_CUDA(cudaFuncSetAttribute(tile_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       tile_finalize_kernel<<<I_, 256, smem, stream_>>>(f);
@@ -1287,7 +1377,9 @@ private:
       MG_TRY(launch_rollout(stride, it));
       MG_TRY(launch_weights());
     }
-    // smoothing + constraints of the new nominal sequences (the host post-processing of computeControl)
+    // smoothing + constraints of the new nominal sequences (the host post-processing of computeControl); the fused
+    // rollout's finalizing CTAs did it already in the last iteration
+    if (tail_finalize()) return MPPI_OK;
     finish_controls_kernel<C><<<I_, 256, sizeof(float) * (size_t)(max_t_ + 4) * C, stream_>>>(
         inst_d_.p, mean_d_.p, first_d_.p, make_sample_shared(sp_, cc_));
     MG_CUDA(cudaGetLastError());
@@ -1320,6 +1412,7 @@ private:
     if (st != MPPI_OK)
     {
       if (g) cudaGraphDestroy(g);
+      (void)cudaGetLastError();  // the invalidated capture's error stays with this call
       return st;
     }
     if (ce != cudaSuccess)
@@ -1452,6 +1545,7 @@ private:
   DevBuf<double> tile_sums_d_;
   DevBuf<unsigned int> tile_min_d_;
   DevBuf<int> inst_tile0_d_;
+  DevBuf<unsigned int> inst_tiles_done_d_;
   int max_tiles_per_inst_ = 1, max_k_ = 1;
   bool weights_stale_ = false;  // weights_d_ not yet derived from the last costs
   DevBuf<float> states_d_;     // split rollout: stepped states [instance][k][t][S]

@@ -175,6 +175,33 @@ struct TileReduce
   double* sums;             // per work tile: sum w, sum w^2 (tile baseline)
   unsigned int* tmin;       // per work tile: ordered-int minimum cost
   float lambda_inv;
+  int u_stride;             // > 0: the fused rollout stages its tile's controls in dynamic shared memory,
+                            // element-major with this row stride (an odd number >= samples per CTA)
+};
+
+// Combines the rollout tiles' partial reductions (TileReduce) into each instance's new mean, one CTA per instance:
+// tile l is rescaled by r_l = exp(-(b_l - b) / lambda) (difference in FP64), b the instance's minimum cost;
+// eta = sum_l r_l sum_w_l (FP64), mean[j] = sum_l r_l S_l[j] / eta (FP32, four interleaved partial sums over the
+// tiles).  Then the same bookkeeping as weights_update_kernel's last block.  Dynamic shared memory: one float per
+// tile of the largest instance.
+struct FinalizeArgs
+{
+  const InstDesc* inst;
+  int num_instances;
+  const int* inst_tile0;  // per instance: its first tile (an instance's tiles are consecutive)
+  int tile_samples;
+  TileReduce tr;
+  unsigned int* baseline_bits;
+  unsigned int* inst_done;
+  unsigned int* noise_counter;
+  float* mean_out;
+  float* baseline_norm;
+  double* stats;
+  int C;
+  // Rollout-tail form (the fused rollout combines each instance in the CTA that finishes its last tile):
+  unsigned int* inst_tiles_done;  // per instance: finished tiles of this launch (reset by the finalizing CTA)
+  float* first_out;               // finish != 0: also smooth and clamp the new mean (finish_instance)
+  int finish;
 };
 
 template <class Model>
@@ -198,13 +225,16 @@ struct RolloutArgs
   int max_t;  // longest horizon of the handle
   SampleShared sh;
   TileReduce tr;
+  int tail;          // the fused rollout finalizes each instance after its last tile (fin below)
+  FinalizeArgs fin;
 };
 
 // The tile epilogue (all threads of the CTA; the tile's costs are in a.costs and its minimum in tile_min).  s_w holds
 // one float per sample of the tile, s_red 64 doubles.
 template <int C, class Args>
 __device__ __forceinline__ void tile_reduce(const Args& a, const InstDesc& d, int tile, int first, int rows,
-                                            unsigned int tile_min, float* s_w, double* s_red)
+                                            unsigned int tile_min, float* s_w, double* s_red,
+                                            const float* s_u = nullptr)
 {
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
   const double bl = (double)ordered_to_float(tile_min);
@@ -237,16 +267,32 @@ __device__ __forceinline__ void tile_reduce(const Args& a, const InstDesc& d, in
   {
     float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
     int k = 0;
-    for (; k + 4 <= rows; k += 4)
+    if (s_u)
     {
-      const float v0 = __ldcg(u + (long long)k * TC + j), v1 = __ldcg(u + (long long)(k + 1) * TC + j);
-      const float v2 = __ldcg(u + (long long)(k + 2) * TC + j), v3 = __ldcg(u + (long long)(k + 3) * TC + j);
-      a0 = fmaf(s_w[k], v0, a0);
-      a1 = fmaf(s_w[k + 1], v1, a1);
-      a2 = fmaf(s_w[k + 2], v2, a2);
-      a3 = fmaf(s_w[k + 3], v3, a3);
+      // the tile's controls staged in shared memory by the rollout (same values, same order of operations)
+      const float* r = s_u + (size_t)j * a.tr.u_stride;
+      for (; k + 4 <= rows; k += 4)
+      {
+        a0 = fmaf(s_w[k], r[k], a0);
+        a1 = fmaf(s_w[k + 1], r[k + 1], a1);
+        a2 = fmaf(s_w[k + 2], r[k + 2], a2);
+        a3 = fmaf(s_w[k + 3], r[k + 3], a3);
+      }
+      for (; k < rows; ++k) a0 = fmaf(s_w[k], r[k], a0);
     }
-    for (; k < rows; ++k) a0 = fmaf(s_w[k], __ldcg(u + (long long)k * TC + j), a0);
+    else
+    {
+      for (; k + 4 <= rows; k += 4)
+      {
+        const float v0 = __ldcg(u + (long long)k * TC + j), v1 = __ldcg(u + (long long)(k + 1) * TC + j);
+        const float v2 = __ldcg(u + (long long)(k + 2) * TC + j), v3 = __ldcg(u + (long long)(k + 3) * TC + j);
+        a0 = fmaf(s_w[k], v0, a0);
+        a1 = fmaf(s_w[k + 1], v1, a1);
+        a2 = fmaf(s_w[k + 2], v2, a2);
+        a3 = fmaf(s_w[k + 3], v3, a3);
+      }
+      for (; k < rows; ++k) a0 = fmaf(s_w[k], __ldcg(u + (long long)k * TC + j), a0);
+    }
     out[j] = (a0 + a1) + (a2 + a3);
   }
   if (tid == 0)
@@ -264,15 +310,133 @@ __device__ __forceinline__ void tile_reduce(const Args& a, const InstDesc& d, in
   __syncthreads();
 }
 
+// Instance i's combine, by all threads of the calling CTA (any block size up to 1024).  s_r: one float per tile of
+// the instance; s_red: 64 doubles; s_eta: one float.  Leaves the instance's baseline reset for the next launch.
+__device__ __forceinline__ void finalize_instance(const FinalizeArgs& a, int i, float* s_r, double* s_red,
+                                                  float* s_eta)
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const InstDesc d = a.inst[i];
+  const int nt = (d.K + a.tile_samples - 1) / a.tile_samples;
+  const int t0 = a.inst_tile0[i];
+  const float b = ordered_to_float(a.baseline_bits[i]);
+  const double bd = (double)b;
+  const double linv = (double)a.tr.lambda_inv;
+  // The tiles' rescale factors: the baseline difference in FP64, the exponential in FP32 like the weights
+  // themselves; the normaliser (and the sum of squared weights) accumulate in FP64.  FP64 is slow on this part, so
+  // only the warps that hold tiles run it, and one thread combines the warps.
+  double eta = 0.0, w2 = 0.0;
+  for (int l = tid; l < nt; l += blockDim.x)
+  {
+    const float r = expf((float)(-((double)ordered_to_float(a.tr.tmin[t0 + l]) - bd) * linv));
+    s_r[l] = r;
+    const double rd = (double)r;
+    eta += rd * __ldcg(a.tr.sums + 2 * (t0 + l));
+    w2 += rd * rd * __ldcg(a.tr.sums + 2 * (t0 + l) + 1);
+  }
+  const int busy_warps = min((nt + 31) / 32, (int)(blockDim.x >> 5));  // at most 32
+  if (warp < busy_warps)
+  {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+    {
+      eta += __shfl_xor_sync(0xffffffffu, eta, off);
+      w2 += __shfl_xor_sync(0xffffffffu, w2, off);
+    }
+    if (lane == 0)
+    {
+      s_red[warp] = eta;
+      s_red[32 + warp] = w2;
+    }
+  }
+  __syncthreads();
+  if (tid == 0)
+  {
+    eta = 0.0;
+    w2 = 0.0;
+    for (int wi = 0; wi < busy_warps; ++wi)
+    {
+      eta += s_red[wi];
+      w2 += s_red[32 + wi];
+    }
+    *s_eta = (float)eta;
+  }
+  __syncthreads();
+  // mean[j] = sum_l r_l S_l[j] / eta in FP32 (the weighted control average itself is FP32, as in the reference)
+  const float eta_f = *s_eta;
+  const int TC = d.T * a.C;
+  const float* p0 = a.tr.partials + a.tr.poff[t0];
+  for (int j = tid; j < TC; j += blockDim.x)
+  {
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    int l = 0;
+    for (; l + 4 <= nt; l += 4)
+    {
+      a0 = fmaf(s_r[l], __ldcg(p0 + (long long)l * TC + j), a0);
+      a1 = fmaf(s_r[l + 1], __ldcg(p0 + (long long)(l + 1) * TC + j), a1);
+      a2 = fmaf(s_r[l + 2], __ldcg(p0 + (long long)(l + 2) * TC + j), a2);
+      a3 = fmaf(s_r[l + 3], __ldcg(p0 + (long long)(l + 3) * TC + j), a3);
+    }
+    for (; l < nt; ++l) a0 = fmaf(s_r[l], __ldcg(p0 + (long long)l * TC + j), a0);
+    a.mean_out[d.t_off + j] = ((a0 + a1) + (a2 + a3)) / eta_f;
+  }
+  if (tid == 0)
+  {
+    a.baseline_norm[2 * i] = b;
+    a.baseline_norm[2 * i + 1] = (float)eta;
+    a.stats[3 * i] = eta;
+    a.stats[3 * i + 1] = w2;
+    a.stats[3 * i + 2] = bd;
+    a.baseline_bits[i] = kOrderedPosInf;
+  }
+}
+
+// Instance i's smoothing and final clamp (finish_controls_kernel's body), by all threads of the calling CTA; buf
+// holds (T + 4) * C floats.
+template <int C>
+__device__ __forceinline__ void finish_instance(const InstDesc& d, int i, float* mean, float* first_out,
+                                                const SampleShared& sh, float* buf)
+{
+  const int tid = threadIdx.x;
+  const int T = d.T;
+  float* u = mean + d.t_off;
+  for (int e = tid; e < (T + 4) * C; e += blockDim.x)
+  {
+    const int tt = e / C, c = e - tt * C;
+    const int src = min(max(tt - 2, 0), T - 1);
+    buf[e] = u[src * C + c];
+  }
+  __syncthreads();
+  const float coef[5] = { -3.0f / 35.0f, 12.0f / 35.0f, 17.0f / 35.0f, 12.0f / 35.0f, -3.0f / 35.0f };
+  for (int e = tid; e < T * C; e += blockDim.x)
+  {
+    const int t = e / C, c = e - t * C;
+    float v;
+    if (t == 0)
+    {
+      v = buf[2 * C + c];
+      first_out[i * C + c] = v;
+    }
+    else
+    {
+      float acc = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 5; ++j) acc += coef[j] * buf[(t + j) * C + c];
+      v = acc;
+    }
+    u[e] = enforce_constraint(v, sh.lower[c], sh.upper[c], sh.deadband[c], sh.zero[c]);
+  }
+}
+
 // The running cost of step t (state cost on the stepped output y, control cost, likelihood-ratio term), in the
 // reference's arithmetic (mppi_common.cu:105-144).  kLik: the likelihood-ratio term is on (control_cost_coeff != 0);
 // a template flag, so a step has no branch.
-template <class Model, bool kLik, class Args>
+template <class Model, bool kLik, class Args, class Ar = ExactArith>
 __device__ __forceinline__ float step_cost(const Args& a, const InstDesc& d, const typename Model::CostParams& cp,
-                                           int k, const float* u, int t, const float* y)
+                                           int k, const float* u, int t, const float* y, Ar&& ar = Ar{})
 {
   constexpr int C = Model::CONTROL_DIM;
-  float c = Model::computeStateCost(cp, a.aux, y, t) + Model::computeControlCost(cp, u, t);
+  float c = Model::computeStateCost(cp, a.aux, y, t, ar) + Model::computeControlCost(cp, u, t);
   if constexpr (kLik)
   {
     // GaussianDistributionImpl::computeLikelihoodRatioCost (gaussian.cu:490-574)
@@ -283,7 +447,7 @@ __device__ __forceinline__ float step_cost(const Args& a, const InstDesc& d, con
     {
       const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + i];
       const float sd = a.sh.std_dev[i];
-      lc += a.sh.control_cost_coeff[i] * m * (m - 2.0f * u[i]) / (sd * sd);
+      lc += ar.div(a.sh.control_cost_coeff[i] * m * (m - 2.0f * u[i]), sd * sd);
     }
     c += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
   }
@@ -310,17 +474,17 @@ struct PendingCost
 };
 
 // One step t of sample k under control u: Euler step, then the running cost of the previous step.
-template <class Model, bool kLik, class Args>
+template <class Model, bool kLik, class Args, class Ar>
 __device__ __forceinline__ void rollout_step(const Args& a, const InstDesc& d,
                                              const typename Model::DynParams& dp,
                                              const typename Model::CostParams& cp, int k, const float* u, int t,
-                                             float* x, float& running, PendingCost<Model>& pc)
+                                             float* x, float& running, PendingCost<Model>& pc, Ar& ar)
 {
   constexpr int S = Model::STATE_DIM;
   constexpr int C = Model::CONTROL_DIM;
   float xn[S];
-  euler_step<Model>(dp, x, u, xn, a.dt);
-  const float c = step_cost<Model, kLik>(a, d, cp, k, pc.u, pc.t < 0 ? 0 : pc.t, pc.y);
+  euler_step<Model>(dp, x, u, xn, a.dt, ar);
+  const float c = step_cost<Model, kLik>(a, d, cp, k, pc.u, pc.t < 0 ? 0 : pc.t, pc.y, ar);
   running += pc.t >= 0 ? c : 0.0f;  // adding +0 leaves the (non-negative zero) initial sum unchanged
 #pragma unroll
   for (int i = 0; i < S; ++i) pc.y[i] = x[i] = xn[i];
@@ -338,6 +502,67 @@ __device__ __forceinline__ void rollout_flush(const Args& a, const InstDesc& d, 
   pc.t = -1;
 }
 
+// Runs `steps(ar)`, a few rollout steps written against an arithmetic policy, with FastArith; if any of their
+// divisions or angle wraps left the range where FastArith equals the IEEE result, restores the rollout state and runs
+// the same steps again with ExactArith, so the outcome is bit-identical to ExactArith either way.  `steps` changes
+// nothing but the state passed here, apart from stores that the replay repeats at the same addresses.  A run of four
+// steps gives the scheduler one branch-free basic block to interleave the dynamics chain with the pending costs.
+template <class Model, class Steps>
+__device__ __forceinline__ void speculate_steps(float* x, float& running, PendingCost<Model>& pc, const Steps& steps)
+{
+  constexpr int S = Model::STATE_DIM;
+  float xs[S];
+#pragma unroll
+  for (int i = 0; i < S; ++i) xs[i] = x[i];
+  const float rs = running;
+  const PendingCost<Model> ps = pc;
+  FastArith fa;
+  steps(fa);
+  if (!fa.ok)
+  {
+#pragma unroll
+    for (int i = 0; i < S; ++i) x[i] = xs[i];
+    running = rs;
+    pc = ps;
+    ExactArith ea;
+    steps(ea);
+  }
+}
+
+// The same for steps that change only the state x (dynamics without costs).
+template <int S, class Steps>
+__device__ __forceinline__ void speculate_dynamics(float* x, const Steps& steps)
+{
+  float xs[S];
+#pragma unroll
+  for (int i = 0; i < S; ++i) xs[i] = x[i];
+  FastArith fa;
+  steps(fa);
+  if (!fa.ok)
+  {
+#pragma unroll
+    for (int i = 0; i < S; ++i) x[i] = xs[i];
+    ExactArith ea;
+    steps(ea);
+  }
+}
+
+// The same for a pure function of the arguments (a step cost).
+template <class F>
+__device__ __forceinline__ float speculate_value(const F& f)
+{
+  FastArith fa;
+  const float v = f(fa);
+  if (fa.ok) return v;
+  ExactArith ea;
+  return f(ea);
+}
+
+// Control quads (float4 of the sample row) per speculated run: four steps.  Shorter runs pay the state save and the
+// branch more often; much longer unrolled runs measured slower (instruction-cache pressure of the unrolled replay).
+template <int C>
+constexpr int kSpecQuads = C < 4 ? C : 1;
+
 // Steps t0 .. t0+nt-1 of sample k from its staged control row.
 template <class Model, bool kLik>
 __device__ __forceinline__ void rollout_chunk(const RolloutArgs<Model>& a, const InstDesc& d,
@@ -346,18 +571,29 @@ __device__ __forceinline__ void rollout_chunk(const RolloutArgs<Model>& a, const
                                               int nt, float* x, float& running, PendingCost<Model>& pc)
 {
   constexpr int C = Model::CONTROL_DIM;
-  auto do_step = [&](const float* u, int t) { rollout_step<Model, kLik>(a, d, dp, cp, k, u, t, x, running, pc); };
   int tt = 0;
   if constexpr (4 % C == 0)
   {
-    // one 16-byte shared-memory read feeds 4/C steps
-    constexpr int G = 4 / C;
-    for (; tt + G <= nt; tt += G)
+    // 16-byte shared-memory reads; Q quads = four steps per speculated run
+    constexpr int Q = kSpecQuads<C>;
+    constexpr int NST = 4 * Q / C;
+    for (; tt + NST <= nt; tt += NST)
     {
-      const float4 v = *reinterpret_cast<const float4*>(urow + tt * C);
-      const float uu[4] = { v.x, v.y, v.z, v.w };
+      float uu[4 * Q];
 #pragma unroll
-      for (int g = 0; g < G; ++g) do_step(uu + g * C, t0 + tt + g);
+      for (int p = 0; p < Q; ++p)
+      {
+        const float4 v = *reinterpret_cast<const float4*>(urow + tt * C + 4 * p);
+        uu[4 * p] = v.x;
+        uu[4 * p + 1] = v.y;
+        uu[4 * p + 2] = v.z;
+        uu[4 * p + 3] = v.w;
+      }
+      speculate_steps<Model>(x, running, pc, [&](auto& ar) {
+#pragma unroll
+        for (int g = 0; g < NST; ++g)
+          rollout_step<Model, kLik>(a, d, dp, cp, k, uu + g * C, t0 + tt + g, x, running, pc, ar);
+      });
     }
   }
   for (; tt < nt; ++tt)
@@ -365,7 +601,9 @@ __device__ __forceinline__ void rollout_chunk(const RolloutArgs<Model>& a, const
     float u[C];
 #pragma unroll
     for (int c = 0; c < C; ++c) u[c] = urow[tt * C + c];
-    do_step(u, t0 + tt);
+    speculate_steps<Model>(x, running, pc, [&](auto& ar) {
+      rollout_step<Model, kLik>(a, d, dp, cp, k, u, t0 + tt, x, running, pc, ar);
+    });
   }
 }
 
@@ -498,17 +736,18 @@ struct FusedNoise
 // setGaussianControls + constraints for the quad of elements rem0 .. rem0+3 of sample k's row (rem = t*C + c), as
 // gaussian_sample_kernel computes them.
 template <int C>
-__device__ __forceinline__ float4 gaussian_quad(const SampleShared& sh, const float* mean_inst, float decay_pow,
-                                                int stride, int k, float pure_threshold, int rem0, float4 z)
+__device__ __forceinline__ float4 gaussian_quad(const SampleShared& sh, float4 mq, float decay_pow, int stride, int k,
+                                                float pure_threshold, int rem0, float4 z)
 {
   const float zz[4] = { z.x, z.y, z.z, z.w };
+  const float mm[4] = { mq.x, mq.y, mq.z, mq.w };
   float out[4];
 #pragma unroll
   for (int j = 0; j < 4; ++j)
   {
     const int rem = rem0 + j;
     const int t = rem / C, c = rem - t * C;
-    const float m = mean_inst[rem];
+    const float m = mm[j];
     const float sd = decay_pow * sh.std_dev[c];
     float u;
     if (k == 0 || t < stride)
@@ -520,6 +759,16 @@ __device__ __forceinline__ float4 gaussian_quad(const SampleShared& sh, const fl
     out[j] = enforce_constraint(u, sh.lower[c], sh.upper[c], sh.deadband[c], sh.zero[c]);
   }
   return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// The same with the quad's nominal controls read from the instance's mean row (rem0 a multiple of 4, the row
+// 16-byte aligned).
+template <int C>
+__device__ __forceinline__ float4 gaussian_quad(const SampleShared& sh, const float* mean_inst, float decay_pow,
+                                                int stride, int k, float pure_threshold, int rem0, float4 z)
+{
+  return gaussian_quad<C>(sh, __ldg(reinterpret_cast<const float4*>(mean_inst + rem0)), decay_pow, stride, k,
+                          pure_threshold, rem0, z);
 }
 
 // The four normals of Philox quad q of instance inst (or the injected ones).
@@ -542,6 +791,10 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
   __shared__ unsigned int s_min;
   __shared__ float s_tw[NS];  // tile_reduce: the tile's weights
   __shared__ double s_tred[64];
+  // a.tr.u_stride > 0: the tile's controls, element-major; after the tile reduction the finalizing CTA reuses it
+  extern __shared__ float s_u[];
+  __shared__ int s_last;
+  __shared__ float s_eta;
   const int tid = threadIdx.x;
   const uint32_t counter = f.noise_counter ? *f.noise_counter : 0u;
   for (;;)
@@ -572,19 +825,47 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
       const long long q0 = (long long)k * nq;
       const float pure_threshold = (1.0f - a.sh.pure_pct) * (float)d.K;
       float* dst = f.samples + d.u_off + 4 * q0;
+      const float4* mrow = reinterpret_cast<const float4*>(a.mean + d.t_off);
+      const int us = a.tr.partials ? a.tr.u_stride : 0;
       auto run = [&](auto lik) {
         float4 zn = fused_noise(f, d, w.x, counter, q0);
-        for (int qi = 0; qi < nq; ++qi)
-        {
-          const float4 z = zn;
-          if (qi + 1 < nq) zn = fused_noise(f, d, w.x, counter, q0 + qi + 1);
-          const float4 o = gaussian_quad<C>(a.sh, a.mean + d.t_off, f.decay_pow, f.stride, k, pure_threshold, 4 * qi, z);
-          *reinterpret_cast<float4*>(dst + 4 * qi) = o;
-          const float out[4] = { o.x, o.y, o.z, o.w };
+        float4 mn = __ldg(mrow);
+        // Q quads (Q * G steps) per speculated run
+        auto quads = [&](int qi, auto q_const) {
+          constexpr int Q = decltype(q_const)::value;
+          float out[4 * Q];
 #pragma unroll
-          for (int g = 0; g < G; ++g)
-            rollout_step<Model, decltype(lik)::value>(a, d, dp, cp, k, out + g * C, qi * G + g, x, running, pc);
-        }
+          for (int p = 0; p < Q; ++p)
+          {
+            const float4 z = zn, m = mn;
+            // the next quad's normals and nominal controls (the last quad reloads its own: no branch in the loop)
+            const int qn = min(qi + p + 1, nq - 1);
+            zn = fused_noise(f, d, w.x, counter, q0 + qn);
+            mn = __ldg(mrow + qn);
+            const float4 o = gaussian_quad<C>(a.sh, m, f.decay_pow, f.stride, k, pure_threshold, 4 * (qi + p), z);
+            *reinterpret_cast<float4*>(dst + 4 * (qi + p)) = o;
+            if (us)
+            {
+              float* col = s_u + (size_t)(4 * (qi + p)) * us + tid;
+              col[0] = o.x;
+              col[us] = o.y;
+              col[2 * us] = o.z;
+              col[3 * us] = o.w;
+            }
+            out[4 * p] = o.x;
+            out[4 * p + 1] = o.y;
+            out[4 * p + 2] = o.z;
+            out[4 * p + 3] = o.w;
+          }
+          speculate_steps<Model>(x, running, pc, [&](auto& ar) {
+#pragma unroll
+            for (int g = 0; g < G * Q; ++g)
+              rollout_step<Model, decltype(lik)::value>(a, d, dp, cp, k, out + g * C, qi * G + g, x, running, pc, ar);
+          });
+        };
+        int qi = 0;
+        for (; qi + kSpecQuads<C> <= nq; qi += kSpecQuads<C>) quads(qi, std::integral_constant<int, kSpecQuads<C>>{});
+        for (; qi < nq; ++qi) quads(qi, std::integral_constant<int, 1>{});
       };
       if (a.use_likelihood)
         run(std::true_type{});
@@ -608,7 +889,29 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
     if ((tid & 31) == 0) atomicMin(&s_min, o);
     __syncthreads();
     if (tid == 0) atomicMin(&a.baseline_bits[w.x], s_min);
-    if (a.tr.partials) tile_reduce<C>(a, d, tile, w.y, min(NS, d.K - w.y), s_min, s_tw, s_tred);
+    if (a.tr.partials)
+      tile_reduce<C>(a, d, tile, w.y, min(NS, d.K - w.y), s_min, s_tw, s_tred, a.tr.u_stride ? s_u : nullptr);
+    if (a.tail)
+    {
+      // the CTA that finishes an instance's last tile combines the instance (threadfence reduction)
+      __threadfence();  // this thread's partial sums before the tile counts as done
+      __syncthreads();
+      if (tid == 0)
+        s_last = atomicAdd(&a.fin.inst_tiles_done[w.x], 1u) == (unsigned int)((d.K + NS - 1) / NS - 1);
+      __syncthreads();
+      if (s_last)
+      {
+        __threadfence();
+        finalize_instance(a.fin, w.x, s_u, s_tred, &s_eta);
+        if (tid == 0) a.fin.inst_tiles_done[w.x] = 0u;
+        if (a.fin.finish)
+        {
+          __syncthreads();
+          finish_instance<C>(d, w.x, a.fin.mean_out, a.fin.first_out, a.sh, s_u);
+        }
+        __syncthreads();
+      }
+    }
   }
   if (tid == 0)
   {
@@ -618,6 +921,8 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
     {
       a.tile_counter[0] = 0u;
       a.tile_counter[1] = 0u;
+      // every CTA has read this launch's noise counter: advance it for the next launch
+      if (a.tail && a.fin.noise_counter) *a.fin.noise_counter += 1u;
       __threadfence();
     }
   }
@@ -681,24 +986,42 @@ __global__ void __launch_bounds__(4 * NS) rollout_coop_kernel(const __grid_const
         }
         const int nquads = min(L, nq - gi * L);
         float my_y[G][S];
+        // quads jj .. jj+Q-1 of the group (Q * G steps) as one speculated run
+        auto quads = [&](int jj, auto q_const) {
+          constexpr int Q = decltype(q_const)::value;
+          float v[4 * Q];
 #pragma unroll
-        for (int jj = 0; jj < L; ++jj)
+          for (int p = 0; p < Q; ++p)
+          {
+            v[4 * p] = __shfl_sync(0xffffffffu, o.x, jj + p, L);
+            v[4 * p + 1] = __shfl_sync(0xffffffffu, o.y, jj + p, L);
+            v[4 * p + 2] = __shfl_sync(0xffffffffu, o.z, jj + p, L);
+            v[4 * p + 3] = __shfl_sync(0xffffffffu, o.w, jj + p, L);
+          }
+          speculate_dynamics<S>(x, [&](auto& ar) {
+#pragma unroll
+            for (int g = 0; g < G * Q; ++g)
+            {
+              float xn[S];
+              euler_step<Model>(dp, x, v + g * C, xn, a.dt, ar);
+#pragma unroll
+              for (int i = 0; i < S; ++i)
+              {
+                if (jj + g / G == j) my_y[g % G][i] = xn[i];
+                x[i] = xn[i];
+              }
+            }
+          });
+        };
+        constexpr int QS = kSpecQuads<C>;
+#pragma unroll
+        for (int jj = 0; jj < L; jj += QS)
         {
           if (jj >= nquads) break;  // uniform over the CTA
-          const float v[4] = { __shfl_sync(0xffffffffu, o.x, jj, L), __shfl_sync(0xffffffffu, o.y, jj, L),
-                               __shfl_sync(0xffffffffu, o.z, jj, L), __shfl_sync(0xffffffffu, o.w, jj, L) };
-#pragma unroll
-          for (int g = 0; g < G; ++g)
-          {
-            float xn[S];
-            euler_step<Model>(dp, x, v + g * C, xn, a.dt);
-#pragma unroll
-            for (int i = 0; i < S; ++i)
-            {
-              if (jj == j) my_y[g][i] = xn[i];
-              x[i] = xn[i];
-            }
-          }
+          if (jj + QS <= nquads)
+            quads(jj, std::integral_constant<int, QS>{});
+          else
+            quads(jj, std::integral_constant<int, 1>{});
         }
         // the running costs of this lane's steps, then all of the group's in step order
         float c[G];
@@ -709,7 +1032,9 @@ __global__ void __launch_bounds__(4 * NS) rollout_coop_kernel(const __grid_const
         {
 #pragma unroll
           for (int g = 0; g < G; ++g)
-            c[g] = step_cost<Model, decltype(lik)::value>(a, d, cp, k, ov + g * C, q * G + g, my_y[g]);
+            c[g] = speculate_value([&](auto& ar) {
+              return step_cost<Model, decltype(lik)::value>(a, d, cp, k, ov + g * C, q * G + g, my_y[g], ar);
+            });
         }
 #pragma unroll
         for (int jj = 0; jj < L; ++jj)
@@ -791,23 +1116,37 @@ __global__ void __launch_bounds__(NS) rollout_dyn_kernel(const __grid_constant__
       float* dst = f.samples + d.u_off + 4 * q0;
       float* ys = states + d.u_off / C * S + (long long)k * d.T * S;
       float4 zn = fused_noise(f, d, w.x, counter, q0);
-      for (int qi = 0; qi < nq; ++qi)
-      {
-        const float4 z = zn;
-        if (qi + 1 < nq) zn = fused_noise(f, d, w.x, counter, q0 + qi + 1);
-        const float4 o = gaussian_quad<C>(a.sh, a.mean + d.t_off, f.decay_pow, f.stride, k, pure_threshold, 4 * qi, z);
-        *reinterpret_cast<float4*>(dst + 4 * qi) = o;
-        const float out[4] = { o.x, o.y, o.z, o.w };
+      auto quads = [&](int qi, auto q_const) {
+        constexpr int Q = decltype(q_const)::value;
+        float out[4 * Q];
 #pragma unroll
-        for (int g = 0; g < G; ++g)
+        for (int p = 0; p < Q; ++p)
         {
-          float xn[S];
-          euler_step<Model>(dp, x, out + g * C, xn, a.dt);
-          float* yt = ys + (long long)(qi * G + g) * S;
-#pragma unroll
-          for (int i = 0; i < S; ++i) yt[i] = x[i] = xn[i];
+          const float4 z = zn;
+          zn = fused_noise(f, d, w.x, counter, q0 + min(qi + p + 1, nq - 1));
+          const float4 o =
+              gaussian_quad<C>(a.sh, a.mean + d.t_off, f.decay_pow, f.stride, k, pure_threshold, 4 * (qi + p), z);
+          *reinterpret_cast<float4*>(dst + 4 * (qi + p)) = o;
+          out[4 * p] = o.x;
+          out[4 * p + 1] = o.y;
+          out[4 * p + 2] = o.z;
+          out[4 * p + 3] = o.w;
         }
-      }
+        speculate_dynamics<S>(x, [&](auto& ar) {
+#pragma unroll
+          for (int g = 0; g < G * Q; ++g)
+          {
+            float xn[S];
+            euler_step<Model>(dp, x, out + g * C, xn, a.dt, ar);
+            float* yt = ys + (long long)(qi * G + g) * S;
+#pragma unroll
+            for (int i = 0; i < S; ++i) yt[i] = x[i] = xn[i];
+          }
+        });
+      };
+      int qi = 0;
+      for (; qi + kSpecQuads<C> <= nq; qi += kSpecQuads<C>) quads(qi, std::integral_constant<int, kSpecQuads<C>>{});
+      for (; qi < nq; ++qi) quads(qi, std::integral_constant<int, 1>{});
     }
   }
   if (tid == 0)
@@ -863,8 +1202,8 @@ __global__ void __launch_bounds__(WARPS * 32) rollout_cost_kernel(const __grid_c
         for (int i = 0; i < S; ++i) y[i] = ys[(long long)t * S + i];
 #pragma unroll
         for (int i = 0; i < C; ++i) u[i] = us[t * C + i];
-        my[t] = a.use_likelihood ? step_cost<Model, true>(a, d, cp, k, u, t, y)
-                                 : step_cost<Model, false>(a, d, cp, k, u, t, y);
+        my[t] = a.use_likelihood ? speculate_value([&](auto& ar) { return step_cost<Model, true>(a, d, cp, k, u, t, y, ar); })
+                                 : speculate_value([&](auto& ar) { return step_cost<Model, false>(a, d, cp, k, u, t, y, ar); });
       }
       __syncwarp();
       if (lane == 0)
@@ -1285,81 +1624,14 @@ __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_consta
   }
 }
 
-// Combines the rollout tiles' partial reductions (TileReduce) into each instance's new mean, one CTA per instance:
-// tile l is rescaled by r_l = exp(-(b_l - b) / lambda) (FP64), b the instance's minimum cost; eta = sum_l r_l sum_w_l,
-// mean[j] = sum_l r_l S_l[j] / eta, summed in tile order.  Then the same bookkeeping as weights_update_kernel's
-// last block.  Dynamic shared memory: one double per tile of the largest instance.
-struct FinalizeArgs
-{
-  const InstDesc* inst;
-  int num_instances;
-  const int* inst_tile0;  // per instance: its first tile (an instance's tiles are consecutive)
-  int tile_samples;
-  TileReduce tr;
-  unsigned int* baseline_bits;
-  unsigned int* inst_done;
-  unsigned int* noise_counter;
-  float* mean_out;
-  float* baseline_norm;
-  double* stats;
-  int C;
-};
-
 static __global__ void __launch_bounds__(256) tile_finalize_kernel(const __grid_constant__ FinalizeArgs a)
 {
-  extern __shared__ double s_r[];
-  __shared__ double s_red[2][8];
-  const int i = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const InstDesc d = a.inst[i];
-  const int nt = (d.K + a.tile_samples - 1) / a.tile_samples;
-  const int t0 = a.inst_tile0[i];
-  const float b = ordered_to_float(a.baseline_bits[i]);
-  const double bd = (double)b;
-  const double linv = (double)a.tr.lambda_inv;
-  double eta = 0.0, w2 = 0.0;
-  for (int l = tid; l < nt; l += blockDim.x)
+  extern __shared__ float s_r[];  // per tile of the instance: exp(-(b_l - b) / lambda)
+  __shared__ double s_red[64];
+  __shared__ float s_eta;
+  finalize_instance(a, blockIdx.x, s_r, s_red, &s_eta);
+  if (threadIdx.x == 0)
   {
-    const double r = exp(-((double)ordered_to_float(a.tr.tmin[t0 + l]) - bd) * linv);
-    s_r[l] = r;
-    eta += r * __ldcg(a.tr.sums + 2 * (t0 + l));
-    w2 += r * r * __ldcg(a.tr.sums + 2 * (t0 + l) + 1);
-  }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1)
-  {
-    eta += __shfl_xor_sync(0xffffffffu, eta, off);
-    w2 += __shfl_xor_sync(0xffffffffu, w2, off);
-  }
-  if (lane == 0)
-  {
-    s_red[0][warp] = eta;
-    s_red[1][warp] = w2;
-  }
-  __syncthreads();
-  eta = 0.0;
-  w2 = 0.0;
-  for (int wi = 0; wi < (int)(blockDim.x >> 5); ++wi)
-  {
-    eta += s_red[0][wi];
-    w2 += s_red[1][wi];
-  }
-  const int TC = d.T * a.C;
-  const float* p0 = a.tr.partials + a.tr.poff[t0];
-  for (int j = tid; j < TC; j += blockDim.x)
-  {
-    double s = 0.0;
-#pragma unroll 8
-    for (int l = 0; l < nt; ++l) s += s_r[l] * (double)__ldcg(p0 + (long long)l * TC + j);
-    a.mean_out[d.t_off + j] = (float)(s / eta);
-  }
-  if (tid == 0)
-  {
-    a.baseline_norm[2 * i] = b;
-    a.baseline_norm[2 * i + 1] = (float)eta;
-    a.stats[3 * i] = eta;
-    a.stats[3 * i + 1] = w2;
-    a.stats[3 * i + 2] = bd;
-    a.baseline_bits[i] = kOrderedPosInf;
     __threadfence();
     const unsigned int fin = atomicAdd(a.inst_done, 1u);
     if (fin == (unsigned int)(a.num_instances - 1))
@@ -1393,36 +1665,7 @@ __global__ void __launch_bounds__(256) finish_controls_kernel(const InstDesc* in
                                                               const __grid_constant__ SampleShared sh)
 {
   extern __shared__ float buf[];
-  const int i = blockIdx.x, tid = threadIdx.x;
-  const InstDesc d = inst[i];
-  const int T = d.T;
-  float* u = mean + d.t_off;
-  for (int e = tid; e < (T + 4) * C; e += blockDim.x)
-  {
-    const int tt = e / C, c = e - tt * C;
-    const int src = min(max(tt - 2, 0), T - 1);
-    buf[e] = u[src * C + c];
-  }
-  __syncthreads();
-  const float coef[5] = { -3.0f / 35.0f, 12.0f / 35.0f, 17.0f / 35.0f, 12.0f / 35.0f, -3.0f / 35.0f };
-  for (int e = tid; e < T * C; e += blockDim.x)
-  {
-    const int t = e / C, c = e - t * C;
-    float v;
-    if (t == 0)
-    {
-      v = buf[2 * C + c];
-      first_out[i * C + c] = v;
-    }
-    else
-    {
-      float acc = 0.0f;
-#pragma unroll
-      for (int j = 0; j < 5; ++j) acc += coef[j] * buf[(t + j) * C + c];
-      v = acc;
-    }
-    u[e] = enforce_constraint(v, sh.lower[c], sh.upper[c], sh.deadband[c], sh.zero[c]);
-  }
+  finish_instance<C>(inst[blockIdx.x], blockIdx.x, mean, first_out, sh, buf);
 }
 
 // Per-system minimum of costs into ordered-int slots (the baseline pass of fullGPUcomputeWeights,

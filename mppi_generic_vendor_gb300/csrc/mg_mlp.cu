@@ -467,7 +467,9 @@ __global__ void __launch_bounds__(128) judge_rollout_kernel(const __grid_constan
     {
       const float2 uv = __ldg(reinterpret_cast<const float2*>(urow + t * C));
       const float u[2] = { uv.x, uv.y };
-      rollout_step<Model, decltype(lik)::value>(a.r, d, dp, cp, k, u, t, x, running, pc);
+      speculate_steps<Model>(x, running, pc, [&](auto& ar) {
+        rollout_step<Model, decltype(lik)::value>(a.r, d, dp, cp, k, u, t, x, running, pc, ar);
+      });
     }
     rollout_flush<Model, decltype(lik)::value>(a.r, d, cp, k, running, pc);
   };

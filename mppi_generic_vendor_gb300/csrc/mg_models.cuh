@@ -37,10 +37,11 @@ struct Texels
 
 // The four texels and the interpolation fractions of point (x, y); split from the blend so a rollout can issue the
 // loads well before it needs the value.
-MG_HD Texels costmap_gather(const CostmapView& m, float x, float y)
+template <class Ar = ExactArith>
+MG_HD Texels costmap_gather(const CostmapView& m, float x, float y, Ar&& ar = Ar{})
 {
-  float px = (x - m.origin_x) / m.resolution - 0.5f;
-  float py = (y - m.origin_y) / m.resolution - 0.5f;
+  float px = ar.div(x - m.origin_x, m.resolution) - 0.5f;
+  float py = ar.div(y - m.origin_y, m.resolution) - 0.5f;
   px = fminf(fmaxf(px, 0.0f), (float)(m.width - 1));
   py = fminf(fmaxf(py, 0.0f), (float)(m.height - 1));
   int x0 = (int)floorf(px);
@@ -73,7 +74,11 @@ MG_HD float costmap_blend(const Texels& t)
   return top * (1.0f - t.fy) + bot * t.fy;
 }
 
-MG_HD float costmap_bilinear(const CostmapView& m, float x, float y) { return costmap_blend(costmap_gather(m, x, y)); }
+template <class Ar = ExactArith>
+MG_HD float costmap_bilinear(const CostmapView& m, float x, float y, Ar&& ar = Ar{})
+{
+  return costmap_blend(costmap_gather(m, x, y, ar));
+}
 
 // Shared (per-launch) data that some costs need besides their parameter block.
 struct ModelAux
@@ -94,21 +99,23 @@ struct CartpoleModel
   using DynParams = mppi_cartpole_params;
   using CostParams = mppi_cartpole_cost_params;
 
-  static MG_HD void computeDynamics(const DynParams& p, const float* x, const float* u, float* xd)
+  template <class Ar = ExactArith>
+  static MG_HD void computeDynamics(const DynParams& p, const float* x, const float* u, float* xd, Ar&& ar = Ar{})
   {
-    const float th = normalize_angle(x[2]);
+    const float th = ar.wrap(x[2]);
     float s, c;
     sincos_f(th, &s, &c);
     const float td = x[3], f = u[0];
     const float mc = p.cart_mass, mp = p.pole_mass, lp = p.pole_length, g = p.gravity;
     xd[0] = x[1];
-    xd[1] = (f + mp * s * (lp * (td * td) + g * c)) / (mc + mp * (s * s));
+    xd[1] = ar.div(f + mp * s * (lp * (td * td) + g * c), mc + mp * (s * s));
     xd[2] = td;
-    xd[3] = (-f * c - mp * lp * (td * td) * c * s - (mc + mp) * g * s) / (lp * (mc + mp * (s * s)));
+    xd[3] = ar.div(-f * c - mp * lp * (td * td) * c * s - (mc + mp) * g * s, lp * (mc + mp * (s * s)));
   }
-  static MG_HD float computeStateCost(const CostParams& q, const ModelAux&, const float* y, int)
+  template <class Ar = ExactArith>
+  static MG_HD float computeStateCost(const CostParams& q, const ModelAux&, const float* y, int, Ar&& ar = Ar{})
   {
-    const float th = normalize_angle(y[2]);
+    const float th = ar.wrap(y[2]);
     float s, c;
     sincos_f(th, &s, &c);
     const float a = 1.0f + c;
@@ -116,9 +123,10 @@ struct CartpoleModel
            q.theta_dot_coeff * (y[3] * y[3]);
   }
   static MG_HD float computeControlCost(const CostParams&, const float*, int) { return 0.0f; }
-  static MG_HD float terminalCost(const CostParams& q, const ModelAux& aux, const float* y)
+  template <class Ar = ExactArith>
+  static MG_HD float terminalCost(const CostParams& q, const ModelAux& aux, const float* y, Ar&& ar = Ar{})
   {
-    return computeStateCost(q, aux, y, 0) * q.terminal_coeff;
+    return computeStateCost(q, aux, y, 0, ar) * q.terminal_coeff;
   }
 };
 
@@ -136,7 +144,8 @@ struct DoubleIntegratorModel
   using DynParams = mppi_double_integrator_params;
   using CostParams = mppi_di_obstacle_cost_params;
 
-  static MG_HD void computeDynamics(const DynParams&, const float* x, const float* u, float* xd)
+  template <class Ar = ExactArith>
+  static MG_HD void computeDynamics(const DynParams&, const float* x, const float* u, float* xd, Ar&& = Ar{})
   {
     xd[0] = x[2];
     xd[1] = x[3];
@@ -148,7 +157,8 @@ struct DoubleIntegratorModel
     const float d0 = y[0] - q.goal[0], d1 = y[1] - q.goal[1], d2 = y[2] - q.goal[2], d3 = y[3] - q.goal[3];
     return q.coeff[0] * (d0 * d0) + q.coeff[1] * (d1 * d1) + q.coeff[2] * (d2 * d2) + q.coeff[3] * (d3 * d3);
   }
-  static MG_HD float computeStateCost(const CostParams& q, const ModelAux&, const float* y, int)
+  template <class Ar = ExactArith>
+  static MG_HD float computeStateCost(const CostParams& q, const ModelAux&, const float* y, int, Ar&& = Ar{})
   {
     float cost = quad(q, y);
     bool inside = false;
@@ -165,7 +175,8 @@ struct DoubleIntegratorModel
     return cost;
   }
   static MG_HD float computeControlCost(const CostParams&, const float*, int) { return 0.0f; }
-  static MG_HD float terminalCost(const CostParams& q, const ModelAux&, const float* y)
+  template <class Ar = ExactArith>
+  static MG_HD float terminalCost(const CostParams& q, const ModelAux&, const float* y, Ar&& = Ar{})
   {
     return quad(q, y) * q.terminal_coeff;
   }
@@ -185,29 +196,33 @@ struct BicycleCostmapModel
   using DynParams = mppi_bicycle_params;
   using CostParams = mppi_costmap_cost_params;
 
-  static MG_HD void computeDynamics(const DynParams& p, const float* x, const float* u, float* xd)
+  template <class Ar = ExactArith>
+  static MG_HD void computeDynamics(const DynParams& p, const float* x, const float* u, float* xd, Ar&& ar = Ar{})
   {
     float sy, cy, sd, cd;
     sincos_f(x[2], &sy, &cy);
     sincos_f(u[1], &sd, &cd);
     xd[0] = x[3] * cy;
     xd[1] = x[3] * sy;
-    xd[2] = x[3] * (sd / cd) / p.wheelbase;
+    xd[2] = ar.div(x[3] * ar.div(sd, cd), p.wheelbase);
     xd[3] = u[0];
   }
-  static MG_HD float speedMapCost(const CostParams& q, const ModelAux& aux, const float* y)
+  template <class Ar = ExactArith>
+  static MG_HD float speedMapCost(const CostParams& q, const ModelAux& aux, const float* y, Ar&& ar = Ar{})
   {
     const float dv = y[3] - q.speed_target;
-    return q.map_coeff * costmap_bilinear(aux.map, y[0], y[1]) + q.speed_coeff * (dv * dv);
+    return q.map_coeff * costmap_bilinear(aux.map, y[0], y[1], ar) + q.speed_coeff * (dv * dv);
   }
-  static MG_HD float computeStateCost(const CostParams& q, const ModelAux& aux, const float* y, int)
+  template <class Ar = ExactArith>
+  static MG_HD float computeStateCost(const CostParams& q, const ModelAux& aux, const float* y, int, Ar&& ar = Ar{})
   {
-    return speedMapCost(q, aux, y);
+    return speedMapCost(q, aux, y, ar);
   }
   static MG_HD float computeControlCost(const CostParams& q, const float* u, int) { return q.steer_coeff * (u[1] * u[1]); }
-  static MG_HD float terminalCost(const CostParams& q, const ModelAux& aux, const float* y)
+  template <class Ar = ExactArith>
+  static MG_HD float terminalCost(const CostParams& q, const ModelAux& aux, const float* y, Ar&& ar = Ar{})
   {
-    return speedMapCost(q, aux, y) * q.terminal_coeff;
+    return speedMapCost(q, aux, y, ar) * q.terminal_coeff;
   }
 };
 
@@ -232,30 +247,32 @@ struct BicycleSlipModel
     xd[1] = x[3] * sy + x[4] * cy;
     xd[2] = x[5];
   }
-  static MG_HD void computeDynamics(const DynParams& p, const float* x, const float* u, float* xd)
+  template <class Ar = ExactArith>
+  static MG_HD void computeDynamics(const DynParams& p, const float* x, const float* u, float* xd, Ar&& ar = Ar{})
   {
     float sy, cy;
     sincos_f(x[2], &sy, &cy);
     const float vx = x[3], vy = x[4], r = x[5], d = x[6];
     const float vxs = fmaxf(vx, p.min_vx);
-    const float af = d - (vy + p.lf * r) / vxs;
-    const float ar = -(vy - p.lr * r) / vxs;
-    const float fyf = p.cornering_stiffness * af;
-    const float fyr = p.cornering_stiffness * ar;
+    const float alpha_f = d - ar.div(vy + p.lf * r, vxs);
+    const float alpha_r = ar.div(-(vy - p.lr * r), vxs);
+    const float fyf = p.cornering_stiffness * alpha_f;
+    const float fyr = p.cornering_stiffness * alpha_r;
     float sd, cd;
     sincos_f(d, &sd, &cd);
     const float fx = p.max_drive_force * u[0] - p.drag * vx;
     xd[0] = vx * cy - vy * sy;
     xd[1] = vx * sy + vy * cy;
     xd[2] = r;
-    xd[3] = (fx - fyf * sd) / p.mass + vy * r;
-    xd[4] = (fyr + fyf * cd) / p.mass - vx * r;
-    xd[5] = (p.lf * fyf * cd - p.lr * fyr) / p.yaw_inertia;
-    xd[6] = (u[1] * p.max_steer - d) / p.steer_time_constant;
+    xd[3] = ar.div(fx - fyf * sd, p.mass) + vy * r;
+    xd[4] = ar.div(fyr + fyf * cd, p.mass) - vx * r;
+    xd[5] = ar.div(p.lf * fyf * cd - p.lr * fyr, p.yaw_inertia);
+    xd[6] = ar.div(u[1] * p.max_steer - d, p.steer_time_constant);
   }
-  static MG_HD float speedMapCost(const CostParams& q, const ModelAux& aux, const float* y)
+  template <class Ar = ExactArith>
+  static MG_HD float speedMapCost(const CostParams& q, const ModelAux& aux, const float* y, Ar&& ar = Ar{})
   {
-    return stateCostFromTexels(q, costmap_gather(aux.map, y[0], y[1]), y);
+    return stateCostFromTexels(q, costmap_gather(aux.map, y[0], y[1], ar), y);
   }
   // The state cost from texels gathered earlier (costmap_gather at y[0], y[1]): the same arithmetic as speedMapCost.
   static MG_HD float stateCostFromTexels(const CostParams& q, const Texels& tx, const float* y)
@@ -263,14 +280,16 @@ struct BicycleSlipModel
     const float dv = y[3] - q.speed_target;
     return q.map_coeff * costmap_blend(tx) + q.speed_coeff * (dv * dv);
   }
-  static MG_HD float computeStateCost(const CostParams& q, const ModelAux& aux, const float* y, int)
+  template <class Ar = ExactArith>
+  static MG_HD float computeStateCost(const CostParams& q, const ModelAux& aux, const float* y, int, Ar&& ar = Ar{})
   {
-    return speedMapCost(q, aux, y);
+    return speedMapCost(q, aux, y, ar);
   }
   static MG_HD float computeControlCost(const CostParams& q, const float* u, int) { return q.steer_coeff * (u[1] * u[1]); }
-  static MG_HD float terminalCost(const CostParams& q, const ModelAux& aux, const float* y)
+  template <class Ar = ExactArith>
+  static MG_HD float terminalCost(const CostParams& q, const ModelAux& aux, const float* y, Ar&& ar = Ar{})
   {
-    return speedMapCost(q, aux, y) * q.terminal_coeff;
+    return speedMapCost(q, aux, y, ar) * q.terminal_coeff;
   }
 };
 
@@ -284,11 +303,12 @@ struct BicycleSlipMLPModel : BicycleSlipModel
 
 // Euler step shared by every model (Dynamics::step -> updateState, dynamics.cu:128-152): x' = x + xdot * dt as one
 // fused multiply-add (the form the reference's device code compiles to).
-template <class Model>
-MG_HD void euler_step(const typename Model::DynParams& p, const float* x, const float* u, float* x_next, float dt)
+template <class Model, class Ar = ExactArith>
+MG_HD void euler_step(const typename Model::DynParams& p, const float* x, const float* u, float* x_next, float dt,
+                      Ar&& ar = Ar{})
 {
   float xd[Model::STATE_DIM];
-  Model::computeDynamics(p, x, u, xd);
+  Model::computeDynamics(p, x, u, xd, ar);
 #pragma unroll
   for (int i = 0; i < Model::STATE_DIM; ++i) x_next[i] = fmaf(xd[i], dt, x[i]);
 }

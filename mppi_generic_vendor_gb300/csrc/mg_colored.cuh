@@ -43,7 +43,18 @@ struct ColoredShape
   static constexpr int THREADS = 32 * SPB * C;
 };
 
-// Horizon class of an instance: 0 = direct transform, 1..4 = register FFT with T = 32, 64, 128, 256.
+// CTA shape of the two-threads-per-row transform for T = 2H (32, 64, 128): threads, resident CTAs the register
+// budget is set for, samples per CTA.
+template <int C, int H>
+struct ColoredPairShape
+{
+  static constexpr int THREADS = 256;
+  static constexpr int MIN_CTAS = H >= 64 ? 1 : 2;  // H = 64 needs ~140 live floats per thread
+  static constexpr int SPB = THREADS / 2 / C;
+};
+
+// Horizon class of an instance: 0 = direct transform, 1..3 = two threads per row with T = 32, 64, 128, 4 = one warp
+// per row with T = 256.
 inline int colored_class(int T)
 {
   switch (T)
@@ -61,5 +72,18 @@ inline int colored_class(int T)
 template <int C>
 mppi_status launch_colored_sampler(const ColoredArgs& a, const int* class_begin, int max_t, int num_sms,
                                    cudaStream_t s);
+
+// Samples per work item of horizon class cls.
+template <int C>
+constexpr int colored_class_spb(int cls)
+{
+  return cls == 1   ? ColoredPairShape<C, 16>::SPB
+         : cls == 2 ? ColoredPairShape<C, 32>::SPB
+         : cls == 3 ? ColoredPairShape<C, 64>::SPB
+                    : ColoredShape<C>::SPB;
+}
+
+// Uploads the sampler's constant twiddle table (once per engine creation, outside any graph capture).
+mppi_status colored_init_constants();
 
 }  // namespace mg

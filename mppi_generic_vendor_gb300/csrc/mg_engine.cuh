@@ -803,6 +803,7 @@ private:
   mppi_status build_colored_tables()
   {
     if (sp_.kind != MPPI_SAMPLER_COLORED_NOISE) return MPPI_OK;
+    MG_TRY(colored_init_constants());
     std::vector<float> tab;
     std::map<int, std::pair<int, int4>> by_t;
     std::vector<int> tab_off(I_);
@@ -917,8 +918,8 @@ private:
       d.spec_off = spec;
       spec += (long long)K_[i] * C * (T_[i] + 1) * 2;
       d.x_off = i * S;
-      for (int k0 = 0; k0 < K_[i]; k0 += kColoredSamplesPerCta)
-        cwork_cls[colored_class(T_[i])].push_back(make_int2(i, k0));
+      const int cls = colored_class(T_[i]);
+      for (int k0 = 0; k0 < K_[i]; k0 += colored_class_spb<C>(cls)) cwork_cls[cls].push_back(make_int2(i, k0));
       d.num_chunks = (K_[i] + kc_ - 1) / kc_;
       chunk0[i] = (int)chunks.size();
       for (int c = 0; c < d.num_chunks; ++c)
@@ -1519,7 +1520,6 @@ private:
   DevBuf<int4> ctab_parts_d_;
   int num_cwork_ = 0, max_t_ = 1;
   int class_begin_[6] = { 0, 0, 0, 0, 0, 0 };
-  static constexpr int kColoredSamplesPerCta = ColoredShape<C>::SPB;
   DevBuf<int4> chunks_d_;
   DevBuf<long long> part_off_d_;
   DevBuf<int> chunk0_d_;

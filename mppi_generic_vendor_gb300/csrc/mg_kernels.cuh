@@ -518,7 +518,7 @@ __device__ __forceinline__ void speculate_steps(float* x, float& running, Pendin
   const PendingCost<Model> ps = pc;
   FastArith fa;
   steps(fa);
-  if (!fa.ok)
+  if (__builtin_expect(!fa.ok, 0))  // rare: keep the replay out of the hot path
   {
 #pragma unroll
     for (int i = 0; i < S; ++i) x[i] = xs[i];
@@ -538,7 +538,7 @@ __device__ __forceinline__ void speculate_dynamics(float* x, const Steps& steps)
   for (int i = 0; i < S; ++i) xs[i] = x[i];
   FastArith fa;
   steps(fa);
-  if (!fa.ok)
+  if (__builtin_expect(!fa.ok, 0))  // rare: keep the replay out of the hot path
   {
 #pragma unroll
     for (int i = 0; i < S; ++i) x[i] = xs[i];
@@ -553,7 +553,7 @@ __device__ __forceinline__ float speculate_value(const F& f)
 {
   FastArith fa;
   const float v = f(fa);
-  if (fa.ok) return v;
+  if (__builtin_expect(fa.ok, 1)) return v;
   ExactArith ea;
   return f(ea);
 }

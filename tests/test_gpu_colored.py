@@ -42,6 +42,27 @@ def test_colored_noise_matches_reference_script(golden, case):
     ctrl.close()
 
 
+@pytest.mark.parametrize("T,stride", [(32, 0), (32, 40), (64, 69), (64, 17), (128, 127), (128, 200), (50, 7)])
+def test_colored_noise_offsets_match_oracle(T, stride):
+    """Every offset branch of the transforms: x[stride] from the first or the second half of the length-2T sequence,
+    odd and even offsets, the two-threads-per-row kernel (T = 32, 64, 128) and the direct transform (T = 50); two
+    controls with different exponents, injected spectrum, against the oracle's FP64 transform."""
+    K, C = 300, 2
+    rng = np.random.default_rng(T + stride)
+    spec = rng.standard_normal(K * C * (T + 1) * 2).astype(np.float32)
+    sampler = ColoredNoiseDistribution(std_dev=(1.0, 1.0), exponents=(1.0, 0.5), offset_decay_rate=0.9,
+                                       pure_noise_trajectories_percentage=0.0)
+    ctrl = BatchedMPPIController(DoubleIntegratorDynamics(), [DoubleIntegratorObstacleCost()], sampler, [K], [T])
+    ctrl.injectNoise(spec)
+    ctrl.generateSamples(stride, 0)
+    got = ctrl.control_samples().reshape(K, T, C)
+    ref = oracle.colored_noise(spec, K, T, C, [1.0, 0.5], fmin=0.0, decay=0.9, offset_t=stride).reshape(K, T, C)
+    err = np.abs(got[1:, stride:] - ref[1:, stride:]).max() if stride < T else 0.0
+    assert err <= 2e-5 * max(1.0, np.abs(ref).max()), err
+    assert np.all(got[:, :min(stride, T)] == 0.0)  # the nominal (zero) sequence before the offset
+    ctrl.close()
+
+
 def test_colored_batched_compute_control_parity():
     rng = np.random.default_rng(31)
     Ks, Ts = [512, 1024, 256, 2048], [32, 64, 128, 50]

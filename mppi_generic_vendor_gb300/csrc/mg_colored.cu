@@ -1,15 +1,19 @@
-// mg_colored.cu — the colored-noise sampler kernel (see mg_colored.cuh for what it restates).
+// mg_colored.cu — the colored-noise sampler kernels (see mg_colored.cuh for what they restate).
 //
-// GB300 design: one warp per (sample, control) row and the whole transform in registers.  The length-2T real inverse
-// FFT is computed as a T-point complex inverse FFT of the even/odd-packed spectrum
+// GB300 design.  The length-2T real inverse FFT of a (sample, control) row is computed as a T-point complex inverse
+// FFT of the even/odd-packed spectrum
 //     Z[k] = (X[k] + conj X[T-k]) + i (X[k] - conj X[T-k]) e^{2 pi i k / 2T},   z = IFFT_T(Z),   z[m] = x[2m] + i x[2m+1]
-// For T = 32 R (R = 1, 2, 4, 8) every lane holds R complex values, element index lane + 32 r.  The decimation-in-
-// frequency stages whose butterfly distance is a multiple of 32 combine registers of the same lane; the five shorter
-// stages exchange values with __shfl_xor_sync.  The output comes out in bit-reversed order and is scattered once into
-// the CTA's output tile.  Per-stage twiddles come from a host-built table laid out [stage][register][lane], so every
-// twiddle read is a contiguous 256-byte warp access.  Horizons that are not 32 x a power of two use a direct
-// transform over a shared-memory copy of the spectrum.  The CTA owns whole samples, so the finished [samples][T][C]
-// tile is written with coalesced stores after the Gaussian rewrite and the control constraints.
+// of which only z[m < T/2] (x[t < T]) and x[offset] are needed.
+//  * T = 32, 64, 128 (colored_quad_kernel): four lanes per row, lane q owning the frequencies k = q (mod 4); each
+//    draws, scales and packs its quarter, runs a T/4-point transform in registers with constant-bank twiddles, and
+//    one exchange through shared memory and a radix-4 combine give the row's T outputs.  Most arithmetic is plain
+//    FMA on registers; per output about one shared-memory word moves.
+//  * T = 256 (colored_sample_kernel, R = 8): one warp per row, every lane holding R complex values (element index
+//    lane + 32 r); the decimation-in-frequency stages of butterfly distance >= 32 stay in a lane's registers, the
+//    five shorter ones exchange values with __shfl_xor_sync, twiddles from a host-built [stage][register][lane] table.
+//  * other T (R = 0): a direct transform over a shared-memory copy of the spectrum.
+// Every form scatters its noise into the CTA's output tile, and the finished [samples][T][C] tile is written with
+// coalesced stores after the Gaussian rewrite and the control constraints.
 #include "mg_colored.cuh"
 #include "mg_common.cuh"
 
@@ -27,9 +31,10 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 // compile-time constants in the unrolled transforms, so each twiddle is a constant-bank operand.
 __constant__ float2 c_w256[128];
 
-// a * e^{2 pi i idx / 256}, idx a compile-time constant; the trivial rotations cost nothing.
+// a * e^{2 pi i idx / 256}, idx a compile-time constant in [0, 256); the trivial rotations cost nothing.
 __device__ __forceinline__ float2 rot256(float2 a, int idx)
 {
+  if (idx >= 128) a = make_float2(-a.x, -a.y), idx -= 128;
   if (idx == 0) return a;
   if (idx == 64) return make_float2(-a.y, a.x);
   return cmul(a, c_w256[idx]);
@@ -70,18 +75,6 @@ __device__ __forceinline__ float4 row_normals(uint32_t lane_block, long long row
                                               uint32_t k0, uint32_t k1)
 {
   const u32x4 r = philox4x32_10(u32x4{ lane_block, (uint32_t)row, (uint32_t)inst | 0x80000000u, counter }, k0, k1);
-  float4 z;
-  box_muller_fast(r.x, r.y, &z.x, &z.y);
-  box_muller_fast(r.z, r.w, &z.z, &z.w);
-  return z;
-}
-
-// Four standard normals for block b of parity class p of a row (the two-threads-per-row transform's stream).
-__device__ __forceinline__ float4 pair_normals(int b, int p, long long row, int inst, uint32_t counter, uint32_t k0,
-                                               uint32_t k1)
-{
-  const u32x4 r = philox4x32_10(
-      u32x4{ (uint32_t)(2 * b + p) | 0x40000000u, (uint32_t)row, (uint32_t)inst | 0x80000000u, counter }, k0, k1);
   float4 z;
   box_muller_fast(r.x, r.y, &z.x, &z.y);
   box_muller_fast(r.z, r.w, &z.z, &z.w);
@@ -365,29 +358,35 @@ __device__ __forceinline__ void colored_store_tile(const ColoredArgs& a, const I
   }
 }
 
-// Two threads per (sample, control) row for T = 2H in {32, 64, 128}.  With M = T the length-2T real inverse FFT is
-// the M-point complex inverse FFT z = IFFT_M(Z) of the packed spectrum (as in row_transform_pow2), and
-// z[m] = E[m] + e^{2 pi i m / M} O[m], E and O the H-point inverse FFTs of Z at even and odd k.  Thread p (the lane's
-// parity) owns the frequencies k = p (mod 2): it draws and scales X[k] (thread 0 also the Nyquist X[M]), packs
-// Z[k] (the partner X[M - k] has the same parity), transforms its half in registers with compile-time twiddles, and
-// after one exchange of half its results with the partner lane forms z[m] for m in [p H/2, (p+1) H/2), i.e. the
-// outputs t in [p H, (p+1) H).  Register r of thread 0 holds k = 2r (r = H: the Nyquist bin); thread 1 holds
-// k = 2r + 1 for r < H/2 and k = 2r - 1 for r > H/2 (register H/2 unused), so that for both threads registers r and
-// H - r hold a conjugate pair (k, M - k).  No shuffles inside the transform, one 16-entry-per-output exchange.
-template <int C, int H>
-__global__ void __launch_bounds__(ColoredPairShape<C, H>::THREADS, ColoredPairShape<C, H>::MIN_CTAS)
-    colored_pair_kernel(const __grid_constant__ ColoredArgs a)
+// Four threads per (sample, control) row for T = M = 4 L (L = 8, 16, 32: T = 32, 64, 128): with k = 4j + q and
+// m = m1 + L m2 (m1 < L),
+//   z[m1 + L m2] = sum_q i^{q m2} W^{q m1} A_q[m1],   A_q = IFFT_L(Z[4j + q]),   W = e^{2 pi i / M}.
+// Thread q (lane & 3) owns the frequencies k = q (mod 4): it draws and scales X[k], packs Z[k] (the partner
+// X[M - k] is its own for q = 0, 2 and lane q ^ 2's for q = 1, 3, exchanged a register pair at a time), runs its
+// L-point transform in registers and writes A_q to shared memory; after a warp barrier it reads A_q'[m1] for
+// m1 = 4 i + q (i < L / 4) of the row's four threads and forms z[m1] and z[m1 + L], i.e. x[t] for the outputs
+// t = 8 i + 2 q (+1) (+2L).  Register r holds j = r (r < L) for q != 0; for q = 0 it holds j = r (r < L/2),
+// j = r + 1 (L/2 <= r < L; r = L - 1: the Nyquist bin) and j = L/2 (r = L), so that registers r and L - 1 - r hold
+// a conjugate pair (k, M - k) for every q.
+template <int C, int L>
+__global__ void __launch_bounds__(256, ColoredQuadShape<C, L>::MIN_CTAS)
+    colored_quad_kernel(const __grid_constant__ ColoredArgs a)
 {
-  constexpr int M = 2 * H;
-  constexpr int SPB = ColoredPairShape<C, H>::SPB;
-  constexpr int LOGH = ilog2(H);
+  constexpr int M = 4 * L;
+  constexpr int LOGL = ilog2(L);
   constexpr int TW = 256 / M;  // c_w256 index step of e^{2 pi i / M}; e^{2 pi i k / 2M} steps by TW / 2
-  extern __shared__ __align__(16) float tile[];
-  const int tid = threadIdx.x, lane = tid & 31, p = tid & 1;
-  const int row_local = tid >> 1;
+  constexpr int SPB = ColoredQuadShape<C, L>::SPB;
+  constexpr int SEG = L + 1;  // float2 per (row, q) segment of the exchange buffer (one float2 of padding)
+  extern __shared__ __align__(16) float smem[];
+  float* tile = smem;
+  float2* xbuf = reinterpret_cast<float2*>(smem + ColoredQuadShape<C, L>::XBUF_OFFSET);
+  const int tid = threadIdx.x, lane = tid & 31, q = tid & 3;
+  const int row_local = tid >> 2;
   const int s_local = row_local / C, c = row_local - s_local * C;
-  const unsigned pair = 3u << (lane & ~1);
+  const unsigned quad = 0xFu << (lane & ~3);
   const uint32_t counter = a.noise_counter ? *a.noise_counter : 0u;
+  float2* my_seg = xbuf + (row_local * 4 + q) * SEG;
+  const float2* row_seg = xbuf + row_local * 4 * SEG;
   for (int item = blockIdx.x; item < a.num_work; item += gridDim.x)
   {
     const int2 w = a.work[item];
@@ -395,20 +394,24 @@ __global__ void __launch_bounds__(ColoredPairShape<C, H>::THREADS, ColoredPairSh
     const float* tab = a.tables + a.tab_off[w.x];
     const int4 parts = a.tab_parts[w.x];
     const int nsamp = min(SPB, d.K - w.y);
-    if (s_local < nsamp)  // both threads of a row take the same branch
+    if (s_local < nsamp)  // the four threads of a row take the same branch
     {
       const long long row = (long long)(w.y + s_local) * C + c;
       const float* scale = tab + parts.x;
       const float* decay_t = tab + parts.z;
       const float inv_div = 1.0f / (tab[parts.y + c] * 2.0f * (float)M);
-      auto freq = [&](int r) { return p == 0 ? 2 * r : (r < H / 2 ? 2 * r + 1 : 2 * r - 1); };
-      float2 v[H + 1];
+      // frequency of register r (0 for thread q != 0's unused register L)
+      auto freq = [&](int r) {
+        if (q == 0) return 4 * (r < L / 2 ? r : (r < L ? r + 1 : L / 2));
+        return r < L ? 4 * r + q : 0;
+      };
+      float2 v[L + 1];
       // ---- 1. the scaled spectrum of this thread's frequencies
       if (a.injected_spec)
       {
         const float* src = a.injected_spec + d.spec_off + row * (long long)(M + 1) * 2;
 #pragma unroll
-        for (int r = 0; r <= H; ++r)
+        for (int r = 0; r <= L; ++r)
         {
           const int f = freq(r);
           v[r] = make_float2(src[2 * f], src[2 * f + 1]);
@@ -417,84 +420,105 @@ __global__ void __launch_bounds__(ColoredPairShape<C, H>::THREADS, ColoredPairSh
       else
       {
 #pragma unroll
-        for (int b = 0; b < H / 2; ++b)
+        for (int b = 0; b < L / 2; ++b)
         {
-          const float4 n = pair_normals(b, p, row, w.x, counter, a.seed_lo, a.seed_hi);
-          v[2 * b] = make_float2(n.x, n.y);
-          v[2 * b + 1] = make_float2(n.z, n.w);
+          const u32x4 u = philox4x32_10(u32x4{ (uint32_t)(4 * b + q) | 0x20000000u, (uint32_t)row,
+                                               (uint32_t)w.x | 0x80000000u, counter },
+                                        a.seed_lo, a.seed_hi);
+          box_muller_fast(u.x, u.y, &v[2 * b].x, &v[2 * b].y);
+          box_muller_fast(u.z, u.w, &v[2 * b + 1].x, &v[2 * b + 1].y);
         }
-        // thread 0: the Nyquist bin takes the DC bin's imaginary draw (which the DC bin discards); thread 1:
-        // register H takes register H/2's draw
-        v[H] = p == 0 ? make_float2(v[0].y, 0.0f) : v[H / 2];
+        // thread 0: j = L/2 takes the imaginary draws the DC and Nyquist bins discard
+        v[L] = make_float2(v[0].y, v[L - 1].y);
       }
 #pragma unroll
-      for (int r = 0; r <= H; ++r)
+      for (int r = 0; r <= L; ++r)
       {
         const float sc = __ldg(scale + freq(r) * C + c);
         v[r].x *= sc;
         v[r].y *= sc;
       }
-      v[0].y = p ? v[0].y : 0.0f;  // DC and Nyquist bins are real
-      v[H].y = p ? v[H].y : 0.0f;
-      // ---- 2. packing Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) e^{2 pi i k / 2M}, pairwise in place
+      v[0].y = q ? v[0].y : 0.0f;  // thread 0: the DC and Nyquist bins are real
+      v[L - 1].y = q ? v[L - 1].y : 0.0f;
+      // ---- 2. packing Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) e^{2 pi i k / 2M}
+      // e^{2 pi i k / 2M} = e^{2 pi i 4 r / 2M} * phi, phi per thread (and per register half for thread 0)
+      const float2 phi_lo = q ? c_w256[q * TW / 2] : make_float2(1.0f, 0.0f);
+      const float2 phi_hi = q ? c_w256[q * TW / 2] : c_w256[4 * TW / 2];
+      auto pack = [&](float2 x, float2 y, int r) {
+        const float2 e = make_float2(x.x + y.x, x.y - y.y);
+        const float2 o =
+            rot256(cmul(make_float2(x.x - y.x, x.y + y.y), r < L / 2 ? phi_lo : phi_hi), 4 * r * TW / 2);
+        return make_float2(e.x - o.y, e.y + o.x);
+      };
 #pragma unroll
-      for (int r = 0; r <= H / 2; ++r)
+      for (int r = 0; r < L / 2; ++r)
       {
-        const int rr = H - r;
+        const int rr = L - 1 - r;
         const float2 x = v[r], y = v[rr];
-        auto pack = [&](float2 xa, float2 xb, int r_of) {
-          const int k0 = 2 * r_of, k1 = r_of < H / 2 ? 2 * r_of + 1 : 2 * r_of - 1;
-          // e^{2 pi i k / 2M} for this thread's k (k = M, thread 0's Nyquist register, has no Z of its own)
-          const float2 w0 = k0 < M ? c_w256[k0 * TW / 2] : make_float2(1.0f, 0.0f);
-          const float2 w1 = c_w256[k1 * TW / 2];
-          const float2 tw = p ? w1 : w0;
-          const float2 e = make_float2(xa.x + xb.x, xa.y - xb.y);
-          const float2 o = cmul(make_float2(xa.x - xb.x, xa.y + xb.y), tw);
-          return make_float2(e.x - o.y, e.y + o.x);
-        };
-        v[r] = pack(x, y, r);
-        if (rr != r) v[rr] = pack(y, x, rr);
+        float2 rx, ry;  // lane q ^ 2's registers r and L - 1 - r
+        rx.x = __shfl_xor_sync(quad, x.x, 2);
+        rx.y = __shfl_xor_sync(quad, x.y, 2);
+        ry.x = __shfl_xor_sync(quad, y.x, 2);
+        ry.y = __shfl_xor_sync(quad, y.y, 2);
+        const bool remote = (q & 1) != 0;
+        v[r] = pack(x, remote ? ry : y, r);
+        v[rr] = pack(y, remote ? rx : x, rr);
       }
-      // ---- 3. this thread's half: u[j] = Z[2j + p]; thread 1's upper half sits one register up
+      {
+        // thread 0's self-conjugate bin k = M/2 (register L): e^{2 pi i (M/2) / 2M} = i
+        const float2 x = v[L];
+        const float2 e = make_float2(2.0f * x.x, 0.0f);
+        const float2 o = make_float2(-2.0f * x.y, 0.0f);  // (x - conj x) * i = (2i Im x) * i
+        v[L] = make_float2(e.x - o.y, e.y + o.x);
+      }
+      // ---- 3. natural order u[j] = Z[4j + q] for thread 0, then the L-point transform
 #pragma unroll
-      for (int j = H / 2; j < H; ++j) v[j] = p ? v[j + 1] : v[j];
-      ifft_dif_regs<H>(v);
-      // ---- 4. exchange and combine: thread 0 holds E, thread 1 holds O, at register bitrev(m)
+      for (int j = L - 1; j >= L / 2 + 1; --j) v[j] = q ? v[j] : v[j - 1];
+      v[L / 2] = q ? v[L / 2] : v[L];
+      ifft_dif_regs<L>(v);
+#pragma unroll
+      for (int m1 = 0; m1 < L; ++m1) my_seg[m1] = v[bitrev(m1, LOGL)];
+      __syncwarp(quad);
+      // ---- 4. z[m1 + L m2] = sum_q' i^{q' m2} W^{q' m1} A_q'[m1] for this thread's m1 = 4 i + q
+      const float2 w1 = c_w256[q * TW], w2 = c_w256[2 * q * TW], w3 = c_w256[3 * q * TW];  // W^{q' q}
       const int m_off = a.stride >> 1;
-      const bool wrap = m_off >= H;  // x[stride] in the second half of z: E[m'] - W^m' O[m']
-      const int mm = wrap ? m_off - H : m_off;
-      const int p_o = mm >= H / 2 ? 1 : 0, i_o = mm - p_o * (H / 2);
-      float2 zz[H / 2];
+      const int m1_o = m_off & (L - 1), m2_o = m_off >> LOGL, q_o = m1_o & 3, i_o = m1_o >> 2;
+      float2 z0[L / 4], z1[L / 4];
       float xo = 0.0f;
 #pragma unroll
-      for (int i = 0; i < H / 2; ++i)
+      for (int i = 0; i < L / 4; ++i)
       {
-        const float2 lo = v[bitrev(i, LOGH)], hi = v[bitrev(H / 2 + i, LOGH)];
-        const float2 send = p ? lo : hi;  // thread 0 sends E[H/2 + i], thread 1 sends O[i]
-        float2 recv;
-        recv.x = __shfl_xor_sync(pair, send.x, 1);
-        recv.y = __shfl_xor_sync(pair, send.y, 1);
-        // m = p H/2 + i: z[m] = E[m] + W^m O[m] with W^m = W^i (thread 0) or i W^i (thread 1)
-        const float2 e = p ? recv : lo;
-        float2 o = p ? hi : recv;
-        o = p ? make_float2(-o.y, o.x) : o;
-        const float2 t = rot256(o, i * TW);
-        zz[i] = make_float2(e.x + t.x, e.y + t.y);
+        const int m1 = 4 * i + q;
+        const float2 b0 = row_seg[m1];
+        const float2 b1 = rot256(cmul(row_seg[SEG + m1], w1), 4 * i * TW);
+        const float2 b2 = rot256(cmul(row_seg[2 * SEG + m1], w2), 8 * i * TW);
+        const float2 b3 = rot256(cmul(row_seg[3 * SEG + m1], w3), 12 * i * TW);
+        const float2 s02 = make_float2(b0.x + b2.x, b0.y + b2.y), d02 = make_float2(b0.x - b2.x, b0.y - b2.y);
+        const float2 s13 = make_float2(b1.x + b3.x, b1.y + b3.y), d13 = make_float2(b1.x - b3.x, b1.y - b3.y);
+        z0[i] = make_float2(s02.x + s13.x, s02.y + s13.y);  // m2 = 0
+        z1[i] = make_float2(d02.x - d13.y, d02.y + d13.x);  // m2 = 1: b0 + i b1 - b2 - i b3
         if (i == i_o)
         {
-          const float2 zo = wrap ? make_float2(e.x - t.x, e.y - t.y) : zz[i];
+          const float2 z2 = make_float2(s02.x - s13.x, s02.y - s13.y);  // m2 = 2
+          const float2 z3 = make_float2(d02.x + d13.y, d02.y - d13.x);  // m2 = 3
+          const float2 zo = m2_o == 0 ? z0[i] : m2_o == 1 ? z1[i] : m2_o == 2 ? z2 : z3;
           xo = (a.stride & 1) ? zo.y : zo.x;
         }
       }
-      const float x_off = __shfl_sync(pair, xo, (lane & ~1) | p_o);
+      const float x_off = __shfl_sync(quad, xo, (lane & ~3) | q_o);
       // ---- 5. eps[t] = (x[t] - x[offset] decay^t) / (sigma_c 2T) into the CTA's tile
       float* tile_row = tile + s_local * tile_row_floats(M, C) + c;
 #pragma unroll
-      for (int i = 0; i < H / 2; ++i)
+      for (int i = 0; i < L / 4; ++i)
       {
-        const int t0 = p * H + 2 * i;
-        tile_row[tile_pos(t0, 0, C)] = (zz[i].x - x_off * __ldg(decay_t + t0)) * inv_div;
-        tile_row[tile_pos(t0 + 1, 0, C)] = (zz[i].y - x_off * __ldg(decay_t + t0 + 1)) * inv_div;
+#pragma unroll
+        for (int m2 = 0; m2 < 2; ++m2)
+        {
+          const float2 z = m2 ? z1[i] : z0[i];
+          const int t0 = 8 * i + 2 * q + 2 * L * m2;
+          tile_row[tile_pos(t0, 0, C)] = (z.x - x_off * __ldg(decay_t + t0)) * inv_div;
+          tile_row[tile_pos(t0 + 1, 0, C)] = (z.y - x_off * __ldg(decay_t + t0 + 1)) * inv_div;
+        }
       }
     }
     __syncthreads();
@@ -502,7 +526,6 @@ __global__ void __launch_bounds__(ColoredPairShape<C, H>::THREADS, ColoredPairSh
     __syncthreads();
   }
 }
-
 
 // One launch per horizon class: R = T / 32 for T = 32, 64, 128, 256, R = 0 for the direct transform.  Specialising
 // the kernel on R keeps the register footprint of a single transform size.
@@ -561,17 +584,17 @@ static mppi_status launch_class(const ColoredArgs& a, int max_t, int num_sms, cu
   return MPPI_OK;
 }
 
-template <int C, int H>
-static mppi_status launch_pair(const ColoredArgs& a, int num_sms, cudaStream_t s)
+template <int C, int L>
+static mppi_status launch_quad(const ColoredArgs& a, int num_sms, cudaStream_t s)
 {
-  using Shape = ColoredPairShape<C, H>;
-  const size_t smem = sizeof(float) * (size_t)Shape::SPB * tile_row_floats(2 * H, C);
-  auto kern = colored_pair_kernel<C, H>;
+  using Shape = ColoredQuadShape<C, L>;
+  const size_t smem = Shape::SMEM_BYTES;
+  auto kern = colored_quad_kernel<C, L>;
   if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 1;
-  MG_CUDA(resident_ctas_per_sm(kern, Shape::THREADS, smem, &per_sm));
+  MG_CUDA(resident_ctas_per_sm(kern, 256, smem, &per_sm));
   const int grid = std::max(1, std::min(a.num_work, std::max(per_sm, 1) * num_sms));
-  kern<<<grid, Shape::THREADS, smem, s>>>(a);
+  kern<<<grid, 256, smem, s>>>(a);
   MG_CUDA(cudaGetLastError());
   return MPPI_OK;
 }
@@ -600,9 +623,9 @@ mppi_status launch_colored_sampler(const ColoredArgs& a, const int* class_begin,
     switch (k)
     {
       case 0: MG_TRY((launch_class<C, 0>(b, max_t, num_sms, s))); break;
-      case 1: MG_TRY((launch_pair<C, 16>(b, num_sms, s))); break;
-      case 2: MG_TRY((launch_pair<C, 32>(b, num_sms, s))); break;
-      case 3: MG_TRY((launch_pair<C, 64>(b, num_sms, s))); break;
+      case 1: MG_TRY((launch_quad<C, 8>(b, num_sms, s))); break;
+      case 2: MG_TRY((launch_quad<C, 16>(b, num_sms, s))); break;
+      case 3: MG_TRY((launch_quad<C, 32>(b, num_sms, s))); break;
       default: MG_TRY((launch_class<C, 8>(b, max_t, num_sms, s))); break;
     }
   }

@@ -43,17 +43,19 @@ struct ColoredShape
   static constexpr int THREADS = 32 * SPB * C;
 };
 
-// CTA shape of the two-threads-per-row transform for T = 2H (32, 64, 128): threads, resident CTAs the register
-// budget is set for, samples per CTA.
-template <int C, int H>
-struct ColoredPairShape
+// CTA shape of the four-threads-per-row transform for T = 4L (L = 8, 16, 32): 256 threads (64 rows), the output
+// tile, then the exchange buffer of the rows' L-point transforms ([64 rows][4][L + 1] float2, 16-byte aligned).
+template <int C, int L>
+struct ColoredQuadShape
 {
-  static constexpr int THREADS = 256;
-  static constexpr int MIN_CTAS = H >= 64 ? 1 : 2;  // H = 64 needs ~140 live floats per thread
-  static constexpr int SPB = THREADS / 2 / C;
+  static constexpr int SPB = 64 / C;
+  static constexpr int MIN_CTAS = L >= 32 ? 2 : 3;
+  static constexpr int TILE_FLOATS = SPB * (4 * L * C + L / 2 + 1);
+  static constexpr int XBUF_OFFSET = (TILE_FLOATS + 3) / 4 * 4;  // floats
+  static constexpr size_t SMEM_BYTES = sizeof(float) * (size_t)XBUF_OFFSET + 8u * 64 * 4 * (L + 1);
 };
 
-// Horizon class of an instance: 0 = direct transform, 1..3 = two threads per row with T = 32, 64, 128, 4 = one warp
+// Horizon class of an instance: 0 = direct transform, 1..3 = four threads per row with T = 32, 64, 128, 4 = one warp
 // per row with T = 256.
 inline int colored_class(int T)
 {
@@ -77,10 +79,7 @@ mppi_status launch_colored_sampler(const ColoredArgs& a, const int* class_begin,
 template <int C>
 constexpr int colored_class_spb(int cls)
 {
-  return cls == 1   ? ColoredPairShape<C, 16>::SPB
-         : cls == 2 ? ColoredPairShape<C, 32>::SPB
-         : cls == 3 ? ColoredPairShape<C, 64>::SPB
-                    : ColoredShape<C>::SPB;
+  return (cls >= 1 && cls <= 3) ? ColoredQuadShape<C, 8>::SPB : ColoredShape<C>::SPB;
 }
 
 // Uploads the sampler's constant twiddle table (once per engine creation, outside any graph capture).

@@ -575,7 +575,7 @@ static mppi_status launch_class(const ColoredArgs& a, int max_t, int num_sms, cu
   const int tmax = (R == 0) ? max_t : 32 * R;
   const size_t smem = xbuf + sizeof(float) * (size_t)SPB * tile_row_floats(tmax, C);
   auto kern = colored_sample_kernel<C, SPB, R>;
-  if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  MG_CUDA(raise_smem_cap(kern, smem));
   int per_sm = 1;
   MG_CUDA(resident_ctas_per_sm(kern, THREADS, smem, &per_sm));
   const int grid = std::max(1, std::min(a.num_work, std::max(per_sm, 1) * num_sms));
@@ -590,7 +590,7 @@ static mppi_status launch_quad(const ColoredArgs& a, int num_sms, cudaStream_t s
   using Shape = ColoredQuadShape<C, L>;
   const size_t smem = Shape::SMEM_BYTES;
   auto kern = colored_quad_kernel<C, L>;
-  if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  MG_CUDA(raise_smem_cap(kern, smem));
   int per_sm = 1;
   MG_CUDA(resident_ctas_per_sm(kern, 256, smem, &per_sm));
   const int grid = std::max(1, std::min(a.num_work, std::max(per_sm, 1) * num_sms));

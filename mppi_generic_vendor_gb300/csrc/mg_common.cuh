@@ -12,6 +12,8 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "../../include/mppi_gb.h"
@@ -138,6 +140,22 @@ struct PinnedBuf
 // The kernel's shared-memory carveout preference is set to the maximum first, so the L1 / shared split leaves room
 // for that many; the count is the smaller of the register, shared-memory, thread and CTA-slot limits (the larger of
 // that and the runtime's occupancy answer).
+// Raises a kernel's dynamic shared-memory cap to at least `bytes`, never lowering it: the cap belongs to the function
+// and is shared by every engine of the process, so an engine with a smaller need must not undercut a larger one's.
+template <class Kernel>
+inline cudaError_t raise_smem_cap(Kernel kern, size_t bytes)
+{
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  static std::mutex mu;
+  static std::map<const void*, size_t> caps;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = caps[reinterpret_cast<const void*>(kern)];
+  if (bytes <= cur) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
 template <class Kernel>
 inline cudaError_t resident_ctas_per_sm(Kernel kern, int threads, size_t dyn_smem, int* out)
 {

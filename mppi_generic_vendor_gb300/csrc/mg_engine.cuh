@@ -1022,10 +1022,7 @@ private:
   template <int NS>
   mppi_status allow_fused_stage()
   {
-    const size_t b = fused_dyn_bytes<NS>(true);
-    if (b > 48 * 1024)
-      MG_CUDA(cudaFuncSetAttribute(rollout_fused_kernel<Model, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)b));
+    MG_CUDA(raise_smem_cap(rollout_fused_kernel<Model, NS>, fused_dyn_bytes<NS>(true)));
     return MPPI_OK;
   }
 
@@ -1200,7 +1197,7 @@ private:
     // one row of max_t_ step costs per warp; every instance's T is at most max_t_ (set at create)
     MG_CHECK(max_t_ >= *std::max_element(T_.begin(), T_.end()), "internal: horizon bound not set");
     const size_t smem = sizeof(float) * WARPS * (size_t)max_t_;
-    if (smem > 48 * 1024) MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MG_CUDA(raise_smem_cap(kern, smem));
     int per_sm = 1;
     MG_CUDA(resident_ctas_per_sm(kern, WARPS * 32, smem, &per_sm));
     const int grid = std::max(1, std::min(num_tiles_, per_sm * num_sms_));
@@ -1334,8 +1331,7 @@ private:
     {
       const FinalizeArgs f = finalize_args();
       const size_t smem = sizeof(float) * (size_t)max_tiles_per_inst_;
-      if (smem > 48 * 1024)
-        MG_CUDA(cudaFuncSetAttribute(tile_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      MG_CUDA(raise_smem_cap(tile_finalize_kernel, smem));
       tile_finalize_kernel<<<I_, 256, smem, stream_>>>(f);
       MG_CUDA(cudaGetLastError());
       weights_stale_ = true;

@@ -348,3 +348,17 @@ def test_device_only_solves_match_compute_control():
         outs.append(ctrl.sample_costs())
         ctrl.close()
     assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
+
+
+def test_engines_with_different_horizons_coexist():
+    """The fused rollout's shared-memory cap is a property of the kernel, shared by every engine: creating a second
+    engine with a shorter horizon (smaller staging) must not break the first one's launches."""
+    x0 = np.array([0.0, 0.0, 0.5, 0.0], np.float32)
+    long_h, _, _ = cartpole_controller(1024, 200, seed=1)
+    long_h.computeControl(x0, 1)
+    short_h, _, _ = cartpole_controller(1024, 100, seed=2)
+    short_h.computeControl(x0, 1)
+    long_h.computeControl(x0, 1)  # 200 x 129 floats of staging per CTA, above the short engine's 100 x 129
+    assert np.all(np.isfinite(long_h.getControlSeq()))
+    long_h.close()
+    short_h.close()

@@ -1244,6 +1244,7 @@ __global__ void __launch_bounds__(WARPS * 32) rollout_cost_kernel(const __grid_c
 // the time loop, so warps run decoupled.  Every wait is bounded: a wait that gives up sets *status and the CTA stops.
 // Requires T*C % 4 == 0 for every instance (16-byte aligned rows and chunks).
 constexpr uint32_t kMaxBarrierSpins = 1u << 22;
+constexpr uint32_t kMaxSleepWaits = 1u << 20;  // tries of up to ~1 us each: about a second before giving up
 
 template <int NS, int C>
 struct BulkRolloutShape

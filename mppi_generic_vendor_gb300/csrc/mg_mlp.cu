@@ -16,13 +16,15 @@ namespace
 // TMEM columns: 31 KB and 64 columns for one tile (at most 7 CTAs per SM, 448 columns), 49 KB and 128 columns for two
 // (at most 4, 512 columns).  The columns of co-resident CTAs therefore fit the SM's 512, so an allocation never waits
 // for another CTA.
-constexpr size_t kMlpFwdSmem = MlpSmem::total(1) + 1024;
-constexpr size_t kMlpRolloutSmem = MlpSmem::total(kMlpTiles) + 1024;
+// The operand tiles are K-major without swizzling, which needs 16-byte alignment only: a 128-byte aligned dynamic
+// block keeps the footprint at 30 KB, so seven rollout CTAs fit an SM.
+constexpr size_t kMlpFwdSmem = MlpSmem::total(1);
+constexpr size_t kMlpRolloutSmem = MlpSmem::total(kMlpTiles);
 
 __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, const float* X, float* Y, int B,
                                                           unsigned int* status)
 {
-  extern __shared__ __align__(1024) unsigned char sm[];
+  extern __shared__ __align__(128) unsigned char sm[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t s_tmem;
   __shared__ int s_fail;
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
   constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM, NT = kTensor ? kMlpTiles : 1;
   static_assert(C == 2, "a fused noise quad holds two steps");
   const uint32_t counter = (kFused && f.noise_counter) ? *f.noise_counter : 0u;
-  extern __shared__ __align__(1024) unsigned char sm[];
+  extern __shared__ __align__(128) unsigned char sm[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t s_tmem;
   __shared__ int s_tile;
@@ -214,7 +216,12 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
 #pragma unroll
       for (int n = 0; n < NT; ++n)
       {
-        tx[n] = costmap_gather(a.aux.map, x[n][0], x[n][1]);  // the state step t - 1 produced
+        {
+          // the state step t - 1 produced; branch-free division, IEEE fallback when out of its exact range
+          FastArith fa;
+          tx[n] = costmap_gather(a.aux.map, x[n][0], x[n][1], fa);
+          if (__builtin_expect(!fa.ok, 0)) tx[n] = costmap_gather(a.aux.map, x[n][0], x[n][1]);
+        }
         if constexpr (kFused)
         {
           // Gaussian sampling fused in, quad by quad, exactly as gaussian_sample_kernel would have written it

@@ -144,7 +144,9 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
                 umma_smem_desc(sbase + MlpSmem::W1, 128, 256), kId64, 0u);
     umma_commit(mbar);
   }
-  if (!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins)) *fail = 1;
+  // one warp sleeps on the MMA's mbarrier, the others at the CTA barrier: waiting costs no issue slots
+  if (warp == 0 && !mbar_wait_sleep_bounded(mbar, phase, kMaxSleepWaits)) *fail = 1;
+  __syncthreads();
   phase ^= 1u;
   tc_fence_after_sync();
 
@@ -167,12 +169,14 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
         for (int h = 0; h < 2; ++h)
         {
           uint4 c;
-          const float* b = bias + 64 * layer + 16 * q + 8 * h;
+          // the biases as two 16-byte shared-memory reads (the same address across the warp: a broadcast)
+          const float4 b0 = *reinterpret_cast<const float4*>(bias + 64 * layer + 16 * q + 8 * h);
+          const float4 b1 = *reinterpret_cast<const float4*>(bias + 64 * layer + 16 * q + 8 * h + 4);
           const float* x = v + 8 * h;
-          c.x = pack_bf16(tanh_fast(fmaf(x[0], sc, b[0])), tanh_fast(fmaf(x[1], sc, b[1])));
-          c.y = pack_bf16(tanh_fast(fmaf(x[2], sc, b[2])), tanh_fast(fmaf(x[3], sc, b[3])));
-          c.z = pack_bf16(tanh_fast(fmaf(x[4], sc, b[4])), tanh_fast(fmaf(x[5], sc, b[5])));
-          c.w = pack_bf16(tanh_fast(fmaf(x[6], sc, b[6])), tanh_fast(fmaf(x[7], sc, b[7])));
+          c.x = pack_bf16(tanh_fast(fmaf(x[0], sc, b0.x)), tanh_fast(fmaf(x[1], sc, b0.y)));
+          c.y = pack_bf16(tanh_fast(fmaf(x[2], sc, b0.z)), tanh_fast(fmaf(x[3], sc, b0.w)));
+          c.z = pack_bf16(tanh_fast(fmaf(x[4], sc, b1.x)), tanh_fast(fmaf(x[5], sc, b1.y)));
+          c.w = pack_bf16(tanh_fast(fmaf(x[6], sc, b1.z)), tanh_fast(fmaf(x[7], sc, b1.w)));
           *reinterpret_cast<uint4*>(act + core_off(m, 16 * q + 8 * h, 64)) = c;
         }
       }
@@ -195,7 +199,8 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
                     umma_smem_desc(wb + 256 * k, 128, 1024), id, k > 0 ? 1u : 0u);
       umma_commit(mbar);
     }
-    if (!mbar_wait_bounded(mbar, phase, kMaxBarrierSpins)) *fail = 1;
+    if (warp == 0 && !mbar_wait_sleep_bounded(mbar, phase, kMaxSleepWaits)) *fail = 1;
+    __syncthreads();
     phase ^= 1u;
     tc_fence_after_sync();
   }

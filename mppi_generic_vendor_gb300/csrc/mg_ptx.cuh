@@ -50,6 +50,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
   return ok != 0;
 }
 
+// try_wait with a suspend-time hint: the thread sleeps until the phase completes or about `ns` nanoseconds pass,
+// instead of returning at once, so a waiting warp takes few issue slots from the SM's other CTAs.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t ns)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded sleeping wait: false if the phase did not complete within max_waits suspended tries.
+__device__ __forceinline__ bool mbar_wait_sleep_bounded(uint64_t* bar, uint32_t parity, uint32_t max_waits)
+{
+  for (uint32_t i = 0; i < max_waits; ++i)
+    if (mbar_try_wait_sleep(bar, parity, 1000u)) return true;
+  return false;
+}
+
 // Bounded wait: returns false if the phase did not complete within max_spins polls (the caller reports an error
 // instead of hanging).
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t max_spins)

@@ -128,21 +128,33 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_workload(name, seed, stream, instances=256, precision=None, params=None):
+def build_workload(name, seed, stream, instances=256, precision=None, params=None, describe_only=False):
+    """The named workload; describe_only: its shapes and description without creating a controller (no GPU work)."""
     from mppi_generic_vendor_gb300 import workloads as W
 
+    kw = dict(seed=seed, stream=stream, describe_only=describe_only)
     if name == "slip_mlp":
-        return W.slip_mlp(seed=seed, precision=precision or "bf16", params=params, stream=stream)
+        return W.slip_mlp(precision=precision or "bf16", params=params, **kw)
     if name == "batched_slip_mlp":
-        return W.batched_slip_mlp(seed=seed, num_instances=instances if instances != 256 else 128,
-                                  precision=precision or "fp8", params=params, stream=stream)
+        return W.batched_slip_mlp(num_instances=instances if instances != 256 else 128, precision=precision or "fp8",
+                                  params=params, **kw)
     if name == "batched_di":
-        return W.batched_di(seed=seed, num_instances=instances, colored=True, stream=stream)
+        return W.batched_di(num_instances=instances, colored=True, **kw)
     if name == "batched_di_gaussian":
-        return W.batched_di(seed=seed, num_instances=instances, colored=False, stream=stream)
+        return W.batched_di(num_instances=instances, colored=False, **kw)
     if name == "cartpole":
-        return W.cartpole(seed=seed, stream=stream)
-    return W.bicycle(seed=seed, stream=stream)
+        return W.cartpole(**kw)
+    return W.bicycle(**kw)
+
+
+def config_of(wl, ws):
+    """The `config` object of a bench line for workload wl at ws GPUs (shared by the GPU and the reference arm)."""
+    return {"workload": wl.name, **wl.description, "num_iters": wl.num_iters,
+            "sample_steps_per_iter": wl.sample_steps_per_iter,
+            "l2": ("inputs larger than L2 (samples buffer %.0f MB)" % (wl.control_floats * 4 / 1e6))
+            if wl.control_floats * 4 > 129e6 else
+            "working set %.1f MB fits in L2; device-resident value is L2-warm" % (wl.control_floats * 4 / 1e6),
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
 
 
 def algorithmic_bytes(wl, colored: bool):
@@ -454,12 +466,7 @@ def run_gpu(args, ws, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded; shapes of the benchmark configuration)",
-        "config": {"workload": wl.name, **wl.description, "num_iters": wl.num_iters,
-                   "sample_steps_per_iter": steps_per_iter,
-                   "l2": ("inputs larger than L2 (samples buffer %.0f MB)" % (wl.control_floats * 4 / 1e6))
-                   if wl.control_floats * 4 > 129e6 else
-                   "working set %.1f MB fits in L2; device-resident value is L2-warm" % (wl.control_floats * 4 / 1e6),
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "config": config_of(wl, ws),
         "iters_per_s": iters_per_s,
         "launch_config": {**dict(zip(["rollout_samples_per_cta", "rollout_time_chunk", "reduction_samples_per_cta"],
                                      ctrl.launchConfig())),
@@ -508,7 +515,8 @@ def run_reference(args, ws, rank):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; shapes of the benchmark configuration)",
-            "config": {"workload": args.workload}, "impl": "reference",
+            "config": config_of(build_workload(args.workload, 0, 0, instances=args.instances, precision=args.precision,
+                                               describe_only=True), ws), "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": "port",
                              "sample": last["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

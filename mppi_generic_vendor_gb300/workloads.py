@@ -30,7 +30,7 @@ from .controller import (BatchedMPPIController, BicycleDynamics, BicycleSlipMLPD
 @dataclass
 class Workload:
     name: str
-    controller: BatchedMPPIController
+    controller: BatchedMPPIController  # None for a description-only workload (describe_only=True)
     x0: np.ndarray            # float32 [num_instances * S]
     K: np.ndarray
     T: np.ndarray
@@ -48,13 +48,13 @@ class Workload:
         return int(np.sum(self.K.astype(np.int64) * self.T)) * self.control_dim
 
 
-def cartpole(seed: int = 0, K: int = 2048, T: int = 100, stream: int = 0) -> Workload:
+def cartpole(seed: int = 0, K: int = 2048, T: int = 100, stream: int = 0, describe_only: bool = False) -> Workload:
     rng = np.random.default_rng(seed)
     dyn = CartpoleDynamics(1.0, 1.0, 1.0, 9.81)
     dyn.setControlRanges([(-5.0, 5.0)])
     cost = CartpoleSwingupCost(10.0, 1.0, 100.0, 1.0, 0.0)
-    ctrl = VanillaMPPIController(dyn, cost, None, GaussianDistribution(std_dev=(1.0,)), 0.02, 1, 1.0, 0.0, T, K,
-                                 stream=stream, seed=seed)
+    ctrl = None if describe_only else VanillaMPPIController(dyn, cost, None, GaussianDistribution(std_dev=(1.0,)),
+                                                            0.02, 1, 1.0, 0.0, T, K, stream=stream, seed=seed)
     x0 = np.array([rng.uniform(-0.1, 0.1), rng.uniform(-0.1, 0.1), rng.uniform(-np.pi, np.pi),
                    rng.uniform(-0.1, 0.1)], dtype=np.float32)
     return Workload("cartpole_K2048_T100", ctrl, x0, np.array([K]), np.array([T]), 4, 1, 1,
@@ -75,7 +75,8 @@ def batched_di_params(seed: int = 0, num_instances: int = 256):
     return Ks.astype(np.int32), Ts.astype(np.int32), costs, np.concatenate(x0)
 
 
-def batched_di(seed: int = 0, num_instances: int = 256, colored: bool = True, stream: int = 0) -> Workload:
+def batched_di(seed: int = 0, num_instances: int = 256, colored: bool = True, stream: int = 0,
+               describe_only: bool = False) -> Workload:
     Ks, Ts, costs, x0 = batched_di_params(seed, num_instances)
     dyn = DoubleIntegratorDynamics()
     dyn.setControlRanges([(-1.0, 1.0), (-1.0, 1.0)])
@@ -83,8 +84,8 @@ def batched_di(seed: int = 0, num_instances: int = 256, colored: bool = True, st
         sampler = ColoredNoiseDistribution(std_dev=(0.5, 0.5), exponents=(1.0, 1.0))
     else:
         sampler = GaussianDistribution(std_dev=(0.5, 0.5))
-    ctrl = BatchedMPPIController(dyn, costs, sampler, Ks, Ts, dt=0.02, max_iter=1, lambda_=1.0, seed=seed,
-                                 stream=stream)
+    ctrl = None if describe_only else BatchedMPPIController(dyn, costs, sampler, Ks, Ts, dt=0.02, max_iter=1,
+                                                            lambda_=1.0, seed=seed, stream=stream)
     name = f"batched_di_{num_instances}x_colored" if colored else f"batched_di_{num_instances}x_gaussian"
     return Workload(name, ctrl, x0, Ks, Ts, 4, 2, 1,
                     dict(model="double_integrator", instances=num_instances, sum_K=int(Ks.sum()),
@@ -105,15 +106,15 @@ def gaussian_bump_costmap(seed: int = 0, size: int = 512, resolution: float = 0.
     return m.astype(np.float32)
 
 
-def bicycle(seed: int = 0, K: int = 16384, T: int = 100, stream: int = 0) -> Workload:
+def bicycle(seed: int = 0, K: int = 16384, T: int = 100, stream: int = 0, describe_only: bool = False) -> Workload:
     rng = np.random.default_rng(seed + 1)
     cmap = gaussian_bump_costmap(seed)
     dyn = BicycleDynamics(2.5)
     dyn.setControlRanges([(-3.0, 3.0), (-1.0, 1.0)])
     cost = CostmapCost(map_coeff=1.0, speed_target=8.0, speed_coeff=1.0, steer_coeff=0.0, terminal_coeff=0.0,
                        costmap=cmap, resolution=0.1, origin=(0.0, 0.0))
-    ctrl = VanillaMPPIController(dyn, cost, None, GaussianDistribution(std_dev=(1.0, 0.3)), 0.02, 1, 2.0, 0.0, T, K,
-                                 stream=stream, seed=seed)
+    ctrl = None if describe_only else VanillaMPPIController(dyn, cost, None, GaussianDistribution(std_dev=(1.0, 0.3)),
+                                                            0.02, 1, 2.0, 0.0, T, K, stream=stream, seed=seed)
     x0 = np.array([rng.uniform(5, 45), rng.uniform(5, 45), rng.uniform(-np.pi, np.pi), 4.0], dtype=np.float32)
     return Workload("bicycle_costmap_K16384_T100", ctrl, x0, np.array([K]), np.array([T]), 4, 2, 1,
                     dict(model="bicycle_costmap", K=K, T=T, map="512x512@0.1m, 32 bumps", lam=2.0, seed=seed))
@@ -144,32 +145,37 @@ def _slip_x0(rng):
 
 
 def slip_mlp(seed: int = 0, K: int = 16384, T: int = 100, precision: str = "bf16", params=None, judge: float = 0.01,
-             stream: int = 0) -> Workload:
+             stream: int = 0, describe_only: bool = False) -> Workload:
     rng = np.random.default_rng(seed + 3)
-    if params is None:
-        params = train_surrogate(stream=stream)
-    dyn = BicycleSlipMLPDynamics(params, precision=precision)
-    ctrl = VanillaMPPIController(dyn, _slip_cost(gaussian_bump_costmap(seed)), None,
-                                 GaussianDistribution(std_dev=(0.5, 0.5)), 0.02, 1, 2.0, 0.0, T, K, stream=stream,
-                                 seed=seed)
-    ctrl.setJudge(judge)
+    ctrl = None
+    if not describe_only:
+        if params is None:
+            params = train_surrogate(stream=stream)
+        dyn = BicycleSlipMLPDynamics(params, precision=precision)
+        ctrl = VanillaMPPIController(dyn, _slip_cost(gaussian_bump_costmap(seed)), None,
+                                     GaussianDistribution(std_dev=(0.5, 0.5)), 0.02, 1, 2.0, 0.0, T, K, stream=stream,
+                                     seed=seed)
+        ctrl.setJudge(judge)
     return Workload(f"slip_mlp_{precision}_K{K}_T{T}", ctrl, _slip_x0(rng), np.array([K]), np.array([T]), 7, 2, 1,
                     dict(model="bicycle_slip_mlp", precision=precision, K=K, T=T, judge=judge,
                          map="512x512@0.1m, 32 bumps", lam=2.0, seed=seed))
 
 
 def batched_slip_mlp(seed: int = 0, num_instances: int = 128, precision: str = "fp8", params=None,
-                     judge: float = 0.01, stream: int = 0) -> Workload:
+                     judge: float = 0.01, stream: int = 0, describe_only: bool = False) -> Workload:
     rng = np.random.default_rng(seed + 5)
-    if params is None:
-        params = train_surrogate(stream=stream)
     Ks = rng.integers(2048, 16385, size=num_instances).astype(np.int32)
     Ts = rng.choice([50, 100, 200], size=num_instances).astype(np.int32)
     x0 = np.concatenate([_slip_x0(rng) for _ in range(num_instances)])
-    dyn = BicycleSlipMLPDynamics(params, precision=precision)
-    ctrl = BatchedMPPIController(dyn, _slip_cost(gaussian_bump_costmap(seed)), GaussianDistribution(std_dev=(0.5, 0.5)),
-                                 Ks, Ts, dt=0.02, max_iter=1, lambda_=2.0, seed=seed, stream=stream)
-    ctrl.setJudge(judge)
+    ctrl = None
+    if not describe_only:
+        if params is None:
+            params = train_surrogate(stream=stream)
+        dyn = BicycleSlipMLPDynamics(params, precision=precision)
+        ctrl = BatchedMPPIController(dyn, _slip_cost(gaussian_bump_costmap(seed)),
+                                     GaussianDistribution(std_dev=(0.5, 0.5)), Ks, Ts, dt=0.02, max_iter=1,
+                                     lambda_=2.0, seed=seed, stream=stream)
+        ctrl.setJudge(judge)
     return Workload(f"batched_slip_mlp_{num_instances}x_{precision}", ctrl, x0, Ks, Ts, 7, 2, 1,
                     dict(model="bicycle_slip_mlp", precision=precision, instances=num_instances, sum_K=int(Ks.sum()),
                          T="U{50,100,200}", judge=judge, map="512x512@0.1m, 32 bumps (shared)", lam=2.0, seed=seed))

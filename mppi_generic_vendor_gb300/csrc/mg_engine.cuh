@@ -795,8 +795,9 @@ private:
   }
 
   // Per-T tables for the colored-noise sampler (mg_colored.cu).  Twiddles are computed in double and rounded to float:
-  //   T = 32 R (R = 1, 2, 4, 8): packing twiddles e^{2 pi i k / 2T} (k < T), then the register-stage twiddles
-  //     [log2 R][R][32] and the lane-stage twiddles [5][32] of the T-point decimation-in-frequency inverse FFT;
+  //   T = 32, 64, 128 (four lanes per row): none here, the kernel's twiddles are the constant table c_w256;
+  //   T = 256 (one warp per row, R = 8): packing twiddles e^{2 pi i k / 2T} (k < T), then the register-stage
+  //     twiddles [log2 R][R][32] and the lane-stage twiddles [5][32] of the decimation-in-frequency inverse FFT;
   //   other T: the full table e^{2 pi i j / 2T}, j < 2T, for the direct transform.
   // Frequency scales and sigma are computed in float in the order of the reference's host code
   // (colored_noise.cu:294-333); decay^t with powf as rearrangeNoise does (colored_noise.cu:44).
@@ -823,9 +824,9 @@ private:
       {
         const int N = 2 * T, F = T + 1;
         const int base = (int)tab.size();
-        const bool pow2 = (T == 32 || T == 64 || T == 128 || T == 256);
+        const bool quad = (T == 32 || T == 64 || T == 128);
         int lane_off = 0;
-        if (pow2)
+        if (T == 256)
         {
           const int R = T / 32;
           for (int k = 0; k < T; ++k) push_tw(k, N);
@@ -842,7 +843,7 @@ private:
               push_tw((lane & half) ? (lane % (2 * half)) - half : 0, 2.0 * half);
           }
         }
-        else
+        else if (!quad)
         {
           for (int j = 0; j < N; ++j) push_tw(j, N);
         }

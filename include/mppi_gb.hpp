@@ -1,0 +1,355 @@
+/*
+ * mppi_gb.hpp — C++ host mirror of MPPI-Generic's plugin / controller surface over the C ABI (mppi_gb.h).
+ *
+ * Header only, C++17, no CUDA or Eigen types: plugin objects carry the engine's POD parameter blocks, and
+ * VanillaMPPIController keeps the reference's template signature and method names
+ * (include/mppi/controllers/MPPI/mppi_controller.cuh:14-78, include/mppi/controllers/controller.cuh:70-1058), so a
+ * reference-side caller changes its includes and types, not its control loop.  Control trajectories are
+ * std::array<float, C * MAX_TIMESTEPS> in the memory order of the reference's column-major Eigen control_trajectory
+ * (C x MAX_T): element (c, t) at t * C + c.  Errors surface as mppi_gb::Error exceptions in the caller's code; the C
+ * ABI underneath never throws.
+ */
+#ifndef MPPI_GB_HPP
+#define MPPI_GB_HPP
+
+#include <array>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "mppi_gb.h"
+
+namespace mppi_gb
+{
+class Error : public std::runtime_error
+{
+public:
+  Error(mppi_status s, const std::string& what) : std::runtime_error(what), status(s) {}
+  mppi_status status;
+};
+
+inline void check(mppi_status s, const char* call)
+{
+  if (s != MPPI_OK) throw Error(s, std::string(call) + ": " + mppi_last_error_string());
+}
+
+// ---- Dynamics plugins (Dynamics<CLASS_T, PARAMS_T>, dynamics.cuh:68-72) ------------------------------------------
+
+// Shared part: the control ranges, deadband and zero control of Dynamics::enforceConstraints (dynamics.cu:107-126).
+template <int S, int C, int MODEL>
+struct DynamicsBase
+{
+  static constexpr int STATE_DIM = S, CONTROL_DIM = C, OUTPUT_DIM = S;
+  static constexpr int MODEL_ID = MODEL;
+  mppi_control_constraints constraints;
+  DynamicsBase() { mppi_default_constraints(&constraints); }
+  // Dynamics::setControlRanges (dynamics.cuh:145): (lower, upper) per control, as the reference's float2 x / y.
+  void setControlRanges(const std::array<std::pair<float, float>, C>& ranges)
+  {
+    for (int i = 0; i < C; ++i)
+    {
+      constraints.lower[i] = ranges[i].first;
+      constraints.upper[i] = ranges[i].second;
+    }
+  }
+  void setControlDeadbands(const std::array<float, C>& deadband)
+  {
+    for (int i = 0; i < C; ++i) constraints.deadband[i] = deadband[i];
+  }
+};
+
+// CartpoleDynamics (cartpole_dynamics.cuh): cart mass, pole mass, pole length; g = 9.81.
+struct CartpoleDynamics : DynamicsBase<4, 1, MPPI_MODEL_CARTPOLE>
+{
+  using DYN_PARAMS_T = mppi_cartpole_params;
+  DYN_PARAMS_T params;
+  explicit CartpoleDynamics(float cart_mass = 1.0f, float pole_mass = 1.0f, float pole_length = 1.0f)
+      : params{ cart_mass, pole_mass, pole_length, 9.81f }
+  {
+  }
+  DYN_PARAMS_T getParams() const { return params; }
+  void setParams(const DYN_PARAMS_T& p) { params = p; }
+};
+
+// DoubleIntegratorDynamics (di_dynamics.cu:46-53): no parameters.
+struct DoubleIntegratorDynamics : DynamicsBase<4, 2, MPPI_MODEL_DOUBLE_INTEGRATOR>
+{
+  using DYN_PARAMS_T = mppi_double_integrator_params;
+  DYN_PARAMS_T params{ 0.0f };
+};
+
+// Kinematic bicycle (x, y, yaw, v) with control (accel, steer); the engine's plugin (no reference model).
+struct BicycleDynamics : DynamicsBase<4, 2, MPPI_MODEL_BICYCLE_COSTMAP>
+{
+  using DYN_PARAMS_T = mppi_bicycle_params;
+  DYN_PARAMS_T params;
+  explicit BicycleDynamics(float wheelbase = 2.5f) : params{ wheelbase }
+  {
+    setControlRanges({ std::pair<float, float>{ -3.0f, 3.0f }, { -1.0f, 1.0f } });
+  }
+};
+
+// 7-state dynamic bicycle with linear tyres; the engine's plugin (no reference model).
+struct BicycleSlipDynamics : DynamicsBase<7, 2, MPPI_MODEL_BICYCLE_SLIP>
+{
+  using DYN_PARAMS_T = mppi_bicycle_slip_params;
+  BicycleSlipDynamics() { setControlRanges({ std::pair<float, float>{ -1.0f, 1.0f }, { -1.0f, 1.0f } }); }
+  // mass, yaw inertia, lf, lr, cornering stiffness, max drive force, drag, max steer, steer time constant, min vx
+  DYN_PARAMS_T params{ 1500.0f, 2500.0f, 1.2f, 1.3f, 8.0e4f, 4000.0f, 50.0f, 0.5f, 0.1f, 1.0f };
+};
+
+// The same vehicle with its derivatives from the learned 9 -> 64 -> 64 -> 5 surrogate (NeuralNetModel,
+// ar_nn_model.cu:127-156, evaluated on the tensor cores).  precision: 0 BF16, 1 FP8 E4M3 + per-layer scale, 2 FP32.
+struct BicycleSlipMLPDynamics : DynamicsBase<7, 2, MPPI_MODEL_BICYCLE_SLIP_MLP>
+{
+  using DYN_PARAMS_T = mppi_bicycle_slip_params;
+  // mass, yaw inertia, lf, lr, cornering stiffness, max drive force, drag, max steer, steer time constant, min vx
+  DYN_PARAMS_T params{ 1500.0f, 2500.0f, 1.2f, 1.3f, 8.0e4f, 4000.0f, 50.0f, 0.5f, 0.1f, 1.0f };
+  std::vector<float> network;  // MPPI_MLP_PARAMS floats (FNNHelper layout + scaling)
+  int precision = 0;
+  float judge_fraction = 0.01f;
+  BicycleSlipMLPDynamics() { setControlRanges({ std::pair<float, float>{ -1.0f, 1.0f }, { -1.0f, 1.0f } }); }
+  BicycleSlipMLPDynamics(std::vector<float> weights, int precision_ = 0) : BicycleSlipMLPDynamics()
+  {
+    network = std::move(weights);
+    precision = precision_;
+  }
+};
+
+// ---- Cost plugins (Cost<CLASS_T, PARAMS_T, DYN_PARAMS_T>, cost.cuh:34-35) ----------------------------------------
+
+struct CartpoleSwingupCost
+{
+  using COST_PARAMS_T = mppi_cartpole_cost_params;
+  COST_PARAMS_T params;
+  explicit CartpoleSwingupCost(float x_coeff = 10.0f, float x_dot_coeff = 1.0f, float cos_coeff = 100.0f,
+                               float theta_dot_coeff = 1.0f, float terminal_coeff = 0.0f)
+      : params{ x_coeff, x_dot_coeff, cos_coeff, theta_dot_coeff, terminal_coeff }
+  {
+  }
+};
+
+struct DoubleIntegratorObstacleCost
+{
+  using COST_PARAMS_T = mppi_di_obstacle_cost_params;
+  COST_PARAMS_T params{};
+  DoubleIntegratorObstacleCost()
+  {
+    for (int i = 0; i < 4; ++i) params.coeff[i] = i < 2 ? 1.0f : 0.1f;
+    params.obstacle_cost = 1000.0f;
+  }
+  void addObstacle(float x, float y, float radius)
+  {
+    if (params.num_obstacles >= MPPI_MAX_OBSTACLES) throw Error(MPPI_EINVAL, "too many obstacles");
+    params.obstacle_x[params.num_obstacles] = x;
+    params.obstacle_y[params.num_obstacles] = y;
+    params.obstacle_radius[params.num_obstacles] = radius;
+    ++params.num_obstacles;
+  }
+};
+
+// Costmap cost shared by the bicycle models; the map is row-major float[height][width].
+struct CostmapCost
+{
+  using COST_PARAMS_T = mppi_costmap_cost_params;
+  COST_PARAMS_T params{ 1.0f, 8.0f, 1.0f, 0.0f, 0.0f };
+  std::vector<float> map;
+  int width = 0, height = 0;
+  float resolution = 0.1f, origin_x = 0.0f, origin_y = 0.0f;
+};
+
+// ---- Sampling distributions (GaussianDistribution / ColoredNoiseDistribution) ------------------------------------
+
+struct GaussianDistribution
+{
+  mppi_sampling_params params;
+  GaussianDistribution()
+  {
+    mppi_default_sampling_params(&params);
+    params.kind = MPPI_SAMPLER_GAUSSIAN;
+  }
+  template <std::size_t C>
+  explicit GaussianDistribution(const std::array<float, C>& std_dev) : GaussianDistribution()
+  {
+    for (std::size_t i = 0; i < C; ++i) params.std_dev[i] = std_dev[i];
+  }
+};
+
+struct ColoredNoiseDistribution
+{
+  mppi_sampling_params params;
+  ColoredNoiseDistribution()
+  {
+    mppi_default_sampling_params(&params);
+    params.kind = MPPI_SAMPLER_COLORED_NOISE;
+  }
+  template <std::size_t C>
+  ColoredNoiseDistribution(const std::array<float, C>& std_dev, const std::array<float, C>& exponents)
+      : ColoredNoiseDistribution()
+  {
+    for (std::size_t i = 0; i < C; ++i)
+    {
+      params.std_dev[i] = std_dev[i];
+      params.exponents[i] = exponents[i];
+    }
+  }
+};
+
+// Feedback controllers are not on the engine's path (DDP is out of its scope); the slot of the reference's
+// constructor is kept and ignored.
+struct NoFeedback
+{
+};
+
+// ---- VanillaMPPIController<DYN_T, COST_T, FB_T, MAX_TIMESTEPS, NUM_ROLLOUTS, SAMPLING_T> ---------------------------
+
+template <class DYN_T, class COST_T, class FB_T, int MAX_TIMESTEPS, int NUM_ROLLOUTS,
+          class SAMPLING_T = GaussianDistribution>
+class VanillaMPPIController
+{
+public:
+  static constexpr int S = DYN_T::STATE_DIM, C = DYN_T::CONTROL_DIM;
+  using state_array = std::array<float, S>;
+  using control_array = std::array<float, C>;
+  using control_trajectory = std::array<float, C * MAX_TIMESTEPS>;  // (c, t) at t * C + c
+  using state_trajectory = std::array<float, S * MAX_TIMESTEPS>;
+  using sampled_cost_traj = std::vector<float>;
+
+  // mppi_controller.cu:16-29 (Controller::Controller, controller.cuh:111-153); stream is a cudaStream_t or null.
+  VanillaMPPIController(DYN_T* model, COST_T* cost, FB_T* /*fb_controller*/, SAMPLING_T* sampler, float dt,
+                        int max_iter, float lambda, float alpha, int num_timesteps = MAX_TIMESTEPS,
+                        const control_trajectory& init_control_traj = control_trajectory{}, void* stream = nullptr,
+                        uint64_t seed = 0)
+      : T_(num_timesteps)
+  {
+    if (num_timesteps < 1 || num_timesteps > MAX_TIMESTEPS) throw Error(MPPI_EINVAL, "num_timesteps out of range");
+    mppi_default_controller_params(&params_);
+    params_.dt = dt;
+    params_.num_iters = max_iter;
+    params_.lambda = lambda;
+    params_.alpha = alpha;
+    params_.num_timesteps = num_timesteps;
+    params_.seed = seed;
+    const int K = NUM_ROLLOUTS;
+    check(mppi_create(DYN_T::MODEL_ID, 1, &K, &T_, &params_, &sampler->params, &model->constraints, &model->params,
+                      sizeof(model->params), &cost->params, sizeof(cost->params), init_control_traj.data(), stream,
+                      &h_),
+          "mppi_create");
+    try
+    {
+      configure(*model, *cost);
+    }
+    catch (...)
+    {
+      mppi_destroy(h_);
+      throw;
+    }
+  }
+  ~VanillaMPPIController()
+  {
+    if (h_) mppi_destroy(h_);
+  }
+  VanillaMPPIController(const VanillaMPPIController&) = delete;
+  VanillaMPPIController& operator=(const VanillaMPPIController&) = delete;
+
+  // VanillaMPPIController::computeControl (mppi_controller.cu:152-237).
+  void computeControl(const state_array& state, int optimization_stride = 1)
+  {
+    check(mppi_compute_control(h_, state.data(), optimization_stride), "mppi_compute_control");
+  }
+  // Controller::getControlSeq (controller.cuh:425-428): the first num_timesteps columns are the solution.
+  control_trajectory getControlSeq() const
+  {
+    control_trajectory out{};
+    check(mppi_get_control_seq(h_, out.data()), "mppi_get_control_seq");
+    return out;
+  }
+  // Controller::setParams with init_control_traj_ (controller.cuh:857-876).
+  void setControlSeq(const control_trajectory& u) { check(mppi_set_control_seq(h_, u.data()), "mppi_set_control_seq"); }
+  // Controller::slideControlSequence (controller.cuh:370-376).
+  void slideControlSequence(int steps)
+  {
+    check(mppi_slide_control_sequence(h_, steps), "mppi_slide_control_sequence");
+  }
+  // Controller::getTargetStateSeq (controller.cuh:433).
+  state_trajectory getTargetStateSeq() const
+  {
+    state_trajectory out{};
+    check(mppi_get_state_seq(h_, out.data()), "mppi_get_state_seq");
+    return out;
+  }
+  // Controller::getBaselineCost / getNormalizerCost (controller.cuh:526-533).
+  float getBaselineCost() const { return baseline_normalizer(0); }
+  float getNormalizerCost() const { return baseline_normalizer(1); }
+  // Controller::getSampledCostSeq (controller.cuh:449-452): the weights the transform leaves in the cost array.
+  sampled_cost_traj getSampledCostSeq() const
+  {
+    sampled_cost_traj out(NUM_ROLLOUTS);
+    check(mppi_get_sample_weights(h_, out.data()), "mppi_get_sample_weights");
+    return out;
+  }
+  // Per-sample trajectory costs before the weight transform.
+  sampled_cost_traj getSampleCosts() const
+  {
+    sampled_cost_traj out(NUM_ROLLOUTS);
+    check(mppi_get_sample_costs(h_, out.data()), "mppi_get_sample_costs");
+    return out;
+  }
+  // Controller::setParams / getParams (controller.cuh:842-876) for lambda, alpha, dt, iterations and slide scale.
+  void setParams(const mppi_controller_params& p)
+  {
+    check(mppi_set_controller_params(h_, &p), "mppi_set_controller_params");
+    params_ = p;
+  }
+  mppi_controller_params getParams() const { return params_; }
+  // Controller::setSamplingParams (controller.cuh:852).
+  void setSamplingParams(const SAMPLING_T& sampler)
+  {
+    check(mppi_set_sampling_params(h_, &sampler.params), "mppi_set_sampling_params");
+  }
+  // Dynamics / Cost setParams after a change on the plugin objects.
+  void updateModel(const DYN_T& model)
+  {
+    check(mppi_set_dynamics_params(h_, &model.params, sizeof(model.params)), "mppi_set_dynamics_params");
+  }
+  void updateCost(const COST_T& cost)
+  {
+    check(mppi_set_cost_params(h_, &cost.params, sizeof(cost.params)), "mppi_set_cost_params");
+  }
+  int getNumTimesteps() const { return T_; }
+  mppi_handle* handle() const { return h_; }
+
+private:
+  float baseline_normalizer(int which) const
+  {
+    float bn[2];
+    check(mppi_get_baseline_normalizer(h_, bn, nullptr), "mppi_get_baseline_normalizer");
+    return bn[which];
+  }
+  template <class D, class Co>
+  void configure(const D& model, const Co& cost)
+  {
+    if constexpr (std::is_same<Co, CostmapCost>::value)
+      if (!cost.map.empty())
+        check(mppi_set_costmap(h_, cost.map.data(), cost.width, cost.height, cost.resolution, cost.origin_x,
+                               cost.origin_y),
+              "mppi_set_costmap");
+    if constexpr (std::is_same<D, BicycleSlipMLPDynamics>::value)
+    {
+      if (!model.network.empty())
+        check(mppi_set_mlp(h_, model.network.data(), model.network.size(), model.precision), "mppi_set_mlp");
+      check(mppi_set_judge(h_, model.judge_fraction), "mppi_set_judge");
+    }
+  }
+
+  mppi_handle* h_ = nullptr;
+  int T_ = MAX_TIMESTEPS;
+  mppi_controller_params params_{};
+};
+
+}  // namespace mppi_gb
+
+#endif  // MPPI_GB_HPP

@@ -92,3 +92,17 @@ def test_kernel_entries_reject_null_pointers_without_gpu():
     assert lib.mppi_kernel_weight_transform(None, None, 1.0, 16, 1, None) == 1
     assert lib.mppi_kernel_weighted_reduction(None, None, None, None, 0, 4, 4, 1, None) == 1
     assert lib.mppi_kernel_philox_normal(None, 4, 0, 0, None) == 1
+
+
+def test_cpp_mirror_header_compiles():
+    """include/mppi_gb.hpp (the C++ host mirror) compiles warning-free against include/mppi_gb.h (no GPU needed)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no C++ compiler")
+    root = Path(__file__).resolve().parents[1]
+    subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
+                    str(root / "tests" / "cpp" / "cartpole_mirror.cpp"), "-I", str(root / "include")], check=True)

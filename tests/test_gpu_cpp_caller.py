@@ -1,5 +1,6 @@
-"""The C ABI from a C++ caller: compiles tests/cpp/cartpole_receding_horizon.cpp against include/mppi_gb.h and
-libmppi_gb.so and runs the reference example's receding-horizon loop (examples/cartpole_example.cu:62-85)."""
+"""The C ABI from C++ callers: compiles tests/cpp/cartpole_receding_horizon.cpp (plain C ABI) and
+tests/cpp/cartpole_mirror.cpp (the C++ host mirror include/mppi_gb.hpp, with the reference's class and method names)
+against libmppi_gb.so and runs the reference example's receding-horizon loop (examples/cartpole_example.cu:62-85)."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -20,5 +21,18 @@ def test_cpp_receding_horizon_swings_up(tmp_path):
     exe = tmp_path / "cartpole"
     subprocess.run([gxx, "-std=c++17", "-O2", str(ROOT / "tests" / "cpp" / "cartpole_receding_horizon.cpp"),
                     "-I", str(ROOT / "include"), str(lib), f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_cpp_mirror_receding_horizon(tmp_path):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no C++ compiler")
+    lib = Path(A.lib()._name)
+    exe = tmp_path / "mirror"
+    subprocess.run([gxx, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror",
+                    str(ROOT / "tests" / "cpp" / "cartpole_mirror.cpp"), "-I", str(ROOT / "include"), str(lib),
+                    f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr

@@ -256,8 +256,9 @@ mppi_status mppi_set_costmap(mppi_handle* h, const float* map, int width, int he
 
 /* Surrogate weights for MPPI_MODEL_BICYCLE_SLIP_MLP: 9->64->64->5 tanh MLP, fp32 row-major W1[64][9], b1[64],
  * W2[64][64], b2[64], W3[5][64], b3[5] (FNNHelper layout, fnn_helper.cu:353-382), plus input / output scaling.
- * precision 0 = bf16 weights on the tensor cores, 1 = fp8 e4m3 weights with one scale per layer on the tensor cores
- * (both FP32 accumulation), 2 = plain FP32 on the CUDA cores (one thread per sample, as FNNHelper evaluates it). */
+ * precision 0 = bf16 weights on the tensor cores (BF16 operands), 1 = fp8 e4m3 weights with one power-of-two scale
+ * per layer on the tensor cores (FP16 operands, in which q * scale is exact), both with FP32 accumulation; 2 = plain
+ * FP32 on the CUDA cores (one thread per sample, as FNNHelper evaluates it). */
 mppi_status mppi_set_mlp(mppi_handle* h, const float* params, size_t num_params, int precision);
 
 /* Analytic judge of the surrogate rollout (MPPI_MODEL_BICYCLE_SLIP_MLP only): after the surrogate rollout the
@@ -356,15 +357,16 @@ mppi_status mppi_surrogate_validate(mppi_surrogate* s, int n, float* rmse5);
 mppi_status mppi_surrogate_get_params(mppi_surrogate* s, float* out);
 mppi_status mppi_surrogate_set_params(mppi_surrogate* s, const float* in);
 
-/* Surrogate forward pass on the tensor cores (BF16 operands, FP32 accumulation) for `batch` rows of physical inputs
+/* Surrogate forward pass on the tensor cores (16-bit operands, FP32 accumulation) for `batch` rows of physical inputs
  * X_d[batch][9], writing physical outputs Y_d[batch][5] (device pointers); params is the host parameter vector and
- * precision selects BF16 (0) or FP8 E4M3 weights with one scale per layer (1).  The evaluation FNNHelper::forward
+ * precision selects BF16 (0) or FP8 E4M3 weights with one power-of-two scale per layer (1, FP16 operands).  The evaluation FNNHelper::forward
  * performs per sample (fnn_helper.cu:418-495), as one GEMM chain per 128 rows. */
 mppi_status mppi_kernel_mlp_forward(const float* params, int precision, const float* X_d, float* Y_d, int batch,
                                     void* stream);
 /* The weights the tensor cores see for a precision: out[MPPI_MLP_PARAMS] is params with every weight replaced by its
  * quantised value q (BF16 rounding happens on the device; FP8: the E4M3 value of W / scale), layer_scales[3] (may be
- * NULL) the per-layer scales (1 for BF16).  W is represented as q * scale. */
+ * NULL) the per-layer scales (1 for BF16; for FP8 the smallest power of two with max |W| / scale <= 448).  W is
+ * represented as q * scale. */
 mppi_status mppi_mlp_quantize(const float* params, int precision, float* out, float* layer_scales);
 
 /* ---- kernel-level entry points (mppi::kernels launchers, include/mppi/core/mppi_common.cuh:206-258) ----------- */

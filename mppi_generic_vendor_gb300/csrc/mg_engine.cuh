@@ -1243,7 +1243,8 @@ private:
       if (!use_analytic_)
       {
         const FusedNoise fn = fused_noise_args(stride, iter);
-        MG_TRY(launch_mlp_rollout(a, mlp_d_.p, mlp_precision_, fused() ? &fn : nullptr, num_sms_, stream_));
+        MG_TRY(launch_mlp_rollout(a, mlp_d_.p, mlp_norm(mlp_host_.data()), mlp_precision_, fused() ? &fn : nullptr,
+                                  num_sms_, stream_));
         if (judge_total_ == 0) return MPPI_OK;
         JudgeArgs j;
         j.r = a;

@@ -1,6 +1,6 @@
 // mg_mlp.cu — tensor-core evaluation of the surrogate MLP: a standalone forward entry point and the rollout kernel of
-// the MLP bicycle model (the per-timestep inference over all samples is one BF16 tcgen05 GEMM chain per 128-sample
-// tile, FP32 accumulation in TMEM; see mg_mlp.cuh).  The rollout's work items hold kMlpTiles tiles of one instance.
+// the MLP bicycle model (the per-timestep inference over all samples is one tcgen05 GEMM chain per 128-sample tile,
+// BF16 operands for BF16 weights and FP16 operands for FP8 weights, FP32 accumulation in TMEM; see mg_mlp.cuh).  The rollout's work items hold kMlpTiles tiles of one instance.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -12,17 +12,16 @@ namespace mg
 {
 namespace
 {
-// A CTA of NT tiles holds MlpSmem::total(NT) bytes of shared memory (+ alignment slack) and MlpSmem::tmem_cols(NT)
-// TMEM columns: 31 KB and 64 columns for one tile (at most 7 CTAs per SM, 448 columns), 49 KB and 128 columns for two
-// (at most 4, 512 columns).  The columns of co-resident CTAs therefore fit the SM's 512, so an allocation never waits
-// for another CTA.
-// The operand tiles are K-major without swizzling, which needs 16-byte alignment only: a 128-byte aligned dynamic
-// block keeps the footprint at 30 KB, so seven rollout CTAs fit an SM.
-constexpr size_t kMlpFwdSmem = MlpSmem::total(1);
-constexpr size_t kMlpRolloutSmem = MlpSmem::total(kMlpTiles);
+// A CTA of NT tiles holds MlpSmem::total(NT, half) bytes of shared memory and MlpSmem::tmem_cols(NT) TMEM columns:
+// 27.3 KB (FP16 operands) or 27.5 KB (BF16) and 64 columns for one tile, so at most eight CTAs per SM by TMEM (512
+// columns) and by shared memory; the columns of co-resident CTAs therefore fit the SM's 512, and an allocation never
+// waits for another CTA.  The operand tiles are K-major without swizzling, which needs 16-byte alignment only (the
+// dynamic block is 128-byte aligned).
+constexpr size_t mlp_smem(bool half) { return MlpSmem::total(kMlpTiles, half); }
 
-__global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, const float* X, float* Y, int B,
-                                                          unsigned int* status)
+template <bool kHalf>
+__global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, const __grid_constant__ MlpNorm nm,
+                                                          const float* X, float* Y, int B, unsigned int* status)
 {
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ __align__(8) uint64_t mbar;
@@ -40,23 +39,23 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* params, c
     mbar_init(&mbar, 1);
     fence_mbarrier_init();
   }
-  mlp_load_weights(sm, params);
+  mlp_load_weights<kHalf>(sm, params);
   tc_fence_before_sync();
   __syncthreads();
   tc_fence_after_sync();
   const uint32_t taddr = s_tmem;
   uint32_t phase = 0;
-  const float* nrm = reinterpret_cast<const float*>(sm + MlpSmem::NORM);
   for (int tile = blockIdx.x; tile * 128 < B; tile += gridDim.x)
   {
     const int row = tile * 128 + tid;
     float x[1][kMlpIn], y[1][kMlpOut];
 #pragma unroll
-    for (int i = 0; i < kMlpIn; ++i) x[0][i] = row < B ? (X[(size_t)row * kMlpIn + i] - nrm[i]) * nrm[32 + i] : 0.0f;
-    if (!mlp_tile_forward<1>(sm, taddr, &mbar, phase, &s_fail, x, y)) break;
+    for (int i = 0; i < kMlpIn; ++i)
+      x[0][i] = row < B ? (X[(size_t)row * kMlpIn + i] - nm.in_mean[i]) * nm.in_scale[i] : 0.0f;
+    if (!mlp_tile_forward<1, kHalf>(sm, taddr, &mbar, phase, &s_fail, x, y)) break;
     if (row < B)
 #pragma unroll
-      for (int j = 0; j < kMlpOut; ++j) Y[(size_t)row * kMlpOut + j] = y[0][j] * nrm[23 + j] + nrm[18 + j];
+      for (int j = 0; j < kMlpOut; ++j) Y[(size_t)row * kMlpOut + j] = y[0][j] * nm.out_std[j] + nm.out_mean[j];
   }
   tc_fence_before_sync();
   __syncthreads();
@@ -108,11 +107,12 @@ __device__ __forceinline__ void mlp_thread_forward(const float* P, const float* 
 // walk work items of 128 * kMlpTiles samples of one instance; thread i owns row i of every tile (samples
 // first + i + 128 n).  The Euler step, the costmap cost and the likelihood term follow rolloutKernel
 // (mppi_common.cu:105-152) exactly as the analytic rollout does.  kTensor: the network runs on the tensor cores
-// (mlp_tile_forward, BF16 or FP8 weights, one MMA round trip per layer for all tiles of the CTA); otherwise in plain
-// FP32 on the CUDA cores (mlp_thread_forward).
-template <bool kTensor, bool kFused>
+// (mlp_tile_forward, one MMA round trip per layer for all tiles of the CTA; kHalf: FP16 operands for FP8 weights,
+// else BF16); otherwise in plain FP32 on the CUDA cores (mlp_thread_forward).
+template <bool kTensor, bool kFused, bool kHalf>
 __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
-    const __grid_constant__ RolloutArgs<BicycleSlipMLPModel> a, const float* mlp, const __grid_constant__ FusedNoise f)
+    const __grid_constant__ RolloutArgs<BicycleSlipMLPModel> a, const float* mlp, const __grid_constant__ MlpNorm nm,
+    const __grid_constant__ FusedNoise f)
 {
   using Model = BicycleSlipMLPModel;
   // tensor cores: 128 threads, each owning row i of kMlpTiles tiles; CUDA cores: one thread per sample
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
       mbar_init(&mbar, 1);
       fence_mbarrier_init();
     }
-    mlp_load_weights(sm, mlp);
+    mlp_load_weights<kHalf>(sm, mlp);
     tc_fence_before_sync();
     __syncthreads();
     tc_fence_after_sync();
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
   }
   const uint32_t taddr = kTensor ? s_tmem : 0u;
   uint32_t phase = 0;
-  const float* nrm = kTensor ? reinterpret_cast<const float*>(sm + MlpSmem::NORM) : pf + kMlpInMean;
+  const float* nrm = pf + kMlpInMean;  // CUDA cores: the normalisation in the shared parameter copy
   bool ok = true;
   for (;;)
   {
@@ -243,11 +243,11 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
         }
         if constexpr (kTensor)
         {
-          // the inputs are rounded to BF16 next, so a multiply by the stored reciprocal stands in for the division
+          // the inputs are rounded to 16 bits next, so a multiply by the reciprocal stands in for the division
 #pragma unroll
-          for (int i = 0; i < S; ++i) xin[n][i] = (x[n][i] - nrm[i]) * nrm[32 + i];
-          xin[n][7] = (u[n][0] - nrm[7]) * nrm[32 + 7];
-          xin[n][8] = (u[n][1] - nrm[8]) * nrm[32 + 8];
+          for (int i = 0; i < S; ++i) xin[n][i] = (x[n][i] - nm.in_mean[i]) * nm.in_scale[i];
+          xin[n][7] = (u[n][0] - nm.in_mean[7]) * nm.in_scale[7];
+          xin[n][8] = (u[n][1] - nm.in_mean[8]) * nm.in_scale[8];
         }
         else
         {
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
       }
       if constexpr (kTensor)
       {
-        ok = mlp_tile_forward<NT>(sm, taddr, &mbar, phase, &s_fail, xin, y);
+        ok = mlp_tile_forward<NT, kHalf>(sm, taddr, &mbar, phase, &s_fail, xin, y);
         if (!ok) break;
       }
       else
@@ -278,7 +278,8 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
         xd[0] = x[n][3] * cy - x[n][4] * sy;
         xd[1] = x[n][3] * sy + x[n][4] * cy;
 #pragma unroll
-        for (int j = 0; j < kMlpOut; ++j) xd[2 + j] = y[n][j] * nrm[23 + j] + nrm[18 + j];
+        for (int j = 0; j < kMlpOut; ++j)
+          xd[2 + j] = kTensor ? y[n][j] * nm.out_std[j] + nm.out_mean[j] : y[n][j] * nrm[23 + j] + nrm[18 + j];
         float xn[S];
 #pragma unroll
         for (int i = 0; i < S; ++i) xn[i] = fmaf(xd[i], a.dt, x[n][i]);
@@ -541,21 +542,22 @@ __global__ void __launch_bounds__(256) judge_finalize_kernel(const __grid_consta
 }
 }  // namespace
 
-mppi_status launch_mlp_rollout(const RolloutArgs<BicycleSlipMLPModel>& a, const float* mlp_d, int precision,
-                               const FusedNoise* fused, int num_sms, cudaStream_t s)
+mppi_status launch_mlp_rollout(const RolloutArgs<BicycleSlipMLPModel>& a, const float* mlp_d, const MlpNorm& norm,
+                               int precision, const FusedNoise* fused, int num_sms, cudaStream_t s)
 {
   const bool tensor = precision != 2;
-  auto kern = tensor ? (fused ? rollout_mlp_kernel<true, true> : rollout_mlp_kernel<true, false>)
-                     : (fused ? rollout_mlp_kernel<false, true> : rollout_mlp_kernel<false, false>);
+  auto kern = precision == 0 ? (fused ? rollout_mlp_kernel<true, true, false> : rollout_mlp_kernel<true, false, false>)
+              : precision == 1 ? (fused ? rollout_mlp_kernel<true, true, true> : rollout_mlp_kernel<true, false, true>)
+                               : (fused ? rollout_mlp_kernel<false, true, false> : rollout_mlp_kernel<false, false, false>);
   FusedNoise f{};
   if (fused) f = *fused;
-  const size_t smem = tensor ? kMlpRolloutSmem : sizeof(float) * kMlpDevParams;
+  const size_t smem = tensor ? mlp_smem(precision == 1) : sizeof(float) * kMlpDevParams;
   MG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 1;
   MG_CUDA(resident_ctas_per_sm(kern, tensor ? 128 : kMlpSamplesPerCta, smem, &per_sm));
   per_sm = std::max(1, tensor ? std::min(per_sm, (int)(512 / MlpSmem::tmem_cols(kMlpTiles))) : per_sm);
   const int grid = std::max(1, std::min(a.num_tiles, per_sm * num_sms));
-  kern<<<grid, tensor ? 128 : kMlpSamplesPerCta, smem, s>>>(a, mlp_d, f);
+  kern<<<grid, tensor ? 128 : kMlpSamplesPerCta, smem, s>>>(a, mlp_d, norm, f);
   MG_CUDA(cudaGetLastError());
   return MPPI_OK;
 }
@@ -597,9 +599,16 @@ void mlp_prepare(const float* params, int precision, float* dev_out, float* effe
     float scale = 1.0f;
     if (precision == 1)
     {
+      // the smallest power of two that brings max |W| to at most 448 (the largest E4M3 value): q * scale is then
+      // exact in FP32 and, for the weights of a trained layer, in FP16
       float amax = 0.0f;
       for (int e = 0; e < w_len[l]; ++e) amax = std::max(amax, std::fabs(params[w_off[l] + e]));
-      if (amax > 0.0f) scale = amax / 448.0f;
+      if (amax > 0.0f)
+      {
+        int ex = 0;
+        const float fr = std::frexp(amax / 448.0f, &ex);  // amax / 448 = fr * 2^ex, fr in [0.5, 1)
+        scale = std::ldexp(1.0f, fr == 0.5f ? ex - 1 : ex);
+      }
       for (int e = 0; e < w_len[l]; ++e)
       {
         const float q = e4m3_round(params[w_off[l] + e] / scale);
@@ -658,11 +667,12 @@ mppi_status mppi_kernel_mlp_forward(const float* params, int precision, const fl
         cudaSuccess)
       break;
     if ((e = cudaMemsetAsync(status, 0, sizeof(unsigned int), s)) != cudaSuccess) break;
-    if ((e = cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kMlpFwdSmem)) != cudaSuccess)
+    auto kern = precision == 1 ? mlp_forward_kernel<true> : mlp_forward_kernel<false>;
+    const size_t smem = MlpSmem::total(1, precision == 1);
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
       break;
     const int tiles = (batch + 127) / 128;
-    mlp_forward_kernel<<<std::min(tiles, 8192), 128, kMlpFwdSmem, s>>>(p_d, X_d, Y_d, batch, status);
+    kern<<<std::min(tiles, 8192), 128, smem, s>>>(p_d, mlp_norm(params), X_d, Y_d, batch, status);
     if ((e = cudaGetLastError()) != cudaSuccess) break;
     unsigned int h = 0;
     if ((e = cudaMemcpyAsync(&h, status, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;

@@ -29,6 +29,13 @@ __host__ __device__ constexpr uint32_t umma_idesc_bf16_f32(int M, int N)
          | ((uint32_t)(N >> 3) << 17)       // N / 8
          | ((uint32_t)(M >> 4) << 24);      // M / 16
 }
+// The same with FP16 A and B (format code 0 for both).
+__host__ __device__ constexpr uint32_t umma_idesc_f16_f32(int M, int N)
+{
+  return (1u << 4)                          // D format: F32
+         | ((uint32_t)(N >> 3) << 17)       // N / 8
+         | ((uint32_t)(M >> 4) << 24);      // M / 16
+}
 
 // Allocate `ncols` TMEM columns (a power of two >= 32); executed by one whole warp; the base address lands in *dst.
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols)
@@ -46,8 +53,9 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
 
-// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread (kind::f16: BF16 or FP16 operands, as the instruction
+// descriptor says).
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                           uint32_t accumulate)
 {
   asm volatile(
@@ -90,6 +98,14 @@ __device__ __forceinline__ float tanh_fast(float x)
 {
   float y;
   asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// tanh.approx.f16x2: two FP16 tanh values from one MUFU operation (inputs and results packed low | high << 16).
+__device__ __forceinline__ uint32_t tanh_f16x2(uint32_t x)
+{
+  uint32_t y;
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(y) : "r"(x));
   return y;
 }
 

@@ -1,7 +1,8 @@
-"""Surrogate MLP on the tensor cores (tcgen05, BF16 operands, FP32 accumulation in TMEM).
+"""Surrogate MLP on the tensor cores (tcgen05; BF16 operands for BF16 weights, FP16 operands for FP8 weights; FP32
+accumulation in TMEM).
 
-* ``mppi_kernel_mlp_forward`` against a NumPy emulation of the BF16 pipeline (operands rounded to BF16 as the kernel
-  stores them, FP64 dot products, exact tanh) and against the oracle's FP64 forward on the FP32 parameters;
+* ``mppi_kernel_mlp_forward`` against a NumPy emulation of the 16-bit pipeline (operands rounded to BF16 or FP16 as the
+  kernel stores them, FP64 dot products, exact tanh) and against the oracle's FP64 forward on the FP32 parameters;
 * the MLP bicycle controller against the oracle's FP32 MLP rollout on the same injected noise, and the drift of the
   surrogate rollout from the FP64 analytic rollout it was trained to imitate.
 """
@@ -41,6 +42,12 @@ def e4m3(a):
     return (np.sign(a) * np.where(m > 0, r, 0.0)).astype(np.float32)
 
 
+def pow2_scale(amax):
+    """The smallest power of two s with amax / s <= 448 (the largest E4M3 value)."""
+    fr, ex = np.frexp(np.float32(amax) / np.float32(448.0))
+    return np.float32(np.ldexp(1.0, int(ex) - 1 if fr == 0.5 else int(ex)))
+
+
 def quantize(p, precision):
     """Weights as the tensor cores see them (q) and the per-layer scales; W = q * scale."""
     p = np.asarray(p, np.float32)
@@ -49,26 +56,32 @@ def quantize(p, precision):
     q = p.copy()
     scales = []
     for lo, hi in [(W1, B1), (W2, B2), (W3, B3)]:
-        amax = np.float32(np.abs(p[lo:hi]).max())
-        s = np.float32(amax / np.float32(448.0))
+        s = pow2_scale(np.abs(p[lo:hi]).max())
         q[lo:hi] = e4m3(p[lo:hi] / s)
         scales.append(s)
     return q, np.array(scales, np.float32)
 
 
+def f16(a):
+    """Round float32 to the nearest FP16 (ties to even), returned as float32."""
+    return np.asarray(a, np.float32).astype(np.float16).astype(np.float32)
+
+
 def emulate_bf16(p, X, precision=0):
-    """The kernel's arithmetic with exact dot products and tanh: BF16 weights (FP8 values are exact in BF16) and
-    activations, per-layer scale and bias applied to the FP32 accumulator."""
+    """The kernel's arithmetic with exact dot products and tanh: weights q * scale and activations rounded to the
+    16-bit operand type (BF16 for BF16 weights; FP16 for FP8 weights, where q * scale is exact), biases added to the
+    FP32 accumulator."""
     p = np.asarray(p, np.float32)
     q, s = quantize(p, precision)
+    r16 = bf16 if precision == 0 else f16
     xin = ((X.astype(np.float32) - p[IN_MEAN:IN_STD]) / p[IN_STD:OUT_MEAN]).astype(np.float32)
-    a0 = bf16(xin).astype(np.float64)
-    w1 = bf16(q[W1:B1]).reshape(64, 9).astype(np.float64)
-    w2 = bf16(q[W2:B2]).reshape(64, 64).astype(np.float64)
-    w3 = bf16(q[W3:B3]).reshape(5, 64).astype(np.float64)
-    h1 = bf16(np.tanh((a0 @ w1.T).astype(np.float32) * s[0] + p[B1:W2])).astype(np.float64)
-    h2 = bf16(np.tanh((h1 @ w2.T).astype(np.float32) * s[1] + p[B2:W3])).astype(np.float64)
-    y = (h2 @ w3.T).astype(np.float32) * s[2] + p[B3:IN_MEAN]
+    a0 = r16(xin).astype(np.float64)
+    w1 = r16(q[W1:B1] * s[0]).reshape(64, 9).astype(np.float64)
+    w2 = r16(q[W2:B2] * s[1]).reshape(64, 64).astype(np.float64)
+    w3 = r16(q[W3:B3] * s[2]).reshape(5, 64).astype(np.float64)
+    h1 = r16(np.tanh((a0 @ w1.T).astype(np.float32) + p[B1:W2])).astype(np.float64)
+    h2 = r16(np.tanh((h1 @ w2.T).astype(np.float32) + p[B2:W3])).astype(np.float64)
+    y = (h2 @ w3.T).astype(np.float32) + p[B3:IN_MEAN]
     return y * p[OUT_STD:] + p[OUT_MEAN:OUT_STD]
 
 
@@ -128,7 +141,11 @@ def test_quantize_matches_e4m3_definition():
     q, s = quantize(p, 1)
     assert np.array_equal(scales, s)
     assert np.array_equal(out, q)
-    assert np.abs(out[W2:B2]).max() == 448.0
+    # power-of-two scales: the largest |q| of a layer lands in [224, 448], and q * scale is exact in FP16
+    for l, (lo, hi) in enumerate([(W1, B1), (W2, B2), (W3, B3)]):
+        assert np.frexp(scales[l])[0] == 0.5
+        assert 224.0 <= np.abs(out[lo:hi]).max() <= 448.0
+        assert np.array_equal(f16(out[lo:hi] * scales[l]), out[lo:hi] * scales[l])
 
 
 def test_forward_rejects_bad_parameters():

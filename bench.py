@@ -172,16 +172,20 @@ def algorithmic_bytes(wl, colored: bool):
 _SURROGATE = {}
 
 
-def surrogate_params():
-    """Surrogate weights for the surrogate workloads, trained once per process on the GPU by the engine's own kernels
-    (the CPU baseline of the reference arm, which has no GPU, falls back to a fixed seeded initialisation)."""
-    if "p" not in _SURROGATE:
+def surrogate_params(weight_format="fp32"):
+    """Surrogate weights for the surrogate workloads, trained once per process on the GPU by the engine's own kernels,
+    with quantisation-aware fine-tuning for a BF16 / FP8 deployment (the CPU baseline of the reference arm, which has
+    no GPU, falls back to a fixed seeded initialisation)."""
+    key = "p" if weight_format == "fp32" else "p_" + weight_format
+    if key not in _SURROGATE and "p" in _SURROGATE and _SURROGATE.get("cpu_only"):
+        return _SURROGATE["p"]
+    if key not in _SURROGATE:
         try:
             if _SURROGATE.get("cpu_only"):
                 raise RuntimeError("no GPU on this arm")
             from mppi_generic_vendor_gb300 import workloads as W
 
-            _SURROGATE["p"] = W.train_surrogate()
+            _SURROGATE[key] = W.train_surrogate(weight_format=weight_format)
         except Exception:
             rng = np.random.default_rng(7)
             p = np.zeros(5153, np.float32)
@@ -191,14 +195,16 @@ def surrogate_params():
             p[5134:5143] = [15.0, 15.0, 1.8, 4.0, 1.2, 0.9, 0.3, 0.6, 0.6]
             p[5125:5134] = [25.6, 25.6, 0.0, 8.0, 0.0, 0.0, 0.0, 0.0, 0.0]
             p[5148:5153] = 1.0
-            _SURROGATE["p"] = p
-    return _SURROGATE["p"]
+            _SURROGATE[key] = p
+    return _SURROGATE[key]
 
 
 def surrogate_extras(args, wl, stream):
     """Surrogate workloads: the plain GPU form (the same instances, analytic model in FP32, one controller per
-    instance solved one after another) timed on the same GPU, and the final-cost error of each instance's nominal
-    control sequence under the surrogate against the FP64 analytic rollout."""
+    instance solved one after another) timed on the same GPU; the cost error of each instance's nominal control
+    sequence under the surrogate against the FP64 analytic rollout; and the final trajectory cost: MPPI on the
+    surrogate (judge on) against MPPI on the analytic model, both from zero control sequences for the same number of
+    iterations, each final sequence costed by the FP64 analytic rollout."""
     import oracle
     from mppi_generic_vendor_gb300 import BicycleSlipDynamics, GaussianDistribution, VanillaMPPIController
     from mppi_generic_vendor_gb300 import _abi as A
@@ -242,12 +248,43 @@ def surrogate_extras(args, wl, stream):
                                    costmap=(cmap, 0.1, (0.0, 0.0)), fp64=True, state_dim=7)
         k0 = int(np.sum(wl.K[:i]))
         errs.append(abs(float(costs[k0]) - float(c64[0])) / abs(float(c64[0])))
+    # final trajectory cost after `iters` MPPI iterations from zero sequences, surrogate (batched) vs analytic
+    iters, nchk = 10, min(n, 16)
+    ctrl.setControlSeqs([np.zeros((2, int(t)), np.float32) for t in wl.T])
+    for _ in range(iters):
+        ctrl.computeControl(wl.x0, 1)
+    u_sur = ctrl.getControlSeqs()
+
+    def cost64(i, u):
+        ut = np.ascontiguousarray(np.asarray(u, np.float32).T)
+        c64, _, _ = oracle.rollout(A.MODEL_BICYCLE_SLIP, BicycleSlipDynamics().getParams(), ctrl._cost_arr[i], x0[i],
+                                   ut, ut, sp, ctrl.constraints_, 2.0, 0.0, 1, int(wl.T[i]), 0.02,
+                                   costmap=(cmap, 0.1, (0.0, 0.0)), fp64=True, state_dim=7)
+        return float(c64[0])
+
+    rel = []
+    for i in range(nchk):
+        c = VanillaMPPIController(BicycleSlipDynamics(), W._slip_cost(cmap), None,
+                                  GaussianDistribution(std_dev=(0.5, 0.5)), 0.02, 1, 2.0, 0.0, int(wl.T[i]),
+                                  int(wl.K[i]), seed=i, stream=stream)
+        for _ in range(iters):
+            c.computeControl(x0[i], 1)
+        u_ana = c.getControlSeq()
+        c.close()
+        rel.append(cost64(i, u_sur[i]) / cost64(i, u_ana) - 1.0)
+    rel = np.array(rel)
     return {"plain_gpu": {"form": "analytic model, FP32, one controller per instance, solved in turn",
                           "iters_per_s": 1.0 / plain_s,
                           "sample_steps_per_s": wl.sample_steps_per_iter / plain_s},
-            "final_cost_error": {"vs": "FP64 analytic rollout of each instance's nominal control sequence",
-                                 "instances": len(errs), "median": float(np.median(errs)),
-                                 "max": float(np.max(errs))}}
+            "surrogate_cost_error": {"vs": "FP64 analytic rollout of each instance's nominal control sequence",
+                                     "instances": len(errs), "median": float(np.median(errs)),
+                                     "max": float(np.max(errs))},
+            "final_trajectory_cost": {"vs": "MPPI on the analytic model, same instances, %d iterations from zero "
+                                            "sequences; both final sequences costed by the FP64 analytic rollout"
+                                            % iters,
+                                      "instances": int(nchk), "median_rel": float(np.median(rel)),
+                                      "max_rel": float(rel.max()),
+                                      "within_1pct": int(np.sum(rel <= 0.01))}}
 
 
 # ------------------------------------------------------------------------------------------------ CPU baseline
@@ -393,8 +430,9 @@ def run_gpu(args, ws, rank, local):
     B.build()
     stream = torch.cuda.Stream()
     surrogate = args.workload in ("slip_mlp", "batched_slip_mlp")
+    wprec = args.precision or ("fp8" if args.workload == "batched_slip_mlp" else "bf16")
     wl = build_workload(args.workload, seed=0, stream=stream.cuda_stream, instances=args.instances,
-                        precision=args.precision, params=surrogate_params() if surrogate else None)
+                        precision=args.precision, params=surrogate_params(wprec) if surrogate else None)
     ctrl = wl.controller
     colored = args.workload == "batched_di"
     x0 = wl.x0

@@ -349,7 +349,12 @@ mppi_status mppi_surrogate_generate(mppi_surrogate* s);
 /* `steps` Adam steps on random mini-batches of `batch` transitions, learning rate decaying geometrically from lr to
  * lr_final; loss_out (may be NULL) receives the mini-batch loss of every step. */
 mppi_status mppi_surrogate_train(mppi_surrogate* s, int steps, int batch, float lr, float lr_final, float* loss_out);
-/* Loss and parameter gradient on a given normalised batch (host X[B][9], Y[B][5]) with the training kernels. */
+/* Weight format the training passes use (quantisation-aware training): 2 = FP32 (default), 0 = weights rounded to
+ * BF16, 1 = E4M3 with the per-layer power-of-two scale of mppi_mlp_quantize.  Forward and backward run through the
+ * rounded weights; Adam updates the FP32 master weights with that gradient (straight-through estimator). */
+mppi_status mppi_surrogate_set_weight_format(mppi_surrogate* s, int precision);
+/* Loss and parameter gradient on a given normalised batch (host X[B][9], Y[B][5]) with the training kernels (in the
+ * weight format set above). */
 mppi_status mppi_surrogate_gradient(mppi_surrogate* s, const float* X, const float* Y, int batch, float* grad_out,
                                     float* loss_out);
 /* Root-mean-square error per output, in physical units, on n fresh transitions of the analytic model. */

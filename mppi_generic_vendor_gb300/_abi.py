@@ -166,6 +166,7 @@ SIGNATURES += [
     ("mppi_surrogate_destroy", C.c_int, [_P]),
     ("mppi_surrogate_generate", C.c_int, [_P]),
     ("mppi_surrogate_train", C.c_int, [_P, C.c_int, C.c_int, C.c_float, C.c_float, _FP]),
+    ("mppi_surrogate_set_weight_format", C.c_int, [_P, C.c_int]),
     ("mppi_surrogate_gradient", C.c_int, [_P, _FP, _FP, C.c_int, _FP, _FP]),
     ("mppi_surrogate_validate", C.c_int, [_P, C.c_int, _FP]),
     ("mppi_surrogate_get_params", C.c_int, [_P, _FP]),

@@ -10,6 +10,14 @@
 // Training step: one CTA per 64 samples computes the forward pass, the loss and the back-propagated gradient of its
 // samples in shared memory and writes its partial gradient row; a second kernel adds the rows in CTA order (a fixed
 // order, so training is deterministic for a given seed) and applies Adam.
+//
+// Quantisation-aware training (weight format BF16 or FP8): the forward and backward passes use the weights as the
+// tensor-core rollout will hold them (rounded to BF16, or E4M3 with the per-layer power-of-two scale of the current
+// weights) and Adam updates the FP32 master weights with that gradient (straight-through: the rounding is treated as
+// the identity when differentiating), so the network learns to work through its own quantisation.
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -113,9 +121,46 @@ __global__ void data_kernel(mppi_bicycle_slip_params p, Box box, uint32_t k0, ui
   }
 }
 
+// Per-layer power-of-two scale of the FP8 weight format (the smallest with max |W| / scale <= 448, 1 for an all-zero
+// layer), the same choice the rollout's weight preparation makes; one CTA per layer.
+__global__ void __launch_bounds__(256) weight_scale_kernel(const float* params, float* scales)
+{
+  __shared__ float s_max[8];
+  const int off[3] = { oW1, oW2, oW3 }, len[3] = { kHid * kIn, kHid * kHid, kOut * kHid };
+  const int l = blockIdx.x;
+  float m = 0.0f;
+  for (int e = threadIdx.x; e < len[l]; e += blockDim.x) m = fmaxf(m, fabsf(params[off[l] + e]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    float a = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a = fmaxf(a, s_max[w]);
+    float scale = 1.0f;
+    if (a > 0.0f)
+    {
+      int ex = 0;
+      const float fr = frexpf(a / 448.0f, &ex);
+      scale = ldexpf(1.0f, fr == 0.5f ? ex - 1 : ex);
+    }
+    scales[l] = scale;
+  }
+}
+
+// A weight as the tensor cores see it in weight format `fmt` (0 BF16, 1 E4M3 times the layer scale, 2 FP32).
+__device__ __forceinline__ float quantize_weight(float w, int fmt, float scale)
+{
+  if (fmt == 0) return __bfloat162float(__float2bfloat16_rn(w));
+  if (fmt == 1) return (float)__nv_fp8_e4m3(w / scale) * scale;
+  return w;
+}
+
 struct GradArgs
 {
   const float* params;
+  int wfmt;             // weight format of the forward / backward passes (2: FP32 master weights as they are)
+  const float* wscale;  // per-layer FP8 scales (wfmt 1)
   const float* X;
   const float* Y;
   int n;               // rows in X / Y
@@ -141,7 +186,12 @@ __global__ void __launch_bounds__(256) grad_kernel(const __grid_constant__ GradA
   const int nb = min(kSB, a.batch - b0);
   const float scale = 2.0f / ((float)a.batch * kOut);
 
-  for (int i = tid; i < kNW; i += nt) W[i] = a.params[i];
+  for (int i = tid; i < kNW; i += nt)
+  {
+    const int l = i < oB1 ? 0 : (i >= oW2 && i < oB2) ? 1 : (i >= oW3 && i < oB3) ? 2 : -1;
+    W[i] = (l >= 0 && a.wfmt != 2) ? quantize_weight(a.params[i], a.wfmt, a.wfmt == 1 ? a.wscale[l] : 1.0f)
+                                   : a.params[i];
+  }
   for (int b = tid; b < kSB; b += nt)
   {
     int row = 0;
@@ -366,12 +416,13 @@ public:
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int num_sms = 1;
-  DevBuf<float> X, Y, params, m, v, partials, loss;
+  DevBuf<float> X, Y, params, m, v, partials, loss, wscale;
   DevBuf<double> stats;
   std::vector<float> host_params = std::vector<float>(kNP, 0.0f);
   Norm norm{};
   bool generated = false;
   int adam_t = 0;
+  int wfmt = 2;  // weight format the training passes see (2: FP32)
 
   ~Surrogate()
   {
@@ -430,6 +481,7 @@ public:
       host_params[oOutStd + j] = 1.0f;
     }
     MG_TRY(params.alloc(kNP));
+    MG_TRY(wscale.alloc(3));
     MG_TRY(m.alloc(kNW));
     MG_TRY(v.alloc(kNW));
     MG_CUDA(cudaMemset(m.p, 0, sizeof(float) * kNW));
@@ -541,9 +593,12 @@ public:
     a.k1 = (uint32_t)(cfg.seed >> 32);
     a.norm = norm;
     a.partials = partials.p;
+    a.wfmt = wfmt;
+    a.wscale = wscale.p;
     for (int s = 0; s < steps; ++s)
     {
       a.step = (uint32_t)(adam_t + 1);
+      if (wfmt == 1) weight_scale_kernel<<<3, 256, 0, stream>>>(params.p, wscale.p);
       grad_kernel<<<nparts, 256, kGradSmem, stream>>>(a);
       ++adam_t;
       const float c1 = 1.0f / (1.0f - std::pow(beta1, (float)adam_t));
@@ -579,7 +634,10 @@ public:
     a.k0 = a.k1 = a.step = 0;
     a.norm = norm;
     a.partials = partials.p;
+    a.wfmt = wfmt;
+    a.wscale = wscale.p;
     const int nparts = (batch + kSB - 1) / kSB;
+    if (wfmt == 1) weight_scale_kernel<<<3, 256, 0, stream>>>(params.p, wscale.p);
     grad_kernel<<<nparts, 256, kGradSmem, stream>>>(a);
     reduce_adam_kernel<<<(kNW + 255) / 256, 256, 0, stream>>>(params.p, m.p, v.p, partials.p, nparts, batch, 0.0f,
                                                                0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0, g.p, l.p);
@@ -686,6 +744,14 @@ mppi_status mppi_surrogate_train(mppi_surrogate* s, int steps, int batch, float 
 {
   SUR_OK(s);
   return s->impl->train(steps, batch, lr, lr_final, loss_out);
+}
+
+mppi_status mppi_surrogate_set_weight_format(mppi_surrogate* s, int precision)
+{
+  SUR_OK(s);
+  MG_CHECK(precision >= 0 && precision <= 2, "weight format must be 0 (bf16), 1 (fp8 e4m3) or 2 (fp32)");
+  s->impl->wfmt = precision;
+  return MPPI_OK;
 }
 
 mppi_status mppi_surrogate_gradient(mppi_surrogate* s, const float* X, const float* Y, int batch, float* grad_out,

@@ -51,6 +51,14 @@ class Surrogate:
     def generate(self):
         A.call("mppi_surrogate_generate", self._h)
 
+    WEIGHT_FORMATS = {"bf16": 0, "fp8": 1, "fp32": 2}
+
+    def set_weight_format(self, fmt: str):
+        """Quantisation-aware training: the forward and backward passes of later train() / gradient() calls use the
+        weights rounded as the tensor cores will hold them ("bf16", or "fp8": E4M3 with the per-layer power-of-two
+        scale) while Adam updates the FP32 master weights; "fp32" (the default) trains the weights as they are."""
+        A.call("mppi_surrogate_set_weight_format", self._h, self.WEIGHT_FORMATS[fmt])
+
     def train(self, steps=3000, batch=8192, lr=3e-3, lr_final=1e-4) -> np.ndarray:
         loss = np.empty(steps, dtype=np.float32)
         A.call("mppi_surrogate_train", self._h, int(steps), int(batch), float(lr), float(lr_final), _fp(loss))

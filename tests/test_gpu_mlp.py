@@ -348,6 +348,19 @@ def test_final_trajectory_cost_within_one_percent(well_trained):
     assert j_surrogate <= 1.01 * j_analytic, (j_surrogate, j_analytic)
 
 
+def test_fp8_final_trajectory_cost_within_one_percent():
+    """The same closed-loop criterion with E4M3 weights: after quantisation-aware fine-tuning (forward and backward
+    through the E4M3 weights) MPPI on the FP8 surrogate settles within 1% of MPPI on the analytic model."""
+    from mppi_generic_vendor_gb300.workloads import train_surrogate
+
+    params = train_surrogate(weight_format="fp8")
+    cmap = gaussian_bump_costmap(6, size=128)
+    x0 = np.array([20.0, 20.0, -0.4, 7.0, 0.0, 0.0, 0.0], np.float32)
+    j_analytic = _final_cost(BicycleSlipDynamics(), cmap, x0)
+    j_surrogate = _final_cost(BicycleSlipMLPDynamics(params, precision="fp8"), cmap, x0, judge=0.01)
+    assert j_surrogate <= 1.01 * j_analytic, (j_surrogate, j_analytic)
+
+
 def test_trained_network_gain_over_nominal_model():
     """What the learned model gains: the plant's true parameters differ from the nominal first-principles model an
     engineer would write down (mass, tyre stiffness and drive force off by 20-40%).  Without the network, MPPI rolls

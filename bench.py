@@ -170,6 +170,7 @@ def algorithmic_bytes(wl, colored: bool):
 
 
 _SURROGATE = {}
+ROLLOUT_MODE_NAMES = ["fused", "split", "cooperative", "sampled", "fused_noise_warps"]
 
 
 def surrogate_params(weight_format="fp32"):
@@ -508,7 +509,7 @@ def run_gpu(args, ws, rank, local):
         "iters_per_s": iters_per_s,
         "launch_config": {**dict(zip(["rollout_samples_per_cta", "rollout_time_chunk", "reduction_samples_per_cta"],
                                      ctrl.launchConfig())),
-                          "rollout_mode": ["fused", "split", "cooperative", "sampled"][ctrl.rolloutMode()[0]]},
+                          "rollout_mode": ROLLOUT_MODE_NAMES[ctrl.rolloutMode()[0]]},
         "kernel_ms": {n: float(v) for n, v in zip(names, kms)},
         "roofline": ({"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                       "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,

@@ -293,10 +293,13 @@ mppi_status mppi_autotune(mppi_handle* h, const char* cache_path);
  * dynamics / cost kernels (the dynamics chain alone, then all (k, t) costs in parallel, as the reference's
  * rolloutDynamicsKernel + rolloutCostKernel, mppi_common.cu:155-369), 2 = cooperative (four lanes per sample share
  * the sampling and cost work off the dynamics chain), 3 = the Gaussian sampler as its own kernel, then the rollout
- * on the staged samples (the reference's order: generateSamples, then the rollout kernel).  Modes 1 and 2 are for
- * problems too small to fill the GPU with one thread per sample; all give bit-identical samples and costs.
- * available (may be NULL) receives the bitmask of modes this handle supports (bit m = mode m); modes 1 to 3 need
- * Gaussian sampling, T * C % 4 == 0 and an analytic model, mode 1 also at most 256 MB of stepped states.
+ * on the staged samples (the reference's order: generateSamples, then the rollout kernel), 4 = the fused kernel with
+ * noise warps (a second set of warps per CTA draws the tile's samples into shared memory ahead of the rollout warps,
+ * which run only the dynamics and costs).  Modes 1, 2 and 4 are for problems too small to fill the GPU with one
+ * thread per sample; all give bit-identical samples and costs.
+ * available (may be NULL) receives the bitmask of modes this handle supports (bit m = mode m); modes 1 to 4 need
+ * Gaussian sampling, T * C % 4 == 0 and an analytic model, mode 1 also at most 256 MB of stepped states, mode 4 a
+ * horizon whose controls fit the shared-memory stage (T * C * 33 floats <= 200 KB).
  * mppi_autotune times every available mode. */
 mppi_status mppi_set_rollout_mode(mppi_handle* h, int mode);
 mppi_status mppi_get_rollout_mode(const mppi_handle* h, int* mode, int* available);

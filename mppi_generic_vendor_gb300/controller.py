@@ -25,6 +25,11 @@ from . import _abi as A
 
 
 def _fptr(a: np.ndarray):
+    """float* of a float32 array.  A ctypes array over the array's own buffer costs under a microsecond, against
+    several for ndarray.ctypes.data_as, which matters on the per-iteration calls; read-only or strided arrays take
+    the general route."""
+    if a.dtype == np.float32 and a.flags.c_contiguous and a.flags.writeable and a.size > 0:
+        return (C.c_float * a.size).from_buffer(a)
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
@@ -412,8 +417,8 @@ class BatchedMPPIController:
 
     def setRolloutMode(self, mode):
         """0 = fused rollout kernel, 1 = split dynamics / cost kernels, 2 = cooperative (four lanes per sample),
-        3 = sampler kernel then the staged rollout; modes 1 and 2 are for small problems; samples and costs are
-        bit-identical."""
+        3 = sampler kernel then the staged rollout, 4 = fused with noise warps; modes 1, 2 and 4 are for small
+        problems; samples and costs are bit-identical."""
         A.call("mppi_set_rollout_mode", self._h, int(mode))
 
     def rolloutMode(self):

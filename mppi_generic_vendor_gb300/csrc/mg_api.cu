@@ -95,7 +95,7 @@ mppi_status autotune_impl(EngineBase* e, const char* cache_path, const std::stri
   const int kc_c[3] = { 64, 128, 256 };
   float best = FLT_MAX;
   int best_ns = 128, best_kc = 128, best_mode = 0;
-  for (int m = 0; m < 4; ++m)
+  for (int m = 0; m < 5; ++m)
   {
     if (!((e->rollout_modes() >> m) & 1)) continue;
     MG_TRY(e->set_rollout_mode(m));

@@ -70,7 +70,8 @@ public:
   virtual mppi_status generate_samples(int stride, int iter) = 0;
   virtual mppi_status set_graph_mode(int enable) = 0;
   virtual mppi_status get_launch_config(int* ns, int* tch, int* kc) const = 0;
-  // Rollout mode: 0 = one fused kernel, 1 = split dynamics / cost kernels; rollout_modes() is the bitmask available.
+  // Rollout mode: 0 = one fused kernel, 1 = split dynamics / cost kernels, 2 = cooperative, 3 = sampler kernel then
+  // the staged rollout, 4 = fused with noise warps; rollout_modes() is the bitmask available.
   virtual mppi_status set_rollout_mode(int mode) = 0;
   virtual int rollout_mode() const = 0;
   virtual int rollout_modes() const = 0;
@@ -473,21 +474,30 @@ public:
   bool coop_available() const { return fusable() && !(Model::kMlp && !use_analytic_); }
   // Mode 3 runs the Gaussian sampler as its own kernel and the staged rollout on the written samples.
   bool unfused_available() const { return fusable() && !(Model::kMlp && !use_analytic_); }
+  // Mode 4 is the fused rollout with noise warps; it reads its controls from the shared-memory stage, so the longest
+  // horizon must fit the stage of the smallest tile (tile sizes whose stage does not fit run mode 0's kernel).
+  bool noise_warps_available() const
+  {
+    return fusable() && tile_reduce_active() && fused_stage_bytes_max<32>() != 0;
+  }
   int rollout_modes() const override
   {
-    return 1 | (split_available() ? 2 : 0) | (coop_available() ? 4 : 0) | (unfused_available() ? 8 : 0);
+    return 1 | (split_available() ? 2 : 0) | (coop_available() ? 4 : 0) | (unfused_available() ? 8 : 0) |
+           (noise_warps_available() ? 16 : 0);
   }
   int rollout_mode() const override { return rollout_mode_; }
   mppi_status set_rollout_mode(int mode) override
   {
-    MG_CHECK(mode >= 0 && mode <= 3, "rollout mode must be 0 (fused), 1 (split dynamics / cost), 2 (cooperative) or "
-             "3 (sampler kernel, then the staged rollout)");
+    MG_CHECK(mode >= 0 && mode <= 4, "rollout mode must be 0 (fused), 1 (split dynamics / cost), 2 (cooperative), "
+             "3 (sampler kernel, then the staged rollout) or 4 (fused with noise warps)");
     MG_CHECK(mode != 1 || split_available(),
              "the split rollout needs Gaussian sampling, T*C %% 4 == 0, an analytic model and <= 256 MB of states");
     MG_CHECK(mode != 2 || coop_available(), "the cooperative rollout needs Gaussian sampling, T*C %% 4 == 0 and an "
              "analytic model");
     MG_CHECK(mode != 3 || unfused_available(), "rollout mode 3 needs Gaussian sampling, T*C %% 4 == 0 and an analytic "
              "model");
+    MG_CHECK(mode != 4 || noise_warps_available(), "rollout mode 4 needs Gaussian sampling, T*C %% 4 == 0, an analytic "
+             "model and a horizon whose controls fit the shared-memory stage");
     if (mode == 1 && !states_d_.p) MG_TRY(states_d_.alloc((size_t)total_u_ / C * S));
     rollout_mode_ = mode;
     split_ = mode == 1;
@@ -1024,12 +1034,22 @@ private:
   mppi_status allow_fused_stage()
   {
     MG_CUDA(raise_smem_cap(rollout_fused_kernel<Model, NS>, fused_dyn_bytes<NS>(true)));
+    MG_CUDA(raise_smem_cap(rollout_fused_kernel<Model, NS, true>, fused_dyn_bytes<NS>(true)));
     return MPPI_OK;
   }
 
   // The fused rollout (mode 0) with tile reduction also combines each instance and, in the last iteration, smooths
   // it: no finalize or smoothing kernel follows it.
-  bool tail_finalize() const { return tile_reduce_active() && fused() && !split_ && rollout_mode_ == 0; }
+  bool tail_finalize() const
+  {
+    return tile_reduce_active() && fused() && !split_ && (rollout_mode_ == 0 || rollout_mode_ == 4);
+  }
+  // Mode 4 at this tile size: the stage holds the longest horizon.
+  template <int NS>
+  bool noise_warps_now() const
+  {
+    return rollout_mode_ == 4 && fused_stage_bytes<NS>() != 0;
+  }
 
   FinalizeArgs finalize_args() const
   {
@@ -1067,7 +1087,10 @@ private:
       a.fin = finalize_args();
       a.fin.finish = iter == cp_.num_iters - 1;
     }
-    rollout_fused_kernel<Model, NS><<<rollout_grid_, NS, fused_dyn_bytes<NS>(stage != 0), stream_>>>(a, f);
+    if (noise_warps_now<NS>())
+      rollout_fused_kernel<Model, NS, true><<<rollout_grid_, 2 * NS, fused_dyn_bytes<NS>(true), stream_>>>(a, f);
+    else
+      rollout_fused_kernel<Model, NS><<<rollout_grid_, NS, fused_dyn_bytes<NS>(stage != 0), stream_>>>(a, f);
   }
 
   template <int NS>
@@ -1080,6 +1103,9 @@ private:
           MG_CUDA(resident_ctas_per_sm(rollout_dyn_kernel<Model, NS>, NS, 0, per_sm));
         else if (rollout_mode_ == 2)
           MG_CUDA(resident_ctas_per_sm(rollout_coop_kernel<Model, NS>, 4 * NS, 0, per_sm));
+        else if (noise_warps_now<NS>())
+          MG_CUDA(resident_ctas_per_sm(rollout_fused_kernel<Model, NS, true>, 2 * NS, fused_dyn_bytes<NS>(true),
+                                       per_sm));
         else
           MG_CUDA(resident_ctas_per_sm(rollout_fused_kernel<Model, NS>, NS,
                                        fused_dyn_bytes<NS>(fused_stage_bytes<NS>() != 0), per_sm));
@@ -1536,7 +1562,7 @@ private:
   DevBuf<float> mlp_d_;
   long long total_u_ = 0;      // control-sample floats over all instances
   bool split_ = false;         // split dynamics / cost rollout (rollout mode 1)
-  int rollout_mode_ = 0;       // 0 fused, 1 split, 2 cooperative (four lanes per sample)
+  int rollout_mode_ = 0;       // 0 fused, 1 split, 2 cooperative, 3 sampler kernel + staged, 4 fused + noise warps
   // tile reduction (TileReduce): per tile partial rows, (sum w, sum w^2), minimum; first tile of each instance
   DevBuf<float> tile_part_d_;
   DevBuf<long long> tile_poff_d_;

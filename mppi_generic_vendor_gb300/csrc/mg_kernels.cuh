@@ -779,13 +779,25 @@ __device__ __forceinline__ float4 fused_noise(const FusedNoise& f, const InstDes
                     : philox_normal4((uint64_t)q, (uint32_t)inst, counter, f.seed_lo, f.seed_hi);
 }
 
-template <class Model, int NS>
-__global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant__ RolloutArgs<Model> a,
-                                                           const __grid_constant__ FusedNoise f)
+// Polls of a noise warp's progress word before a rollout warp gives up (each poll is one shared-memory read).
+constexpr uint32_t kMaxProgressPolls = 1u << 22;
+// Quads a noise warp publishes at a time.
+constexpr int kNoiseChunkQuads = 4;
+
+// The fused rollout.  kNoiseWarps: the CTA holds 2 * NS threads; threads NS .. 2NS-1 draw the tile's Gaussian
+// control quads into the shared-memory stage (and the samples buffer) ahead of the rollout, publishing their progress
+// per warp, while threads 0 .. NS-1 run only the dynamics and the costs, reading their controls from the stage.  The
+// arithmetic of every sample is the same as with one thread per sample; the noise generation just leaves the
+// rollout's dependent chain for other schedulers, which pays when the grid has fewer warps than the GPU has
+// schedulers (small K).  Needs the stage (a.tr.u_stride > 0).
+template <class Model, int NS, bool kNoiseWarps = false>
+__global__ void __launch_bounds__(kNoiseWarps ? 2 * NS : NS)
+    rollout_fused_kernel(const __grid_constant__ RolloutArgs<Model> a, const __grid_constant__ FusedNoise f)
 {
   constexpr int S = Model::STATE_DIM;
   constexpr int C = Model::CONTROL_DIM;
   static_assert(4 % C == 0, "a quad must hold whole steps");
+  static_assert((NS & (NS - 1)) == 0 && NS >= 32, "tile sizes are powers of two of at least a warp");
   constexpr int G = 4 / C;
   __shared__ int s_tile;
   __shared__ unsigned int s_min;
@@ -795,7 +807,10 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
   extern __shared__ float s_u[];
   __shared__ int s_last;
   __shared__ float s_eta;
+  __shared__ int s_prog[kNoiseWarps ? NS / 32 : 1];  // quads staged so far, per noise warp
   const int tid = threadIdx.x;
+  const bool noise_warp = kNoiseWarps && tid >= NS;
+  const int slot = tid & (NS - 1);  // the sample slot of this thread within the tile
   const uint32_t counter = f.noise_counter ? *f.noise_counter : 0u;
   for (;;)
   {
@@ -804,12 +819,13 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
       s_tile = (int)atomicAdd(&a.tile_counter[0], 1u);
       s_min = kOrderedPosInf;
     }
+    if (kNoiseWarps && tid < NS / 32) s_prog[tid] = 0;
     __syncthreads();
     const int tile = s_tile;
     if (tile >= a.num_tiles) break;
     const int2 w = a.tiles[tile];
     const InstDesc d = a.inst[w.x];
-    const int k = w.y + tid;
+    const int k = w.y + slot;
     const bool active = k < d.K;
     const typename Model::DynParams dp = a.dyn[w.x];
     const typename Model::CostParams cp = a.cost[w.x];
@@ -819,7 +835,79 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
     float running = 0.0f;
     PendingCost<Model> pc;
     pc.reset(x);
-    if (active)
+    if (noise_warp)
+    {
+      // draw the tile's quads in order into the stage and the samples buffer; publish after each chunk (the whole
+      // warp takes part, active or not, so the progress word always advances)
+      const int nq = d.T * C / 4;
+      const long long q0 = (long long)k * nq;
+      const float pure_threshold = (1.0f - a.sh.pure_pct) * (float)d.K;
+      float* dst = f.samples + d.u_off + 4 * q0;
+      const float4* mrow = reinterpret_cast<const float4*>(a.mean + d.t_off);
+      const int us = a.tr.u_stride;
+      volatile int* prog = s_prog + ((tid - NS) >> 5);
+      for (int c0 = 0; c0 < nq; c0 += kNoiseChunkQuads)
+      {
+        const int c1 = min(c0 + kNoiseChunkQuads, nq);
+        if (active)
+          for (int qi = c0; qi < c1; ++qi)
+          {
+            const float4 o = gaussian_quad<C>(a.sh, __ldg(mrow + qi), f.decay_pow, f.stride, k, pure_threshold,
+                                              4 * qi, fused_noise(f, d, w.x, counter, q0 + qi));
+            *reinterpret_cast<float4*>(dst + 4 * qi) = o;
+            float* col = s_u + (size_t)(4 * qi) * us + slot;
+            col[0] = o.x;
+            col[us] = o.y;
+            col[2 * us] = o.z;
+            col[3 * us] = o.w;
+          }
+        __syncwarp();
+        if ((tid & 31) == 0)
+        {
+          __threadfence_block();
+          *prog = c1;
+        }
+      }
+    }
+    else if (kNoiseWarps && active)
+    {
+      // the rollout warps: controls from the stage once the paired noise warp has published them
+      const int nq = d.T * C / 4;
+      const int us = a.tr.u_stride;
+      volatile int* prog = s_prog + (tid >> 5);
+      bool waited_out = false;
+      auto run = [&](auto lik) {
+        auto quads = [&](int qi, auto q_const) {
+          constexpr int Q = decltype(q_const)::value;
+          if (*prog < qi + Q)
+          {
+            uint32_t i = 0;
+            while (*prog < qi + Q && ++i < kMaxProgressPolls)
+            {
+            }
+            waited_out |= i >= kMaxProgressPolls;
+          }
+          __threadfence_block();
+          float out[4 * Q];
+#pragma unroll
+          for (int e = 0; e < 4 * Q; ++e) out[e] = s_u[(size_t)(4 * qi + e) * us + slot];
+          speculate_steps<Model>(x, running, pc, [&](auto& ar) {
+#pragma unroll
+            for (int g = 0; g < G * Q; ++g)
+              rollout_step<Model, decltype(lik)::value>(a, d, dp, cp, k, out + g * C, qi * G + g, x, running, pc, ar);
+          });
+        };
+        int qi = 0;
+        for (; qi + kSpecQuads<C> <= nq; qi += kSpecQuads<C>) quads(qi, std::integral_constant<int, kSpecQuads<C>>{});
+        for (; qi < nq; ++qi) quads(qi, std::integral_constant<int, 1>{});
+      };
+      if (a.use_likelihood)
+        run(std::true_type{});
+      else
+        run(std::false_type{});
+      if (waited_out) atomicOr(a.status, 1u);
+    }
+    else if (active)
     {
       const int nq = d.T * C / 4;
       const long long q0 = (long long)k * nq;
@@ -873,7 +961,7 @@ __global__ void __launch_bounds__(NS) rollout_fused_kernel(const __grid_constant
         run(std::false_type{});
     }
     unsigned int o = kOrderedPosInf;
-    if (active)
+    if (active && !noise_warp)
     {
       if (a.use_likelihood)
         rollout_flush<Model, true>(a, d, cp, k, running, pc);

@@ -245,19 +245,19 @@ def test_autotune_cache_roundtrip(tmp_path):
 
 @pytest.mark.parametrize("lik", [False, True])
 def test_split_rollout_bit_identical_to_fused(lik):
-    """Rollout modes 1 (dynamics chain, then all (k, t) costs in parallel), 2 (four lanes per sample) and 3 (the
-    sampler kernel, then the staged rollout) give the fused kernel's samples and costs bit for bit, with and without
-    the likelihood-ratio term, over several iterations of Philox noise (T = 100 is not a multiple of the cooperative
-    kernel's 16-step groups)."""
+    """Rollout modes 1 (dynamics chain, then all (k, t) costs in parallel), 2 (four lanes per sample), 3 (the
+    sampler kernel, then the staged rollout) and 4 (fused with noise warps) give the fused kernel's samples and costs
+    bit for bit, with and without the likelihood-ratio term, over several iterations of Philox noise (T = 100 is not
+    a multiple of the cooperative kernel's 16-step groups)."""
     outs = []
-    for mode in (0, 1, 2, 3):
+    for mode in (0, 1, 2, 3, 4):
         dyn = CartpoleDynamics(1.0, 1.0, 1.0)
         dyn.setControlRanges([(-5.0, 5.0)])
         sampler = GaussianDistribution(std_dev=(1.0,), control_cost_coeff=(1.0,) if lik else (0.0,))
         ctrl = VanillaMPPIController(dyn, CartpoleSwingupCost(10.0, 1.0, 100.0, 1.0, 0.0), None, sampler, 0.02, 3, 1.0,
                                      0.0, 100, 2048, seed=5)
         m, avail = ctrl.rolloutMode()
-        assert m == 0 and avail == 15
+        assert m == 0 and avail == 31
         ctrl.setRolloutMode(mode)
         assert ctrl.rolloutMode()[0] == mode
         x0 = np.array([0.0, 0.0, 2.0, 0.0], np.float32)
@@ -265,14 +265,14 @@ def test_split_rollout_bit_identical_to_fused(lik):
         ctrl.computeControl(x0, 1)
         outs.append((ctrl.sample_costs(), ctrl.getControlSeq(), ctrl.control_samples(), ctrl.kernelsPerCompute()))
         ctrl.close()
-    (c0, u0, s0, n0), (c1, u1, s1, n1), (c2, u2, s2, n2), (c3, u3, s3, n3) = outs
-    for c, u, smp in ((c1, u1, s1), (c2, u2, s2), (c3, u3, s3)):
+    (c0, u0, s0, n0), (c1, u1, s1, n1), (c2, u2, s2, n2), (c3, u3, s3, n3), (c4, u4, s4, n4) = outs
+    for c, u, smp in ((c1, u1, s1), (c2, u2, s2), (c3, u3, s3), (c4, u4, s4)):
         assert np.array_equal(s0, smp)
         assert np.array_equal(c0.view(np.uint32), c.view(np.uint32))
         assert np.array_equal(u0, u)
-    # three iterations: mode 0's rollout also combines and (last iteration) smooths, mode 2 launches the combine and
-    # the smoothing kernels, modes 1 and 3 one more kernel per iteration (the cost kernel, the sampler)
-    assert n0 == 3
+    # three iterations: modes 0 and 4 combine and (last iteration) smooth in the rollout, mode 2 launches the combine
+    # and the smoothing kernels, modes 1 and 3 one more kernel per iteration (the cost kernel, the sampler)
+    assert n0 == n4 == 3
     assert n2 == 2 * 3 + 1
     assert n1 == n3 == 3 * 3 + 1
 
@@ -293,7 +293,7 @@ def A_colored():
 
 
 def test_cooperative_rollout_bit_identical_for_two_controls():
-    """Modes 2 and 3 with C = 2 (a quad holds two steps) on the kinematic bicycle: samples, costs and the update
+    """Modes 2, 3 and 4 with C = 2 (a quad holds two steps) on the kinematic bicycle: samples, costs and the update
     equal mode 0's bit for bit; the weights served after the tile reduction equal the oracle's within 1e-5."""
     from mppi_generic_vendor_gb300 import BicycleDynamics, CostmapCost
     from mppi_generic_vendor_gb300.workloads import gaussian_bump_costmap
@@ -305,7 +305,7 @@ def test_cooperative_rollout_bit_identical_for_two_controls():
     init = rng.uniform(-0.3, 0.3, (T, 2)).astype(np.float32)
     x0 = np.array([6.0, 5.0, 0.4, 4.0], np.float32)
     outs = []
-    for mode in (0, 2, 3):
+    for mode in (0, 2, 3, 4):
         cost = CostmapCost(map_coeff=1.0, speed_target=8.0, speed_coeff=1.0, steer_coeff=0.5, terminal_coeff=2.0,
                            costmap=cmap, resolution=0.1, origin=(0.0, 0.0))
         ctrl = VanillaMPPIController(BicycleDynamics(2.5), cost, None, GaussianDistribution(std_dev=(1.0, 0.3)), 0.02,

@@ -1073,6 +1073,8 @@ private:
     f.inst_tiles_done = inst_tiles_done_d_.p;
     f.first_out = first_d_.p;
     f.finish = 0;
+    f.host_mean = f.host_first = f.host_bn = nullptr;
+    f.host_stats = nullptr;
     return f;
   }
 
@@ -1086,6 +1088,13 @@ private:
       a.tail = 1;
       a.fin = finalize_args();
       a.fin.finish = iter == cp_.num_iters - 1;
+      if (a.fin.finish && direct_out_)
+      {
+        a.fin.host_mean = out_mean_h_.p;
+        a.fin.host_first = first_h_.p;
+        a.fin.host_bn = out_bn_h_.p;
+        a.fin.host_stats = out_stats_h_.p;
+      }
     }
     if (noise_warps_now<NS>())
       rollout_fused_kernel<Model, NS, true><<<rollout_grid_, 2 * NS, fused_dyn_bytes<NS>(true), stream_>>>(a, f);
@@ -1417,8 +1426,14 @@ private:
     const size_t tc = control_.size();
     (void)tc;
     MG_CUDA(cudaMemcpyAsync(io_d_.p, io_in_h_.p, io_in_bytes_, cudaMemcpyHostToDevice, stream_));
-    MG_TRY(enqueue_kernels(stride));
-    MG_CUDA(cudaMemcpyAsync(io_out_h_.p, io_d_.p + io_out_off_, io_out_bytes_, cudaMemcpyDeviceToHost, stream_));
+    // when the fused rollout finishes the solve it writes the results to the pinned host block itself
+    direct_out_ = tail_finalize();
+    const mppi_status st = enqueue_kernels(stride);
+    const bool direct = direct_out_;
+    direct_out_ = false;
+    MG_TRY(st);
+    if (!direct)
+      MG_CUDA(cudaMemcpyAsync(io_out_h_.p, io_d_.p + io_out_off_, io_out_bytes_, cudaMemcpyDeviceToHost, stream_));
     return MPPI_OK;
   }
 
@@ -1563,6 +1578,7 @@ private:
   long long total_u_ = 0;      // control-sample floats over all instances
   bool split_ = false;         // split dynamics / cost rollout (rollout mode 1)
   int rollout_mode_ = 0;       // 0 fused, 1 split, 2 cooperative, 3 sampler kernel + staged, 4 fused + noise warps
+  bool direct_out_ = false;    // enqueue_solve: the finishing rollout CTA writes the results to the host block
   // tile reduction (TileReduce): per tile partial rows, (sum w, sum w^2), minimum; first tile of each instance
   DevBuf<float> tile_part_d_;
   DevBuf<long long> tile_poff_d_;

@@ -202,6 +202,12 @@ struct FinalizeArgs
   unsigned int* inst_tiles_done;  // per instance: finished tiles of this launch (reset by the finalizing CTA)
   float* first_out;               // finish != 0: also smooth and clamp the new mean (finish_instance)
   int finish;
+  // finish != 0 and host_mean != nullptr: the instance's results also go straight to these pinned host arrays
+  // (device-accessible under unified addressing), so no device-to-host copy has to follow the solve
+  float* host_mean;
+  float* host_first;
+  float* host_bn;
+  double* host_stats;
 };
 
 template <class Model>
@@ -996,6 +1002,19 @@ __global__ void __launch_bounds__(kNoiseWarps ? 2 * NS : NS)
         {
           __syncthreads();
           finish_instance<C>(d, w.x, a.fin.mean_out, a.fin.first_out, a.sh, s_u);
+          if (a.fin.host_mean)
+          {
+            __syncthreads();  // the smoothed mean and the first controls are written
+            for (int e = tid; e < d.T * C; e += blockDim.x)
+              a.fin.host_mean[d.t_off + e] = a.fin.mean_out[d.t_off + e];
+            if (tid < C) a.fin.host_first[w.x * C + tid] = a.fin.first_out[w.x * C + tid];
+            if (tid == 0)
+            {
+              a.fin.host_bn[2 * w.x] = a.fin.baseline_norm[2 * w.x];
+              a.fin.host_bn[2 * w.x + 1] = a.fin.baseline_norm[2 * w.x + 1];
+              for (int j = 0; j < 3; ++j) a.fin.host_stats[3 * w.x + j] = a.fin.stats[3 * w.x + j];
+            }
+          }
         }
         __syncthreads();
       }

@@ -183,6 +183,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   const uint32_t sbase = smem_u32(sm);
   const float* b2 = reinterpret_cast<const float*>(sm + MlpSmem::bias_f32(NT));
   const float* b3 = reinterpret_cast<const float*>(sm + MlpSmem::BIAS_B3);
+  constexpr uint32_t kOutCol = 32;  // output-layer accumulator columns (after the packed hidden-2 columns)
   constexpr uint32_t kId64 = kHalf ? umma_idesc_f16_f32(128, 64) : umma_idesc_bf16_f32(128, 64);
   constexpr uint32_t kId16 = kHalf ? umma_idesc_f16_f32(128, 16) : umma_idesc_bf16_f32(128, 16);
 
@@ -223,8 +224,10 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   phase ^= 1u;
   tc_fence_after_sync();
 
-  // ---- hidden layers 1 and 2: tanh epilogue (plus the second bias) into the tile's activation buffer, then the
-  // next GEMM
+  // ---- hidden layers 1 and 2: tanh epilogue (plus the second bias), then the next GEMM.  Hidden 1 goes to the
+  // tile's shared-memory activation buffer (the A operand of layer 2); hidden 2 goes back into TMEM columns 0-31 of
+  // the tile's accumulator, packed two per column (each chunk overwrites columns already read), and is the A operand
+  // of the output layer, whose result lands in columns 32-47: no shared-memory traffic for the output layer.
 #pragma unroll
   for (int layer = 0; layer < 2; ++layer)
   {
@@ -236,6 +239,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
       for (int q = 0; q < 4; ++q)
       {
         float v[16];
+        uint32_t hp[8];  // layer 2: this chunk's eight packed activation columns
         tmem_ld16(taddr + n * MlpSmem::TILE_COLS + lane_base + 16 * q, v);
         tmem_ld_wait();
 #pragma unroll
@@ -283,26 +287,42 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
             c.z = pack_bf16(tanh_fast(x[4] + b1.x), tanh_fast(x[5] + b1.y));
             c.w = pack_bf16(tanh_fast(x[6] + b1.z), tanh_fast(x[7] + b1.w));
           }
-          *reinterpret_cast<uint4*>(act + core_off(m, 16 * q + 8 * h, 64)) = c;
+          if (layer == 0)
+            *reinterpret_cast<uint4*>(act + core_off(m, 16 * q + 8 * h, 64)) = c;
+          else
+          {
+            hp[4 * h] = c.x;
+            hp[4 * h + 1] = c.y;
+            hp[4 * h + 2] = c.z;
+            hp[4 * h + 3] = c.w;
+          }
         }
+        if (layer == 1) tmem_st8(taddr + n * MlpSmem::TILE_COLS + lane_base + 8 * q, hp);
       }
     }
-    fence_proxy_async_smem();
+    if (layer == 0)
+      fence_proxy_async_smem();
+    else
+      tmem_st_wait();
     tc_fence_before_sync();
     __syncthreads();
     if (*fail) return false;  // CTA-uniform: read after the barrier
     if (m == 0)
     {
       tc_fence_after_sync();
-      const uint32_t wb = sbase + (layer == 0 ? MlpSmem::W2 : MlpSmem::W3);
-      const uint32_t id = layer == 0 ? kId64 : kId16;
 #pragma unroll
       for (int n = 0; n < NT; ++n)
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-          umma_f16(taddr + n * MlpSmem::TILE_COLS,
-                    umma_smem_desc(sbase + MlpSmem::ACT + n * MlpSmem::ACT_BYTES + 256 * k, 128, 1024),
-                    umma_smem_desc(wb + 256 * k, 128, 1024), id, k > 0 ? 1u : 0u);
+        {
+          if (layer == 0)
+            umma_f16(taddr + n * MlpSmem::TILE_COLS,
+                     umma_smem_desc(sbase + MlpSmem::ACT + n * MlpSmem::ACT_BYTES + 256 * k, 128, 1024),
+                     umma_smem_desc(sbase + MlpSmem::W2 + 256 * k, 128, 1024), kId64, k > 0 ? 1u : 0u);
+          else
+            umma_f16_ts(taddr + n * MlpSmem::TILE_COLS + kOutCol, taddr + n * MlpSmem::TILE_COLS + 8 * k,
+                        umma_smem_desc(sbase + MlpSmem::W3 + 256 * k, 128, 1024), kId16, k > 0 ? 1u : 0u);
+        }
       umma_commit(mbar);
     }
     if (!mbar_wait_sleep_bounded(mbar, phase, kMaxSleepWaits)) *fail = 1;
@@ -315,7 +335,7 @@ __device__ __forceinline__ bool mlp_tile_forward(unsigned char* sm, uint32_t tad
   for (int n = 0; n < NT; ++n)
   {
     float v[16];
-    tmem_ld16(taddr + n * MlpSmem::TILE_COLS + lane_base, v);
+    tmem_ld16(taddr + n * MlpSmem::TILE_COLS + lane_base + kOutCol, v);
     tmem_ld_wait();
 #pragma unroll
     for (int j = 0; j < kMlpOut; ++j) yout[n][j] = v[j] + b3[j];

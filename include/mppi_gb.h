@@ -236,6 +236,19 @@ mppi_status mppi_get_sample_weights(mppi_handle* h, float* out);
 /* Control samples of the last iteration after the constraints were applied, host float[sum_i K_i*T_i*C].
  * SamplingDistribution::getControlSample (sampling_distribution.cuh:234-236). */
 mppi_status mppi_get_control_samples(mppi_handle* h, float* out);
+/* Sampled-trajectory read-out for visualisation (VanillaMPPIController::calculateSampledStateTrajectories ->
+ * visualizeKernel, mppi_common.cu:371-533; getSampledOutputTrajectories / getSampledCostTrajectories,
+ * controller.cuh:281-289): samples idx[0..n-1] of `instance` from the last mppi_compute_control are re-rolled on the
+ * GPU from their stored, constrained controls.  states[n][T][S] holds the state after each step, step_costs[n][T] the
+ * running cost of each step and terminal[n] the terminal cost; the sample's cost is (the step costs summed in step
+ * order) / T + terminal / T, bit for bit.  The likelihood-ratio term uses the nominal sequence the solve started
+ * from.  Analytic models only (MPPI_EUNSUPPORTED for the surrogate). */
+mppi_status mppi_get_sampled_trajectories(mppi_handle* h, int instance, const int* idx, int n, float* states,
+                                          float* step_costs, float* terminal);
+/* Controller::copyTopControlFromDevice's selection (controller.cu:126-181), on the host: the n highest of
+ * weights[0..num_samples-1] (the transformed costs, mppi_get_sample_weights), by the reference's replacement scan,
+ * in the order of its list slots.  No handle or GPU involved. */
+mppi_status mppi_select_top_samples(const float* weights, int num_samples, int n, int* indices);
 /* Free-energy statistics of instance i (MPPIFreeEnergyStatistics, controller.cuh:22-38; computeFreeEnergy,
  * mppi_common.cu:1101-1117): out[0..5] = mean, variance, modified variance, normaliser percent, increase,
  * previous baseline. */

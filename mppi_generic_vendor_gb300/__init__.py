@@ -8,9 +8,10 @@ from ._abi import MPPIError
 from .controller import (BatchedMPPIController, BicycleDynamics, BicycleSlipDynamics, BicycleSlipMLPDynamics,
                          CartpoleDynamics,
                          CartpoleSwingupCost, ColoredNoiseDistribution, CostmapCost, DoubleIntegratorDynamics,
-                         DoubleIntegratorObstacleCost, GaussianDistribution, VanillaMPPIController)
+                         DoubleIntegratorObstacleCost, GaussianDistribution, VanillaMPPIController,
+                         select_top_samples)
 
 __all__ = ["MPPIError", "BatchedMPPIController", "VanillaMPPIController", "CartpoleDynamics", "CartpoleSwingupCost",
            "DoubleIntegratorDynamics", "DoubleIntegratorObstacleCost", "BicycleDynamics", "BicycleSlipDynamics",
            "BicycleSlipMLPDynamics",
-           "CostmapCost", "GaussianDistribution", "ColoredNoiseDistribution", "_abi"]
+           "CostmapCost", "GaussianDistribution", "ColoredNoiseDistribution", "select_top_samples", "_abi"]

@@ -115,6 +115,8 @@ SIGNATURES = [
     ("mppi_get_sample_costs", C.c_int, [_P, _FP]),
     ("mppi_get_sample_weights", C.c_int, [_P, _FP]),
     ("mppi_get_control_samples", C.c_int, [_P, _FP]),
+    ("mppi_get_sampled_trajectories", C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_int, _FP, _FP, _FP]),
+    ("mppi_select_top_samples", C.c_int, [_FP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     ("mppi_get_free_energy", C.c_int, [_P, C.c_int, _FP]),
     ("mppi_set_dynamics_params", C.c_int, [_P, _P, C.c_size_t]),
     ("mppi_set_cost_params", C.c_int, [_P, _P, C.c_size_t]),

@@ -33,6 +33,15 @@ def _fptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
+def select_top_samples(weights, n):
+    """Controller::copyTopControlFromDevice's selection (controller.cu:126-181): indices of the n highest weights by the
+    reference's replacement scan, in its list order."""
+    w = np.ascontiguousarray(weights, dtype=np.float32)
+    out = np.empty(int(n), dtype=np.int32)
+    A.call("mppi_select_top_samples", _fptr(w), int(w.size), int(n), out.ctypes.data_as(C.POINTER(C.c_int)))
+    return out
+
+
 # ------------------------------------------------------------------------------------------------------ plugins
 class _Plugin:
     model_id: int = 0
@@ -351,6 +360,56 @@ class BatchedMPPIController:
         out = np.empty(n, dtype=np.float32)
         A.call("mppi_get_control_samples", self._h, _fptr(out))
         return out
+
+    # ---- sampled trajectories for visualisation (Controller::setPercentageSampledControlTrajectoriesHelper,
+    #      setTopNSampledControlTrajectoriesHelper, controller.cuh:754-767; calculateSampledStateTrajectories,
+    #      getSampledOutputTrajectories, getSampledCostTrajectories, getTopTransformedCosts, controller.cuh:234-314)
+    def setPercentageSampledControlTrajectories(self, perc):
+        self._vis_perc = float(perc)
+
+    def setTopNSampledControlTrajectories(self, n):
+        self._vis_top = int(n)
+
+    def calculateSampledStateTrajectories(self, instance=0, seed=0):
+        """Re-roll on the GPU a random share of the last solve's samples (drawn without replacement from the first
+        98%, copySampledControlFromDevice, controller.cu:57-105) followed by the top-N by weight
+        (copyTopControlFromDevice's selection, controller.cu:126-181)."""
+        i = int(instance)
+        K, T = int(self.K[i]), int(self.T[i])
+        perc, top_n = getattr(self, "_vis_perc", 0.0), getattr(self, "_vis_top", 0)
+        n_rand = int(perc * K)
+        if perc > 0.98:
+            rand = np.arange(n_rand, dtype=np.int32)
+        else:
+            rand = np.random.default_rng(seed).choice(int(K * 0.98), n_rand, replace=False).astype(np.int32)
+        w = self.sample_weights()[int(self._k_off[i]):int(self._k_off[i + 1])].copy()
+        top = select_top_samples(w, top_n) if top_n > 0 else np.empty(0, np.int32)
+        idx = np.ascontiguousarray(np.concatenate([rand, top]).astype(np.int32))
+        n = idx.size
+        states = np.empty(max(n, 1) * T * self.S, np.float32)
+        step_costs = np.empty(max(n, 1) * T, np.float32)
+        terminal = np.empty(max(n, 1), np.float32)
+        if n:
+            A.call("mppi_get_sampled_trajectories", self._h, i, idx.ctypes.data_as(C.POINTER(C.c_int)), n,
+                   _fptr(states), _fptr(step_costs), _fptr(terminal))
+        self.sampled_indices_ = idx
+        self.sampled_trajectories_ = [states[j * T * self.S:(j + 1) * T * self.S].reshape(T, self.S).T.copy()
+                                      for j in range(n)]
+        self.sampled_costs_ = [step_costs[j * T:(j + 1) * T].copy() for j in range(n)]
+        self.sampled_terminal_costs_ = terminal[:n].copy()
+        self.top_n_costs_ = w[top] / self.getNormalizerCost(i) if top_n > 0 else np.empty(0, np.float32)
+
+    def getSampledOutputTrajectories(self):
+        """(S, T) state trajectory of each re-rolled sample (the outputs equal the states for these models)."""
+        return getattr(self, "sampled_trajectories_", [])
+
+    def getSampledCostTrajectories(self):
+        """Running cost of every step of each re-rolled sample."""
+        return getattr(self, "sampled_costs_", [])
+
+    def getTopTransformedCosts(self):
+        """Weights of the top-N samples divided by the normaliser."""
+        return getattr(self, "top_n_costs_", np.empty(0, np.float32))
 
     def getFreeEnergyStatistics(self, ind=0):
         out = np.empty(6, dtype=np.float32)

@@ -357,6 +357,41 @@ mppi_status mppi_get_control_samples(mppi_handle* h, float* out)
   HANDLE_OK(h);
   return h->engine->get_control_samples(out);
 }
+mppi_status mppi_get_sampled_trajectories(mppi_handle* h, int instance, const int* idx, int n, float* states,
+                                          float* step_costs, float* terminal)
+{
+  HANDLE_OK(h);
+  return h->engine->get_sampled_trajectories(instance, idx, n, states, step_costs, terminal);
+}
+mppi_status mppi_select_top_samples(const float* weights, int num_samples, int n, int* indices)
+{
+  clear_error();
+  MG_CHECK(weights && indices, "pointers must not be NULL");
+  MG_CHECK(num_samples >= 1 && n >= 1 && n <= num_samples, "need 1 <= n <= num_samples");
+  // Controller::copyTopControlFromDevice (controller.cu:126-181): start from the first n samples, then every later
+  // weight strictly above the current minimum of the list replaces that minimum (first minimum in list order)
+  for (int s = 0; s < n; ++s) indices[s] = s;
+  int mi = 0;
+  float mv = weights[indices[0]];
+  auto find_min = [&]() {
+    mi = 0;
+    mv = weights[indices[0]];
+    for (int s = 1; s < n; ++s)
+      if (weights[indices[s]] < mv)
+      {
+        mv = weights[indices[s]];
+        mi = s;
+      }
+  };
+  find_min();
+  for (int k = n; k < num_samples; ++k)
+    if (weights[k] > mv)
+    {
+      indices[mi] = k;
+      find_min();
+    }
+  return MPPI_OK;
+}
 mppi_status mppi_get_free_energy(mppi_handle* h, int instance, float* out6)
 {
   HANDLE_OK(h);

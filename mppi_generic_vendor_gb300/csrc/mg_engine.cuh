@@ -60,6 +60,8 @@ public:
   virtual mppi_status get_sample_costs(float* out) = 0;
   virtual mppi_status get_sample_weights(float* out) = 0;
   virtual mppi_status get_control_samples(float* out) = 0;
+  virtual mppi_status get_sampled_trajectories(int i, const int* idx, int n, float* states, float* step_costs,
+                                               float* terminal) = 0;
   virtual mppi_status get_free_energy(int i, float* out6) = 0;
   virtual mppi_status set_dynamics_params(const void* p, size_t bytes) = 0;
   virtual mppi_status set_cost_params(const void* p, size_t bytes) = 0;
@@ -335,6 +337,48 @@ public:
       o += n;
     }
     return MPPI_OK;
+  }
+  // VanillaMPPIController::calculateSampledStateTrajectories (visualizeKernel, mppi_common.cu:371-533): samples idx
+  // of instance i of the last solve, re-rolled on the GPU.  The likelihood-ratio term uses the nominal sequence the
+  // solve started from (the samples' own nominal when num_iters is 1).
+  mppi_status get_sampled_trajectories(int i, const int* idx, int n, float* states, float* step_costs,
+                                       float* terminal) override
+  {
+    MG_CHECK(i >= 0 && i < I_, "instance %d out of range", i);
+    MG_CHECK(n >= 0, "n must be >= 0");
+    if (n == 0) return MPPI_OK;
+    MG_CHECK(idx && states && step_costs && terminal, "pointers must not be NULL");
+    for (int j = 0; j < n; ++j)
+      MG_CHECK(idx[j] >= 0 && idx[j] < K_[i], "sample index %d (entry %d) is out of range", idx[j], j);
+    if constexpr (Model::kMlp)
+    {
+      set_error("sampled trajectories are re-rolled with an analytic model; the surrogate model has none here");
+      return MPPI_EUNSUPPORTED;
+    }
+    else
+    {
+      const int T = T_[i];
+      DevBuf<int> idx_d;
+      DevBuf<float> st_d, c_d, term_d, mean0_d;
+      MG_TRY(idx_d.alloc(n));
+      MG_TRY(st_d.alloc((size_t)n * T * S));
+      MG_TRY(c_d.alloc((size_t)n * T));
+      MG_TRY(term_d.alloc(n));
+      MG_TRY(mean0_d.alloc(control_.size()));
+      MG_CUDA(cudaStreamSynchronize(stream_));
+      MG_CUDA(cudaMemcpy(idx_d.p, idx, sizeof(int) * n, cudaMemcpyHostToDevice));
+      MG_CUDA(cudaMemcpy(mean0_d.p, mean_h_.p, sizeof(float) * control_.size(), cudaMemcpyHostToDevice));
+      RolloutArgs<Model> a = base_rollout_args();
+      a.mean = mean0_d.p;
+      sampled_trajectories_kernel<Model><<<(n + 127) / 128, 128, 0, stream_>>>(a, i, idx_d.p, n, st_d.p, c_d.p,
+                                                                                 term_d.p);
+      MG_CUDA(cudaGetLastError());
+      MG_CUDA(cudaStreamSynchronize(stream_));
+      MG_CUDA(cudaMemcpy(states, st_d.p, sizeof(float) * n * T * S, cudaMemcpyDeviceToHost));
+      MG_CUDA(cudaMemcpy(step_costs, c_d.p, sizeof(float) * n * T, cudaMemcpyDeviceToHost));
+      MG_CUDA(cudaMemcpy(terminal, term_d.p, sizeof(float) * n, cudaMemcpyDeviceToHost));
+      return MPPI_OK;
+    }
   }
   // computeFreeEnergy (mppi_common.cu:1101-1117) from the device sums of w and w^2.
   mppi_status get_free_energy(int i, float* out6) override
@@ -1242,7 +1286,8 @@ private:
     return MPPI_OK;
   }
 
-  mppi_status launch_rollout(int stride, int iter)
+  // The rollout arguments every rollout kernel shares.
+  RolloutArgs<Model> base_rollout_args() const
   {
     RolloutArgs<Model> a{};
     a.inst = inst_d_.p;
@@ -1266,6 +1311,12 @@ private:
       if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
     a.max_t = max_t_;
     a.sh = make_sample_shared(sp_, cc_);
+    return a;
+  }
+
+  mppi_status launch_rollout(int stride, int iter)
+  {
+    RolloutArgs<Model> a = base_rollout_args();
     if (tile_reduce_active())
     {
       a.tr.partials = tile_part_d_.p;

@@ -785,6 +785,42 @@ __device__ __forceinline__ float4 fused_noise(const FusedNoise& f, const InstDes
                     : philox_normal4((uint64_t)q, (uint32_t)inst, counter, f.seed_lo, f.seed_hi);
 }
 
+// Re-roll of chosen samples for visualisation (VanillaMPPIController::calculateSampledStateTrajectories ->
+// visualizeKernel, mppi_common.cu:371-533): one thread per chosen sample of one instance runs the sample's stored,
+// constrained controls through the dynamics again and records the stepped state and the running cost of every step,
+// in the rollout's arithmetic, so the sample's cost is (the step costs summed in step order) / T + terminal / T.
+template <class Model>
+__global__ void __launch_bounds__(128) sampled_trajectories_kernel(const __grid_constant__ RolloutArgs<Model> a,
+                                                                   int inst, const int* idx, int n, float* states,
+                                                                   float* step_costs, float* terminal)
+{
+  constexpr int S = Model::STATE_DIM;
+  constexpr int C = Model::CONTROL_DIM;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const InstDesc d = a.inst[inst];
+  const int k = idx[j];
+  const typename Model::DynParams dp = a.dyn[inst];
+  const typename Model::CostParams cp = a.cost[inst];
+  float x[S];
+#pragma unroll
+  for (int i = 0; i < S; ++i) x[i] = a.x0[d.x_off + i];
+  const float* us = a.samples + d.u_off + (long long)k * d.T * C;
+  float* ys = states + (long long)j * d.T * S;
+  for (int t = 0; t < d.T; ++t)
+  {
+    float u[C], xn[S];
+#pragma unroll
+    for (int c = 0; c < C; ++c) u[c] = us[t * C + c];
+    euler_step<Model>(dp, x, u, xn, a.dt);
+#pragma unroll
+    for (int i = 0; i < S; ++i) ys[(long long)t * S + i] = x[i] = xn[i];
+    step_costs[(long long)j * d.T + t] =
+        a.use_likelihood ? step_cost<Model, true>(a, d, cp, k, u, t, x) : step_cost<Model, false>(a, d, cp, k, u, t, x);
+  }
+  terminal[j] = Model::terminalCost(cp, a.aux, x);
+}
+
 // Polls of a noise warp's progress word before a rollout warp gives up (each poll is one shared-memory read).
 constexpr uint32_t kMaxProgressPolls = 1u << 22;
 // Quads a noise warp publishes at a time.

@@ -106,3 +106,48 @@ def test_cpp_mirror_header_compiles():
     root = Path(__file__).resolve().parents[1]
     subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
                     str(root / "tests" / "cpp" / "cartpole_mirror.cpp"), "-I", str(root / "include")], check=True)
+
+
+def _reference_top_scan(w, n):
+    """controller.cu:126-181 restated: first n indices, then every later weight strictly above the list's current
+    minimum (first minimum in list order) replaces it."""
+    idx = list(range(n))
+
+    def find_min():
+        mi, mv = 0, w[idx[0]]
+        for s in range(1, n):
+            if w[idx[s]] < mv:
+                mi, mv = s, w[idx[s]]
+        return mi, mv
+
+    mi, mv = find_min()
+    for k in range(n, len(w)):
+        if w[k] > mv:
+            idx[mi] = k
+            mi, mv = find_min()
+    return idx
+
+
+@pytest.mark.parametrize("K,n,ties", [(1, 1, False), (50, 5, False), (1000, 17, False), (300, 10, True),
+                                      (64, 64, False)])
+def test_select_top_samples_matches_reference_scan(K, n, ties):
+    """mppi_select_top_samples (host only) picks the same indices, in the same slot order, as the reference's scan,
+    and they are the n largest weights."""
+    from mppi_generic_vendor_gb300 import select_top_samples
+
+    rng = np.random.default_rng(K + n)
+    w = rng.exponential(1.0, K).astype(np.float32)
+    if ties:
+        w = np.round(w * 4.0).astype(np.float32) / 4.0  # many equal weights
+    got = select_top_samples(w, n)
+    assert got.tolist() == _reference_top_scan(w.tolist(), n)
+    assert np.array_equal(np.sort(w[got]), np.sort(w)[-n:])
+
+
+def test_select_top_samples_rejects_bad_arguments():
+    from mppi_generic_vendor_gb300 import select_top_samples
+
+    with pytest.raises(A.MPPIError):
+        select_top_samples(np.ones(4, np.float32), 5)
+    with pytest.raises(A.MPPIError):
+        select_top_samples(np.ones(4, np.float32), 0)

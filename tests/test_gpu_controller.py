@@ -362,3 +362,58 @@ def test_engines_with_different_horizons_coexist():
     assert np.all(np.isfinite(long_h.getControlSeq()))
     long_h.close()
     short_h.close()
+
+
+@pytest.mark.parametrize("lik", [False, True])
+def test_sampled_trajectories_match_oracle(lik):
+    """calculateSampledStateTrajectories (visualizeKernel's read-out): a random 1% of the samples plus the top five by
+    weight are re-rolled on the GPU; their states equal the oracle's FP32 trajectories of the same constrained
+    controls bit for bit, the top five are the five largest weights, and (step costs summed in step order) / T +
+    terminal / T reproduces each sample's cost from the solve bit for bit (with and without the likelihood term)."""
+    K, T = 1024, 60
+    dyn = CartpoleDynamics(1.0, 1.0, 1.0)
+    dyn.setControlRanges([(-5.0, 5.0)])
+    sampler = GaussianDistribution(std_dev=(1.0,), control_cost_coeff=(1.0,) if lik else (0.0,))
+    ctrl = VanillaMPPIController(dyn, CartpoleSwingupCost(10.0, 1.0, 100.0, 1.0, 0.0), None, sampler, 0.02, 1, 1.0,
+                                 0.0, T, K, seed=3)
+    x0 = np.array([0.1, 0.0, 2.5, 0.0], np.float32)
+    init = np.random.default_rng(9).uniform(-1.0, 1.0, (T, 1)).astype(np.float32)
+    ctrl.setControlSeq(init.T)
+    ctrl.computeControl(x0, 1)
+    ctrl.setPercentageSampledControlTrajectories(0.01)
+    ctrl.setTopNSampledControlTrajectories(5)
+    ctrl.calculateSampledStateTrajectories(seed=4)
+    idx = ctrl.sampled_indices_
+    assert idx.size == int(0.01 * K) + 5
+    w = ctrl.sample_weights()
+    assert np.array_equal(np.sort(w[idx[-5:]]), np.sort(w)[-5:])
+    top = ctrl.getTopTransformedCosts()
+    assert np.allclose(top, w[idx[-5:]] / ctrl.getNormalizerCost(), rtol=0, atol=0)
+    samples = ctrl.control_samples().reshape(K, T, 1)
+    _, _, traj = oracle.rollout(A.MODEL_CARTPOLE, ctrl._dyn_arr[0], ctrl._cost_arr[0], x0,
+                                np.ascontiguousarray(samples[idx]), init, sampler.to_c(), ctrl.constraints_, 1.0, 0.0,
+                                idx.size, T, 0.02, want_traj=True)
+    got = np.stack([s.T for s in ctrl.getSampledOutputTrajectories()])  # [n][T][S]
+    assert np.array_equal(got, traj.reshape(idx.size, T, 4).astype(np.float32))
+    costs = ctrl.sample_costs()
+    for j, k in enumerate(idx):
+        running = np.float32(0.0)
+        for c in ctrl.getSampledCostTrajectories()[j]:
+            running = np.float32(running + c)
+        cost = np.float32(running / np.float32(T)) + np.float32(ctrl.sampled_terminal_costs_[j] / np.float32(T))
+        assert np.float32(cost).view(np.uint32) == costs[k].view(np.uint32), (j, k, cost, costs[k])
+    ctrl.close()
+
+
+def test_sampled_trajectories_reject_bad_indices():
+    dyn = CartpoleDynamics(1.0, 1.0, 1.0)
+    ctrl = VanillaMPPIController(dyn, CartpoleSwingupCost(), None, GaussianDistribution(std_dev=(1.0,)), 0.02, 1, 1.0,
+                                 0.0, 20, 256)
+    ctrl.computeControl(np.zeros(4, np.float32), 1)
+    bad = np.array([0, 256], np.int32)
+    out = np.empty(2 * 20 * 4, np.float32)
+    with pytest.raises(MPPIError):
+        A.call("mppi_get_sampled_trajectories", ctrl._h, 0, bad.ctypes.data_as(C.POINTER(C.c_int)), 2,
+               out.ctypes.data_as(C.POINTER(C.c_float)), out.ctypes.data_as(C.POINTER(C.c_float)),
+               out.ctypes.data_as(C.POINTER(C.c_float)))
+    ctrl.close()

@@ -322,6 +322,53 @@ public:
   int getNumTimesteps() const { return T_; }
   mppi_handle* handle() const { return h_; }
 
+  // Sampled trajectories for visualisation (Controller::setTopNSampledControlTrajectoriesHelper, controller.cuh:762;
+  // calculateSampledStateTrajectories, mppi_controller.cu:280-284; getSampledOutputTrajectories /
+  // getSampledCostTrajectories / getTopTransformedCosts, controller.cuh:281-314).  The top-N samples by weight of
+  // the last computeControl are re-rolled on the GPU; extra sample indices (a random share, as
+  // copySampledControlFromDevice draws them) can be passed in front of them.
+  void setTopNSampledControlTrajectories(int n) { top_n_ = n; }
+  void calculateSampledStateTrajectories(const std::vector<int>& extra_samples = {})
+  {
+    std::vector<int> idx(extra_samples);
+    sampled_cost_traj w;
+    if (top_n_ > 0)
+    {
+      w = getSampledCostSeq();
+      std::vector<int> top(top_n_);
+      check(mppi_select_top_samples(w.data(), NUM_ROLLOUTS, top_n_, top.data()), "mppi_select_top_samples");
+      idx.insert(idx.end(), top.begin(), top.end());
+    }
+    const int n = (int)idx.size();
+    sampled_states_.assign((size_t)n * T_ * S, 0.0f);
+    sampled_costs_.assign((size_t)n * T_, 0.0f);
+    sampled_terminal_.assign((size_t)n, 0.0f);
+    if (n > 0)
+      check(mppi_get_sampled_trajectories(h_, 0, idx.data(), n, sampled_states_.data(), sampled_costs_.data(),
+                                          sampled_terminal_.data()),
+            "mppi_get_sampled_trajectories");
+    top_costs_.clear();
+    const float norm = top_n_ > 0 ? getNormalizerCost() : 1.0f;
+    for (int j = n - top_n_; j < n && top_n_ > 0; ++j) top_costs_.push_back(w[idx[j]] / norm);
+    sampled_idx_ = idx;
+  }
+  // Per re-rolled sample: states [t][s] (the outputs equal the states for these models) and step costs [t].
+  std::vector<std::vector<float>> getSampledOutputTrajectories() const
+  {
+    std::vector<std::vector<float>> out;
+    for (size_t j = 0; j < sampled_idx_.size(); ++j)
+      out.emplace_back(sampled_states_.begin() + j * T_ * S, sampled_states_.begin() + (j + 1) * T_ * S);
+    return out;
+  }
+  std::vector<std::vector<float>> getSampledCostTrajectories() const
+  {
+    std::vector<std::vector<float>> out;
+    for (size_t j = 0; j < sampled_idx_.size(); ++j)
+      out.emplace_back(sampled_costs_.begin() + j * T_, sampled_costs_.begin() + (j + 1) * T_);
+    return out;
+  }
+  std::vector<float> getTopTransformedCosts() const { return top_costs_; }
+
 private:
   float baseline_normalizer(int which) const
   {
@@ -348,6 +395,9 @@ private:
   mppi_handle* h_ = nullptr;
   int T_ = MAX_TIMESTEPS;
   mppi_controller_params params_{};
+  int top_n_ = 0;
+  std::vector<int> sampled_idx_;
+  std::vector<float> sampled_states_, sampled_costs_, sampled_terminal_, top_costs_;
 };
 
 }  // namespace mppi_gb

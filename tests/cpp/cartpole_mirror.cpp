@@ -40,6 +40,14 @@ int main()
   }
   std::printf("cart-pole: upright for %d of 500 steps, last baseline %.4f, normaliser %.4f\n", upright,
               controller.getBaselineCost(), controller.getNormalizerCost());
+  // visualisation read-out: the five highest-weight samples of the last solve, re-rolled on the GPU
+  controller.setTopNSampledControlTrajectories(5);
+  controller.calculateSampledStateTrajectories({ 0, 1 });
+  const auto vis = controller.getSampledOutputTrajectories();
+  const auto top = controller.getTopTransformedCosts();
+  bool vis_ok = vis.size() == 7 && top.size() == 5 && vis[0].size() == (size_t)4 * T;
+  for (float v : top) vis_ok = vis_ok && v > 0.0f && v <= 1.0f;
+  std::printf("sampled trajectories: %zu, top weights ok %d\n", vis.size(), (int)vis_ok);
 
   BicycleDynamics bike(2.5f);
   CostmapCost map_cost;
@@ -64,5 +72,5 @@ int main()
     threw = e.status == MPPI_EINVAL;
   }
   std::printf("bicycle: finite controls %d, bad argument reported %d\n", (int)finite, (int)threw);
-  return upright > 100 && finite && threw ? 0 : 1;
+  return upright > 100 && finite && threw && vis_ok ? 0 : 1;
 }

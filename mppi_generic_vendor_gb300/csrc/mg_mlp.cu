@@ -1,6 +1,7 @@
 // mg_mlp.cu — tensor-core evaluation of the surrogate MLP: a standalone forward entry point and the rollout kernel of
 // the MLP bicycle model (the per-timestep inference over all samples is one tcgen05 GEMM chain per 128-sample tile,
-// BF16 operands for BF16 weights and FP16 operands for FP8 weights, FP32 accumulation in TMEM; see mg_mlp.cuh).  The rollout's work items hold kMlpTiles tiles of one instance.
+// BF16 operands for BF16 weights and FP16 operands for FP8 weights, FP32 accumulation in TMEM; see mg_mlp.cuh).  The
+// rollout's work items hold kMlpTiles tiles of one instance.
 #include <algorithm>
 #include <cmath>
 #include <vector>

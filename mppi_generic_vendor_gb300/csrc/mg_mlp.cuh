@@ -34,7 +34,7 @@ constexpr int kMlpScale = kMlpNumParams, kMlpDevParams = kMlpScale + 3;
 
 // Tiles of 128 samples per CTA of the surrogate rollout; its work items hold kMlpSamplesPerCta samples of one
 // instance.  One tile per CTA measured fastest: two tiles per CTA halve the MMA round trips per tile but double the
-// epilogue work between barriers and cut the resident CTAs per SM from 7 to 4, which cost more than they saved.
+// epilogue work between barriers and halve the resident CTAs per SM, which cost more than they saved.
 constexpr int kMlpTiles = 1;
 constexpr int kMlpSamplesPerCta = 128 * kMlpTiles;
 

@@ -151,3 +151,25 @@ def test_select_top_samples_rejects_bad_arguments():
         select_top_samples(np.ones(4, np.float32), 5)
     with pytest.raises(A.MPPIError):
         select_top_samples(np.ones(4, np.float32), 0)
+
+
+def test_fp8_quantisation_host_only():
+    """mppi_mlp_quantize runs on the host: E4M3 weights with one power-of-two scale per layer (the smallest with
+    max |W| / scale <= 448), so q * scale is exact in FP16 and FP32; BF16 keeps the weights and scale 1."""
+    rng = np.random.default_rng(3)
+    p = np.zeros(A.MLP_PARAMS, np.float32)
+    p[:A.MLP_WEIGHTS] = rng.normal(0.0, 0.3, A.MLP_WEIGHTS).astype(np.float32)
+    p[A.MLP_WEIGHTS + 9:A.MLP_WEIGHTS + 18] = 1.0  # input scales
+    q = np.empty(A.MLP_PARAMS, np.float32)
+    sc = np.empty(3, np.float32)
+    fp = C.POINTER(C.c_float)
+    A.call("mppi_mlp_quantize", p.ctypes.data_as(fp), 1, q.ctypes.data_as(fp), sc.ctypes.data_as(fp))
+    for l, (lo, hi) in enumerate([(0, 576), (640, 4736), (4800, 5120)]):
+        m, e = np.frexp(sc[l])
+        assert m == 0.5
+        assert np.abs(p[lo:hi]).max() / sc[l] <= 448.0 < 2.0 * np.abs(p[lo:hi]).max() / sc[l]
+        w = q[lo:hi] * sc[l]
+        assert np.array_equal(w.astype(np.float16).astype(np.float32), w)
+        assert np.abs(w - p[lo:hi]).max() <= 2.0 ** -4 * np.abs(p[lo:hi]).max()
+    A.call("mppi_mlp_quantize", p.ctypes.data_as(fp), 0, q.ctypes.data_as(fp), sc.ctypes.data_as(fp))
+    assert np.array_equal(q, p) and np.array_equal(sc, np.ones(3, np.float32))

@@ -254,7 +254,8 @@ mppi_status mppi_select_top_samples(const float* weights, int num_samples, int n
  * previous baseline. */
 mppi_status mppi_get_free_energy(mppi_handle* h, int instance, float* out6);
 
-/* Replace the model parameters of every instance (Dynamics::setParams / Cost::setParams). */
+/* Replace the model parameters (Dynamics::setParams / Cost::setParams): one block of the model's parameter struct
+ * for every instance (bytes = sizeof the struct), or one block per instance (bytes = instances * sizeof). */
 mppi_status mppi_set_dynamics_params(mppi_handle* h, const void* dyn_params, size_t dyn_bytes);
 mppi_status mppi_set_cost_params(mppi_handle* h, const void* cost_params, size_t cost_bytes);
 /* Replace the sampling parameters (Controller::setSamplingParams, controller.cuh:852). */

@@ -431,6 +431,28 @@ class BatchedMPPIController:
         A.call("mppi_set_sampling_params", self._h, C.byref(sp))
         self.sampler_ = sampler
 
+    def updateDynamicsParams(self, model):
+        """Dynamics::setParams of every instance (the plugin's current parameters)."""
+        p = model.getParams()
+        arr = (type(p) * self.num_instances)(*([p] * self.num_instances))
+        A.call("mppi_set_dynamics_params", self._h, C.cast(arr, C.c_void_p), C.sizeof(arr))
+        self._dyn_arr = arr
+
+    def updateCostParams(self, cost):
+        """Cost::setParams of every instance (the plugin's current parameters)."""
+        p = cost.getParams()
+        arr = (type(p) * self.num_instances)(*([p] * self.num_instances))
+        A.call("mppi_set_cost_params", self._h, C.cast(arr, C.c_void_p), C.sizeof(arr))
+        self._cost_arr = arr
+
+    def getDt(self) -> float:
+        """Controller::getDt."""
+        return float(self.params_.dt)
+
+    def getNumTimesteps(self) -> int:
+        """Controller::getNumTimesteps (the longest horizon of the handle)."""
+        return int(self.T.max())
+
     def setCostmap(self, costmap, resolution=0.1, origin=(0.0, 0.0)):
         m = np.ascontiguousarray(costmap, dtype=np.float32)
         A.call("mppi_set_costmap", self._h, _fptr(m), int(m.shape[1]), int(m.shape[0]), float(resolution),

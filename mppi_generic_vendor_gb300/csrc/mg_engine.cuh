@@ -402,21 +402,28 @@ public:
     return MPPI_OK;
   }
 
-  mppi_status set_dynamics_params(const void* p, size_t bytes) override
+  // One parameter block for every instance, or one block per instance (bytes = I * block).
+  template <class P>
+  mppi_status replace_params(std::vector<P>& host, P* dev, const void* p, size_t bytes, const char* what)
   {
-    MG_CHECK(p && bytes == sizeof(DynParams), "dynamics parameter block must be %zu bytes", sizeof(DynParams));
-    memcpy(dyn_.data(), p, sizeof(DynParams) * I_);
-    MG_CUDA(cudaMemcpyAsync(dyn_d_.p, dyn_.data(), sizeof(DynParams) * I_, cudaMemcpyHostToDevice, stream_));
+    MG_CHECK(p && (bytes == sizeof(P) || bytes == sizeof(P) * I_),
+             "%s parameters must be one %zu-byte block (all instances) or %d of them (one per instance)", what,
+             sizeof(P), I_);
+    if (bytes == sizeof(P))
+      for (int i = 0; i < I_; ++i) memcpy(&host[i], p, sizeof(P));
+    else
+      memcpy(host.data(), p, sizeof(P) * I_);
+    MG_CUDA(cudaMemcpyAsync(dev, host.data(), sizeof(P) * I_, cudaMemcpyHostToDevice, stream_));
     MG_CUDA(cudaStreamSynchronize(stream_));
     return MPPI_OK;
   }
+  mppi_status set_dynamics_params(const void* p, size_t bytes) override
+  {
+    return replace_params(dyn_, dyn_d_.p, p, bytes, "dynamics");
+  }
   mppi_status set_cost_params(const void* p, size_t bytes) override
   {
-    MG_CHECK(p && bytes == sizeof(CostParams), "cost parameter block must be %zu bytes", sizeof(CostParams));
-    memcpy(cost_.data(), p, sizeof(CostParams) * I_);
-    MG_CUDA(cudaMemcpyAsync(cost_d_.p, cost_.data(), sizeof(CostParams) * I_, cudaMemcpyHostToDevice, stream_));
-    MG_CUDA(cudaStreamSynchronize(stream_));
-    return MPPI_OK;
+    return replace_params(cost_, cost_d_.p, p, bytes, "cost");
   }
   mppi_status set_sampling_params(const mppi_sampling_params* sp) override
   {

@@ -34,6 +34,7 @@ _SIGS = [
                               _P, _P, C.c_float, C.c_float, C.c_int, C.c_int, C.c_float, _DP, _DP, C.c_int,
                               C.c_int]),
     ("orc_weights", None, [_FP, C.c_int, C.c_float, _FP, _FP, _DP]),
+    ("orc_tsallis", None, [_FP, C.c_int, C.c_float, C.c_float, C.c_float, _FP]),
     ("orc_weighted_mean", None, [_FP, C.c_float, _FP, C.c_int, C.c_int, C.c_int, _DP, _DP]),
     ("orc_smooth", None, [_FP, C.c_int, C.c_int]),
     ("orc_slide", None, [_FP, C.c_int, C.c_int, C.c_int, _FP, _FP]),
@@ -161,6 +162,15 @@ def weights(costs, lambda_=None, lambda_inv=None):
     linv = np.float32(lambda_inv) if lambda_inv is not None else np.float32(1.0) / np.float32(lambda_)
     lib().orc_weights(_fp(c), c.size, float(linv), _fp(w), C.byref(b), C.byref(n))
     return w, b.value, n.value
+
+
+def tsallis(costs, gamma, r, baseline):
+    """TsallisTransform (mppi_common.cu:1004-1021): weights (1 - d / gamma)^(1 / (r - 1)) for d = c - baseline <
+    gamma, else 0."""
+    c = _f32(costs)
+    w = np.empty_like(c)
+    lib().orc_tsallis(_fp(c), c.size, float(gamma), float(r), float(baseline), _fp(w))
+    return w
 
 
 def weighted_mean(w, normalizer, controls, K, T, Cdim):

@@ -572,6 +572,18 @@ static void weights(const float* costs, int K, float lambda_inv, float* w, float
   *normalizer = sum;
 }
 
+// TsallisTransform (mppi_common.cu:1004-1021), ColoredMPPI's alternative to the exponential: with d = c - baseline,
+// w = exp(log(1 - d / gamma) / (r - 1)) for d < gamma, else 0.  The reference forms 1 - d / gamma with a double 1.0
+// (the float quotient promoted), so the log's argument is that double narrowed back to float; kept here.
+static void tsallis(const float* costs, int K, float gamma, float r, float baseline, float* w)
+{
+  for (int k = 0; k < K; ++k)
+  {
+    const float d = costs[k] - baseline;
+    w[k] = d < gamma ? expf(logf((float)(1.0 - (double)(d / gamma))) / (r - 1.0f)) : 0.0f;
+  }
+}
+
 // strideControlWeightReduction + rolloutWeightReductionAndSaveControl (mppi_common.cu:1151-1196):
 // u_new[t][c] = sum_k (w_k / eta) * u_k[t][c].  Accumulated in double here (exact-ish reference value).
 static void weighted_mean(const float* w, float normalizer, const float* controls, int K, int T, int C, double* out,
@@ -875,6 +887,11 @@ int orc_rollout(int model, const void* dyn, const void* cost, const float* map, 
 void orc_weights(const float* costs, int K, float lambda_inv, float* w, float* baseline, double* normalizer)
 {
   orc::weights(costs, K, lambda_inv, w, baseline, normalizer);
+}
+
+void orc_tsallis(const float* costs, int K, float gamma, float r, float baseline, float* w)
+{
+  orc::tsallis(costs, K, gamma, r, baseline, w);
 }
 
 void orc_weighted_mean(const float* w, float normalizer, const float* controls, int K, int T, int C, double* out,

@@ -127,3 +127,28 @@ def test_colored_scales_follow_fftfreq_cutoff():
     w = ref[1:].copy()
     w[-1] *= 0.5
     assert math.isclose(sigma[0], 2 * np.sqrt(np.sum(w ** 2)) / 8, rel_tol=1e-6)
+
+
+@pytest.mark.parametrize("gamma,r", [(5.0, 2.0), (20.0, 1.5), (2.5, 3.0)])
+def test_tsallis_transform_restatement(gamma, r):
+    """The oracle's TsallisTransform (mppi_common.cu:1004-1021) against a NumPy restatement of the same float
+    arithmetic (1 - d / gamma formed in double, narrowed to float before the log): libm and NumPy round log / exp
+    differently in the last place, and the exponent |log(1 - d / gamma)| / (r - 1) scales that, so the bound is a few
+    ulps times that exponent; exactly 1 at the baseline, exactly 0 from d >= gamma on, non-increasing in the cost."""
+    rng = np.random.default_rng(int(gamma * 10 + r))
+    c = (100.0 + rng.exponential(gamma / 2, 4096)).astype(np.float32)
+    b = np.float32(c.min())
+    w = oracle.tsallis(c, gamma, r, b)
+    d = (c - b).astype(np.float32)
+    q = (d / np.float32(gamma)).astype(np.float32)
+    arg = (1.0 - q.astype(np.float64)).astype(np.float32)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ref = np.where(d < np.float32(gamma),
+                       np.exp(np.log(arg) / np.float32(np.float32(r) - np.float32(1.0))), 0.0).astype(np.float32)
+    expo = np.abs(np.log(np.maximum(arg, np.float32(1e-30)).astype(np.float64))) / (r - 1.0)
+    tol = 4.0 * 2.0 ** -23 * (1.0 + expo) * ref + 1e-30
+    assert np.all(np.abs(w.astype(np.float64) - ref) <= tol)
+    assert w[np.argmin(c)] == 1.0
+    assert np.all(w[d >= np.float32(gamma)] == 0.0) and np.any(d >= np.float32(gamma))
+    order = np.argsort(c, kind="stable")
+    assert np.all(np.diff(w[order]) <= 0.0)

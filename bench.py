@@ -301,11 +301,11 @@ def cpu_baseline(name, seed, budget_s):
     if name in ("batched_di", "batched_di_gaussian"):
         colored = name == "batched_di"
         Ks, Ts, costs, x0 = W.batched_di_params(seed)
-        cp = A.default_controller_params()
+        cp = A.default_controller_params(native=False)
         cp.dt, cp.lambda_, cp.num_iters = 0.02, 1.0, 1
-        sp = A.default_sampling_params()
+        sp = A.default_sampling_params(native=False)
         sp.std_dev[0] = sp.std_dev[1] = 0.5
-        cc = A.default_constraints()
+        cc = A.default_constraints(native=False)
         for i in range(2):
             cc.lower[i], cc.upper[i] = -1.0, 1.0
         dyn = A.DoubleIntegratorParams(0.0)
@@ -336,11 +336,11 @@ def cpu_baseline(name, seed, budget_s):
             r = np.random.default_rng(seed + 5)
             shapes = list(zip(r.integers(2048, 16385, size=128).tolist(), r.choice([50, 100, 200], size=128).tolist()))
         cmap = (W.gaussian_bump_costmap(seed), 0.1, (0.0, 0.0))
-        cp = A.default_controller_params()
+        cp = A.default_controller_params(native=False)
         cp.dt, cp.lambda_, cp.num_iters = 0.02, 2.0, 1
-        sp = A.default_sampling_params()
+        sp = A.default_sampling_params(native=False)
         sp.std_dev[0] = sp.std_dev[1] = 0.5
-        cc = A.default_constraints()
+        cc = A.default_constraints(native=False)
         for i in range(2):
             cc.lower[i], cc.upper[i] = -1.0, 1.0
         dyn = A.BicycleSlipParams(1500.0, 2500.0, 1.2, 1.3, 8e4, 4000.0, 50.0, 0.5, 0.1, 1.0)
@@ -374,12 +374,12 @@ def cpu_baseline(name, seed, budget_s):
             lam, std = 2.0, (1.0, 0.3)
             lo = [(-3.0, 3.0), (-1.0, 1.0)]
             x0 = np.array([25.0, 25.0, 0.3, 4.0], np.float32)
-        cp = A.default_controller_params()
+        cp = A.default_controller_params(native=False)
         cp.dt, cp.lambda_, cp.num_iters = 0.02, lam, 1
-        sp = A.default_sampling_params()
+        sp = A.default_sampling_params(native=False)
         for i, s in enumerate(std):
             sp.std_dev[i] = s
-        cc = A.default_constraints()
+        cc = A.default_constraints(native=False)
         for i, (a, b) in enumerate(lo):
             cc.lower[i], cc.upper[i] = a, b
         u = np.zeros((wl_t, Cd), np.float32)

@@ -407,8 +407,9 @@ mppi_status mppi_kernel_weighted_reduction(const float* weights_d, const float* 
 /* Same result as mppi_kernel_weighted_reduction for callers that may not allocate memory (a control loop with a
  * frozen memory map, a process whose GPU memory belongs to another allocator, a build that forbids allocation after
  * start-up).  No counterpart in the reference.  The scratch is one 4 MiB array inside the library's device image,
- * kept by every GPU that loads the library until exit; the first call on a device looks up its address
- * (cudaGetSymbolAddress), so make that first call before any stream capture.  Limits: num_rollouts <= 65536 and
+ * kept by every GPU that loads the library until exit; every call outside stream capture looks up its address on
+ * the current device (cudaGetSymbolAddress) and a call under capture reuses the last address found there, so make
+ * the first call on a device before any stream capture.  Limits: num_rollouts <= 65536 and
  * num_timesteps * control_dim <= 1024, else MPPI_EINVAL.  Calls share the array: calls that overlap on the GPU race
  * and must be serialised by the caller. */
 mppi_status mppi_kernel_weighted_reduction_noalloc(const float* weights_d, const float* controls_d, float* new_u_d,

@@ -5,6 +5,7 @@ the host-side mirror of the reference's interface.  Build the library with ``pyt
 """
 from . import _abi
 from ._abi import MPPIError
+from . import nn_io
 from .controller import (BatchedMPPIController, BicycleDynamics, BicycleSlipDynamics, BicycleSlipMLPDynamics,
                          CartpoleDynamics,
                          CartpoleSwingupCost, ColoredNoiseDistribution, CostmapCost, DoubleIntegratorDynamics,
@@ -14,4 +15,4 @@ from .controller import (BatchedMPPIController, BicycleDynamics, BicycleSlipDyna
 __all__ = ["MPPIError", "BatchedMPPIController", "VanillaMPPIController", "CartpoleDynamics", "CartpoleSwingupCost",
            "DoubleIntegratorDynamics", "DoubleIntegratorObstacleCost", "BicycleDynamics", "BicycleSlipDynamics",
            "BicycleSlipMLPDynamics",
-           "CostmapCost", "GaussianDistribution", "ColoredNoiseDistribution", "select_top_samples", "_abi"]
+           "CostmapCost", "GaussianDistribution", "ColoredNoiseDistribution", "select_top_samples", "_abi", "nn_io"]

@@ -221,19 +221,40 @@ def call(name: str, *args):
     return st
 
 
-def default_controller_params() -> ControllerParams:
+def default_controller_params(native: bool = True) -> ControllerParams:
+    """ControllerParams defaults (controller.cuh:46-68).  native=False fills them without loading the engine library
+    (for code that must not map it, such as the CPU baseline); a CPU test keeps both forms equal."""
     p = ControllerParams()
-    lib().mppi_default_controller_params(C.byref(p))
+    if native:
+        lib().mppi_default_controller_params(C.byref(p))
+    else:
+        p.dt, p.lambda_, p.alpha, p.num_timesteps, p.num_iters, p.seed = 0.02, 1.0, 0.0, 100, 1, 0
     return p
 
 
-def default_sampling_params() -> SamplingParams:
+def default_sampling_params(native: bool = True) -> SamplingParams:
+    """GaussianParamsImpl / ColoredNoiseParamsImpl defaults (gaussian.cuh:21-61, colored_noise.cuh:44-73)."""
     p = SamplingParams()
-    lib().mppi_default_sampling_params(C.byref(p))
+    if native:
+        lib().mppi_default_sampling_params(C.byref(p))
+    else:
+        p.kind = 0
+        for i in range(MPPI_MAX_CONTROL_DIM):
+            p.std_dev[i] = 1.0
+        p.pure_noise_trajectories_percentage = 0.01
+        p.std_dev_decay = 1.0
+        p.offset_decay_rate = 0.97
+        p.fmin = 0.0
     return p
 
 
-def default_constraints() -> ControlConstraints:
+def default_constraints(native: bool = True) -> ControlConstraints:
+    """Unbounded control ranges (Dynamics::setDefaultControlRanges, dynamics.cu:19-26)."""
     c = ControlConstraints()
-    lib().mppi_default_constraints(C.byref(c))
+    if native:
+        lib().mppi_default_constraints(C.byref(c))
+    else:
+        flt_max = 3.4028234663852886e38  # FLT_MAX
+        for i in range(MPPI_MAX_CONTROL_DIM):
+            c.lower[i], c.upper[i], c.deadband[i], c.zero_control[i] = -flt_max, flt_max, 0.0, 0.0
     return c

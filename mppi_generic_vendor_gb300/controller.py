@@ -166,10 +166,13 @@ class BicycleSlipMLPDynamics(BicycleSlipDynamics):
             raise ValueError(f"surrogate parameter vector must hold {A.MLP_PARAMS} floats")
         self.mlp_params = p
 
-    def loadParams(self, path):
-        """Parameters saved by ``Surrogate.save`` (npz)."""
-        with np.load(path) as f:
-            self.updateModel(f["params"])
+    def loadParams(self, path, prefix=""):
+        """Network from an npz file: a ``Surrogate.save`` checkpoint, or the reference's FNNHelper arrays
+        ``dynamics_W{i}`` / ``dynamics_b{i}`` (FNNHelper::loadParams, fnn_helper.cu:64-127), which carry no
+        normalisation (identity scaling)."""
+        from . import nn_io
+
+        self.updateModel(nn_io.load(path, prefix))
 
 
 class CostmapCost(_Plugin):

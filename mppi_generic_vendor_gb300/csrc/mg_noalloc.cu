@@ -7,10 +7,11 @@
 // array that lives in the library's device image instead, so a call performs no allocation or free of any kind.
 //
 // The array is `g_reduction_scratch` below: kNoAllocScratchBytes (4 MiB) of device memory that every GPU loading the
-// library keeps until the process exits.  Host code reaches it through its device address, looked up once per
-// device with cudaGetSymbolAddress on the first call on that device (so make the first call before any stream
-// capture).  All calls share the array: calls that overlap on the GPU (on different streams, or from different host
-// threads) race on it and must be serialised by the caller.  Each call clears the counters that must start at zero.
+// library keeps until the process exits.  Host code reaches it through its device address, looked up with
+// cudaGetSymbolAddress by every call made outside stream capture; a call under capture reuses the address the last
+// uncaptured call on that device found (so make the first call on a device before any stream capture).  All calls
+// share the array: calls that overlap on the GPU (on different streams, or from different host threads) race on it
+// and must be serialised by the caller.  Each call clears the counters that must start at zero.
 #include <mutex>
 
 #include "mg_common.cuh"
@@ -87,13 +88,19 @@ struct DeviceScratch
 };
 DeviceScratch g_scratch;
 
-mppi_status scratch_address(void** out)
+// The array's device address on the current device.  Outside stream capture it is looked up on every call (a host-
+// side table lookup, no allocation), so a context that was torn down and created again (cudaDeviceReset) hands out
+// the array's new address; during capture, where the lookup could load the module, the address recorded by the
+// last call outside capture on this device is used.
+mppi_status scratch_address(cudaStream_t s, void** out)
 {
   int dev = 0;
   MG_CUDA(cudaGetDevice(&dev));
   MG_CHECK(dev >= 0 && dev < 256, "device ordinal %d out of range", dev);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  MG_CUDA(cudaStreamIsCapturing(s, &cap));
   std::lock_guard<std::mutex> lock(g_scratch.mu);
-  if (!g_scratch.addr[dev])
+  if (cap == cudaStreamCaptureStatusNone)
   {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_reduction_scratch);
@@ -104,6 +111,8 @@ mppi_status scratch_address(void** out)
     }
     g_scratch.addr[dev] = p;
   }
+  MG_CHECK(g_scratch.addr[dev] != nullptr,
+           "the first allocation-free call on device %d must come before any stream capture", dev);
   *out = g_scratch.addr[dev];
   return MPPI_OK;
 }
@@ -136,9 +145,9 @@ mppi_status mppi_kernel_weighted_reduction_noalloc(const float* weights_d, const
   const ScratchLayout L = layout_for(nch, (int)tc);
   MG_CHECK(L.total <= kNoAllocScratchBytes, "problem needs %zu scratch bytes, more than the %zu available", L.total,
            kNoAllocScratchBytes);
-  void* scratch = nullptr;
-  MG_TRY(scratch_address(&scratch));
   cudaStream_t s = (cudaStream_t)stream;
+  void* scratch = nullptr;
+  MG_TRY(scratch_address(s, &scratch));
   noalloc_setup_kernel<<<(nch + 255) / 256, 256, 0, s>>>(L, num_rollouts, num_timesteps, nch, (int)tc);
   MG_CUDA(cudaGetLastError());
   char* base = (char*)scratch;

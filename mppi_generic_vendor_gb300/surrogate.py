@@ -88,12 +88,21 @@ class Surrogate:
             raise ValueError(f"expected {A.MLP_PARAMS} parameters")
         A.call("mppi_surrogate_set_params", self._h, _fp(p))
 
-    def save(self, path):
-        """Checkpoint: weights, normalisation and the generating configuration as an .npz file."""
+    def save(self, path, format="engine"):
+        """Checkpoint as an .npz file: ``format="engine"`` stores weights, normalisation and the generating
+        configuration; ``format="reference"`` stores the reference's FNNHelper arrays (normalisation folded in)."""
+        if format == "reference":
+            from . import nn_io
+
+            nn_io.save_reference(path, self.params())
+            return
+        if format != "engine":
+            raise ValueError("format must be 'engine' or 'reference'")
         np.savez(path, params=self.params(), seed=np.uint64(self.config.seed),
                  state_lower=np.array(self.config.state_lower[:], np.float32),
                  state_upper=np.array(self.config.state_upper[:], np.float32))
 
-    def load(self, path):
-        d = np.load(path)
-        self.set_params(d["params"])
+    def load(self, path, prefix=""):
+        from . import nn_io
+
+        self.set_params(nn_io.load(path, prefix))

@@ -67,7 +67,9 @@ def colored_noise(ref_root: Path):
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the MPPI-Generic checkout>")
+    ref = Path(sys.argv[1])
     reference_kats()
     colored_noise(ref)
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))

@@ -50,6 +50,12 @@ def test_reference_defaults():
     assert cp.lambda_ == 1.0 and cp.alpha == 0.0 and cp.num_iters == 1
 
 
+def test_defaults_without_the_library_equal_the_library_defaults():
+    """The CPU baseline fills its parameter blocks without mapping libmppi_gb.so; the values must be the same."""
+    for f in (A.default_controller_params, A.default_sampling_params, A.default_constraints):
+        assert bytes(f(native=False)) == bytes(f()), f.__name__
+
+
 def _create(model=A.MODEL_CARTPOLE, K=(64,), T=(16,), dyn_bytes=None, **over):
     cp = A.default_controller_params()
     sp = A.default_sampling_params()

@@ -26,6 +26,8 @@ _U32P = C.POINTER(C.c_uint32)
 _SIGS = [
     ("orc_sincosf", None, [_FP, _FP, _FP, C.c_size_t]),
     ("orc_normalize_angle", C.c_float, [C.c_float]),
+    ("orc_set_trig_mode", None, [C.c_int]),
+    ("orc_get_trig_mode", C.c_int, []),
     ("orc_philox4x32_10", None, [_U32P, _U32P, _U32P]),
     ("orc_gaussian_rewrite", None, [_FP, _FP, _FP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, _FP]),
     ("orc_enforce_constraints", None, [_FP, C.c_size_t, C.c_int, _P]),
@@ -92,6 +94,19 @@ def sincosf(x):
     c = np.empty_like(x)
     lib().orc_sincosf(_fp(x), _fp(s), _fp(c), x.size)
     return s, c
+
+
+class libm_trig:
+    """Context manager: the float oracle evaluates sine / cosine with libm sinf / cosf (the reference's host twins,
+    e.g. cartpole_dynamics.cu:48-53) instead of the engine's own sincos_f."""
+
+    def __enter__(self):
+        lib().orc_set_trig_mode(1)
+        return self
+
+    def __exit__(self, *exc):
+        lib().orc_set_trig_mode(0)
+        return False
 
 
 def normalize_angle(a: float) -> float:

@@ -22,6 +22,7 @@
 #include <cstdint>
 #include <cstring>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "../include/mppi_gb.h"
@@ -66,12 +67,26 @@ static inline void sincos_f(float x, float* s_out, float* c_out)
   *c_out = c;
 }
 
+// Trigonometry of the float instantiation: 0 = the engine's sincos_f above (the default; bit-identical to the
+// engine), 1 = libm sinf / cosf, the functions the reference's host twins call (CartpoleDynamics::computeDynamics,
+// cartpole_dynamics.cu:48-53), to measure what the choice of sine / cosine moves.
+static std::atomic<int> g_trig_mode{ 0 };
+
 template <class R>
 struct M;
 template <>
 struct M<float>
 {
-  static inline void sincos(float x, float* s, float* c) { sincos_f(x, s, c); }
+  static inline void sincos(float x, float* s, float* c)
+  {
+    if (g_trig_mode.load(std::memory_order_relaxed) == 1)
+    {
+      *s = sinf(x);
+      *c = cosf(x);
+      return;
+    }
+    sincos_f(x, s, c);
+  }
   static inline float fma(float a, float b, float c) { return fmaf(a, b, c); }
   static inline float sqrt(float a) { return sqrtf(a); }
   static inline float fabs(float a) { return fabsf(a); }
@@ -167,15 +182,22 @@ static inline R costmap_bilinear(const CostmapView& m, R x, R y)
 }
 
 template <class R>
+static inline bool libm_float()
+{
+  return std::is_same<R, float>::value && g_trig_mode.load(std::memory_order_relaxed) == 1;
+}
+
+template <class R>
 struct Cartpole
 {
   static const int S = 4, C = 1;
   const mppi_cartpole_params& p;
   const mppi_cartpole_cost_params& q;
-  // CartpoleDynamics::computeDynamics, device version (cartpole_dynamics.cu:87-105)
+  // CartpoleDynamics::computeDynamics, device version (cartpole_dynamics.cu:87-105); with libm trigonometry the host
+  // twin (cartpole_dynamics.cu:48-67), which takes sinf / cosf of the unwrapped angle
   void deriv(const R* x, const R* u, R* xd) const
   {
-    const R th = M<R>::normalize_angle(x[2]);
+    const R th = libm_float<R>() ? x[2] : M<R>::normalize_angle(x[2]);
     R s, c;
     M<R>::sincos(th, &s, &c);
     const R td = x[3], f = u[0];
@@ -812,6 +834,9 @@ double orc_mlp_loss_grad(const double* params, const float* X, const float* Y, i
 {
   return orc::mlp_loss_grad(params, X, Y, B, grad);
 }
+
+void orc_set_trig_mode(int mode) { orc::g_trig_mode.store(mode == 1 ? 1 : 0); }
+int orc_get_trig_mode(void) { return orc::g_trig_mode.load(); }
 
 void orc_sincosf(const float* x, float* s, float* c, size_t n)
 {

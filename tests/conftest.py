@@ -17,4 +17,5 @@ def golden():
     import numpy as np
 
     d = ROOT / "tests" / "golden"
-    return {"kats": np.load(d / "reference_kats.npz"), "colored": np.load(d / "colored_noise.npz")}
+    return {"kats": np.load(d / "reference_kats.npz"), "colored": np.load(d / "colored_noise.npz"),
+            "tsallis": np.load(d / "tsallis_kats.npz")}

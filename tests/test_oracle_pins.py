@@ -152,3 +152,40 @@ def test_tsallis_transform_restatement(gamma, r):
     assert np.all(w[d >= np.float32(gamma)] == 0.0) and np.any(d >= np.float32(gamma))
     order = np.argsort(c, kind="stable")
     assert np.all(np.diff(w[order]) <= 0.0)
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_tsallis_matches_reference_function(golden, case):
+    """orc_tsallis bit for bit against the reference's own TsallisTransform (mppi_common.cu:1004-1021), compiled for
+    the host from the reference checkout and run on the fixture's costs (tests/golden/make_golden.py)."""
+    g = golden["tsallis"]
+    w = oracle.tsallis(g[f"t{case}_costs"], float(g[f"t{case}_gamma"]), float(g[f"t{case}_r"]),
+                       float(g[f"t{case}_baseline"]))
+    assert np.array_equal(w.view(np.uint32), g[f"t{case}_weights"].view(np.uint32))
+
+
+def test_cartpole_trig_choice_moves_costs_below_parity_tolerance():
+    """The reference's host twin evaluates the cart-pole with libm sinf / cosf (cartpole_dynamics.cu:48-53), its
+    device code with the __sinf / __cosf intrinsics after normalizeAngle (:87-105); the engine and the oracle use
+    the engine's own sincos_f.  On the benchmark cart-pole rollout (K = 2048, T = 100, +-5 N clamp) the per-sample
+    costs of the two float forms differ by at most 1e-5 relative (measured: median <= 1e-7, max ~1.3e-6) and both
+    are equally close to the FP64 rollout."""
+    K, T = 2048, 100
+    rng = np.random.default_rng(0)
+    dyn, cost = A.CartpoleParams(1, 1, 1, 9.81), A.CartpoleCostParams(10, 1, 100, 1, 0)
+    sp, cc = A.default_sampling_params(native=False), A.default_constraints(native=False)
+    cc.lower[0], cc.upper[0] = -5.0, 5.0
+    for _ in range(3):
+        x0 = np.array([rng.uniform(-0.1, 0.1), rng.uniform(-0.1, 0.1), rng.uniform(-np.pi, np.pi),
+                       rng.uniform(-0.1, 0.1)], np.float32)
+        u = np.clip(rng.standard_normal(K * T).astype(np.float32), -5, 5)
+        own, _, _ = oracle.rollout(A.MODEL_CARTPOLE, dyn, cost, x0, u, u[:T], sp, cc, 1.0, 0.0, K, T, 0.02)
+        with oracle.libm_trig():
+            libm, _, _ = oracle.rollout(A.MODEL_CARTPOLE, dyn, cost, x0, u, u[:T], sp, cc, 1.0, 0.0, K, T, 0.02)
+        c64, _, _ = oracle.rollout(A.MODEL_CARTPOLE, dyn, cost, x0, u, u[:T], sp, cc, 1.0, 0.0, K, T, 0.02,
+                                   fp64=True)
+        rel = np.abs(own - libm) / np.abs(libm)
+        assert np.median(rel) <= 1e-6 and rel.max() <= 1e-5, (np.median(rel), rel.max())
+        e_own, e_libm = np.abs(own - c64) / np.abs(c64), np.abs(libm - c64) / np.abs(c64)
+        assert np.median(e_own) <= 2 * np.median(e_libm) + 1e-8 and e_own.max() <= 1e-5
+    assert oracle.lib().orc_get_trig_mode() == 0

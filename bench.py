@@ -39,10 +39,11 @@ UNIT = "sample-steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: enough for about 1.2 s of device time, at least 20)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="batched_di", choices=["batched_di", "cartpole", "bicycle",
+    ap.add_argument("--workload", default="batched_slip_mlp", choices=["batched_di", "cartpole", "bicycle",
                                                                  "batched_di_gaussian", "slip_mlp",
                                                                  "batched_slip_mlp"])
     ap.add_argument("--precision", default=None, choices=["bf16", "fp8", "fp32"],
@@ -207,7 +208,8 @@ def surrogate_extras(args, wl, stream):
     surrogate (judge on) against MPPI on the analytic model, both from zero control sequences for the same number of
     iterations, each final sequence costed by the FP64 analytic rollout."""
     import oracle
-    from mppi_generic_vendor_gb300 import BicycleSlipDynamics, GaussianDistribution, VanillaMPPIController
+    from mppi_generic_vendor_gb300 import (BatchedMPPIController, BicycleSlipDynamics, GaussianDistribution,
+                                           VanillaMPPIController)
     from mppi_generic_vendor_gb300 import _abi as A
     from mppi_generic_vendor_gb300 import workloads as W
 
@@ -274,9 +276,34 @@ def surrogate_extras(args, wl, stream):
         c.close()
         rel.append(cost64(i, u_sur[i]) / cost64(i, u_ana) - 1.0)
     rel = np.array(rel)
-    return {"plain_gpu": {"form": "analytic model, FP32, one controller per instance, solved in turn",
+    # batched analytic: the same instances in one handle with the analytic model in FP32 (no surrogate), timed like
+    # `value` (device-resident solves, CUDA events on the handle's stream)
+    import torch
+
+    ana = BatchedMPPIController(BicycleSlipDynamics(), W._slip_cost(cmap), GaussianDistribution(std_dev=(0.5, 0.5)),
+                                wl.K, wl.T, dt=0.02, max_iter=1, lambda_=2.0, seed=0, stream=stream)
+    ana.computeControl(wl.x0, 1)
+    ana.autotune(ROOT / "mppi_generic_vendor_gb300" / "_build" / "autotune_cache.json")
+    ana.computeControl(wl.x0, 1)
+    ana.enqueueSolve(1, 3)
+    ana.synchronize()
+    n_ana = max(20, min(400, args.steps))
+    s = torch.cuda.ExternalStream(stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    ana.enqueueSolve(1, n_ana)
+    e1.record(s)
+    e1.synchronize()
+    ana_s = e0.elapsed_time(e1) / 1e3 / n_ana
+    ana.close()
+    return {"plain_gpu": {"form": "analytic model, FP32, one controller per instance, solved in turn "
+                                  "(computeControl with host buffers)",
                           "iters_per_s": 1.0 / plain_s,
                           "sample_steps_per_s": wl.sample_steps_per_iter / plain_s},
+            "batched_analytic_gpu": {"form": "analytic model, FP32, all instances in one handle, device-resident "
+                                             "solves (as value)",
+                                     "iters_per_s": 1.0 / ana_s, "ms_per_iter": 1e3 * ana_s,
+                                     "sample_steps_per_s": wl.sample_steps_per_iter / ana_s},
             "surrogate_cost_error": {"vs": "FP64 analytic rollout of each instance's nominal control sequence",
                                      "instances": len(errs), "median": float(np.median(errs)),
                                      "max": float(np.max(errs))},
@@ -444,6 +471,15 @@ def run_gpu(args, ws, rank, local):
     ctrl.computeControl(x0, 1)  # uploads x0 and the nominal controls, builds the graphs
     ctrl.enqueueSolve(1, max(args.warmup, 3))
     ctrl.synchronize()
+    if args.steps is None:
+        # enough steps for about 1.2 s of device time (the clock sampler sees several readings under load)
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        ctrl.enqueueSolve(1, 3)
+        p1.record(stream)
+        p1.synchronize()
+        args.steps = int(min(5000, max(20, np.ceil(1200.0 / (p0.elapsed_time(p1) / 3)))))
+        args.steps = int(max_over_ranks(args.steps, dist))  # every rank times the same number of steps
     clocks = ClockSampler(local)
     clocks.start()
     if dist:
@@ -527,6 +563,12 @@ def run_gpu(args, ws, rank, local):
         line["dtype"] = {"bf16": "bf16 weights, f32 accumulate/state", "fp8": "fp8-e4m3 weights, f32 accumulate/state",
                          "fp32": "f32"}[wl.description["precision"]]
         line.update(surrogate_extras(args, wl, stream.cuda_stream))
+        # the metric's comparison: surrogate + batched against the plain GPU form (and against batching the
+        # analytic model, which needs no surrogate)
+        line["speedup"] = {
+            "vs_plain_gpu": iters_per_s / line["plain_gpu"]["iters_per_s"],
+            "vs_plain_gpu_e2e": line["e2e"]["iters_per_s"] / line["plain_gpu"]["iters_per_s"],
+            "vs_batched_analytic_gpu": iters_per_s / line["batched_analytic_gpu"]["iters_per_s"]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, 0, args.cpu_seconds)
     if rank == 0:
@@ -540,6 +582,8 @@ def run_reference(args, ws, rank):
     if rank != 0:
         return
     _SURROGATE["cpu_only"] = True
+    if args.steps is None:
+        args.steps = 10
     per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
     for _ in range(args.warmup):
         cpu_baseline(args.workload, 0, per_step)

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define MPPI_GB_ABI_VERSION 1
+#define MPPI_GB_ABI_VERSION 2
 #define MPPI_MAX_STATE_DIM 8
 #define MPPI_MAX_CONTROL_DIM 4
 #define MPPI_MAX_OBSTACLES 8
@@ -61,7 +61,16 @@ typedef enum mppi_sampler_kind
   MPPI_SAMPLER_COLORED_NOISE = 1  /* ColoredNoiseDistributionImpl (colored_noise.cuh:79) */
 } mppi_sampler_kind;
 
-/* ControllerParams (include/mppi/controllers/controller.cuh:46-68).  Block dimensions are chosen by the engine. */
+/* Controller kinds: which controller's computeControl the handle runs. */
+typedef enum mppi_controller_kind
+{
+  MPPI_CONTROLLER_VANILLA = 0, /* VanillaMPPIController (mppi_controller.cu:152-237) */
+  MPPI_CONTROLLER_COLORED = 1  /* ColoredMPPIController (colored_mppi_controller.cu:145-249): Tsallis weights when
+                                  tsallis_gamma != 0 and tsallis_r != 0, state leash, final clamp of control 1 only */
+} mppi_controller_kind;
+
+/* ControllerParams (include/mppi/controllers/controller.cuh:46-68) and the fields ColoredMPPIParams adds
+ * (colored_mppi_controller.cuh:17-22).  Block dimensions are chosen by the engine. */
 typedef struct mppi_controller_params
 {
   float dt;
@@ -71,6 +80,12 @@ typedef struct mppi_controller_params
   int num_iters;     /* optimisation iterations per computeControl */
   uint64_t seed;     /* Philox key */
   float slide_control_scale[MPPI_MAX_CONTROL_DIM];
+  int controller;    /* mppi_controller_kind (default MPPI_CONTROLLER_VANILLA) */
+  float tsallis_r;   /* ColoredMPPIParams::r (default 2.0) */
+  float tsallis_gamma; /* ColoredMPPIParams::gamma (default 0 = exponential weights) */
+  int leash_active;  /* ColoredMPPIController::leash_active_ (default 0); the leash holds x0 near the nominal state
+                        at the step the last slideControlSequence moved by (leash_jump_, 1 before any slide) */
+  float state_leash_dist[MPPI_MAX_STATE_DIM]; /* ColoredMPPIParams::state_leash_dist_ (default 0) */
 } mppi_controller_params;
 
 /* GaussianParamsImpl (gaussian.cuh:21-61) and ColoredNoiseParamsImpl (colored_noise.cuh:44-73). */

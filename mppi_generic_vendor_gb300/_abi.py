@@ -23,6 +23,7 @@ MODEL_BICYCLE_SLIP = 4
 MODEL_BICYCLE_SLIP_MLP = 5
 
 SAMPLER_GAUSSIAN = 0
+CONTROLLER_VANILLA, CONTROLLER_COLORED = 0, 1
 SAMPLER_COLORED_NOISE = 1
 
 _F4 = C.c_float * MPPI_MAX_CONTROL_DIM
@@ -31,7 +32,9 @@ _FO = C.c_float * MPPI_MAX_OBSTACLES
 
 class ControllerParams(C.Structure):
     _fields_ = [("dt", C.c_float), ("lambda_", C.c_float), ("alpha", C.c_float), ("num_timesteps", C.c_int),
-                ("num_iters", C.c_int), ("seed", C.c_uint64), ("slide_control_scale", _F4)]
+                ("num_iters", C.c_int), ("seed", C.c_uint64), ("slide_control_scale", _F4), ("controller", C.c_int),
+                ("tsallis_r", C.c_float), ("tsallis_gamma", C.c_float), ("leash_active", C.c_int),
+                ("state_leash_dist", C.c_float * MPPI_MAX_STATE_DIM)]
 
 
 class SamplingParams(C.Structure):
@@ -229,6 +232,7 @@ def default_controller_params(native: bool = True) -> ControllerParams:
         lib().mppi_default_controller_params(C.byref(p))
     else:
         p.dt, p.lambda_, p.alpha, p.num_timesteps, p.num_iters, p.seed = 0.02, 1.0, 0.0, 100, 1, 0
+        p.controller, p.tsallis_r, p.tsallis_gamma, p.leash_active = CONTROLLER_VANILLA, 2.0, 0.0, 0
     return p
 
 

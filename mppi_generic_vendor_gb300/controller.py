@@ -570,3 +570,67 @@ class VanillaMPPIController(BatchedMPPIController):
 
     def getNormalizerPercent(self) -> float:
         return self.getNormalizerCost() / float(self.K[0])
+
+
+class ColoredMPPIController(VanillaMPPIController):
+    """ColoredMPPIController(model, cost, fb_controller, sampler, dt, max_iter, lambda, alpha, num_timesteps, ...)
+    (controllers/ColoredMPPI/colored_mppi_controller.cuh:40-196): the same iteration with Tsallis weights
+    (TsallisTransform, mppi_common.cu:1004-1021) once gamma and r are both non-zero, an optional state leash
+    (Dynamics::enforceLeash) and, after smoothing, a clamp of control 1 only (colored_mppi_controller.cu:224-229).
+    ColoredMPPIParams' defaults: r = 2, gamma = 0 (exponential weights), leash off."""
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        cp = self.getParams()
+        cp.controller = A.CONTROLLER_COLORED
+        self.setParams(cp)
+
+    def _update(self, **fields):
+        cp = self.getParams()
+        for k, v in fields.items():
+            setattr(cp, k, v)
+        self.setParams(cp)
+
+    def setGamma(self, gamma):
+        self._update(tsallis_gamma=float(gamma))
+
+    def getGamma(self) -> float:
+        return float(self.params_.tsallis_gamma)
+
+    def setRExp(self, r):
+        self._update(tsallis_r=float(r))
+
+    def getRExp(self) -> float:
+        return float(self.params_.tsallis_r)
+
+    def setStateLeashLength(self, new_state_leash, index=0):
+        cp = self.getParams()
+        cp.state_leash_dist[index] = float(new_state_leash)
+        self.setParams(cp)
+
+    def getStateLeashLength(self, index) -> float:
+        return float(self.params_.state_leash_dist[index])
+
+    def setLeashActive(self, active):
+        self._update(leash_active=int(bool(active)))
+
+    def getLeashActive(self) -> bool:
+        return bool(self.params_.leash_active)
+
+    def setOffsetDecayRate(self, rate):
+        self.sampler_.offset_decay_rate = float(rate)
+        self.setSamplingParams(self.sampler_)
+
+    def getOffsetDecayRate(self) -> float:
+        return float(self.sampler_.offset_decay_rate)
+
+    def setColoredNoiseExponents(self, exponents):
+        self.sampler_.exponents = tuple(float(v) for v in exponents)
+        self.setSamplingParams(self.sampler_)
+
+    def getColoredNoiseExponents(self):
+        return list(self.sampler_.exponents)[:self.Cdim]
+
+    def setNoiseDecay(self, decay):
+        self.sampler_.std_dev_decay = float(decay)
+        self.setSamplingParams(self.sampler_)

@@ -224,6 +224,10 @@ void mppi_default_controller_params(mppi_controller_params* p)
   p->num_timesteps = 100;
   p->num_iters = 1;
   p->seed = 0;
+  p->controller = MPPI_CONTROLLER_VANILLA;
+  p->tsallis_r = 2.0f;  // ColoredMPPIParams defaults (colored_mppi_controller.cuh:17-22)
+  p->tsallis_gamma = 0.0f;
+  p->leash_active = 0;
 }
 
 void mppi_default_sampling_params(mppi_sampling_params* p)
@@ -572,7 +576,7 @@ mppi_status mppi_kernel_weight_transform(float* costs_d, float* out2_d, float la
   dim3 mg_grid((num_rollouts + 255) / 256, num_systems);
   if (mg_grid.x > 64) mg_grid.x = 64;
   min_cost_kernel<<<mg_grid, 256, 0, s>>>(costs_d, num_rollouts, num_systems, bits);
-  WeightsArgs a;
+  WeightsArgs a{};
   a.inst = (const InstDesc*)(base + o_inst);
   a.chunks = (const int4*)(base + o_chunks);
   a.part_off = (const long long*)(base + o_poff);
@@ -644,7 +648,7 @@ mppi_status mppi_kernel_weighted_reduction(const float* weights_d, const float* 
   MG_CUDA(cudaMemcpyAsync(base + o_poff, part_off.data(), sizeof(long long) * nch, cudaMemcpyHostToDevice, s));
   MG_CUDA(cudaMemcpyAsync(base + o_c0, &chunk0, sizeof(int), cudaMemcpyHostToDevice, s));
   MG_CUDA(cudaMemsetAsync(base + o_cnt, 0, sizeof(unsigned int) * 4, s));
-  WeightsArgs a;
+  WeightsArgs a{};
   a.inst = (const InstDesc*)(base + o_inst);
   a.chunks = (const int4*)(base + o_chunks);
   a.part_off = (const long long*)(base + o_poff);

@@ -113,9 +113,11 @@ struct RolloutShape
   static constexpr int TCH = (NS * (32 * C + 4) * 4 <= 48 * 1024) ? 32 : 16;
 };
 
-inline SampleShared make_sample_shared(const mppi_sampling_params& sp, const mppi_control_constraints& cc)
+inline SampleShared make_sample_shared(const mppi_sampling_params& sp, const mppi_control_constraints& cc,
+                                       int final_clamp = 0)
 {
-  SampleShared sh;
+  SampleShared sh{};
+  sh.final_clamp = final_clamp;
   for (int i = 0; i < kMaxC; ++i)
   {
     sh.std_dev[i] = sp.std_dev[i];
@@ -199,6 +201,29 @@ public:
         return MPPI_ENAN;
       }
     for (int i = 0; i < I_; ++i) prev_baseline_[i] = baseline_norm_[2 * i];
+    if (cp_.controller == MPPI_CONTROLLER_COLORED && cp_.leash_active)
+    {
+      // ColoredMPPIController::computeControl (colored_mppi_controller.cu:150-153): the state the solve starts from
+      // is held within state_leash_dist of the nominal state at step leash_jump_ of the previous solve
+      // (Dynamics::enforceLeash, dynamics.cuh:445-463)
+      if (traj_dirty_) compute_state_seq();
+      leashed_x0_.assign(x0, x0 + (size_t)I_ * S);
+      size_t so = 0;
+      for (int i = 0; i < I_; ++i)
+      {
+        const int j = std::min(std::max(leash_jump_, 0), T_[i] - 1);
+        const float* nominal = state_seq_.data() + so + (size_t)j * S;
+        float* xo = leashed_x0_.data() + (size_t)i * S;
+        for (int s = 0; s < S; ++s)
+        {
+          const float xt = x0[(size_t)i * S + s], xn = nominal[s], leash = cp_.state_leash_dist[s];
+          const float diff = fabsf(xn - xt);
+          xo[s] = leash < diff ? xt + fminf(fmaxf(xn - xt, -leash), leash) : xn;
+        }
+        so += (size_t)T_[i] * S;
+      }
+      x0 = leashed_x0_.data();
+    }
     memcpy(x0_h_.p, x0, sizeof(float) * I_ * S);
     memcpy(mean_h_.p, control_.data(), sizeof(float) * control_.size());
     if (graph_mode_)
@@ -232,6 +257,7 @@ public:
   mppi_status slide_control_sequence(int steps) override
   {
     MG_CHECK(steps >= 0, "steps must be >= 0");
+    leash_jump_ = steps;  // ColoredMPPIController::slideControlSequence (colored_mppi_controller.cu:260-268)
     for (int i = 0; i < I_; ++i)
     {
       float* u = control_.data() + t_off_[i];
@@ -294,6 +320,16 @@ public:
           float xd[S];
           mlp_host_dynamics(mlp_host_.data(), x, uc, xd);
           for (int s = 0; s < S; ++s) xn[s] = fmaf(xd[s], cp_.dt, x[s]);
+        }
+        else if (cp_.controller == MPPI_CONTROLLER_COLORED)
+        {
+          // ColoredMPPI clamps only control 1 after smoothing; computeOutputTrajectoryHelper still passes every
+          // control through enforceConstraints (controller.cuh:676-680).  (With a deadband and a smoothed control 1
+          // outside its range the reference would constrain the unclamped value; the clamp comes first here.)
+          float ucon[C];
+          for (int c = 0; c < C; ++c)
+            ucon[c] = enforce_constraint(uc[c], cc_.lower[c], cc_.upper[c], cc_.deadband[c], cc_.zero_control[c]);
+          euler_step<Model>(dyn_[i], x, ucon, xn, cp_.dt);
         }
         else
         {
@@ -440,11 +476,32 @@ public:
   mppi_status set_controller_params(const mppi_controller_params* cp) override
   {
     MG_CHECK(cp, "controller params must not be NULL");
-    MG_CHECK(cp->num_iters >= 1, "num_iters must be >= 1");
-    MG_CHECK(cp->lambda > 0.0f && std::isfinite(cp->lambda), "lambda must be positive");
-    MG_CHECK(std::isfinite(cp->dt), "dt must be finite");
+    MG_TRY(check_controller(*cp));
+    const bool tile_reduce_before = tile_reduce_active();
     cp_ = *cp;
+    if (tile_reduce_active() != tile_reduce_before)
+    {
+      // the weight path changed: mode 4 needs the tile reduction, and the rollout's shared memory follows it
+      if (rollout_mode_ == 4 && !noise_warps_available()) rollout_mode_ = 0;
+      MG_TRY(build_work_lists());
+    }
     invalidate_graphs();
+    return MPPI_OK;
+  }
+  mppi_status check_controller(const mppi_controller_params& cp) const
+  {
+    MG_CHECK(cp.num_iters >= 1, "num_iters must be >= 1");
+    MG_CHECK(cp.lambda > 0.0f && std::isfinite(cp.lambda), "lambda must be positive");
+    MG_CHECK(std::isfinite(cp.dt), "dt must be finite");
+    MG_CHECK(cp.controller == MPPI_CONTROLLER_VANILLA || cp.controller == MPPI_CONTROLLER_COLORED,
+             "controller must be MPPI_CONTROLLER_VANILLA (0) or MPPI_CONTROLLER_COLORED (1)");
+    MG_CHECK(std::isfinite(cp.tsallis_gamma) && std::isfinite(cp.tsallis_r), "tsallis_gamma and tsallis_r must be "
+             "finite");
+    MG_CHECK(cp.controller != MPPI_CONTROLLER_COLORED || cp.tsallis_gamma == 0.0f || cp.tsallis_r != 1.0f,
+             "tsallis_r = 1 makes the Tsallis exponent 1 / (r - 1) infinite");
+    for (int i = 0; i < S; ++i)
+      MG_CHECK(std::isfinite(cp.state_leash_dist[i]) && cp.state_leash_dist[i] >= 0.0f,
+               "state_leash_dist[%d] must be finite and >= 0", i);
     return MPPI_OK;
   }
   mppi_status set_costmap(const float* map, int w, int h, float res, float ox, float oy) override
@@ -731,11 +788,9 @@ private:
   mppi_status init(const CreateArgs& a)
   {
     I_ = a.num_instances;
+    MG_TRY(check_controller(a.cp));
     cp_ = a.cp;
     cc_ = a.cc;
-    MG_CHECK(cp_.num_iters >= 1, "num_iters must be >= 1");
-    MG_CHECK(cp_.lambda > 0.0f && std::isfinite(cp_.lambda), "lambda must be positive");
-    MG_CHECK(std::isfinite(cp_.dt), "dt must be finite");
     K_.assign(a.K, a.K + I_);
     T_.assign(a.T, a.T + I_);
     MG_TRY(check_sampling(a.sp));
@@ -1210,7 +1265,7 @@ private:
     a.seed_hi = (uint32_t)(cp_.seed >> 32);
     a.stride = stride;
     a.decay_pow = powf(sp_.std_dev_decay, (float)iter);
-    a.sh = make_sample_shared(sp_, cc_);
+    a.sh = sample_shared();
     if (sp_.kind == MPPI_SAMPLER_COLORED_NOISE) return launch_colored(a);
     const int grid = std::min(num_swork_, 8 * num_sms_);
     gaussian_sample_kernel<C><<<grid, 256, 0, stream_>>>(a);
@@ -1317,7 +1372,7 @@ private:
     for (int c = 0; c < C; ++c)
       if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
     a.max_t = max_t_;
-    a.sh = make_sample_shared(sp_, cc_);
+    a.sh = sample_shared();
     return a;
   }
 
@@ -1412,8 +1467,20 @@ private:
   }
 
   // The rollout tiles reduce the samples themselves (TileReduce) unless the surrogate rollout is in use (its judge
-  // rewrites costs after the rollout); then weights_update_kernel reads the samples again.
-  bool tile_reduce_active() const { return !(Model::kMlp && !use_analytic_); }
+  // rewrites costs after the rollout) or the weights are Tsallis weights (not a product of a per-tile factor and a
+  // tile-local weight, so they need the instance's baseline first); then weights_update_kernel reads the samples
+  // again.
+  bool tile_reduce_active() const { return !(Model::kMlp && !use_analytic_) && !tsallis(); }
+  // ColoredMPPIController::computeControl's weight choice (colored_mppi_controller.cu:197-207): Tsallis weights when
+  // gamma and r are both non-zero, else the exponential transform.
+  bool tsallis() const
+  {
+    return cp_.controller == MPPI_CONTROLLER_COLORED && cp_.tsallis_gamma != 0.0f && cp_.tsallis_r != 0.0f;
+  }
+  SampleShared sample_shared() const
+  {
+    return make_sample_shared(sp_, cc_, cp_.controller == MPPI_CONTROLLER_COLORED ? 1 : 0);
+  }
 
   mppi_status launch_weights()
   {
@@ -1433,7 +1500,7 @@ private:
       return MPPI_OK;
     }
     weights_stale_ = false;
-    WeightsArgs a;
+    WeightsArgs a{};
     a.inst = inst_d_.p;
     a.chunks = chunks_d_.p;
     a.part_off = part_off_d_.p;
@@ -1455,6 +1522,9 @@ private:
     a.lambda_inv = 1.0f / cp_.lambda;
     a.weights_given = 0;
     a.given_norm = nullptr;
+    a.transform = tsallis() ? 1 : 0;
+    a.tsallis_gamma = cp_.tsallis_gamma;
+    a.tsallis_r = cp_.tsallis_r;
     weights_update_kernel<C><<<num_chunks_, 256, 0, stream_>>>(a);
     MG_CUDA(cudaGetLastError());
     return MPPI_OK;
@@ -1473,7 +1543,7 @@ private:
     // rollout's finalizing CTAs did it already in the last iteration
     if (tail_finalize()) return MPPI_OK;
     finish_controls_kernel<C><<<I_, 256, sizeof(float) * (size_t)(max_t_ + 4) * C, stream_>>>(
-        inst_d_.p, mean_d_.p, first_d_.p, make_sample_shared(sp_, cc_));
+        inst_d_.p, mean_d_.p, first_d_.p, sample_shared());
     MG_CUDA(cudaGetLastError());
     return MPPI_OK;
   }
@@ -1592,6 +1662,8 @@ private:
   ModelAux aux_{};
   std::vector<float> control_, state_seq_, history_, last_pre_smooth_, baseline_norm_, prev_baseline_;
   std::vector<float> traj_u_, traj_x0_;  // constrained nominal controls and x0 of the last solve
+  std::vector<float> leashed_x0_;        // ColoredMPPI with the leash on: the initial states the solve starts from
+  int leash_jump_ = 1;                   // steps of the last slide (ColoredMPPIController::leash_jump_)
   bool traj_dirty_ = false;
   std::vector<double> stats_;
 

@@ -41,6 +41,10 @@ struct SampleShared
   float control_cost_coeff[kMaxC];
   float lower[kMaxC], upper[kMaxC], deadband[kMaxC], zero[kMaxC];
   float pure_pct;
+  // The constraint pass after smoothing: 0 = Dynamics::enforceConstraints on every control (VanillaMPPIController);
+  // 1 = ColoredMPPIController's pass, a plain clamp of control 1 to its range and nothing else
+  // (colored_mppi_controller.cu:224-229).
+  int final_clamp;
 };
 
 // Ordered-integer encoding of a float so unsigned atomicMin orders like the float (NaN counts as +inf).
@@ -430,7 +434,10 @@ __device__ __forceinline__ void finish_instance(const InstDesc& d, int i, float*
       for (int j = 0; j < 5; ++j) acc += coef[j] * buf[(t + j) * C + c];
       v = acc;
     }
-    u[e] = enforce_constraint(v, sh.lower[c], sh.upper[c], sh.deadband[c], sh.zero[c]);
+    if (sh.final_clamp == 1)
+      u[e] = c == 1 ? fminf(fmaxf(v, sh.lower[1]), sh.upper[1]) : v;
+    else
+      u[e] = enforce_constraint(v, sh.lower[c], sh.upper[c], sh.deadband[c], sh.zero[c]);
   }
 }
 
@@ -1554,7 +1561,19 @@ struct WeightsArgs
   float lambda_inv;
   int weights_given;        // 1: read w from `weights` instead of computing it from `costs`
   const float* given_norm;  // non-null: divide by given_norm[0] (a device float) instead of the summed weights
+  // 0: the exponential transform; 1: TsallisTransform (mppi_common.cu:1004-1021) with tsallis_gamma / tsallis_r
+  int transform;
+  float tsallis_gamma, tsallis_r;
 };
+
+// TsallisTransform (mppi_common.cu:1004-1021), the ColoredMPPI controller's weight: with d = c - baseline,
+// w = exp(log(1 - d / gamma) / (r - 1)) for d < gamma, else 0.  1 - d / gamma is formed in double from the float
+// quotient and narrowed to float for the logarithm, as the reference's expression evaluates.
+__device__ __forceinline__ float tsallis_weight(float c, float baseline, float gamma, float r)
+{
+  const float dif = c - baseline;
+  return dif < gamma ? expf(logf((float)(1.0 - (double)(dif / gamma))) / (r - 1.0f)) : 0.0f;
+}
 
 template <int C>
 __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_constant__ WeightsArgs a)
@@ -1584,8 +1603,15 @@ __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_consta
     else
     {
       const float c = a.costs[d.k_off + kb + i];
-      const double diff = (double)c - bd;
-      wk = expf((float)(-diff * linv));
+      if (a.transform == 1)
+      {
+        wk = tsallis_weight(c, b, a.tsallis_gamma, a.tsallis_r);
+      }
+      else
+      {
+        const double diff = (double)c - bd;
+        wk = expf((float)(-diff * linv));
+      }
       a.weights[d.k_off + kb + i] = wk;
     }
     s_w[i] = wk;

@@ -151,7 +151,7 @@ mppi_status mppi_kernel_weighted_reduction_noalloc(const float* weights_d, const
   noalloc_setup_kernel<<<(nch + 255) / 256, 256, 0, s>>>(L, num_rollouts, num_timesteps, nch, (int)tc);
   MG_CUDA(cudaGetLastError());
   char* base = (char*)scratch;
-  WeightsArgs a;
+  WeightsArgs a{};
   a.inst = (const InstDesc*)(base + L.inst);
   a.chunks = (const int4*)(base + L.chunks);
   a.part_off = (const long long*)(base + L.part_off);

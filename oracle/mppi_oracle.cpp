@@ -967,6 +967,10 @@ int orc_compute_control(int model, const void* dyn, const void* cost, const floa
   std::vector<double> costs(K), mean_d((size_t)T * C);
   float baseline = 0.0f;
   double normalizer = 0.0;
+  // ColoredMPPIController (colored_mppi_controller.cu:145-249): Tsallis weights when gamma and r are non-zero, and a
+  // final clamp of control 1 alone
+  const bool colored = cp->controller == MPPI_CONTROLLER_COLORED;
+  const bool tsallis = colored && cp->tsallis_gamma != 0.0f && cp->tsallis_r != 0.0f;
   for (int it = 0; it < cp->num_iters; ++it)
   {
     const float* e = eps + (eps_per_iter_stride_zero ? 0 : (size_t)it * n);
@@ -976,6 +980,12 @@ int orc_compute_control(int model, const void* dyn, const void* cost, const floa
                                  cp->dt, costs.data(), threads, nullptr);
     for (int k = 0; k < K; ++k) costs_f[k] = (float)costs[k];
     orc::weights(costs_f.data(), K, 1.0f / cp->lambda, w.data(), &baseline, &normalizer);
+    if (tsallis)
+    {
+      orc::tsallis(costs_f.data(), K, cp->tsallis_gamma, cp->tsallis_r, baseline, w.data());
+      normalizer = 0.0;
+      for (int k = 0; k < K; ++k) normalizer += w[k];  // computeNormalizer (mppi_common.cu:1091-1099)
+    }
     orc::weighted_mean(w.data(), (float)normalizer, samples.data(), K, T, C, mean_d.data(), nullptr);
     for (size_t j = 0; j < (size_t)T * C; ++j) control[j] = (float)mean_d[j];
   }
@@ -988,6 +998,7 @@ int orc_compute_control(int model, const void* dyn, const void* cost, const floa
     orc::with_model<float>(b, [&](auto& m) {
       for (int t = 0; t < T - 1; ++t)
       {
+        // the constraint inside computeOutputTrajectoryHelper (controller.cuh:676-680)
         for (int i = 0; i < C; ++i) u[i] = orc::enforce_constraint(control[(size_t)t * C + i], *cc, i);
         m.deriv(x, u, xd);
         for (int i = 0; i < S; ++i)
@@ -999,7 +1010,14 @@ int orc_compute_control(int model, const void* dyn, const void* cost, const floa
     });
   }
   for (int t = 0; t < T; ++t)
-    for (int i = 0; i < C; ++i) control[(size_t)t * C + i] = orc::enforce_constraint(control[(size_t)t * C + i], *cc, i);
+    for (int i = 0; i < C; ++i)
+    {
+      float& v = control[(size_t)t * C + i];
+      if (!colored)
+        v = orc::enforce_constraint(v, *cc, i);
+      else if (i == 1)
+        v = fminf(fmaxf(v, cc->lower[1]), cc->upper[1]);  // colored_mppi_controller.cu:224-229
+    }
   if (costs_out) std::copy(costs_f.begin(), costs_f.end(), costs_out);
   if (weights_out) std::copy(w.begin(), w.end(), weights_out);
   if (samples_out) std::copy(samples.begin(), samples.end(), samples_out);

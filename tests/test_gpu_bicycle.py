@@ -4,6 +4,7 @@ per-sample costs are bit-identical; the FP64 oracle measures the float rollout's
 import numpy as np
 import pytest
 
+import _parity
 import oracle
 from mppi_generic_vendor_gb300 import (BicycleDynamics, BicycleSlipDynamics, CostmapCost, GaussianDistribution,
                                        VanillaMPPIController)
@@ -13,8 +14,8 @@ from mppi_generic_vendor_gb300.workloads import gaussian_bump_costmap
 pytestmark = pytest.mark.gpu
 
 
-def run_parity(dyn, x0, std, lam, K, T, seed):
-    cmap = gaussian_bump_costmap(seed, size=128)
+def run_parity(dyn, x0, std, lam, K, T, seed, map_size=128):
+    cmap = gaussian_bump_costmap(seed, size=map_size)
     cost = CostmapCost(map_coeff=1.0, speed_target=8.0, speed_coeff=1.0, steer_coeff=0.5, terminal_coeff=2.0,
                        costmap=cmap, resolution=0.1, origin=(0.0, 0.0))
     ctrl = VanillaMPPIController(dyn, cost, None, GaussianDistribution(std_dev=std), 0.02, 1, lam, 0.0, T, K)
@@ -31,8 +32,7 @@ def run_parity(dyn, x0, std, lam, K, T, seed):
     got = ctrl.sample_costs()
     assert np.array_equal(got.view(np.uint32), ref["costs"].view(np.uint32))
     assert ctrl.getBaselineCost() == ref["baseline"]
-    scale = max(1.0, float(np.abs(ref["samples"]).max()))
-    assert np.abs(ctrl.getControlSeq().T - ref["control"]).max() <= 1e-5 * scale
+    _parity.check_control(ctrl.getControlSeq().T, ref, K, T, Cd)
     # accuracy of the float rollout against FP64 (same constrained samples)
     sp = ctrl.sampler_.to_c()
     r64, _, _ = oracle.rollout(ctrl.model_id, ctrl._dyn_arr[0], ctrl._cost_arr[0], x0, ref["samples"], init, sp,
@@ -47,6 +47,16 @@ def test_bicycle_costmap_parity():
     dyn = BicycleDynamics(2.5)
     x0 = np.array([6.0, 5.0, 0.4, 4.0], np.float32)
     rel = run_parity(dyn, x0, (1.0, 0.3), 2.0, 2048, 100, 3)
+    assert np.median(rel) < 1e-5
+
+
+def test_bicycle_costmap_parity_benchmark_size():
+    """The kinematic-bicycle benchmark configuration itself: K = 16384, T = 100, the 512 x 512 costmap of 32 bumps at
+    0.1 m cells, sigma (1.0, 0.3), lambda 2.0."""
+    dyn = BicycleDynamics(2.5)
+    dyn.setControlRanges([(-3.0, 3.0), (-1.0, 1.0)])
+    x0 = np.array([25.0, 25.0, 0.3, 4.0], np.float32)
+    rel = run_parity(dyn, x0, (1.0, 0.3), 2.0, 16384, 100, 0, map_size=512)
     assert np.median(rel) < 1e-5
 
 

@@ -7,6 +7,7 @@ import math
 import numpy as np
 import pytest
 
+import _parity
 import oracle
 from mppi_generic_vendor_gb300 import (BatchedMPPIController, CartpoleDynamics, CartpoleSwingupCost,
                                        DoubleIntegratorDynamics, DoubleIntegratorObstacleCost, GaussianDistribution,
@@ -42,11 +43,16 @@ def oracle_solve(ctrl, i, x0, eps, control_tc, stride=1, dyn=None, cost=None):
                                   control_tc, stride=stride)
 
 
-def check_control(got_tc, ref, tol=1e-5):
-    # the update is a weighted sum; compare relative to the sample-control scale
-    scale = max(1.0, float(np.abs(ref["samples"]).max()))
-    err = np.abs(got_tc - ref["control"]).max()
-    assert err <= tol * scale, (err, scale)
+def check_control(got_tc, ref, rtol=1e-5):
+    """Element-wise: each updated control within rtol of the magnitude of the weighted terms it sums (_parity)."""
+    T, Cdim = np.asarray(ref["control"]).shape
+    return _parity.check_control(got_tc, ref, ref["weights"].size, T, Cdim, rtol=rtol)
+
+
+def check_weights(w, ref_w, rtol=1e-5):
+    """Every weight within rtol relative, with an absolute floor of the smallest normal float (weights that underflow
+    to subnormals or zero carry no share of the update)."""
+    assert np.all(np.abs(w - ref_w) <= rtol * ref_w + np.finfo(np.float32).tiny)
 
 
 @pytest.mark.parametrize("iters", [1, 3])
@@ -67,16 +73,16 @@ def test_cartpole_compute_control_parity(iters):
         assert np.array_equal(got_costs.view(np.uint32), ref["costs"].view(np.uint32))
         assert np.array_equal(ctrl.control_samples().view(np.uint32), ref["samples"].view(np.uint32))
         assert ctrl.getBaselineCost() == ref["baseline"]
-        w = ctrl.sample_weights()
-        big = ref["weights"] > 1e-30
-        assert np.all(np.abs(w[big] - ref["weights"][big]) <= 1e-5 * ref["weights"][big])
+        check_weights(ctrl.sample_weights(), ref["weights"])
         bn, n64 = ctrl.baseline_normalizer()
         assert abs(n64[0] - ref["normalizer"]) <= 1e-5 * ref["normalizer"]
         check_control(ctrl.getControlSeq().T, ref)
     else:
-        # later iterations start from an update that differs by float rounding; costs stay within 1e-5 relative
+        # iterations 2 and 3 sample around an update that already differs by float rounding (the engine's FP32 sum
+        # against the oracle's FP64 sum); the exponential weights amplify a cost difference dc by dc / lambda, so
+        # the third update is held to 1e-3 of its term magnitude while the costs stay within 1e-5 relative
         assert np.median(np.abs(got_costs - ref["costs"]) / np.abs(ref["costs"])) < 1e-5
-        check_control(ctrl.getControlSeq().T, ref, tol=1e-3)
+        check_control(ctrl.getControlSeq().T, ref, rtol=1e-3)
     st = ctrl.getTargetStateSeq().T
     assert np.allclose(st, ref["state_seq"], rtol=1e-4, atol=1e-4)
     ctrl.close()
@@ -318,9 +324,7 @@ def test_cooperative_rollout_bit_identical_for_two_controls():
         ref = oracle.compute_control(ctrl.model_id, ctrl._dyn_arr[0], ctrl._cost_arr[0], ctrl.getParams(),
                                      ctrl.sampler_.to_c(), ctrl.constraints_, K, T, 2, 4, x0, eps, init,
                                      costmap=(cmap, 0.1, (0.0, 0.0)))
-        w = outs[-1][2]
-        big = ref["weights"] > 1e-30
-        assert np.all(np.abs(w[big] - ref["weights"][big]) <= 1e-5 * ref["weights"][big])
+        check_weights(outs[-1][2], ref["weights"])
         check_control(outs[-1][1].T, ref)
         ctrl.close()
     c0, u0, w0, s0 = outs[0]

@@ -1,0 +1,196 @@
+"""Parity at the benchmarked sizes.
+
+* The batched double-integrator benchmark itself (256 instances, K ~ U{512 .. 8192}, T ~ U{32, 64, 128}, colored
+  noise with exponents (1, 1), sigma 0.5, controls clamped to +-1), built as one handle with an injected spectrum,
+  checked in two halves on nine instances, three of each horizon class:
+    - given the engine's own shaped samples (mppi_get_control_samples), the oracle's rollout, weights and update
+      (mppi_controller.cu:162-216) reproduce the per-sample costs bit for bit and the updated control within 1e-5
+      of each element's term magnitude (tests/_parity.py);
+    - the shaping alone (ColoredNoiseDistributionImpl::generateSamples, colored_noise.cu:285-392) against the
+      oracle's FP64 inverse DFT within 1e-5 of the noise scale.
+* The batched surrogate benchmark (128 instances, K ~ U[2048, 16384], T ~ U{50, 100, 200}, FP8 E4M3 weights) as one
+  handle, eight instances against the oracle's FP32 surrogate rollout of the dequantised weights.
+* The engine's slideControlSequence against the oracle's (controller.cuh:370-376, 609-636).
+"""
+import numpy as np
+import pytest
+
+import _parity
+import oracle
+from mppi_generic_vendor_gb300 import (BatchedMPPIController, ColoredNoiseDistribution, DoubleIntegratorDynamics,
+                                       DoubleIntegratorObstacleCost)
+from mppi_generic_vendor_gb300 import _abi as A
+from mppi_generic_vendor_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _pick(Ts, per_class=3):
+    """The first `per_class` instances of every horizon class, in index order."""
+    out = []
+    for t in sorted(set(int(v) for v in Ts)):
+        out += [i for i in range(len(Ts)) if int(Ts[i]) == t][:per_class]
+    return sorted(out)
+
+
+@pytest.fixture(scope="module")
+def colored_headline():
+    wl = W.batched_di(seed=0, num_instances=256, colored=True)
+    ctrl = wl.controller
+    rng = np.random.default_rng(123)
+    Ks, Ts = wl.K.astype(np.int64), wl.T.astype(np.int64)
+    sizes = Ks * 2 * (Ts + 1) * 2
+    spec = rng.standard_normal(int(sizes.sum()), dtype=np.float32)
+    ctrl.injectNoise(spec)
+    init = [rng.uniform(-0.3, 0.3, (int(T), 2)).astype(np.float32) for T in Ts]
+    ctrl.setControlSeqs([u.T for u in init])
+    ctrl.computeControl(wl.x0, 1)
+    out = dict(wl=wl, spec=spec, spec_off=np.concatenate([[0], np.cumsum(sizes)]), init=init,
+               costs=ctrl.sample_costs(), samples=ctrl.control_samples(), control=ctrl.getControlSeqs(),
+               bn=ctrl.baseline_normalizer()[0])
+    yield out
+    ctrl.close()
+
+
+def test_colored_headline_rollout_and_update_on_engine_samples(colored_headline):
+    h = colored_headline
+    wl, ctrl = h["wl"], h["wl"].controller
+    Ks, Ts = wl.K.astype(np.int64), wl.T.astype(np.int64)
+    koff = np.concatenate([[0], np.cumsum(Ks)])
+    uoff = np.concatenate([[0], np.cumsum(Ks * Ts * 2)])
+    checked = _pick(Ts)
+    assert len(checked) >= 9 and {int(Ts[i]) for i in checked} == {32, 64, 128}
+    worst = 0.0
+    for i in checked:
+        K, T = int(Ks[i]), int(Ts[i])
+        s = h["samples"][uoff[i]:uoff[i + 1]]
+        ref = _parity.solve_from_samples(ctrl.model_id, ctrl._dyn_arr[i], ctrl._cost_arr[i], ctrl.getParams(),
+                                         ctrl.sampler_.to_c(), ctrl.constraints_, K, T, 2, 4,
+                                         wl.x0[4 * i:4 * i + 4], s, h["init"][i])
+        got = h["costs"][koff[i]:koff[i + 1]]
+        assert np.array_equal(got.view(np.uint32), ref["costs"].view(np.uint32)), i
+        assert h["bn"][i, 0] == ref["baseline"], i
+        ratio, _ = _parity.check_control(h["control"][i].T, ref, K, T, 2)
+        worst = max(worst, ratio)
+    assert worst <= 1e-5
+
+
+def test_colored_headline_shaping_against_fp64_transform(colored_headline):
+    """Unclamped entries of the engine's samples give back its noise: eps = (u - mean) / sigma for ordinary samples,
+    u / sigma for the zero-mean tail; the oracle's FP64 transform of the same spectrum agrees within 1e-5 of the
+    noise scale (the shaped noise has unit standard deviation per row by construction)."""
+    h = colored_headline
+    wl = h["wl"]
+    Ks, Ts = wl.K.astype(np.int64), wl.T.astype(np.int64)
+    uoff = np.concatenate([[0], np.cumsum(Ks * Ts * 2)])
+    sigma = np.float32(0.5)
+    worst = 0.0
+    for i in _pick(Ts):
+        K, T = int(Ks[i]), int(Ts[i])
+        spec = h["spec"][h["spec_off"][i]:h["spec_off"][i + 1]]
+        eps = oracle.colored_noise(spec, K, T, 2, [1.0, 1.0], fmin=0.0, decay=0.97, offset_t=1).reshape(K, T, 2)
+        u = h["samples"][uoff[i]:uoff[i + 1]].reshape(K, T, 2).astype(np.float64)
+        mean = np.broadcast_to(h["init"][i][None], (K, T, 2)).astype(np.float64).copy()
+        mean[int(np.ceil(0.99 * K)):] = 0.0  # pure-noise tail: (1 - 0.01) K and above
+        est = (u - mean) / sigma
+        ok = np.abs(u) < 1.0  # not clamped
+        ok[0] = False         # sample 0 is the nominal sequence
+        ok[:, :1] = False     # t < stride keeps the nominal control
+        err = np.abs(est - eps)[ok]
+        # the recovered noise carries the rounding of mean + sigma * eps (one ulp of |u| <= 1, over sigma)
+        bound = 1e-5 * max(1.0, float(np.abs(eps).max())) + 2.0 * 2.0 ** -24 / sigma
+        assert err.max() <= bound, (i, err.max(), bound)
+        worst = max(worst, float(err.max()))
+    assert worst > 0.0
+
+
+@pytest.mark.parametrize("T", [32, 64, 128])
+def test_colored_shaping_headline_horizons(T):
+    """The shaping alone at the headline's horizons and largest K, unclamped, zero nominal, sigma 1: engine noise
+    against the oracle's FP64 inverse DFT of the same spectrum, within 1e-5 of each row's largest value."""
+    K, C = 8192, 2
+    rng = np.random.default_rng(T)
+    spec = rng.standard_normal(K * C * (T + 1) * 2, dtype=np.float32)
+    sampler = ColoredNoiseDistribution(std_dev=(1.0, 1.0), exponents=(1.0, 1.0), offset_decay_rate=0.97,
+                                       pure_noise_trajectories_percentage=0.0)
+    ctrl = BatchedMPPIController(DoubleIntegratorDynamics(), [DoubleIntegratorObstacleCost()], sampler, [K], [T])
+    ctrl.injectNoise(spec)
+    ctrl.generateSamples(1, 0)
+    got = ctrl.control_samples().reshape(K, T, C).astype(np.float64)
+    ref = oracle.colored_noise(spec, K, T, C, [1.0, 1.0], fmin=0.0, decay=0.97, offset_t=1).reshape(K, T, C)
+    row_max = np.abs(ref[1:, 1:]).max(axis=1, keepdims=True)
+    err = np.abs(got[1:, 1:] - ref[1:, 1:])
+    assert np.all(err <= 1e-5 * row_max), float((err / row_max).max())
+    ctrl.close()
+
+
+@pytest.fixture(scope="module")
+def fp8_params():
+    return W.train_surrogate(weight_format="fp8")
+
+
+def test_batched_surrogate_fp8_handle_against_oracle(fp8_params):
+    """The 128-instance FP8 surrogate benchmark as one handle (judge off, injected noise): per-sample costs of eight
+    instances across the three horizons against the oracle's FP32 rollout of the dequantised weights, at the
+    tolerances of the single-instance surrogate test (median 5e-3, max 2e-2 relative; the 16-bit activations of the
+    tensor-core path), and the updated controls within 5e-2 of their range."""
+    from test_gpu_mlp import COST_TOL, effective_params
+
+    wl = W.batched_slip_mlp(seed=0, num_instances=128, precision="fp8", params=fp8_params)
+    ctrl = wl.controller
+    ctrl.setJudge(0.0)
+    Ks, Ts = wl.K.astype(np.int64), wl.T.astype(np.int64)
+    rng = np.random.default_rng(77)
+    eps = rng.standard_normal(int((Ks * Ts * 2).sum()), dtype=np.float32)
+    init = [rng.uniform(-0.2, 0.2, (int(T), 2)).astype(np.float32) for T in Ts]
+    ctrl.setControlSeqs([u.T for u in init])
+    ctrl.injectNoise(eps)
+    ctrl.computeControl(wl.x0, 1)
+    costs, ctl = ctrl.sample_costs(), ctrl.getControlSeqs()
+    koff = np.concatenate([[0], np.cumsum(Ks)])
+    eoff = np.concatenate([[0], np.cumsum(Ks * Ts * 2)])
+    cmap = W.gaussian_bump_costmap(0)
+    oracle.set_mlp(effective_params(fp8_params, "fp8"))
+    med_tol, max_tol = COST_TOL["fp8"]
+    checked = _pick(Ts)
+    assert len(checked) >= 8 and {int(Ts[i]) for i in checked} == {50, 100, 200}
+    stats = []
+    for i in checked:
+        K, T = int(Ks[i]), int(Ts[i])
+        ref = oracle.compute_control(A.MODEL_BICYCLE_SLIP_MLP, ctrl._dyn_arr[i], ctrl._cost_arr[i], ctrl.getParams(),
+                                     ctrl.sampler_.to_c(), ctrl.constraints_, K, T, 2, 7, wl.x0[7 * i:7 * i + 7],
+                                     eps[eoff[i]:eoff[i + 1]], init[i], costmap=(cmap, 0.1, (0.0, 0.0)))
+        rel = np.abs(costs[koff[i]:koff[i + 1]] - ref["costs"]) / np.abs(ref["costs"])
+        span = float(np.abs(ref["control"]).max())
+        stats.append((i, T, float(np.median(rel)), float(rel.max()),
+                      float(np.abs(ctl[i].T - ref["control"]).max() / span)))
+    ctrl.close()
+    for i, T, med, mx, cerr in stats:
+        scale = max(1.0, T / 60.0)  # the single-instance tolerances hold at T = 60; drift grows with the horizon
+        assert med <= med_tol * scale and mx <= max_tol * scale and cerr <= 5e-2, stats
+
+
+@pytest.mark.parametrize("steps", [0, 1, 2, 5, 40, 60])
+def test_slide_control_sequence_matches_oracle(steps):
+    """Controller::slideControlSequence on the engine's host copy of every instance against the oracle's
+    slideControlSequenceHelper (controller.cuh:609-621), with a slide scale and zero control that differ per
+    control."""
+    from mppi_generic_vendor_gb300 import GaussianDistribution
+
+    Ts = [50, 32, 17]
+    dyn = DoubleIntegratorDynamics()
+    ctrl = BatchedMPPIController(dyn, [DoubleIntegratorObstacleCost()] * 3, GaussianDistribution(std_dev=(0.5, 0.5)),
+                                 [64, 64, 64], Ts)
+    cp = ctrl.getParams()
+    cp.slide_control_scale[0], cp.slide_control_scale[1] = 0.5, 1.25
+    ctrl.setParams(cp)
+    rng = np.random.default_rng(steps)
+    seqs = [rng.uniform(-1, 1, (T, 2)).astype(np.float32) for T in Ts]
+    ctrl.setControlSeqs([u.T for u in seqs])
+    ctrl.slideControlSequence(steps)
+    got = ctrl.getControlSeqs()
+    zero = np.array([ctrl.constraints_.zero_control[0], ctrl.constraints_.zero_control[1]], np.float32)
+    for u, g in zip(seqs, got):
+        ref = oracle.slide(u, steps, [0.5, 1.25], zero)
+        assert np.array_equal(g.T, ref)
+    ctrl.close()

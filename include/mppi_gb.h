@@ -52,7 +52,9 @@ typedef enum mppi_model
   MPPI_MODEL_DOUBLE_INTEGRATOR = 2,   /* DoubleIntegratorDynamics (di_dynamics.cu:46-53) + goal/obstacle cost */
   MPPI_MODEL_BICYCLE_COSTMAP = 3,     /* kinematic bicycle + bilinear costmap + speed cost (no reference model) */
   MPPI_MODEL_BICYCLE_SLIP = 4,        /* 7-state dynamic bicycle with linear tyres (no reference model) */
-  MPPI_MODEL_BICYCLE_SLIP_MLP = 5     /* same cost, dynamics from the learned MLP surrogate */
+  MPPI_MODEL_BICYCLE_SLIP_MLP = 5,    /* same cost, dynamics from the learned MLP surrogate */
+  MPPI_MODEL_PLUGIN = 100             /* a caller's Dynamics / Cost plugin pair, instantiated by MPPI_GB_PLUGIN
+                                         (mppi_gb_plugin.cuh); created by the plugin library's NAME_create */
 } mppi_model;
 
 typedef enum mppi_sampler_kind
@@ -222,6 +224,13 @@ mppi_status mppi_destroy(mppi_handle* h);
 
 /* Number of instances, and K / T of instance i. */
 mppi_status mppi_get_instance_dims(const mppi_handle* h, int instance, int* num_rollouts, int* num_timesteps);
+/* The handle's model id (MPPI_MODEL_PLUGIN for plugin handles), STATE_DIM, CONTROL_DIM and OUTPUT_DIM (any may be
+ * NULL).  Dynamics::STATE_DIM / CONTROL_DIM / OUTPUT_DIM (dynamics.cuh:75-77) of the handle's plugin. */
+mppi_status mppi_get_model_dims(const mppi_handle* h, int* model, int* state_dim, int* control_dim, int* output_dim);
+/* Wrap an engine that a plugin library built (MPPI_GB_PLUGIN's NAME_create calls this) in a handle of this library.
+ * abi_version must equal MPPI_GB_ABI_VERSION; on success the handle owns the engine (mppi_destroy frees it).  No
+ * counterpart in the reference, whose plugin templates are instantiated inside the caller's own program. */
+mppi_status mppi_handle_adopt(void* engine, int abi_version, mppi_handle** out);
 
 /*
  * One MPC solve for every instance: num_iters x (sample -> rollout -> weights -> update), then the host-side
@@ -257,9 +266,12 @@ mppi_status mppi_get_control_samples(mppi_handle* h, float* out);
  * GPU from their stored, constrained controls.  states[n][T][S] holds the state after each step, step_costs[n][T] the
  * running cost of each step and terminal[n] the terminal cost; the sample's cost is (the step costs summed in step
  * order) / T + terminal / T, bit for bit.  The likelihood-ratio term uses the nominal sequence the solve started
- * from.  Analytic models only (MPPI_EUNSUPPORTED for the surrogate). */
+ * from.  crash_status (may be NULL) receives int[n][T], the sample's crash flag after each step's running cost
+ * (crash_status_d of visualizeKernel, mppi_common.cu:371-376; always 0 for the built-in costs).  For a plugin handle
+ * states holds the outputs (stateToOutput) after each step, [n][T][OUTPUT_DIM].  Analytic models and plugins only
+ * (MPPI_EUNSUPPORTED for the surrogate). */
 mppi_status mppi_get_sampled_trajectories(mppi_handle* h, int instance, const int* idx, int n, float* states,
-                                          float* step_costs, float* terminal);
+                                          float* step_costs, float* terminal, int* crash_status);
 /* Controller::copyTopControlFromDevice's selection (controller.cu:126-181), on the host: the n highest of
  * weights[0..num_samples-1] (the transformed costs, mppi_get_sample_weights), by the reference's replacement scan,
  * in the order of its list slots.  No handle or GPU involved. */

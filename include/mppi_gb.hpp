@@ -345,7 +345,7 @@ public:
     sampled_terminal_.assign((size_t)n, 0.0f);
     if (n > 0)
       check(mppi_get_sampled_trajectories(h_, 0, idx.data(), n, sampled_states_.data(), sampled_costs_.data(),
-                                          sampled_terminal_.data()),
+                                          sampled_terminal_.data(), nullptr),
             "mppi_get_sampled_trajectories");
     top_costs_.clear();
     const float norm = top_n_ > 0 ? getNormalizerCost() : 1.0f;

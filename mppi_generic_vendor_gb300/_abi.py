@@ -13,6 +13,7 @@ MPPI_MAX_CONTROL_DIM = 4
 MPPI_MAX_OBSTACLES = 8
 
 MPPI_OK = 0
+MPPI_EINVAL, MPPI_ECUDA, MPPI_ENAN, MPPI_ETIMEOUT, MPPI_ENOMEM, MPPI_EUNSUPPORTED = 1, 2, 3, 4, 5, 6
 STATUS_NAMES = {0: "MPPI_OK", 1: "MPPI_EINVAL", 2: "MPPI_ECUDA", 3: "MPPI_ENAN", 4: "MPPI_ETIMEOUT",
                 5: "MPPI_ENOMEM", 6: "MPPI_EUNSUPPORTED"}
 
@@ -21,6 +22,7 @@ MODEL_DOUBLE_INTEGRATOR = 2
 MODEL_BICYCLE_COSTMAP = 3
 MODEL_BICYCLE_SLIP = 4
 MODEL_BICYCLE_SLIP_MLP = 5
+MODEL_PLUGIN = 100
 
 SAMPLER_GAUSSIAN = 0
 CONTROLLER_VANILLA, CONTROLLER_COLORED = 0, 1
@@ -118,7 +120,9 @@ SIGNATURES = [
     ("mppi_get_sample_costs", C.c_int, [_P, _FP]),
     ("mppi_get_sample_weights", C.c_int, [_P, _FP]),
     ("mppi_get_control_samples", C.c_int, [_P, _FP]),
-    ("mppi_get_sampled_trajectories", C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_int, _FP, _FP, _FP]),
+    ("mppi_get_sampled_trajectories", C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_int, _FP, _FP, _FP, _IP]),
+    ("mppi_get_model_dims", C.c_int, [_P, _IP, _IP, _IP, _IP]),
+    ("mppi_handle_adopt", C.c_int, [_P, C.c_int, C.POINTER(_P)]),
     ("mppi_select_top_samples", C.c_int, [_FP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     ("mppi_get_free_energy", C.c_int, [_P, C.c_int, _FP]),
     ("mppi_set_dynamics_params", C.c_int, [_P, _P, C.c_size_t]),

@@ -248,9 +248,10 @@ class BatchedMPPIController:
         self.sampler_ = sampler
         self.model_id = self.model_.model_id
         self.S, self.Cdim = self.model_.STATE_DIM, self.model_.CONTROL_DIM
+        self.output_dim = getattr(self.model_, "OUTPUT_DIM", self.S)
         self.K = np.asarray(num_rollouts, dtype=np.int32)
         self.T = np.asarray(num_timesteps, dtype=np.int32)
-        dyn_t, cost_t = A.MODEL_PARAM_TYPES[self.model_id]
+        dyn_t, cost_t = type(dyn_list[0].getParams()), type(cost_list[0].getParams())
         self._dyn_arr = (dyn_t * self.num_instances)(*[d.getParams() for d in dyn_list])
         self._cost_arr = (cost_t * self.num_instances)(*[c.getParams() for c in cost_list])
         cp = A.default_controller_params()
@@ -272,19 +273,24 @@ class BatchedMPPIController:
             init = np.ascontiguousarray(np.asarray(init_control_traj, dtype=np.float32).reshape(-1))
             if init.size != self._t_off[-1]:
                 raise ValueError(f"init_control_traj must hold {self._t_off[-1]} floats")
-        h = C.c_void_p()
         sp = sampler.to_c()
-        A.call("mppi_create", self.model_id, self.num_instances, self.K.ctypes.data_as(C.POINTER(C.c_int)),
-               self.T.ctypes.data_as(C.POINTER(C.c_int)), C.byref(cp), C.byref(sp), C.byref(cc),
-               C.cast(self._dyn_arr, C.c_void_p), C.sizeof(dyn_t), C.cast(self._cost_arr, C.c_void_p),
-               C.sizeof(cost_t), None if init is None else _fptr(init), C.c_void_p(stream or None), C.byref(h))
-        self._h = h
+        self._h = self._create_handle(cp, sp, cc, None if init is None else _fptr(init), stream)
         cm = getattr(self.cost_, "costmap", None)
         if cm is not None:
             self.setCostmap(cm, self.cost_.resolution, self.cost_.origin)
         mlp = getattr(self.model_, "mlp_params", None)
         if mlp is not None:
             self.setMLP(mlp, self.model_.precision)
+
+    def _create_handle(self, cp, sp, cc, init, stream):
+        """mppi_create for a built-in model (VanillaMPPIController's constructor, mppi_controller.cu:16-29)."""
+        h = C.c_void_p()
+        dyn_t, cost_t = type(self._dyn_arr[0]), type(self._cost_arr[0])
+        A.call("mppi_create", self.model_id, self.num_instances, self.K.ctypes.data_as(C.POINTER(C.c_int)),
+               self.T.ctypes.data_as(C.POINTER(C.c_int)), C.byref(cp), C.byref(sp), C.byref(cc),
+               C.cast(self._dyn_arr, C.c_void_p), C.sizeof(dyn_t), C.cast(self._cost_arr, C.c_void_p),
+               C.sizeof(cost_t), init, C.c_void_p(stream or None), C.byref(h))
+        return h
 
     # ---- lifecycle
     def close(self):
@@ -389,16 +395,18 @@ class BatchedMPPIController:
         top = select_top_samples(w, top_n) if top_n > 0 else np.empty(0, np.int32)
         idx = np.ascontiguousarray(np.concatenate([rand, top]).astype(np.int32))
         n = idx.size
-        states = np.empty(max(n, 1) * T * self.S, np.float32)
+        O = self.output_dim
+        states = np.empty(max(n, 1) * T * O, np.float32)
         step_costs = np.empty(max(n, 1) * T, np.float32)
         terminal = np.empty(max(n, 1), np.float32)
+        crash = np.empty(max(n, 1) * T, np.int32)
         if n:
             A.call("mppi_get_sampled_trajectories", self._h, i, idx.ctypes.data_as(C.POINTER(C.c_int)), n,
-                   _fptr(states), _fptr(step_costs), _fptr(terminal))
+                   _fptr(states), _fptr(step_costs), _fptr(terminal), crash.ctypes.data_as(C.POINTER(C.c_int)))
         self.sampled_indices_ = idx
-        self.sampled_trajectories_ = [states[j * T * self.S:(j + 1) * T * self.S].reshape(T, self.S).T.copy()
-                                      for j in range(n)]
+        self.sampled_trajectories_ = [states[j * T * O:(j + 1) * T * O].reshape(T, O).T.copy() for j in range(n)]
         self.sampled_costs_ = [step_costs[j * T:(j + 1) * T].copy() for j in range(n)]
+        self.sampled_crash_status_ = [crash[j * T:(j + 1) * T].copy() for j in range(n)]
         self.sampled_terminal_costs_ = terminal[:n].copy()
         self.top_n_costs_ = w[top] / self.getNormalizerCost(i) if top_n > 0 else np.empty(0, np.float32)
 
@@ -409,6 +417,10 @@ class BatchedMPPIController:
     def getSampledCostTrajectories(self):
         """Running cost of every step of each re-rolled sample."""
         return getattr(self, "sampled_costs_", [])
+
+    def getSampledCrashStatus(self):
+        """Crash flag after every step of each re-rolled sample (crash_status_d of visualizeKernel)."""
+        return getattr(self, "sampled_crash_status_", [])
 
     def getTopTransformedCosts(self):
         """Weights of the top-N samples divided by the normaliser."""

@@ -299,6 +299,31 @@ mppi_status mppi_create(int model, int num_instances, const int* num_rollouts, c
   return MPPI_OK;
 }
 
+mppi_status mppi_handle_adopt(void* engine, int abi_version, mppi_handle** out)
+{
+  clear_error();
+  MG_CHECK(out, "out must not be NULL");
+  *out = nullptr;
+  MG_CHECK(engine, "engine must not be NULL");
+  MG_CHECK(abi_version == MPPI_GB_ABI_VERSION,
+           "the plugin was built against ABI version %d of mppi_gb.h; this library is version %d: rebuild the plugin",
+           abi_version, MPPI_GB_ABI_VERSION);
+  mppi_handle* h = new mppi_handle;
+  h->engine = static_cast<EngineBase*>(engine);
+  *out = h;
+  return MPPI_OK;
+}
+
+mppi_status mppi_get_model_dims(const mppi_handle* h, int* model, int* state_dim, int* control_dim, int* output_dim)
+{
+  HANDLE_OK(h);
+  if (model) *model = h->engine->model();
+  if (state_dim) *state_dim = h->engine->state_dim();
+  if (control_dim) *control_dim = h->engine->control_dim();
+  if (output_dim) *output_dim = h->engine->output_dim();
+  return MPPI_OK;
+}
+
 mppi_status mppi_destroy(mppi_handle* h)
 {
   if (!h) return MPPI_OK;
@@ -362,10 +387,10 @@ mppi_status mppi_get_control_samples(mppi_handle* h, float* out)
   return h->engine->get_control_samples(out);
 }
 mppi_status mppi_get_sampled_trajectories(mppi_handle* h, int instance, const int* idx, int n, float* states,
-                                          float* step_costs, float* terminal)
+                                          float* step_costs, float* terminal, int* crash_status)
 {
   HANDLE_OK(h);
-  return h->engine->get_sampled_trajectories(instance, idx, n, states, step_costs, terminal);
+  return h->engine->get_sampled_trajectories(instance, idx, n, states, step_costs, terminal, crash_status);
 }
 mppi_status mppi_select_top_samples(const float* weights, int num_samples, int n, int* indices)
 {

@@ -22,6 +22,7 @@
 #include "mg_colored.cuh"
 #include "mg_kernels.cuh"
 #include "mg_mlp.cuh"
+#include "mg_plugin.cuh"
 
 namespace mg
 {
@@ -61,7 +62,8 @@ public:
   virtual mppi_status get_sample_weights(float* out) = 0;
   virtual mppi_status get_control_samples(float* out) = 0;
   virtual mppi_status get_sampled_trajectories(int i, const int* idx, int n, float* states, float* step_costs,
-                                               float* terminal) = 0;
+                                               float* terminal, int* crash) = 0;
+  virtual int output_dim() const = 0;
   virtual mppi_status get_free_energy(int i, float* out6) = 0;
   virtual mppi_status set_dynamics_params(const void* p, size_t bytes) = 0;
   virtual mppi_status set_cost_params(const void* p, size_t bytes) = 0;
@@ -164,6 +166,7 @@ public:
 
   int model() const override { return Model::kModelId; }
   int state_dim() const override { return S; }
+  int output_dim() const override { return Model::OUTPUT_DIM; }
   int control_dim() const override { return C; }
   int num_instances() const override { return I_; }
   void dims(int i, int* K, int* T) const override
@@ -315,7 +318,13 @@ public:
       for (int t = 0; t < T - 1; ++t)
       {
         const float* uc = u + (size_t)t * C;
-        if (Model::kMlp && !use_analytic_)
+        if constexpr (Model::kPlugin)
+        {
+          // the plugin's own step (Dynamics::step, dynamics.cu:142-152) on its host twin
+          float xd[S], y[Model::OUTPUT_DIM];
+          dyn_[i].step(x, xn, xd, uc, y, t, cp_.dt);
+        }
+        else if (Model::kMlp && !use_analytic_)
         {
           float xd[S];
           mlp_host_dynamics(mlp_host_.data(), x, uc, xd);
@@ -378,7 +387,7 @@ public:
   // of instance i of the last solve, re-rolled on the GPU.  The likelihood-ratio term uses the nominal sequence the
   // solve started from (the samples' own nominal when num_iters is 1).
   mppi_status get_sampled_trajectories(int i, const int* idx, int n, float* states, float* step_costs,
-                                       float* terminal) override
+                                       float* terminal, int* crash) override
   {
     MG_CHECK(i >= 0 && i < I_, "instance %d out of range", i);
     MG_CHECK(n >= 0, "n must be >= 0");
@@ -394,10 +403,12 @@ public:
     else
     {
       const int T = T_[i];
-      DevBuf<int> idx_d;
+      constexpr int SO = Model::kPlugin ? Model::OUTPUT_DIM : S;  // plugins report outputs, the others states
+      DevBuf<int> idx_d, crash_d;
       DevBuf<float> st_d, c_d, term_d, mean0_d;
       MG_TRY(idx_d.alloc(n));
-      MG_TRY(st_d.alloc((size_t)n * T * S));
+      MG_TRY(crash_d.alloc((size_t)n * T));
+      MG_TRY(st_d.alloc((size_t)n * T * SO));
       MG_TRY(c_d.alloc((size_t)n * T));
       MG_TRY(term_d.alloc(n));
       MG_TRY(mean0_d.alloc(control_.size()));
@@ -406,11 +417,22 @@ public:
       MG_CUDA(cudaMemcpy(mean0_d.p, mean_h_.p, sizeof(float) * control_.size(), cudaMemcpyHostToDevice));
       RolloutArgs<Model> a = base_rollout_args();
       a.mean = mean0_d.p;
-      sampled_trajectories_kernel<Model><<<(n + 127) / 128, 128, 0, stream_>>>(a, i, idx_d.p, n, st_d.p, c_d.p,
-                                                                                 term_d.p);
+      if constexpr (Model::kPlugin)
+      {
+        sampled_trajectories_plugin_kernel<Model><<<(n + 127) / 128, 128, 0, stream_>>>(
+            a, i, idx_d.p, n, st_d.p, c_d.p, term_d.p, crash_d.p);
+      }
+      else
+      {
+        // the built-in costs never set a crash flag
+        MG_CUDA(cudaMemsetAsync(crash_d.p, 0, sizeof(int) * (size_t)n * T, stream_));
+        sampled_trajectories_kernel<Model><<<(n + 127) / 128, 128, 0, stream_>>>(a, i, idx_d.p, n, st_d.p, c_d.p,
+                                                                                   term_d.p);
+      }
       MG_CUDA(cudaGetLastError());
       MG_CUDA(cudaStreamSynchronize(stream_));
-      MG_CUDA(cudaMemcpy(states, st_d.p, sizeof(float) * n * T * S, cudaMemcpyDeviceToHost));
+      MG_CUDA(cudaMemcpy(states, st_d.p, sizeof(float) * n * T * SO, cudaMemcpyDeviceToHost));
+      if (crash) MG_CUDA(cudaMemcpy(crash, crash_d.p, sizeof(int) * n * T, cudaMemcpyDeviceToHost));
       MG_CUDA(cudaMemcpy(step_costs, c_d.p, sizeof(float) * n * T, cudaMemcpyDeviceToHost));
       MG_CUDA(cudaMemcpy(terminal, term_d.p, sizeof(float) * n, cudaMemcpyDeviceToHost));
       return MPPI_OK;
@@ -896,7 +918,7 @@ private:
     MG_CUDA(cudaGetLastError());
     max_t_ = *std::max_element(T_.begin(), T_.end());  // sizes per-launch shared buffers (split cost kernel)
     if (Model::kMlp) ns_ = kMlpSamplesPerCta;
-    if constexpr ((4 % C) == 0)
+    if constexpr ((4 % C) == 0 && !Model::kPlugin)
     {
       MG_TRY(allow_fused_stage<32>());
       MG_TRY(allow_fused_stage<64>());
@@ -1211,6 +1233,20 @@ private:
   template <int NS>
   mppi_status occupancy_ns(int* per_sm)
   {
+    if constexpr (Model::kPlugin)
+    {
+      MG_CUDA(resident_ctas_per_sm(rollout_plugin_kernel<Model, NS, RolloutShape<NS, C>::TCH>, NS, 0, per_sm));
+      if (*per_sm < 1) *per_sm = 1;
+      return MPPI_OK;
+    }
+    else
+    {
+      return occupancy_builtin<NS>(per_sm);
+    }
+  }
+  template <int NS>
+  mppi_status occupancy_builtin(int* per_sm)
+  {
     if constexpr ((4 % C) == 0)
       if (fused())
       {
@@ -1314,7 +1350,7 @@ private:
   // Gaussian noise is generated inside the rollout (rollout_fused_kernel) when every row holds whole quads of steps;
   // the standalone sampler then runs only for mppi_generate_samples.
   // Gaussian sampling can run inside the rollout kernels (every row holds whole control quads) ...
-  bool fusable() const { return sp_.kind == MPPI_SAMPLER_GAUSSIAN && (4 % C) == 0 && use_bulk_; }
+  bool fusable() const { return !Model::kPlugin && sp_.kind == MPPI_SAMPLER_GAUSSIAN && (4 % C) == 0 && use_bulk_; }
   // ... and does, unless rollout mode 3 asks for the separate sampler kernel.
   bool fused() const { return fusable() && rollout_mode_ != 3; }
 
@@ -1377,6 +1413,37 @@ private:
   }
 
   mppi_status launch_rollout(int stride, int iter)
+  {
+    if constexpr (Model::kPlugin)
+    {
+      RolloutArgs<Model> a = base_rollout_args();
+      a.tr.partials = tile_part_d_.p;
+      a.tr.poff = tile_poff_d_.p;
+      a.tr.sums = tile_sums_d_.p;
+      a.tr.tmin = tile_min_d_.p;
+      a.tr.lambda_inv = 1.0f / cp_.lambda;
+      if (!tile_reduce_active()) a.tr.partials = nullptr;
+      switch (ns_)
+      {
+        case 32: launch_plugin_ns<32>(a); break;
+        case 64: launch_plugin_ns<64>(a); break;
+        case 128: launch_plugin_ns<128>(a); break;
+        default: launch_plugin_ns<256>(a); break;
+      }
+      MG_CUDA(cudaGetLastError());
+      return MPPI_OK;
+    }
+    else
+    {
+      return launch_rollout_builtin(stride, iter);
+    }
+  }
+  template <int NS>
+  void launch_plugin_ns(const RolloutArgs<Model>& a)
+  {
+    rollout_plugin_kernel<Model, NS, RolloutShape<NS, C>::TCH><<<rollout_grid_, NS, 0, stream_>>>(a);
+  }
+  mppi_status launch_rollout_builtin(int stride, int iter)
   {
     RolloutArgs<Model> a = base_rollout_args();
     if (tile_reduce_active())

@@ -95,6 +95,7 @@ struct CartpoleModel
   static constexpr int kModelId = MPPI_MODEL_CARTPOLE;
   static constexpr bool kNeedsCostmap = false;
   static constexpr bool kMlp = false;
+  static constexpr bool kPlugin = false;
   static constexpr int kFlopsPerStep = 60;  // counted from the source below (sin/cos polynomial included)
   using DynParams = mppi_cartpole_params;
   using CostParams = mppi_cartpole_cost_params;
@@ -140,6 +141,7 @@ struct DoubleIntegratorModel
   static constexpr int kModelId = MPPI_MODEL_DOUBLE_INTEGRATOR;
   static constexpr bool kNeedsCostmap = false;
   static constexpr bool kMlp = false;
+  static constexpr bool kPlugin = false;
   static constexpr int kFlopsPerStep = 8 + 11 + 8 * 6;
   using DynParams = mppi_double_integrator_params;
   using CostParams = mppi_di_obstacle_cost_params;
@@ -192,6 +194,7 @@ struct BicycleCostmapModel
   static constexpr int kModelId = MPPI_MODEL_BICYCLE_COSTMAP;
   static constexpr bool kNeedsCostmap = true;
   static constexpr bool kMlp = false;
+  static constexpr bool kPlugin = false;
   static constexpr int kFlopsPerStep = 2 * 22 + 12 + 25;
   using DynParams = mppi_bicycle_params;
   using CostParams = mppi_costmap_cost_params;
@@ -235,6 +238,7 @@ struct BicycleSlipModel
   static constexpr int kModelId = MPPI_MODEL_BICYCLE_SLIP;
   static constexpr bool kNeedsCostmap = true;
   static constexpr bool kMlp = false;
+  static constexpr bool kPlugin = false;
   static constexpr int kFlopsPerStep = 3 * 22 + 45 + 25;
   using DynParams = mppi_bicycle_slip_params;
   using CostParams = mppi_costmap_cost_params;

@@ -378,6 +378,17 @@ static inline R likelihood_cost(const R* u, const float* mean_t, const mppi_samp
   return (R)0.5 * lambda * ((R)1 - alpha) * cost;
 }
 
+// Models that carry a crash flag through the rollout (the plugin-test pair) step themselves and take the flag in
+// their running cost.
+template <class M_, class = void>
+struct HasCrash : std::false_type
+{
+};
+template <class M_>
+struct HasCrash<M_, std::void_t<decltype(M_::kCrash)>> : std::true_type
+{
+};
+
 // ------------------------------------------------------------------------------------------------ rollout
 // Per-sample rollout in the order of rolloutKernel (mppi_common.cu:105-152) and its host twin launchCPURolloutKernel
 // (tests/include/kernel_tests/core/rollout_kernel_test.cu:504-541): read u, enforce constraints, write u back, Euler
@@ -396,6 +407,7 @@ static void rollout_range(const Model& m, const float* x0, float* controls, bool
     R x[MPPI_MAX_STATE_DIM], xn[MPPI_MAX_STATE_DIM], xd[MPPI_MAX_STATE_DIM], u[MPPI_MAX_CONTROL_DIM];
     for (int i = 0; i < S; ++i) x[i] = (R)x0[i];
     R running = 0;
+    int crash = 0;  // crash_status (mppi_common.cu:85-86): zero at the start of every rollout
     for (int t = 0; t < T; ++t)
     {
       float* uk = controls + ((size_t)k * T + t) * C;
@@ -405,9 +417,19 @@ static void rollout_range(const Model& m, const float* x0, float* controls, bool
         if (write_back) uk[i] = uc;
         u[i] = (R)uc;
       }
-      m.deriv(x, u, xd);
-      for (int i = 0; i < S; ++i) xn[i] = M<R>::fma(xd[i], (R)dt, x[i]);
-      R step_cost = m.state_cost(xn, t) + m.control_cost(u, t);
+      R step_cost;
+      if constexpr (HasCrash<Model>::value)
+      {
+        // plugin pair: its own step, and computeRunningCost with the sample's crash flag
+        m.step(x, u, xn, (R)dt);
+        step_cost = m.running_cost(xn, u, t, &crash);
+      }
+      else
+      {
+        m.deriv(x, u, xd);
+        for (int i = 0; i < S; ++i) xn[i] = M<R>::fma(xd[i], (R)dt, x[i]);
+        step_cost = m.state_cost(xn, t) + m.control_cost(u, t);
+      }
       if (use_likelihood) step_cost += likelihood_cost<R>(u, mean + (size_t)t * C, sp, C, k, K, (R)lambda, (R)alpha);
       running += step_cost;
       if (traj_out)
@@ -480,6 +502,79 @@ struct BicycleSlipMLP : BicycleSlip<R>
   }
 };
 
+// The plugin pair of the engine's plugin tests (tests/plugins/di_plugins.cu), restated: DoubleIntegratorDynamics
+// (di_dynamics.cu:46-53) with an optional linear damping, stepped by the default Euler update or (symplectic) by the
+// plugin's own step override (velocity first, then position with the new velocity); QuadraticCostImpl's device
+// state cost (quadratic_cost.cu:35-48, the square written as a product) with a crash wall: once x > wall_x the
+// sample's crash flag stays set and every later step pays crash_cost (the crash argument of computeRunningCost,
+// cost.cuh:221-222).
+struct mppi_test_di_plugin
+{
+  float damping;
+};
+struct mppi_test_quad_wall_cost
+{
+  float s_goal[4];
+  float s_coeffs[4];
+  float wall_x;
+  float crash_cost;
+  float terminal_coeff;
+};
+constexpr int kTestPluginEuler = 101, kTestPluginSymplectic = 102;
+
+template <class R>
+struct TestDIPlugin
+{
+  static const int S = 4, C = 2;
+  static constexpr bool kCrash = true;
+  const mppi_test_di_plugin& p;
+  const mppi_test_quad_wall_cost& q;
+  bool symplectic;
+  void deriv(const R* x, const R* u, R* xd) const
+  {
+    xd[0] = x[2];
+    xd[1] = x[3];
+    xd[2] = u[0] - (R)p.damping * x[2];
+    xd[3] = u[1] - (R)p.damping * x[3];
+  }
+  void step(const R* x, const R* u, R* xn, R dt) const
+  {
+    R xd[4];
+    deriv(x, u, xd);
+    if (symplectic)
+    {
+      xn[2] = M<R>::fma(xd[2], dt, x[2]);
+      xn[3] = M<R>::fma(xd[3], dt, x[3]);
+      xn[0] = M<R>::fma(xn[2], dt, x[0]);
+      xn[1] = M<R>::fma(xn[3], dt, x[1]);
+    }
+    else
+    {
+      for (int i = 0; i < 4; ++i) xn[i] = M<R>::fma(xd[i], dt, x[i]);
+    }
+  }
+  R quad(const R* y) const
+  {
+    R cost = 0;
+    for (int i = 0; i < 4; ++i)
+    {
+      const R e = y[i] - (R)q.s_goal[i];
+      cost += e * e * (R)q.s_coeffs[i];
+    }
+    return cost;
+  }
+  R running_cost(const R* y, const R*, int, int* crash) const
+  {
+    R cost = quad(y);
+    if (y[0] > (R)q.wall_x) *crash = 1;
+    if (*crash) cost += (R)q.crash_cost;
+    return cost;
+  }
+  R state_cost(const R* y, int) const { return quad(y); }
+  R control_cost(const R*, int) const { return (R)0; }
+  R terminal_cost(const R* y) const { return quad(y) * (R)q.terminal_coeff; }
+};
+
 struct ModelBlob
 {
   int model;
@@ -524,6 +619,14 @@ static void with_model(const ModelBlob& b, F&& f)
       f(m);
       break;
     }
+    case kTestPluginEuler:
+    case kTestPluginSymplectic:
+    {
+      TestDIPlugin<R> m{ *(const mppi_test_di_plugin*)b.dyn, *(const mppi_test_quad_wall_cost*)b.cost,
+                         b.model == kTestPluginSymplectic };
+      f(m);
+      break;
+    }
     default: break;
   }
 }
@@ -537,6 +640,8 @@ static int model_state_dim(int model)
     case MPPI_MODEL_BICYCLE_COSTMAP: return 4;
     case MPPI_MODEL_BICYCLE_SLIP: return 7;
     case MPPI_MODEL_BICYCLE_SLIP_MLP: return g_mlp_d.empty() ? 0 : 7;
+    case kTestPluginEuler: return 4;
+    case kTestPluginSymplectic: return 4;
     default: return 0;
   }
 }
@@ -549,6 +654,8 @@ static int model_control_dim(int model)
     case MPPI_MODEL_BICYCLE_COSTMAP: return 2;
     case MPPI_MODEL_BICYCLE_SLIP: return 2;
     case MPPI_MODEL_BICYCLE_SLIP_MLP: return 2;
+    case kTestPluginEuler: return 2;
+    case kTestPluginSymplectic: return 2;
     default: return 0;
   }
 }
@@ -1000,12 +1107,17 @@ int orc_compute_control(int model, const void* dyn, const void* cost, const floa
       {
         // the constraint inside computeOutputTrajectoryHelper (controller.cuh:676-680)
         for (int i = 0; i < C; ++i) u[i] = orc::enforce_constraint(control[(size_t)t * C + i], *cc, i);
-        m.deriv(x, u, xd);
-        for (int i = 0; i < S; ++i)
+        float xn[MPPI_MAX_STATE_DIM];
+        if constexpr (orc::HasCrash<std::decay_t<decltype(m)>>::value)
         {
-          x[i] = fmaf(xd[i], cp->dt, x[i]);
-          state_seq_out[(size_t)(t + 1) * S + i] = x[i];
+          m.step(x, u, xn, cp->dt);
         }
+        else
+        {
+          m.deriv(x, u, xd);
+          for (int i = 0; i < S; ++i) xn[i] = fmaf(xd[i], cp->dt, x[i]);
+        }
+        for (int i = 0; i < S; ++i) x[i] = state_seq_out[(size_t)(t + 1) * S + i] = xn[i];
       }
     });
   }

@@ -41,14 +41,21 @@ def _solve(ctrl, K, T, rng, x0, x0_oracle=None):
     return ref
 
 
-@pytest.mark.parametrize("gamma,r", [(50.0, 2.0), (400.0, 1.5), (20.0, 3.0)])
-def test_tsallis_weights_and_update_match_oracle(gamma, r):
+@pytest.mark.parametrize("frac,r", [(0.3, 2.0), (0.05, 1.5), (0.8, 3.0)])
+def test_tsallis_weights_and_update_match_oracle(frac, r):
+    """gamma is set to a fraction of the sampled cost spread, so part of the samples get weight exactly zero."""
     K, T = 4096, 64
     ctrl = _controller(ColoredMPPIController, K, T)
+    x0 = np.array([-3.0, 2.0, 0.5, -0.2], np.float32)
+    state = np.random.default_rng(int(100 * frac)).bit_generator.state
+    rng = np.random.default_rng()
+    rng.bit_generator.state = state
+    _solve(ctrl, K, T, rng, x0)  # exponential weights: only to read the cost spread of these samples
+    c = ctrl.sample_costs()
+    gamma = float(frac * (c.max() - c.min()))
     ctrl.setGamma(gamma)
     ctrl.setRExp(r)
-    rng = np.random.default_rng(int(gamma))
-    x0 = np.array([-3.0, 2.0, 0.5, -0.2], np.float32)
+    rng.bit_generator.state = state  # the same noise and initial sequence again
     ref = _solve(ctrl, K, T, rng, x0)
     got = ctrl.sample_costs()
     assert np.array_equal(got.view(np.uint32), ref["costs"].view(np.uint32))

@@ -419,5 +419,5 @@ def test_sampled_trajectories_reject_bad_indices():
     with pytest.raises(MPPIError):
         A.call("mppi_get_sampled_trajectories", ctrl._h, 0, bad.ctypes.data_as(C.POINTER(C.c_int)), 2,
                out.ctypes.data_as(C.POINTER(C.c_float)), out.ctypes.data_as(C.POINTER(C.c_float)),
-               out.ctypes.data_as(C.POINTER(C.c_float)))
+               out.ctypes.data_as(C.POINTER(C.c_float)), None)
     ctrl.close()

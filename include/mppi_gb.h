@@ -67,8 +67,18 @@ typedef enum mppi_sampler_kind
 typedef enum mppi_controller_kind
 {
   MPPI_CONTROLLER_VANILLA = 0, /* VanillaMPPIController (mppi_controller.cu:152-237) */
-  MPPI_CONTROLLER_COLORED = 1  /* ColoredMPPIController (colored_mppi_controller.cu:145-249): Tsallis weights when
+  MPPI_CONTROLLER_COLORED = 1, /* ColoredMPPIController (colored_mppi_controller.cu:145-249): Tsallis weights when
                                   tsallis_gamma != 0 and tsallis_r != 0, state leash, final clamp of control 1 only */
+  MPPI_CONTROLLER_TUBE = 2     /* TubeMPPIController (tube_mppi_controller.cu:158-296): the handle holds exactly two
+                                  instances of equal K and T, the reference's two sampling distributions
+                                  [D = 2][K][T][C]: instance 0 is the actual system, rolled out from the state
+                                  given to mppi_compute_control (STATE_DIM floats), instance 1 the nominal system,
+                                  rolled out from the handle's nominal state (the first state given, then advanced
+                                  one step along the nominal sequence by every slide).  After each iteration the
+                                  nominal pair takes over the actual pair's state and control sequences when the
+                                  actual baseline is below the nominal baseline + nominal_threshold.  Only the
+                                  nominal sequence is smoothed; neither is clamped.  The ancillary feedback
+                                  controller is not part of this engine. */
 } mppi_controller_kind;
 
 /* ControllerParams (include/mppi/controllers/controller.cuh:46-68) and the fields ColoredMPPIParams adds
@@ -88,6 +98,7 @@ typedef struct mppi_controller_params
   int leash_active;  /* ColoredMPPIController::leash_active_ (default 0); the leash holds x0 near the nominal state
                         at the step the last slideControlSequence moved by (leash_jump_, 1 before any slide) */
   float state_leash_dist[MPPI_MAX_STATE_DIM]; /* ColoredMPPIParams::state_leash_dist_ (default 0) */
+  float nominal_threshold; /* TubeMPPIParams::nominal_threshold_ (tube_mppi_controller.cuh:20, default 20) */
 } mppi_controller_params;
 
 /* GaussianParamsImpl (gaussian.cuh:21-61) and ColoredNoiseParamsImpl (colored_noise.cuh:44-73). */
@@ -276,6 +287,9 @@ mppi_status mppi_get_sampled_trajectories(mppi_handle* h, int instance, const in
  * weights[0..num_samples-1] (the transformed costs, mppi_get_sample_weights), by the reference's replacement scan,
  * in the order of its list slots.  No handle or GPU involved. */
 mppi_status mppi_select_top_samples(const float* weights, int num_samples, int n, int* indices);
+/* Tube-MPPI handles: 1 if the last iteration kept the nominal system (its baseline was not beaten by the actual
+ * system's, FreeEnergyStatistics::nominal_state_used), else 0. */
+mppi_status mppi_get_nominal_state_used(mppi_handle* h, int* used);
 /* Free-energy statistics of instance i (MPPIFreeEnergyStatistics, controller.cuh:22-38; computeFreeEnergy,
  * mppi_common.cu:1101-1117): out[0..5] = mean, variance, modified variance, normaliser percent, increase,
  * previous baseline. */

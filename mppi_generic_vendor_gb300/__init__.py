@@ -6,13 +6,13 @@ the host-side mirror of the reference's interface.  Build the library with ``pyt
 from . import _abi
 from ._abi import MPPIError
 from . import nn_io
-from .controller import (BatchedMPPIController, BicycleDynamics, ColoredMPPIController, BicycleSlipDynamics, BicycleSlipMLPDynamics,
+from .controller import (BatchedMPPIController, BicycleDynamics, ColoredMPPIController, TubeMPPIController, BicycleSlipDynamics, BicycleSlipMLPDynamics,
                          CartpoleDynamics,
                          CartpoleSwingupCost, ColoredNoiseDistribution, CostmapCost, DoubleIntegratorDynamics,
                          DoubleIntegratorObstacleCost, GaussianDistribution, VanillaMPPIController,
                          select_top_samples)
 
-__all__ = ["MPPIError", "BatchedMPPIController", "VanillaMPPIController", "ColoredMPPIController", "CartpoleDynamics", "CartpoleSwingupCost",
+__all__ = ["MPPIError", "BatchedMPPIController", "VanillaMPPIController", "ColoredMPPIController", "TubeMPPIController", "CartpoleDynamics", "CartpoleSwingupCost",
            "DoubleIntegratorDynamics", "DoubleIntegratorObstacleCost", "BicycleDynamics", "BicycleSlipDynamics",
            "BicycleSlipMLPDynamics",
            "CostmapCost", "GaussianDistribution", "ColoredNoiseDistribution", "select_top_samples", "_abi", "nn_io"]

@@ -25,7 +25,7 @@ MODEL_BICYCLE_SLIP_MLP = 5
 MODEL_PLUGIN = 100
 
 SAMPLER_GAUSSIAN = 0
-CONTROLLER_VANILLA, CONTROLLER_COLORED = 0, 1
+CONTROLLER_VANILLA, CONTROLLER_COLORED, CONTROLLER_TUBE = 0, 1, 2
 SAMPLER_COLORED_NOISE = 1
 
 _F4 = C.c_float * MPPI_MAX_CONTROL_DIM
@@ -36,7 +36,7 @@ class ControllerParams(C.Structure):
     _fields_ = [("dt", C.c_float), ("lambda_", C.c_float), ("alpha", C.c_float), ("num_timesteps", C.c_int),
                 ("num_iters", C.c_int), ("seed", C.c_uint64), ("slide_control_scale", _F4), ("controller", C.c_int),
                 ("tsallis_r", C.c_float), ("tsallis_gamma", C.c_float), ("leash_active", C.c_int),
-                ("state_leash_dist", C.c_float * MPPI_MAX_STATE_DIM)]
+                ("state_leash_dist", C.c_float * MPPI_MAX_STATE_DIM), ("nominal_threshold", C.c_float)]
 
 
 class SamplingParams(C.Structure):
@@ -122,6 +122,7 @@ SIGNATURES = [
     ("mppi_get_control_samples", C.c_int, [_P, _FP]),
     ("mppi_get_sampled_trajectories", C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_int, _FP, _FP, _FP, _IP]),
     ("mppi_get_model_dims", C.c_int, [_P, _IP, _IP, _IP, _IP]),
+    ("mppi_get_nominal_state_used", C.c_int, [_P, _IP]),
     ("mppi_handle_adopt", C.c_int, [_P, C.c_int, C.POINTER(_P)]),
     ("mppi_select_top_samples", C.c_int, [_FP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     ("mppi_get_free_energy", C.c_int, [_P, C.c_int, _FP]),
@@ -237,6 +238,7 @@ def default_controller_params(native: bool = True) -> ControllerParams:
     else:
         p.dt, p.lambda_, p.alpha, p.num_timesteps, p.num_iters, p.seed = 0.02, 1.0, 0.0, 100, 1, 0
         p.controller, p.tsallis_r, p.tsallis_gamma, p.leash_active = CONTROLLER_VANILLA, 2.0, 0.0, 0
+        p.nominal_threshold = 20.0
     return p
 
 

@@ -646,3 +646,63 @@ class ColoredMPPIController(VanillaMPPIController):
     def setNoiseDecay(self, decay):
         self.sampler_.std_dev_decay = float(decay)
         self.setSamplingParams(self.sampler_)
+
+
+class TubeMPPIController(BatchedMPPIController):
+    """TubeMPPIController(model, cost, fb_controller, sampler, dt, max_iter, lambda, alpha, num_timesteps,
+    num_rollouts, ...) (controllers/Tube-MPPI/tube_mppi_controller.cuh:29-141): two sampling distributions of
+    num_rollouts samples each, the actual system (instance 0, rolled out from the state given to computeControl) and
+    the nominal system (instance 1, from the nominal state the controller keeps); the nominal pair takes over the
+    actual pair's sequences when the actual baseline beats the nominal one by nominal_threshold.  The ancillary
+    feedback controller (fb_controller) is not part of this engine."""
+
+    def __init__(self, model, cost, fb_controller, sampler, dt, max_iter, lambda_, alpha, num_timesteps,
+                 num_rollouts, init_control_traj=None, stream=0, seed=0, nominal_threshold=20.0):
+        del fb_controller
+        init = None
+        if init_control_traj is not None:
+            one = np.asarray(init_control_traj, dtype=np.float32).reshape(model.CONTROL_DIM, num_timesteps).T
+            init = np.concatenate([one.reshape(-1), one.reshape(-1)])
+        super().__init__(model, cost, sampler, [num_rollouts] * 2, [num_timesteps] * 2, dt=dt, max_iter=max_iter,
+                         lambda_=lambda_, alpha=alpha, seed=seed, init_control_traj=init, stream=stream)
+        cp = self.getParams()
+        cp.controller = A.CONTROLLER_TUBE
+        cp.nominal_threshold = float(nominal_threshold)
+        self.setParams(cp)
+
+    def computeControl(self, state, optimization_stride=1):
+        """TubeMPPIController::computeControl (tube_mppi_controller.cu:158-296); state: the actual system's."""
+        x = np.ascontiguousarray(np.asarray(state, dtype=np.float32).reshape(-1))
+        if x.size != self.S:
+            raise ValueError(f"state must hold {self.S} floats")
+        A.call("mppi_compute_control", self._h, _fptr(x), int(optimization_stride))
+
+    def getControlSeq(self) -> np.ndarray:
+        return self.getControlSeqs()[0]
+
+    def getNominalControlSeq(self) -> np.ndarray:
+        return self.getControlSeqs()[1]
+
+    def setControlSeq(self, seq):
+        s = np.asarray(seq, np.float32)
+        self.setControlSeqs([s, s])
+
+    def getTargetStateSeq(self) -> np.ndarray:
+        return self.getTargetStateSeqs()[0]
+
+    def getNominalStateSeq(self) -> np.ndarray:
+        return self.getTargetStateSeqs()[1]
+
+    def getNominalThreshold(self) -> float:
+        return float(self.params_.nominal_threshold)
+
+    def setNominalThreshold(self, threshold):
+        cp = self.getParams()
+        cp.nominal_threshold = float(threshold)
+        self.setParams(cp)
+
+    def nominalStateUsed(self) -> int:
+        """FreeEnergyStatistics::nominal_state_used of the last computeControl."""
+        v = C.c_int()
+        A.call("mppi_get_nominal_state_used", self._h, C.byref(v))
+        return v.value

@@ -228,6 +228,7 @@ void mppi_default_controller_params(mppi_controller_params* p)
   p->tsallis_r = 2.0f;  // ColoredMPPIParams defaults (colored_mppi_controller.cuh:17-22)
   p->tsallis_gamma = 0.0f;
   p->leash_active = 0;
+  p->nominal_threshold = 20.0f;  // TubeMPPIParams (tube_mppi_controller.cuh:20)
 }
 
 void mppi_default_sampling_params(mppi_sampling_params* p)
@@ -322,6 +323,13 @@ mppi_status mppi_get_model_dims(const mppi_handle* h, int* model, int* state_dim
   if (control_dim) *control_dim = h->engine->control_dim();
   if (output_dim) *output_dim = h->engine->output_dim();
   return MPPI_OK;
+}
+
+mppi_status mppi_get_nominal_state_used(mppi_handle* h, int* used)
+{
+  HANDLE_OK(h);
+  MG_CHECK(used, "used must not be NULL");
+  return h->engine->nominal_state_used(used);
 }
 
 mppi_status mppi_destroy(mppi_handle* h)

@@ -89,6 +89,7 @@ public:
   virtual mppi_status set_judge(float fraction) = 0;
   virtual mppi_status get_judge_stats(float* out) = 0;
   virtual mppi_status use_analytic(int enable) = 0;
+  virtual mppi_status nominal_state_used(int* used) = 0;
 };
 
 // Factories, one per model translation unit.
@@ -184,10 +185,11 @@ public:
       for (int k = 0; k < 5; ++k) sampler += class_begin_[k + 1] > class_begin_[k] ? 1 : 0;
     }
     const int judge = (Model::kMlp && !use_analytic_ && judge_total_ > 0) ? 3 : 0;
-    if (tail_finalize()) return cp_.num_iters;  // one fused rollout per iteration, nothing else
+    const int iters = tube() ? 1 : cp_.num_iters;  // Tube-MPPI runs its iterations one graph launch at a time
+    if (tail_finalize()) return iters;  // one fused rollout per iteration, nothing else
     if (fused()) sampler = 0;
     if (fused() && split_) sampler = 1;  // the cost kernel
-    return (sampler + 2 + judge) * cp_.num_iters + 1;  // + the smoothing / constraint kernel
+    return (sampler + 2 + judge) * iters + (tube() ? 0 : 1);  // + the smoothing / constraint kernel
   }
 
   // ------------------------------------------------------------------------------------------------ computeControl
@@ -195,6 +197,7 @@ public:
   {
     MG_CHECK(x0 != nullptr, "x0 must not be NULL");
     MG_CHECK(stride >= 0, "optimization_stride must be >= 0");
+    if (tube()) return compute_control_tube(x0, stride);
     MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
     MG_CHECK(!Model::kMlp || use_analytic_ || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
     for (int i = 0; i < I_ * S; ++i)
@@ -261,6 +264,12 @@ public:
   {
     MG_CHECK(steps >= 0, "steps must be >= 0");
     leash_jump_ = steps;  // ColoredMPPIController::slideControlSequence (colored_mppi_controller.cu:260-268)
+    if (tube())
+    {
+      // TubeMPPIController::slideControlSequence (tube_mppi_controller.cu:313-324): the nominal state advances one
+      // step along the nominal sequence (Dynamics::step, no constraint), then both sequences slide
+      if (nominal_init_) advance_nominal_state();
+    }
     for (int i = 0; i < I_; ++i)
     {
       float* u = control_.data() + t_off_[i];
@@ -515,8 +524,13 @@ public:
     MG_CHECK(cp.num_iters >= 1, "num_iters must be >= 1");
     MG_CHECK(cp.lambda > 0.0f && std::isfinite(cp.lambda), "lambda must be positive");
     MG_CHECK(std::isfinite(cp.dt), "dt must be finite");
-    MG_CHECK(cp.controller == MPPI_CONTROLLER_VANILLA || cp.controller == MPPI_CONTROLLER_COLORED,
-             "controller must be MPPI_CONTROLLER_VANILLA (0) or MPPI_CONTROLLER_COLORED (1)");
+    MG_CHECK(cp.controller == MPPI_CONTROLLER_VANILLA || cp.controller == MPPI_CONTROLLER_COLORED ||
+                 cp.controller == MPPI_CONTROLLER_TUBE,
+             "controller must be MPPI_CONTROLLER_VANILLA (0), MPPI_CONTROLLER_COLORED (1) or MPPI_CONTROLLER_TUBE (2)");
+    MG_CHECK(std::isfinite(cp.nominal_threshold), "nominal_threshold must be finite");
+    if (cp.controller == MPPI_CONTROLLER_TUBE && !K_.empty())
+      MG_CHECK(I_ == 2 && K_[0] == K_[1] && T_[0] == T_[1],
+               "a Tube-MPPI handle holds two instances of equal num_rollouts and num_timesteps (actual, nominal)");
     MG_CHECK(std::isfinite(cp.tsallis_gamma) && std::isfinite(cp.tsallis_r), "tsallis_gamma and tsallis_r must be "
              "finite");
     MG_CHECK(cp.controller != MPPI_CONTROLLER_COLORED || cp.tsallis_gamma == 0.0f || cp.tsallis_r != 1.0f,
@@ -711,6 +725,164 @@ public:
     return MPPI_OK;
   }
 
+  // ------------------------------------------------------------------------------------------------ Tube-MPPI
+  bool tube() const { return cp_.controller == MPPI_CONTROLLER_TUBE; }
+
+  mppi_status nominal_state_used(int* used) override
+  {
+    MG_CHECK(tube(), "only a Tube-MPPI handle keeps a nominal system");
+    *used = nominal_used_;
+    return MPPI_OK;
+  }
+
+  // One state step of instance i's model from x with control u (Dynamics::step; no constraint applied).
+  void model_step(int i, const float* x, const float* u, float* xn, int t) const
+  {
+    if constexpr (Model::kPlugin)
+    {
+      float xd[S], y[Model::OUTPUT_DIM];
+      dyn_[i].step(x, xn, xd, u, y, t, cp_.dt);
+    }
+    else if constexpr (Model::kMlp)
+    {
+      if (!use_analytic_)
+      {
+        float xd[S];
+        mlp_host_dynamics(mlp_host_.data(), x, u, xd);
+        for (int s = 0; s < S; ++s) xn[s] = fmaf(xd[s], cp_.dt, x[s]);
+        return;
+      }
+      euler_step<Model>(dyn_[i], x, u, xn, cp_.dt);
+    }
+    else
+    {
+      euler_step<Model>(dyn_[i], x, u, xn, cp_.dt);
+    }
+  }
+
+  // Controller::computeStateTrajectoryHelper (controller.cuh:645-662): x0, then T-1 steps, each control passed
+  // through enforceConstraints first.
+  void state_trajectory(int i, const float* x0, const float* u, float* out) const
+  {
+    const int T = T_[i];
+    float x[S], xn[S], uc[C];
+    for (int s = 0; s < S; ++s) x[s] = out[s] = x0[s];
+    for (int t = 0; t < T - 1; ++t)
+    {
+      for (int c = 0; c < C; ++c)
+        uc[c] = enforce_constraint(u[(size_t)t * C + c], cc_.lower[c], cc_.upper[c], cc_.deadband[c], cc_.zero_control[c]);
+      model_step(i, x, uc, xn, t);
+      for (int s = 0; s < S; ++s) x[s] = out[(size_t)(t + 1) * S + s] = xn[s];
+    }
+  }
+
+  // TubeMPPIController::computeStateTrajectory (tube_mppi_controller.cu:334-341): the nominal system from the nominal
+  // state along the nominal sequence, the actual system from the given state along the actual sequence.
+  void tube_state_trajectories(const float* x_actual)
+  {
+    state_trajectory(0, x_actual, control_.data() + t_off_[0], state_seq_.data());
+    state_trajectory(1, nominal_x0_.data(), control_.data() + t_off_[1], state_seq_.data() + (size_t)T_[0] * S);
+    traj_dirty_ = false;
+  }
+
+  // TubeMPPIController::updateNominalState (tube_mppi_controller.cu:343-349)
+  void advance_nominal_state()
+  {
+    float xn[S];
+    model_step(1, nominal_x0_.data(), control_.data() + t_off_[1], xn, 0);
+    for (int s = 0; s < S; ++s) nominal_x0_[s] = xn[s];
+  }
+
+  // Controller::smoothControlTrajectoryHelper (controller.cuh:573-607) on the host, in the order of the device
+  // smoothing (finish_instance): each tap product rounded to FP32 and added in tap order, u[0] kept.
+  void smooth_host(float* u, int T) const
+  {
+    const float coef[5] = { -3.0f / 35.0f, 12.0f / 35.0f, 17.0f / 35.0f, 12.0f / 35.0f, -3.0f / 35.0f };
+    std::vector<float> buf((size_t)(T + 4) * C);
+    for (int e = 0; e < (T + 4) * C; ++e)
+    {
+      const int tt = e / C, c = e - tt * C;
+      buf[e] = u[(size_t)std::min(std::max(tt - 2, 0), T - 1) * C + c];
+    }
+    for (int t = 1; t < T; ++t)
+      for (int c = 0; c < C; ++c)
+      {
+        float acc = 0.0f;
+        for (int j = 0; j < 5; ++j) acc += coef[j] * buf[(size_t)(t + j) * C + c];
+        u[(size_t)t * C + c] = acc;
+      }
+  }
+
+  // TubeMPPIController::computeControl (tube_mppi_controller.cu:158-296): per iteration one graph launch of the
+  // device work of both systems (sample, rollout, weights, update, no smoothing), then the nominal-state decision on
+  // the host; the nominal sequence is smoothed once at the end.
+  mppi_status compute_control_tube(const float* x, int stride)
+  {
+    for (int i = 0; i < S; ++i)
+      if (!std::isfinite(x[i]))
+      {
+        set_error("initial state has a non-finite entry at index %d", i);
+        return MPPI_ENAN;
+      }
+    if (!nominal_init_)
+    {
+      nominal_x0_.assign(x, x + S);
+      nominal_init_ = true;
+    }
+    for (int i = 0; i < I_; ++i) prev_baseline_[i] = baseline_norm_[2 * i];
+    for (int it = 0; it < cp_.num_iters; ++it)
+    {
+      memcpy(x0_h_.p, x, sizeof(float) * S);
+      memcpy(x0_h_.p + S, nominal_x0_.data(), sizeof(float) * S);
+      memcpy(mean_h_.p, control_.data(), sizeof(float) * control_.size());
+      if (graph_mode_)
+      {
+        cudaGraphExec_t exec = nullptr;
+        MG_TRY(get_graph(stride, &exec));
+        MG_CUDA(cudaGraphLaunch(exec, stream_));
+      }
+      else
+      {
+        MG_TRY(enqueue_solve(stride));
+      }
+      MG_CUDA(cudaStreamSynchronize(stream_));
+      if (status_h_.p[0] != 0u)
+      {
+        status_h_.p[0] = 0u;
+        MG_CUDA(cudaMemsetAsync(status_d_, 0, sizeof(unsigned int), stream_));
+        MG_CUDA(cudaStreamSynchronize(stream_));
+        set_error("a bounded wait for staged control data gave up inside the rollout kernel");
+        return MPPI_ETIMEOUT;
+      }
+      memcpy(control_.data(), out_mean_h_.p, sizeof(float) * control_.size());
+      memcpy(baseline_norm_.data(), out_bn_h_.p, sizeof(float) * 2 * I_);
+      memcpy(stats_.data(), out_stats_h_.p, sizeof(double) * 3 * I_);
+      tube_state_trajectories(x);
+      if (baseline_norm_[0] < baseline_norm_[2] + cp_.nominal_threshold)
+      {
+        // the disturbance that separated the systems improved the cost: the nominal system restarts from the actual
+        nominal_used_ = 0;
+        const size_t ts = (size_t)T_[0] * S, tc = (size_t)T_[0] * C;
+        std::copy(state_seq_.begin(), state_seq_.begin() + ts, state_seq_.begin() + ts);
+        nominal_x0_.assign(x, x + S);
+        std::copy(control_.begin() + t_off_[0], control_.begin() + t_off_[0] + tc, control_.begin() + t_off_[1]);
+      }
+      else
+      {
+        nominal_used_ = 1;
+      }
+    }
+    smooth_host(control_.data() + t_off_[1], T_[1]);
+    tube_state_trajectories(x);
+    for (int i = 0; i < I_; ++i)
+      if (!std::isfinite(baseline_norm_[2 * i]) || !(stats_[3 * i] > 0.0))
+      {
+        set_error("a sampled cost or the normaliser is not finite (NaN state or noise?)");
+        return MPPI_ENAN;
+      }
+    return MPPI_OK;
+  }
+
   mppi_status enqueue_device_solves(int stride, int count) override
   {
     MG_CHECK(stride >= 0 && count >= 0, "stride and count must be >= 0");
@@ -815,6 +987,7 @@ private:
     cc_ = a.cc;
     K_.assign(a.K, a.K + I_);
     T_.assign(a.T, a.T + I_);
+    MG_TRY(check_controller(cp_));  // the Tube-MPPI shape rule needs K and T
     MG_TRY(check_sampling(a.sp));
     sp_ = a.sp;
     long long total_u = 0;
@@ -1215,7 +1388,7 @@ private:
     {
       a.tail = 1;
       a.fin = finalize_args();
-      a.fin.finish = iter == cp_.num_iters - 1;
+      a.fin.finish = !tube() && iter == cp_.num_iters - 1;
       if (a.fin.finish && direct_out_)
       {
         a.fin.host_mean = out_mean_h_.p;
@@ -1600,7 +1773,7 @@ private:
   // num_iters x (sample, rollout, weights+update), in stream order.
   mppi_status enqueue_kernels(int stride)
   {
-    for (int it = 0; it < cp_.num_iters; ++it)
+    for (int it = 0; it < (tube() ? 1 : cp_.num_iters); ++it)
     {
       if (!fused()) MG_TRY(launch_sampler(stride, it));
       MG_TRY(launch_rollout(stride, it));
@@ -1608,7 +1781,7 @@ private:
     }
     // smoothing + constraints of the new nominal sequences (the host post-processing of computeControl); the fused
     // rollout's finalizing CTAs did it already in the last iteration
-    if (tail_finalize()) return MPPI_OK;
+    if (tail_finalize() || tube()) return MPPI_OK;  // Tube-MPPI smooths its nominal sequence on the host
     finish_controls_kernel<C><<<I_, 256, sizeof(float) * (size_t)(max_t_ + 4) * C, stream_>>>(
         inst_d_.p, mean_d_.p, first_d_.p, sample_shared());
     MG_CUDA(cudaGetLastError());
@@ -1622,7 +1795,7 @@ private:
     (void)tc;
     MG_CUDA(cudaMemcpyAsync(io_d_.p, io_in_h_.p, io_in_bytes_, cudaMemcpyHostToDevice, stream_));
     // when the fused rollout finishes the solve it writes the results to the pinned host block itself
-    direct_out_ = tail_finalize();
+    direct_out_ = tail_finalize() && !tube();
     const mppi_status st = enqueue_kernels(stride);
     const bool direct = direct_out_;
     direct_out_ = false;
@@ -1731,6 +1904,9 @@ private:
   std::vector<float> traj_u_, traj_x0_;  // constrained nominal controls and x0 of the last solve
   std::vector<float> leashed_x0_;        // ColoredMPPI with the leash on: the initial states the solve starts from
   int leash_jump_ = 1;                   // steps of the last slide (ColoredMPPIController::leash_jump_)
+  std::vector<float> nominal_x0_;        // Tube-MPPI: the nominal system's state
+  bool nominal_init_ = false;            // Tube-MPPI: nominal_x0_ set (nominalStateInit_)
+  int nominal_used_ = 0;                 // Tube-MPPI: the last iteration kept the nominal system
   bool traj_dirty_ = false;
   std::vector<double> stats_;
 

@@ -302,3 +302,50 @@ def set_mlp(params):
     L = lib()
     L.orc_set_mlp.argtypes = [_FP]
     L.orc_set_mlp(_fp(p))
+
+
+def tube_compute_control(model, dyn, cost, cparams, sampling, constraints, K, T, Cdim, S, x_actual, nominal_x0, eps,
+                         control, stride=1, costmap=None, threads=None):
+    """One TubeMPPIController::computeControl on the CPU.  eps: [2][K][T][C] standard normals (actual, nominal);
+    control: [2][T][C] (actual, nominal) in; returns a dict with both updated sequences, the nominal state after the
+    call, costs / weights / samples of both distributions, baselines, normalisers, nominal_used and both state
+    trajectories."""
+    ctl = _f32(control).copy().reshape(-1)
+    xa = _f32(x_actual).reshape(-1)
+    xn = _f32(nominal_x0).copy().reshape(-1)
+    e = _f32(eps).reshape(-1)
+    costs = np.empty(2 * K, np.float32)
+    w = np.empty(2 * K, np.float32)
+    samples = np.empty(2 * K * T * Cdim, np.float32)
+    b = np.empty(2, np.float32)
+    n = np.empty(2, np.float64)
+    used = C.c_int()
+    states = np.empty(2 * T * S, np.float32)
+    if costmap is not None:
+        data, res, (ox, oy) = costmap
+        data = _f32(data)
+        mp, mw, mh = _fp(data), data.shape[1], data.shape[0]
+    else:
+        mp, mw, mh, res, ox, oy = None, 0, 0, 1.0, 0.0, 0.0
+    L = lib()
+    L.orc_tube_compute_control.restype = C.c_int
+    rc = L.orc_tube_compute_control(model, _ptr(dyn), _ptr(cost), mp, mw, mh, C.c_float(res), C.c_float(ox),
+                                    C.c_float(oy), _ptr(cparams), _ptr(sampling), _ptr(constraints), K, T, _fp(xa),
+                                    _fp(xn), _fp(e), stride, _fp(ctl), _fp(costs), _fp(w), _fp(samples), _fp(b),
+                                    n.ctypes.data_as(_DP), C.byref(used), _fp(states), threads or threads_default())
+    if rc != 0:
+        raise ValueError(f"oracle has no model {model}")
+    return dict(control=ctl.reshape(2, T, Cdim), nominal_x0=xn, costs=costs.reshape(2, K), weights=w.reshape(2, K),
+                samples=samples.reshape(2, K * T * Cdim), baselines=b, normalizers=n, nominal_used=used.value,
+                state_seq=states.reshape(2, T, S))
+
+
+def step_state(model, dyn, cost, x, u, dt):
+    """x after one Dynamics::step with control u (no constraint), in float."""
+    xs = _f32(x).copy().reshape(-1)
+    us = _f32(u).reshape(-1)
+    L = lib()
+    L.orc_step_state.restype = C.c_int
+    if L.orc_step_state(model, _ptr(dyn), _ptr(cost), _fp(us), C.c_float(dt), _fp(xs)) != 0:
+        raise ValueError(f"oracle has no model {model}")
+    return xs

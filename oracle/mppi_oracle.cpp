@@ -1138,4 +1138,113 @@ int orc_compute_control(int model, const void* dyn, const void* cost, const floa
   return 0;
 }
 
+// TubeMPPIController::computeControl (include/mppi/controllers/Tube-MPPI/tube_mppi_controller.cu:158-296) for one
+// controller: distribution 0 (actual system, from x_actual, around control[0]) and distribution 1 (nominal system,
+// from nominal_x0, around control[1]) each sample K controls from their own eps block ([2][K][T][C], the same every
+// iteration), roll out, weight and update; after each iteration the nominal pair takes the actual pair's state and
+// control sequences when baseline_actual < baseline_nominal + nominal_threshold.  Then the nominal sequence is
+// smoothed and both state trajectories are recomputed (computeStateTrajectoryHelper, controller.cuh:645-662).
+int orc_tube_compute_control(int model, const void* dyn, const void* cost, const float* map, int map_w, int map_h,
+                             float map_res, float map_ox, float map_oy, const mppi_controller_params* cp,
+                             const mppi_sampling_params* sp, const mppi_control_constraints* cc, int K, int T,
+                             const float* x_actual, float* nominal_x0, const float* eps, int stride, float* control,
+                             float* costs_out, float* weights_out, float* samples_out, float* baselines_out,
+                             double* normalizers_out, int* nominal_used_out, float* state_seq_out, int threads)
+{
+  orc::ModelBlob b{ model, dyn, cost, { map, map_w, map_h, map_res, map_ox, map_oy } };
+  const int S = orc::model_state_dim(model), C = orc::model_control_dim(model);
+  if (!S) return 1;
+  const size_t n = (size_t)K * T * C, tc = (size_t)T * C;
+  std::vector<float> samples(2 * n), w(2 * K), costs_f(2 * K);
+  std::vector<double> costs(K), mean_d(tc);
+  float baseline[2] = { 0.0f, 0.0f };
+  double normalizer[2] = { 0.0, 0.0 };
+  int nominal_used = 0;
+  auto state_traj = [&](const float* x0, const float* u, float* out) {
+    float x[MPPI_MAX_STATE_DIM], xn[MPPI_MAX_STATE_DIM], xd[MPPI_MAX_STATE_DIM], uc[MPPI_MAX_CONTROL_DIM];
+    for (int i = 0; i < S; ++i) x[i] = out[i] = x0[i];
+    orc::with_model<float>(b, [&](auto& m) {
+      for (int t = 0; t < T - 1; ++t)
+      {
+        for (int i = 0; i < C; ++i) uc[i] = orc::enforce_constraint(u[(size_t)t * C + i], *cc, i);
+        if constexpr (orc::HasCrash<std::decay_t<decltype(m)>>::value)
+        {
+          m.step(x, uc, xn, cp->dt);
+        }
+        else
+        {
+          m.deriv(x, uc, xd);
+          for (int i = 0; i < S; ++i) xn[i] = fmaf(xd[i], cp->dt, x[i]);
+        }
+        for (int i = 0; i < S; ++i) x[i] = out[(size_t)(t + 1) * S + i] = xn[i];
+      }
+    });
+  };
+  for (int it = 0; it < cp->num_iters; ++it)
+  {
+    for (int d = 0; d < 2; ++d)
+    {
+      float* sd = samples.data() + d * n;
+      float* ctl = control + d * tc;
+      orc::gaussian_rewrite(eps + d * n, ctl, sp->std_dev, K, T, C, stride, powf(sp->std_dev_decay, (float)it),
+                            sp->pure_noise_trajectories_percentage, sd);
+      orc::rollout_parallel<float>(b, d == 0 ? x_actual : nominal_x0, sd, true, ctl, *sp, *cc, cp->lambda,
+                                   cp->alpha, K, T, cp->dt, costs.data(), threads, nullptr);
+      for (int k = 0; k < K; ++k) costs_f[d * K + k] = (float)costs[k];
+      orc::weights(costs_f.data() + d * K, K, 1.0f / cp->lambda, w.data() + d * K, &baseline[d], &normalizer[d]);
+      orc::weighted_mean(w.data() + d * K, (float)normalizer[d], sd, K, T, C, mean_d.data(), nullptr);
+      for (size_t j = 0; j < tc; ++j) ctl[j] = (float)mean_d[j];
+    }
+    state_traj(x_actual, control, state_seq_out);
+    state_traj(nominal_x0, control + tc, state_seq_out + (size_t)T * S);
+    if (baseline[0] < baseline[1] + cp->nominal_threshold)
+    {
+      nominal_used = 0;
+      std::copy(state_seq_out, state_seq_out + (size_t)T * S, state_seq_out + (size_t)T * S);
+      std::copy(x_actual, x_actual + S, nominal_x0);
+      std::copy(control, control + tc, control + tc);
+    }
+    else
+    {
+      nominal_used = 1;
+    }
+  }
+  orc::smooth(control + tc, T, C);
+  state_traj(x_actual, control, state_seq_out);
+  state_traj(nominal_x0, control + tc, state_seq_out + (size_t)T * S);
+  if (costs_out) std::copy(costs_f.begin(), costs_f.end(), costs_out);
+  if (weights_out) std::copy(w.begin(), w.end(), weights_out);
+  if (samples_out) std::copy(samples.begin(), samples.end(), samples_out);
+  for (int d = 0; d < 2; ++d)
+  {
+    if (baselines_out) baselines_out[d] = baseline[d];
+    if (normalizers_out) normalizers_out[d] = normalizer[d];
+  }
+  if (nominal_used_out) *nominal_used_out = nominal_used;
+  return 0;
+}
+
+// One nominal-state update of TubeMPPIController::slideControlSequence (updateNominalState,
+// tube_mppi_controller.cu:343-349): x <- step(x, u), no constraint.
+int orc_step_state(int model, const void* dyn, const void* cost, const float* u, float dt, float* x)
+{
+  orc::ModelBlob b{ model, dyn, cost, { nullptr, 0, 0, 1.0f, 0.0f, 0.0f } };
+  const int S = orc::model_state_dim(model);
+  if (!S) return 1;
+  float xn[MPPI_MAX_STATE_DIM], xd[MPPI_MAX_STATE_DIM];
+  orc::with_model<float>(b, [&](auto& m) {
+    if constexpr (orc::HasCrash<std::decay_t<decltype(m)>>::value)
+    {
+      m.step(x, u, xn, dt);
+    }
+    else
+    {
+      m.deriv(x, u, xd);
+      for (int i = 0; i < S; ++i) xn[i] = fmaf(xd[i], dt, x[i]);
+    }
+  });
+  for (int i = 0; i < S; ++i) x[i] = xn[i];
+  return 0;
+}
+
 }  // extern "C"

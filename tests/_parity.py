@@ -17,10 +17,12 @@ import oracle
 TAPS = np.array([-3.0, 12.0, 17.0, 12.0, -3.0]) / 35.0
 
 
-def term_magnitude(weights, normalizer, samples, K, T, Cdim):
-    """A_j of the module docstring, float64 [T][C]."""
+def term_magnitude(weights, normalizer, samples, K, T, Cdim, smoothed=True):
+    """A_j of the module docstring, float64 [T][C] (smoothed=False: the unsmoothed update, A_j = the inner sum)."""
     _, absout = oracle.weighted_mean(weights, np.float32(normalizer), samples, K, T, Cdim)
     a = absout.reshape(T, Cdim)
+    if not smoothed:
+        return a
     pad = np.concatenate([a[:1], a[:1], a, a[-1:], a[-1:]])
     out = np.zeros_like(a)
     for i, c in enumerate(TAPS):
@@ -29,11 +31,11 @@ def term_magnitude(weights, normalizer, samples, K, T, Cdim):
     return out
 
 
-def check_control(got_tc, ref, K, T, Cdim, rtol=1e-5, samples=None):
+def check_control(got_tc, ref, K, T, Cdim, rtol=1e-5, samples=None, smoothed=True):
     """Element-wise check of an updated control sequence (float [T][C]) against an oracle result dict (control,
     weights, normalizer, samples); returns (max error / A_j, median element-wise relative error)."""
     s = ref["samples"] if samples is None else samples
-    A = term_magnitude(ref["weights"], ref["normalizer"], s, K, T, Cdim)
+    A = term_magnitude(ref["weights"], ref["normalizer"], s, K, T, Cdim, smoothed=smoothed)
     got = np.asarray(got_tc, np.float64).reshape(T, Cdim)
     exp = np.asarray(ref["control"], np.float64).reshape(T, Cdim)
     err = np.abs(got - exp)

@@ -325,6 +325,12 @@ mppi_status mppi_get_model_dims(const mppi_handle* h, int* model, int* state_dim
   return MPPI_OK;
 }
 
+mppi_status mppi_set_progress_poll_limit(mppi_handle* h, uint32_t polls)
+{
+  HANDLE_OK(h);
+  return h->engine->set_progress_poll_limit(polls);
+}
+
 mppi_status mppi_get_nominal_state_used(mppi_handle* h, int* used)
 {
   HANDLE_OK(h);

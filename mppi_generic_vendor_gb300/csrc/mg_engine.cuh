@@ -90,6 +90,7 @@ public:
   virtual mppi_status get_judge_stats(float* out) = 0;
   virtual mppi_status use_analytic(int enable) = 0;
   virtual mppi_status nominal_state_used(int* used) = 0;
+  virtual mppi_status set_progress_poll_limit(uint32_t polls) = 0;
 };
 
 // Factories, one per model translation unit.
@@ -721,6 +722,14 @@ public:
     MG_CHECK(Model::kMlp, "only the surrogate model has an analytic fallback");
     use_analytic_ = enable != 0;
     MG_TRY(build_work_lists());  // the rollout kernel, and so its grid, changes
+    invalidate_graphs();
+    return MPPI_OK;
+  }
+
+  // Diagnostics: the bound of rollout mode 4's progress-word poll (0 restores the default).
+  mppi_status set_progress_poll_limit(uint32_t polls) override
+  {
+    max_polls_ = polls ? polls : kMaxProgressPolls;
     invalidate_graphs();
     return MPPI_OK;
   }
@@ -1582,6 +1591,7 @@ private:
       if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
     a.max_t = max_t_;
     a.sh = sample_shared();
+    a.max_polls = max_polls_;
     return a;
   }
 
@@ -1907,6 +1917,7 @@ private:
   std::vector<float> nominal_x0_;        // Tube-MPPI: the nominal system's state
   bool nominal_init_ = false;            // Tube-MPPI: nominal_x0_ set (nominalStateInit_)
   int nominal_used_ = 0;                 // Tube-MPPI: the last iteration kept the nominal system
+  uint32_t max_polls_ = kMaxProgressPolls;  // rollout mode 4's bounded poll (mppi_set_progress_poll_limit)
   bool traj_dirty_ = false;
   std::vector<double> stats_;
 

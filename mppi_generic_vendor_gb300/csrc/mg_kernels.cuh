@@ -237,6 +237,7 @@ struct RolloutArgs
   TileReduce tr;
   int tail;          // the fused rollout finalizes each instance after its last tile (fin below)
   FinalizeArgs fin;
+  uint32_t max_polls;  // rollout mode 4: polls of a noise warp's progress word before a rollout warp gives up
 };
 
 // The tile epilogue (all threads of the CTA; the tile's costs are in a.costs and its minimum in tile_min).  s_w holds
@@ -931,10 +932,10 @@ __global__ void __launch_bounds__(kNoiseWarps ? 2 * NS : NS)
           if (*prog < qi + Q)
           {
             uint32_t i = 0;
-            while (*prog < qi + Q && ++i < kMaxProgressPolls)
+            while (*prog < qi + Q && ++i < a.max_polls)
             {
             }
-            waited_out |= i >= kMaxProgressPolls;
+            waited_out |= i >= a.max_polls;
           }
           __threadfence_block();
           float out[4 * Q];

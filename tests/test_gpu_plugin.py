@@ -70,7 +70,12 @@ def test_plugin_controller_matches_oracle(plugin_path, name, damping):
         assert np.array_equal(samples[uoff[i]:uoff[i + 1]].view(np.uint32), ref["samples"].view(np.uint32)), i
         assert bn[i, 0] == ref["baseline"]
         _parity.check_control(ctl[i].T, ref, K, T, 2)
-        assert np.array_equal(states[i].T.view(np.uint32), ref["state_seq"].view(np.uint32)), i
+        # the nominal state trajectory: the plugin's own step on the host, along the engine's updated sequence
+        _, _, tr = oracle.rollout(_plugins.ORACLE_MODEL[name], ctrl._dyn_arr[i], ctrl._cost_arr[i], x0[i],
+                                  np.ascontiguousarray(ctl[i].T), init[i], ctrl.sampler_.to_c(), ctrl.constraints_,
+                                  1.0, 0.0, 1, T, 0.05, want_traj=True, state_dim=4)
+        expect = np.concatenate([x0[i][None], tr.reshape(T, 4)[:-1].astype(np.float32)])
+        assert np.array_equal(states[i].T.view(np.uint32), expect.view(np.uint32)), i
         # the crash wall is reached by part of the samples
         _, _, traj = oracle.rollout(_plugins.ORACLE_MODEL[name], ctrl._dyn_arr[i], ctrl._cost_arr[i], x0[i],
                                     ref["samples"], init[i], ctrl.sampler_.to_c(), ctrl.constraints_, 1.0, 0.0, K, T,

@@ -79,6 +79,8 @@ struct DoubleIntegratorDynamics : DynamicsBase<4, 2, MPPI_MODEL_DOUBLE_INTEGRATO
 {
   using DYN_PARAMS_T = mppi_double_integrator_params;
   DYN_PARAMS_T params{ 0.0f };
+  DYN_PARAMS_T getParams() const { return params; }
+  void setParams(const DYN_PARAMS_T& p) { params = p; }
 };
 
 // Kinematic bicycle (x, y, yaw, v) with control (accel, steer); the engine's plugin (no reference model).
@@ -130,6 +132,8 @@ struct CartpoleSwingupCost
       : params{ x_coeff, x_dot_coeff, cos_coeff, theta_dot_coeff, terminal_coeff }
   {
   }
+  COST_PARAMS_T getParams() const { return params; }
+  void setParams(const COST_PARAMS_T& p) { params = p; }
 };
 
 struct DoubleIntegratorObstacleCost
@@ -206,12 +210,24 @@ struct NoFeedback
 
 // ---- VanillaMPPIController<DYN_T, COST_T, FB_T, MAX_TIMESTEPS, NUM_ROLLOUTS, SAMPLING_T> ---------------------------
 
+// Free-energy statistics of the last computeControl (MPPIFreeEnergyStatistics::real_sys, controller.cuh:22-38).
+struct FreeEnergyStatistics
+{
+  float freeEnergyMean, freeEnergyVariance, freeEnergyModifiedVariance, normalizerPercent, increase,
+      previousBaseline;
+};
+
 template <class DYN_T, class COST_T, class FB_T, int MAX_TIMESTEPS, int NUM_ROLLOUTS,
           class SAMPLING_T = GaussianDistribution>
 class VanillaMPPIController
 {
 public:
   static constexpr int S = DYN_T::STATE_DIM, C = DYN_T::CONTROL_DIM;
+  // the template arguments, as the reference's Controller exposes them (controller.cuh:76-95)
+  using TEMPLATED_DYNAMICS = DYN_T;
+  using TEMPLATED_COSTS = COST_T;
+  using TEMPLATED_SAMPLING = SAMPLING_T;
+  using TEMPLATED_PARAMS = mppi_controller_params;
   using state_array = std::array<float, S>;
   using control_array = std::array<float, C>;
   using control_trajectory = std::array<float, C * MAX_TIMESTEPS>;  // (c, t) at t * C + c
@@ -319,7 +335,24 @@ public:
   {
     check(mppi_set_cost_params(h_, &cost.params, sizeof(cost.params)), "mppi_set_cost_params");
   }
+  // Dynamics::setParams / Cost::setParams from a parameter block (what BasePlant::updateParameters hands over).
+  void setDynamicsParams(const typename DYN_T::DYN_PARAMS_T& p)
+  {
+    check(mppi_set_dynamics_params(h_, &p, sizeof(p)), "mppi_set_dynamics_params");
+  }
+  void setCostParams(const typename COST_T::COST_PARAMS_T& p)
+  {
+    check(mppi_set_cost_params(h_, &p, sizeof(p)), "mppi_set_cost_params");
+  }
   int getNumTimesteps() const { return T_; }
+  float getDt() const { return params_.dt; }
+  // Controller::getFreeEnergyStatistics (controller.cuh:540-543).
+  FreeEnergyStatistics getFreeEnergyStatistics() const
+  {
+    float v[6];
+    check(mppi_get_free_energy(h_, 0, v), "mppi_get_free_energy");
+    return FreeEnergyStatistics{ v[0], v[1], v[2], v[3], v[4], v[5] };
+  }
   mppi_handle* handle() const { return h_; }
 
   // Sampled trajectories for visualisation (Controller::setTopNSampledControlTrajectoriesHelper, controller.cuh:762;

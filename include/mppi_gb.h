@@ -363,10 +363,12 @@ mppi_status mppi_get_launch_config(const mppi_handle* h, int* rollout_samples_pe
                                    int* reduction_samples_per_cta);
 mppi_status mppi_set_launch_config(mppi_handle* h, int rollout_samples_per_cta, int rollout_time_chunk,
                                    int reduction_samples_per_cta);
-/* Diagnostics (no counterpart in the reference): the number of polls a rollout warp of rollout mode 4 spends on its
- * noise warp's progress word before it gives up (the solve then returns MPPI_ETIMEOUT and the handle stays usable).
- * 0 restores the default (2^22 polls).  Lets a test make that bounded wait run out on purpose. */
-mppi_status mppi_set_progress_poll_limit(mppi_handle* h, uint32_t polls);
+/* Diagnostics (no counterpart in the reference) of rollout mode 4's one bounded wait: a rollout warp polls its noise
+ * warp's progress word in shared memory at most max_polls times per quad of controls (0 restores the default, 2^22),
+ * then gives up; the solve returns MPPI_ETIMEOUT and the handle stays usable.  withhold_progress != 0 makes the noise
+ * warps stage their quads without publishing progress, so a test can make the wait run out on purpose (the kernel
+ * still ends: every wait is bounded). */
+mppi_status mppi_set_wait_diagnostics(mppi_handle* h, uint32_t max_polls, int withhold_progress);
 /* Number of kernels one computeControl launches (for launch accounting). */
 mppi_status mppi_kernels_per_compute(const mppi_handle* h, int* count);
 /* Enqueue `count` device-resident solves (num_iters x sample/rollout/update each, as one replayed CUDA graph) on the

@@ -123,7 +123,7 @@ SIGNATURES = [
     ("mppi_get_sampled_trajectories", C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_int, _FP, _FP, _FP, _IP]),
     ("mppi_get_model_dims", C.c_int, [_P, _IP, _IP, _IP, _IP]),
     ("mppi_get_nominal_state_used", C.c_int, [_P, _IP]),
-    ("mppi_set_progress_poll_limit", C.c_int, [_P, C.c_uint32]),
+    ("mppi_set_wait_diagnostics", C.c_int, [_P, C.c_uint32, C.c_int]),
     ("mppi_handle_adopt", C.c_int, [_P, C.c_int, C.POINTER(_P)]),
     ("mppi_select_top_samples", C.c_int, [_FP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     ("mppi_get_free_energy", C.c_int, [_P, C.c_int, _FP]),

@@ -325,10 +325,10 @@ mppi_status mppi_get_model_dims(const mppi_handle* h, int* model, int* state_dim
   return MPPI_OK;
 }
 
-mppi_status mppi_set_progress_poll_limit(mppi_handle* h, uint32_t polls)
+mppi_status mppi_set_wait_diagnostics(mppi_handle* h, uint32_t max_polls, int withhold_progress)
 {
   HANDLE_OK(h);
-  return h->engine->set_progress_poll_limit(polls);
+  return h->engine->set_wait_diagnostics(max_polls, withhold_progress);
 }
 
 mppi_status mppi_get_nominal_state_used(mppi_handle* h, int* used)

@@ -90,7 +90,7 @@ public:
   virtual mppi_status get_judge_stats(float* out) = 0;
   virtual mppi_status use_analytic(int enable) = 0;
   virtual mppi_status nominal_state_used(int* used) = 0;
-  virtual mppi_status set_progress_poll_limit(uint32_t polls) = 0;
+  virtual mppi_status set_wait_diagnostics(uint32_t max_polls, int withhold_progress) = 0;
 };
 
 // Factories, one per model translation unit.
@@ -726,10 +726,12 @@ public:
     return MPPI_OK;
   }
 
-  // Diagnostics: the bound of rollout mode 4's progress-word poll (0 restores the default).
-  mppi_status set_progress_poll_limit(uint32_t polls) override
+  // Diagnostics: the bound of rollout mode 4's progress-word poll (0 restores the default) and whether its noise
+  // warps withhold their progress (so the rollout warps' bounded wait runs out).
+  mppi_status set_wait_diagnostics(uint32_t max_polls, int withhold_progress) override
   {
-    max_polls_ = polls ? polls : kMaxProgressPolls;
+    max_polls_ = max_polls ? max_polls : kMaxProgressPolls;
+    withhold_progress_ = withhold_progress != 0;
     invalidate_graphs();
     return MPPI_OK;
   }
@@ -1592,6 +1594,7 @@ private:
     a.max_t = max_t_;
     a.sh = sample_shared();
     a.max_polls = max_polls_;
+    a.withhold_progress = withhold_progress_ ? 1 : 0;
     return a;
   }
 
@@ -1917,7 +1920,8 @@ private:
   std::vector<float> nominal_x0_;        // Tube-MPPI: the nominal system's state
   bool nominal_init_ = false;            // Tube-MPPI: nominal_x0_ set (nominalStateInit_)
   int nominal_used_ = 0;                 // Tube-MPPI: the last iteration kept the nominal system
-  uint32_t max_polls_ = kMaxProgressPolls;  // rollout mode 4's bounded poll (mppi_set_progress_poll_limit)
+  uint32_t max_polls_ = kMaxProgressPolls;  // rollout mode 4's bounded poll (mppi_set_wait_diagnostics)
+  bool withhold_progress_ = false;          // mode 4's noise warps publish no progress (mppi_set_wait_diagnostics)
   bool traj_dirty_ = false;
   std::vector<double> stats_;
 

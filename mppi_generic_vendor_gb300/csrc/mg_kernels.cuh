@@ -238,6 +238,7 @@ struct RolloutArgs
   int tail;          // the fused rollout finalizes each instance after its last tile (fin below)
   FinalizeArgs fin;
   uint32_t max_polls;  // rollout mode 4: polls of a noise warp's progress word before a rollout warp gives up
+  int withhold_progress;  // diagnostics: mode 4's noise warps stage their quads without publishing progress
 };
 
 // The tile epilogue (all threads of the CTA; the tile's costs are in a.costs and its minimum in tile_min).  s_w holds
@@ -912,7 +913,7 @@ __global__ void __launch_bounds__(kNoiseWarps ? 2 * NS : NS)
             col[3 * us] = o.w;
           }
         __syncwarp();
-        if ((tid & 31) == 0)
+        if ((tid & 31) == 0 && !a.withhold_progress)
         {
           __threadfence_block();
           *prog = c1;

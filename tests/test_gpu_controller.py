@@ -425,9 +425,9 @@ def test_sampled_trajectories_reject_bad_indices():
 
 def test_bounded_wait_gives_up_and_handle_recovers():
     """Rollout mode 4's rollout warps poll a shared-memory progress word written by the CTA's noise warps, a bounded
-    wait with nothing asynchronous in flight.  With the bound cut to one poll the rollout warps give up at the first
-    quad that is not staged yet: the solve returns MPPI_ETIMEOUT and leaves no state behind, so the next solve with
-    the default bound matches the oracle bit for bit."""
+    wait with nothing asynchronous in flight.  With the noise warps withholding their progress (a flag nothing sets)
+    and the bound cut to 16 polls, every rollout warp gives up: the solve returns MPPI_ETIMEOUT and leaves no state
+    behind, so the next solve with the default bound matches the oracle bit for bit."""
     K, T = 2048, 100
     ctrl, dyn, cost = cartpole_controller(K, T)
     if not (ctrl.rolloutMode()[1] >> 4) & 1:
@@ -439,11 +439,11 @@ def test_bounded_wait_gives_up_and_handle_recovers():
     init = rng.uniform(-1, 1, (T, 1)).astype(np.float32)
     ctrl.setControlSeqs([init.T])
     ctrl.injectNoise(eps)
-    A.call("mppi_set_progress_poll_limit", ctrl._h, 1)
+    A.call("mppi_set_wait_diagnostics", ctrl._h, 16, 1)
     with pytest.raises(MPPIError) as err:
         ctrl.computeControl(x0, 1)
     assert err.value.status == A.MPPI_ETIMEOUT
-    A.call("mppi_set_progress_poll_limit", ctrl._h, 0)
+    A.call("mppi_set_wait_diagnostics", ctrl._h, 0, 0)
     ctrl.setControlSeqs([init.T])
     ctrl.computeControl(x0, 1)
     ref = oracle_solve(ctrl, 0, x0, eps, init)

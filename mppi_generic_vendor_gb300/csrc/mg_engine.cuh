@@ -675,11 +675,16 @@ public:
   // device FP32 copy the rollout kernel converts to BF16 tensor-core operands.
   mppi_status set_mlp(const float* params, size_t n, int precision) override
   {
-    if (!Model::kMlp)
+    if constexpr (!Model::kMlp)
     {
       set_error("this handle's model has no learned surrogate");
       return MPPI_EUNSUPPORTED;
     }
+    else
+      return set_mlp_impl(params, n, precision);
+  }
+  mppi_status set_mlp_impl(const float* params, size_t n, int precision)
+  {
     MG_CHECK(params && n == (size_t)MPPI_MLP_PARAMS, "the MLP parameter vector holds %d floats", MPPI_MLP_PARAMS);
     MG_CHECK(precision >= 0 && precision <= 2, "MLP precision must be 0 (bf16), 1 (fp8 e4m3) or 2 (fp32)");
     for (size_t i = 0; i < n; ++i) MG_CHECK(std::isfinite(params[i]), "MLP parameter %zu is not finite", i);
@@ -696,34 +701,48 @@ public:
 
   mppi_status set_judge(float fraction) override
   {
-    MG_CHECK(Model::kMlp, "the analytic judge applies to the surrogate model only");
-    MG_CHECK(std::isfinite(fraction) && fraction >= 0.0f && fraction <= 1.0f, "judge fraction must be in [0, 1]");
-    judge_frac_ = fraction;
-    MG_TRY(build_judge_lists());
-    invalidate_graphs();
-    return MPPI_OK;
+    if constexpr (!Model::kMlp)
+    {
+      set_error("the analytic judge applies to the surrogate model only");
+      return MPPI_EINVAL;
+    }
+    else
+    {
+      MG_CHECK(std::isfinite(fraction) && fraction >= 0.0f && fraction <= 1.0f, "judge fraction must be in [0, 1]");
+      judge_frac_ = fraction;
+      MG_TRY(build_judge_lists());
+      invalidate_graphs();
+      return MPPI_OK;
+    }
   }
 
   mppi_status get_judge_stats(float* out) override
   {
     MG_CHECK(out, "out must not be NULL");
-    if (!Model::kMlp || judge_total_ == 0 || use_analytic_)
+    if (Model::kMlp && judge_total_ > 0 && !use_analytic_)
     {
-      std::fill(out, out + 2 * I_, 0.0f);
+      MG_CUDA(cudaStreamSynchronize(stream_));
+      MG_CUDA(cudaMemcpy(out, judge_stats_d_.p, sizeof(float) * 2 * I_, cudaMemcpyDeviceToHost));
       return MPPI_OK;
     }
-    MG_CUDA(cudaStreamSynchronize(stream_));
-    MG_CUDA(cudaMemcpy(out, judge_stats_d_.p, sizeof(float) * 2 * I_, cudaMemcpyDeviceToHost));
+    std::fill(out, out + 2 * I_, 0.0f);
     return MPPI_OK;
   }
 
   mppi_status use_analytic(int enable) override
   {
-    MG_CHECK(Model::kMlp, "only the surrogate model has an analytic fallback");
-    use_analytic_ = enable != 0;
-    MG_TRY(build_work_lists());  // the rollout kernel, and so its grid, changes
-    invalidate_graphs();
-    return MPPI_OK;
+    if constexpr (!Model::kMlp)
+    {
+      set_error("only the surrogate model has an analytic fallback");
+      return MPPI_EINVAL;
+    }
+    else
+    {
+      use_analytic_ = enable != 0;
+      MG_TRY(build_work_lists());  // the rollout kernel, and so its grid, changes
+      invalidate_graphs();
+      return MPPI_OK;
+    }
   }
 
   // Diagnostics: the bound of rollout mode 4's progress-word poll (0 restores the default) and whether its noise

@@ -1406,6 +1406,7 @@ private:
     f.finish = 0;
     f.host_mean = f.host_first = f.host_bn = nullptr;
     f.host_stats = nullptr;
+    f.host_status = nullptr;
     return f;
   }
 
@@ -1425,6 +1426,7 @@ private:
         a.fin.host_first = first_h_.p;
         a.fin.host_bn = out_bn_h_.p;
         a.fin.host_stats = out_stats_h_.p;
+        a.fin.host_status = status_h_.p;
       }
     }
     if (noise_warps_now<NS>())

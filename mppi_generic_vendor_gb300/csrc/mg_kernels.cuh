@@ -212,6 +212,8 @@ struct FinalizeArgs
   float* host_first;
   float* host_bn;
   double* host_stats;
+  // with host_mean: the CTA that completes the launch copies the bounded-wait status word here as well
+  unsigned int* host_status;
 };
 
 template <class Model>
@@ -1075,6 +1077,8 @@ __global__ void __launch_bounds__(kNoiseWarps ? 2 * NS : NS)
       a.tile_counter[1] = 0u;
       // every CTA has read this launch's noise counter: advance it for the next launch
       if (a.tail && a.fin.noise_counter) *a.fin.noise_counter += 1u;
+      // every CTA's give-up flag is set by now (each sets it before its own arrival above)
+      if (a.tail && a.fin.host_status) *a.fin.host_status = *reinterpret_cast<volatile unsigned int*>(a.status);
       __threadfence();
     }
   }

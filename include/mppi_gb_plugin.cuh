@@ -30,8 +30,14 @@
  * Differences from the reference's surface, all from running one sample per GPU thread:
  *  - no theta_s / theta_c shared-memory scratch arguments (a sample's state lives in registers);
  *  - methods are const and __host__ __device__ (the host twin computes the nominal state trajectory);
- *  - enforceConstraints is the engine's, the reference's default (deadband, then clamp to the control ranges of the
- *    handle's mppi_control_constraints), applied when the samples are written; a plugin may not replace it;
+ *  - enforceConstraints: by default the engine's, the reference's default (deadband, then clamp to the control ranges
+ *    of the handle's mppi_control_constraints), applied when the samples are written.  A dynamics class that defines
+ *        void enforceConstraints(float* state, float* control) const
+ *    replaces it, with the reference's placement: the samples are written unconstrained, each rollout step passes
+ *    its control through the method with the current state and writes the result back as the sample
+ *    (rolloutKernel, mppi_common.cu:114-123), the sampled-trajectory re-roll does the same (:453), the nominal state
+ *    trajectory applies it with the state to the smoothed sequence (controller.cuh:676-680), and the final pass after
+ *    smoothing applies it with a zero state to every control (mppi_controller.cu:222-226);
  *  - crash is one int per sample, zero at the start of every rollout, passed to each running cost call, and reported
  *    per step by mppi_get_sampled_trajectories (the reference's crash_status_d, mppi_common.cu:371-376).
  * The plugin rollout is a sampler kernel followed by one rollout kernel (one thread per sample, the tile's controls

@@ -190,7 +190,7 @@ public:
     if (tail_finalize()) return iters;  // one fused rollout per iteration, nothing else
     if (fused()) sampler = 0;
     if (fused() && split_) sampler = 1;  // the cost kernel
-    return (sampler + 2 + judge) * iters + (tube() ? 0 : 1);  // + the smoothing / constraint kernel
+    return (sampler + 2 + judge) * iters;  // the last combine smooths and constrains
   }
 
   // ------------------------------------------------------------------------------------------------ computeControl
@@ -330,9 +330,12 @@ public:
         const float* uc = u + (size_t)t * C;
         if constexpr (Model::kPlugin)
         {
-          // the plugin's own step (Dynamics::step, dynamics.cu:142-152) on its host twin
-          float xd[S], y[Model::OUTPUT_DIM];
-          dyn_[i].step(x, xn, xd, uc, y, t, cp_.dt);
+          // the plugin's own step (Dynamics::step, dynamics.cu:142-152) on its host twin; a plugin with its own
+          // enforceConstraints sees the smoothed control with the state first (controller.cuh:676-680)
+          float xd[S], y[Model::OUTPUT_DIM], ucon[C];
+          for (int c = 0; c < C; ++c) ucon[c] = uc[c];
+          if constexpr (Model::kOwnConstraints) dyn_[i].enforceConstraints(x, ucon);
+          dyn_[i].step(x, xn, xd, ucon, y, t, cp_.dt);
         }
         else if (Model::kMlp && !use_analytic_)
         {
@@ -799,8 +802,17 @@ public:
     for (int s = 0; s < S; ++s) x[s] = out[s] = x0[s];
     for (int t = 0; t < T - 1; ++t)
     {
-      for (int c = 0; c < C; ++c)
-        uc[c] = enforce_constraint(u[(size_t)t * C + c], cc_.lower[c], cc_.upper[c], cc_.deadband[c], cc_.zero_control[c]);
+      if constexpr (Model::kOwnConstraints)
+      {
+        for (int c = 0; c < C; ++c) uc[c] = u[(size_t)t * C + c];
+        dyn_[i].enforceConstraints(x, uc);
+      }
+      else
+      {
+        for (int c = 0; c < C; ++c)
+          uc[c] = enforce_constraint(u[(size_t)t * C + c], cc_.lower[c], cc_.upper[c], cc_.deadband[c],
+                                     cc_.zero_control[c]);
+      }
       model_step(i, x, uc, xn, t);
       for (int s = 0; s < S; ++s) x[s] = out[(size_t)(t + 1) * S + s] = xn[s];
     }
@@ -825,6 +837,27 @@ public:
 
   // Controller::smoothControlTrajectoryHelper (controller.cuh:573-607) on the host, in the order of the device
   // smoothing (finish_instance): each tap product rounded to FP32 and added in tap order, u[0] kept.
+  // A plugin with its own enforceConstraints: the final pass after smoothing on the host, the plugin's method with a
+  // zero state on every control (mppi_controller.cu:222-226), or ColoredMPPIController's clamp of control 1 alone
+  // (colored_mppi_controller.cu:224-229).  The smoothed sequence came back unconstrained (sample_shared).
+  void final_constraints_host()
+  {
+    for (int i = 0; i < I_; ++i)
+      for (int t = 0; t < T_[i]; ++t)
+      {
+        float* u = control_.data() + t_off_[i] + (size_t)t * C;
+        if (cp_.controller == MPPI_CONTROLLER_COLORED)
+        {
+          if (C > 1) u[1] = fminf(fmaxf(u[1], cc_.lower[1]), cc_.upper[1]);
+        }
+        else if constexpr (Model::kOwnConstraints)
+        {
+          float zero[S] = {};
+          dyn_[i].enforceConstraints(zero, u);
+        }
+      }
+  }
+
   void smooth_host(float* u, int T) const
   {
     const float coef[5] = { -3.0f / 35.0f, 12.0f / 35.0f, 17.0f / 35.0f, 12.0f / 35.0f, -3.0f / 35.0f };
@@ -961,7 +994,7 @@ public:
       MG_CUDA(cudaEventRecord(ev[1], stream_));
       MG_TRY(launch_rollout(stride, 0));
       MG_CUDA(cudaEventRecord(ev[2], stream_));
-      MG_TRY(launch_weights());
+      MG_TRY(launch_weights(0));
       MG_CUDA(cudaEventRecord(ev[3], stream_));
       MG_CUDA(cudaEventSynchronize(ev[3]));
       if (r == 0) continue;  // warm-up
@@ -1407,6 +1440,7 @@ private:
     f.host_mean = f.host_first = f.host_bn = nullptr;
     f.host_stats = nullptr;
     f.host_status = nullptr;
+    f.status = status_d_;
     return f;
   }
 
@@ -1753,22 +1787,48 @@ private:
   }
   SampleShared sample_shared() const
   {
-    return make_sample_shared(sp_, cc_, cp_.controller == MPPI_CONTROLLER_COLORED ? 1 : 0);
+    SampleShared sh = make_sample_shared(sp_, cc_, cp_.controller == MPPI_CONTROLLER_COLORED ? 1 : 0);
+    if constexpr (Model::kOwnConstraints)
+    {
+      // the plugin's enforceConstraints replaces the deadband + clamp: samples and the smoothed mean leave the GPU
+      // unconstrained (an infinite range with no deadband leaves every value as it is)
+      for (int c = 0; c < kMaxC; ++c)
+      {
+        sh.lower[c] = -INFINITY;
+        sh.upper[c] = INFINITY;
+        sh.deadband[c] = 0.0f;
+      }
+    }
+    return sh;
   }
 
-  mppi_status launch_weights()
+  // Iteration `iter` of a solve: the combine of the instances (tile partial sums or the weights pass); the last
+  // iteration's combine also smooths and clamps the new means and, in a solve whose results go straight to the host
+  // block (direct_out_), publishes them there.
+  mppi_status launch_weights(int iter)
   {
     if (tail_finalize())  // the fused rollout combined the instances itself
     {
       weights_stale_ = true;
       return MPPI_OK;
     }
+    const bool finish = !tube() && iter == cp_.num_iters - 1;
+    const size_t fin_floats = finish ? (size_t)(max_t_ + 4) * C : 0;
     if (tile_reduce_active())
     {
-      const FinalizeArgs f = finalize_args();
-      const size_t smem = sizeof(float) * (size_t)max_tiles_per_inst_;
-      MG_CUDA(raise_smem_cap(tile_finalize_kernel, smem));
-      tile_finalize_kernel<<<I_, 256, smem, stream_>>>(f);
+      FinalizeArgs f = finalize_args();
+      f.finish = finish ? 1 : 0;
+      if (finish && direct_out_)
+      {
+        f.host_mean = out_mean_h_.p;
+        f.host_first = first_h_.p;
+        f.host_bn = out_bn_h_.p;
+        f.host_stats = out_stats_h_.p;
+        f.host_status = status_h_.p;
+      }
+      const size_t smem = sizeof(float) * std::max((size_t)max_tiles_per_inst_, fin_floats);
+      MG_CUDA(raise_smem_cap(tile_finalize_kernel<C>, smem));
+      tile_finalize_kernel<C><<<I_, 256, smem, stream_>>>(f, sample_shared());
       MG_CUDA(cudaGetLastError());
       weights_stale_ = true;
       return MPPI_OK;
@@ -1799,7 +1859,21 @@ private:
     a.transform = tsallis() ? 1 : 0;
     a.tsallis_gamma = cp_.tsallis_gamma;
     a.tsallis_r = cp_.tsallis_r;
-    weights_update_kernel<C><<<num_chunks_, 256, 0, stream_>>>(a);
+    a.finish = finish ? 1 : 0;
+    a.first_out = first_d_.p;
+    a.sh = sample_shared();
+    a.status = status_d_;
+    if (finish && direct_out_)
+    {
+      a.host_mean = out_mean_h_.p;
+      a.host_first = first_h_.p;
+      a.host_bn = out_bn_h_.p;
+      a.host_stats = out_stats_h_.p;
+      a.host_status = status_h_.p;
+    }
+    const size_t smem = sizeof(float) * fin_floats;
+    MG_CUDA(raise_smem_cap(weights_update_kernel<C>, smem));
+    weights_update_kernel<C><<<num_chunks_, 256, smem, stream_>>>(a);
     MG_CUDA(cudaGetLastError());
     return MPPI_OK;
   }
@@ -1807,18 +1881,15 @@ private:
   // num_iters x (sample, rollout, weights+update), in stream order.
   mppi_status enqueue_kernels(int stride)
   {
+    // the smoothing + constraints of the new nominal sequences (the host post-processing of computeControl) run in
+    // the last iteration's combine: the fused rollout's finalizing CTAs, tile_finalize_kernel or the weights pass;
+    // Tube-MPPI smooths its nominal sequence on the host
     for (int it = 0; it < (tube() ? 1 : cp_.num_iters); ++it)
     {
       if (!fused()) MG_TRY(launch_sampler(stride, it));
       MG_TRY(launch_rollout(stride, it));
-      MG_TRY(launch_weights());
+      MG_TRY(launch_weights(it));
     }
-    // smoothing + constraints of the new nominal sequences (the host post-processing of computeControl); the fused
-    // rollout's finalizing CTAs did it already in the last iteration
-    if (tail_finalize() || tube()) return MPPI_OK;  // Tube-MPPI smooths its nominal sequence on the host
-    finish_controls_kernel<C><<<I_, 256, sizeof(float) * (size_t)(max_t_ + 4) * C, stream_>>>(
-        inst_d_.p, mean_d_.p, first_d_.p, sample_shared());
-    MG_CUDA(cudaGetLastError());
     return MPPI_OK;
   }
 
@@ -1828,8 +1899,8 @@ private:
     const size_t tc = control_.size();
     (void)tc;
     MG_CUDA(cudaMemcpyAsync(io_d_.p, io_in_h_.p, io_in_bytes_, cudaMemcpyHostToDevice, stream_));
-    // when the fused rollout finishes the solve it writes the results to the pinned host block itself
-    direct_out_ = tail_finalize() && !tube();
+    // the CTAs that finish the solve write the results to the pinned host block themselves
+    direct_out_ = !tube();
     const mppi_status st = enqueue_kernels(stride);
     const bool direct = direct_out_;
     direct_out_ = false;
@@ -1897,7 +1968,8 @@ private:
     memcpy(control_.data(), out_mean_h_.p, sizeof(float) * control_.size());
     memcpy(baseline_norm_.data(), out_bn_h_.p, sizeof(float) * 2 * I_);
     memcpy(stats_.data(), out_stats_h_.p, sizeof(double) * 3 * I_);
-    // control_ arrives smoothed and constrained (finish_controls_kernel); first_h_ holds the unclamped first controls
+    // control_ arrives smoothed and constrained (finish_instance in the last combine); first_h_ holds the unclamped
+    // first controls
     memcpy(last_pre_smooth_.data(), first_h_.p, sizeof(float) * I_ * C);
     bool bad = false;
     for (int i = 0; i < I_; ++i)
@@ -1906,6 +1978,7 @@ private:
     traj_u_ = control_;
     traj_x0_.assign(x0, x0 + (size_t)I_ * S);
     traj_dirty_ = true;
+    if constexpr (Model::kOwnConstraints) final_constraints_host();
     if (bad)
     {
       set_error("a sampled cost or the normaliser is not finite (NaN state or noise?)");

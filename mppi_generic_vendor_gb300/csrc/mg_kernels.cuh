@@ -212,8 +212,9 @@ struct FinalizeArgs
   float* host_first;
   float* host_bn;
   double* host_stats;
-  // with host_mean: the CTA that completes the launch copies the bounded-wait status word here as well
+  // with host_mean: the CTA that completes the launch copies the bounded-wait status word (status) here as well
   unsigned int* host_status;
+  const unsigned int* status;
 };
 
 template <class Model>
@@ -405,8 +406,11 @@ __device__ __forceinline__ void finalize_instance(const FinalizeArgs& a, int i, 
   }
 }
 
-// Instance i's smoothing and final clamp (finish_controls_kernel's body), by all threads of the calling CTA; buf
-// holds (T + 4) * C floats.
+// Controller::smoothControlTrajectoryHelper (controller.cuh:573-607) and the final constraint pass, on the device,
+// by all threads of the CTA that has combined instance i: the new mean is smoothed in place with the 5-tap
+// Savitzky-Golay filter [-3, 12, 17, 12, -3] / 35 (edges replicated, the first control kept; each tap product rounded
+// to FP32 and added in tap order), then clamped, and the unclamped first control is recorded (the slide history).
+// buf holds (T + 4) * C floats.
 template <int C>
 __device__ __forceinline__ void finish_instance(const InstDesc& d, int i, float* mean, float* first_out,
                                                 const SampleShared& sh, float* buf)
@@ -443,6 +447,33 @@ __device__ __forceinline__ void finish_instance(const InstDesc& d, int i, float*
     else
       u[e] = enforce_constraint(v, sh.lower[c], sh.upper[c], sh.deadband[c], sh.zero[c]);
   }
+}
+
+// The end of a solve for instance i, by all threads of the CTA that has just written the instance's new mean: the
+// smoothing and final clamp (finish_instance) and, with host pointers, the results copied straight to the pinned
+// host block (device-accessible under unified addressing), so no device-to-host copy has to follow the solve.
+template <int C>
+__device__ __forceinline__ void finish_and_publish(const InstDesc& d, int i, float* mean, float* first_out,
+                                                   const float* bn, const double* stats, const SampleShared& sh,
+                                                   float* buf, float* host_mean, float* host_first, float* host_bn,
+                                                   double* host_stats)
+{
+  const int tid = threadIdx.x;
+  __syncthreads();  // the new mean is written
+  finish_instance<C>(d, i, mean, first_out, sh, buf);
+  if (host_mean)
+  {
+    __syncthreads();  // the smoothed mean and the first controls are written
+    for (int e = tid; e < d.T * C; e += blockDim.x) host_mean[d.t_off + e] = mean[d.t_off + e];
+    if (tid < C) host_first[i * C + tid] = first_out[i * C + tid];
+    if (tid == 0)
+    {
+      host_bn[2 * i] = bn[2 * i];
+      host_bn[2 * i + 1] = bn[2 * i + 1];
+      for (int j = 0; j < 3; ++j) host_stats[3 * i + j] = stats[3 * i + j];
+    }
+  }
+  __syncthreads();
 }
 
 // The running cost of step t (state cost on the stepped output y, control cost, likelihood-ratio term), in the
@@ -1046,23 +1077,8 @@ __global__ void __launch_bounds__(kNoiseWarps ? 2 * NS : NS)
         finalize_instance(a.fin, w.x, s_u, s_tred, &s_eta);
         if (tid == 0) a.fin.inst_tiles_done[w.x] = 0u;
         if (a.fin.finish)
-        {
-          __syncthreads();
-          finish_instance<C>(d, w.x, a.fin.mean_out, a.fin.first_out, a.sh, s_u);
-          if (a.fin.host_mean)
-          {
-            __syncthreads();  // the smoothed mean and the first controls are written
-            for (int e = tid; e < d.T * C; e += blockDim.x)
-              a.fin.host_mean[d.t_off + e] = a.fin.mean_out[d.t_off + e];
-            if (tid < C) a.fin.host_first[w.x * C + tid] = a.fin.first_out[w.x * C + tid];
-            if (tid == 0)
-            {
-              a.fin.host_bn[2 * w.x] = a.fin.baseline_norm[2 * w.x];
-              a.fin.host_bn[2 * w.x + 1] = a.fin.baseline_norm[2 * w.x + 1];
-              for (int j = 0; j < 3; ++j) a.fin.host_stats[3 * w.x + j] = a.fin.stats[3 * w.x + j];
-            }
-          }
-        }
+          finish_and_publish<C>(d, w.x, a.fin.mean_out, a.fin.first_out, a.fin.baseline_norm, a.fin.stats, a.sh, s_u,
+                                a.fin.host_mean, a.fin.host_first, a.fin.host_bn, a.fin.host_stats);
         __syncthreads();
       }
     }
@@ -1570,6 +1586,18 @@ struct WeightsArgs
   // 0: the exponential transform; 1: TsallisTransform (mppi_common.cu:1004-1021) with tsallis_gamma / tsallis_r
   int transform;
   float tsallis_gamma, tsallis_r;
+  // finish != 0 (the last iteration of a solve): the instance's last CTA also smooths and clamps the new mean
+  // (finish_and_publish; dynamic shared memory of (T_max + 4) * C floats) and, with host_mean, publishes the results
+  // to the pinned host block; the last instance's CTA then copies the status word to host_status
+  int finish;
+  float* first_out;
+  SampleShared sh;
+  float* host_mean;
+  float* host_first;
+  float* host_bn;
+  double* host_stats;
+  unsigned int* host_status;
+  const unsigned int* status;
 };
 
 // TsallisTransform (mppi_common.cu:1004-1021), the ColoredMPPI controller's weight: with d = c - baseline,
@@ -1789,10 +1817,21 @@ __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_consta
     a.stats[3 * ch.x + 2] = bd;
     a.arrive[ch.x] = 0u;
     a.baseline_bits[ch.x] = kOrderedPosInf;
+  }
+  if (a.finish)
+  {
+    extern __shared__ float s_fin[];  // (T_max + 4) * C floats, launched only with finish
+    finish_and_publish<C>(d, ch.x, a.mean_out, a.first_out, a.baseline_norm, a.stats, a.sh, s_fin, a.host_mean,
+                          a.host_first, a.host_bn, a.host_stats);
+  }
+  if (tid == 0)
+  {
     __threadfence();
     const unsigned int fin = atomicAdd(a.inst_done, 1u);
     if (fin == (unsigned int)(a.num_instances - 1))
     {
+      // every earlier kernel of the solve has set its give-up flag by now
+      if (a.host_status) *a.host_status = *reinterpret_cast<const volatile unsigned int*>(a.status);
       *a.inst_done = 0u;
       if (a.noise_counter) *a.noise_counter += 1u;
       __threadfence();
@@ -1800,12 +1839,21 @@ __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_consta
   }
 }
 
-static __global__ void __launch_bounds__(256) tile_finalize_kernel(const __grid_constant__ FinalizeArgs a)
+// With a.finish (the last iteration of a solve) the CTA also smooths and clamps the instance's new mean and, with
+// host pointers, publishes the results to the pinned host block; the last CTA then copies the status word.  Dynamic
+// shared memory: max(tiles of the largest instance, (T_max + 4) * C) floats, the tile factors and then the smoothing
+// buffer.
+template <int C>
+__global__ void __launch_bounds__(256) tile_finalize_kernel(const __grid_constant__ FinalizeArgs a,
+                                                            const __grid_constant__ SampleShared sh)
 {
-  extern __shared__ float s_r[];  // per tile of the instance: exp(-(b_l - b) / lambda)
+  extern __shared__ float s_r[];  // per tile of the instance: exp(-(b_l - b) / lambda); then the smoothing buffer
   __shared__ double s_red[64];
   __shared__ float s_eta;
   finalize_instance(a, blockIdx.x, s_r, s_red, &s_eta);
+  if (a.finish)
+    finish_and_publish<C>(a.inst[blockIdx.x], blockIdx.x, a.mean_out, a.first_out, a.baseline_norm, a.stats, sh, s_r,
+                          a.host_mean, a.host_first, a.host_bn, a.host_stats);
   if (threadIdx.x == 0)
   {
     __threadfence();
@@ -1814,6 +1862,8 @@ static __global__ void __launch_bounds__(256) tile_finalize_kernel(const __grid_
     {
       *a.inst_done = 0u;
       if (a.noise_counter) *a.noise_counter += 1u;
+      // every earlier kernel of the solve has set its give-up flag by now
+      if (a.host_status) *a.host_status = *reinterpret_cast<const volatile unsigned int*>(a.status);
       __threadfence();
     }
   }
@@ -1830,18 +1880,6 @@ static __global__ void weights_from_costs_kernel(const InstDesc* inst, const flo
   const double linv = (double)lambda_inv;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.K; k += gridDim.x * blockDim.x)
     weights[d.k_off + k] = expf((float)(-((double)costs[d.k_off + k] - bd) * linv));
-}
-
-// Controller::smoothControlTrajectoryHelper (controller.cuh:573-607) and the final constraint pass, on the device:
-// one CTA per instance smooths its new mean in place with the 5-tap Savitzky-Golay filter [-3, 12, 17, 12, -3] / 35
-// (edges replicated, the first control kept; each tap product rounded to FP32 and added in tap order), clamps it,
-// and records the unclamped first control (the slide history).  Dynamic shared memory: (T_max + 4) * C floats.
-template <int C>
-__global__ void __launch_bounds__(256) finish_controls_kernel(const InstDesc* inst, float* mean, float* first_out,
-                                                              const __grid_constant__ SampleShared sh)
-{
-  extern __shared__ float buf[];
-  finish_instance<C>(inst[blockIdx.x], blockIdx.x, mean, first_out, sh, buf);
 }
 
 // Per-system minimum of costs into ordered-int slots (the baseline pass of fullGPUcomputeWeights,

@@ -96,6 +96,7 @@ struct CartpoleModel
   static constexpr bool kNeedsCostmap = false;
   static constexpr bool kMlp = false;
   static constexpr bool kPlugin = false;
+  static constexpr bool kOwnConstraints = false;  // the engine's deadband + clamp, applied when sampling
   static constexpr int kFlopsPerStep = 60;  // counted from the source below (sin/cos polynomial included)
   using DynParams = mppi_cartpole_params;
   using CostParams = mppi_cartpole_cost_params;
@@ -142,6 +143,7 @@ struct DoubleIntegratorModel
   static constexpr bool kNeedsCostmap = false;
   static constexpr bool kMlp = false;
   static constexpr bool kPlugin = false;
+  static constexpr bool kOwnConstraints = false;  // the engine's deadband + clamp, applied when sampling
   static constexpr int kFlopsPerStep = 8 + 11 + 8 * 6;
   using DynParams = mppi_double_integrator_params;
   using CostParams = mppi_di_obstacle_cost_params;
@@ -154,24 +156,30 @@ struct DoubleIntegratorModel
     xd[2] = u[0];
     xd[3] = u[1];
   }
+  // coeff_0 d_0^2 + coeff_1 d_1^2 + coeff_2 d_2^2 + coeff_3 d_3^2 added left to right, d = y - goal; the
+  // subtractions and products in (position, velocity) pairs
   static MG_HD float quad(const CostParams& q, const float* y)
   {
-    const float d0 = y[0] - q.goal[0], d1 = y[1] - q.goal[1], d2 = y[2] - q.goal[2], d3 = y[3] - q.goal[3];
-    return q.coeff[0] * (d0 * d0) + q.coeff[1] * (d1 * d1) + q.coeff[2] * (d2 * d2) + q.coeff[3] * (d3 * d3);
+    const f32x2 d01 = sub2({ y[0], y[1] }, { q.goal[0], q.goal[1] });
+    const f32x2 d23 = sub2({ y[2], y[3] }, { q.goal[2], q.goal[3] });
+    const f32x2 t01 = mul2({ q.coeff[0], q.coeff[1] }, mul2(d01, d01));
+    const f32x2 t23 = mul2({ q.coeff[2], q.coeff[3] }, mul2(d23, d23));
+    return t01.x + t01.y + t23.x + t23.y;
   }
   template <class Ar = ExactArith>
   static MG_HD float computeStateCost(const CostParams& q, const ModelAux&, const float* y, int, Ar&& = Ar{})
   {
     float cost = quad(q, y);
     bool inside = false;
-    // fixed trip count with a guard, so the obstacle table can live in registers for a whole rollout
+    // fixed trip count with a guard, so the obstacle table can live in registers for a whole rollout; the offsets
+    // and squares of (x, y) as pairs, their sum ox^2 + oy^2 scalar
 #pragma unroll
     for (int j = 0; j < MPPI_MAX_OBSTACLES; ++j)
     {
-      const float ox = y[0] - q.obstacle_x[j];
-      const float oy = y[1] - q.obstacle_y[j];
+      const f32x2 o = sub2({ y[0], y[1] }, { q.obstacle_x[j], q.obstacle_y[j] });
+      const f32x2 o2 = mul2(o, o);
       const float r = q.obstacle_radius[j];
-      inside = inside || (j < q.num_obstacles && ox * ox + oy * oy < r * r);
+      inside = inside || (j < q.num_obstacles && o2.x + o2.y < r * r);
     }
     if (inside) cost = cost + q.obstacle_cost;
     return cost;
@@ -195,6 +203,7 @@ struct BicycleCostmapModel
   static constexpr bool kNeedsCostmap = true;
   static constexpr bool kMlp = false;
   static constexpr bool kPlugin = false;
+  static constexpr bool kOwnConstraints = false;  // the engine's deadband + clamp, applied when sampling
   static constexpr int kFlopsPerStep = 2 * 22 + 12 + 25;
   using DynParams = mppi_bicycle_params;
   using CostParams = mppi_costmap_cost_params;
@@ -239,6 +248,7 @@ struct BicycleSlipModel
   static constexpr bool kNeedsCostmap = true;
   static constexpr bool kMlp = false;
   static constexpr bool kPlugin = false;
+  static constexpr bool kOwnConstraints = false;  // the engine's deadband + clamp, applied when sampling
   static constexpr int kFlopsPerStep = 3 * 22 + 45 + 25;
   using DynParams = mppi_bicycle_slip_params;
   using CostParams = mppi_costmap_cost_params;

@@ -1,19 +1,35 @@
 // mg_plugin.cuh — the engine's model concept over a caller's Dynamics / Cost plugin pair (mppi_gb_plugin.cuh), and
 // the two kernels that run plugin models: the rollout and the sampled-trajectory read-out.
 //
-// A plugin model runs rollout mode 0 as: the Gaussian (or colored) sampler kernel writes the constrained samples,
+// A plugin model runs rollout mode 0 as: the Gaussian (or colored) sampler kernel writes the constrained samples (or,
+// for a plugin with its own enforceConstraints, the unconstrained ones, constrained step by step in the rollout),
 // rollout_plugin_kernel integrates them (one thread per sample, controls staged per time chunk in shared memory with
 // 16-byte loads, as rollout_kernel does) calling the plugin's step and computeRunningCost in the order of
 // rolloutKernel (mppi_common.cu:105-152), folds the tile's weighted partial sums (tile_reduce), and
 // tile_finalize_kernel combines the tiles of each instance.
 #pragma once
 
+#include <type_traits>
+
 #include "mg_kernels.cuh"
 
 namespace mg
 {
+// Whether a plugin's dynamics class defines its own enforceConstraints(state, control).
+template <class T, class = void>
+struct DefinesEnforceConstraints : std::false_type
+{
+};
+template <class T>
+struct DefinesEnforceConstraints<T, std::void_t<decltype(&T::enforceConstraints)>> : std::true_type
+{
+};
+
 // The engine's Model concept for a plugin pair: the plugin structs are the parameter blocks (one per instance),
-// copied to the device by value.
+// copied to the device by value.  kOwnConstraints: the dynamics class defines enforceConstraints, which then
+// replaces the engine's deadband + clamp: the samples are written unconstrained and each rollout step passes its
+// control through the plugin's method with the current state and writes the result back (rolloutKernel,
+// mppi_common.cu:114-123).
 template <class D, class Cst>
 struct PluginModel
 {
@@ -22,6 +38,7 @@ struct PluginModel
   static constexpr bool kNeedsCostmap = false;
   static constexpr bool kMlp = false;
   static constexpr bool kPlugin = true;
+  static constexpr bool kOwnConstraints = DefinesEnforceConstraints<D>::value;
   using DynParams = D;
   using CostParams = Cst;
 };
@@ -114,6 +131,15 @@ __global__ void __launch_bounds__(NS) rollout_plugin_kernel(const __grid_constan
           float u[C];
 #pragma unroll
           for (int c = 0; c < C; ++c) u[c] = stage[tid * ROW + tt * C + c];
+          if constexpr (Model::kOwnConstraints)
+          {
+            // the plugin's constraint with the state, written back as the sample (the samples buffer is the
+            // engine's own; the tile's weighted sums read it after the CTA barrier that follows)
+            dyn.enforceConstraints(x, u);
+            float* wb = const_cast<float*>(a.samples) + d.u_off + ((long long)k * d.T + t) * C;
+#pragma unroll
+            for (int c = 0; c < C; ++c) wb[c] = u[c];
+          }
           dyn.step(x, xn, xd, u, y, t, a.dt);
           float c = cost.computeRunningCost(y, u, t, &crash);
           if (a.use_likelihood) c += likelihood_ratio_cost<C>(a, d, k, u, t);
@@ -179,6 +205,7 @@ __global__ void __launch_bounds__(128) sampled_trajectories_plugin_kernel(const 
     float u[C];
 #pragma unroll
     for (int c = 0; c < C; ++c) u[c] = us[t * C + c];
+    if constexpr (Model::kOwnConstraints) dyn.enforceConstraints(x, u);  // as visualizeKernel (mppi_common.cu:453)
     dyn.step(x, xn, xd, u, y, t, a.dt);
     float c = cost.computeRunningCost(y, u, t, &crash);
     if (a.use_likelihood) c += likelihood_ratio_cost<C>(a, d, k, u, t);

@@ -13,15 +13,6 @@
 
 namespace mg
 {
-template <class T, class = void>
-struct DefinesEnforceConstraints : std::false_type
-{
-};
-template <class T>
-struct DefinesEnforceConstraints<T, std::void_t<decltype(&T::enforceConstraints)>> : std::true_type
-{
-};
-
 template <class D, class Cst>
 mppi_status plugin_create(int num_instances, const int* num_rollouts, const int* num_timesteps,
                           const mppi_controller_params* params, const mppi_sampling_params* sampling,
@@ -35,9 +26,6 @@ mppi_status plugin_create(int num_instances, const int* num_rollouts, const int*
   static_assert(D::CONTROL_DIM >= 1 && D::CONTROL_DIM <= MPPI_MAX_CONTROL_DIM, "CONTROL_DIM must be in [1, 4]");
   static_assert(Cst::OUTPUT_DIM == D::OUTPUT_DIM && Cst::CONTROL_DIM == D::CONTROL_DIM,
                 "the cost's OUTPUT_DIM / CONTROL_DIM must match the dynamics'");
-  static_assert(!DefinesEnforceConstraints<D>::value,
-                "enforceConstraints is the engine's (deadband + clamp to the handle's control ranges, applied when "
-                "the samples are written); a plugin cannot replace it");
   clear_error();
   MG_CHECK(out, "out must not be NULL");
   *out = nullptr;

@@ -411,11 +411,27 @@ static void rollout_range(const Model& m, const float* x0, float* controls, bool
     for (int t = 0; t < T; ++t)
     {
       float* uk = controls + ((size_t)k * T + t) * C;
-      for (int i = 0; i < C; ++i)
+      bool own = false;
+      if constexpr (HasCrash<Model>::value) own = m.lim != nullptr;
+      if (own)
       {
-        const float uc = enforce_constraint(uk[i], cc, i);
-        if (write_back) uk[i] = uc;
-        u[i] = (R)uc;
+        // a plugin's own enforceConstraints, with the state (rolloutKernel, mppi_common.cu:114-123)
+        if constexpr (HasCrash<Model>::value)
+        {
+          for (int i = 0; i < C; ++i) u[i] = (R)uk[i];
+          m.constrain(x, u);
+          if (write_back)
+            for (int i = 0; i < C; ++i) uk[i] = (float)u[i];
+        }
+      }
+      else
+      {
+        for (int i = 0; i < C; ++i)
+        {
+          const float uc = enforce_constraint(uk[i], cc, i);
+          if (write_back) uk[i] = uc;
+          u[i] = (R)uc;
+        }
       }
       R step_cost;
       if constexpr (HasCrash<Model>::value)
@@ -512,6 +528,14 @@ struct mppi_test_di_plugin
 {
   float damping;
 };
+// The third test pair's dynamics: the same double integrator with its own enforceConstraints, an acceleration limit
+// that shrinks with speed, |u_i| <= max(0.5, a_max - speed_gain * |v_i|).
+struct mppi_test_di_constrained_plugin
+{
+  float damping;
+  float a_max;
+  float speed_gain;
+};
 struct mppi_test_quad_wall_cost
 {
   float s_goal[4];
@@ -520,7 +544,7 @@ struct mppi_test_quad_wall_cost
   float crash_cost;
   float terminal_coeff;
 };
-constexpr int kTestPluginEuler = 101, kTestPluginSymplectic = 102;
+constexpr int kTestPluginEuler = 101, kTestPluginSymplectic = 102, kTestPluginConstrained = 103;
 
 template <class R>
 struct TestDIPlugin
@@ -530,6 +554,16 @@ struct TestDIPlugin
   const mppi_test_di_plugin& p;
   const mppi_test_quad_wall_cost& q;
   bool symplectic;
+  const mppi_test_di_constrained_plugin* lim;  // non-null: the plugin's own enforceConstraints
+  // the plugin's enforceConstraints(state, control), in the arithmetic of its device code
+  void constrain(const R* x, R* u) const
+  {
+    for (int i = 0; i < 2; ++i)
+    {
+      const R amax = std::fmax((R)0.5, (R)lim->a_max - (R)lim->speed_gain * std::fabs(x[2 + i]));
+      u[i] = std::fmin(std::fmax(u[i], -amax), amax);
+    }
+  }
   void deriv(const R* x, const R* u, R* xd) const
   {
     xd[0] = x[2];
@@ -621,9 +655,11 @@ static void with_model(const ModelBlob& b, F&& f)
     }
     case kTestPluginEuler:
     case kTestPluginSymplectic:
+    case kTestPluginConstrained:
     {
       TestDIPlugin<R> m{ *(const mppi_test_di_plugin*)b.dyn, *(const mppi_test_quad_wall_cost*)b.cost,
-                         b.model == kTestPluginSymplectic };
+                         b.model == kTestPluginSymplectic,
+                         b.model == kTestPluginConstrained ? (const mppi_test_di_constrained_plugin*)b.dyn : nullptr };
       f(m);
       break;
     }
@@ -642,6 +678,7 @@ static int model_state_dim(int model)
     case MPPI_MODEL_BICYCLE_SLIP_MLP: return g_mlp_d.empty() ? 0 : 7;
     case kTestPluginEuler: return 4;
     case kTestPluginSymplectic: return 4;
+    case kTestPluginConstrained: return 4;
     default: return 0;
   }
 }
@@ -656,6 +693,7 @@ static int model_control_dim(int model)
     case MPPI_MODEL_BICYCLE_SLIP_MLP: return 2;
     case kTestPluginEuler: return 2;
     case kTestPluginSymplectic: return 2;
+    case kTestPluginConstrained: return 2;
     default: return 0;
   }
 }
@@ -1110,6 +1148,11 @@ int orc_compute_control(int model, const void* dyn, const void* cost, const floa
         float xn[MPPI_MAX_STATE_DIM];
         if constexpr (orc::HasCrash<std::decay_t<decltype(m)>>::value)
         {
+          if (m.lim)
+          {
+            for (int i = 0; i < C; ++i) u[i] = control[(size_t)t * C + i];
+            m.constrain(x, u);
+          }
           m.step(x, u, xn, cp->dt);
         }
         else
@@ -1121,15 +1164,33 @@ int orc_compute_control(int model, const void* dyn, const void* cost, const floa
       }
     });
   }
-  for (int t = 0; t < T; ++t)
-    for (int i = 0; i < C; ++i)
-    {
-      float& v = control[(size_t)t * C + i];
-      if (!colored)
-        v = orc::enforce_constraint(v, *cc, i);
-      else if (i == 1)
-        v = fminf(fmaxf(v, cc->lower[1]), cc->upper[1]);  // colored_mppi_controller.cu:224-229
-    }
+  bool own = false;
+  orc::with_model<float>(b, [&](auto& m) {
+    if constexpr (orc::HasCrash<std::decay_t<decltype(m)>>::value) own = m.lim != nullptr;
+  });
+  if (own && !colored)
+  {
+    // the final pass with a plugin's own enforceConstraints: a zero state (mppi_controller.cu:222-226)
+    orc::with_model<float>(b, [&](auto& m) {
+      if constexpr (orc::HasCrash<std::decay_t<decltype(m)>>::value)
+      {
+        const float zero[MPPI_MAX_STATE_DIM] = {};
+        for (int t = 0; t < T; ++t) m.constrain(zero, control + (size_t)t * C);
+      }
+    });
+  }
+  else
+  {
+    for (int t = 0; t < T; ++t)
+      for (int i = 0; i < C; ++i)
+      {
+        float& v = control[(size_t)t * C + i];
+        if (!colored)
+          v = orc::enforce_constraint(v, *cc, i);
+        else if (i == 1)
+          v = fminf(fmaxf(v, cc->lower[1]), cc->upper[1]);  // colored_mppi_controller.cu:224-229
+      }
+  }
   if (costs_out) std::copy(costs_f.begin(), costs_f.end(), costs_out);
   if (weights_out) std::copy(w.begin(), w.end(), weights_out);
   if (samples_out) std::copy(samples.begin(), samples.end(), samples_out);
@@ -1169,6 +1230,11 @@ int orc_tube_compute_control(int model, const void* dyn, const void* cost, const
         for (int i = 0; i < C; ++i) uc[i] = orc::enforce_constraint(u[(size_t)t * C + i], *cc, i);
         if constexpr (orc::HasCrash<std::decay_t<decltype(m)>>::value)
         {
+          if (m.lim)
+          {
+            for (int i = 0; i < C; ++i) uc[i] = u[(size_t)t * C + i];
+            m.constrain(x, uc);
+          }
           m.step(x, uc, xn, cp->dt);
         }
         else

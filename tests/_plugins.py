@@ -4,12 +4,16 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 SOURCE = HERE / "plugins" / "di_plugins.cu"
-# the oracle's model ids for the two pairs (oracle/mppi_oracle.cpp, TestDIPlugin)
-ORACLE_MODEL = {"di_quadratic": 101, "di_symplectic_quadratic": 102}
+# the oracle's model ids for the three pairs (oracle/mppi_oracle.cpp, TestDIPlugin)
+ORACLE_MODEL = {"di_quadratic": 101, "di_symplectic_quadratic": 102, "di_constrained_quadratic": 103}
 
 
 class DIPlugin(C.Structure):
     _fields_ = [("damping", C.c_float)]
+
+
+class DIConstrainedPlugin(C.Structure):
+    _fields_ = [("damping", C.c_float), ("a_max", C.c_float), ("speed_gain", C.c_float)]
 
 
 class QuadraticWallCost(C.Structure):

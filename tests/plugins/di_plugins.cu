@@ -1,9 +1,9 @@
-// Two Dynamics / Cost plugin pairs written against include/mppi_gb_plugin.cuh, outside the engine's sources, the way
-// a user of the library would write them: the double integrator (DoubleIntegratorDynamics, di_dynamics.cu:46-53)
-// with an optional linear damping, once with the default Euler step and once with its own step override
-// (semi-implicit: velocity first, then position with the new velocity), and QuadraticCostImpl's state cost
-// (quadratic_cost.cu:35-48) with a crash wall that uses the crash argument of computeRunningCost: once x > wall_x the
-// sample's crash flag stays set and every later step pays crash_cost.
+// Three Dynamics / Cost plugin pairs written against include/mppi_gb_plugin.cuh, outside the engine's sources, the
+// way a user of the library would write them: the double integrator (DoubleIntegratorDynamics, di_dynamics.cu:46-53)
+// with an optional linear damping, once with the default Euler step, once with its own step override (semi-implicit:
+// velocity first, then position with the new velocity) and once with its own enforceConstraints; and
+// QuadraticCostImpl's state cost (quadratic_cost.cu:35-48) with a crash wall that uses the crash argument of
+// computeRunningCost: once x > wall_x the sample's crash flag stays set and every later step pays crash_cost.
 #include "mppi_gb_plugin.cuh"
 
 struct DIPlugin : mppi_gb::Dynamics<DIPlugin, 4, 2>
@@ -39,6 +39,31 @@ struct DISymplecticPlugin : mppi_gb::Dynamics<DISymplecticPlugin, 4, 2>
   }
 };
 
+// Its own enforceConstraints (Dynamics::enforceConstraints, dynamics.cu:107-126, overridden): an acceleration limit
+// that shrinks with speed, |u_i| <= max(0.5, a_max - speed_gain * |v_i|), in place of the handle's control ranges.
+struct DIConstrainedPlugin : mppi_gb::Dynamics<DIConstrainedPlugin, 4, 2>
+{
+  float damping;
+  float a_max;
+  float speed_gain;
+  MPPI_GB_HD void computeDynamics(const float* x, const float* u, float* xd) const
+  {
+    xd[0] = x[2];
+    xd[1] = x[3];
+    xd[2] = u[0] - damping * x[2];
+    xd[3] = u[1] - damping * x[3];
+  }
+  MPPI_GB_HD void enforceConstraints(float* x, float* u) const
+  {
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+    {
+      const float amax = fmaxf(0.5f, a_max - speed_gain * fabsf(x[2 + i]));
+      u[i] = fminf(fmaxf(u[i], -amax), amax);
+    }
+  }
+};
+
 struct QuadraticWallCost : mppi_gb::Cost<QuadraticWallCost, 4, 2>
 {
   float s_goal[4];
@@ -69,3 +94,4 @@ struct QuadraticWallCost : mppi_gb::Cost<QuadraticWallCost, 4, 2>
 
 MPPI_GB_PLUGIN(di_quadratic, DIPlugin, QuadraticWallCost)
 MPPI_GB_PLUGIN(di_symplectic_quadratic, DISymplecticPlugin, QuadraticWallCost)
+MPPI_GB_PLUGIN(di_constrained_quadratic, DIConstrainedPlugin, QuadraticWallCost)

@@ -277,10 +277,11 @@ def test_split_rollout_bit_identical_to_fused(lik):
         assert np.array_equal(c0.view(np.uint32), c.view(np.uint32))
         assert np.array_equal(u0, u)
     # three iterations: modes 0 and 4 combine and (last iteration) smooth in the rollout, mode 2 launches the combine
-    # and the smoothing kernels, modes 1 and 3 one more kernel per iteration (the cost kernel, the sampler)
+    # kernel, which smooths in the last iteration, modes 1 and 3 one more kernel per iteration (the cost kernel, the
+    # sampler)
     assert n0 == n4 == 3
-    assert n2 == 2 * 3 + 1
-    assert n1 == n3 == 3 * 3 + 1
+    assert n2 == 2 * 3
+    assert n1 == n3 == 3 * 3
 
 
 def test_split_rollout_unavailable_for_colored_noise():

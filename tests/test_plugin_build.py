@@ -14,13 +14,15 @@ def plugin_lib():
     return _plugins.library_path()
 
 
-@pytest.mark.parametrize("name", ["di_quadratic", "di_symplectic_quadratic"])
-def test_plugin_library_exports_and_sizes(plugin_lib, name):
+@pytest.mark.parametrize("name,dyn_struct", [("di_quadratic", _plugins.DIPlugin),
+                                             ("di_symplectic_quadratic", _plugins.DIPlugin),
+                                             ("di_constrained_quadratic", _plugins.DIConstrainedPlugin)])
+def test_plugin_library_exports_and_sizes(plugin_lib, name, dyn_struct):
     lib = PluginLibrary(plugin_lib, name)
     assert (lib.STATE_DIM, lib.CONTROL_DIM, lib.OUTPUT_DIM) == (4, 2, 4)
-    assert lib.dyn_bytes == C.sizeof(_plugins.DIPlugin)
+    assert lib.dyn_bytes == C.sizeof(dyn_struct)
     assert lib.cost_bytes == C.sizeof(_plugins.QuadraticWallCost)
-    d = PluginDynamics(lib, _plugins.DIPlugin(0.1))
+    d = PluginDynamics(lib, dyn_struct(0.1))
     assert d.model_id == A.MODEL_PLUGIN and d.STATE_DIM == 4
     PluginCost(lib, _plugins.QuadraticWallCost())
     with pytest.raises(ValueError):

@@ -490,12 +490,25 @@ __device__ __forceinline__ float step_cost(const Args& a, const InstDesc& d, con
     // GaussianDistributionImpl::computeLikelihoodRatioCost (gaussian.cu:490-574)
     const bool zero_mean = (float)k >= (1.0f - a.sh.pure_pct) * (float)d.K;
     float lc = 0.0f;
+    // coeff_i m_i (m_i - 2 u_i) / sd_i^2 added in control order; two controls per paired instruction (2 u formed as
+    // u + u, exact like 2.0f * u)
 #pragma unroll
-    for (int i = 0; i < C; ++i)
+    for (int i = 0; i + 1 < C; i += 2)
     {
-      const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + i];
-      const float sd = a.sh.std_dev[i];
-      lc += ar.div(a.sh.control_cost_coeff[i] * m * (m - 2.0f * u[i]), sd * sd);
+      const float* mr = a.mean + d.t_off + t * C + i;
+      const f32x2 m = zero_mean ? f32x2{ 0.0f, 0.0f } : f32x2{ mr[0], mr[1] };
+      const f32x2 sd = { a.sh.std_dev[i], a.sh.std_dev[i + 1] };
+      const f32x2 num = mul2(mul2({ a.sh.control_cost_coeff[i], a.sh.control_cost_coeff[i + 1] }, m),
+                             sub2(m, add2({ u[i], u[i + 1] }, { u[i], u[i + 1] })));
+      const f32x2 q = ar.div2(num, mul2(sd, sd));
+      lc += q.x;
+      lc += q.y;
+    }
+    if constexpr (C % 2 == 1)
+    {
+      const float m = zero_mean ? 0.0f : a.mean[d.t_off + t * C + C - 1];
+      const float sd = a.sh.std_dev[C - 1];
+      lc += ar.div(a.sh.control_cost_coeff[C - 1] * m * (m - 2.0f * u[C - 1]), sd * sd);
     }
     c += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
   }

@@ -194,15 +194,20 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
       float c = Model::stateCostFromTexels(cp, tx, yv) + Model::computeControlCost(cp, uv, tt);
       if (a.use_likelihood)
       {
+        // the two controls' terms as pairs; the divisions branch-free (the IEEE quotient, re-done exactly when an
+        // operand leaves the range where the fast form is exact)
         const bool zero_mean = (float)k[n] >= (1.0f - a.sh.pure_pct) * (float)d.K;
+        const float* mr = a.mean + d.t_off + tt * C;
+        const f32x2 m = zero_mean ? f32x2{ 0.0f, 0.0f } : f32x2{ mr[0], mr[1] };
+        const f32x2 sd = { a.sh.std_dev[0], a.sh.std_dev[1] };
+        const f32x2 num = mul2(mul2({ a.sh.control_cost_coeff[0], a.sh.control_cost_coeff[1] }, m),
+                               sub2(m, add2({ uv[0], uv[1] }, { uv[0], uv[1] })));
+        FastArith fa;
+        f32x2 q = fa.div2(num, mul2(sd, sd));
+        if (__builtin_expect(!fa.ok, 0)) q = ExactArith{}.div2(num, mul2(sd, sd));
         float lc = 0.0f;
-#pragma unroll
-        for (int c2 = 0; c2 < C; ++c2)
-        {
-          const float m = zero_mean ? 0.0f : a.mean[d.t_off + tt * C + c2];
-          const float sd = a.sh.std_dev[c2];
-          lc += a.sh.control_cost_coeff[c2] * m * (m - 2.0f * uv[c2]) / (sd * sd);
-        }
+        lc += q.x;
+        lc += q.y;
         c += 0.5f * a.lambda * (1.0f - a.alpha) * lc;
       }
       return c;
@@ -244,11 +249,18 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
         }
         if constexpr (kTensor)
         {
-          // the inputs are rounded to 16 bits next, so a multiply by the reciprocal stands in for the division
+          // the inputs are rounded to 16 bits next, so a multiply by the reciprocal stands in for the division; the
+          // nine inputs (state, then controls) in pairs
+          const float raw[kMlpIn] = { x[n][0], x[n][1], x[n][2], x[n][3], x[n][4], x[n][5], x[n][6], u[n][0], u[n][1] };
 #pragma unroll
-          for (int i = 0; i < S; ++i) xin[n][i] = (x[n][i] - nm.in_mean[i]) * nm.in_scale[i];
-          xin[n][7] = (u[n][0] - nm.in_mean[7]) * nm.in_scale[7];
-          xin[n][8] = (u[n][1] - nm.in_mean[8]) * nm.in_scale[8];
+          for (int i = 0; i + 1 < kMlpIn; i += 2)
+          {
+            const f32x2 v = mul2(sub2({ raw[i], raw[i + 1] }, { nm.in_mean[i], nm.in_mean[i + 1] }),
+                                 { nm.in_scale[i], nm.in_scale[i + 1] });
+            xin[n][i] = v.x;
+            xin[n][i + 1] = v.y;
+          }
+          xin[n][8] = (raw[8] - nm.in_mean[8]) * nm.in_scale[8];
         }
         else
         {
@@ -275,17 +287,41 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
         up[n][1] = u[n][1];
         float xd[S];
         float sy, cy;
-        sincos_f(x[n][2], &sy, &cy);
-        xd[0] = x[n][3] * cy - x[n][4] * sy;
-        xd[1] = x[n][3] * sy + x[n][4] * cy;
+        if constexpr (kTensor)
+          __sincosf(x[n][2], &sy, &cy);  // the surrogate's kinematics: the hardware sine and cosine suffice
+        else
+          sincos_f(x[n][2], &sy, &cy);
+        // x' = vx cos - vy sin, y' = vx sin + vy cos: the products in pairs, the sums scalar (as the analytic model)
+        const f32x2 kv = mul2({ x[n][3], x[n][3] }, { cy, sy }), kw = mul2({ x[n][4], x[n][4] }, { sy, cy });
+        xd[0] = kv.x - kw.x;
+        xd[1] = kv.y + kw.y;
+        if constexpr (kTensor)
+        {
+          // denormalised outputs y * out_std + out_mean, paired fused multiply-adds
 #pragma unroll
-        for (int j = 0; j < kMlpOut; ++j)
-          xd[2 + j] = kTensor ? y[n][j] * nm.out_std[j] + nm.out_mean[j] : y[n][j] * nrm[23 + j] + nrm[18 + j];
-        float xn[S];
+          for (int j = 0; j + 1 < kMlpOut; j += 2)
+          {
+            const f32x2 o = fma2({ y[n][j], y[n][j + 1] }, { nm.out_std[j], nm.out_std[j + 1] },
+                                 { nm.out_mean[j], nm.out_mean[j + 1] });
+            xd[2 + j] = o.x;
+            xd[3 + j] = o.y;
+          }
+          xd[2 + kMlpOut - 1] = fmaf(y[n][kMlpOut - 1], nm.out_std[kMlpOut - 1], nm.out_mean[kMlpOut - 1]);
+        }
+        else
+        {
 #pragma unroll
-        for (int i = 0; i < S; ++i) xn[i] = fmaf(xd[i], a.dt, x[n][i]);
+          for (int j = 0; j < kMlpOut; ++j) xd[2 + j] = y[n][j] * nrm[23 + j] + nrm[18 + j];
+        }
+        // Euler step, two states per paired FMA
 #pragma unroll
-        for (int i = 0; i < S; ++i) x[n][i] = xn[i];
+        for (int i = 0; i + 1 < S; i += 2)
+        {
+          const f32x2 xn = fma2({ xd[i], xd[i + 1] }, { a.dt, a.dt }, { x[n][i], x[n][i + 1] });
+          x[n][i] = xn.x;
+          x[n][i + 1] = xn.y;
+        }
+        x[n][S - 1] = fmaf(xd[S - 1], a.dt, x[n][S - 1]);
       }
     }
     if (ok)

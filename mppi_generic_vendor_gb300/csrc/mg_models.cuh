@@ -40,8 +40,10 @@ struct Texels
 template <class Ar = ExactArith>
 MG_HD Texels costmap_gather(const CostmapView& m, float x, float y, Ar&& ar = Ar{})
 {
-  float px = ar.div(x - m.origin_x, m.resolution) - 0.5f;
-  float py = ar.div(y - m.origin_y, m.resolution) - 0.5f;
+  // (x, y) as a pair: offsets, the divisions by the cell size and the half-cell shift
+  const f32x2 pp = sub2(ar.div2(sub2({ x, y }, { m.origin_x, m.origin_y }), { m.resolution, m.resolution }),
+                        { 0.5f, 0.5f });
+  float px = pp.x, py = pp.y;
   px = fminf(fmaxf(px, 0.0f), (float)(m.width - 1));
   py = fminf(fmaxf(py, 0.0f), (float)(m.height - 1));
   int x0 = (int)floorf(px);
@@ -49,8 +51,9 @@ MG_HD Texels costmap_gather(const CostmapView& m, float x, float y, Ar&& ar = Ar
   x0 = x0 < m.width - 2 ? x0 : m.width - 2;
   y0 = y0 < m.height - 2 ? y0 : m.height - 2;
   Texels t;
-  t.fx = px - (float)x0;
-  t.fy = py - (float)y0;
+  const f32x2 fr = sub2({ px, py }, { (float)x0, (float)y0 });
+  t.fx = fr.x;
+  t.fy = fr.y;
   const float* row0 = m.data + (size_t)y0 * m.width;
   const float* row1 = row0 + m.width;
 #if defined(__CUDA_ARCH__)
@@ -67,11 +70,16 @@ MG_HD Texels costmap_gather(const CostmapView& m, float x, float y, Ar&& ar = Ar
   return t;
 }
 
+// top = q00 (1 - fx) + q01 fx and bot = q10 (1 - fx) + q11 fx, then top (1 - fy) + bot fy: the products in pairs, every
+// sum scalar (a paired add of paired products is fused into a paired FMA by the code generator, which would change
+// the rounding)
 MG_HD float costmap_blend(const Texels& t)
 {
-  const float top = t.q00 * (1.0f - t.fx) + t.q01 * t.fx;
-  const float bot = t.q10 * (1.0f - t.fx) + t.q11 * t.fx;
-  return top * (1.0f - t.fy) + bot * t.fy;
+  const float gx = 1.0f - t.fx;
+  const f32x2 p = mul2({ t.q00, t.q10 }, { gx, gx });
+  const f32x2 r = mul2({ t.q01, t.q11 }, { t.fx, t.fx });
+  const f32x2 w = mul2({ p.x + r.x, p.y + r.y }, { 1.0f - t.fy, t.fy });
+  return w.x + w.y;
 }
 
 template <class Ar = ExactArith>
@@ -109,10 +117,15 @@ struct CartpoleModel
     sincos_f(th, &s, &c);
     const float td = x[3], f = u[0];
     const float mc = p.cart_mass, mp = p.pole_mass, lp = p.pole_length, g = p.gravity;
+    const float den = mc + mp * (s * s);
+    // the two accelerations' divisions as one pair
+    const float num1 = f + mp * s * (lp * (td * td) + g * c);
+    const float num3 = -f * c - mp * lp * (td * td) * c * s - (mc + mp) * g * s;
+    const f32x2 acc = ar.div2({ num1, num3 }, { den, lp * den });
     xd[0] = x[1];
-    xd[1] = ar.div(f + mp * s * (lp * (td * td) + g * c), mc + mp * (s * s));
+    xd[1] = acc.x;
     xd[2] = td;
-    xd[3] = ar.div(-f * c - mp * lp * (td * td) * c * s - (mc + mp) * g * s, lp * (mc + mp * (s * s)));
+    xd[3] = acc.y;
   }
   template <class Ar = ExactArith>
   static MG_HD float computeStateCost(const CostParams& q, const ModelAux&, const float* y, int, Ar&& ar = Ar{})
@@ -121,8 +134,12 @@ struct CartpoleModel
     float s, c;
     sincos_f(th, &s, &c);
     const float a = 1.0f + c;
-    return q.x_coeff * (y[0] * y[0]) + q.x_dot_coeff * (y[1] * y[1]) + q.cos_coeff * (a * a) +
-           q.theta_dot_coeff * (y[3] * y[3]);
+    // x_coeff x^2 + x_dot_coeff xdot^2 + cos_coeff (1 + cos)^2 + theta_dot_coeff thetadot^2, added left to right; the
+    // squares and coefficient products in pairs
+    const f32x2 s01 = { y[0], y[1] }, s23 = { a, y[3] };
+    const f32x2 t01 = mul2({ q.x_coeff, q.x_dot_coeff }, mul2(s01, s01));
+    const f32x2 t23 = mul2({ q.cos_coeff, q.theta_dot_coeff }, mul2(s23, s23));
+    return t01.x + t01.y + t23.x + t23.y;
   }
   static MG_HD float computeControlCost(const CostParams&, const float*, int) { return 0.0f; }
   template <class Ar = ExactArith>
@@ -214,8 +231,9 @@ struct BicycleCostmapModel
     float sy, cy, sd, cd;
     sincos_f(x[2], &sy, &cy);
     sincos_f(u[1], &sd, &cd);
-    xd[0] = x[3] * cy;
-    xd[1] = x[3] * sy;
+    const f32x2 vxy = mul2({ x[3], x[3] }, { cy, sy });
+    xd[0] = vxy.x;
+    xd[1] = vxy.y;
     xd[2] = ar.div(x[3] * ar.div(sd, cd), p.wheelbase);
     xd[3] = u[0];
   }
@@ -268,6 +286,8 @@ struct BicycleSlipModel
     sincos_f(x[2], &sy, &cy);
     const float vx = x[3], vy = x[4], r = x[5], d = x[6];
     const float vxs = fmaxf(vx, p.min_vx);
+    // scalar on purpose: paired forms of this model's arithmetic raise the fused rollout's register count by a third
+    // (fewer resident CTAs), which costs more than the saved instructions
     const float alpha_f = d - ar.div(vy + p.lf * r, vxs);
     const float alpha_r = ar.div(-(vy - p.lr * r), vxs);
     const float fyf = p.cornering_stiffness * alpha_f;
@@ -323,8 +343,16 @@ MG_HD void euler_step(const typename Model::DynParams& p, const float* x, const 
 {
   float xd[Model::STATE_DIM];
   Model::computeDynamics(p, x, u, xd, ar);
+  // two states per paired FMA
 #pragma unroll
-  for (int i = 0; i < Model::STATE_DIM; ++i) x_next[i] = fmaf(xd[i], dt, x[i]);
+  for (int i = 0; i + 1 < Model::STATE_DIM; i += 2)
+  {
+    const f32x2 n = fma2({ xd[i], xd[i + 1] }, { dt, dt }, { x[i], x[i + 1] });
+    x_next[i] = n.x;
+    x_next[i + 1] = n.y;
+  }
+  if constexpr (Model::STATE_DIM % 2 == 1)
+    x_next[Model::STATE_DIM - 1] = fmaf(xd[Model::STATE_DIM - 1], dt, x[Model::STATE_DIM - 1]);
 }
 
 }  // namespace mg

@@ -26,6 +26,18 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// complex sum and difference as one paired FP32 instruction each (add / sub .rn.f32x2)
+__device__ __forceinline__ float2 cadd(float2 a, float2 b)
+{
+  const f32x2 r = add2({ a.x, a.y }, { b.x, b.y });
+  return make_float2(r.x, r.y);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b)
+{
+  const f32x2 r = sub2({ a.x, a.y }, { b.x, b.y });
+  return make_float2(r.x, r.y);
+}
+
 // e^{2 pi i j / 256}, j < 128 (FP64 cos / sin rounded to float): the packing twiddles e^{2 pi i k / 2T}, the
 // half-length transforms' twiddles and the final combine's e^{2 pi i m / T}, for every T <= 128.  Indexed with
 // compile-time constants in the unrolled transforms, so each twiddle is a constant-bank operand.
@@ -64,8 +76,8 @@ __device__ __forceinline__ void ifft_dif_regs(float2 (&v)[H + 1])
       for (int j = 0; j < half; ++j)
       {
         const float2 x = v[blk + j], y = v[blk + j + half];
-        v[blk + j] = make_float2(x.x + y.x, x.y + y.y);
-        v[blk + j + half] = rot256(make_float2(x.x - y.x, x.y - y.y), j * (256 / len));
+        v[blk + j] = cadd(x, y);
+        v[blk + j + half] = rot256(csub(x, y), j * (256 / len));
       }
   }
 }
@@ -435,8 +447,8 @@ __global__ void __launch_bounds__(256, ColoredQuadShape<C, L>::MIN_CTAS)
       for (int r = 0; r <= L; ++r)
       {
         const float sc = __ldg(scale + freq(r) * C + c);
-        v[r].x *= sc;
-        v[r].y *= sc;
+        const f32x2 w = mul2({ v[r].x, v[r].y }, { sc, sc });
+        v[r] = make_float2(w.x, w.y);
       }
       v[0].y = q ? v[0].y : 0.0f;  // thread 0: the DC and Nyquist bins are real
       v[L - 1].y = q ? v[L - 1].y : 0.0f;
@@ -493,9 +505,9 @@ __global__ void __launch_bounds__(256, ColoredQuadShape<C, L>::MIN_CTAS)
         const float2 b1 = rot256(cmul(row_seg[SEG + m1], w1), 4 * i * TW);
         const float2 b2 = rot256(cmul(row_seg[2 * SEG + m1], w2), 8 * i * TW);
         const float2 b3 = rot256(cmul(row_seg[3 * SEG + m1], w3), 12 * i * TW);
-        const float2 s02 = make_float2(b0.x + b2.x, b0.y + b2.y), d02 = make_float2(b0.x - b2.x, b0.y - b2.y);
-        const float2 s13 = make_float2(b1.x + b3.x, b1.y + b3.y), d13 = make_float2(b1.x - b3.x, b1.y - b3.y);
-        z0[i] = make_float2(s02.x + s13.x, s02.y + s13.y);  // m2 = 0
+        const float2 s02 = cadd(b0, b2), d02 = csub(b0, b2);
+        const float2 s13 = cadd(b1, b3), d13 = csub(b1, b3);
+        z0[i] = cadd(s02, s13);  // m2 = 0
         z1[i] = make_float2(d02.x - d13.y, d02.y + d13.x);  // m2 = 1: b0 + i b1 - b2 - i b3
         if (i == i_o)
         {
@@ -516,8 +528,11 @@ __global__ void __launch_bounds__(256, ColoredQuadShape<C, L>::MIN_CTAS)
         {
           const float2 z = m2 ? z1[i] : z0[i];
           const int t0 = 8 * i + 2 * q + 2 * L * m2;
-          tile_row[tile_pos(t0, 0, C)] = (z.x - x_off * __ldg(decay_t + t0)) * inv_div;
-          tile_row[tile_pos(t0 + 1, 0, C)] = (z.y - x_off * __ldg(decay_t + t0 + 1)) * inv_div;
+          // (x[t] - x[offset] decay^t) / (sigma_c 2T) for the output pair (t0, t0 + 1)
+          const f32x2 e = mul2(fma2({ -x_off, -x_off }, { __ldg(decay_t + t0), __ldg(decay_t + t0 + 1) }, { z.x, z.y }),
+                               { inv_div, inv_div });
+          tile_row[tile_pos(t0, 0, C)] = e.x;
+          tile_row[tile_pos(t0 + 1, 0, C)] = e.y;
         }
       }
     }

@@ -505,16 +505,49 @@ __global__ void __launch_bounds__(128) judge_rollout_kernel(const __grid_constan
   float running = 0.0f;
   PendingCost<Model> pc;
   pc.reset(x);
-  // the same step as the analytic rollout kernels
-  auto run = [&](auto lik) {
-#pragma unroll 4
-    for (int t = 0; t < d.T; ++t)
+  // the same step as the analytic rollout kernels; the controls of the next eight steps are loaded while the current
+  // eight run, so the chain of dependent steps does not wait on memory.  Rows start on 8-byte boundaries (T * C is
+  // even); where T * C % 4 == 0 they also start on 16-byte ones and the eight steps are four 16-byte loads.
+  const bool quads = ((d.T * C) & 3) == 0;
+  const float4* uq = reinterpret_cast<const float4*>(urow);
+  const float2* up = reinterpret_cast<const float2*>(urow);
+  auto load8 = [&](int t0, float2 (&dst)[8]) {
+    if (quads)
     {
-      const float2 uv = __ldg(reinterpret_cast<const float2*>(urow + t * C));
-      const float u[2] = { uv.x, uv.y };
-      speculate_steps<Model>(x, running, pc, [&](auto& ar) {
-        rollout_step<Model, decltype(lik)::value>(a.r, d, dp, cp, k, u, t, x, running, pc, ar);
-      });
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        const float4 q = t0 + 2 * j < d.T ? __ldg(uq + t0 / 2 + j) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        dst[2 * j] = make_float2(q.x, q.y);
+        dst[2 * j + 1] = make_float2(q.z, q.w);
+      }
+    }
+    else
+    {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) dst[j] = t0 + j < d.T ? __ldg(up + t0 + j) : make_float2(0.0f, 0.0f);
+    }
+  };
+  auto run = [&](auto lik) {
+    float2 cur[8], nxt[8];
+    load8(0, cur);
+    for (int t0 = 0; t0 < d.T; t0 += 8)
+    {
+      if (t0 + 8 < d.T) load8(t0 + 8, nxt);
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+      {
+        const int t = t0 + s;
+        if (t < d.T)
+        {
+          const float u[2] = { cur[s].x, cur[s].y };
+          speculate_steps<Model>(x, running, pc, [&](auto& ar) {
+            rollout_step<Model, decltype(lik)::value>(a.r, d, dp, cp, k, u, t, x, running, pc, ar);
+          });
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) cur[j] = nxt[j];
     }
     rollout_flush<Model, decltype(lik)::value>(a.r, d, cp, k, running, pc);
   };

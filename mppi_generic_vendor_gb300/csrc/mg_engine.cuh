@@ -620,8 +620,9 @@ public:
   }
   // The cooperative rollout (four lanes per sample) needs the fused Gaussian sampler and an analytic model.
   bool coop_available() const { return fusable() && !(Model::kMlp && !use_analytic_); }
-  // Mode 3 runs the Gaussian sampler as its own kernel and the staged rollout on the written samples.
-  bool unfused_available() const { return fusable() && !(Model::kMlp && !use_analytic_); }
+  // Mode 3 runs the Gaussian sampler as its own kernel and the rollout on the written samples (for the surrogate:
+  // the tensor-core rollout reading its controls from memory instead of drawing them).
+  bool unfused_available() const { return fusable(); }
   // Mode 4 is the fused rollout with noise warps; it reads its controls from the shared-memory stage, so the longest
   // horizon must fit the stage of the smallest tile (tile sizes whose stage does not fit run mode 0's kernel).
   bool noise_warps_available() const
@@ -642,8 +643,7 @@ public:
              "the split rollout needs Gaussian sampling, T*C %% 4 == 0, an analytic model and <= 256 MB of states");
     MG_CHECK(mode != 2 || coop_available(), "the cooperative rollout needs Gaussian sampling, T*C %% 4 == 0 and an "
              "analytic model");
-    MG_CHECK(mode != 3 || unfused_available(), "rollout mode 3 needs Gaussian sampling, T*C %% 4 == 0 and an analytic "
-             "model");
+    MG_CHECK(mode != 3 || unfused_available(), "rollout mode 3 needs Gaussian sampling and T*C %% 4 == 0");
     MG_CHECK(mode != 4 || noise_warps_available(), "rollout mode 4 needs Gaussian sampling, T*C %% 4 == 0, an analytic "
              "model and a horizon whose controls fit the shared-memory stage");
     if (mode == 1 && !states_d_.p) MG_TRY(states_d_.alloc((size_t)total_u_ / C * S));

@@ -516,6 +516,22 @@ def run_gpu(args, ws, rank, local):
         dom = 1
         peak, peak_kind = measured_peaks("tensor")
         achieved = MLP_FLOPS * steps_per_iter / (kms[1] * 1e-3) / 1e12
+    sfu = None
+    sfile = ROOT / "profiles" / "sfu.json"
+    if surrogate and sfile.exists():
+        try:
+            sj = json.loads(sfile.read_text())
+            ent = sj.get(wl.name)
+            if ent:
+                # the unit that binds the surrogate rollout: every hidden activation is one MUFU tanh
+                ach = float(ent["mufu_ops_per_sample_step"]) * steps_per_iter / (kms[1] * 1e-3)
+                peak_sfu = float(sj["peak_mufu_ops_per_s"])
+                sfu = {"unit": "MUFU ops/s", "achieved": ach, "peak": peak_sfu, "frac": ach / peak_sfu,
+                       "ops_per_sample_step": float(ent["mufu_ops_per_sample_step"]),
+                       "peak_kind": "measured (tests/cuda/sfu_throughput.cu)",
+                       "time": "rollout incl. judge kernels"}
+        except Exception:
+            sfu = None
     traffic = None
     tfile = ROOT / "profiles" / "dram_traffic.json"
     if tfile.exists():
@@ -556,7 +572,7 @@ def run_gpu(args, ws, rank, local):
                       "algorithmic_bytes": abytes[names[dom]]} if not surrogate else
                      {"bound": "tensor", "kernel": "rollout (surrogate + judge)", "achieved": achieved, "peak": peak,
                       "unit": "TFLOP/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                      "algorithmic_flops": MLP_FLOPS * steps_per_iter}),
+                      "algorithmic_flops": MLP_FLOPS * steps_per_iter, "binding_unit_sfu": sfu}),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "iters_per_s": ws * iters / e2e_s},
         "gpu_launches": kernels * args.steps,

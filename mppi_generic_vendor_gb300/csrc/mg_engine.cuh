@@ -125,6 +125,7 @@ inline SampleShared make_sample_shared(const mppi_sampling_params& sp, const mpp
   for (int i = 0; i < kMaxC; ++i)
   {
     sh.std_dev[i] = sp.std_dev[i];
+    sh.inv_var[i] = 1.0f / (sp.std_dev[i] * sp.std_dev[i]);
     sh.control_cost_coeff[i] = sp.control_cost_coeff[i];
     sh.lower[i] = cc.lower[i];
     sh.upper[i] = cc.upper[i];

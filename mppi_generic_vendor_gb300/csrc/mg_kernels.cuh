@@ -38,6 +38,7 @@ struct InstDesc
 struct SampleShared
 {
   float std_dev[kMaxC];
+  float inv_var[kMaxC];  // 1 / std_dev^2 (the surrogate rollout's likelihood term multiplies by it)
   float control_cost_coeff[kMaxC];
   float lower[kMaxC], upper[kMaxC], deadband[kMaxC], zero[kMaxC];
   float pure_pct;

@@ -190,6 +190,25 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
     }
     // Step t's running cost is added at step t + 1: its costmap texels are gathered before step t + 1's network
     // pass, which hides their latency, and blended after it.  The sum keeps step order.
+    // The tensor-core forms are held to tolerances, so there the step's divisions by constants (the costmap's cell
+    // size, the control variances) become products with host-computed reciprocals (kernel parameters): the
+    // special-function unit that bounds this kernel then does no per-step division work.
+    auto gather = [&](float px, float py) {
+      if constexpr (kTensor)
+      {
+        const float ir = a.aux.map.inv_resolution;
+        const f32x2 c = sub2(mul2(sub2({ px, py }, { a.aux.map.origin_x, a.aux.map.origin_y }), { ir, ir }),
+                             { 0.5f, 0.5f });
+        return costmap_gather_cell(a.aux.map, c.x, c.y);
+      }
+      else
+      {
+        FastArith fa;
+        Texels t = costmap_gather(a.aux.map, px, py, fa);
+        if (__builtin_expect(!fa.ok, 0)) t = costmap_gather(a.aux.map, px, py);
+        return t;
+      }
+    };
     auto step_cost_tx = [&](int n, const Texels& tx, const float* yv, const float* uv, int tt) {
       float c = Model::stateCostFromTexels(cp, tx, yv) + Model::computeControlCost(cp, uv, tt);
       if (a.use_likelihood)
@@ -202,9 +221,17 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
         const f32x2 sd = { a.sh.std_dev[0], a.sh.std_dev[1] };
         const f32x2 num = mul2(mul2({ a.sh.control_cost_coeff[0], a.sh.control_cost_coeff[1] }, m),
                                sub2(m, add2({ uv[0], uv[1] }, { uv[0], uv[1] })));
-        FastArith fa;
-        f32x2 q = fa.div2(num, mul2(sd, sd));
-        if (__builtin_expect(!fa.ok, 0)) q = ExactArith{}.div2(num, mul2(sd, sd));
+        f32x2 q;
+        if constexpr (kTensor)
+        {
+          q = mul2(num, { a.sh.inv_var[0], a.sh.inv_var[1] });  // the surrogate forms: products with reciprocals
+        }
+        else
+        {
+          FastArith fa;
+          q = fa.div2(num, mul2(sd, sd));
+          if (__builtin_expect(!fa.ok, 0)) q = ExactArith{}.div2(num, mul2(sd, sd));
+        }
         float lc = 0.0f;
         lc += q.x;
         lc += q.y;
@@ -222,12 +249,7 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
 #pragma unroll
       for (int n = 0; n < NT; ++n)
       {
-        {
-          // the state step t - 1 produced; branch-free division, IEEE fallback when out of its exact range
-          FastArith fa;
-          tx[n] = costmap_gather(a.aux.map, x[n][0], x[n][1], fa);
-          if (__builtin_expect(!fa.ok, 0)) tx[n] = costmap_gather(a.aux.map, x[n][0], x[n][1]);
-        }
+        tx[n] = gather(x[n][0], x[n][1]);  // the state step t - 1 produced
         if constexpr (kFused)
         {
           // Gaussian sampling fused in, quad by quad, exactly as gaussian_sample_kernel would have written it
@@ -328,7 +350,7 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
 #pragma unroll
       for (int n = 0; n < NT; ++n)
         if (active[n] && d.T > 0)
-          running[n] += step_cost_tx(n, costmap_gather(a.aux.map, x[n][0], x[n][1]), x[n], up[n], d.T - 1);
+          running[n] += step_cost_tx(n, gather(x[n][0], x[n][1]), x[n], up[n], d.T - 1);
     if (!ok)
     {
       if (tid == 0) atomicOr(a.status, 1u);

@@ -22,7 +22,7 @@ struct CostmapView
 {
   const float* data;
   int width, height;
-  float inv_resolution;  // unused by the lookup (kept for callers); the lookup divides by resolution
+  float inv_resolution;  // 1 / resolution: the surrogate rollout's lookup multiplies by it; the exact one divides
   float resolution, origin_x, origin_y;
 };
 
@@ -35,15 +35,9 @@ struct Texels
   float q00, q01, q10, q11, fx, fy;
 };
 
-// The four texels and the interpolation fractions of point (x, y); split from the blend so a rollout can issue the
-// loads well before it needs the value.
-template <class Ar = ExactArith>
-MG_HD Texels costmap_gather(const CostmapView& m, float x, float y, Ar&& ar = Ar{})
+// The texels and fractions around cell coordinates (px, py) (clamped to the map).
+MG_HD Texels costmap_gather_cell(const CostmapView& m, float px, float py)
 {
-  // (x, y) as a pair: offsets, the divisions by the cell size and the half-cell shift
-  const f32x2 pp = sub2(ar.div2(sub2({ x, y }, { m.origin_x, m.origin_y }), { m.resolution, m.resolution }),
-                        { 0.5f, 0.5f });
-  float px = pp.x, py = pp.y;
   px = fminf(fmaxf(px, 0.0f), (float)(m.width - 1));
   py = fminf(fmaxf(py, 0.0f), (float)(m.height - 1));
   int x0 = (int)floorf(px);
@@ -68,6 +62,17 @@ MG_HD Texels costmap_gather(const CostmapView& m, float x, float y, Ar&& ar = Ar
   t.q11 = row1[x0 + 1];
 #endif
   return t;
+}
+
+// The four texels and the interpolation fractions of point (x, y); split from the blend so a rollout can issue the
+// loads well before it needs the value.
+template <class Ar = ExactArith>
+MG_HD Texels costmap_gather(const CostmapView& m, float x, float y, Ar&& ar = Ar{})
+{
+  // (x, y) as a pair: offsets, the divisions by the cell size and the half-cell shift
+  const f32x2 pp = sub2(ar.div2(sub2({ x, y }, { m.origin_x, m.origin_y }), { m.resolution, m.resolution }),
+                        { 0.5f, 0.5f });
+  return costmap_gather_cell(m, pp.x, pp.y);
 }
 
 // top = q00 (1 - fx) + q01 fx and bot = q10 (1 - fx) + q11 fx, then top (1 - fy) + bot fy: the products in pairs, every

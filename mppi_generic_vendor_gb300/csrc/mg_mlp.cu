@@ -103,6 +103,32 @@ __device__ __forceinline__ void mlp_thread_forward(const float* P, const float* 
   }
 }
 
+// costmap_gather_cell for the surrogate rollout: the cell index by round-to-nearest of p - 1/2 through the 1.5 * 2^23
+// magic-number addition (FMA and integer pipes) instead of floorf and a float-to-int conversion, which run on the
+// special-function unit that bounds the kernel.  Where p is an integer the index may be one below floor(p) with the
+// fraction 1 instead of 0: the same bilinear value.
+__device__ __forceinline__ Texels costmap_gather_cell_rn(const CostmapView& m, float px, float py)
+{
+  px = fminf(fmaxf(px, 0.0f), (float)(m.width - 1));
+  py = fminf(fmaxf(py, 0.0f), (float)(m.height - 1));
+  const float magic = 12582912.0f;  // 1.5 * 2^23: the sum's last mantissa bit has weight 1
+  const f32x2 r = add2(sub2({ px, py }, { 0.5f, 0.5f }), { magic, magic });
+  int x0 = (int)(__float_as_uint(r.x) - __float_as_uint(magic));
+  int y0 = (int)(__float_as_uint(r.y) - __float_as_uint(magic));
+  x0 = min(max(x0, 0), m.width - 2);
+  y0 = min(max(y0, 0), m.height - 2);
+  Texels t;
+  t.fx = px - (float)x0;
+  t.fy = py - (float)y0;
+  const float* row0 = m.data + (size_t)y0 * m.width;
+  const float* row1 = row0 + m.width;
+  t.q00 = __ldg(row0 + x0);
+  t.q01 = __ldg(row0 + x0 + 1);
+  t.q10 = __ldg(row1 + x0);
+  t.q11 = __ldg(row1 + x0 + 1);
+  return t;
+}
+
 // Surrogate rollout: BicycleSlipModel with the (yaw, vx, vy, yaw_rate, steer) derivatives from the MLP and the
 // x / y rows analytic (NeuralNetModel::computeKinematics, ar_nn_model.cu:119-124).  Persistent CTAs of 128 threads
 // walk work items of 128 * kMlpTiles samples of one instance; thread i owns row i of every tile (samples
@@ -199,7 +225,7 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
         const float ir = a.aux.map.inv_resolution;
         const f32x2 c = sub2(mul2(sub2({ px, py }, { a.aux.map.origin_x, a.aux.map.origin_y }), { ir, ir }),
                              { 0.5f, 0.5f });
-        return costmap_gather_cell(a.aux.map, c.x, c.y);
+        return costmap_gather_cell_rn(a.aux.map, c.x, c.y);
       }
       else
       {

@@ -1687,7 +1687,7 @@ __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_consta
                     ((reinterpret_cast<uintptr_t>(ubase) | reinterpret_cast<uintptr_t>(prow)) & 15) == 0;
   if (vec4)
   {
-    // 16-byte loads, four samples in flight per thread: G groups of Q = TC / 4 threads, thread (g, j) sums float4
+    // 16-byte loads, up to eight samples in flight per thread: G groups of Q = TC / 4 threads, thread (g, j) sums float4
     // column j over samples g, g + G, ... in four interleaved accumulators, then the groups are combined in group
     // order (a fixed order, so the result does not depend on scheduling)
     __shared__ float4 s_part4[256];
@@ -1705,6 +1705,21 @@ __global__ void __launch_bounds__(256) weights_update_kernel(const __grid_consta
     {
       float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
       int i = g;
+      // eight 16-byte loads in flight per thread, then four per thread, then one
+      for (; i + 7 * G < nk; i += 8 * G)
+      {
+        float4 v[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) v[m] = __ldg(ub + (long long)(i + m * G) * Q + j);
+        fma4(s_w[i], v[0], a0);
+        fma4(s_w[i + G], v[1], a1);
+        fma4(s_w[i + 2 * G], v[2], a2);
+        fma4(s_w[i + 3 * G], v[3], a3);
+        fma4(s_w[i + 4 * G], v[4], a0);
+        fma4(s_w[i + 5 * G], v[5], a1);
+        fma4(s_w[i + 6 * G], v[6], a2);
+        fma4(s_w[i + 7 * G], v[7], a3);
+      }
       for (; i + 3 * G < nk; i += 4 * G)
       {
         const float4 v0 = __ldg(ub + (long long)i * Q + j);

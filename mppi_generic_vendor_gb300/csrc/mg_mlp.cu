@@ -422,28 +422,32 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
   }
 }
 
-// Exclusive prefix count of `flag` over the CTA in thread order (ballot + popc per warp, one warp scans the warp
-// totals); *total receives the CTA's count.  s_warp holds 64 ints.  Every thread of the CTA must call it.
-__device__ __forceinline__ int block_excl_count(bool flag, int* s_warp, int* total)
+// Exclusive prefix counts of two flags over the CTA in thread order (ballot + popc per warp, one warp scans the
+// warp totals), packed as (count of f0) | (count of f1) << 16; *total receives the CTA's packed counts.  s_warp
+// holds 64 words; counts stay below 2^16 for blockDim.x <= 1024.  Every thread of the CTA must call it (three CTA
+// barriers).
+__device__ __forceinline__ unsigned int block_excl_count2(bool f0, bool f1, unsigned int* s_warp,
+                                                          unsigned int* total)
 {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const unsigned int b = __ballot_sync(0xffffffffu, flag);
-  const int in_warp = __popc(b & ((1u << lane) - 1u));
-  if (lane == 0) s_warp[warp] = __popc(b);
+  const unsigned int b0 = __ballot_sync(0xffffffffu, f0), b1 = __ballot_sync(0xffffffffu, f1);
+  const unsigned int below = (1u << lane) - 1u;
+  const unsigned int in_warp = (unsigned int)__popc(b0 & below) | ((unsigned int)__popc(b1 & below) << 16);
+  if (lane == 0) s_warp[warp] = (unsigned int)__popc(b0) | ((unsigned int)__popc(b1) << 16);
   __syncthreads();
   if (warp == 0)
   {
-    int v = lane < nw ? s_warp[lane] : 0;
+    unsigned int v = lane < nw ? s_warp[lane] : 0u;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1)
     {
-      const int n = __shfl_up_sync(0xffffffffu, v, off);
+      const unsigned int n = __shfl_up_sync(0xffffffffu, v, off);
       if (lane >= off) v += n;
     }
     s_warp[32 + lane] = v;  // inclusive
   }
   __syncthreads();
-  const int before = warp ? s_warp[32 + warp - 1] : 0;
+  const unsigned int before = warp ? s_warp[32 + warp - 1] : 0u;
   *total = s_warp[32 + nw - 1];
   __syncthreads();
   return before + in_warp;
@@ -462,48 +466,91 @@ __device__ __forceinline__ unsigned int block_min_u32(unsigned int v, unsigned i
 
 // One CTA per instance: radix selection (4 passes of 8 bits over the ordered-int costs) of the M-th smallest key,
 // then an index-ordered compaction of the keys below it plus the first ties, so the judged set and its order are
-// deterministic.  Also records the minimum over the samples that are not judged.
+// deterministic.  Also records the minimum over the samples that are not judged.  The first 16 keys of each thread
+// (K <= 16384 at 1024 threads) stay in registers across the passes; keys beyond are read again per pass.
 __global__ void __launch_bounds__(1024) judge_select_kernel(const __grid_constant__ JudgeArgs a)
 {
+  constexpr int KR = 16;
   __shared__ unsigned int hist[256];
-  __shared__ int s_warp[64];
+  __shared__ unsigned int s_warp[64];
   __shared__ unsigned int s_min[32];
   __shared__ unsigned int s_bin, s_need;
-  const int i = blockIdx.x, tid = threadIdx.x;
+  const int i = blockIdx.x, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
   const int base = a.sel_off[i], M = a.sel_off[i + 1] - base;
   const InstDesc d = a.r.inst[i];
+  const int K = d.K;
   const float* c = a.r.costs + d.k_off;
   if (M <= 0)
   {
     if (tid == 0) a.unjudged_min[i] = a.r.baseline_bits[i];
     return;
   }
+  unsigned int kc[KR];
+#pragma unroll
+  for (int r = 0; r < KR; ++r)
+  {
+    const int k = tid + r * nt;
+    kc[r] = k < K ? float_to_ordered(c[k]) : 0u;
+  }
+  const int cached = KR * nt;
+
   unsigned int prefix = 0u, mask = 0u, need = (unsigned int)M;
   for (int shift = 24; shift >= 0; shift -= 8)
   {
-    for (int b = tid; b < 256; b += blockDim.x) hist[b] = 0u;
+    for (int b = tid; b < 256; b += nt) hist[b] = 0u;
     __syncthreads();
     // the costs share their leading bits, so most lanes of a warp hit the same bin: one atomic per distinct bin
     // and warp (__match_any_sync) instead of one per lane
-    for (int k0 = 0; k0 < d.K; k0 += blockDim.x)
+    auto count = [&](unsigned int key, bool valid) {
+      const unsigned int bin = (valid && (key & mask) == prefix) ? ((key >> shift) & 255u) : 256u;
+      const unsigned int same = __match_any_sync(0xffffffffu, bin);
+      if (bin < 256u && lane == __ffs(same) - 1) atomicAdd(&hist[bin], __popc(same));
+    };
+#pragma unroll
+    for (int r = 0; r < KR; ++r)
+    {
+      if (r * nt >= K) break;  // CTA-uniform
+      count(kc[r], tid + r * nt < K);
+    }
+    for (int k0 = cached; k0 < K; k0 += nt)
     {
       const int k = k0 + tid;
-      const unsigned int key = k < d.K ? float_to_ordered(c[k]) : 0u;
-      const unsigned int bin = (k < d.K && (key & mask) == prefix) ? ((key >> shift) & 255u) : 256u;
-      const unsigned int same = __match_any_sync(0xffffffffu, bin);
-      if (bin < 256u && (threadIdx.x & 31) == (unsigned int)(__ffs(same) - 1)) atomicAdd(&hist[bin], __popc(same));
+      count(k < K ? float_to_ordered(c[k]) : 0u, k < K);
     }
     __syncthreads();
-    if (tid == 0)
+    // the first bin b whose inclusive count reaches `need` (255 if none does): lane L of warp 0 holds bins
+    // 8L .. 8L+7, an inclusive scan over the lanes finds the lane, and that lane walks its eight bins
+    if (tid < 32)
     {
-      unsigned int cum = 0u, b = 0u;
-      for (; b < 255u; ++b)
+      unsigned int h[8], own = 0u;
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
       {
-        if (cum + hist[b] >= need) break;
-        cum += hist[b];
+        h[j] = hist[8 * lane + j];
+        own += h[j];
       }
-      s_bin = b;
-      s_need = need - cum;
+      unsigned int incl = own;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1)
+      {
+        const unsigned int n = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += n;
+      }
+      const unsigned int reach = __ballot_sync(0xffffffffu, incl >= need);
+      const int L = reach ? __ffs(reach) - 1 : 31;
+      if (lane == L)
+      {
+        unsigned int cum = incl - own;
+        int b = 7;
+#pragma unroll
+        for (int j = 0; j < 7; ++j)
+        {
+          if (b == 7 && cum + h[j] >= need) b = j;
+          if (b == 7) cum += h[j];
+        }
+        s_bin = 8u * (unsigned int)L + (unsigned int)b;
+        s_need = need - cum;
+      }
     }
     __syncthreads();
     prefix |= s_bin << shift;
@@ -511,24 +558,32 @@ __global__ void __launch_bounds__(1024) judge_select_kernel(const __grid_constan
     need = s_need;
     __syncthreads();
   }
-  const unsigned int thr = prefix;
-  const int need_eq = (int)need;
-  int n_eq = 0, n_sel = 0;
-  unsigned int my_min = kOrderedPosInf;
-  for (int k0 = 0; k0 < d.K; k0 += blockDim.x)
+  // compaction: sample k is judged when key < thr, or key == thr among the first need_eq ties; its slot is the
+  // number of judged samples before it in index order: (keys below thr before it) + min(ties before it, need_eq)
+  const unsigned int thr = prefix, need_eq = need;
+  unsigned int n_lt = 0u, n_eq = 0u, my_min = kOrderedPosInf;
+  auto place = [&](unsigned int key, bool valid, int k) {
+    const bool lt = valid && key < thr, eq = valid && key == thr;
+    unsigned int tot;
+    const unsigned int ex = block_excl_count2(lt, eq, s_warp, &tot);
+    const unsigned int r_eq = n_eq + (ex >> 16);
+    const bool sel = lt || (eq && r_eq < need_eq);
+    const unsigned int pos = n_lt + (ex & 0xffffu) + min(r_eq, need_eq);
+    if (sel && pos < (unsigned int)M) a.sel[base + pos] = k;
+    if (valid && !sel) my_min = min(my_min, key);
+    n_lt += tot & 0xffffu;
+    n_eq += tot >> 16;
+  };
+#pragma unroll
+  for (int r = 0; r < KR; ++r)
+  {
+    if (r * nt >= K) break;  // CTA-uniform
+    place(kc[r], tid + r * nt < K, tid + r * nt);
+  }
+  for (int k0 = cached; k0 < K; k0 += nt)
   {
     const int k = k0 + tid;
-    const bool valid = k < d.K;
-    const unsigned int key = valid ? float_to_ordered(c[k]) : 0u;
-    const bool eq = valid && key == thr;
-    int tot;
-    const int r_eq = n_eq + block_excl_count(eq, s_warp, &tot);
-    n_eq += tot;
-    const bool sel = valid && (key < thr || (eq && r_eq < need_eq));
-    const int pos = n_sel + block_excl_count(sel, s_warp, &tot);
-    n_sel += tot;
-    if (sel && pos < M) a.sel[base + pos] = k;
-    if (valid && !sel) my_min = min(my_min, key);
+    place(k < K ? float_to_ordered(c[k]) : 0u, k < K, k);
   }
   const unsigned int m = block_min_u32(my_min, s_min);
   if (tid == 0) a.unjudged_min[i] = m;

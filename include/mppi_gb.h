@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define MPPI_GB_ABI_VERSION 2
+#define MPPI_GB_ABI_VERSION 3
 #define MPPI_MAX_STATE_DIM 8
 #define MPPI_MAX_CONTROL_DIM 4
 #define MPPI_MAX_OBSTACLES 8
@@ -78,7 +78,7 @@ typedef enum mppi_controller_kind
                                   nominal pair takes over the actual pair's state and control sequences when the
                                   actual baseline is below the nominal baseline + nominal_threshold.  Only the
                                   nominal sequence is smoothed; neither is clamped.  The ancillary feedback
-                                  controller is not part of this engine. */
+                                  controller (mppi_compute_feedback) tracks the nominal system. */
 } mppi_controller_kind;
 
 /* ControllerParams (include/mppi/controllers/controller.cuh:46-68) and the fields ColoredMPPIParams adds
@@ -290,6 +290,49 @@ mppi_status mppi_select_top_samples(const float* weights, int num_samples, int n
 /* Tube-MPPI handles: 1 if the last iteration kept the nominal system (its baseline was not beaten by the actual
  * system's, FreeEnergyStatistics::nominal_state_used), else 0. */
 mppi_status mppi_get_nominal_state_used(mppi_handle* h, int* used);
+
+/* ---- ancillary feedback controller: DDP around the nominal trajectory (DDPFeedback,
+ *      feedback_controllers/DDP/ddp.cu:48-120; the solver ddp/ddp.h:40-195 with the tracking costs of
+ *      ddp/ddp_tracking_costs.h), computed on the host after a solve.  It serves a handle with one instance, or a
+ *      Tube-MPPI handle, where it tracks the nominal system (getControlSeq / getTargetStateSeq of
+ *      tube_mppi_controller.cuh:61-72). ------------------------------------------------------------------------ */
+
+/* DDPParams (feedback_controllers/DDP/ddp.cuh:16-25): tracking weights Q and Q_f (STATE_DIM x STATE_DIM) and R
+ * (CONTROL_DIM x CONTROL_DIM), column-major; NULL keeps the current matrix (identity at creation); num_iterations
+ * >= 1 (1 at creation). */
+mppi_status mppi_set_feedback_params(mppi_handle* h, const float* Q, const float* Q_f, const float* R,
+                                     int num_iterations);
+/* 1: Controller::initFeedback (controller.cuh:265-269), feedback on with the gains reset to zero; 0:
+ * disableFeedbackController (controller.cuh:730-733). */
+mppi_status mppi_enable_feedback(mppi_handle* h, int enable);
+/* Controller::getFeedbackEnabled (controller.cuh:740-743). */
+mppi_status mppi_get_feedback_enabled(const mppi_handle* h, int* enabled);
+/* Controller::computeFeedback(state) (controller.cuh:551-565): DDP from `state` (host float[STATE_DIM]) around the
+ * nominal state trajectory and the control sequence of the last solve, for the gains of every step; nothing while
+ * feedback is off.  MPPI_EINVAL when a control Hessian of the backward pass is not positive definite, where the
+ * reference's solver exits the process (ddp.h:130-139). */
+mppi_status mppi_compute_feedback(mppi_handle* h, const float* state);
+/* The gains (DDPFeedbackState::fb_gain_traj_, ddp.cuh:28-37): host float[T][CONTROL_DIM * STATE_DIM], step t's
+ * CONTROL_DIM x STATE_DIM matrix column-major (element (r, c) at t * C * S + r + c * C); the last step's is zero. */
+mppi_status mppi_get_feedback_gains(const mppi_handle* h, float* out);
+/* Controller::getFeedbackControl (controller.cuh:567-571) = DDPFeedback::k_ (ddp.cuh:139-146): out[CONTROL_DIM] =
+ * K_t (state - goal_state), 0 <= t < T. */
+mppi_status mppi_get_feedback_control(const mppi_handle* h, const float* state, const float* goal_state, int t,
+                                      float* out);
+/* Controller::computeFeedbackPropagatedStateSeq + getFeedbackPropagatedStateSeq (controller.cuh:495-524): host
+ * float[T][STATE_DIM], from the state the last solve started at, each step under the nominal control plus the
+ * feedback against that step's target state, stepped by the model without constraints.  Recomputed while feedback
+ * is on; with feedback off the previous result (zeros at first) is returned. */
+mppi_status mppi_get_feedback_propagated_state_seq(mppi_handle* h, float* out);
+/* The same solver without a handle or a GPU, over a built-in analytic model's host dynamics (MPPI_MODEL_CARTPOLE,
+ * DOUBLE_INTEGRATOR, BICYCLE_COSTMAP with analytic Jacobians; BICYCLE_SLIP with forward differences): gains_out
+ * receives float[T][CONTROL_DIM * STATE_DIM] for the nominal trajectory target_states[T][STATE_DIM] /
+ * nominal_controls[T][CONTROL_DIM] from x0, control range control_min / control_max, weights as above (NULL =
+ * identity). */
+mppi_status mppi_ddp_feedback_gains(int model, const void* dyn_params, size_t dyn_bytes, int num_timesteps, float dt,
+                                    const float* x0, const float* target_states, const float* nominal_controls,
+                                    const float* Q, const float* Q_f, const float* R, int num_iterations,
+                                    const float* control_min, const float* control_max, float* gains_out);
 /* Free-energy statistics of instance i (MPPIFreeEnergyStatistics, controller.cuh:22-38; computeFreeEnergy,
  * mppi_common.cu:1101-1117): out[0..5] = mean, variance, modified variance, normaliser percent, increase,
  * previous baseline. */

@@ -12,7 +12,10 @@
 #ifndef MPPI_GB_HPP
 #define MPPI_GB_HPP
 
+#include <algorithm>
 #include <array>
+#include <atomic>
+#include <cmath>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -202,8 +205,83 @@ struct ColoredNoiseDistribution
   }
 };
 
-// Feedback controllers are not on the engine's path (DDP is out of its scope); the slot of the reference's
-// constructor is kept and ignored.
+// ---- the ancillary feedback controller: DDPFeedback<DYN_T, NUM_TIMESTEPS> (feedback_controllers/DDP/ddp.cuh:104-160)
+
+template <int N>
+std::array<float, N * N> identity_matrix()
+{
+  std::array<float, N * N> m{};
+  for (int i = 0; i < N; ++i) m[(size_t)i * N + i] = 1.0f;
+  return m;
+}
+
+// DDPParams (ddp.cuh:16-25): tracking weights Q, Q_f (STATE_DIM x STATE_DIM) and R (CONTROL_DIM x CONTROL_DIM),
+// column-major like the reference's Eigen matrices, identities by default, and the number of DDP iterations.
+template <class DYN_T>
+struct DDPParams
+{
+  static constexpr int S = DYN_T::STATE_DIM, C = DYN_T::CONTROL_DIM;
+  std::array<float, S * S> Q = identity_matrix<S>();
+  std::array<float, S * S> Q_f = identity_matrix<S>();
+  std::array<float, C * C> R = identity_matrix<C>();
+  int num_iterations = 1;
+};
+
+// DDPFeedbackState (ddp.cuh:28-37): per step a CONTROL_DIM x STATE_DIM gain, column-major.
+template <class DYN_T, int N_TIMESTEPS>
+struct DDPFeedbackState
+{
+  static constexpr int FEEDBACK_SIZE = DYN_T::CONTROL_DIM * DYN_T::STATE_DIM * N_TIMESTEPS;
+  static constexpr int NUM_TIMESTEPS = N_TIMESTEPS;
+  std::array<float, FEEDBACK_SIZE> fb_gain_traj_{};
+  bool operator==(const DDPFeedbackState& other) const { return fb_gain_traj_ == other.fb_gain_traj_; }
+};
+
+// The object a controller is built with.  It holds the DDPParams; the controller's handle runs the solver
+// (mppi_compute_feedback) on the host after a solve, and setParams reaches every controller built with it, as the
+// reference's controller shares the feedback object.
+template <class DYN_T, int NUM_TIMESTEPS>
+class DDPFeedback
+{
+public:
+  using TEMPLATED_PARAMS = DDPParams<DYN_T>;
+  using TEMPLATED_FEEDBACK_STATE = DDPFeedbackState<DYN_T, NUM_TIMESTEPS>;
+  DDPFeedback(DYN_T* model, float dt, int num_timesteps = NUM_TIMESTEPS)
+      : model_(model), dt_(dt), num_timesteps_(num_timesteps)
+  {
+  }
+  TEMPLATED_PARAMS getParams() const { return params_; }
+  void setParams(const TEMPLATED_PARAMS& params)
+  {
+    params_ = params;
+    for (mppi_handle* h : handles_) push(h);
+  }
+  float getDt() const { return dt_; }
+  int getNumTimesteps() const { return num_timesteps_; }
+
+  // used by the controllers built with this object
+  void attach(mppi_handle* h)
+  {
+    handles_.push_back(h);
+    push(h);
+  }
+  void detach(mppi_handle* h) { handles_.erase(std::remove(handles_.begin(), handles_.end(), h), handles_.end()); }
+
+private:
+  void push(mppi_handle* h) const
+  {
+    check(mppi_set_feedback_params(h, params_.Q.data(), params_.Q_f.data(), params_.R.data(), params_.num_iterations),
+          "mppi_set_feedback_params");
+  }
+  DYN_T* model_;
+  float dt_;
+  int num_timesteps_;
+  TEMPLATED_PARAMS params_{};
+  std::vector<mppi_handle*> handles_;
+};
+
+// No feedback object: the slot of the reference's constructor left empty; turning feedback on then tracks with
+// identity weights.
 struct NoFeedback
 {
 };
@@ -235,11 +313,14 @@ public:
   using sampled_cost_traj = std::vector<float>;
 
   // mppi_controller.cu:16-29 (Controller::Controller, controller.cuh:111-153); stream is a cudaStream_t or null.
-  VanillaMPPIController(DYN_T* model, COST_T* cost, FB_T* /*fb_controller*/, SAMPLING_T* sampler, float dt,
+  using TEMPLATED_FEEDBACK_STATE = DDPFeedbackState<DYN_T, MAX_TIMESTEPS>;
+  using TEMPLATED_FEEDBACK_PARAMS = DDPParams<DYN_T>;
+
+  VanillaMPPIController(DYN_T* model, COST_T* cost, FB_T* fb_controller, SAMPLING_T* sampler, float dt,
                         int max_iter, float lambda, float alpha, int num_timesteps = MAX_TIMESTEPS,
                         const control_trajectory& init_control_traj = control_trajectory{}, void* stream = nullptr,
                         uint64_t seed = 0)
-      : T_(num_timesteps)
+      : T_(num_timesteps), constraints_(model->constraints)
   {
     if (num_timesteps < 1 || num_timesteps > MAX_TIMESTEPS) throw Error(MPPI_EINVAL, "num_timesteps out of range");
     mppi_default_controller_params(&params_);
@@ -257,6 +338,19 @@ public:
     try
     {
       configure(*model, *cost);
+      // the feedback object's parameters go to the handle; feedback stays off until initFeedback()
+      if constexpr (!std::is_same<FB_T, NoFeedback>::value)
+      {
+        if (fb_controller)
+        {
+          fb_controller->attach(h_);
+          fb_ = fb_controller;
+        }
+      }
+      else
+      {
+        (void)fb_controller;
+      }
     }
     catch (...)
     {
@@ -266,6 +360,8 @@ public:
   }
   ~VanillaMPPIController()
   {
+    if constexpr (!std::is_same<FB_T, NoFeedback>::value)
+      if (fb_) fb_->detach(h_);
     if (h_) mppi_destroy(h_);
   }
   VanillaMPPIController(const VanillaMPPIController&) = delete;
@@ -402,7 +498,121 @@ public:
   }
   std::vector<float> getTopTransformedCosts() const { return top_costs_; }
 
+  // ---- the feedback controller (Controller, controller.cuh:265-269, 347-414, 495-571, 730-743)
+  // The enabled flag is kept here as well, so that getCurrentControl (called by a plant's state-estimator thread
+  // while another thread optimises) does not enter the handle.
+  void initFeedback()
+  {
+    check(mppi_enable_feedback(h_, 1), "mppi_enable_feedback");
+    fb_enabled_ = true;
+  }
+  void disableFeedbackController()
+  {
+    check(mppi_enable_feedback(h_, 0), "mppi_enable_feedback");
+    fb_enabled_ = false;
+  }
+  bool getFeedbackEnabled() const { return fb_enabled_.load(); }
+  void setFeedbackParams(const TEMPLATED_FEEDBACK_PARAMS& p)
+  {
+    check(mppi_set_feedback_params(h_, p.Q.data(), p.Q_f.data(), p.R.data(), p.num_iterations),
+          "mppi_set_feedback_params");
+  }
+  // Controller::computeFeedback(state): DDP from `state` around the nominal trajectory of the last solve.
+  void computeFeedback(const state_array& state)
+  {
+    check(mppi_compute_feedback(h_, state.data()), "mppi_compute_feedback");
+  }
+  TEMPLATED_FEEDBACK_STATE getFeedbackState() const
+  {
+    TEMPLATED_FEEDBACK_STATE fb{};
+    check(mppi_get_feedback_gains(h_, fb.fb_gain_traj_.data()), "mppi_get_feedback_gains");
+    return fb;
+  }
+  // Controller::getFeedbackControl: K_t (state - goal_state).
+  control_array getFeedbackControl(const state_array& state, const state_array& goal_state, int t) const
+  {
+    control_array u{};
+    check(mppi_get_feedback_control(h_, state.data(), goal_state.data(), t, u.data()), "mppi_get_feedback_control");
+    return u;
+  }
+  void computeFeedbackPropagatedStateSeq()
+  {
+    check(mppi_get_feedback_propagated_state_seq(h_, fb_prop_.data()), "mppi_get_feedback_propagated_state_seq");
+  }
+  state_trajectory getFeedbackPropagatedStateSeq() const { return fb_prop_; }
+  // Controller::interpolateControls / interpolateState (controller.cuh:383-403): linear between the bracketing
+  // steps (both indices held inside the horizon, where the reference reads column lower + 1 unchecked).
+  control_array interpolateControls(double rel_time, const control_trajectory& c_traj) const
+  {
+    int lo, hi;
+    const double a = bracket(rel_time, &lo, &hi);
+    control_array u{};
+    for (int c = 0; c < C; ++c)
+      u[c] = (float)((1.0 - a) * c_traj[(size_t)lo * C + c] + a * c_traj[(size_t)hi * C + c]);
+    return u;
+  }
+  state_array interpolateState(const state_trajectory& s_traj, double rel_time) const
+  {
+    int lo, hi;
+    const double a = bracket(rel_time, &lo, &hi);
+    state_array x{};
+    for (int s = 0; s < S; ++s)
+      x[s] = (float)((1.0 - a) * s_traj[(size_t)lo * S + s] + a * s_traj[(size_t)hi * S + s]);
+    return x;
+  }
+  // FeedbackController::interpolateFeedback_ (feedback.cuh:216-228): the gains of the bracketing steps blended.
+  control_array interpolateFeedback(const state_array& state, const state_array& target_nominal_state,
+                                    double rel_time, const TEMPLATED_FEEDBACK_STATE& fb_state) const
+  {
+    int lo, hi;
+    const double a = bracket(rel_time, &lo, &hi);
+    control_array u{};
+    for (int r = 0; r < C; ++r)
+    {
+      float k_lo = 0.0f, k_hi = 0.0f;
+      for (int c = 0; c < S; ++c)
+      {
+        const float e = state[c] - target_nominal_state[c];
+        k_lo += fb_state.fb_gain_traj_[(size_t)lo * C * S + r + (size_t)c * C] * e;
+        k_hi += fb_state.fb_gain_traj_[(size_t)hi * C * S + r + (size_t)c * C] * e;
+      }
+      u[r] = (float)((1.0 - a) * k_lo + a * k_hi);
+    }
+    return u;
+  }
+  // Controller::getCurrentControl (controller.cuh:347-362): nominal control at rel_time plus, with feedback on,
+  // the interpolated feedback, then the constraints with a zero state (deadband, then clamp; dynamics.cu:107-126).
+  control_array getCurrentControl(const state_array& state, double rel_time, const state_array& target_nominal_state,
+                                  const control_trajectory& c_traj, const TEMPLATED_FEEDBACK_STATE& fb_state) const
+  {
+    control_array u = interpolateControls(rel_time, c_traj);
+    if (getFeedbackEnabled())
+    {
+      const control_array fb = interpolateFeedback(state, target_nominal_state, rel_time, fb_state);
+      for (int c = 0; c < C; ++c) u[c] += fb[c];
+    }
+    for (int c = 0; c < C; ++c)
+    {
+      const float db = constraints_.deadband[c];
+      if (std::fabs(u[c]) < db)
+        u[c] = constraints_.zero_control[c];
+      else
+        u[c] += db * -(float)((u[c] > 0.0f) - (u[c] < 0.0f));
+      u[c] = std::fmin(std::fmax(constraints_.lower[c], u[c]), constraints_.upper[c]);
+    }
+    return u;
+  }
+
 private:
+  double bracket(double rel_time, int* lo, int* hi) const
+  {
+    const double dt = params_.dt;
+    const int lower = (int)(rel_time / dt);
+    *lo = std::min(std::max(lower, 0), T_ - 1);
+    *hi = std::min(std::max(lower + 1, 0), T_ - 1);
+    return (rel_time - lower * dt) / dt;
+  }
+
   float baseline_normalizer(int which) const
   {
     float bn[2];
@@ -427,6 +637,10 @@ private:
 
   mppi_handle* h_ = nullptr;
   int T_ = MAX_TIMESTEPS;
+  mppi_control_constraints constraints_{};
+  FB_T* fb_ = nullptr;
+  std::atomic<bool> fb_enabled_{ false };
+  state_trajectory fb_prop_{};
   mppi_controller_params params_{};
   int top_n_ = 0;
   std::vector<int> sampled_idx_;

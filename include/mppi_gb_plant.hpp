@@ -9,10 +9,12 @@
  * (updateParameters).  A subclass provides the robot side: pubControl, pubNominalState, pubFreeEnergyStatistics,
  * checkStatus, getCurrentTime and getPoseTime, as in the reference.
  *
- * Differences from the reference: no feedback controller (the published control is the nominal sequence linearly
- * interpolated at the requested time, which is what the reference's getCurrentControl returns without feedback), no
- * buffered-dynamics hook, and the wait for a new state is bounded (max_wait_s), after which the iteration returns
- * false instead of spinning forever.
+ * With the controller's feedback on, every solve is followed by the DDP feedback computation (computeFeedback from
+ * the state optimised from) and the published control is the controller's getCurrentControl: the nominal control
+ * at the requested time plus the interpolated feedback against the interpolated nominal state, constrained.
+ *
+ * Differences from the reference: no buffered-dynamics hook, and the wait for a new state is bounded (max_wait_s),
+ * after which the iteration returns false instead of spinning forever.
  */
 #ifndef MPPI_GB_PLANT_HPP
 #define MPPI_GB_PLANT_HPP
@@ -44,6 +46,7 @@ public:
   using COST_PARAMS_T = typename CONTROLLER_T::TEMPLATED_COSTS::COST_PARAMS_T;
   using CONTROLLER_PARAMS_T = typename CONTROLLER_T::TEMPLATED_PARAMS;
   using SAMPLER_T = typename CONTROLLER_T::TEMPLATED_SAMPLING;
+  using FB_STATE_T = typename CONTROLLER_T::TEMPLATED_FEEDBACK_STATE;
 
   std::shared_ptr<CONTROLLER_T> controller_;
 
@@ -84,6 +87,12 @@ public:
   }
   void setDebugMode(bool mode) { debug_mode_ = mode; }
   void resetStateTime() { last_used_state_update_time_ = -1.0; }
+  FB_STATE_T getFeedbackState()
+  {
+    std::lock_guard<std::mutex> lck(access_guard_);
+    return feedback_state_;
+  }
+  double getAvgFeedbackTime() const { return avg_feedback_time_ms_; }
   double getAvgOptimizationTime() const { return avg_optimize_time_ms_; }
   double getAvgLoopTime() const { return avg_loop_time_ms_; }
   int getTargetOptimizationStride() const { return optimization_stride_; }
@@ -94,12 +103,14 @@ public:
   int getNumIterations() const { return num_iter_; }
 
   // BasePlant::setSolution (base_plant.hpp:274-287)
-  virtual void setSolution(const s_traj& state_seq, const c_traj& control_seq, double timestamp)
+  virtual void setSolution(const s_traj& state_seq, const c_traj& control_seq, const FB_STATE_T& fb_state,
+                           double timestamp)
   {
     std::lock_guard<std::mutex> guard(access_guard_);
     last_used_state_update_time_ = timestamp;
     state_traj_ = state_seq;
     control_traj_ = control_seq;
+    feedback_state_ = fb_state;
     ++num_iter_;
   }
 
@@ -121,9 +132,8 @@ public:
       const double since = time - t0;
       if (since > 0.0 && time >= t0 && time < t0 + dt * controller_->getNumTimesteps())
       {
-        const double steps = since / dt;
-        interpolate(control_traj_.data(), C, steps, u.data());
-        interpolate(state_traj_.data(), S, steps, nominal.data());
+        nominal = controller_->interpolateState(state_traj_, since);
+        u = controller_->getCurrentControl(state, since, nominal, control_traj_, feedback_state_);
         publish = true;
       }
     }
@@ -241,10 +251,20 @@ public:
     for (int i = 0; i < S * controller_->getNumTimesteps(); ++i)
       if (!std::isfinite(s[i])) throw std::runtime_error("state trajectory inside the plant has a NaN");
     optimization_duration_ = std::chrono::duration<double, std::milli>(clock::now() - opt_start).count();
-    setSolution(s, u, state_time);
+    const auto fb_start = clock::now();
+    FB_STATE_T fb_state{};
+    if (controller_->getFeedbackEnabled())
+    {
+      controller_->computeFeedback(state);
+      fb_state = controller_->getFeedbackState();
+    }
+    feedback_duration_ = std::chrono::duration<double, std::milli>(clock::now() - fb_start).count();
+    setSolution(s, u, fb_state, state_time);
     pubFreeEnergyStatistics(fe);
+    controller_->computeFeedbackPropagatedStateSeq();
     const double n = num_iter_;
     avg_optimize_time_ms_ += (optimization_duration_ - avg_optimize_time_ms_) / n;
+    avg_feedback_time_ms_ += (feedback_duration_ - avg_feedback_time_ms_) / n;
     optimize_loop_duration_ = std::chrono::duration<double, std::milli>(clock::now() - loop_start).count();
     avg_loop_time_ms_ += (optimize_loop_duration_ - avg_loop_time_ms_) / n;
     return true;
@@ -271,16 +291,6 @@ public:
   }
 
 protected:
-  // Column `steps` (fractional) of a trajectory stored [t][dim]: linear between steps, held at the ends.
-  void interpolate(const float* traj, int dim, double steps, float* out) const
-  {
-    const int T = controller_->getNumTimesteps();
-    const int i = std::min(std::max((int)std::floor(steps), 0), T - 1);
-    const int j = std::min(i + 1, T - 1);
-    const float a = (float)std::min(std::max(steps - i, 0.0), 1.0);
-    for (int d = 0; d < dim; ++d) out[d] = (1.0f - a) * traj[(size_t)i * dim + d] + a * traj[(size_t)j * dim + d];
-  }
-
   std::mutex access_guard_, params_guard_;
   int hz_ = 10;
   int optimization_stride_ = 1;
@@ -289,6 +299,7 @@ protected:
   s_array state_{};
   s_traj state_traj_{};
   c_traj control_traj_{};
+  FB_STATE_T feedback_state_{};
   std::atomic<double> state_time_{ 0.0 };
   std::atomic<double> last_used_state_update_time_{ 0.0 };
   std::atomic<bool> has_received_state_{ false };
@@ -300,8 +311,8 @@ protected:
   SAMPLER_T sampler_{};
   std::atomic<int> num_iter_{ 0 };
   int status_ = 1;
-  double optimization_duration_ = 0.0, optimize_loop_duration_ = 0.0, sleep_duration_ = 0.0;
-  double avg_optimize_time_ms_ = 0.0, avg_loop_time_ms_ = 0.0, avg_sleep_time_ms_ = 0.0;
+  double optimization_duration_ = 0.0, optimize_loop_duration_ = 0.0, sleep_duration_ = 0.0, feedback_duration_ = 0.0;
+  double avg_optimize_time_ms_ = 0.0, avg_loop_time_ms_ = 0.0, avg_sleep_time_ms_ = 0.0, avg_feedback_time_ms_ = 0.0;
 };
 }  // namespace mppi_gb
 

@@ -39,7 +39,14 @@
  *    trajectory applies it with the state to the smoothed sequence (controller.cuh:676-680), and the final pass after
  *    smoothing applies it with a zero state to every control (mppi_controller.cu:222-226);
  *  - crash is one int per sample, zero at the start of every rollout, passed to each running cost call, and reported
- *    per step by mppi_get_sampled_trajectories (the reference's crash_status_d, mppi_common.cu:371-376).
+ *    per step by mppi_get_sampled_trajectories (the reference's crash_status_d, mppi_common.cu:371-376);
+ *  - computeGrad (Dynamics::computeGrad, dynamics.cuh:236-242) is optional and host-only: a dynamics class that
+ *    defines
+ *        bool computeGrad(const float* state, const float* control, float* A, float* B) const
+ *    with A = d xdot / d state (row-major STATE_DIM x STATE_DIM) and B = d xdot / d control (row-major STATE_DIM x
+ *    CONTROL_DIM), both zero on entry, gives the DDP feedback controller (mppi_compute_feedback) its Jacobians;
+ *    without it, or when it returns false, the controller takes forward differences of the step's derivative, as
+ *    the reference's ModelWrapperDDP does (ddp_model_wrapper.h:81-94).
  * The plugin rollout is a sampler kernel followed by one rollout kernel (one thread per sample, the tile's controls
  * staged in shared memory, the tile's weighted partial sums at the end), then the per-instance combine.
  */

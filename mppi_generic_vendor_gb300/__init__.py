@@ -7,7 +7,7 @@ from . import _abi
 from ._abi import MPPIError
 from . import nn_io
 from .controller import (BatchedMPPIController, BicycleDynamics, ColoredMPPIController, TubeMPPIController, BicycleSlipDynamics, BicycleSlipMLPDynamics,
-                         CartpoleDynamics,
+                         CartpoleDynamics, DDPFeedback, DDPFeedbackState, DDPParams,
                          CartpoleSwingupCost, ColoredNoiseDistribution, CostmapCost, DoubleIntegratorDynamics,
                          DoubleIntegratorObstacleCost, GaussianDistribution, VanillaMPPIController,
                          select_top_samples)
@@ -15,4 +15,5 @@ from .controller import (BatchedMPPIController, BicycleDynamics, ColoredMPPICont
 __all__ = ["MPPIError", "BatchedMPPIController", "VanillaMPPIController", "ColoredMPPIController", "TubeMPPIController", "CartpoleDynamics", "CartpoleSwingupCost",
            "DoubleIntegratorDynamics", "DoubleIntegratorObstacleCost", "BicycleDynamics", "BicycleSlipDynamics",
            "BicycleSlipMLPDynamics",
-           "CostmapCost", "GaussianDistribution", "ColoredNoiseDistribution", "select_top_samples", "_abi", "nn_io"]
+           "CostmapCost", "GaussianDistribution", "ColoredNoiseDistribution", "select_top_samples", "_abi", "nn_io",
+           "DDPFeedback", "DDPFeedbackState", "DDPParams"]

@@ -123,6 +123,15 @@ SIGNATURES = [
     ("mppi_get_sampled_trajectories", C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_int, _FP, _FP, _FP, _IP]),
     ("mppi_get_model_dims", C.c_int, [_P, _IP, _IP, _IP, _IP]),
     ("mppi_get_nominal_state_used", C.c_int, [_P, _IP]),
+    ("mppi_set_feedback_params", C.c_int, [_P, _FP, _FP, _FP, C.c_int]),
+    ("mppi_enable_feedback", C.c_int, [_P, C.c_int]),
+    ("mppi_get_feedback_enabled", C.c_int, [_P, _IP]),
+    ("mppi_compute_feedback", C.c_int, [_P, _FP]),
+    ("mppi_get_feedback_gains", C.c_int, [_P, _FP]),
+    ("mppi_get_feedback_control", C.c_int, [_P, _FP, _FP, C.c_int, _FP]),
+    ("mppi_get_feedback_propagated_state_seq", C.c_int, [_P, _FP]),
+    ("mppi_ddp_feedback_gains", C.c_int, [C.c_int, _P, C.c_size_t, C.c_int, C.c_float, _FP, _FP, _FP, _FP, _FP, _FP,
+                                          C.c_int, _FP, _FP, _FP]),
     ("mppi_set_wait_diagnostics", C.c_int, [_P, C.c_uint32, C.c_int]),
     ("mppi_handle_adopt", C.c_int, [_P, C.c_int, C.POINTER(_P)]),
     ("mppi_select_top_samples", C.c_int, [_FP, C.c_int, C.c_int, C.POINTER(C.c_int)]),

@@ -229,6 +229,63 @@ class ColoredNoiseDistribution(GaussianDistribution):
 
 
 # ------------------------------------------------------------------------------------------------ controllers
+# ------------------------------------------------------------------------------------------- feedback controller
+@dataclass
+class DDPParams:
+    """DDPParams (feedback_controllers/DDP/ddp.cuh:16-25): tracking weights Q, Q_f (S x S) and R (C x C) and the
+    number of DDP iterations; None means the identity."""
+    Q: np.ndarray | None = None
+    Q_f: np.ndarray | None = None
+    R: np.ndarray | None = None
+    num_iterations: int = 1
+
+
+@dataclass
+class DDPFeedbackState:
+    """DDPFeedbackState (ddp.cuh:28-37): the gain trajectory, per step a C x S matrix stored column-major."""
+    fb_gain_traj_: np.ndarray
+    state_dim: int
+    control_dim: int
+
+    def gain(self, t: int) -> np.ndarray:
+        """K_t as a (C, S) array."""
+        n = self.state_dim * self.control_dim
+        return self.fb_gain_traj_[t * n:(t + 1) * n].reshape(self.state_dim, self.control_dim).T
+
+
+class DDPFeedback:
+    """DDPFeedback(model, dt, num_timesteps) (feedback_controllers/DDP/ddp.cuh:104-160): the ancillary controller a
+    VanillaMPPIController / TubeMPPIController is built with.  It holds the DDPParams; the controller's handle runs the
+    solver (mppi_compute_feedback) on the host after a solve."""
+
+    def __init__(self, model, dt, num_timesteps=None):
+        self.model_ = model
+        self.dt_ = float(dt)
+        self.num_timesteps_ = num_timesteps
+        S, Cd = model.STATE_DIM, model.CONTROL_DIM
+        self.params_ = DDPParams(np.eye(S, dtype=np.float32), np.eye(S, dtype=np.float32),
+                                 np.eye(Cd, dtype=np.float32), 1)
+        self._controllers = []
+
+    def getParams(self) -> DDPParams:
+        return DDPParams(*(None if m is None else np.array(m, np.float32) for m in
+                           (self.params_.Q, self.params_.Q_f, self.params_.R)), self.params_.num_iterations)
+
+    def setParams(self, params: DDPParams):
+        """FeedbackController::setParams (ddp.cu:81-87); handed on to every controller built with this object."""
+        self.params_ = params
+        for c in self._controllers:
+            c.setFeedbackParams(params)
+
+
+def _col_major(m, n):
+    """A float32 n x n matrix in column-major order (the reference's Eigen storage), or None for the identity."""
+    if m is None:
+        return None
+    a = np.asarray(m, dtype=np.float32).reshape(n, n)
+    return np.ascontiguousarray(a.T.reshape(-1))
+
+
 class BatchedMPPIController:
     """Many independent VanillaMPPIControllers of one plugin pair, solved by one set of GPU launches.
 
@@ -552,6 +609,124 @@ class BatchedMPPIController:
     def stream(self) -> int:
         return A.lib().mppi_get_stream(self._h) or 0
 
+    # ---- ancillary feedback controller (Controller's feedback methods, controller.cuh:265-269,354-414,455-571,730-743)
+    def _attach_feedback(self, fb_controller):
+        self.fb_controller_ = fb_controller
+        self._fb_prop = None
+        if fb_controller is not None:
+            fb_controller._controllers.append(self)
+            self.setFeedbackParams(fb_controller.params_)
+
+    def setFeedbackParams(self, params: DDPParams):
+        """Controller::setFeedbackParams (controller.cuh:735-738)."""
+        S, Cd = self.S, self.Cdim
+        q, qf, r = _col_major(params.Q, S), _col_major(params.Q_f, S), _col_major(params.R, Cd)
+        A.call("mppi_set_feedback_params", self._h, None if q is None else _fptr(q),
+               None if qf is None else _fptr(qf), None if r is None else _fptr(r), int(params.num_iterations))
+        self._fb_params = params
+
+    def getFeedbackParams(self) -> DDPParams:
+        return getattr(self, "_fb_params", DDPParams())
+
+    def initFeedback(self):
+        """Controller::initFeedback: feedback on, gains reset to zero."""
+        A.call("mppi_enable_feedback", self._h, 1)
+        self._fb_enabled = True
+
+    def disableFeedbackController(self):
+        A.call("mppi_enable_feedback", self._h, 0)
+        self._fb_enabled = False
+
+    def getFeedbackEnabled(self) -> bool:
+        """Kept on this object as well, so that getCurrentControl (a plant's state-estimator thread) does not enter
+        the handle while another thread optimises."""
+        return getattr(self, "_fb_enabled", False)
+
+    def computeFeedback(self, state):
+        """Controller::computeFeedback(state): DDP from `state` around the nominal trajectory of the last solve."""
+        x = np.ascontiguousarray(np.asarray(state, dtype=np.float32).reshape(-1))
+        if x.size != self.S:
+            raise ValueError(f"state must hold {self.S} floats")
+        A.call("mppi_compute_feedback", self._h, _fptr(x))
+
+    def _fb_T(self) -> int:
+        return int(self.T[1] if self.params_.controller == A.CONTROLLER_TUBE else self.T[0])
+
+    def getFeedbackState(self) -> DDPFeedbackState:
+        """Controller::getFeedbackState: a copy of the current gain trajectory."""
+        g = np.empty(self._fb_T() * self.Cdim * self.S, dtype=np.float32)
+        A.call("mppi_get_feedback_gains", self._h, _fptr(g))
+        return DDPFeedbackState(g, self.S, self.Cdim)
+
+    def getFeedbackControl(self, state, goal_state, t):
+        """Controller::getFeedbackControl: K_t (state - goal_state)."""
+        x = np.ascontiguousarray(np.asarray(state, dtype=np.float32).reshape(-1))
+        g = np.ascontiguousarray(np.asarray(goal_state, dtype=np.float32).reshape(-1))
+        if x.size != self.S or g.size != self.S:
+            raise ValueError(f"state and goal_state must hold {self.S} floats")
+        out = np.empty(self.Cdim, dtype=np.float32)
+        A.call("mppi_get_feedback_control", self._h, _fptr(x), _fptr(g), int(t), _fptr(out))
+        return out
+
+    def computeFeedbackPropagatedStateSeq(self):
+        """Controller::computeFeedbackPropagatedStateSeq: the state trajectory under nominal control plus feedback."""
+        out = np.empty(self._fb_T() * self.S, dtype=np.float32)
+        A.call("mppi_get_feedback_propagated_state_seq", self._h, _fptr(out))
+        self._fb_prop = out.reshape(-1, self.S).T.copy()
+
+    def getFeedbackPropagatedStateSeq(self) -> np.ndarray:
+        if getattr(self, "_fb_prop", None) is None:
+            return np.zeros((self.S, self._fb_T()), np.float32)
+        return self._fb_prop
+
+    def _rel_index(self, rel_time, T):
+        dt = self.getDt()
+        lower = int(rel_time / dt)
+        alpha = (rel_time - lower * dt) / dt
+        # the reference reads column lower + 1 unchecked; both indices are held inside the horizon here
+        return min(max(lower, 0), T - 1), min(max(lower + 1, 0), T - 1), alpha
+
+    def interpolateControls(self, rel_time, c_traj):
+        """Controller::interpolateControls (controller.cuh:384-394): linear between the bracketing steps."""
+        c = np.asarray(c_traj, dtype=np.float32)
+        lo, hi, a = self._rel_index(rel_time, c.shape[1])
+        return ((1.0 - a) * c[:, lo] + a * c[:, hi]).astype(np.float32)
+
+    def interpolateState(self, s_traj, rel_time):
+        """Controller::interpolateState (controller.cuh:396-403) with Dynamics::interpolateState (linear)."""
+        s = np.asarray(s_traj, dtype=np.float32)
+        lo, hi, a = self._rel_index(rel_time, s.shape[1])
+        return ((1.0 - a) * s[:, lo] + a * s[:, hi]).astype(np.float32)
+
+    def interpolateFeedback(self, state, target_nominal_state, rel_time, fb_state: DDPFeedbackState):
+        """FeedbackController::interpolateFeedback_ (feedback.cuh:216-228): the gains of the bracketing steps,
+        blended linearly, applied to state - target_nominal_state."""
+        e = np.asarray(state, np.float32).reshape(-1) - np.asarray(target_nominal_state, np.float32).reshape(-1)
+        T = fb_state.fb_gain_traj_.size // (self.S * self.Cdim)
+        lo, hi, a = self._rel_index(rel_time, T)
+        return ((1.0 - a) * (fb_state.gain(lo) @ e) + a * (fb_state.gain(hi) @ e)).astype(np.float32)
+
+    def enforceConstraints(self, u):
+        """Dynamics::enforceConstraints (dynamics.cu:107-126) with the handle's constraints: deadband, then clamp."""
+        cc = self.constraints_
+        out = np.array(u, dtype=np.float32).reshape(-1)
+        for i in range(out.size):
+            db = np.float32(cc.deadband[i])
+            if abs(out[i]) < db:
+                out[i] = np.float32(cc.zero_control[i])
+            else:
+                out[i] = out[i] + db * -np.sign(out[i])
+            out[i] = min(max(np.float32(cc.lower[i]), out[i]), np.float32(cc.upper[i]))
+        return out
+
+    def getCurrentControl(self, state, rel_time, target_nominal_state, c_traj, fb_state=None):
+        """Controller::getCurrentControl (controller.cuh:347-362): the nominal control at rel_time plus, with feedback
+        on, the interpolated feedback against target_nominal_state, then the constraints with a zero state."""
+        u = self.interpolateControls(rel_time, c_traj)
+        if fb_state is not None and self.getFeedbackEnabled():
+            u = u + self.interpolateFeedback(state, target_nominal_state, rel_time, fb_state)
+        return self.enforceConstraints(u)
+
 
 class VanillaMPPIController(BatchedMPPIController):
     """VanillaMPPIController(model, cost, fb_controller, sampler, dt, max_iter, lambda, alpha, num_timesteps,
@@ -559,13 +734,14 @@ class VanillaMPPIController(BatchedMPPIController):
 
     def __init__(self, model, cost, fb_controller, sampler, dt, max_iter, lambda_, alpha, num_timesteps,
                  num_rollouts, init_control_traj=None, stream=0, seed=0, slide_control_scale=None):
-        del fb_controller  # feedback controllers are not part of the plain MPPI path
         init = None
         if init_control_traj is not None:
             init = np.asarray(init_control_traj, dtype=np.float32).reshape(model.CONTROL_DIM, num_timesteps).T
         super().__init__(model, cost, sampler, [num_rollouts], [num_timesteps], dt=dt, max_iter=max_iter,
                          lambda_=lambda_, alpha=alpha, seed=seed, init_control_traj=init, stream=stream,
                          slide_control_scale=slide_control_scale)
+        # the feedback controller's parameters go to the handle; feedback stays off until initFeedback()
+        self._attach_feedback(fb_controller)
 
     def getControlSeq(self) -> np.ndarray:
         return self.getControlSeqs()[0]
@@ -653,12 +829,12 @@ class TubeMPPIController(BatchedMPPIController):
     num_rollouts, ...) (controllers/Tube-MPPI/tube_mppi_controller.cuh:29-141): two sampling distributions of
     num_rollouts samples each, the actual system (instance 0, rolled out from the state given to computeControl) and
     the nominal system (instance 1, from the nominal state the controller keeps); the nominal pair takes over the
-    actual pair's sequences when the actual baseline beats the nominal one by nominal_threshold.  The ancillary
-    feedback controller (fb_controller) is not part of this engine."""
+    actual pair's sequences when the actual baseline beats the nominal one by nominal_threshold.  getControlSeq and
+    getTargetStateSeq are the nominal system's, as in the reference; the ancillary feedback controller (a
+    DDPFeedback, or identity weights when fb_controller is None) tracks it and is on from construction."""
 
     def __init__(self, model, cost, fb_controller, sampler, dt, max_iter, lambda_, alpha, num_timesteps,
                  num_rollouts, init_control_traj=None, stream=0, seed=0, nominal_threshold=20.0):
-        del fb_controller
         init = None
         if init_control_traj is not None:
             one = np.asarray(init_control_traj, dtype=np.float32).reshape(model.CONTROL_DIM, num_timesteps).T
@@ -669,6 +845,9 @@ class TubeMPPIController(BatchedMPPIController):
         cp.controller = A.CONTROLLER_TUBE
         cp.nominal_threshold = float(nominal_threshold)
         self.setParams(cp)
+        # Tube-MPPI runs its ancillary controller from the start (tube_mppi_controller.cu:27-29)
+        self._attach_feedback(fb_controller)
+        self.initFeedback()
 
     def computeControl(self, state, optimization_stride=1):
         """TubeMPPIController::computeControl (tube_mppi_controller.cu:158-296); state: the actual system's."""
@@ -678,20 +857,30 @@ class TubeMPPIController(BatchedMPPIController):
         A.call("mppi_compute_control", self._h, _fptr(x), int(optimization_stride))
 
     def getControlSeq(self) -> np.ndarray:
-        return self.getControlSeqs()[0]
+        """The nominal control sequence (TubeMPPIController::getControlSeq, tube_mppi_controller.cuh:61-64)."""
+        return self.getControlSeqs()[1]
 
     def getNominalControlSeq(self) -> np.ndarray:
         return self.getControlSeqs()[1]
+
+    def getActualControlSeq(self) -> np.ndarray:
+        """The actual system's control sequence (TubeMPPIController::getActualControlSeq, :77-80)."""
+        return self.getControlSeqs()[0]
 
     def setControlSeq(self, seq):
         s = np.asarray(seq, np.float32)
         self.setControlSeqs([s, s])
 
     def getTargetStateSeq(self) -> np.ndarray:
-        return self.getTargetStateSeqs()[0]
+        """The nominal state trajectory (TubeMPPIController::getTargetStateSeq, tube_mppi_controller.cuh:69-72)."""
+        return self.getTargetStateSeqs()[1]
 
     def getNominalStateSeq(self) -> np.ndarray:
         return self.getTargetStateSeqs()[1]
+
+    def getActualStateSeq(self) -> np.ndarray:
+        """The actual system's state trajectory (Controller::getActualStateSeq, controller.cuh:538-541)."""
+        return self.getTargetStateSeqs()[0]
 
     def getNominalThreshold(self) -> float:
         return float(self.params_.nominal_threshold)

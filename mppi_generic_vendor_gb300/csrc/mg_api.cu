@@ -338,6 +338,100 @@ mppi_status mppi_get_nominal_state_used(mppi_handle* h, int* used)
   return h->engine->nominal_state_used(used);
 }
 
+mppi_status mppi_set_feedback_params(mppi_handle* h, const float* Q, const float* Q_f, const float* R,
+                                     int num_iterations)
+{
+  HANDLE_OK(h);
+  return h->engine->set_feedback_params(Q, Q_f, R, num_iterations);
+}
+mppi_status mppi_enable_feedback(mppi_handle* h, int enable)
+{
+  HANDLE_OK(h);
+  return h->engine->enable_feedback(enable);
+}
+mppi_status mppi_get_feedback_enabled(const mppi_handle* h, int* enabled)
+{
+  HANDLE_OK(h);
+  MG_CHECK(enabled, "enabled must not be NULL");
+  *enabled = h->engine->feedback_enabled();
+  return MPPI_OK;
+}
+mppi_status mppi_compute_feedback(mppi_handle* h, const float* state)
+{
+  HANDLE_OK(h);
+  return h->engine->compute_feedback(state);
+}
+mppi_status mppi_get_feedback_gains(const mppi_handle* h, float* out)
+{
+  HANDLE_OK(h);
+  return h->engine->get_feedback_gains(out);
+}
+mppi_status mppi_get_feedback_control(const mppi_handle* h, const float* state, const float* goal_state, int t,
+                                      float* out)
+{
+  HANDLE_OK(h);
+  return h->engine->feedback_control(state, goal_state, t, out);
+}
+mppi_status mppi_get_feedback_propagated_state_seq(mppi_handle* h, float* out)
+{
+  HANDLE_OK(h);
+  MG_CHECK(out, "out must not be NULL");
+  return h->engine->feedback_propagated_state_seq(out);
+}
+
+mppi_status mppi_ddp_feedback_gains(int model, const void* dyn_params, size_t dyn_bytes, int num_timesteps, float dt,
+                                    const float* x0, const float* target_states, const float* nominal_controls,
+                                    const float* Q, const float* Q_f, const float* R, int num_iterations,
+                                    const float* control_min, const float* control_max, float* gains_out)
+{
+  MG_CHECK(dyn_params && x0 && target_states && nominal_controls && control_min && control_max && gains_out,
+           "pointer arguments other than the weights must not be NULL");
+  MG_CHECK(num_timesteps >= 2, "num_timesteps must be >= 2 (got %d)", num_timesteps);
+  MG_CHECK(num_iterations >= 1, "num_iterations must be >= 1 (got %d)", num_iterations);
+  MG_CHECK(std::isfinite(dt) && dt > 0.0f, "dt must be positive");
+  auto run = [&](auto model_tag) -> mppi_status {
+    using Model = decltype(model_tag);
+    constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM;
+    using P = typename Model::DynParams;
+    MG_CHECK(dyn_bytes == sizeof(P), "dyn_bytes must be %zu for this model (got %zu)", sizeof(P), dyn_bytes);
+    P p;
+    memcpy(&p, dyn_params, sizeof(P));
+    DdpWeights w;
+    w.Q.assign((size_t)S * S, 0.0);
+    w.Qf.assign((size_t)S * S, 0.0);
+    w.R.assign((size_t)C * C, 0.0);
+    for (int e = 0; e < S; ++e) w.Q[(size_t)e * S + e] = w.Qf[(size_t)e * S + e] = 1.0;
+    for (int e = 0; e < C; ++e) w.R[(size_t)e * C + e] = 1.0;
+    if (Q)
+      for (int e = 0; e < S * S; ++e) w.Q[e] = Q[e];
+    if (Q_f)
+      for (int e = 0; e < S * S; ++e) w.Qf[e] = Q_f[e];
+    if (R)
+      for (int e = 0; e < C * C; ++e) w.R[e] = R[e];
+    w.iterations = num_iterations;
+    auto f = [&](const float* x, const float* u, float* xd) { Model::computeDynamics(p, x, u, xd); };
+    auto df = [&](const float* x, const float* u, double* A, double* B) {
+      if constexpr (HasAnalyticGrad<Model>::value)
+      {
+        if (Model::computeGrad(p, x, u, A, B)) return;
+      }
+      numeric_jacobian<S, C>(f, x, u, A, B);
+    };
+    const bool ok = ddp_tracking_gains<S, C>(f, df, x0, target_states, nominal_controls, num_timesteps, dt, w,
+                                             control_min, control_max, gains_out);
+    MG_CHECK(ok, "DDP feedback: a control Hessian is not positive definite (check R)");
+    return MPPI_OK;
+  };
+  switch (model)
+  {
+    case MPPI_MODEL_CARTPOLE: return run(CartpoleModel{});
+    case MPPI_MODEL_DOUBLE_INTEGRATOR: return run(DoubleIntegratorModel{});
+    case MPPI_MODEL_BICYCLE_COSTMAP: return run(BicycleCostmapModel{});
+    case MPPI_MODEL_BICYCLE_SLIP: return run(BicycleSlipModel{});
+    default: set_error("mppi_ddp_feedback_gains: model %d has no host dynamics here", model); return MPPI_EUNSUPPORTED;
+  }
+}
+
 mppi_status mppi_destroy(mppi_handle* h)
 {
   if (!h) return MPPI_OK;

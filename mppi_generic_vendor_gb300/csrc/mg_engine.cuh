@@ -23,6 +23,7 @@
 #include "mg_kernels.cuh"
 #include "mg_mlp.cuh"
 #include "mg_plugin.cuh"
+#include "mg_ddp.h"
 
 namespace mg
 {
@@ -91,6 +92,14 @@ public:
   virtual mppi_status use_analytic(int enable) = 0;
   virtual mppi_status nominal_state_used(int* used) = 0;
   virtual mppi_status set_wait_diagnostics(uint32_t max_polls, int withhold_progress) = 0;
+  // ancillary feedback controller (DDPFeedback, feedback_controllers/DDP/ddp.cu)
+  virtual mppi_status set_feedback_params(const float* Q, const float* Qf, const float* R, int iterations) = 0;
+  virtual mppi_status enable_feedback(int enable) = 0;
+  virtual int feedback_enabled() const = 0;
+  virtual mppi_status compute_feedback(const float* x0) = 0;
+  virtual mppi_status get_feedback_gains(float* out) const = 0;
+  virtual mppi_status feedback_control(const float* x, const float* goal, int t, float* u) const = 0;
+  virtual mppi_status feedback_propagated_state_seq(float* out) = 0;
 };
 
 // Factories, one per model translation unit.
@@ -759,6 +768,162 @@ public:
     return MPPI_OK;
   }
 
+  // ------------------------------------------------------------------------------------------ DDP feedback
+  // The instance whose nominal trajectory the feedback tracks: Tube-MPPI's nominal system (its getControlSeq and
+  // getTargetStateSeq, tube_mppi_controller.cuh:61-72), else the handle's single controller.
+  int fb_instance() const { return tube() ? 1 : 0; }
+  size_t state_off(int i) const
+  {
+    size_t off = 0;
+    for (int j = 0; j < i; ++j) off += (size_t)T_[j] * S;
+    return off;
+  }
+
+  // xdot of instance i's model on the host, the function the solver linearises (ModelWrapperDDP::f,
+  // ddp_model_wrapper.h:66-79: the derivative the model's step computes)
+  void host_xdot(int i, const float* x, const float* u, float* xd) const
+  {
+    if constexpr (Model::kPlugin)
+    {
+      float xn[S], y[Model::OUTPUT_DIM];
+      dyn_[i].step(x, xn, xd, u, y, 0, cp_.dt);
+    }
+    else if constexpr (Model::kMlp)
+    {
+      if (!use_analytic_)
+        mlp_host_dynamics(mlp_host_.data(), x, u, xd);
+      else
+        Model::computeDynamics(dyn_[i], x, u, xd);
+    }
+    else
+    {
+      Model::computeDynamics(dyn_[i], x, u, xd);
+    }
+  }
+
+  // d xdot / dx and d xdot / du (row-major, zeroed by the caller): the model's analytic computeGrad where it has one,
+  // else forward differences (ModelWrapperDDP::df, ddp_model_wrapper.h:81-94)
+  void host_jacobian(int i, const float* x, const float* u, double* A, double* B) const
+  {
+    if constexpr (Model::kPlugin)
+    {
+      if constexpr (DefinesComputeGrad<typename Model::DynParams>::value)
+      {
+        float Af[S * S] = {}, Bf[S * C] = {};
+        if (dyn_[i].computeGrad(x, u, Af, Bf))
+        {
+          for (int e = 0; e < S * S; ++e) A[e] = Af[e];
+          for (int e = 0; e < S * C; ++e) B[e] = Bf[e];
+          return;
+        }
+      }
+    }
+    else if constexpr (HasAnalyticGrad<Model>::value)
+    {
+      if (!(Model::kMlp && !use_analytic_) && Model::computeGrad(dyn_[i], x, u, A, B)) return;
+    }
+    numeric_jacobian<S, C>([&](const float* xx, const float* uu, float* xd) { host_xdot(i, xx, uu, xd); }, x, u, A,
+                           B);
+  }
+
+  mppi_status feedback_shape_ok() const
+  {
+    MG_CHECK(I_ == 1 || tube(), "the feedback controller serves a single controller (or Tube-MPPI's nominal system)");
+    return MPPI_OK;
+  }
+
+  // FeedbackController::setParams with DDPParams (ddp.cu:81-87): NULL keeps a matrix
+  mppi_status set_feedback_params(const float* Q, const float* Qf, const float* R, int iterations) override
+  {
+    MG_CHECK(iterations >= 1, "num_iterations must be >= 1 (got %d)", iterations);
+    auto load = [](std::vector<double>& dst, const float* src, int n) {
+      if (!src) return true;
+      for (int e = 0; e < n; ++e)
+        if (!std::isfinite(src[e])) return false;
+      for (int e = 0; e < n; ++e) dst[e] = src[e];
+      return true;
+    };
+    std::vector<double> q = fb_w_.Q, qf = fb_w_.Qf, r = fb_w_.R;
+    MG_CHECK(load(q, Q, S * S) && load(qf, Qf, S * S) && load(r, R, C * C), "feedback weights must be finite");
+    fb_w_.Q.swap(q);
+    fb_w_.Qf.swap(qf);
+    fb_w_.R.swap(r);
+    fb_w_.iterations = iterations;
+    return MPPI_OK;
+  }
+
+  // Controller::initFeedback (controller.cuh:265-269: on, gains reset to zero by initTrackingController) and
+  // disableFeedbackController (:730-733)
+  mppi_status enable_feedback(int enable) override
+  {
+    MG_TRY(feedback_shape_ok());
+    fb_enabled_ = enable != 0;
+    if (fb_enabled_) std::fill(fb_gains_.begin(), fb_gains_.end(), 0.0f);
+    return MPPI_OK;
+  }
+  int feedback_enabled() const override { return fb_enabled_ ? 1 : 0; }
+
+  // Controller::computeFeedback(state) (controller.cuh:551-565): DDP from x0 around getTargetStateSeq() and
+  // getControlSeq(); nothing while feedback is off
+  mppi_status compute_feedback(const float* x0) override
+  {
+    MG_CHECK(x0, "state must not be NULL");
+    MG_TRY(feedback_shape_ok());
+    if (!fb_enabled_) return MPPI_OK;
+    const int i = fb_instance();
+    MG_CHECK(T_[i] >= 2, "the feedback controller needs at least two time steps");
+    if (traj_dirty_) compute_state_seq();
+    auto f = [&](const float* x, const float* u, float* xd) { host_xdot(i, x, u, xd); };
+    auto df = [&](const float* x, const float* u, double* A, double* B) { host_jacobian(i, x, u, A, B); };
+    const bool ok = ddp_tracking_gains<S, C>(f, df, x0, state_seq_.data() + state_off(i), control_.data() + t_off_[i],
+                                             T_[i], cp_.dt, fb_w_, cc_.lower, cc_.upper, fb_gains_.data());
+    MG_CHECK(ok, "DDP feedback: a control Hessian is not positive definite (check R)");
+    return MPPI_OK;
+  }
+
+  mppi_status get_feedback_gains(float* out) const override
+  {
+    MG_CHECK(out, "out must not be NULL");
+    memcpy(out, fb_gains_.data(), sizeof(float) * fb_gains_.size());
+    return MPPI_OK;
+  }
+
+  // Controller::getFeedbackControl (controller.cuh:567-571): K_t (x - goal)
+  mppi_status feedback_control(const float* x, const float* goal, int t, float* u) const override
+  {
+    MG_CHECK(x && goal && u, "state, goal_state and out must not be NULL");
+    const int T = T_[fb_instance()];
+    MG_CHECK(t >= 0 && t < T, "t must be in [0, %d) (got %d)", T, t);
+    ddp_feedback_control<S, C>(fb_gains_.data(), t, x, goal, u);
+    return MPPI_OK;
+  }
+
+  // Controller::computeFeedbackPropagatedStateSeq (controller.cuh:495-517): from the state the last solve started
+  // at, each step's control is the nominal control plus the feedback against that step's target state, stepped by
+  // the model without constraints; with feedback off the previous result stays
+  mppi_status feedback_propagated_state_seq(float* out) override
+  {
+    MG_TRY(feedback_shape_ok());
+    if (fb_enabled_)
+    {
+      if (traj_dirty_) compute_state_seq();
+      const int i = fb_instance(), T = T_[i];
+      const float* xt = state_seq_.data() + state_off(i);
+      const float* un = control_.data() + t_off_[i];
+      float x[S], xn[S], u[C], ufb[C];
+      for (int s = 0; s < S; ++s) x[s] = fb_prop_[s] = state_seq_[s];  // actual state sequence, column 0
+      for (int t = 0; t < T - 1; ++t)
+      {
+        ddp_feedback_control<S, C>(fb_gains_.data(), t, x, xt + (size_t)t * S, ufb);
+        for (int c = 0; c < C; ++c) u[c] = un[(size_t)t * C + c] + ufb[c];
+        model_step(i, x, u, xn, t);
+        for (int s = 0; s < S; ++s) x[s] = fb_prop_[(size_t)(t + 1) * S + s] = xn[s];
+      }
+    }
+    if (out) memcpy(out, fb_prop_.data(), sizeof(float) * fb_prop_.size());
+    return MPPI_OK;
+  }
+
   // ------------------------------------------------------------------------------------------------ Tube-MPPI
   bool tube() const { return cp_.controller == MPPI_CONTROLLER_TUBE; }
 
@@ -1085,6 +1250,13 @@ private:
     stats_.assign((size_t)3 * I_, 0.0);
     prev_baseline_.assign(I_, 0.0f);
     memset(&aux_, 0, sizeof(aux_));
+    fb_w_.Q.assign((size_t)S * S, 0.0);
+    fb_w_.Qf.assign((size_t)S * S, 0.0);
+    fb_w_.R.assign((size_t)C * C, 0.0);
+    for (int e = 0; e < S; ++e) fb_w_.Q[(size_t)e * S + e] = fb_w_.Qf[(size_t)e * S + e] = 1.0;
+    for (int e = 0; e < C; ++e) fb_w_.R[(size_t)e * C + e] = 1.0;
+    fb_gains_.assign((size_t)T_[fb_instance()] * C * S, 0.0f);
+    fb_prop_.assign((size_t)T_[fb_instance()] * S, 0.0f);
 
     if (a.stream)
     {
@@ -2019,6 +2191,9 @@ private:
   bool withhold_progress_ = false;          // mode 4's noise warps publish no progress (mppi_set_wait_diagnostics)
   bool traj_dirty_ = false;
   std::vector<double> stats_;
+  bool fb_enabled_ = false;                // Controller::enable_feedback_
+  DdpWeights fb_w_;                        // DDPParams: identities and one iteration until set
+  std::vector<float> fb_gains_, fb_prop_;  // gains of the feedback instance; feedback-propagated states
 
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;

@@ -132,6 +132,28 @@ struct CartpoleModel
     xd[2] = td;
     xd[3] = acc.y;
   }
+  // Host Jacobians of xdot (CartpoleDynamics::computeGrad, cartpole_dynamics.cu:10-45): A = d xdot / dx (row-major
+  // 4 x 4), B = d xdot / du (4 x 1), differentiated from the two accelerations above in double.
+  static bool computeGrad(const DynParams& p, const float* x, const float* u, double* A, double* B)
+  {
+    const double th = x[2], td = x[3], f = u[0];
+    const double mc = p.cart_mass, mp = p.pole_mass, lp = p.pole_length, g = p.gravity;
+    const double s = std::sin(th), c = std::cos(th);
+    const double den = mc + mp * s * s, dden = 2.0 * mp * s * c;  // d den / d theta
+    const double n1 = f + mp * s * (lp * td * td + g * c);
+    const double n3 = -f * c - mp * lp * td * td * c * s - (mc + mp) * g * s;
+    const double dn1 = mp * c * (lp * td * td + g * c) - mp * g * s * s;
+    const double dn3 = f * s - mp * lp * td * td * (c * c - s * s) - (mc + mp) * g * c;
+    A[0 * 4 + 1] = 1.0;
+    A[1 * 4 + 2] = dn1 / den - n1 * dden / (den * den);
+    A[1 * 4 + 3] = 2.0 * mp * lp * td * s / den;
+    A[2 * 4 + 3] = 1.0;
+    A[3 * 4 + 2] = dn3 / (lp * den) - n3 * dden / (lp * den * den);
+    A[3 * 4 + 3] = -2.0 * mp * td * c * s / den;
+    B[1] = 1.0 / den;
+    B[3] = -c / (lp * den);
+    return true;
+  }
   template <class Ar = ExactArith>
   static MG_HD float computeStateCost(const CostParams& q, const ModelAux&, const float* y, int, Ar&& ar = Ar{})
   {
@@ -177,6 +199,16 @@ struct DoubleIntegratorModel
     xd[1] = x[3];
     xd[2] = u[0];
     xd[3] = u[1];
+  }
+  // Host Jacobians (DoubleIntegratorDynamics::computeGrad, di_dynamics.cu:24-34): A = d xdot / dx (row-major 4 x 4),
+  // B = d xdot / du (4 x 2).
+  static bool computeGrad(const DynParams&, const float*, const float*, double* A, double* B)
+  {
+    A[0 * 4 + 2] = 1.0;
+    A[1 * 4 + 3] = 1.0;
+    B[2 * 2 + 0] = 1.0;
+    B[3 * 2 + 1] = 1.0;
+    return true;
   }
   // coeff_0 d_0^2 + coeff_1 d_1^2 + coeff_2 d_2^2 + coeff_3 d_3^2 added left to right, d = y - goal; the
   // subtractions and products in (position, velocity) pairs
@@ -241,6 +273,20 @@ struct BicycleCostmapModel
     xd[1] = vxy.y;
     xd[2] = ar.div(x[3] * ar.div(sd, cd), p.wheelbase);
     xd[3] = u[0];
+  }
+  // Host Jacobians of the kinematic bicycle in double: A = d xdot / dx (row-major 4 x 4), B = d xdot / du (4 x 2).
+  static bool computeGrad(const DynParams& p, const float* x, const float* u, double* A, double* B)
+  {
+    const double yaw = x[2], v = x[3], steer = u[1], L = p.wheelbase;
+    const double sy = std::sin(yaw), cy = std::cos(yaw), cd = std::cos(steer);
+    A[0 * 4 + 2] = -v * sy;
+    A[0 * 4 + 3] = cy;
+    A[1 * 4 + 2] = v * cy;
+    A[1 * 4 + 3] = sy;
+    A[2 * 4 + 3] = std::tan(steer) / L;
+    B[2 * 2 + 1] = v / (L * cd * cd);
+    B[3 * 2 + 0] = 1.0;
+    return true;
   }
   template <class Ar = ExactArith>
   static MG_HD float speedMapCost(const CostParams& q, const ModelAux& aux, const float* y, Ar&& ar = Ar{})

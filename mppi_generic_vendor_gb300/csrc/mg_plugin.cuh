@@ -25,6 +25,18 @@ struct DefinesEnforceConstraints<T, std::void_t<decltype(&T::enforceConstraints)
 {
 };
 
+// Whether a plugin's dynamics class defines host Jacobians, bool computeGrad(const float* x, const float* u, float* A,
+// float* B) (Dynamics::computeGrad, dynamics.cuh:236-242; used by the DDP feedback controller, which otherwise takes
+// forward differences).
+template <class T, class = void>
+struct DefinesComputeGrad : std::false_type
+{
+};
+template <class T>
+struct DefinesComputeGrad<T, std::void_t<decltype(&T::computeGrad)>> : std::true_type
+{
+};
+
 // The engine's Model concept for a plugin pair: the plugin structs are the parameter blocks (one per instance),
 // copied to the device by value.  kOwnConstraints: the dynamics class defines enforceConstraints, which then
 // replaces the engine's deadband + clamp: the samples are written unconstrained and each rollout step passes its

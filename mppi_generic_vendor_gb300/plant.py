@@ -5,13 +5,15 @@ publishes the control for that time from the latest solution; ``runControlLoop``
 newest state, sliding the nominal sequence by the robot time that passed.  Subclasses provide the robot side
 (``pubControl``, ``pubNominalState``, ``pubFreeEnergyStatistics``, ``checkStatus``, ``getCurrentTime``,
 ``getPoseTime``), as in the reference.  Parameter updates arrive from any thread and are applied between
-optimisations.  Feedback controllers are not part of this engine, so the published control is the nominal sequence
-interpolated at the requested time.
+optimisations.  With the controller's feedback on, each solve is followed by the DDP feedback computation, and the
+published control is the controller's getCurrentControl: the nominal control at the requested time plus the
+feedback against the interpolated nominal state, constrained.
 
 The controller is any object with the ``VanillaMPPIController`` methods used here (``computeControl``,
 ``getControlSeq``, ``getTargetStateSeq``, ``slideControlSequence``, ``getFreeEnergyStatistics``, ``getDt``,
 ``getNumTimesteps`` and, for parameter updates, ``updateDynamicsParams``, ``updateCostParams``, ``setParams``,
-``setSamplingParams``).
+``setSamplingParams``).  A controller without ``getCurrentControl`` (and the feedback methods) has the nominal
+sequence interpolated at the requested time published.
 """
 from __future__ import annotations
 
@@ -38,6 +40,9 @@ class BasePlant:
         self.last_used_state_update_time_ = 0.0
         self.state_traj_ = None
         self.control_traj_ = None
+        self.feedback_state_ = None
+        self.feedback_duration_ = 0.0
+        self.avg_feedback_time_ms_ = 0.0
         self.num_iter_ = 0
         self.status_ = 0
         self.optimization_duration_ = 0.0
@@ -116,13 +121,21 @@ class BasePlant:
             if self.num_iter_ == 0:
                 return
             t0 = self.last_used_state_update_time_
-            u_traj, s_traj = self.control_traj_, self.state_traj_
-        dt = self.controller_.getDt()
+            u_traj, s_traj, fb_state = self.control_traj_, self.state_traj_, self.feedback_state_
+            x = self.state_
+        c = self.controller_
+        dt = c.getDt()
         since = t - t0
-        if since > 0 and t0 <= t < t0 + dt * self.controller_.getNumTimesteps():
-            self.pubControl(self._interpolate(u_traj, since / dt))
-            if self.debug_mode_:
-                self.pubNominalState(self._interpolate(s_traj, since / dt))
+        if since > 0 and t0 <= t < t0 + dt * c.getNumTimesteps():
+            if hasattr(c, "getCurrentControl"):
+                target = c.interpolateState(s_traj, since)
+                self.pubControl(c.getCurrentControl(x, since, target, u_traj, fb_state))
+                if self.debug_mode_:
+                    self.pubNominalState(target)
+            else:
+                self.pubControl(self._interpolate(u_traj, since / dt))
+                if self.debug_mode_:
+                    self.pubNominalState(self._interpolate(s_traj, since / dt))
 
     # ---- parameter updates from any thread (set*Params, then applied by updateParameters)
     def setDynamicsParams(self, params):
@@ -169,12 +182,19 @@ class BasePlant:
         return bool(pending)
 
     # ---- optimisation
-    def setSolution(self, state_seq, control_seq, timestamp: float):
+    def setSolution(self, state_seq, control_seq, timestamp: float, feedback_state=None):
         with self._guard:
             self.last_used_state_update_time_ = float(timestamp)
             self.state_traj_ = state_seq
             self.control_traj_ = control_seq
+            self.feedback_state_ = feedback_state
             self.num_iter_ += 1
+
+    def getFeedbackState(self):
+        return self.feedback_state_
+
+    def getAvgFeedbackTime(self) -> float:
+        return self.avg_feedback_time_ms_
 
     def runControlIteration(self, is_alive: threading.Event, poll_s: float = 5e-5, max_wait_s: float = 1.0) -> bool:
         """BasePlant::runControlIteration (base_plant.hpp:466-595): wait (bounded) for a state newer than the last
@@ -221,10 +241,19 @@ class BasePlant:
         if not np.all(np.isfinite(s)):
             raise RuntimeError("state trajectory inside the plant has a NaN")
         self.optimization_duration_ = (time.perf_counter() - opt_start) * 1e3
-        self.setSolution(s, u, state_time)
+        fb_start = time.perf_counter()
+        fb_state = None
+        if getattr(c, "getFeedbackEnabled", None) is not None and c.getFeedbackEnabled():
+            c.computeFeedback(state)
+            fb_state = c.getFeedbackState()
+        self.feedback_duration_ = (time.perf_counter() - fb_start) * 1e3
+        self.setSolution(s, u, state_time, fb_state)
         self.pubFreeEnergyStatistics(stats)
+        if getattr(c, "computeFeedbackPropagatedStateSeq", None) is not None:
+            c.computeFeedbackPropagatedStateSeq()
         n = self.num_iter_
         self.avg_optimize_time_ms_ += (self.optimization_duration_ - self.avg_optimize_time_ms_) / n
+        self.avg_feedback_time_ms_ += (self.feedback_duration_ - self.avg_feedback_time_ms_) / n
         self.optimize_loop_duration_ = (time.perf_counter() - loop_start) * 1e3
         self.avg_loop_time_ms_ += (self.optimize_loop_duration_ - self.avg_loop_time_ms_) / n
         return True

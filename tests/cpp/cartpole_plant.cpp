@@ -4,8 +4,13 @@
 //  1. single-threaded: the robot and runControlIteration alternate; the pole must be swung up and held
 //     (1 + cos theta < 0.05) for more than 100 of the 500 control periods, every iteration must slide by the
 //     target stride, and a parameter block handed over between iterations must reach the controller;
-//  2. threaded: runControlLoop on its own thread against the robot on the main thread, stopped through is_alive.
+//  2. threaded: runControlLoop on its own thread against the robot on the main thread, stopped through is_alive;
+//  3. with the DDP feedback controller on: every solve is followed by computeFeedback, the plant keeps the gains of
+//     the last solve and publishes getCurrentControl (nominal control plus feedback, constrained): the gains must be
+//     finite and not all zero, the published controls inside the control range, the feedback-propagated states
+//     finite and starting at the state optimised from.
 // Exits 0 on success.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -16,20 +21,26 @@
 
 using Controller = mppi_gb::VanillaMPPIController<mppi_gb::CartpoleDynamics, mppi_gb::CartpoleSwingupCost,
                                                   mppi_gb::NoFeedback, 100, 2048>;
+using Feedback = mppi_gb::DDPFeedback<mppi_gb::CartpoleDynamics, 100>;
+using FBController = mppi_gb::VanillaMPPIController<mppi_gb::CartpoleDynamics, mppi_gb::CartpoleSwingupCost, Feedback,
+                                                    100, 2048>;
 
-class CartpolePlant : public mppi_gb::BasePlant<Controller>
+template <class CTRL>
+class CartpolePlantT : public mppi_gb::BasePlant<CTRL>
 {
 public:
-  using BasePlant::BasePlant;
-  std::atomic<float> u{ 0.0f };
+  using Base = mppi_gb::BasePlant<CTRL>;
+  using Base::Base;
+  std::atomic<float> u{ 0.0f }, max_abs_u{ 0.0f };
   std::atomic<int> published{ 0 }, stats{ 0 };
   double now = 0.0;
-  void pubControl(const c_array& v) override
+  void pubControl(const typename Base::c_array& v) override
   {
     u = v[0];
+    max_abs_u = std::max(max_abs_u.load(), std::fabs(v[0]));
     ++published;
   }
-  void pubNominalState(const s_array&) override {}
+  void pubNominalState(const typename Base::s_array&) override {}
   void pubFreeEnergyStatistics(const mppi_gb::FreeEnergyStatistics& fe) override
   {
     if (std::isfinite(fe.freeEnergyMean)) ++stats;
@@ -38,6 +49,7 @@ public:
   double getCurrentTime() override { return now; }
   double getPoseTime() override { return now; }
 };
+using CartpolePlant = CartpolePlantT<Controller>;
 
 // explicit Euler of the cart-pole ODE (cartpole_dynamics.cu:48-67) over h seconds
 static void robot_step(double* x, double f, double h)
@@ -123,6 +135,56 @@ int main()
     std::printf("threaded: %d iterations, average optimisation %.3f ms\n", plant.getNumIterations(),
                 plant.getAvgOptimizationTime());
     if (plant.getNumIterations() < 40) ++failures;
+  }
+  // ---- 3. the DDP feedback controller on
+  {
+    mppi_gb::CartpoleDynamics dyn(1.0f, 1.0f, 1.0f);
+    dyn.setControlRanges({ std::pair<float, float>{ -5.0f, 5.0f } });
+    mppi_gb::CartpoleSwingupCost cost(10.0f, 1.0f, 100.0f, 1.0f, 0.0f);
+    mppi_gb::GaussianDistribution sampler(std::array<float, 1>{ 1.0f });
+    Feedback fb(&dyn, 0.02f);
+    auto ctrl = std::make_shared<FBController>(&dyn, &cost, &fb, &sampler, 0.02f, 1, 1.0f, 0.0f, 100,
+                                               FBController::control_trajectory{}, nullptr, 7);
+    auto params = fb.getParams();
+    params.Q = { 10.0f, 0, 0, 0, 0, 1.0f, 0, 0, 0, 0, 50.0f, 0, 0, 0, 0, 1.0f };
+    params.R = { 0.1f };
+    fb.setParams(params);  // reaches the controller built with fb
+    ctrl->initFeedback();
+    CartpolePlantT<FBController> plant(ctrl, 50, 1);
+    std::atomic<bool> alive{ true };
+    double x[4] = { 0.0, 0.0, 0.0, 0.0 };
+    plant.updateState(as_state(x), 0.0);
+    for (int k = 0; k < 200; ++k)
+    {
+      if (!plant.runControlIteration(&alive)) ++failures;
+      for (int sub = 0; sub < 4; ++sub)
+      {
+        robot_step(x, plant.u.load(), 0.005);
+        plant.now += 0.005;
+        plant.updateState(as_state(x), plant.now);
+      }
+    }
+    const auto gains = plant.getFeedbackState();
+    int nonzero = 0, nonfinite = 0;
+    for (float g : gains.fb_gain_traj_)
+    {
+      nonzero += g != 0.0f;
+      nonfinite += !std::isfinite(g);
+    }
+    const auto prop = ctrl->getFeedbackPropagatedStateSeq();
+    const auto target = ctrl->getTargetStateSeq();
+    int prop_bad = 0;
+    for (int i = 0; i < 4 * 100; ++i) prop_bad += !std::isfinite(prop[i]);
+    for (int i = 0; i < 4; ++i) prop_bad += prop[i] != target[i];
+    std::printf("feedback: %d iterations, %d non-zero gains, max |u| published %.3f, average feedback %.3f ms, "
+                "theta=%.3f\n",
+                plant.getNumIterations(), nonzero, plant.max_abs_u.load(), plant.getAvgFeedbackTime(), x[2]);
+    if (plant.getNumIterations() != 200 || nonzero == 0 || nonfinite || prop_bad || plant.max_abs_u.load() > 5.0f ||
+        !(plant.getAvgFeedbackTime() > 0.0) || !ctrl->getFeedbackEnabled())
+    {
+      std::printf("FAILED: nonfinite=%d prop_bad=%d\n", nonfinite, prop_bad);
+      ++failures;
+    }
   }
   return failures == 0 ? 0 : 1;
 }

@@ -1,7 +1,9 @@
 // Three Dynamics / Cost plugin pairs written against include/mppi_gb_plugin.cuh, outside the engine's sources, the
 // way a user of the library would write them: the double integrator (DoubleIntegratorDynamics, di_dynamics.cu:46-53)
-// with an optional linear damping, once with the default Euler step, once with its own step override (semi-implicit:
-// velocity first, then position with the new velocity) and once with its own enforceConstraints; and
+// with an optional linear damping, once with the default Euler step and its analytic Jacobians (computeGrad, for the
+// DDP feedback controller), once with its own step override (semi-implicit: velocity first, then position with the
+// new velocity; no computeGrad, so the feedback controller differentiates numerically) and once with its own
+// enforceConstraints; and
 // QuadraticCostImpl's state cost (quadratic_cost.cu:35-48) with a crash wall that uses the crash argument of
 // computeRunningCost: once x > wall_x the sample's crash flag stays set and every later step pays crash_cost.
 #include "mppi_gb_plugin.cuh"
@@ -15,6 +17,17 @@ struct DIPlugin : mppi_gb::Dynamics<DIPlugin, 4, 2>
     xd[1] = x[3];
     xd[2] = u[0] - damping * x[2];
     xd[3] = u[1] - damping * x[3];
+  }
+  // host Jacobians for the DDP feedback controller (Dynamics::computeGrad, dynamics.cuh:236-242)
+  bool computeGrad(const float*, const float*, float* A, float* B) const
+  {
+    A[0 * 4 + 2] = 1.0f;
+    A[1 * 4 + 3] = 1.0f;
+    A[2 * 4 + 2] = -damping;
+    A[3 * 4 + 3] = -damping;
+    B[2 * 2 + 0] = 1.0f;
+    B[3 * 2 + 1] = 1.0f;
+    return true;
   }
 };
 

@@ -23,7 +23,7 @@ def test_header_symbols_exported_and_bound():
     for n in names:
         assert hasattr(lib, n), f"{n} declared in mppi_gb.h but not exported"
         assert n in bound, f"{n} has no ctypes signature"
-    assert lib.mppi_abi_version() == 2
+    assert lib.mppi_abi_version() == 3
 
 
 @pytest.mark.parametrize("model", [A.MODEL_CARTPOLE, A.MODEL_DOUBLE_INTEGRATOR, A.MODEL_BICYCLE_COSTMAP,

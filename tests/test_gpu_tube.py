@@ -32,7 +32,7 @@ def _check(ctrl, ref, K, T):
               samples=ref["samples"][i]) for i in range(2)]
     # the actual sequence is the (unsmoothed) update of distribution 0; the nominal one the smoothed update of
     # distribution 1, or of distribution 0 when the nominal system took over the actual one
-    _parity.check_control(ctrl.getControlSeq().T, d[0], K, T, 2, smoothed=False)
+    _parity.check_control(ctrl.getActualControlSeq().T, d[0], K, T, 2, smoothed=False)
     src = d[1] if ref["nominal_used"] else d[0]
     _parity.check_control(ctrl.getNominalControlSeq().T, dict(src, control=ref["control"][1]), K, T, 2)
     states = ctrl.getTargetStateSeqs()
@@ -59,13 +59,16 @@ def test_tube_solve_slide_solve_matches_oracle(threshold):
     _check(ctrl, ref, K, T)
     # slide: the nominal state advances one step along the nominal sequence, both sequences slide; then a disturbed
     # actual state and fresh noise
-    u_nom, u_act = ctrl.getNominalControlSeq().T.copy(), ctrl.getControlSeq().T.copy()
+    u_nom, u_act = ctrl.getNominalControlSeq().T.copy(), ctrl.getActualControlSeq().T.copy()
     nominal_x0 = oracle.step_state(ctrl.model_id, ctrl._dyn_arr[0], ctrl._cost_arr[0], ref["nominal_x0"], u_nom[0],
                                    0.02)
     ctrl.slideControlSequence(1)
     zero = np.zeros(2, np.float32)
     seqs = np.stack([oracle.slide(u_act, 1, [0.0, 0.0], zero), oracle.slide(u_nom, 1, [0.0, 0.0], zero)])
-    assert np.array_equal(ctrl.getControlSeq().T, seqs[0]) and np.array_equal(ctrl.getNominalControlSeq().T, seqs[1])
+    assert np.array_equal(ctrl.getActualControlSeq().T, seqs[0])
+    assert np.array_equal(ctrl.getNominalControlSeq().T, seqs[1])
+    # the reference's getControlSeq / getTargetStateSeq of a Tube-MPPI controller are the nominal system's
+    assert np.array_equal(ctrl.getControlSeq(), ctrl.getNominalControlSeq())
     x2 = np.array([0.05, -0.03, 0.25, -0.1], np.float32)
     eps2 = rng.standard_normal(2 * K * T * 2).astype(np.float32)
     ctrl.injectNoise(eps2)

@@ -112,6 +112,10 @@ typedef struct mppi_sampling_params
   float exponents[MPPI_MAX_CONTROL_DIM];    /* colored noise: PSD ~ 1/f^exponent */
   float offset_decay_rate;                  /* colored noise, default 0.97 */
   float fmin;                               /* colored noise low-frequency cutoff, default 0 */
+  int use_same_noise_for_all_distributions; /* SamplingParams (sampling_distribution.cuh:20), default 1: the two
+                                               distributions of a Tube-MPPI handle draw the same standard normals
+                                               (gaussian.cu:378-390), each around its own mean; independent
+                                               controllers of a batched handle always draw their own */
 } mppi_sampling_params;
 
 /* Dynamics::control_rngs_, control_deadband_, zero_control_ (dynamics.cuh:508; dynamics.cu:107-126). */
@@ -374,7 +378,9 @@ mppi_status mppi_use_analytic_dynamics(mppi_handle* h, int enable);
  * Parity hook: use the given standard-normal noise for every subsequent iteration instead of Philox noise.
  * Gaussian: host float[sum_i K_i*T_i*C], the epsilon that curandGenerateNormal writes before setGaussianControls
  * (gaussian.cu:375-431).  Colored noise: host float[sum_i K_i*C*(T_i+1)*2], the complex spectrum before
- * configureFrequencyNoise (colored_noise.cu:343).  noise == NULL clears the injection.
+ * configureFrequencyNoise (colored_noise.cu:343).  noise == NULL clears the injection.  On a Tube-MPPI handle with
+ * use_same_noise_for_all_distributions both distributions read instance 0's part (the second part is ignored), as
+ * the reference's generateSamples copies one draw to every distribution (gaussian.cu:378-390).
  */
 mppi_status mppi_inject_noise(mppi_handle* h, const float* noise, size_t count);
 

@@ -42,7 +42,8 @@ class ControllerParams(C.Structure):
 class SamplingParams(C.Structure):
     _fields_ = [("kind", C.c_int), ("std_dev", _F4), ("control_cost_coeff", _F4),
                 ("pure_noise_trajectories_percentage", C.c_float), ("std_dev_decay", C.c_float),
-                ("exponents", _F4), ("offset_decay_rate", C.c_float), ("fmin", C.c_float)]
+                ("exponents", _F4), ("offset_decay_rate", C.c_float), ("fmin", C.c_float),
+                ("use_same_noise_for_all_distributions", C.c_int)]
 
 
 class ControlConstraints(C.Structure):
@@ -265,6 +266,7 @@ def default_sampling_params(native: bool = True) -> SamplingParams:
         p.std_dev_decay = 1.0
         p.offset_decay_rate = 0.97
         p.fmin = 0.0
+        p.use_same_noise_for_all_distributions = 1
     return p
 
 

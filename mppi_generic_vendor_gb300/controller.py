@@ -194,6 +194,9 @@ class GaussianDistribution:
     control_cost_coeff: tuple = (0.0,)
     pure_noise_trajectories_percentage: float = 0.01
     std_dev_decay: float = 1.0
+    # SamplingParams::use_same_noise_for_all_distributions (sampling_distribution.cuh:20): Tube-MPPI's two
+    # distributions draw the same standard normals
+    use_same_noise_for_all_distributions: bool = True
     kind: int = field(default=A.SAMPLER_GAUSSIAN, init=False)
 
     def to_c(self) -> A.SamplingParams:
@@ -205,6 +208,7 @@ class GaussianDistribution:
             p.control_cost_coeff[i] = v
         p.pure_noise_trajectories_percentage = self.pure_noise_trajectories_percentage
         p.std_dev_decay = self.std_dev_decay
+        p.use_same_noise_for_all_distributions = int(bool(self.use_same_noise_for_all_distributions))
         return p
 
 

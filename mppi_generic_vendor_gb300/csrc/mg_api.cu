@@ -241,6 +241,7 @@ void mppi_default_sampling_params(mppi_sampling_params* p)
   p->std_dev_decay = 1.0f;
   p->offset_decay_rate = 0.97f;
   p->fmin = 0.0f;
+  p->use_same_noise_for_all_distributions = 1;
 }
 
 void mppi_default_constraints(mppi_control_constraints* c)

@@ -121,7 +121,7 @@ __device__ __forceinline__ void row_transform_pow2(const ColoredArgs& a, const I
   // ---- 1. scaled spectrum, element f = lane + 32 r, Nyquist (f = M) on lane 0
   if (a.injected_spec)
   {
-    const float* src = a.injected_spec + d.spec_off + row * (long long)(M + 1) * 2;
+    const float* src = a.injected_spec + d.noise_spec_off + row * (long long)(M + 1) * 2;
 #pragma unroll
     for (int r = 0; r < R; ++r)
     {
@@ -278,7 +278,7 @@ __device__ __forceinline__ void row_transform_direct(const ColoredArgs& a, const
     float4 n;
     if (a.injected_spec)
     {
-      const float* src = a.injected_spec + d.spec_off + row * (long long)F * 2 + 2 * f0;
+      const float* src = a.injected_spec + d.noise_spec_off + row * (long long)F * 2 + 2 * f0;
       n.x = src[0];
       n.y = src[1];
       n.z = (f0 + 1 < F) ? src[2] : 0.0f;
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(256, ColoredQuadShape<C, L>::MIN_CTAS)
       // ---- 1. the scaled spectrum of this thread's frequencies
       if (a.injected_spec)
       {
-        const float* src = a.injected_spec + d.spec_off + row * (long long)(M + 1) * 2;
+        const float* src = a.injected_spec + d.noise_spec_off + row * (long long)(M + 1) * 2;
 #pragma unroll
         for (int r = 0; r <= L; ++r)
         {
@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(256, ColoredQuadShape<C, L>::MIN_CTAS)
         for (int b = 0; b < L / 2; ++b)
         {
           const u32x4 u = philox4x32_10(u32x4{ (uint32_t)(4 * b + q) | 0x20000000u, (uint32_t)row,
-                                               (uint32_t)w.x | 0x80000000u, counter },
+                                               (uint32_t)d.noise_inst | 0x80000000u, counter },
                                         a.seed_lo, a.seed_hi);
           box_muller_fast(u.x, u.y, &v[2 * b].x, &v[2 * b].y);
           box_muller_fast(u.z, u.w, &v[2 * b + 1].x, &v[2 * b + 1].y);
@@ -569,10 +569,10 @@ __global__ void __launch_bounds__(32 * SPB * C, (R >= 8 || R == 0) ? 2 : 3)
       const long long row = (long long)(w.y + s_local) * C + c;
       float* tile_row = tile + s_local * tile_row_floats(T, C) + c;
       if constexpr (R > 0)
-        row_transform_pow2<C, R>(a, d, w.x, row, c, lane, tab, parts, tile_row, counter);
+        row_transform_pow2<C, R>(a, d, d.noise_inst, row, c, lane, tab, parts, tile_row, counter);
       else
-        row_transform_direct<C>(a, d, w.x, row, c, lane, tab, parts, tile_row, Xall + warp * (kColoredMaxT + 2),
-                                counter);
+        row_transform_direct<C>(a, d, d.noise_inst, row, c, lane, tab, parts, tile_row,
+                                Xall + warp * (kColoredMaxT + 2), counter);
     }
     __syncthreads();
     colored_store_tile<C>(a, d, w.y, nsamp, tile);

@@ -514,6 +514,7 @@ public:
     if (kind_changed) injected_d_.reset();
     sp_ = *sp;
     if (kind_changed) MG_TRY(build_work_lists());  // the rollout kernel (fused or not) and its grid follow the kind
+    MG_TRY(refresh_noise_sources());
     MG_TRY(build_colored_tables());
     invalidate_graphs();
     return MPPI_OK;
@@ -530,6 +531,7 @@ public:
       if (rollout_mode_ == 4 && !noise_warps_available()) rollout_mode_ = 0;
       MG_TRY(build_work_lists());
     }
+    MG_TRY(refresh_noise_sources());
     invalidate_graphs();
     return MPPI_OK;
   }
@@ -1447,6 +1449,30 @@ private:
 
   // Work lists: rollout tiles ordered by decreasing horizon (the cost of a tile is proportional to T), sampler items,
   // and weight/update chunks with the offsets of their partial rows.
+  // Which noise each instance draws (InstDesc::noise_*): its own, except that the second distribution of a Tube-MPPI
+  // handle draws the first one's when use_same_noise_for_all_distributions is set (generateSamples copies one draw to
+  // every distribution, gaussian.cu:378-390).
+  void set_noise_sources(std::vector<InstDesc>& inst) const
+  {
+    const bool shared = tube() && sp_.use_same_noise_for_all_distributions != 0;
+    for (int i = 0; i < I_; ++i)
+    {
+      const int src = shared ? 0 : i;
+      inst[i].noise_inst = src;
+      inst[i].noise_off = inst[src].u_off;
+      inst[i].noise_spec_off = inst[src].spec_off;
+    }
+  }
+  // after a change of the controller kind or of the sampling parameters
+  mppi_status refresh_noise_sources()
+  {
+    if (inst_h_.empty()) return MPPI_OK;
+    set_noise_sources(inst_h_);
+    MG_CUDA(cudaStreamSynchronize(stream_));
+    MG_CUDA(cudaMemcpy(inst_d_.p, inst_h_.data(), sizeof(InstDesc) * I_, cudaMemcpyHostToDevice));
+    return MPPI_OK;
+  }
+
   mppi_status build_work_lists()
   {
     std::vector<InstDesc> inst(I_);
@@ -1530,6 +1556,8 @@ private:
     MG_TRY(chunk0_d_.alloc(I_));
     MG_TRY(partials_d_.alloc((size_t)std::max<long long>(poff, 1)));
     MG_TRY(part_w_d_.alloc(2 * chunks.size()));
+    set_noise_sources(inst);
+    inst_h_ = inst;
     MG_CUDA(cudaMemcpy(inst_d_.p, inst.data(), sizeof(InstDesc) * I_, cudaMemcpyHostToDevice));
     MG_CUDA(cudaMemcpy(tiles_d_.p, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice));
     MG_CUDA(cudaMemcpy(swork_d_.p, swork.data(), sizeof(int2) * swork.size(), cudaMemcpyHostToDevice));
@@ -2211,6 +2239,7 @@ private:
   DevBuf<CostParams> cost_d_;
   DevBuf<unsigned int> baseline_bits_d_, arrive_d_, counters_d_;
   DevBuf<InstDesc> inst_d_;
+  std::vector<InstDesc> inst_h_;  // host copy of inst_d_
   DevBuf<int2> tiles_d_, swork_d_, cwork_d_;
   DevBuf<float> ctab_d_;
   DevBuf<int> ctab_off_d_;

@@ -32,6 +32,11 @@ struct InstDesc
   long long spec_off;  // into the colored-noise spectrum (floats)
   int x_off;         // into x0 (floats)
   int num_chunks;    // weight/update chunks of this instance
+  // the noise this instance draws: its own Philox stream and injected noise, or those of instance noise_inst (a
+  // Tube-MPPI handle's second distribution with use_same_noise_for_all_distributions)
+  int noise_inst;
+  long long noise_off;       // injected Gaussian noise (floats, samples layout)
+  long long noise_spec_off;  // injected colored-noise spectrum (floats)
 };
 
 // Uniform (per handle) sampling + constraint parameters.
@@ -108,7 +113,7 @@ __global__ void __launch_bounds__(256) gaussian_sample_kernel(const __grid_const
       float4 z;
       if (a.injected)
       {
-        const float* src = a.injected + d.u_off + 4 * q;
+        const float* src = a.injected + d.noise_off + 4 * q;
         if (4 * q + 3 < n)
         {
           z = *reinterpret_cast<const float4*>(src);
@@ -123,7 +128,7 @@ __global__ void __launch_bounds__(256) gaussian_sample_kernel(const __grid_const
       }
       else
       {
-        z = philox_normal4((uint64_t)q, (uint32_t)w.x, counter, a.seed_lo, a.seed_hi);
+        z = philox_normal4((uint64_t)q, (uint32_t)d.noise_inst, counter, a.seed_lo, a.seed_hi);
       }
       float zz[4] = { z.x, z.y, z.z, z.w };
       float out[4];
@@ -833,12 +838,11 @@ __device__ __forceinline__ float4 gaussian_quad(const SampleShared& sh, const fl
                           pure_threshold, rem0, z);
 }
 
-// The four normals of Philox quad q of instance inst (or the injected ones).
-__device__ __forceinline__ float4 fused_noise(const FusedNoise& f, const InstDesc& d, int inst, uint32_t counter,
-                                              long long q)
+// The four normals of Philox quad q of the instance's noise stream (or the injected ones).
+__device__ __forceinline__ float4 fused_noise(const FusedNoise& f, const InstDesc& d, uint32_t counter, long long q)
 {
-  return f.injected ? *reinterpret_cast<const float4*>(f.injected + d.u_off + 4 * q)
-                    : philox_normal4((uint64_t)q, (uint32_t)inst, counter, f.seed_lo, f.seed_hi);
+  return f.injected ? *reinterpret_cast<const float4*>(f.injected + d.noise_off + 4 * q)
+                    : philox_normal4((uint64_t)q, (uint32_t)d.noise_inst, counter, f.seed_lo, f.seed_hi);
 }
 
 // Re-roll of chosen samples for visualisation (VanillaMPPIController::calculateSampledStateTrajectories ->
@@ -951,7 +955,7 @@ __global__ void __launch_bounds__(kNoiseWarps ? 2 * NS : NS)
           for (int qi = c0; qi < c1; ++qi)
           {
             const float4 o = gaussian_quad<C>(a.sh, __ldg(mrow + qi), f.decay_pow, f.stride, k, pure_threshold,
-                                              4 * qi, fused_noise(f, d, w.x, counter, q0 + qi));
+                                              4 * qi, fused_noise(f, d, counter, q0 + qi));
             *reinterpret_cast<float4*>(dst + 4 * qi) = o;
             float* col = s_u + (size_t)(4 * qi) * us + slot;
             col[0] = o.x;
@@ -1014,7 +1018,7 @@ __global__ void __launch_bounds__(kNoiseWarps ? 2 * NS : NS)
       const float4* mrow = reinterpret_cast<const float4*>(a.mean + d.t_off);
       const int us = a.tr.partials ? a.tr.u_stride : 0;
       auto run = [&](auto lik) {
-        float4 zn = fused_noise(f, d, w.x, counter, q0);
+        float4 zn = fused_noise(f, d, counter, q0);
         float4 mn = __ldg(mrow);
         // Q quads (Q * G steps) per speculated run
         auto quads = [&](int qi, auto q_const) {
@@ -1026,7 +1030,7 @@ __global__ void __launch_bounds__(kNoiseWarps ? 2 * NS : NS)
             const float4 z = zn, m = mn;
             // the next quad's normals and nominal controls (the last quad reloads its own: no branch in the loop)
             const int qn = min(qi + p + 1, nq - 1);
-            zn = fused_noise(f, d, w.x, counter, q0 + qn);
+            zn = fused_noise(f, d, counter, q0 + qn);
             mn = __ldg(mrow + qn);
             const float4 o = gaussian_quad<C>(a.sh, m, f.decay_pow, f.stride, k, pure_threshold, 4 * (qi + p), z);
             *reinterpret_cast<float4*>(dst + 4 * (qi + p)) = o;
@@ -1167,7 +1171,7 @@ __global__ void __launch_bounds__(4 * NS) rollout_coop_kernel(const __grid_const
         if (q < nq && active)
         {
           o = gaussian_quad<C>(a.sh, a.mean + d.t_off, f.decay_pow, f.stride, k, pure_threshold, 4 * q,
-                               fused_noise(f, d, w.x, counter, q0 + q));
+                               fused_noise(f, d, counter, q0 + q));
           *reinterpret_cast<float4*>(dst + 4 * q) = o;
         }
         const int nquads = min(L, nq - gi * L);
@@ -1301,7 +1305,7 @@ __global__ void __launch_bounds__(NS) rollout_dyn_kernel(const __grid_constant__
       const float pure_threshold = (1.0f - a.sh.pure_pct) * (float)d.K;
       float* dst = f.samples + d.u_off + 4 * q0;
       float* ys = states + d.u_off / C * S + (long long)k * d.T * S;
-      float4 zn = fused_noise(f, d, w.x, counter, q0);
+      float4 zn = fused_noise(f, d, counter, q0);
       auto quads = [&](int qi, auto q_const) {
         constexpr int Q = decltype(q_const)::value;
         float out[4 * Q];
@@ -1309,7 +1313,7 @@ __global__ void __launch_bounds__(NS) rollout_dyn_kernel(const __grid_constant__
         for (int p = 0; p < Q; ++p)
         {
           const float4 z = zn;
-          zn = fused_noise(f, d, w.x, counter, q0 + min(qi + p + 1, nq - 1));
+          zn = fused_noise(f, d, counter, q0 + min(qi + p + 1, nq - 1));
           const float4 o =
               gaussian_quad<C>(a.sh, a.mean + d.t_off, f.decay_pow, f.stride, k, pure_threshold, 4 * (qi + p), z);
           *reinterpret_cast<float4*>(dst + 4 * (qi + p)) = o;

@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(kMlpSamplesPerCta) rollout_mlp_kernel(
           {
             const long long q = (long long)k[n] * nq_row + (t >> 1);
             uq[n] = gaussian_quad<C>(a.sh, a.mean + d.t_off, f.decay_pow, f.stride, k[n], pure_threshold, t * C,
-                                     fused_noise(f, d, w.x, counter, q));
+                                     fused_noise(f, d, counter, q));
             *reinterpret_cast<float4*>(f.samples + d.u_off + 4 * q) = uq[n];
           }
           u[n][0] = (t & 1) ? uq[n].z : uq[n].x;

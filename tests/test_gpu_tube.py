@@ -13,13 +13,22 @@ from mppi_generic_vendor_gb300 import TubeMPPIController
 pytestmark = pytest.mark.gpu
 
 
-def _tube(K, T, threshold):
+def _tube(K, T, threshold, same_noise=True):
     dyn = DoubleIntegratorDynamics()
     dyn.setControlRanges([(-2.0, 2.0), (-2.0, 2.0)])
     cost = DoubleIntegratorObstacleCost(goal=(1.5, -0.5, 0.0, 0.0), coeff=(1.0, 1.0, 0.1, 0.1), terminal_coeff=5.0,
                                         obstacles=[(0.7, 0.0, 0.3)], obstacle_cost=100.0)
-    return TubeMPPIController(dyn, cost, None, GaussianDistribution(std_dev=(0.6, 0.6)), 0.02, 1, 1.0, 0.0, T, K,
-                              nominal_threshold=threshold)
+    sampler = GaussianDistribution(std_dev=(0.6, 0.6), use_same_noise_for_all_distributions=same_noise)
+    return TubeMPPIController(dyn, cost, None, sampler, 0.02, 1, 1.0, 0.0, T, K, nominal_threshold=threshold)
+
+
+def _draw(rng, K, T, same_noise):
+    """Injected noise for both distributions: with use_same_noise_for_all_distributions the second reads the first's
+    (generateSamples copies one draw, gaussian.cu:378-390), so the oracle gets the first half twice."""
+    if same_noise:
+        e = rng.standard_normal(K * T * 2).astype(np.float32)
+        return np.concatenate([e, e])
+    return rng.standard_normal(2 * K * T * 2).astype(np.float32)
 
 
 def _check(ctrl, ref, K, T):
@@ -43,15 +52,19 @@ def _check(ctrl, ref, K, T):
 
 
 @pytest.mark.parametrize("threshold", [20.0, -1e9])
-def test_tube_solve_slide_solve_matches_oracle(threshold):
+@pytest.mark.parametrize("same_noise", [True, False])
+def test_tube_solve_slide_solve_matches_oracle(threshold, same_noise):
     K, T = 2048, 48
     rng = np.random.default_rng(11 if threshold > 0 else 12)
-    ctrl = _tube(K, T, threshold)
+    ctrl = _tube(K, T, threshold, same_noise)
     init = rng.uniform(-0.5, 0.5, (T, 2)).astype(np.float32)
     ctrl.setControlSeq(init.T)
     x = np.array([0.0, 0.0, 0.3, -0.2], np.float32)
-    eps = rng.standard_normal(2 * K * T * 2).astype(np.float32)
-    ctrl.injectNoise(eps)
+    eps = _draw(rng, K, T, same_noise)
+    injected = eps.copy()
+    if same_noise:  # the engine reads only the first half, so the second may hold anything
+        injected[K * T * 2:] = rng.standard_normal(K * T * 2).astype(np.float32)
+    ctrl.injectNoise(injected)
     ctrl.computeControl(x, 1)
     ref = oracle.tube_compute_control(ctrl.model_id, ctrl._dyn_arr[0], ctrl._cost_arr[0], ctrl.getParams(),
                                       ctrl.sampler_.to_c(), ctrl.constraints_, K, T, 2, 4, x, x, eps,
@@ -70,7 +83,7 @@ def test_tube_solve_slide_solve_matches_oracle(threshold):
     # the reference's getControlSeq / getTargetStateSeq of a Tube-MPPI controller are the nominal system's
     assert np.array_equal(ctrl.getControlSeq(), ctrl.getNominalControlSeq())
     x2 = np.array([0.05, -0.03, 0.25, -0.1], np.float32)
-    eps2 = rng.standard_normal(2 * K * T * 2).astype(np.float32)
+    eps2 = _draw(rng, K, T, same_noise)
     ctrl.injectNoise(eps2)
     ctrl.computeControl(x2, 1)
     ref2 = oracle.tube_compute_control(ctrl.model_id, ctrl._dyn_arr[0], ctrl._cost_arr[0], ctrl.getParams(),
@@ -79,6 +92,20 @@ def test_tube_solve_slide_solve_matches_oracle(threshold):
     _check(ctrl, ref2, K, T)
     assert np.array_equal(ctrl.getNominalStateSeq()[:, 0], ref2["nominal_x0"])
     assert ref2["nominal_used"] == (0 if threshold > 0 else 1)
+    ctrl.close()
+
+
+@pytest.mark.parametrize("same_noise", [True, False])
+def test_tube_distributions_share_philox_noise(same_noise):
+    """With both distributions around the same mean, use_same_noise_for_all_distributions gives bit-identical
+    samples for the two (one Philox draw); without it they are independent."""
+    K, T = 1024, 32
+    ctrl = _tube(K, T, 20.0, same_noise)
+    init = np.random.default_rng(3).uniform(-0.5, 0.5, (T, 2)).astype(np.float32)
+    ctrl.setControlSeq(init.T)
+    ctrl.generateSamples(1, 0)
+    s = ctrl.control_samples().reshape(2, K, T, 2)
+    assert np.array_equal(s[0], s[1]) == same_noise
     ctrl.close()
 
 

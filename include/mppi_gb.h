@@ -69,7 +69,7 @@ typedef enum mppi_controller_kind
   MPPI_CONTROLLER_VANILLA = 0, /* VanillaMPPIController (mppi_controller.cu:152-237) */
   MPPI_CONTROLLER_COLORED = 1, /* ColoredMPPIController (colored_mppi_controller.cu:145-249): Tsallis weights when
                                   tsallis_gamma != 0 and tsallis_r != 0, state leash, final clamp of control 1 only */
-  MPPI_CONTROLLER_TUBE = 2     /* TubeMPPIController (tube_mppi_controller.cu:158-296): the handle holds exactly two
+  MPPI_CONTROLLER_TUBE = 2,    /* TubeMPPIController (tube_mppi_controller.cu:158-296): the handle holds exactly two
                                   instances of equal K and T, the reference's two sampling distributions
                                   [D = 2][K][T][C]: instance 0 is the actual system, rolled out from the state
                                   given to mppi_compute_control (STATE_DIM floats), instance 1 the nominal system,
@@ -79,6 +79,15 @@ typedef enum mppi_controller_kind
                                   actual baseline is below the nominal baseline + nominal_threshold.  Only the
                                   nominal sequence is smoothed; neither is clamped.  The ancillary feedback
                                   controller (mppi_compute_feedback) tracks the nominal system. */
+  MPPI_CONTROLLER_RMPPI = 3    /* RobustMPPIController (robust_mppi_controller.cu:635-744): two instances of equal K
+                                  and T, the reference's distributions [D = 2][K][T][C] in its order: instance 0 the
+                                  nominal system, rolled out from the nominal state, instance 1 the real system,
+                                  rolled out from the state given to mppi_compute_control (STATE_DIM floats) with
+                                  the DDP feedback K_t (x_real - x_nominal) added to its controls.  Both sample
+                                  around the nominal sequence (the importance sampler); the nominal costs blend in
+                                  the real system's (rolloutRMPPIKernel, rmppi_kernels.cu:666-861).  Call
+                                  mppi_rmppi_update_importance_sampler before each mppi_compute_control.  Built-in
+                                  analytic models with Gaussian sampling. */
 } mppi_controller_kind;
 
 /* ControllerParams (include/mppi/controllers/controller.cuh:46-68) and the fields ColoredMPPIParams adds
@@ -99,6 +108,11 @@ typedef struct mppi_controller_params
                         at the step the last slideControlSequence moved by (leash_jump_, 1 before any slide) */
   float state_leash_dist[MPPI_MAX_STATE_DIM]; /* ColoredMPPIParams::state_leash_dist_ (default 0) */
   float nominal_threshold; /* TubeMPPIParams::nominal_threshold_ (tube_mppi_controller.cuh:20, default 20) */
+  float value_function_threshold;    /* RobustMPPIParams::value_function_threshold_ (robust_mppi_controller.cuh:17,
+                                        default 1000) */
+  int num_candidate_nominal_states;  /* RobustMPPIParams::num_candidate_nominal_states_ (default 9; odd, >= 3) */
+  int num_eval_samples_per_candidate; /* samples per candidate of the initial-state evaluation (the eval kernel's
+                                         block width in the reference; default 64); candidates x samples <= K */
 } mppi_controller_params;
 
 /* GaussianParamsImpl (gaussian.cuh:21-61) and ColoredNoiseParamsImpl (colored_noise.cuh:44-73). */
@@ -113,7 +127,8 @@ typedef struct mppi_sampling_params
   float offset_decay_rate;                  /* colored noise, default 0.97 */
   float fmin;                               /* colored noise low-frequency cutoff, default 0 */
   int use_same_noise_for_all_distributions; /* SamplingParams (sampling_distribution.cuh:20), default 1: the two
-                                               distributions of a Tube-MPPI handle draw the same standard normals
+                                               distributions of a Tube-MPPI or R-MPPI handle draw the same standard
+                                               normals
                                                (gaussian.cu:378-390), each around its own mean; independent
                                                controllers of a batched handle always draw their own */
 } mppi_sampling_params;
@@ -291,6 +306,21 @@ mppi_status mppi_get_sampled_trajectories(mppi_handle* h, int instance, const in
  * weights[0..num_samples-1] (the transformed costs, mppi_get_sample_weights), by the reference's replacement scan,
  * in the order of its list slots.  No handle or GPU involved. */
 mppi_status mppi_select_top_samples(const float* weights, int num_samples, int n, int* indices);
+/* RobustMPPIController::updateImportanceSamplingControl (robust_mppi_controller.cu:548-569), before each
+ * mppi_compute_control of an R-MPPI handle: the first call takes `state` (the real system's) as the nominal state;
+ * later calls place num_candidate_nominal_states candidates on the lines from the nominal trajectory's first state
+ * to its second and on to `state` (getInitNominalStateCandidates / computeLineSearchWeights, :351-363, 480-511),
+ * roll out num_eval_samples_per_candidate samples from each (initEvalKernel, rmppi_kernels.cu:231-357), and take the
+ * last candidate whose free energy is below value_function_threshold (computeBestIndex, :527-546) as the nominal
+ * state, with its stride; then the nominal sequence slides by that stride, its state trajectory is recomputed and the
+ * DDP feedback gains are computed from `state` (computeNominalFeedbackGains). */
+mppi_status mppi_rmppi_update_importance_sampler(mppi_handle* h, const float* state, int optimization_stride);
+/* The last candidate evaluation of an R-MPPI handle: best_index and nominal_stride (either may be NULL), and when not
+ * NULL candidate_states[num_candidates][STATE_DIM], candidate_strides[num_candidates], candidate_free_energy
+ * [num_candidates] and eval_costs[num_candidates * num_eval_samples_per_candidate]. */
+mppi_status mppi_rmppi_get_candidates(mppi_handle* h, int* best_index, int* nominal_stride, float* candidate_states,
+                                      int* candidate_strides, float* candidate_free_energy, float* eval_costs);
+
 /* Tube-MPPI handles: 1 if the last iteration kept the nominal system (its baseline was not beaten by the actual
  * system's, FreeEnergyStatistics::nominal_state_used), else 0. */
 mppi_status mppi_get_nominal_state_used(mppi_handle* h, int* used);
@@ -378,9 +408,9 @@ mppi_status mppi_use_analytic_dynamics(mppi_handle* h, int enable);
  * Parity hook: use the given standard-normal noise for every subsequent iteration instead of Philox noise.
  * Gaussian: host float[sum_i K_i*T_i*C], the epsilon that curandGenerateNormal writes before setGaussianControls
  * (gaussian.cu:375-431).  Colored noise: host float[sum_i K_i*C*(T_i+1)*2], the complex spectrum before
- * configureFrequencyNoise (colored_noise.cu:343).  noise == NULL clears the injection.  On a Tube-MPPI handle with
- * use_same_noise_for_all_distributions both distributions read instance 0's part (the second part is ignored), as
- * the reference's generateSamples copies one draw to every distribution (gaussian.cu:378-390).
+ * configureFrequencyNoise (colored_noise.cu:343).  noise == NULL clears the injection.  On a Tube-MPPI or R-MPPI
+ * handle with use_same_noise_for_all_distributions both distributions read instance 0's part (the second part is
+ * ignored), as the reference's generateSamples copies one draw to every distribution (gaussian.cu:378-390).
  */
 mppi_status mppi_inject_noise(mppi_handle* h, const float* noise, size_t count);
 

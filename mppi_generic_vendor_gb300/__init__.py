@@ -7,6 +7,7 @@ from . import _abi
 from ._abi import MPPIError
 from . import nn_io
 from .controller import (BatchedMPPIController, BicycleDynamics, ColoredMPPIController, TubeMPPIController, BicycleSlipDynamics, BicycleSlipMLPDynamics,
+                         RobustMPPIController,
                          CartpoleDynamics, DDPFeedback, DDPFeedbackState, DDPParams,
                          CartpoleSwingupCost, ColoredNoiseDistribution, CostmapCost, DoubleIntegratorDynamics,
                          DoubleIntegratorObstacleCost, GaussianDistribution, VanillaMPPIController,
@@ -16,4 +17,4 @@ __all__ = ["MPPIError", "BatchedMPPIController", "VanillaMPPIController", "Color
            "DoubleIntegratorDynamics", "DoubleIntegratorObstacleCost", "BicycleDynamics", "BicycleSlipDynamics",
            "BicycleSlipMLPDynamics",
            "CostmapCost", "GaussianDistribution", "ColoredNoiseDistribution", "select_top_samples", "_abi", "nn_io",
-           "DDPFeedback", "DDPFeedbackState", "DDPParams"]
+           "DDPFeedback", "DDPFeedbackState", "DDPParams", "RobustMPPIController"]

@@ -25,7 +25,7 @@ MODEL_BICYCLE_SLIP_MLP = 5
 MODEL_PLUGIN = 100
 
 SAMPLER_GAUSSIAN = 0
-CONTROLLER_VANILLA, CONTROLLER_COLORED, CONTROLLER_TUBE = 0, 1, 2
+CONTROLLER_VANILLA, CONTROLLER_COLORED, CONTROLLER_TUBE, CONTROLLER_RMPPI = 0, 1, 2, 3
 SAMPLER_COLORED_NOISE = 1
 
 _F4 = C.c_float * MPPI_MAX_CONTROL_DIM
@@ -36,7 +36,9 @@ class ControllerParams(C.Structure):
     _fields_ = [("dt", C.c_float), ("lambda_", C.c_float), ("alpha", C.c_float), ("num_timesteps", C.c_int),
                 ("num_iters", C.c_int), ("seed", C.c_uint64), ("slide_control_scale", _F4), ("controller", C.c_int),
                 ("tsallis_r", C.c_float), ("tsallis_gamma", C.c_float), ("leash_active", C.c_int),
-                ("state_leash_dist", C.c_float * MPPI_MAX_STATE_DIM), ("nominal_threshold", C.c_float)]
+                ("state_leash_dist", C.c_float * MPPI_MAX_STATE_DIM), ("nominal_threshold", C.c_float),
+                ("value_function_threshold", C.c_float), ("num_candidate_nominal_states", C.c_int),
+                ("num_eval_samples_per_candidate", C.c_int)]
 
 
 class SamplingParams(C.Structure):
@@ -124,6 +126,8 @@ SIGNATURES = [
     ("mppi_get_sampled_trajectories", C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.c_int, _FP, _FP, _FP, _IP]),
     ("mppi_get_model_dims", C.c_int, [_P, _IP, _IP, _IP, _IP]),
     ("mppi_get_nominal_state_used", C.c_int, [_P, _IP]),
+    ("mppi_rmppi_update_importance_sampler", C.c_int, [_P, _FP, C.c_int]),
+    ("mppi_rmppi_get_candidates", C.c_int, [_P, _IP, _IP, _FP, _IP, _FP, _FP]),
     ("mppi_set_feedback_params", C.c_int, [_P, _FP, _FP, _FP, C.c_int]),
     ("mppi_enable_feedback", C.c_int, [_P, C.c_int]),
     ("mppi_get_feedback_enabled", C.c_int, [_P, _IP]),
@@ -250,6 +254,7 @@ def default_controller_params(native: bool = True) -> ControllerParams:
         p.dt, p.lambda_, p.alpha, p.num_timesteps, p.num_iters, p.seed = 0.02, 1.0, 0.0, 100, 1, 0
         p.controller, p.tsallis_r, p.tsallis_gamma, p.leash_active = CONTROLLER_VANILLA, 2.0, 0.0, 0
         p.nominal_threshold = 20.0
+        p.value_function_threshold, p.num_candidate_nominal_states, p.num_eval_samples_per_candidate = 1000.0, 9, 64
     return p
 
 

@@ -899,3 +899,115 @@ class TubeMPPIController(BatchedMPPIController):
         v = C.c_int()
         A.call("mppi_get_nominal_state_used", self._h, C.byref(v))
         return v.value
+
+
+class RobustMPPIController(BatchedMPPIController):
+    """RobustMPPIController(model, cost, fb_controller, sampler, dt, max_iter, lambda, alpha, value_function_threshold,
+    num_timesteps, num_rollouts, init_control_traj, num_candidate_nominal_states, optimization_stride, ...)
+    (controllers/R-MPPI/robust_mppi_controller.cu:12-45): two sampling distributions of num_rollouts samples in the
+    reference's order, the nominal system (instance 0, from the nominal state) and the real system (instance 1, from
+    the state given to computeControl, its controls corrected by the DDP feedback against the nominal state), both
+    around the nominal sequence.  updateImportanceSamplingControl(state, stride) chooses the nominal state among
+    candidates between the nominal trajectory and the real state, slides the nominal sequence and computes the
+    feedback gains; call it before each computeControl.  getControlSeq is the real system's sequence and
+    getTargetStateSeq the nominal state trajectory, as in the reference; slideControlSequence and computeFeedback do
+    nothing (the importance-sampler update does both).  Built-in analytic models with Gaussian sampling."""
+
+    def __init__(self, model, cost, fb_controller, sampler, dt, max_iter, lambda_, alpha, value_function_threshold,
+                 num_timesteps, num_rollouts, init_control_traj=None, num_candidate_nominal_states=9,
+                 optimization_stride=1, num_eval_samples_per_candidate=64, stream=0, seed=0):
+        init = None
+        if init_control_traj is not None:
+            one = np.asarray(init_control_traj, dtype=np.float32).reshape(model.CONTROL_DIM, num_timesteps).T
+            init = np.concatenate([one.reshape(-1), one.reshape(-1)])
+        super().__init__(model, cost, sampler, [num_rollouts] * 2, [num_timesteps] * 2, dt=dt, max_iter=max_iter,
+                         lambda_=lambda_, alpha=alpha, seed=seed, init_control_traj=init, stream=stream)
+        cp = self.getParams()
+        cp.controller = A.CONTROLLER_RMPPI
+        cp.value_function_threshold = float(value_function_threshold)
+        cp.num_candidate_nominal_states = int(num_candidate_nominal_states)
+        cp.num_eval_samples_per_candidate = int(num_eval_samples_per_candidate)
+        self.setParams(cp)
+        self.optimization_stride_ = int(optimization_stride)
+        # the constructor turns the feedback on (robust_mppi_controller.cu:37-43)
+        self._attach_feedback(fb_controller)
+        self._fb_enabled = True
+
+    def updateImportanceSamplingControl(self, state, stride=1):
+        """RobustMPPIController::updateImportanceSamplingControl (robust_mppi_controller.cu:548-569)."""
+        x = np.ascontiguousarray(np.asarray(state, dtype=np.float32).reshape(-1))
+        if x.size != self.S:
+            raise ValueError(f"state must hold {self.S} floats")
+        A.call("mppi_rmppi_update_importance_sampler", self._h, _fptr(x), int(stride))
+
+    def computeControl(self, state, optimization_stride=1):
+        """RobustMPPIController::computeControl (robust_mppi_controller.cu:635-744); state: the real system's."""
+        x = np.ascontiguousarray(np.asarray(state, dtype=np.float32).reshape(-1))
+        if x.size != self.S:
+            raise ValueError(f"state must hold {self.S} floats")
+        A.call("mppi_compute_control", self._h, _fptr(x), int(optimization_stride))
+
+    def getControlSeq(self) -> np.ndarray:
+        """The real system's sequence (RobustMPPIController::getControlSeq, robust_mppi_controller.cuh:136-139)."""
+        return self.getControlSeqs()[1]
+
+    def getNominalControlSeq(self) -> np.ndarray:
+        return self.getControlSeqs()[0]
+
+    def setControlSeq(self, seq):
+        s = np.asarray(seq, np.float32)
+        self.setControlSeqs([s, s])
+
+    def getTargetStateSeq(self) -> np.ndarray:
+        """The nominal state trajectory (RobustMPPIController::getTargetStateSeq, :141-144)."""
+        return self.getTargetStateSeqs()[0]
+
+    def getActualStateSeq(self) -> np.ndarray:
+        """The real system's state trajectory under its sequence, from the state of the last computeControl."""
+        return self.getTargetStateSeqs()[1]
+
+    def _candidates(self):
+        cp = self.params_
+        N, J = int(cp.num_candidate_nominal_states), int(cp.num_eval_samples_per_candidate)
+        best, stride = C.c_int(), C.c_int()
+        states = np.zeros(N * self.S, np.float32)
+        strides = np.zeros(N, np.int32)
+        fe = np.zeros(N, np.float32)
+        costs = np.zeros(N * J, np.float32)
+        A.call("mppi_rmppi_get_candidates", self._h, C.byref(best), C.byref(stride), _fptr(states),
+               strides.ctypes.data_as(C.POINTER(C.c_int)), _fptr(fe), _fptr(costs))
+        return best.value, stride.value, states.reshape(N, self.S), strides, fe, costs
+
+    def getNominalState(self) -> np.ndarray:
+        """RobustMPPIController::getNominalState: the nominal system's initial state."""
+        return self.getTargetStateSeq()[:, 0].copy()
+
+    def getBestIndex(self) -> int:
+        return self._candidates()[0]
+
+    def getNominalStride(self) -> int:
+        return self._candidates()[1]
+
+    def getCandidateStates(self) -> np.ndarray:
+        return self._candidates()[2]
+
+    def getCandidateStrides(self) -> np.ndarray:
+        return self._candidates()[3]
+
+    def getCandidateFreeEnergy(self) -> np.ndarray:
+        return self._candidates()[4]
+
+    def getCandidateEvalCosts(self) -> np.ndarray:
+        return self._candidates()[5]
+
+    def getValueFunctionThreshold(self) -> float:
+        return float(self.params_.value_function_threshold)
+
+    def getNumCandidates(self) -> int:
+        return int(self.params_.num_candidate_nominal_states)
+
+    def getNumEvalSamplesPerCandidate(self) -> int:
+        return int(self.params_.num_eval_samples_per_candidate)
+
+    def getOptimizationStride(self) -> int:
+        return self.optimization_stride_

@@ -229,6 +229,9 @@ void mppi_default_controller_params(mppi_controller_params* p)
   p->tsallis_gamma = 0.0f;
   p->leash_active = 0;
   p->nominal_threshold = 20.0f;  // TubeMPPIParams (tube_mppi_controller.cuh:20)
+  p->value_function_threshold = 1000.0f;  // RobustMPPIParams (robust_mppi_controller.cuh:15-22)
+  p->num_candidate_nominal_states = 9;
+  p->num_eval_samples_per_candidate = 64;
 }
 
 void mppi_default_sampling_params(mppi_sampling_params* p)
@@ -337,6 +340,19 @@ mppi_status mppi_get_nominal_state_used(mppi_handle* h, int* used)
   HANDLE_OK(h);
   MG_CHECK(used, "used must not be NULL");
   return h->engine->nominal_state_used(used);
+}
+
+mppi_status mppi_rmppi_update_importance_sampler(mppi_handle* h, const float* state, int optimization_stride)
+{
+  HANDLE_OK(h);
+  return h->engine->rmppi_update_importance_sampler(state, optimization_stride);
+}
+mppi_status mppi_rmppi_get_candidates(mppi_handle* h, int* best_index, int* nominal_stride, float* candidate_states,
+                                      int* candidate_strides, float* candidate_free_energy, float* eval_costs)
+{
+  HANDLE_OK(h);
+  return h->engine->rmppi_get_candidates(best_index, nominal_stride, candidate_states, candidate_strides,
+                                         candidate_free_energy, eval_costs);
 }
 
 mppi_status mppi_set_feedback_params(mppi_handle* h, const float* Q, const float* Q_f, const float* R,

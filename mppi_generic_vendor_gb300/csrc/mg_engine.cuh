@@ -24,6 +24,7 @@
 #include "mg_mlp.cuh"
 #include "mg_plugin.cuh"
 #include "mg_ddp.h"
+#include "mg_rmppi.cuh"
 
 namespace mg
 {
@@ -100,6 +101,10 @@ public:
   virtual mppi_status get_feedback_gains(float* out) const = 0;
   virtual mppi_status feedback_control(const float* x, const float* goal, int t, float* u) const = 0;
   virtual mppi_status feedback_propagated_state_seq(float* out) = 0;
+  // the robust controller's importance sampler (RobustMPPIController::updateImportanceSamplingControl)
+  virtual mppi_status rmppi_update_importance_sampler(const float* x, int stride) = 0;
+  virtual mppi_status rmppi_get_candidates(int* best, int* nominal_stride, float* states, int* strides, float* fe,
+                                           float* eval_costs) const = 0;
 };
 
 // Factories, one per model translation unit.
@@ -209,6 +214,7 @@ public:
     MG_CHECK(x0 != nullptr, "x0 must not be NULL");
     MG_CHECK(stride >= 0, "optimization_stride must be >= 0");
     if (tube()) return compute_control_tube(x0, stride);
+    if (rmppi()) return compute_control_rmppi(x0, stride);
     MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
     MG_CHECK(!Model::kMlp || use_analytic_ || !mlp_host_.empty(), "this model needs surrogate weights (mppi_set_mlp)");
     for (int i = 0; i < I_ * S; ++i)
@@ -281,7 +287,15 @@ public:
       // step along the nominal sequence (Dynamics::step, no constraint), then both sequences slide
       if (nominal_init_) advance_nominal_state();
     }
-    for (int i = 0; i < I_; ++i)
+    // RobustMPPIController::slideControlSequence does nothing (robust_mppi_controller.cuh:186-190): the nominal
+    // sequence slides inside the importance-sampler update (mppi_rmppi_update_importance_sampler)
+    if (rmppi()) return MPPI_OK;
+    for (int i = 0; i < I_; ++i) slide_one(i, steps);
+    return MPPI_OK;
+  }
+  // Controller::saveControlHistoryHelper + slideControlSequenceHelper (controller.cuh:609-636) for instance i
+  void slide_one(int i, int steps)
+  {
     {
       float* u = control_.data() + t_off_[i];
       const int T = T_[i];
@@ -314,7 +328,6 @@ public:
         }
       }
     }
-    return MPPI_OK;
   }
   mppi_status get_state_seq(float* out) override
   {
@@ -524,7 +537,14 @@ public:
     MG_CHECK(cp, "controller params must not be NULL");
     MG_TRY(check_controller(*cp));
     const bool tile_reduce_before = tile_reduce_active();
+    const bool was_rmppi = rmppi();
     cp_ = *cp;
+    if (rmppi() && !was_rmppi)
+    {
+      // RobustMPPIController's constructor turns its feedback on (robust_mppi_controller.cu:37-43)
+      fb_enabled_ = true;
+      std::fill(fb_gains_.begin(), fb_gains_.end(), 0.0f);
+    }
     if (tile_reduce_active() != tile_reduce_before)
     {
       // the weight path changed: mode 4 needs the tile reduction, and the rollout's shared memory follows it
@@ -541,12 +561,30 @@ public:
     MG_CHECK(cp.lambda > 0.0f && std::isfinite(cp.lambda), "lambda must be positive");
     MG_CHECK(std::isfinite(cp.dt), "dt must be finite");
     MG_CHECK(cp.controller == MPPI_CONTROLLER_VANILLA || cp.controller == MPPI_CONTROLLER_COLORED ||
-                 cp.controller == MPPI_CONTROLLER_TUBE,
-             "controller must be MPPI_CONTROLLER_VANILLA (0), MPPI_CONTROLLER_COLORED (1) or MPPI_CONTROLLER_TUBE (2)");
+                 cp.controller == MPPI_CONTROLLER_TUBE || cp.controller == MPPI_CONTROLLER_RMPPI,
+             "controller must be MPPI_CONTROLLER_VANILLA (0), MPPI_CONTROLLER_COLORED (1), MPPI_CONTROLLER_TUBE (2) "
+             "or MPPI_CONTROLLER_RMPPI (3)");
     MG_CHECK(std::isfinite(cp.nominal_threshold), "nominal_threshold must be finite");
     if (cp.controller == MPPI_CONTROLLER_TUBE && !K_.empty())
       MG_CHECK(I_ == 2 && K_[0] == K_[1] && T_[0] == T_[1],
                "a Tube-MPPI handle holds two instances of equal num_rollouts and num_timesteps (actual, nominal)");
+    if (cp.controller == MPPI_CONTROLLER_RMPPI)
+    {
+      MG_CHECK(!Model::kMlp && !Model::kPlugin, "R-MPPI runs the built-in analytic models");
+      MG_CHECK(std::isfinite(cp.value_function_threshold), "value_function_threshold must be finite");
+      // RobustMPPIController::updateNumCandidates (robust_mppi_controller.cu:424-457)
+      MG_CHECK(cp.num_candidate_nominal_states >= 3 && cp.num_candidate_nominal_states % 2 == 1,
+               "num_candidate_nominal_states must be odd and >= 3 (got %d)", cp.num_candidate_nominal_states);
+      MG_CHECK(cp.num_eval_samples_per_candidate >= 1, "num_eval_samples_per_candidate must be >= 1");
+      if (!K_.empty())
+      {
+        MG_CHECK(I_ == 2 && K_[0] == K_[1] && T_[0] == T_[1] && T_[0] >= 2,
+                 "an R-MPPI handle holds two instances of equal num_rollouts and num_timesteps >= 2 (nominal, real)");
+        MG_CHECK((long long)cp.num_candidate_nominal_states * cp.num_eval_samples_per_candidate <= K_[0],
+                 "num_candidate_nominal_states x num_eval_samples_per_candidate must not exceed num_rollouts");
+        MG_CHECK(sp_.kind == MPPI_SAMPLER_GAUSSIAN, "R-MPPI samples Gaussian noise");
+      }
+    }
     MG_CHECK(std::isfinite(cp.tsallis_gamma) && std::isfinite(cp.tsallis_r), "tsallis_gamma and tsallis_r must be "
              "finite");
     MG_CHECK(cp.controller != MPPI_CONTROLLER_COLORED || cp.tsallis_gamma == 0.0f || cp.tsallis_r != 1.0f,
@@ -772,7 +810,8 @@ public:
 
   // ------------------------------------------------------------------------------------------ DDP feedback
   // The instance whose nominal trajectory the feedback tracks: Tube-MPPI's nominal system (its getControlSeq and
-  // getTargetStateSeq, tube_mppi_controller.cuh:61-72), else the handle's single controller.
+  // getTargetStateSeq, tube_mppi_controller.cuh:61-72), R-MPPI's nominal system (instance 0), else the handle's single
+  // controller.
   int fb_instance() const { return tube() ? 1 : 0; }
   size_t state_off(int i) const
   {
@@ -830,7 +869,8 @@ public:
 
   mppi_status feedback_shape_ok() const
   {
-    MG_CHECK(I_ == 1 || tube(), "the feedback controller serves a single controller (or Tube-MPPI's nominal system)");
+    MG_CHECK(I_ == 1 || tube() || rmppi(),
+             "the feedback controller serves a single controller (or Tube-MPPI's / R-MPPI's nominal system)");
     return MPPI_OK;
   }
 
@@ -871,6 +911,13 @@ public:
   {
     MG_CHECK(x0, "state must not be NULL");
     MG_TRY(feedback_shape_ok());
+    // RobustMPPIController::computeFeedback does nothing (robust_mppi_controller.cuh:192-196): its gains come with the
+    // importance-sampler update
+    if (rmppi()) return MPPI_OK;
+    return run_feedback(x0);
+  }
+  mppi_status run_feedback(const float* x0)
+  {
     if (!fb_enabled_) return MPPI_OK;
     const int i = fb_instance();
     MG_CHECK(T_[i] >= 2, "the feedback controller needs at least two time steps");
@@ -926,12 +973,249 @@ public:
     return MPPI_OK;
   }
 
+  // ------------------------------------------------------------------------------------------------ R-MPPI
+  bool rmppi() const { return cp_.controller == MPPI_CONTROLLER_RMPPI; }
+
+  // RobustMPPIController::computeLineSearchWeights (robust_mppi_controller.cu:480-498): column i of the 3 x N weights
+  // (row-major here) mixes the nominal trajectory's first state, its second state and the real state
+  void line_search_weights(std::vector<float>& w) const
+  {
+    const int N = cp_.num_candidate_nominal_states, h = N / 2;
+    w.assign((size_t)3 * N, 0.0f);
+    for (int i = 0; i < h + 1; ++i)
+    {
+      w[i] = 1 - i / float(h);
+      w[N + i] = i / float(h);
+      w[2 * N + i] = 0.0f;
+    }
+    for (int i = 1; i < h + 1; ++i)
+    {
+      w[h + i] = 0.0f;
+      w[N + h + i] = 1 - i / float(h);
+      w[2 * N + h + i] = i / float(h);
+    }
+  }
+
+  mppi_status launch_rmppi_rollout()
+  {
+    RmppiArgs<Model> a{};
+    a.inst = inst_d_.p;
+    a.samples = samples_d_.p;
+    a.mean = mean_d_.p;
+    a.x0 = x0_d_.p;
+    a.gains = fb_gains_d_.p;
+    a.costs = costs_d_.p;
+    a.baseline_bits = baseline_bits_d_.p;
+    a.dyn = dyn_d_.p;
+    a.cost = cost_d_.p;
+    a.aux = aux_;
+    a.sh = make_sample_shared(sp_, cc_);  // the real constraints (the samples came unconstrained)
+    a.lambda = cp_.lambda;
+    a.alpha = cp_.alpha;
+    a.dt = cp_.dt;
+    a.value_threshold = cp_.value_function_threshold;
+    a.use_likelihood = 0;
+    for (int c = 0; c < C; ++c)
+      if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
+    rmppi_rollout_kernel<Model><<<(K_[0] + 127) / 128, 128, 0, stream_>>>(a);
+    MG_CUDA(cudaGetLastError());
+    return MPPI_OK;
+  }
+
+  // RobustMPPIController::computeControl (robust_mppi_controller.cu:635-744): per iteration one graph launch of the
+  // device work of both distributions (samples around the nominal sequence, the coupled rollout, weights and update);
+  // the iteration's nominal sequence is the next iteration's importance sampler.  Both sequences are smoothed at the
+  // end and the nominal state trajectory is recomputed.  x is the real system's state.
+  mppi_status compute_control_rmppi(const float* x, int stride)
+  {
+    if constexpr (Model::kPlugin || Model::kMlp)
+    {
+      set_error("R-MPPI runs the built-in analytic models");
+      return MPPI_EUNSUPPORTED;
+    }
+    for (int i = 0; i < S; ++i)
+      if (!std::isfinite(x[i]))
+      {
+        set_error("initial state has a non-finite entry at index %d", i);
+        return MPPI_ENAN;
+      }
+    MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
+    if (!nominal_init_) nominal_x0_.assign(S, 0.0f);  // nominal_state_ before the first importance-sampler update
+    if (!fb_gains_d_.p) MG_TRY(fb_gains_d_.alloc(fb_gains_.size()));
+    MG_CUDA(cudaMemcpyAsync(fb_gains_d_.p, fb_gains_.data(), sizeof(float) * fb_gains_.size(), cudaMemcpyHostToDevice,
+                            stream_));
+    for (int i = 0; i < I_; ++i) prev_baseline_[i] = baseline_norm_[2 * i];
+    const size_t tc = (size_t)T_[0] * C;
+    for (int it = 0; it < cp_.num_iters; ++it)
+    {
+      memcpy(x0_h_.p, nominal_x0_.data(), sizeof(float) * S);
+      memcpy(x0_h_.p + S, x, sizeof(float) * S);
+      memcpy(mean_h_.p + t_off_[0], control_.data() + t_off_[0], sizeof(float) * tc);
+      memcpy(mean_h_.p + t_off_[1], control_.data() + t_off_[0], sizeof(float) * tc);
+      if (graph_mode_)
+      {
+        cudaGraphExec_t exec = nullptr;
+        MG_TRY(get_graph(stride, &exec));
+        MG_CUDA(cudaGraphLaunch(exec, stream_));
+      }
+      else
+      {
+        MG_TRY(enqueue_solve(stride));
+      }
+      MG_CUDA(cudaStreamSynchronize(stream_));
+      memcpy(control_.data(), out_mean_h_.p, sizeof(float) * control_.size());
+      memcpy(baseline_norm_.data(), out_bn_h_.p, sizeof(float) * 2 * I_);
+      memcpy(stats_.data(), out_stats_h_.p, sizeof(double) * 3 * I_);
+    }
+    smooth_host(control_.data() + t_off_[0], T_[0]);
+    smooth_host(control_.data() + t_off_[1], T_[1]);
+    state_trajectory(0, nominal_x0_.data(), control_.data() + t_off_[0], state_seq_.data());
+    state_trajectory(1, x, control_.data() + t_off_[1], state_seq_.data() + (size_t)T_[0] * S);
+    traj_dirty_ = false;
+    for (int i = 0; i < I_; ++i)
+      if (!std::isfinite(baseline_norm_[2 * i]) || !(stats_[3 * i] > 0.0))
+      {
+        set_error("a sampled cost or the normaliser is not finite (NaN state or noise?)");
+        return MPPI_ENAN;
+      }
+    return MPPI_OK;
+  }
+
+  // RobustMPPIController::updateImportanceSamplingControl (robust_mppi_controller.cu:548-627)
+  mppi_status rmppi_update_importance_sampler(const float* x, int stride) override
+  {
+    MG_CHECK(rmppi(), "mppi_rmppi_update_importance_sampler needs an R-MPPI handle");
+    MG_CHECK(x, "state must not be NULL");
+    MG_CHECK(stride >= 0, "optimization_stride must be >= 0");
+    for (int i = 0; i < S; ++i)
+      if (!std::isfinite(x[i]))
+      {
+        set_error("state has a non-finite entry at index %d", i);
+        return MPPI_ENAN;
+      }
+    if constexpr (Model::kPlugin || Model::kMlp)
+    {
+      set_error("R-MPPI runs the built-in analytic models");
+      return MPPI_EUNSUPPORTED;
+    }
+    else
+    {
+      MG_CHECK(!Model::kNeedsCostmap || aux_.map.data != nullptr, "this model needs a costmap (mppi_set_costmap)");
+      const int N = cp_.num_candidate_nominal_states, J = cp_.num_eval_samples_per_candidate;
+      if (!nominal_init_)
+      {
+        // computeNominalStateAndStride (:571-578): the first state is the nominal state
+        nominal_x0_.assign(x, x + S);
+        nominal_init_ = true;
+        rm_nominal_stride_ = 0;
+      }
+      else
+      {
+        // candidates on the lines nominal x_0 -> nominal x_1 -> real state (getInitNominalStateCandidates, :351-363)
+        // with their strides round((0, stride, stride) . w_i) (computeImportanceSamplerStride, :500-511)
+        const float* p0 = state_seq_.data();
+        const float* p1 = p0 + S;
+        std::vector<float> w;
+        line_search_weights(w);
+        rm_cand_.assign((size_t)N * S, 0.0f);
+        rm_strides_.assign(N, 0);
+        const float sf = (float)stride;
+        for (int i = 0; i < N; ++i)
+        {
+          for (int s = 0; s < S; ++s) rm_cand_[(size_t)i * S + s] = (p0[s] * w[i] + p1[s] * w[N + i]) + x[s] * w[2 * N + i];
+          rm_strides_[i] = (int)std::round((0.0f * w[i] + sf * w[N + i]) + sf * w[2 * N + i]);
+        }
+        // the nominal distribution's samples around the nominal sequence (copyNominalControlToDevice,
+        // generateSamples), then initEvalKernel
+        const size_t tc = (size_t)T_[0] * C;
+        memcpy(mean_h_.p + t_off_[0], control_.data() + t_off_[0], sizeof(float) * tc);
+        memcpy(mean_h_.p + t_off_[1], control_.data() + t_off_[0], sizeof(float) * tc);
+        MG_CUDA(cudaMemcpyAsync(mean_d_.p, mean_h_.p, sizeof(float) * control_.size(), cudaMemcpyHostToDevice, stream_));
+        if (rm_cand_d_.n < (size_t)N * S) MG_TRY(rm_cand_d_.alloc((size_t)N * S));
+        if (rm_strides_d_.n < (size_t)N) MG_TRY(rm_strides_d_.alloc(N));
+        if (rm_eval_d_.n < (size_t)N * J) MG_TRY(rm_eval_d_.alloc((size_t)N * J));
+        MG_CUDA(cudaMemcpyAsync(rm_cand_d_.p, rm_cand_.data(), sizeof(float) * N * S, cudaMemcpyHostToDevice, stream_));
+        MG_CUDA(cudaMemcpyAsync(rm_strides_d_.p, rm_strides_.data(), sizeof(int) * N, cudaMemcpyHostToDevice, stream_));
+        MG_TRY(launch_sampler(stride, 0));
+        RmppiEvalArgs<Model> e{};
+        e.d = inst_h_[0];
+        e.samples = samples_d_.p;
+        e.mean = mean_d_.p;
+        e.cand_states = rm_cand_d_.p;
+        e.cand_strides = rm_strides_d_.p;
+        e.num_cand = N;
+        e.per_cand = J;
+        e.costs = rm_eval_d_.p;
+        e.dyn = dyn_d_.p;
+        e.cost = cost_d_.p;
+        e.aux = aux_;
+        e.sh = make_sample_shared(sp_, cc_);
+        e.lambda = cp_.lambda;
+        e.alpha = cp_.alpha;
+        e.dt = cp_.dt;
+        e.use_likelihood = 0;
+        for (int c = 0; c < C; ++c)
+          if (sp_.control_cost_coeff[c] != 0.0f) e.use_likelihood = 1;
+        rmppi_eval_kernel<Model><<<(N * J + 63) / 64, 64, 0, stream_>>>(e);
+        MG_CUDA(cudaGetLastError());
+        bump_u32_kernel<<<1, 1, 0, stream_>>>(counters_d_.p + 3);  // the solve draws fresh noise
+        MG_CUDA(cudaGetLastError());
+        rm_eval_.assign((size_t)N * J, 0.0f);
+        MG_CUDA(cudaMemcpyAsync(rm_eval_.data(), rm_eval_d_.p, sizeof(float) * N * J, cudaMemcpyDeviceToHost, stream_));
+        MG_CUDA(cudaStreamSynchronize(stream_));
+        // computeBestIndex (:527-546): the free energy of each candidate's samples against the smallest evaluated
+        // cost; the last candidate below the threshold wins (the previous choice stays when none is)
+        float baseline = rm_eval_[0];
+        for (int g = 1; g < N * J; ++g)
+          if (rm_eval_[g] < baseline) baseline = rm_eval_[g];
+        rm_fe_.assign(N, 0.0f);
+        for (int i = 0; i < N; ++i)
+        {
+          float fe = 0.0f;
+          for (int j = 0; j < J; ++j)
+            fe += expf((float)(-1.0 / (double)cp_.lambda * (double)(rm_eval_[(size_t)i * J + j] - baseline)));
+          fe = (float)((double)fe / (1.0 * J));
+          fe = -cp_.lambda * logf(fe) + baseline;
+          rm_fe_[i] = fe;
+          if (fe < cp_.value_function_threshold) rm_best_ = i;
+        }
+        nominal_used_ = rm_best_;
+        rm_nominal_stride_ = rm_strides_[rm_best_];
+        nominal_x0_.assign(rm_cand_.begin() + (size_t)rm_best_ * S, rm_cand_.begin() + (size_t)(rm_best_ + 1) * S);
+      }
+      // the nominal sequence slides by the nominal stride; its state trajectory follows; the feedback gains are
+      // computed from the real state around it (computeNominalFeedbackGains, :629-633)
+      slide_one(0, rm_nominal_stride_);
+      state_trajectory(0, nominal_x0_.data(), control_.data() + t_off_[0], state_seq_.data());
+      traj_dirty_ = false;
+      MG_TRY(run_feedback(x));
+      return MPPI_OK;
+    }
+  }
+
+  mppi_status rmppi_get_candidates(int* best, int* nominal_stride, float* states, int* strides, float* fe,
+                                   float* eval_costs) const override
+  {
+    MG_CHECK(rmppi(), "mppi_rmppi_get_candidates needs an R-MPPI handle");
+    if (best) *best = rm_best_;
+    if (nominal_stride) *nominal_stride = rm_nominal_stride_;
+    const int N = cp_.num_candidate_nominal_states, J = cp_.num_eval_samples_per_candidate;
+    auto copy = [](const auto& v, auto* dst, size_t n) {
+      for (size_t e = 0; e < n; ++e) dst[e] = e < v.size() ? v[e] : 0;
+    };
+    if (states) copy(rm_cand_, states, (size_t)N * S);
+    if (strides) copy(rm_strides_, strides, (size_t)N);
+    if (fe) copy(rm_fe_, fe, (size_t)N);
+    if (eval_costs) copy(rm_eval_, eval_costs, (size_t)N * J);
+    return MPPI_OK;
+  }
+
   // ------------------------------------------------------------------------------------------------ Tube-MPPI
   bool tube() const { return cp_.controller == MPPI_CONTROLLER_TUBE; }
 
   mppi_status nominal_state_used(int* used) override
   {
-    MG_CHECK(tube(), "only a Tube-MPPI handle keeps a nominal system");
+    MG_CHECK(tube() || rmppi(), "only a Tube-MPPI or R-MPPI handle keeps a nominal system");
     *used = nominal_used_;
     return MPPI_OK;
   }
@@ -1450,11 +1734,11 @@ private:
   // Work lists: rollout tiles ordered by decreasing horizon (the cost of a tile is proportional to T), sampler items,
   // and weight/update chunks with the offsets of their partial rows.
   // Which noise each instance draws (InstDesc::noise_*): its own, except that the second distribution of a Tube-MPPI
-  // handle draws the first one's when use_same_noise_for_all_distributions is set (generateSamples copies one draw to
-  // every distribution, gaussian.cu:378-390).
+  // or R-MPPI handle draws the first one's when use_same_noise_for_all_distributions is set (generateSamples copies
+  // one draw to every distribution, gaussian.cu:378-390).
   void set_noise_sources(std::vector<InstDesc>& inst) const
   {
-    const bool shared = tube() && sp_.use_same_noise_for_all_distributions != 0;
+    const bool shared = (tube() || rmppi()) && sp_.use_same_noise_for_all_distributions != 0;
     for (int i = 0; i < I_; ++i)
     {
       const int src = shared ? 0 : i;
@@ -1792,7 +2076,7 @@ private:
   // Gaussian sampling can run inside the rollout kernels (every row holds whole control quads) ...
   bool fusable() const { return !Model::kPlugin && sp_.kind == MPPI_SAMPLER_GAUSSIAN && (4 % C) == 0 && use_bulk_; }
   // ... and does, unless rollout mode 3 asks for the separate sampler kernel.
-  bool fused() const { return fusable() && rollout_mode_ != 3; }
+  bool fused() const { return fusable() && rollout_mode_ != 3 && !rmppi(); }
 
   FusedNoise fused_noise_args(int stride, int iter) const
   {
@@ -1856,6 +2140,8 @@ private:
 
   mppi_status launch_rollout(int stride, int iter)
   {
+    if constexpr (!Model::kPlugin && !Model::kMlp)
+      if (rmppi()) return launch_rmppi_rollout();
     if constexpr (Model::kPlugin)
     {
       RolloutArgs<Model> a = base_rollout_args();
@@ -1979,7 +2265,7 @@ private:
   // rewrites costs after the rollout) or the weights are Tsallis weights (not a product of a per-tile factor and a
   // tile-local weight, so they need the instance's baseline first); then weights_update_kernel reads the samples
   // again.
-  bool tile_reduce_active() const { return !(Model::kMlp && !use_analytic_) && !tsallis(); }
+  bool tile_reduce_active() const { return !(Model::kMlp && !use_analytic_) && !tsallis() && !rmppi(); }
   // ColoredMPPIController::computeControl's weight choice (colored_mppi_controller.cu:197-207): Tsallis weights when
   // gamma and r are both non-zero, else the exponential transform.
   bool tsallis() const
@@ -1989,10 +2275,11 @@ private:
   SampleShared sample_shared() const
   {
     SampleShared sh = make_sample_shared(sp_, cc_, cp_.controller == MPPI_CONTROLLER_COLORED ? 1 : 0);
-    if constexpr (Model::kOwnConstraints)
+    if (Model::kOwnConstraints || rmppi())
     {
-      // the plugin's enforceConstraints replaces the deadband + clamp: samples and the smoothed mean leave the GPU
-      // unconstrained (an infinite range with no deadband leaves every value as it is)
+      // the plugin's enforceConstraints replaces the deadband + clamp, and R-MPPI constrains each step's control
+      // (with the feedback added) inside its rollout: samples and the smoothed mean leave the GPU unconstrained (an
+      // infinite range with no deadband leaves every value as it is)
       for (int c = 0; c < kMaxC; ++c)
       {
         sh.lower[c] = -INFINITY;
@@ -2013,7 +2300,7 @@ private:
       weights_stale_ = true;
       return MPPI_OK;
     }
-    const bool finish = !tube() && iter == cp_.num_iters - 1;
+    const bool finish = !tube() && !rmppi() && iter == cp_.num_iters - 1;
     const size_t fin_floats = finish ? (size_t)(max_t_ + 4) * C : 0;
     if (tile_reduce_active())
     {
@@ -2085,7 +2372,7 @@ private:
     // the smoothing + constraints of the new nominal sequences (the host post-processing of computeControl) run in
     // the last iteration's combine: the fused rollout's finalizing CTAs, tile_finalize_kernel or the weights pass;
     // Tube-MPPI smooths its nominal sequence on the host
-    for (int it = 0; it < (tube() ? 1 : cp_.num_iters); ++it)
+    for (int it = 0; it < (tube() || rmppi() ? 1 : cp_.num_iters); ++it)
     {
       if (!fused()) MG_TRY(launch_sampler(stride, it));
       MG_TRY(launch_rollout(stride, it));
@@ -2101,7 +2388,7 @@ private:
     (void)tc;
     MG_CUDA(cudaMemcpyAsync(io_d_.p, io_in_h_.p, io_in_bytes_, cudaMemcpyHostToDevice, stream_));
     // the CTAs that finish the solve write the results to the pinned host block themselves
-    direct_out_ = !tube();
+    direct_out_ = !tube() && !rmppi();
     const mppi_status st = enqueue_kernels(stride);
     const bool direct = direct_out_;
     direct_out_ = false;
@@ -2222,6 +2509,13 @@ private:
   bool fb_enabled_ = false;                // Controller::enable_feedback_
   DdpWeights fb_w_;                        // DDPParams: identities and one iteration until set
   std::vector<float> fb_gains_, fb_prop_;  // gains of the feedback instance; feedback-propagated states
+  DevBuf<float> fb_gains_d_;               // the gains for R-MPPI's rollout
+  // R-MPPI's importance sampler: the last candidate evaluation and the chosen candidate
+  std::vector<float> rm_cand_, rm_fe_, rm_eval_;
+  std::vector<int> rm_strides_;
+  DevBuf<float> rm_cand_d_, rm_eval_d_;
+  DevBuf<int> rm_strides_d_;
+  int rm_best_ = 0, rm_nominal_stride_ = 0;
 
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;

@@ -1,0 +1,194 @@
+// mg_rmppi.cuh — the two kernels of the robust controller (R-MPPI):
+//  * rmppi_rollout_kernel: rolloutRMPPIKernel (rmppi_kernels.cu:666-861).  The reference runs the nominal and the real
+//    system of a sample as two threads (threadIdx.z) sharing the nominal state through shared memory; here one thread
+//    runs both in lockstep, so the real system's feedback K_t (x_real - x_nominal) sees the nominal state of the same
+//    step in registers.  Both controls pass through the constraints (deadband, clamp) every step and are written back
+//    as the samples the update averages.  Costs (running cost on the stepped state, likelihood-ratio term, terminal
+//    cost, all divided by T): the real system pays running + likelihood; the nominal one
+//        0.5 J_nom + 0.5 max(min(J_real_fb, threshold), J_nom) + likelihood_nom,
+//    with J_real_fb the real system's running cost plus the feedback cost (computeFeedbackCost, gaussian.cu:577-630).
+//    The reference's device feedback (DeviceDDPImpl::k, ddp.cu:11-44) overwrites instead of accumulating for an even
+//    control dimension; the kernel applies the whole product K_t e, as the reference's host DDPFeedback::k_ does.
+//  * rmppi_eval_kernel: initEvalKernel (rmppi_kernels.cu:231-357): num_candidates x samples_per_candidate rollouts,
+//    candidate c from its state with the samples of the nominal distribution read at t + stride_c (held at T-1).
+// One thread per sample, no shared memory and no waits.
+#pragma once
+
+#include "mg_kernels.cuh"
+#include "mg_plugin.cuh"
+
+namespace mg
+{
+
+// One increment of a device counter (the Philox noise counter after the candidate evaluation's sampling).
+static __global__ void bump_u32_kernel(unsigned int* p) { *p += 1u; }
+
+template <class Model>
+struct RmppiArgs
+{
+  const InstDesc* inst;  // [0] nominal distribution, [1] real distribution
+  float* samples;        // unconstrained samples in, the constrained controls (real: with feedback) out
+  const float* mean;     // both distributions' means (the importance sampler)
+  const float* x0;       // [nominal state | real state]
+  const float* gains;    // per step a CONTROL_DIM x STATE_DIM gain, column-major
+  float* costs;
+  unsigned int* baseline_bits;  // per distribution: ordered-int minimum of its costs
+  const typename Model::DynParams* dyn;
+  const typename Model::CostParams* cost;
+  ModelAux aux;
+  SampleShared sh;  // the control constraints, standard deviations, cost coefficients and pure-noise share
+  float lambda, alpha, dt, value_threshold;
+  int use_likelihood;
+};
+
+// GaussianDistributionImpl::computeFeedbackCost (gaussian.cu:577-630): 0.5 lambda (1 - alpha) sum_i coeff_i fb_i^2 /
+// sd_i^2, the terms added in control order.
+template <int C, class Args>
+__device__ __forceinline__ float feedback_cost(const Args& a, const float* fb)
+{
+  float c = 0.0f;
+#pragma unroll
+  for (int i = 0; i < C; ++i) c += a.sh.control_cost_coeff[i] * (fb[i] * fb[i]) / (a.sh.std_dev[i] * a.sh.std_dev[i]);
+  return 0.5f * a.lambda * (1.0f - a.alpha) * c;
+}
+
+template <class Model>
+__global__ void __launch_bounds__(128) rmppi_rollout_kernel(const __grid_constant__ RmppiArgs<Model> a)
+{
+  constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM;
+  const InstDesc dn = a.inst[0], dr = a.inst[1];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= dn.K) return;
+  const int T = dn.T;
+  const typename Model::DynParams& dp = a.dyn[0];
+  const typename Model::CostParams& cp = a.cost[0];
+  float xn[S], xr[S];
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+  {
+    xn[s] = a.x0[s];
+    xr[s] = a.x0[S + s];
+  }
+  float* un_row = a.samples + dn.u_off + (long long)k * T * C;
+  float* ur_row = a.samples + dr.u_off + (long long)k * T * C;
+  float run_n = 0.0f, lik_n = 0.0f, run_r = 0.0f, extra_r = 0.0f;
+  for (int t = 0; t < T; ++t)
+  {
+    float un[C], ur[C], fb[C], xn2[S], xr2[S];
+    // the nominal system takes its sample, constrained (no feedback on the nominal system)
+#pragma unroll
+    for (int c = 0; c < C; ++c)
+    {
+      un[c] = enforce_constraint(un_row[t * C + c], a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c], a.sh.zero[c]);
+      un_row[t * C + c] = un[c];
+    }
+    // the real system adds the feedback against the nominal state of this step
+    const float* K = a.gains + (size_t)t * C * S;
+#pragma unroll
+    for (int r = 0; r < C; ++r)
+    {
+      float acc = 0.0f;
+#pragma unroll
+      for (int c = 0; c < S; ++c) acc += K[r + c * C] * (xr[c] - xn[c]);
+      fb[r] = acc;
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c)
+    {
+      ur[c] = enforce_constraint(ur_row[t * C + c] + fb[c], a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c],
+                                 a.sh.zero[c]);
+      ur_row[t * C + c] = ur[c];
+    }
+    euler_step<Model>(dp, xn, un, xn2, a.dt);
+    euler_step<Model>(dp, xr, ur, xr2, a.dt);
+    const float cn = Model::computeStateCost(cp, a.aux, xn2, t) + Model::computeControlCost(cp, un, t);
+    const float cr = Model::computeStateCost(cp, a.aux, xr2, t) + Model::computeControlCost(cp, ur, t);
+    run_n += cn;
+    if (a.use_likelihood)
+    {
+      lik_n += likelihood_ratio_cost<C>(a, dn, k, un, t);
+      run_r += cr + likelihood_ratio_cost<C>(a, dr, k, ur, t);
+    }
+    else
+    {
+      run_r += cr;
+    }
+    extra_r += cr + feedback_cost<C>(a, fb);
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+      xn[s] = xn2[s];
+      xr[s] = xr2[s];
+    }
+  }
+  run_n += Model::terminalCost(cp, a.aux, xn);
+  const float term_r = Model::terminalCost(cp, a.aux, xr);
+  run_r += term_r;
+  extra_r += term_r;
+  const float Tf = (float)T;
+  run_n /= Tf;
+  lik_n /= Tf;
+  run_r /= Tf;
+  extra_r /= Tf;
+  // 0.5 J_nom + 0.5 max(min(J_real_fb, threshold), J_nom), formed in double as the reference's double literals make it
+  float cost_n = (float)(0.5 * (double)run_n + 0.5 * (double)fmaxf(fminf(extra_r, a.value_threshold), run_n));
+  cost_n += lik_n;
+  a.costs[dn.k_off + k] = cost_n;
+  a.costs[dr.k_off + k] = run_r;
+  atomicMin(&a.baseline_bits[0], float_to_ordered(cost_n));
+  atomicMin(&a.baseline_bits[1], float_to_ordered(run_r));
+}
+
+template <class Model>
+struct RmppiEvalArgs
+{
+  InstDesc d;              // the nominal distribution: its samples, mean and K
+  const float* samples;
+  const float* mean;
+  const float* cand_states;  // [num_cand][STATE_DIM]
+  const int* cand_strides;   // [num_cand]
+  int num_cand, per_cand;
+  float* costs;              // [num_cand * per_cand]
+  const typename Model::DynParams* dyn;
+  const typename Model::CostParams* cost;
+  ModelAux aux;
+  SampleShared sh;
+  float lambda, alpha, dt;
+  int use_likelihood;
+};
+
+template <class Model>
+__global__ void __launch_bounds__(64) rmppi_eval_kernel(const __grid_constant__ RmppiEvalArgs<Model> a)
+{
+  constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= a.num_cand * a.per_cand) return;
+  const int cand = g / a.per_cand, j = g - cand * a.per_cand;
+  const int T = a.d.T, stride = a.cand_strides[cand];
+  const typename Model::DynParams& dp = a.dyn[0];
+  const typename Model::CostParams& cp = a.cost[0];
+  const float* row = a.samples + a.d.u_off + (long long)j * T * C;
+  float x[S];
+#pragma unroll
+  for (int s = 0; s < S; ++s) x[s] = a.cand_states[cand * S + s];
+  float running = 0.0f;
+  for (int t = 0; t < T; ++t)
+  {
+    const int tc = min(t + stride, T - 1);
+    float u[C], xn[S];
+#pragma unroll
+    for (int c = 0; c < C; ++c)
+      u[c] = enforce_constraint(row[tc * C + c], a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c], a.sh.zero[c]);
+    euler_step<Model>(dp, x, u, xn, a.dt);
+    float c = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
+    // the likelihood term of sample g (its index among the evaluation rollouts) against the mean at step t
+    if (a.use_likelihood) c += likelihood_ratio_cost<C>(a, a.d, g, u, t);
+    running += c;
+#pragma unroll
+    for (int s = 0; s < S; ++s) x[s] = xn[s];
+  }
+  const float Tf = (float)T;
+  a.costs[g] = running / Tf + Model::terminalCost(cp, a.aux, x) / Tf;
+}
+
+}  // namespace mg

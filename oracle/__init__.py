@@ -43,6 +43,12 @@ _SIGS = [
     ("orc_colored_scales", None, [C.c_int, C.c_int, _FP, C.c_float, _FP, _FP]),
     ("orc_colored_noise", None, [_FP, C.c_int, C.c_int, C.c_int, _FP, C.c_float, C.c_float, C.c_int, _FP,
                                  C.c_int]),
+    ("orc_rmppi_rollout", C.c_int, [C.c_int, _P, _P, _FP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, _FP,
+                                    _FP, _FP, _FP, _FP, _FP, _FP, _P, _P, C.c_float, C.c_float, C.c_float, C.c_int,
+                                    C.c_int, C.c_float, _FP, _FP, C.c_int]),
+    ("orc_rmppi_eval", C.c_int, [C.c_int, _P, _P, _FP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, _FP,
+                                 C.POINTER(C.c_int), C.c_int, C.c_int, _FP, _FP, _P, _P, C.c_float, C.c_float, C.c_int,
+                                 C.c_int, C.c_float, _FP]),
     ("orc_compute_control", C.c_int, [C.c_int, _P, _P, _FP, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, _P,
                                       _P, _P, C.c_int, C.c_int, _FP, _FP, C.c_int, C.c_int, _FP, _FP, _FP, _FP,
                                       _FP, _DP, _FP, C.c_int]),
@@ -338,6 +344,49 @@ def tube_compute_control(model, dyn, cost, cparams, sampling, constraints, K, T,
     return dict(control=ctl.reshape(2, T, Cdim), nominal_x0=xn, costs=costs.reshape(2, K), weights=w.reshape(2, K),
                 samples=samples.reshape(2, K * T * Cdim), baselines=b, normalizers=n, nominal_used=used.value,
                 state_seq=states.reshape(2, T, S))
+
+
+def _map_args(costmap):
+    if costmap is not None:
+        data, res, (ox, oy) = costmap
+        data = _f32(data)
+        return data, (_fp(data), data.shape[1], data.shape[0], res, ox, oy)
+    return None, (None, 0, 0, 1.0, 0.0, 0.0)
+
+
+def rmppi_rollout(model, dyn, cost, x0_nom, x0_real, samples_nom, samples_real, mean_nom, mean_real, gains, sampling,
+                  constraints, lambda_, alpha, threshold, K, T, dt, costmap=None, threads=None):
+    """rolloutRMPPIKernel restated: returns (nominal costs, real costs, constrained nominal samples, constrained real
+    samples with feedback), all float32; gains are [T][C*S] (column-major per step)."""
+    un = _f32(samples_nom).copy().reshape(-1)
+    ur = _f32(samples_real).copy().reshape(-1)
+    cn = np.empty(K, np.float32)
+    cr = np.empty(K, np.float32)
+    keep, m = _map_args(costmap)
+    args = [_f32(a).reshape(-1) for a in (x0_nom, x0_real, mean_nom, mean_real, gains)]
+    rc = lib().orc_rmppi_rollout(model, _ptr(dyn), _ptr(cost), *m, _fp(args[0]), _fp(args[1]), _fp(un), _fp(ur),
+                                 _fp(args[2]), _fp(args[3]), _fp(args[4]), _ptr(sampling), _ptr(constraints), lambda_,
+                                 alpha, threshold, K, T, dt, _fp(cn), _fp(cr), threads or threads_default())
+    if rc != 0:
+        raise ValueError(f"oracle has no R-MPPI model {model}")
+    return cn, cr, un, ur
+
+
+def rmppi_eval(model, dyn, cost, cand_states, cand_strides, per_cand, samples, mean, sampling, constraints, lambda_,
+               alpha, K, T, dt, costmap=None):
+    """initEvalKernel restated: costs float32[num_cand * per_cand]."""
+    cs = _f32(cand_states).reshape(-1)
+    st = np.ascontiguousarray(cand_strides, dtype=np.int32)
+    smp = _f32(samples).reshape(-1)
+    mn = _f32(mean).reshape(-1)
+    out = np.empty(st.size * per_cand, np.float32)
+    keep, m = _map_args(costmap)
+    rc = lib().orc_rmppi_eval(model, _ptr(dyn), _ptr(cost), *m, _fp(cs), st.ctypes.data_as(C.POINTER(C.c_int)),
+                              st.size, per_cand, _fp(smp), _fp(mn), _ptr(sampling), _ptr(constraints), lambda_, alpha,
+                              K, T, dt, _fp(out))
+    if rc != 0:
+        raise ValueError(f"oracle has no R-MPPI model {model}")
+    return out
 
 
 def step_state(model, dyn, cost, x, u, dt):

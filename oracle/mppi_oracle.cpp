@@ -1292,6 +1292,183 @@ int orc_tube_compute_control(int model, const void* dyn, const void* cost, const
 
 // One nominal-state update of TubeMPPIController::slideControlSequence (updateNominalState,
 // tube_mppi_controller.cu:343-349): x <- step(x, u), no constraint.
+}  // extern "C"
+
+// ---- R-MPPI (the robust controller's two rollouts), for the built-in models in float ------------------------------
+
+namespace orc
+{
+// rolloutRMPPIKernel (rmppi_kernels.cu:666-861) for samples [kb, ke): per step the nominal system's sample,
+// constrained and written back; the real system's sample plus the feedback K_t (x_real - x_nominal) (the whole
+// product, as DDPFeedback::k_ forms it, ddp.cuh:139-146), constrained and written back; Euler steps; running costs
+// on the stepped states.  The real system pays running + likelihood; the nominal one 0.5 J_nom + 0.5 max(min(J_fb,
+// threshold), J_nom) + likelihood_nom, J_fb the real running cost plus the feedback cost (computeFeedbackCost,
+// gaussian.cu:577-630); all divided by T, terminal costs added before.
+template <class Model>
+static void rmppi_rollout_range(const Model& m, const float* x0n, const float* x0r, float* un_all, float* ur_all,
+                                const float* mean_n, const float* mean_r, const float* gains,
+                                const mppi_sampling_params& sp, const mppi_control_constraints& cc, float lambda,
+                                float alpha, float thr, int K, int T, float dt, int kb, int ke, float* cost_n_out,
+                                float* cost_r_out)
+{
+  const int S = Model::S, C = Model::C;
+  const bool use_likelihood = std::any_of(sp.control_cost_coeff, sp.control_cost_coeff + C,
+                                          [](float v) { return v != 0.0f; });
+  for (int k = kb; k < ke; ++k)
+  {
+    float xn[MPPI_MAX_STATE_DIM], xr[MPPI_MAX_STATE_DIM];
+    for (int s = 0; s < S; ++s)
+    {
+      xn[s] = x0n[s];
+      xr[s] = x0r[s];
+    }
+    float run_n = 0.0f, lik_n = 0.0f, run_r = 0.0f, extra_r = 0.0f;
+    for (int t = 0; t < T; ++t)
+    {
+      float* un = un_all + ((size_t)k * T + t) * C;
+      float* ur = ur_all + ((size_t)k * T + t) * C;
+      float u_n[MPPI_MAX_CONTROL_DIM], u_r[MPPI_MAX_CONTROL_DIM], fb[MPPI_MAX_CONTROL_DIM];
+      float xn2[MPPI_MAX_STATE_DIM], xr2[MPPI_MAX_STATE_DIM], xd[MPPI_MAX_STATE_DIM];
+      for (int c = 0; c < C; ++c)
+      {
+        u_n[c] = enforce_constraint(un[c], cc, c);
+        un[c] = u_n[c];
+      }
+      for (int r = 0; r < C; ++r)
+      {
+        float acc = 0.0f;
+        for (int c = 0; c < S; ++c) acc += gains[(size_t)t * C * S + r + (size_t)c * C] * (xr[c] - xn[c]);
+        fb[r] = acc;
+      }
+      for (int c = 0; c < C; ++c)
+      {
+        u_r[c] = enforce_constraint(ur[c] + fb[c], cc, c);
+        ur[c] = u_r[c];
+      }
+      m.deriv(xn, u_n, xd);
+      for (int s = 0; s < S; ++s) xn2[s] = fmaf(xd[s], dt, xn[s]);
+      m.deriv(xr, u_r, xd);
+      for (int s = 0; s < S; ++s) xr2[s] = fmaf(xd[s], dt, xr[s]);
+      const float cn = m.state_cost(xn2, t) + m.control_cost(u_n, t);
+      const float cr = m.state_cost(xr2, t) + m.control_cost(u_r, t);
+      run_n += cn;
+      if (use_likelihood)
+      {
+        lik_n += likelihood_cost<float>(u_n, mean_n + (size_t)t * C, sp, C, k, K, lambda, alpha);
+        run_r += cr + likelihood_cost<float>(u_r, mean_r + (size_t)t * C, sp, C, k, K, lambda, alpha);
+      }
+      else
+      {
+        run_r += cr;
+      }
+      float fc = 0.0f;
+      for (int i = 0; i < C; ++i)
+        fc += sp.control_cost_coeff[i] * (fb[i] * fb[i]) / (sp.std_dev[i] * sp.std_dev[i]);
+      extra_r += cr + 0.5f * lambda * (1.0f - alpha) * fc;
+      for (int s = 0; s < S; ++s)
+      {
+        xn[s] = xn2[s];
+        xr[s] = xr2[s];
+      }
+    }
+    run_n += m.terminal_cost(xn);
+    const float tr = m.terminal_cost(xr);
+    run_r += tr;
+    extra_r += tr;
+    const float Tf = (float)T;
+    run_n /= Tf;
+    lik_n /= Tf;
+    run_r /= Tf;
+    extra_r /= Tf;
+    float cn = (float)(0.5 * (double)run_n + 0.5 * (double)fmaxf(fminf(extra_r, thr), run_n));
+    cn += lik_n;
+    cost_n_out[k] = cn;
+    cost_r_out[k] = run_r;
+  }
+}
+
+// initEvalKernel (rmppi_kernels.cu:231-357): rollout g = candidate * per_cand + j from the candidate's state with
+// sample j of the nominal distribution read at min(t + stride, T - 1), constrained, not written back; running cost
+// plus the likelihood term of sample index g against the mean at t; cost = running / T + terminal / T.
+template <class Model>
+static void rmppi_eval_range(const Model& m, const float* cand, const int* strides, int per_cand,
+                             const float* samples, const float* mean, const mppi_sampling_params& sp,
+                             const mppi_control_constraints& cc, float lambda, float alpha, int K, int T, float dt,
+                             int gb, int ge, float* out)
+{
+  const int S = Model::S, C = Model::C;
+  const bool use_likelihood = std::any_of(sp.control_cost_coeff, sp.control_cost_coeff + C,
+                                          [](float v) { return v != 0.0f; });
+  for (int g = gb; g < ge; ++g)
+  {
+    const int ci = g / per_cand, j = g - ci * per_cand, stride = strides[ci];
+    float x[MPPI_MAX_STATE_DIM], xn[MPPI_MAX_STATE_DIM], xd[MPPI_MAX_STATE_DIM], u[MPPI_MAX_CONTROL_DIM];
+    for (int s = 0; s < S; ++s) x[s] = cand[(size_t)ci * S + s];
+    float running = 0.0f;
+    for (int t = 0; t < T; ++t)
+    {
+      const int tc = std::min(t + stride, T - 1);
+      for (int c = 0; c < C; ++c) u[c] = enforce_constraint(samples[((size_t)j * T + tc) * C + c], cc, c);
+      m.deriv(x, u, xd);
+      for (int s = 0; s < S; ++s) xn[s] = fmaf(xd[s], dt, x[s]);
+      float c = m.state_cost(xn, t) + m.control_cost(u, t);
+      if (use_likelihood) c += likelihood_cost<float>(u, mean + (size_t)t * C, sp, C, g, K, lambda, alpha);
+      running += c;
+      for (int s = 0; s < S; ++s) x[s] = xn[s];
+    }
+    out[g] = running / (float)T + m.terminal_cost(x) / (float)T;
+  }
+}
+
+static bool rmppi_model(int model) { return model >= MPPI_MODEL_CARTPOLE && model <= MPPI_MODEL_BICYCLE_SLIP; }
+}  // namespace orc
+
+extern "C" {
+
+int orc_rmppi_rollout(int model, const void* dyn, const void* cost, const float* map, int map_w, int map_h,
+                      float map_res, float map_ox, float map_oy, const float* x0_nom, const float* x0_real,
+                      float* samples_nom, float* samples_real, const float* mean_nom, const float* mean_real,
+                      const float* gains, const mppi_sampling_params* sp, const mppi_control_constraints* cc,
+                      float lambda, float alpha, float threshold, int K, int T, float dt, float* costs_nom,
+                      float* costs_real, int threads)
+{
+  if (!orc::rmppi_model(model)) return 1;
+  orc::ModelBlob b{ model, dyn, cost, { map, map_w, map_h, map_res, map_ox, map_oy } };
+  threads = std::max(1, std::min(threads, K));
+  std::vector<std::thread> pool;
+  const int per = (K + threads - 1) / threads;
+  for (int w = 0; w < threads; ++w)
+  {
+    const int kb = w * per, ke = std::min(K, kb + per);
+    if (kb >= ke) break;
+    pool.emplace_back([&, kb, ke]() {
+      orc::with_model<float>(b, [&](auto& m) {
+        if constexpr (!orc::HasCrash<std::decay_t<decltype(m)>>::value)
+          orc::rmppi_rollout_range(m, x0_nom, x0_real, samples_nom, samples_real, mean_nom, mean_real, gains, *sp,
+                                   *cc, lambda, alpha, threshold, K, T, dt, kb, ke, costs_nom, costs_real);
+      });
+    });
+  }
+  for (auto& th : pool) th.join();
+  return 0;
+}
+
+int orc_rmppi_eval(int model, const void* dyn, const void* cost, const float* map, int map_w, int map_h,
+                   float map_res, float map_ox, float map_oy, const float* cand_states, const int* cand_strides,
+                   int num_cand, int per_cand, const float* samples, const float* mean,
+                   const mppi_sampling_params* sp, const mppi_control_constraints* cc, float lambda, float alpha,
+                   int K, int T, float dt, float* costs_out)
+{
+  if (!orc::rmppi_model(model)) return 1;
+  orc::ModelBlob b{ model, dyn, cost, { map, map_w, map_h, map_res, map_ox, map_oy } };
+  orc::with_model<float>(b, [&](auto& m) {
+    if constexpr (!orc::HasCrash<std::decay_t<decltype(m)>>::value)
+      orc::rmppi_eval_range(m, cand_states, cand_strides, per_cand, samples, mean, *sp, *cc, lambda, alpha, K, T, dt,
+                            0, num_cand * per_cand, costs_out);
+  });
+  return 0;
+}
+
 int orc_step_state(int model, const void* dyn, const void* cost, const float* u, float dt, float* x)
 {
   orc::ModelBlob b{ model, dyn, cost, { nullptr, 0, 0, 1.0f, 0.0f, 0.0f } };

@@ -320,20 +320,42 @@ public:
                         int max_iter, float lambda, float alpha, int num_timesteps = MAX_TIMESTEPS,
                         const control_trajectory& init_control_traj = control_trajectory{}, void* stream = nullptr,
                         uint64_t seed = 0)
-      : T_(num_timesteps), constraints_(model->constraints)
+      : VanillaMPPIController(1, model, cost, fb_controller, sampler,
+                              make_params(dt, max_iter, lambda, alpha, num_timesteps, seed), init_control_traj, stream)
   {
-    if (num_timesteps < 1 || num_timesteps > MAX_TIMESTEPS) throw Error(MPPI_EINVAL, "num_timesteps out of range");
-    mppi_default_controller_params(&params_);
-    params_.dt = dt;
-    params_.num_iters = max_iter;
-    params_.lambda = lambda;
-    params_.alpha = alpha;
-    params_.num_timesteps = num_timesteps;
-    params_.seed = seed;
-    const int K = NUM_ROLLOUTS;
-    check(mppi_create(DYN_T::MODEL_ID, 1, &K, &T_, &params_, &sampler->params, &model->constraints, &model->params,
-                      sizeof(model->params), &cost->params, sizeof(cost->params), init_control_traj.data(), stream,
-                      &h_),
+  }
+
+protected:
+  static mppi_controller_params make_params(float dt, int max_iter, float lambda, float alpha, int num_timesteps,
+                                            uint64_t seed, int controller = MPPI_CONTROLLER_VANILLA)
+  {
+    mppi_controller_params p;
+    mppi_default_controller_params(&p);
+    p.dt = dt;
+    p.num_iters = max_iter;
+    p.lambda = lambda;
+    p.alpha = alpha;
+    p.num_timesteps = num_timesteps;
+    p.seed = seed;
+    p.controller = controller;
+    return p;
+  }
+  // A handle of `distributions` instances of NUM_ROLLOUTS x num_timesteps (two for Tube-MPPI and R-MPPI, the
+  // reference's sampling distributions), every instance starting from init_control_traj.
+  VanillaMPPIController(int distributions, DYN_T* model, COST_T* cost, FB_T* fb_controller, SAMPLING_T* sampler,
+                        const mppi_controller_params& params, const control_trajectory& init_control_traj,
+                        void* stream)
+      : T_(params.num_timesteps), D_(distributions), constraints_(model->constraints), params_(params)
+  {
+    if (T_ < 1 || T_ > MAX_TIMESTEPS) throw Error(MPPI_EINVAL, "num_timesteps out of range");
+    std::vector<int> K(D_, NUM_ROLLOUTS), T(D_, T_);
+    std::vector<float> init((size_t)D_ * T_ * C);
+    for (int d = 0; d < D_; ++d) std::copy(init_control_traj.begin(), init_control_traj.begin() + T_ * C,
+                                           init.begin() + (size_t)d * T_ * C);
+    std::vector<typename DYN_T::DYN_PARAMS_T> dyn(D_, model->params);
+    std::vector<typename COST_T::COST_PARAMS_T> cst(D_, cost->params);
+    check(mppi_create(DYN_T::MODEL_ID, D_, K.data(), T.data(), &params_, &sampler->params, &model->constraints,
+                      dyn.data(), sizeof(model->params), cst.data(), sizeof(cost->params), init.data(), stream, &h_),
           "mppi_create");
     try
     {
@@ -358,6 +380,8 @@ public:
       throw;
     }
   }
+
+public:
   ~VanillaMPPIController()
   {
     if constexpr (!std::is_same<FB_T, NoFeedback>::value)
@@ -373,42 +397,40 @@ public:
     check(mppi_compute_control(h_, state.data(), optimization_stride), "mppi_compute_control");
   }
   // Controller::getControlSeq (controller.cuh:425-428): the first num_timesteps columns are the solution.
-  control_trajectory getControlSeq() const
+  control_trajectory getControlSeq() const { return control_of(seq_instance_); }
+  // Controller::setParams with init_control_traj_ (controller.cuh:857-876); every distribution gets the sequence.
+  void setControlSeq(const control_trajectory& u)
   {
-    control_trajectory out{};
-    check(mppi_get_control_seq(h_, out.data()), "mppi_get_control_seq");
-    return out;
+    std::vector<float> all((size_t)D_ * T_ * C);
+    for (int d = 0; d < D_; ++d) std::copy(u.begin(), u.begin() + T_ * C, all.begin() + (size_t)d * T_ * C);
+    check(mppi_set_control_seq(h_, all.data()), "mppi_set_control_seq");
   }
-  // Controller::setParams with init_control_traj_ (controller.cuh:857-876).
-  void setControlSeq(const control_trajectory& u) { check(mppi_set_control_seq(h_, u.data()), "mppi_set_control_seq"); }
   // Controller::slideControlSequence (controller.cuh:370-376).
   void slideControlSequence(int steps)
   {
     check(mppi_slide_control_sequence(h_, steps), "mppi_slide_control_sequence");
   }
   // Controller::getTargetStateSeq (controller.cuh:433).
-  state_trajectory getTargetStateSeq() const
-  {
-    state_trajectory out{};
-    check(mppi_get_state_seq(h_, out.data()), "mppi_get_state_seq");
-    return out;
-  }
-  // Controller::getBaselineCost / getNormalizerCost (controller.cuh:526-533).
-  float getBaselineCost() const { return baseline_normalizer(0); }
-  float getNormalizerCost() const { return baseline_normalizer(1); }
-  // Controller::getSampledCostSeq (controller.cuh:449-452): the weights the transform leaves in the cost array.
+  state_trajectory getTargetStateSeq() const { return state_of(target_instance_); }
+  // Controller::getBaselineCost / getNormalizerCost (controller.cuh:526-533) of distribution ind.
+  float getBaselineCost(int ind = 0) const { return baseline_normalizer(2 * ind); }
+  float getNormalizerCost(int ind = 0) const { return baseline_normalizer(2 * ind + 1); }
+  // Controller::getSampledCostSeq (controller.cuh:449-452): the weights the transform leaves in the cost array (of the
+  // distribution the controller reports: the real system's for R-MPPI, the actual one's for Tube-MPPI).
   sampled_cost_traj getSampledCostSeq() const
   {
-    sampled_cost_traj out(NUM_ROLLOUTS);
-    check(mppi_get_sample_weights(h_, out.data()), "mppi_get_sample_weights");
-    return out;
+    sampled_cost_traj all((size_t)D_ * NUM_ROLLOUTS);
+    check(mppi_get_sample_weights(h_, all.data()), "mppi_get_sample_weights");
+    return sampled_cost_traj(all.begin() + (size_t)cost_instance_ * NUM_ROLLOUTS,
+                             all.begin() + (size_t)(cost_instance_ + 1) * NUM_ROLLOUTS);
   }
-  // Per-sample trajectory costs before the weight transform.
+  // Per-sample trajectory costs before the weight transform (same distribution).
   sampled_cost_traj getSampleCosts() const
   {
-    sampled_cost_traj out(NUM_ROLLOUTS);
-    check(mppi_get_sample_costs(h_, out.data()), "mppi_get_sample_costs");
-    return out;
+    sampled_cost_traj all((size_t)D_ * NUM_ROLLOUTS);
+    check(mppi_get_sample_costs(h_, all.data()), "mppi_get_sample_costs");
+    return sampled_cost_traj(all.begin() + (size_t)cost_instance_ * NUM_ROLLOUTS,
+                             all.begin() + (size_t)(cost_instance_ + 1) * NUM_ROLLOUTS);
   }
   // Controller::setParams / getParams (controller.cuh:842-876) for lambda, alpha, dt, iterations and slide scale.
   void setParams(const mppi_controller_params& p)
@@ -603,7 +625,23 @@ public:
     return u;
   }
 
-private:
+protected:
+  control_trajectory control_of(int d) const
+  {
+    std::vector<float> all((size_t)D_ * T_ * C);
+    check(mppi_get_control_seq(h_, all.data()), "mppi_get_control_seq");
+    control_trajectory out{};
+    std::copy(all.begin() + (size_t)d * T_ * C, all.begin() + (size_t)(d + 1) * T_ * C, out.begin());
+    return out;
+  }
+  state_trajectory state_of(int d) const
+  {
+    std::vector<float> all((size_t)D_ * T_ * S);
+    check(mppi_get_state_seq(h_, all.data()), "mppi_get_state_seq");
+    state_trajectory out{};
+    std::copy(all.begin() + (size_t)d * T_ * S, all.begin() + (size_t)(d + 1) * T_ * S, out.begin());
+    return out;
+  }
   double bracket(double rel_time, int* lo, int* hi) const
   {
     const double dt = params_.dt;
@@ -615,9 +653,9 @@ private:
 
   float baseline_normalizer(int which) const
   {
-    float bn[2];
-    check(mppi_get_baseline_normalizer(h_, bn, nullptr), "mppi_get_baseline_normalizer");
-    return bn[which];
+    std::vector<float> bn((size_t)2 * D_);
+    check(mppi_get_baseline_normalizer(h_, bn.data(), nullptr), "mppi_get_baseline_normalizer");
+    return bn.at(which);
   }
   template <class D, class Co>
   void configure(const D& model, const Co& cost)
@@ -637,6 +675,10 @@ private:
 
   mppi_handle* h_ = nullptr;
   int T_ = MAX_TIMESTEPS;
+  int D_ = 1;               // sampling distributions (instances) of the handle
+  int seq_instance_ = 0;    // the distribution getControlSeq returns
+  int target_instance_ = 0; // the distribution getTargetStateSeq returns
+  int cost_instance_ = 0;   // the distribution getSampledCostSeq returns
   mppi_control_constraints constraints_{};
   FB_T* fb_ = nullptr;
   std::atomic<bool> fb_enabled_{ false };
@@ -645,6 +687,171 @@ private:
   int top_n_ = 0;
   std::vector<int> sampled_idx_;
   std::vector<float> sampled_states_, sampled_costs_, sampled_terminal_, top_costs_;
+};
+
+// ---- ColoredMPPIController (controllers/ColoredMPPI/colored_mppi_controller.cuh:40-196) ----------------------------
+// The MPPI iteration with Tsallis weights once gamma and r are both non-zero, an optional state leash and, after
+// smoothing, a clamp of control 1 only.
+template <class DYN_T, class COST_T, class FB_T, int MAX_TIMESTEPS, int NUM_ROLLOUTS,
+          class SAMPLING_T = ColoredNoiseDistribution>
+class ColoredMPPIController : public VanillaMPPIController<DYN_T, COST_T, FB_T, MAX_TIMESTEPS, NUM_ROLLOUTS, SAMPLING_T>
+{
+  using Base = VanillaMPPIController<DYN_T, COST_T, FB_T, MAX_TIMESTEPS, NUM_ROLLOUTS, SAMPLING_T>;
+
+public:
+  using typename Base::control_trajectory;
+  ColoredMPPIController(DYN_T* model, COST_T* cost, FB_T* fb_controller, SAMPLING_T* sampler, float dt, int max_iter,
+                        float lambda, float alpha, int num_timesteps = MAX_TIMESTEPS,
+                        const control_trajectory& init_control_traj = control_trajectory{}, void* stream = nullptr,
+                        uint64_t seed = 0)
+      : Base(1, model, cost, fb_controller, sampler,
+             Base::make_params(dt, max_iter, lambda, alpha, num_timesteps, seed, MPPI_CONTROLLER_COLORED),
+             init_control_traj, stream)
+  {
+  }
+  void setGamma(float gamma) { update([&](mppi_controller_params& p) { p.tsallis_gamma = gamma; }); }
+  float getGamma() const { return this->params_.tsallis_gamma; }
+  void setRExp(float r) { update([&](mppi_controller_params& p) { p.tsallis_r = r; }); }
+  float getRExp() const { return this->params_.tsallis_r; }
+  void setLeashActive(bool active) { update([&](mppi_controller_params& p) { p.leash_active = active ? 1 : 0; }); }
+  bool getLeashActive() const { return this->params_.leash_active != 0; }
+  void setStateLeashLength(float length, int index)
+  {
+    update([&](mppi_controller_params& p) { p.state_leash_dist[index] = length; });
+  }
+  float getStateLeashLength(int index) const { return this->params_.state_leash_dist[index]; }
+
+private:
+  template <class F>
+  void update(F&& f)
+  {
+    mppi_controller_params p = this->params_;
+    f(p);
+    this->setParams(p);
+  }
+};
+
+// ---- TubeMPPIController (controllers/Tube-MPPI/tube_mppi_controller.cuh:29-141) ------------------------------------
+// Two distributions, the actual system (0) and the nominal system (1); getControlSeq / getTargetStateSeq are the
+// nominal system's; the feedback controller is on from construction and tracks the nominal system.
+template <class DYN_T, class COST_T, class FB_T, int MAX_TIMESTEPS, int NUM_ROLLOUTS,
+          class SAMPLING_T = GaussianDistribution>
+class TubeMPPIController : public VanillaMPPIController<DYN_T, COST_T, FB_T, MAX_TIMESTEPS, NUM_ROLLOUTS, SAMPLING_T>
+{
+  using Base = VanillaMPPIController<DYN_T, COST_T, FB_T, MAX_TIMESTEPS, NUM_ROLLOUTS, SAMPLING_T>;
+
+public:
+  using typename Base::control_trajectory;
+  using typename Base::state_trajectory;
+  TubeMPPIController(DYN_T* model, COST_T* cost, FB_T* fb_controller, SAMPLING_T* sampler, float dt, int max_iter,
+                     float lambda, float alpha, int num_timesteps = MAX_TIMESTEPS,
+                     const control_trajectory& init_control_traj = control_trajectory{}, void* stream = nullptr,
+                     uint64_t seed = 0, float nominal_threshold = 20.0f)
+      : Base(2, model, cost, fb_controller, sampler, tube_params(dt, max_iter, lambda, alpha, num_timesteps, seed,
+                                                                 nominal_threshold),
+             init_control_traj, stream)
+  {
+    this->seq_instance_ = 1;
+    this->target_instance_ = 1;
+    this->initFeedback();
+  }
+  control_trajectory getActualControlSeq() const { return this->control_of(0); }
+  state_trajectory getActualStateSeq() const { return this->state_of(0); }
+  float getNominalThreshold() const { return this->params_.nominal_threshold; }
+  void setNominalThreshold(float threshold)
+  {
+    mppi_controller_params p = this->params_;
+    p.nominal_threshold = threshold;
+    this->setParams(p);
+  }
+  // FreeEnergyStatistics::nominal_state_used of the last computeControl
+  int getNominalStateUsed() const
+  {
+    int used = 0;
+    check(mppi_get_nominal_state_used(this->h_, &used), "mppi_get_nominal_state_used");
+    return used;
+  }
+
+private:
+  static mppi_controller_params tube_params(float dt, int max_iter, float lambda, float alpha, int T, uint64_t seed,
+                                            float threshold)
+  {
+    mppi_controller_params p = Base::make_params(dt, max_iter, lambda, alpha, T, seed, MPPI_CONTROLLER_TUBE);
+    p.nominal_threshold = threshold;
+    return p;
+  }
+};
+
+// ---- RobustMPPIController (controllers/R-MPPI/robust_mppi_controller.cuh:59-322) -----------------------------------
+// Two distributions in the reference's order, nominal (0) and real (1); updateImportanceSamplingControl before each
+// computeControl; getControlSeq is the real system's sequence, getTargetStateSeq the nominal trajectory;
+// slideControlSequence and computeFeedback do nothing, as in the reference.
+template <class DYN_T, class COST_T, class FB_T, int MAX_TIMESTEPS, int NUM_ROLLOUTS,
+          class SAMPLING_T = GaussianDistribution>
+class RobustMPPIController : public VanillaMPPIController<DYN_T, COST_T, FB_T, MAX_TIMESTEPS, NUM_ROLLOUTS, SAMPLING_T>
+{
+  using Base = VanillaMPPIController<DYN_T, COST_T, FB_T, MAX_TIMESTEPS, NUM_ROLLOUTS, SAMPLING_T>;
+
+public:
+  using typename Base::control_trajectory;
+  using typename Base::state_array;
+  RobustMPPIController(DYN_T* model, COST_T* cost, FB_T* fb_controller, SAMPLING_T* sampler, float dt, int max_iter,
+                       float lambda, float alpha, float value_function_threshold, int num_timesteps = MAX_TIMESTEPS,
+                       const control_trajectory& init_control_traj = control_trajectory{},
+                       int num_candidate_nominal_states = 9, int optimization_stride = 1, void* stream = nullptr,
+                       uint64_t seed = 0, int num_eval_samples_per_candidate = 64)
+      : Base(2, model, cost, fb_controller, sampler,
+             rmppi_params(dt, max_iter, lambda, alpha, num_timesteps, seed, value_function_threshold,
+                          num_candidate_nominal_states, num_eval_samples_per_candidate),
+             init_control_traj, stream),
+        optimization_stride_(optimization_stride)
+  {
+    this->seq_instance_ = 1;
+    this->target_instance_ = 0;
+    this->cost_instance_ = 1;
+    this->initFeedback();
+  }
+  // RobustMPPIController::updateImportanceSamplingControl (robust_mppi_controller.cu:548-569)
+  void updateImportanceSamplingControl(const state_array& state, int stride)
+  {
+    check(mppi_rmppi_update_importance_sampler(this->h_, state.data(), stride), "mppi_rmppi_update_importance_sampler");
+  }
+  state_array getNominalState() const
+  {
+    const auto s = this->state_of(0);
+    state_array x{};
+    std::copy(s.begin(), s.begin() + Base::S, x.begin());
+    return x;
+  }
+  int getBestIndex() const
+  {
+    int best = 0;
+    check(mppi_rmppi_get_candidates(this->h_, &best, nullptr, nullptr, nullptr, nullptr, nullptr),
+          "mppi_rmppi_get_candidates");
+    return best;
+  }
+  std::vector<float> getCandidateFreeEnergy() const
+  {
+    std::vector<float> fe(this->params_.num_candidate_nominal_states);
+    check(mppi_rmppi_get_candidates(this->h_, nullptr, nullptr, nullptr, nullptr, fe.data(), nullptr),
+          "mppi_rmppi_get_candidates");
+    return fe;
+  }
+  float getValueFunctionThreshold() const { return this->params_.value_function_threshold; }
+  int getNumCandidates() const { return this->params_.num_candidate_nominal_states; }
+  int getOptimizationStride() const { return optimization_stride_; }
+
+private:
+  static mppi_controller_params rmppi_params(float dt, int max_iter, float lambda, float alpha, int T, uint64_t seed,
+                                             float threshold, int candidates, int eval_samples)
+  {
+    mppi_controller_params p = Base::make_params(dt, max_iter, lambda, alpha, T, seed, MPPI_CONTROLLER_RMPPI);
+    p.value_function_threshold = threshold;
+    p.num_candidate_nominal_states = candidates;
+    p.num_eval_samples_per_candidate = eval_samples;
+    return p;
+  }
+  int optimization_stride_;
 };
 
 }  // namespace mppi_gb

@@ -405,6 +405,9 @@ public:
     for (int d = 0; d < D_; ++d) std::copy(u.begin(), u.begin() + T_ * C, all.begin() + (size_t)d * T_ * C);
     check(mppi_set_control_seq(h_, all.data()), "mppi_set_control_seq");
   }
+  // Controller::updateImportanceSamplingControl (controller.cuh:322-329): nothing here; the robust controller's
+  // replaces it.  BasePlant calls it before every slide (base_plant.hpp:536-540).
+  void updateImportanceSamplingControl(const state_array&, int) {}
   // Controller::slideControlSequence (controller.cuh:370-376).
   void slideControlSequence(int steps)
   {

@@ -240,7 +240,11 @@ public:
       last_optimization_stride_ = std::max((int)std::round(dt / controller_->getDt()), optimization_stride_);
     }
     if (last_optimization_stride_ > 0 && last_optimization_stride_ < controller_->getNumTimesteps())
+    {
+      // the robust controller's importance sampler first (a no-op for the others), then the slide
+      controller_->updateImportanceSamplingControl(state, last_optimization_stride_);
       controller_->slideControlSequence(last_optimization_stride_);
+    }
     const auto opt_start = clock::now();
     controller_->computeControl(state, last_optimization_stride_);
     const FreeEnergyStatistics fe = controller_->getFreeEnergyStatistics();

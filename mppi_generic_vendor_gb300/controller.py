@@ -393,6 +393,10 @@ class BatchedMPPIController:
         flat = np.ascontiguousarray(flat)
         A.call("mppi_set_control_seq", self._h, _fptr(flat))
 
+    def updateImportanceSamplingControl(self, state, stride=1):
+        """Controller::updateImportanceSamplingControl (controller.cuh:322-329): nothing here; the robust
+        controller's replaces it.  The plant calls it before every slide (base_plant.hpp:536-540)."""
+
     def slideControlSequence(self, steps):
         """Controller::slideControlSequence (controllers/controller.cuh:370-376)."""
         A.call("mppi_slide_control_sequence", self._h, int(steps))

@@ -230,6 +230,9 @@ class BasePlant:
             self.last_optimization_stride_ = max(int(math.copysign(math.floor(abs(steps) + 0.5), steps)),
                                                  self.optimization_stride_)
         if 0 < self.last_optimization_stride_ < c.getNumTimesteps():
+            # the robust controller's importance sampler first (a no-op for the others), then the slide
+            if getattr(c, "updateImportanceSamplingControl", None) is not None:
+                c.updateImportanceSamplingControl(state, self.last_optimization_stride_)
             c.slideControlSequence(self.last_optimization_stride_)
         opt_start = time.perf_counter()
         c.computeControl(state, self.last_optimization_stride_)

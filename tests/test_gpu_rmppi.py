@@ -14,27 +14,38 @@ import pytest
 import _parity
 import oracle
 from _ddp import engine_gains
-from mppi_generic_vendor_gb300 import (DDPFeedback, DDPParams, DoubleIntegratorDynamics, DoubleIntegratorObstacleCost,
-                                       GaussianDistribution, RobustMPPIController)
+from mppi_generic_vendor_gb300 import (CartpoleDynamics, CartpoleSwingupCost, DDPFeedback, DDPParams,
+                                       DoubleIntegratorDynamics, DoubleIntegratorObstacleCost, GaussianDistribution,
+                                       RobustMPPIController)
 from mppi_generic_vendor_gb300 import _abi as A
 
 pytestmark = pytest.mark.gpu
 
 K, T, DT, N, J = 1024, 40, 0.02, 5, 32
 Q = np.diag([4.0, 4.0, 1.0, 1.0]).astype(np.float32)
-R = np.diag([0.5, 0.5]).astype(np.float32)
+
+# (model id, dynamics, cost, control bound, std dev, likelihood coefficient, x, disturbance, second state)
+MODELS = {
+    "double_integrator": (A.MODEL_DOUBLE_INTEGRATOR, DoubleIntegratorDynamics,
+                          lambda: DoubleIntegratorObstacleCost(goal=(1.5, -0.5, 0.0, 0.0), coeff=(1.0, 1.0, 0.1, 0.1),
+                                                               terminal_coeff=5.0, obstacles=[(0.7, 0.0, 0.3)],
+                                                               obstacle_cost=100.0),
+                          2.0, 0.6, 0.3, [0.1, -0.05, 0.3, 0.1], [0.05, -0.03, 0.1, 0.05], [0.16, -0.1, 0.35, 0.02]),
+    "cartpole": (A.MODEL_CARTPOLE, CartpoleDynamics, lambda: CartpoleSwingupCost(), 5.0, 1.0, 0.2,
+                 [0.0, 0.1, 2.6, -0.2], [0.02, -0.05, 0.08, 0.1], [0.05, 0.0, 2.7, 0.3]),
+}
 
 
-def _controller(threshold):
-    dyn = DoubleIntegratorDynamics()
-    dyn.setControlRanges([(-2.0, 2.0), (-2.0, 2.0)])
-    cost = DoubleIntegratorObstacleCost(goal=(1.5, -0.5, 0.0, 0.0), coeff=(1.0, 1.0, 0.1, 0.1), terminal_coeff=5.0,
-                                        obstacles=[(0.7, 0.0, 0.3)], obstacle_cost=100.0)
+def _controller(name, threshold):
+    mid, dyn_cls, cost_fn, bound, sd, coeff = MODELS[name][:6]
+    dyn = dyn_cls()
+    Cd = dyn.CONTROL_DIM
+    dyn.setControlRanges([(-bound, bound)] * Cd)
     fb = DDPFeedback(dyn, DT)
-    fb.setParams(DDPParams(Q, None, R, 1))
-    sampler = GaussianDistribution(std_dev=(0.6, 0.6), control_cost_coeff=(0.3, 0.3))
-    init = np.random.default_rng(2).uniform(-0.3, 0.3, (2, T)).astype(np.float32)
-    return RobustMPPIController(dyn, cost, fb, sampler, DT, 1, 1.0, 0.0, threshold, T, K, init_control_traj=init,
+    fb.setParams(DDPParams(Q, None, 0.5 * np.eye(Cd, dtype=np.float32), 1))
+    sampler = GaussianDistribution(std_dev=(sd,) * Cd, control_cost_coeff=(coeff,) * Cd)
+    init = np.random.default_rng(2).uniform(-0.3, 0.3, (Cd, T)).astype(np.float32)
+    return RobustMPPIController(dyn, cost_fn(), fb, sampler, DT, 1, 1.0, 0.0, threshold, T, K, init_control_traj=init,
                                 num_candidate_nominal_states=N, num_eval_samples_per_candidate=J)
 
 
@@ -44,9 +55,11 @@ def _gains(ctrl):
 
 
 def _check_gains(ctrl, x):
-    lo, hi = np.array([-2.0, -2.0], np.float32), np.array([2.0, 2.0], np.float32)
-    st, host = engine_gains(A.MODEL_DOUBLE_INTEGRATOR, ctrl._dyn_arr[0], x, ctrl.getTargetStateSeq().T.copy(),
-                            ctrl.getNominalControlSeq().T.copy(), DT, Q, np.eye(4, dtype=np.float32), R, 1, lo, hi)
+    Cd = ctrl.Cdim
+    lo, hi = np.array(ctrl.constraints_.lower[:Cd], np.float32), np.array(ctrl.constraints_.upper[:Cd], np.float32)
+    st, host = engine_gains(ctrl.model_id, ctrl._dyn_arr[0], x, ctrl.getTargetStateSeq().T.copy(),
+                            ctrl.getNominalControlSeq().T.copy(), DT, Q, np.eye(4, dtype=np.float32),
+                            0.5 * np.eye(Cd, dtype=np.float32), 1, lo, hi)
     assert st == A.MPPI_OK
     got = _gains(ctrl)
     assert np.array_equal(got.view(np.uint32), host.view(np.uint32))
@@ -67,13 +80,16 @@ def _line_weights(n):
 
 
 @pytest.mark.parametrize("threshold", [1e9, -1e9])
-def test_rmppi_update_solve_update_matches_oracle(threshold):
-    ctrl = _controller(threshold)
+@pytest.mark.parametrize("name", list(MODELS))
+def test_rmppi_update_solve_update_matches_oracle(name, threshold):
+    ctrl = _controller(name, threshold)
+    mid, Cd = ctrl.model_id, ctrl.Cdim
+    sd = np.full(Cd, MODELS[name][4], np.float32)
     rng = np.random.default_rng(7)
-    eps = rng.standard_normal(K * T * 2).astype(np.float32)
+    eps = rng.standard_normal(K * T * Cd).astype(np.float32)
     # one noise draw serves both distributions (use_same_noise_for_all_distributions): the second half is ignored
-    ctrl.injectNoise(np.concatenate([eps, rng.standard_normal(K * T * 2).astype(np.float32)]))
-    x = np.array([0.1, -0.05, 0.3, 0.1], np.float32)
+    ctrl.injectNoise(np.concatenate([eps, rng.standard_normal(K * T * Cd).astype(np.float32)]))
+    x = np.array(MODELS[name][6], np.float32)
     dyn, cost, sp, cc = ctrl._dyn_arr[0], ctrl._cost_arr[0], ctrl.sampler_.to_c(), ctrl.constraints_
     # ---- 1. the first update: the nominal state is the real state; gains around the nominal trajectory
     ctrl.updateImportanceSamplingControl(x, 1)
@@ -82,35 +98,35 @@ def test_rmppi_update_solve_update_matches_oracle(threshold):
     # ---- 2. the solve
     u_nom = ctrl.getNominalControlSeq().T.copy()
     x_nom = ctrl.getNominalState()
-    x_real = (x + np.array([0.05, -0.03, 0.1, 0.05], np.float32)).astype(np.float32)  # disturbed off the nominal
+    x_real = (x + np.array(MODELS[name][7], np.float32)).astype(np.float32)  # disturbed off the nominal
     ctrl.computeControl(x_real, 1)
-    raw = oracle.gaussian_rewrite(eps, u_nom, np.array([0.6, 0.6], np.float32), K, T, 2, 1)
-    cn, cr, un, ur = oracle.rmppi_rollout(A.MODEL_DOUBLE_INTEGRATOR, dyn, cost, x_nom, x_real, raw, raw, u_nom, u_nom,
+    raw = oracle.gaussian_rewrite(eps, u_nom, sd, K, T, Cd, 1)
+    cn, cr, un, ur = oracle.rmppi_rollout(mid, dyn, cost, x_nom, x_real, raw, raw, u_nom, u_nom,
                                           gains.transpose(0, 2, 1).reshape(T, -1), sp, cc, 1.0, 0.0, threshold, K,
                                           T, DT)
     costs = ctrl.sample_costs().reshape(2, K)
     assert np.array_equal(costs[0].view(np.uint32), cn.view(np.uint32))
     assert np.array_equal(costs[1].view(np.uint32), cr.view(np.uint32))
-    samples = ctrl.control_samples().reshape(2, K * T * 2)
+    samples = ctrl.control_samples().reshape(2, K * T * Cd)
     assert np.array_equal(samples[0], un) and np.array_equal(samples[1], ur)
     assert not np.array_equal(un, ur)  # the feedback moved the real system's controls
     bn, _ = ctrl.baseline_normalizer()
     for d, (c, s, got) in enumerate([(cn, un, ctrl.getNominalControlSeq()), (cr, ur, ctrl.getControlSeq())]):
         w, b, n = oracle.weights(c, lambda_inv=np.float32(1.0))
         assert bn[d, 0] == b
-        mean, _ = oracle.weighted_mean(w, np.float32(n), s, K, T, 2)
-        ref = oracle.smooth(mean.astype(np.float32).reshape(T, 2))
-        _parity.check_control(got.T, dict(control=ref, weights=w, normalizer=n, samples=s), K, T, 2)
+        mean, _ = oracle.weighted_mean(w, np.float32(n), s, K, T, Cd)
+        ref = oracle.smooth(mean.astype(np.float32).reshape(T, Cd))
+        _parity.check_control(got.T, dict(control=ref, weights=w, normalizer=n, samples=s), K, T, Cd)
     # the nominal state trajectory: from the nominal state along the (constrained) nominal sequence
     traj = [x_nom]
     for t in range(T - 1):
-        u_c = oracle.enforce_constraints(ctrl.getNominalControlSeq().T[t], 2, cc)
-        traj.append(oracle.step_state(A.MODEL_DOUBLE_INTEGRATOR, dyn, cost, traj[-1], u_c, DT))
+        u_c = oracle.enforce_constraints(ctrl.getNominalControlSeq().T[t], Cd, cc)
+        traj.append(oracle.step_state(mid, dyn, cost, traj[-1], u_c, DT))
     assert np.array_equal(ctrl.getTargetStateSeq().T, np.stack(traj))
     # ---- 3. the second update from a disturbed real state
     p = ctrl.getTargetStateSeq().T.copy()
     u_prev = ctrl.getNominalControlSeq().T.copy()
-    x2 = np.array([0.16, -0.1, 0.35, 0.02], np.float32)
+    x2 = np.array(MODELS[name][8], np.float32)
     ctrl.updateImportanceSamplingControl(x2, 1)
     best, stride, cand, strides, fe, evc = ctrl._candidates()
     w = _line_weights(N)
@@ -119,21 +135,25 @@ def test_rmppi_update_solve_update_matches_oracle(threshold):
     # Eigen's round (std::round) takes halves away from zero
     exp_strides = np.floor(((np.float32(0) * w[0] + np.float32(1) * w[1]) + np.float32(1) * w[2]) + 0.5).astype(np.int32)
     assert np.array_equal(strides, exp_strides)
-    raw_eval = oracle.gaussian_rewrite(eps, u_prev, np.array([0.6, 0.6], np.float32), K, T, 2, 1)
-    ref_eval = oracle.rmppi_eval(A.MODEL_DOUBLE_INTEGRATOR, dyn, cost, cand, strides, J, raw_eval, u_prev, sp, cc, 1.0,
-                                 0.0, K, T, DT)
+    raw_eval = oracle.gaussian_rewrite(eps, u_prev, sd, K, T, Cd, 1)
+    ref_eval = oracle.rmppi_eval(mid, dyn, cost, cand, strides, J, raw_eval, u_prev, sp, cc, 1.0, 0.0, K, T, DT)
     assert np.array_equal(evc.view(np.uint32), ref_eval.view(np.uint32))
+    # computeBestIndex: exponentials in FP32 (a candidate whose samples all lie far above the best one sums to zero
+    # and gets an infinite free energy), the last candidate below the threshold, else the previous choice (0)
     base = ref_eval.min()
-    ref_fe = np.array([-1.0 * np.log(np.mean(np.exp(-(ref_eval[i * J:(i + 1) * J] - base).astype(np.float64))))
-                       + base for i in range(N)])
+    with np.errstate(divide="ignore"):
+        ref_fe = np.array([-1.0 * np.log(np.exp((base - ref_eval[i * J:(i + 1) * J]).astype(np.float32))
+                                         .astype(np.float64).mean()) + base for i in range(N)])
     assert np.allclose(fe, ref_fe, rtol=1e-5, atol=1e-5)
-    exp_best = N - 1 if threshold > 0 else 0  # all below: the last candidate; none: the previous choice (0)
+    below = [i for i in range(N) if ref_fe[i] < threshold]
+    exp_best = below[-1] if below else 0
+    assert (exp_best == N - 1) if threshold > 0 else (exp_best == 0)
     assert best == exp_best and stride == strides[exp_best]
     nom = np.zeros(1, np.int32)
     A.call("mppi_get_nominal_state_used", ctrl._h, nom.ctypes.data_as(A._IP))
     assert nom[0] == exp_best
     assert np.array_equal(ctrl.getNominalState(), cand[exp_best])
-    slid = oracle.slide(u_prev, int(stride), [0.0, 0.0], np.zeros(2, np.float32))
+    slid = oracle.slide(u_prev, int(stride), np.zeros(Cd, np.float32), np.zeros(Cd, np.float32))
     assert np.array_equal(ctrl.getNominalControlSeq().T, slid)
     _check_gains(ctrl, x2)
     # slideControlSequence and computeFeedback do nothing on a robust controller

@@ -1052,16 +1052,10 @@ public:
       memcpy(x0_h_.p + S, x, sizeof(float) * S);
       memcpy(mean_h_.p + t_off_[0], control_.data() + t_off_[0], sizeof(float) * tc);
       memcpy(mean_h_.p + t_off_[1], control_.data() + t_off_[0], sizeof(float) * tc);
-      if (graph_mode_)
-      {
-        cudaGraphExec_t exec = nullptr;
-        MG_TRY(get_graph(stride, &exec));
-        MG_CUDA(cudaGraphLaunch(exec, stream_));
-      }
-      else
-      {
-        MG_TRY(enqueue_solve(stride));
-      }
+      host_iter_ = it;
+      const mppi_status st = launch_host_iteration(stride);
+      host_iter_ = 0;
+      MG_TRY(st);
       MG_CUDA(cudaStreamSynchronize(stream_));
       memcpy(control_.data(), out_mean_h_.p, sizeof(float) * control_.size());
       memcpy(baseline_norm_.data(), out_bn_h_.p, sizeof(float) * 2 * I_);
@@ -1328,6 +1322,19 @@ public:
       }
   }
 
+  // One iteration of a host-iterated solve (iteration host_iter_): its graph, or plain stream launches.
+  mppi_status launch_host_iteration(int stride)
+  {
+    if (graph_mode_)
+    {
+      cudaGraphExec_t exec = nullptr;
+      MG_TRY(get_graph(stride, &exec));
+      MG_CUDA(cudaGraphLaunch(exec, stream_));
+      return MPPI_OK;
+    }
+    return enqueue_solve(stride);
+  }
+
   // TubeMPPIController::computeControl (tube_mppi_controller.cu:158-296): per iteration one graph launch of the
   // device work of both systems (sample, rollout, weights, update, no smoothing), then the nominal-state decision on
   // the host; the nominal sequence is smoothed once at the end.
@@ -1350,16 +1357,10 @@ public:
       memcpy(x0_h_.p, x, sizeof(float) * S);
       memcpy(x0_h_.p + S, nominal_x0_.data(), sizeof(float) * S);
       memcpy(mean_h_.p, control_.data(), sizeof(float) * control_.size());
-      if (graph_mode_)
-      {
-        cudaGraphExec_t exec = nullptr;
-        MG_TRY(get_graph(stride, &exec));
-        MG_CUDA(cudaGraphLaunch(exec, stream_));
-      }
-      else
-      {
-        MG_TRY(enqueue_solve(stride));
-      }
+      host_iter_ = it;
+      const mppi_status st = launch_host_iteration(stride);
+      host_iter_ = 0;
+      MG_TRY(st);
       MG_CUDA(cudaStreamSynchronize(stream_));
       if (status_h_.p[0] != 0u)
       {
@@ -2372,11 +2373,15 @@ private:
     // the smoothing + constraints of the new nominal sequences (the host post-processing of computeControl) run in
     // the last iteration's combine: the fused rollout's finalizing CTAs, tile_finalize_kernel or the weights pass;
     // Tube-MPPI smooths its nominal sequence on the host
-    for (int it = 0; it < (tube() || rmppi() ? 1 : cp_.num_iters); ++it)
+    // Tube-MPPI and R-MPPI iterate on the host, one launch per iteration: host_iter_ is that iteration's index (the
+    // sampler's std_dev_decay power)
+    const bool host_loop = tube() || rmppi();
+    for (int it = 0; it < (host_loop ? 1 : cp_.num_iters); ++it)
     {
-      if (!fused()) MG_TRY(launch_sampler(stride, it));
-      MG_TRY(launch_rollout(stride, it));
-      MG_TRY(launch_weights(it));
+      const int iter = host_loop ? host_iter_ : it;
+      if (!fused()) MG_TRY(launch_sampler(stride, iter));
+      MG_TRY(launch_rollout(stride, iter));
+      MG_TRY(launch_weights(iter));
     }
     return MPPI_OK;
   }
@@ -2400,7 +2405,9 @@ private:
 
   mppi_status get_graph(int stride, cudaGraphExec_t* exec)
   {
-    auto it = graphs_.find(stride);
+    // a host-iterated solve (Tube-MPPI, R-MPPI) with a decaying sampling deviation captures one graph per iteration
+    const int key = ((tube() || rmppi()) && sp_.std_dev_decay != 1.0f) ? stride + (host_iter_ << 20) : stride;
+    auto it = graphs_.find(key);
     if (it != graphs_.end())
     {
       *exec = it->second;
@@ -2429,7 +2436,7 @@ private:
       set_error("cudaGraphInstantiate failed: %s", cudaGetErrorString(ce));
       return MPPI_ECUDA;
     }
-    graphs_[stride] = e;
+    graphs_[key] = e;
     *exec = e;
     return MPPI_OK;
   }
@@ -2505,6 +2512,7 @@ private:
   uint32_t max_polls_ = kMaxProgressPolls;  // rollout mode 4's bounded poll (mppi_set_wait_diagnostics)
   bool withhold_progress_ = false;          // mode 4's noise warps publish no progress (mppi_set_wait_diagnostics)
   bool traj_dirty_ = false;
+  int host_iter_ = 0;  // the iteration of a host-iterated solve (Tube-MPPI, R-MPPI) being enqueued
   std::vector<double> stats_;
   bool fb_enabled_ = false;                // Controller::enable_feedback_
   DdpWeights fb_w_;                        // DDPParams: identities and one iteration until set

@@ -95,6 +95,34 @@ def test_tube_solve_slide_solve_matches_oracle(threshold, same_noise):
     ctrl.close()
 
 
+def test_tube_iterations_apply_the_std_dev_decay():
+    """Two iterations with std_dev_decay = 0.8: the second iteration's samples are drawn with 0.8 sigma
+    (generateSamples(stride, opt_iter), tube_mppi_controller.cu:188-196) although the solve iterates on the host.  The
+    second iteration starts from the first one's means, which the engine sums in FP32 and the oracle in FP64, so the
+    costs agree to 1e-4 here rather than bit for bit (without the decay they would differ by percents)."""
+    K, T = 2048, 48
+    dyn = DoubleIntegratorDynamics()
+    dyn.setControlRanges([(-2.0, 2.0), (-2.0, 2.0)])
+    cost = DoubleIntegratorObstacleCost(goal=(1.5, -0.5, 0.0, 0.0), coeff=(1.0, 1.0, 0.1, 0.1), terminal_coeff=5.0,
+                                        obstacles=[(0.7, 0.0, 0.3)], obstacle_cost=100.0)
+    sampler = GaussianDistribution(std_dev=(0.6, 0.6), std_dev_decay=0.8)
+    ctrl = TubeMPPIController(dyn, cost, None, sampler, 0.02, 2, 1.0, 0.0, T, K, nominal_threshold=-1e9)
+    rng = np.random.default_rng(21)
+    init = rng.uniform(-0.5, 0.5, (T, 2)).astype(np.float32)
+    ctrl.setControlSeq(init.T)
+    x = np.array([0.0, 0.0, 0.3, -0.2], np.float32)
+    eps = _draw(rng, K, T, True)
+    ctrl.injectNoise(eps)
+    ctrl.computeControl(x, 1)
+    ref = oracle.tube_compute_control(ctrl.model_id, ctrl._dyn_arr[0], ctrl._cost_arr[0], ctrl.getParams(),
+                                      ctrl.sampler_.to_c(), ctrl.constraints_, K, T, 2, 4, x, x, eps,
+                                      np.stack([init, init]))
+    costs = ctrl.sample_costs().reshape(2, K)
+    rel = np.abs(costs - ref["costs"]) / np.abs(ref["costs"])
+    assert rel.max() < 1e-4, rel.max()
+    ctrl.close()
+
+
 @pytest.mark.parametrize("same_noise", [True, False])
 def test_tube_distributions_share_philox_noise(same_noise):
     """With both distributions around the same mean, use_same_noise_for_all_distributions gives bit-identical

@@ -86,8 +86,8 @@ typedef enum mppi_controller_kind
                                   the DDP feedback K_t (x_real - x_nominal) added to its controls.  Both sample
                                   around the nominal sequence (the importance sampler); the nominal costs blend in
                                   the real system's (rolloutRMPPIKernel, rmppi_kernels.cu:666-861).  Call
-                                  mppi_rmppi_update_importance_sampler before each mppi_compute_control.  Built-in
-                                  analytic models with Gaussian sampling. */
+                                  mppi_rmppi_update_importance_sampler before each mppi_compute_control.  Analytic
+                                  models (built-in and plugin pairs) with Gaussian sampling. */
 } mppi_controller_kind;
 
 /* ControllerParams (include/mppi/controllers/controller.cuh:46-68) and the fields ColoredMPPIParams adds

@@ -915,7 +915,8 @@ class RobustMPPIController(BatchedMPPIController):
     candidates between the nominal trajectory and the real state, slides the nominal sequence and computes the
     feedback gains; call it before each computeControl.  getControlSeq is the real system's sequence and
     getTargetStateSeq the nominal state trajectory, as in the reference; slideControlSequence and computeFeedback do
-    nothing (the importance-sampler update does both).  Built-in analytic models with Gaussian sampling."""
+    nothing (the importance-sampler update does both).  Analytic models with Gaussian sampling: the built-in ones here,
+    a caller's plugin pair through plugin.PluginRobustMPPIController."""
 
     def __init__(self, model, cost, fb_controller, sampler, dt, max_iter, lambda_, alpha, value_function_threshold,
                  num_timesteps, num_rollouts, init_control_traj=None, num_candidate_nominal_states=9,

@@ -570,7 +570,7 @@ public:
                "a Tube-MPPI handle holds two instances of equal num_rollouts and num_timesteps (actual, nominal)");
     if (cp.controller == MPPI_CONTROLLER_RMPPI)
     {
-      MG_CHECK(!Model::kMlp && !Model::kPlugin, "R-MPPI runs the built-in analytic models");
+      MG_CHECK(!Model::kMlp, "R-MPPI runs analytic models (the built-in ones and plugins)");
       MG_CHECK(std::isfinite(cp.value_function_threshold), "value_function_threshold must be finite");
       // RobustMPPIController::updateNumCandidates (robust_mppi_controller.cu:424-457)
       MG_CHECK(cp.num_candidate_nominal_states >= 3 && cp.num_candidate_nominal_states % 2 == 1,
@@ -1028,9 +1028,9 @@ public:
   // end and the nominal state trajectory is recomputed.  x is the real system's state.
   mppi_status compute_control_rmppi(const float* x, int stride)
   {
-    if constexpr (Model::kPlugin || Model::kMlp)
+    if constexpr (Model::kMlp)
     {
-      set_error("R-MPPI runs the built-in analytic models");
+      set_error("R-MPPI runs analytic models (the built-in ones and plugins)");
       return MPPI_EUNSUPPORTED;
     }
     for (int i = 0; i < S; ++i)
@@ -1087,9 +1087,9 @@ public:
         set_error("state has a non-finite entry at index %d", i);
         return MPPI_ENAN;
       }
-    if constexpr (Model::kPlugin || Model::kMlp)
+    if constexpr (Model::kMlp)
     {
-      set_error("R-MPPI runs the built-in analytic models");
+      set_error("R-MPPI runs analytic models (the built-in ones and plugins)");
       return MPPI_EUNSUPPORTED;
     }
     else
@@ -2141,7 +2141,7 @@ private:
 
   mppi_status launch_rollout(int stride, int iter)
   {
-    if constexpr (!Model::kPlugin && !Model::kMlp)
+    if constexpr (!Model::kMlp)
       if (rmppi()) return launch_rmppi_rollout();
     if constexpr (Model::kPlugin)
     {

@@ -11,7 +11,8 @@
 //    control dimension; the kernel applies the whole product K_t e, as the reference's host DDPFeedback::k_ does.
 //  * rmppi_eval_kernel: initEvalKernel (rmppi_kernels.cu:231-357): num_candidates x samples_per_candidate rollouts,
 //    candidate c from its state with the samples of the nominal distribution read at t + stride_c (held at T-1).
-// One thread per sample, no shared memory and no waits.
+// Both run the built-in models and a caller's plugin pair (its own step, computeRunningCost with the sample's crash
+// flag, and its own enforceConstraints when it defines one).  One thread per sample, no shared memory and no waits.
 #pragma once
 
 #include "mg_kernels.cuh"
@@ -41,6 +42,54 @@ struct RmppiArgs
   int use_likelihood;
 };
 
+// The control constraint of a step: a plugin's own enforceConstraints with the state, else the deadband and the clamp
+// of the handle's ranges (Dynamics::enforceConstraints, dynamics.cu:107-126).
+template <class Model, class Args>
+__device__ __forceinline__ void rmppi_constrain(const Args& a, const typename Model::DynParams& dp, float* x, float* u)
+{
+  if constexpr (Model::kOwnConstraints)
+  {
+    dp.enforceConstraints(x, u);
+  }
+  else
+  {
+#pragma unroll
+    for (int c = 0; c < Model::CONTROL_DIM; ++c)
+      u[c] = enforce_constraint(u[c], a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c], a.sh.zero[c]);
+  }
+}
+
+// One step x -> xn under u and its running cost on the output y (Dynamics::step, Cost::computeRunningCost with the
+// crash flag, cost.cu:39-53): a plugin's own step, or the explicit Euler step of a built-in model (y = xn).
+template <class Model, class Args>
+__device__ __forceinline__ float rmppi_step(const Args& a, const typename Model::DynParams& dp,
+                                            const typename Model::CostParams& cp, const float* x, const float* u,
+                                            float* xn, float* y, int t, int* crash)
+{
+  if constexpr (Model::kPlugin)
+  {
+    float xd[Model::STATE_DIM];
+    dp.step(x, xn, xd, u, y, t, a.dt);
+    return cp.computeRunningCost(y, u, t, crash);
+  }
+  else
+  {
+    euler_step<Model>(dp, x, u, xn, a.dt);
+#pragma unroll
+    for (int s = 0; s < Model::STATE_DIM; ++s) y[s] = xn[s];
+    return Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
+  }
+}
+
+template <class Model, class Args>
+__device__ __forceinline__ float rmppi_terminal(const Args& a, const typename Model::CostParams& cp, const float* y)
+{
+  if constexpr (Model::kPlugin)
+    return cp.terminalCost(y);
+  else
+    return Model::terminalCost(cp, a.aux, y);
+}
+
 // GaussianDistributionImpl::computeFeedbackCost (gaussian.cu:577-630): 0.5 lambda (1 - alpha) sum_i coeff_i fb_i^2 /
 // sd_i^2, the terms added in control order.
 template <int C, class Args>
@@ -55,14 +104,15 @@ __device__ __forceinline__ float feedback_cost(const Args& a, const float* fb)
 template <class Model>
 __global__ void __launch_bounds__(128) rmppi_rollout_kernel(const __grid_constant__ RmppiArgs<Model> a)
 {
-  constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM;
+  constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM, O = Model::OUTPUT_DIM;
   const InstDesc dn = a.inst[0], dr = a.inst[1];
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= dn.K) return;
   const int T = dn.T;
   const typename Model::DynParams& dp = a.dyn[0];
   const typename Model::CostParams& cp = a.cost[0];
-  float xn[S], xr[S];
+  float xn[S], xr[S], yn[O], yr[O];
+  int crash_n = 0, crash_r = 0;  // crash_status of each system (mppi_common.cu:85-86)
 #pragma unroll
   for (int s = 0; s < S; ++s)
   {
@@ -77,11 +127,10 @@ __global__ void __launch_bounds__(128) rmppi_rollout_kernel(const __grid_constan
     float un[C], ur[C], fb[C], xn2[S], xr2[S];
     // the nominal system takes its sample, constrained (no feedback on the nominal system)
 #pragma unroll
-    for (int c = 0; c < C; ++c)
-    {
-      un[c] = enforce_constraint(un_row[t * C + c], a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c], a.sh.zero[c]);
-      un_row[t * C + c] = un[c];
-    }
+    for (int c = 0; c < C; ++c) un[c] = un_row[t * C + c];
+    rmppi_constrain<Model>(a, dp, xn, un);
+#pragma unroll
+    for (int c = 0; c < C; ++c) un_row[t * C + c] = un[c];
     // the real system adds the feedback against the nominal state of this step
     const float* K = a.gains + (size_t)t * C * S;
 #pragma unroll
@@ -93,16 +142,12 @@ __global__ void __launch_bounds__(128) rmppi_rollout_kernel(const __grid_constan
       fb[r] = acc;
     }
 #pragma unroll
-    for (int c = 0; c < C; ++c)
-    {
-      ur[c] = enforce_constraint(ur_row[t * C + c] + fb[c], a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c],
-                                 a.sh.zero[c]);
-      ur_row[t * C + c] = ur[c];
-    }
-    euler_step<Model>(dp, xn, un, xn2, a.dt);
-    euler_step<Model>(dp, xr, ur, xr2, a.dt);
-    const float cn = Model::computeStateCost(cp, a.aux, xn2, t) + Model::computeControlCost(cp, un, t);
-    const float cr = Model::computeStateCost(cp, a.aux, xr2, t) + Model::computeControlCost(cp, ur, t);
+    for (int c = 0; c < C; ++c) ur[c] = ur_row[t * C + c] + fb[c];
+    rmppi_constrain<Model>(a, dp, xr, ur);
+#pragma unroll
+    for (int c = 0; c < C; ++c) ur_row[t * C + c] = ur[c];
+    const float cn = rmppi_step<Model>(a, dp, cp, xn, un, xn2, yn, t, &crash_n);
+    const float cr = rmppi_step<Model>(a, dp, cp, xr, ur, xr2, yr, t, &crash_r);
     run_n += cn;
     if (a.use_likelihood)
     {
@@ -121,8 +166,8 @@ __global__ void __launch_bounds__(128) rmppi_rollout_kernel(const __grid_constan
       xr[s] = xr2[s];
     }
   }
-  run_n += Model::terminalCost(cp, a.aux, xn);
-  const float term_r = Model::terminalCost(cp, a.aux, xr);
+  run_n += rmppi_terminal<Model>(a, cp, yn);
+  const float term_r = rmppi_terminal<Model>(a, cp, yr);
   run_r += term_r;
   extra_r += term_r;
   const float Tf = (float)T;
@@ -160,7 +205,7 @@ struct RmppiEvalArgs
 template <class Model>
 __global__ void __launch_bounds__(64) rmppi_eval_kernel(const __grid_constant__ RmppiEvalArgs<Model> a)
 {
-  constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM;
+  constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM, O = Model::OUTPUT_DIM;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= a.num_cand * a.per_cand) return;
   const int cand = g / a.per_cand, j = g - cand * a.per_cand;
@@ -168,19 +213,19 @@ __global__ void __launch_bounds__(64) rmppi_eval_kernel(const __grid_constant__ 
   const typename Model::DynParams& dp = a.dyn[0];
   const typename Model::CostParams& cp = a.cost[0];
   const float* row = a.samples + a.d.u_off + (long long)j * T * C;
-  float x[S];
+  float x[S], y[O];
 #pragma unroll
   for (int s = 0; s < S; ++s) x[s] = a.cand_states[cand * S + s];
   float running = 0.0f;
+  int crash = 0;
   for (int t = 0; t < T; ++t)
   {
     const int tc = min(t + stride, T - 1);
     float u[C], xn[S];
 #pragma unroll
-    for (int c = 0; c < C; ++c)
-      u[c] = enforce_constraint(row[tc * C + c], a.sh.lower[c], a.sh.upper[c], a.sh.deadband[c], a.sh.zero[c]);
-    euler_step<Model>(dp, x, u, xn, a.dt);
-    float c = Model::computeStateCost(cp, a.aux, xn, t) + Model::computeControlCost(cp, u, t);
+    for (int c = 0; c < C; ++c) u[c] = row[tc * C + c];
+    rmppi_constrain<Model>(a, dp, x, u);
+    float c = rmppi_step<Model>(a, dp, cp, x, u, xn, y, t, &crash);
     // the likelihood term of sample g (its index among the evaluation rollouts) against the mean at step t
     if (a.use_likelihood) c += likelihood_ratio_cost<C>(a, a.d, g, u, t);
     running += c;
@@ -188,7 +233,7 @@ __global__ void __launch_bounds__(64) rmppi_eval_kernel(const __grid_constant__ 
     for (int s = 0; s < S; ++s) x[s] = xn[s];
   }
   const float Tf = (float)T;
-  a.costs[g] = running / Tf + Model::terminalCost(cp, a.aux, x) / Tf;
+  a.costs[g] = running / Tf + rmppi_terminal<Model>(a, cp, y) / Tf;
 }
 
 }  // namespace mg

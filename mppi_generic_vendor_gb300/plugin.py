@@ -5,7 +5,8 @@ linked against libmppi_gb.so (the engine is instantiated over the plugin pair in
 own compile flags).  ``PluginLibrary(path, name)`` loads it; ``PluginDynamics`` / ``PluginCost`` hold the plugin
 structs as ctypes structures whose fields mirror the C++ structs; ``PluginMPPIController`` is a
 ``BatchedMPPIController`` whose handle the plugin library's ``name_create`` made — every other method is the
-same C entry point as for the built-in models.
+same C entry point as for the built-in models; ``PluginTubeMPPIController`` and ``PluginRobustMPPIController`` are
+the Tube-MPPI and R-MPPI controllers over a plugin pair (the reference's controllers take any Dynamics / Cost pair).
 """
 from __future__ import annotations
 
@@ -15,7 +16,7 @@ from pathlib import Path
 
 from . import _abi as A
 from . import build as B
-from .controller import BatchedMPPIController, _Plugin
+from .controller import BatchedMPPIController, RobustMPPIController, TubeMPPIController, _Plugin
 
 INCLUDE = B.INCLUDE
 
@@ -110,3 +111,14 @@ class PluginMPPIController(BatchedMPPIController):
                    C.sizeof(dyn_t) * self.num_instances, C.cast(self._cost_arr, C.c_void_p),
                    C.sizeof(cost_t) * self.num_instances, init, C.c_void_p(stream or None), C.byref(h))
         return h
+
+
+class PluginTubeMPPIController(PluginMPPIController, TubeMPPIController):
+    """TubeMPPIController over a plugin pair: TubeMPPIController's constructor and methods, the plugin library's
+    handle."""
+
+
+class PluginRobustMPPIController(PluginMPPIController, RobustMPPIController):
+    """RobustMPPIController over a plugin pair: RobustMPPIController's constructor and methods, the plugin library's
+    handle.  Both R-MPPI rollouts run the plugin's own step, its computeRunningCost with each system's crash flag and
+    its own enforceConstraints when it defines one."""

@@ -1298,10 +1298,43 @@ int orc_tube_compute_control(int model, const void* dyn, const void* cost, const
 
 namespace orc
 {
+// One step's control constraint for the robust controller's rollouts: the plugin-test pair's own enforceConstraints
+// with the state when it has one, else the deadband and clamp (Dynamics::enforceConstraints, dynamics.cu:107-126).
+template <class Model>
+static void rm_constrain(const Model& m, const float* x, float* u, const mppi_control_constraints& cc)
+{
+  if constexpr (HasCrash<Model>::value)
+    if (m.lim)
+    {
+      m.constrain(x, u);
+      return;
+    }
+  for (int c = 0; c < Model::C; ++c) u[c] = enforce_constraint(u[c], cc, c);
+}
+
+// One step x -> xn and its running cost on the stepped state: the plugin-test pair's own step and computeRunningCost
+// with the system's crash flag, else the Euler step and state + control cost.
+template <class Model>
+static float rm_step(const Model& m, const float* x, const float* u, float* xn, int t, float dt, int* crash)
+{
+  if constexpr (HasCrash<Model>::value)
+  {
+    m.step(x, u, xn, dt);
+    return m.running_cost(xn, u, t, crash);
+  }
+  else
+  {
+    float xd[MPPI_MAX_STATE_DIM];
+    m.deriv(x, u, xd);
+    for (int s = 0; s < Model::S; ++s) xn[s] = fmaf(xd[s], dt, x[s]);
+    return m.state_cost(xn, t) + m.control_cost(u, t);
+  }
+}
+
 // rolloutRMPPIKernel (rmppi_kernels.cu:666-861) for samples [kb, ke): per step the nominal system's sample,
 // constrained and written back; the real system's sample plus the feedback K_t (x_real - x_nominal) (the whole
 // product, as DDPFeedback::k_ forms it, ddp.cuh:139-146), constrained and written back; Euler steps; running costs
-// on the stepped states.  The real system pays running + likelihood; the nominal one 0.5 J_nom + 0.5 max(min(J_fb,
+// on the stepped states (each system with its own crash flag for the plugin-test pair).  The real system pays running + likelihood; the nominal one 0.5 J_nom + 0.5 max(min(J_fb,
 // threshold), J_nom) + likelihood_nom, J_fb the real running cost plus the feedback cost (computeFeedbackCost,
 // gaussian.cu:577-630); all divided by T, terminal costs added before.
 template <class Model>
@@ -1323,34 +1356,27 @@ static void rmppi_rollout_range(const Model& m, const float* x0n, const float* x
       xr[s] = x0r[s];
     }
     float run_n = 0.0f, lik_n = 0.0f, run_r = 0.0f, extra_r = 0.0f;
+    int crash_n = 0, crash_r = 0;
     for (int t = 0; t < T; ++t)
     {
       float* un = un_all + ((size_t)k * T + t) * C;
       float* ur = ur_all + ((size_t)k * T + t) * C;
       float u_n[MPPI_MAX_CONTROL_DIM], u_r[MPPI_MAX_CONTROL_DIM], fb[MPPI_MAX_CONTROL_DIM];
-      float xn2[MPPI_MAX_STATE_DIM], xr2[MPPI_MAX_STATE_DIM], xd[MPPI_MAX_STATE_DIM];
-      for (int c = 0; c < C; ++c)
-      {
-        u_n[c] = enforce_constraint(un[c], cc, c);
-        un[c] = u_n[c];
-      }
+      float xn2[MPPI_MAX_STATE_DIM], xr2[MPPI_MAX_STATE_DIM];
+      for (int c = 0; c < C; ++c) u_n[c] = un[c];
+      rm_constrain(m, xn, u_n, cc);
+      for (int c = 0; c < C; ++c) un[c] = u_n[c];
       for (int r = 0; r < C; ++r)
       {
         float acc = 0.0f;
         for (int c = 0; c < S; ++c) acc += gains[(size_t)t * C * S + r + (size_t)c * C] * (xr[c] - xn[c]);
         fb[r] = acc;
       }
-      for (int c = 0; c < C; ++c)
-      {
-        u_r[c] = enforce_constraint(ur[c] + fb[c], cc, c);
-        ur[c] = u_r[c];
-      }
-      m.deriv(xn, u_n, xd);
-      for (int s = 0; s < S; ++s) xn2[s] = fmaf(xd[s], dt, xn[s]);
-      m.deriv(xr, u_r, xd);
-      for (int s = 0; s < S; ++s) xr2[s] = fmaf(xd[s], dt, xr[s]);
-      const float cn = m.state_cost(xn2, t) + m.control_cost(u_n, t);
-      const float cr = m.state_cost(xr2, t) + m.control_cost(u_r, t);
+      for (int c = 0; c < C; ++c) u_r[c] = ur[c] + fb[c];
+      rm_constrain(m, xr, u_r, cc);
+      for (int c = 0; c < C; ++c) ur[c] = u_r[c];
+      const float cn = rm_step(m, xn, u_n, xn2, t, dt, &crash_n);
+      const float cr = rm_step(m, xr, u_r, xr2, t, dt, &crash_r);
       run_n += cn;
       if (use_likelihood)
       {
@@ -1402,16 +1428,16 @@ static void rmppi_eval_range(const Model& m, const float* cand, const int* strid
   for (int g = gb; g < ge; ++g)
   {
     const int ci = g / per_cand, j = g - ci * per_cand, stride = strides[ci];
-    float x[MPPI_MAX_STATE_DIM], xn[MPPI_MAX_STATE_DIM], xd[MPPI_MAX_STATE_DIM], u[MPPI_MAX_CONTROL_DIM];
+    float x[MPPI_MAX_STATE_DIM], xn[MPPI_MAX_STATE_DIM], u[MPPI_MAX_CONTROL_DIM];
     for (int s = 0; s < S; ++s) x[s] = cand[(size_t)ci * S + s];
     float running = 0.0f;
+    int crash = 0;
     for (int t = 0; t < T; ++t)
     {
       const int tc = std::min(t + stride, T - 1);
-      for (int c = 0; c < C; ++c) u[c] = enforce_constraint(samples[((size_t)j * T + tc) * C + c], cc, c);
-      m.deriv(x, u, xd);
-      for (int s = 0; s < S; ++s) xn[s] = fmaf(xd[s], dt, x[s]);
-      float c = m.state_cost(xn, t) + m.control_cost(u, t);
+      for (int c = 0; c < C; ++c) u[c] = samples[((size_t)j * T + tc) * C + c];
+      rm_constrain(m, x, u, cc);
+      float c = rm_step(m, x, u, xn, t, dt, &crash);
       if (use_likelihood) c += likelihood_cost<float>(u, mean + (size_t)t * C, sp, C, g, K, lambda, alpha);
       running += c;
       for (int s = 0; s < S; ++s) x[s] = xn[s];
@@ -1420,7 +1446,11 @@ static void rmppi_eval_range(const Model& m, const float* cand, const int* strid
   }
 }
 
-static bool rmppi_model(int model) { return model >= MPPI_MODEL_CARTPOLE && model <= MPPI_MODEL_BICYCLE_SLIP; }
+static bool rmppi_model(int model)
+{
+  return (model >= MPPI_MODEL_CARTPOLE && model <= MPPI_MODEL_BICYCLE_SLIP) ||
+         (model >= kTestPluginEuler && model <= kTestPluginConstrained);
+}
 }  // namespace orc
 
 extern "C" {
@@ -1443,9 +1473,8 @@ int orc_rmppi_rollout(int model, const void* dyn, const void* cost, const float*
     if (kb >= ke) break;
     pool.emplace_back([&, kb, ke]() {
       orc::with_model<float>(b, [&](auto& m) {
-        if constexpr (!orc::HasCrash<std::decay_t<decltype(m)>>::value)
-          orc::rmppi_rollout_range(m, x0_nom, x0_real, samples_nom, samples_real, mean_nom, mean_real, gains, *sp,
-                                   *cc, lambda, alpha, threshold, K, T, dt, kb, ke, costs_nom, costs_real);
+        orc::rmppi_rollout_range(m, x0_nom, x0_real, samples_nom, samples_real, mean_nom, mean_real, gains, *sp, *cc,
+                                 lambda, alpha, threshold, K, T, dt, kb, ke, costs_nom, costs_real);
       });
     });
   }
@@ -1462,9 +1491,8 @@ int orc_rmppi_eval(int model, const void* dyn, const void* cost, const float* ma
   if (!orc::rmppi_model(model)) return 1;
   orc::ModelBlob b{ model, dyn, cost, { map, map_w, map_h, map_res, map_ox, map_oy } };
   orc::with_model<float>(b, [&](auto& m) {
-    if constexpr (!orc::HasCrash<std::decay_t<decltype(m)>>::value)
-      orc::rmppi_eval_range(m, cand_states, cand_strides, per_cand, samples, mean, *sp, *cc, lambda, alpha, K, T, dt,
-                            0, num_cand * per_cand, costs_out);
+    orc::rmppi_eval_range(m, cand_states, cand_strides, per_cand, samples, mean, *sp, *cc, lambda, alpha, K, T, dt, 0,
+                          num_cand * per_cand, costs_out);
   });
   return 0;
 }

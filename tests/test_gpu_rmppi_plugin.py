@@ -8,7 +8,9 @@ samples cross, cost.cuh:221-222) and, for di_constrained_quadratic, its own enfo
   * a solve: the coupled rollout's costs and the written-back samples bit-identical to the oracle's; the sequences
     within 1e-5 of their term magnitude; the nominal state trajectory bit-identical;
   * a second update: candidates, strides, evaluation costs bit for bit, free energies, the chosen candidate and the
-    slid nominal sequence."""
+    slid nominal sequence.
+TubeMPPIController over the same crash-wall pair (tube_mppi_controller.cu:158-296) against the oracle's Tube-MPPI
+iteration: both distributions' costs bit for bit, baselines, the nominal-state decision and both sequences."""
 import numpy as np
 import pytest
 
@@ -17,8 +19,10 @@ import _plugins
 import oracle
 from oracle import ddp as oddp
 from mppi_generic_vendor_gb300 import DDPFeedback, DDPParams, GaussianDistribution
-from mppi_generic_vendor_gb300.plugin import PluginCost, PluginDynamics, PluginLibrary, PluginRobustMPPIController
+from mppi_generic_vendor_gb300.plugin import (PluginCost, PluginDynamics, PluginLibrary, PluginRobustMPPIController,
+                                              PluginTubeMPPIController)
 from test_gpu_rmppi import _line_weights
+from test_gpu_tube import _check as _check_tube
 
 pytestmark = pytest.mark.gpu
 
@@ -150,4 +154,25 @@ def test_plugin_rmppi_update_solve_update_matches_oracle(plugin_path, name, thre
     assert np.array_equal(ctrl.getNominalState(), cand[exp_best])
     slid = oracle.slide(u_prev, int(stride), np.zeros(2, np.float32), np.zeros(2, np.float32))
     assert np.array_equal(ctrl.getNominalControlSeq().T, slid)
+    ctrl.close()
+
+
+@pytest.mark.parametrize("threshold", [20.0, -1e9])
+def test_plugin_tube_matches_oracle(plugin_path, threshold):
+    lib = PluginLibrary(plugin_path, "di_quadratic")
+    dyn = PluginDynamics(lib, _plugins.DIPlugin(0.3))
+    dyn.setControlRanges([(-2.0, 2.0), (-2.0, 2.0)])
+    ctrl = PluginTubeMPPIController(dyn, PluginCost(lib, _cost(0.45)), None, GaussianDistribution(std_dev=(SD, SD)),
+                                    DT, 1, 1.0, 0.0, T, K, nominal_threshold=threshold)
+    rng = np.random.default_rng(5)
+    init = rng.uniform(-0.5, 0.5, (T, 2)).astype(np.float32)
+    ctrl.setControlSeq(init.T)
+    e = rng.standard_normal(K * T * 2).astype(np.float32)
+    ctrl.injectNoise(np.concatenate([e, rng.standard_normal(K * T * 2).astype(np.float32)]))
+    x = np.array([0.1, -0.05, 0.9, 0.1], np.float32)
+    ctrl.computeControl(x, 1)
+    ref = oracle.tube_compute_control(_plugins.ORACLE_MODEL["di_quadratic"], ctrl._dyn_arr[0], ctrl._cost_arr[0],
+                                      ctrl.getParams(), ctrl.sampler_.to_c(), ctrl.constraints_, K, T, 2, 4, x, x,
+                                      np.concatenate([e, e]), np.stack([init, init]))
+    _check_tube(ctrl, ref, K, T)
     ctrl.close()

@@ -7,42 +7,65 @@ rolloutRMPPIKernel and initEvalKernel, rmppi_kernels.cu:231-357, 666-861), given
     are bit-identical to the oracle's; the updated and smoothed sequences are within 1e-5 of their term magnitude;
   * a second update: candidate states and strides on the line search, the evaluation rollouts' costs bit for bit,
     the free energies, the chosen candidate (all below the threshold: the last; none: the previous choice), the nominal
-    sequence slid by the chosen stride and the new gains."""
+    sequence slid by the chosen stride and the new gains.
+Models: the double integrator with an obstacle, the cart-pole, the kinematic bicycle on a costmap (the costmap lookup
+inside both R-MPPI kernels) and the 7-state dynamic bicycle on the same costmap."""
 import numpy as np
 import pytest
 
 import _parity
 import oracle
 from _ddp import engine_gains
-from mppi_generic_vendor_gb300 import (CartpoleDynamics, CartpoleSwingupCost, DDPFeedback, DDPParams,
-                                       DoubleIntegratorDynamics, DoubleIntegratorObstacleCost, GaussianDistribution,
-                                       RobustMPPIController)
+from mppi_generic_vendor_gb300 import (BicycleDynamics, BicycleSlipDynamics, CartpoleDynamics, CartpoleSwingupCost,
+                                       CostmapCost, DDPFeedback, DDPParams, DoubleIntegratorDynamics,
+                                       DoubleIntegratorObstacleCost, GaussianDistribution, RobustMPPIController)
 from mppi_generic_vendor_gb300 import _abi as A
+from mppi_generic_vendor_gb300.workloads import gaussian_bump_costmap
 
 pytestmark = pytest.mark.gpu
 
 K, T, DT, N, J = 1024, 40, 0.02, 5, 32
-Q = np.diag([4.0, 4.0, 1.0, 1.0]).astype(np.float32)
+CMAP = gaussian_bump_costmap(3, size=128)  # 12.8 m square at 0.1 m cells
 
-# (model id, dynamics, cost, control bound, std dev, likelihood coefficient, x, disturbance, second state)
+
+def _costmap_cost():
+    return CostmapCost(map_coeff=1.0, speed_target=8.0, speed_coeff=1.0, steer_coeff=0.5, terminal_coeff=2.0,
+                       costmap=CMAP, resolution=0.1, origin=(0.0, 0.0))
+
+
+# (model id, dynamics, cost, control ranges, std dev, likelihood coefficient, x, disturbance, second state)
 MODELS = {
     "double_integrator": (A.MODEL_DOUBLE_INTEGRATOR, DoubleIntegratorDynamics,
                           lambda: DoubleIntegratorObstacleCost(goal=(1.5, -0.5, 0.0, 0.0), coeff=(1.0, 1.0, 0.1, 0.1),
                                                                terminal_coeff=5.0, obstacles=[(0.7, 0.0, 0.3)],
                                                                obstacle_cost=100.0),
-                          2.0, 0.6, 0.3, [0.1, -0.05, 0.3, 0.1], [0.05, -0.03, 0.1, 0.05], [0.16, -0.1, 0.35, 0.02]),
-    "cartpole": (A.MODEL_CARTPOLE, CartpoleDynamics, lambda: CartpoleSwingupCost(), 5.0, 1.0, 0.2,
+                          [(-2.0, 2.0)] * 2, 0.6, 0.3, [0.1, -0.05, 0.3, 0.1], [0.05, -0.03, 0.1, 0.05],
+                          [0.16, -0.1, 0.35, 0.02]),
+    "cartpole": (A.MODEL_CARTPOLE, CartpoleDynamics, lambda: CartpoleSwingupCost(), [(-5.0, 5.0)], 1.0, 0.2,
                  [0.0, 0.1, 2.6, -0.2], [0.02, -0.05, 0.08, 0.1], [0.05, 0.0, 2.7, 0.3]),
+    "bicycle_costmap": (A.MODEL_BICYCLE_COSTMAP, lambda: BicycleDynamics(2.5), _costmap_cost, [(-3.0, 3.0), (-1.0, 1.0)],
+                        0.5, 0.2, [6.0, 5.0, 0.4, 4.0], [0.1, -0.08, 0.05, 0.3], [6.3, 5.2, 0.38, 4.4]),
+    "bicycle_slip": (A.MODEL_BICYCLE_SLIP, BicycleSlipDynamics, _costmap_cost, [(-3.0, 3.0), (-0.5, 0.5)], 0.4, 0.2,
+                     [6.0, 5.0, 0.2, 6.0, 0.0, 0.0, 0.0], [0.1, -0.05, 0.02, 0.2, 0.05, 0.01, 0.0],
+                     [6.3, 5.1, 0.22, 6.2, 0.02, 0.01, 0.0]),
 }
 
 
+def _Q(S):
+    return np.diag([4.0, 4.0, 1.0, 1.0] + [1.0] * (S - 4)).astype(np.float32)
+
+
+def _map(name):
+    return (CMAP, 0.1, (0.0, 0.0)) if name.startswith("bicycle") else None
+
+
 def _controller(name, threshold):
-    mid, dyn_cls, cost_fn, bound, sd, coeff = MODELS[name][:6]
+    mid, dyn_cls, cost_fn, ranges, sd, coeff = MODELS[name][:6]
     dyn = dyn_cls()
     Cd = dyn.CONTROL_DIM
-    dyn.setControlRanges([(-bound, bound)] * Cd)
+    dyn.setControlRanges(ranges)
     fb = DDPFeedback(dyn, DT)
-    fb.setParams(DDPParams(Q, None, 0.5 * np.eye(Cd, dtype=np.float32), 1))
+    fb.setParams(DDPParams(_Q(dyn.STATE_DIM), None, 0.5 * np.eye(Cd, dtype=np.float32), 1))
     sampler = GaussianDistribution(std_dev=(sd,) * Cd, control_cost_coeff=(coeff,) * Cd)
     init = np.random.default_rng(2).uniform(-0.3, 0.3, (Cd, T)).astype(np.float32)
     return RobustMPPIController(dyn, cost_fn(), fb, sampler, DT, 1, 1.0, 0.0, threshold, T, K, init_control_traj=init,
@@ -57,8 +80,9 @@ def _gains(ctrl):
 def _check_gains(ctrl, x):
     Cd = ctrl.Cdim
     lo, hi = np.array(ctrl.constraints_.lower[:Cd], np.float32), np.array(ctrl.constraints_.upper[:Cd], np.float32)
+    S = ctrl.S
     st, host = engine_gains(ctrl.model_id, ctrl._dyn_arr[0], x, ctrl.getTargetStateSeq().T.copy(),
-                            ctrl.getNominalControlSeq().T.copy(), DT, Q, np.eye(4, dtype=np.float32),
+                            ctrl.getNominalControlSeq().T.copy(), DT, _Q(S), np.eye(S, dtype=np.float32),
                             0.5 * np.eye(Cd, dtype=np.float32), 1, lo, hi)
     assert st == A.MPPI_OK
     got = _gains(ctrl)
@@ -103,7 +127,7 @@ def test_rmppi_update_solve_update_matches_oracle(name, threshold):
     raw = oracle.gaussian_rewrite(eps, u_nom, sd, K, T, Cd, 1)
     cn, cr, un, ur = oracle.rmppi_rollout(mid, dyn, cost, x_nom, x_real, raw, raw, u_nom, u_nom,
                                           gains.transpose(0, 2, 1).reshape(T, -1), sp, cc, 1.0, 0.0, threshold, K,
-                                          T, DT)
+                                          T, DT, costmap=_map(name))
     costs = ctrl.sample_costs().reshape(2, K)
     assert np.array_equal(costs[0].view(np.uint32), cn.view(np.uint32))
     assert np.array_equal(costs[1].view(np.uint32), cr.view(np.uint32))
@@ -127,6 +151,7 @@ def test_rmppi_update_solve_update_matches_oracle(name, threshold):
     p = ctrl.getTargetStateSeq().T.copy()
     u_prev = ctrl.getNominalControlSeq().T.copy()
     x2 = np.array(MODELS[name][8], np.float32)
+    S = ctrl.S
     ctrl.updateImportanceSamplingControl(x2, 1)
     best, stride, cand, strides, fe, evc = ctrl._candidates()
     w = _line_weights(N)
@@ -136,7 +161,8 @@ def test_rmppi_update_solve_update_matches_oracle(name, threshold):
     exp_strides = np.floor(((np.float32(0) * w[0] + np.float32(1) * w[1]) + np.float32(1) * w[2]) + 0.5).astype(np.int32)
     assert np.array_equal(strides, exp_strides)
     raw_eval = oracle.gaussian_rewrite(eps, u_prev, sd, K, T, Cd, 1)
-    ref_eval = oracle.rmppi_eval(mid, dyn, cost, cand, strides, J, raw_eval, u_prev, sp, cc, 1.0, 0.0, K, T, DT)
+    ref_eval = oracle.rmppi_eval(mid, dyn, cost, cand, strides, J, raw_eval, u_prev, sp, cc, 1.0, 0.0, K, T, DT,
+                                 costmap=_map(name))
     assert np.array_equal(evc.view(np.uint32), ref_eval.view(np.uint32))
     # computeBestIndex: exponentials in FP32 (a candidate whose samples all lie far above the best one sums to zero
     # and gets an infinite free energy), the last candidate below the threshold, else the previous choice (0)

@@ -11,6 +11,11 @@ A step is one MPPI iteration (sample -> rollout -> weights -> update) over every
 * cpu_baseline — the CPU oracle (a restatement of the reference's host rollout + weight + update path) on a bounded
   sample of the same workload, all host threads.
 
+``--workload cartpole_rmppi`` times the robust controller (R-MPPI), a host-iterated controller: every iteration runs
+the importance-sampler update (candidate evaluation kernel, free energies and the DDP gains on the host) and the solve
+through the public calls, so its line reports the end-to-end rate as `value` too, with the solve's kernel times
+beside it.
+
 Multi-GPU: the path does not shard across GPUs; ``--gpus N`` under torchrun runs N independent replicas (weak scaling).
 ``--impl reference`` times the reference's CPU path (the oracle port) and prints its own line.
 """
@@ -45,7 +50,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched_slip_mlp", choices=["batched_di", "cartpole", "bicycle",
                                                                  "batched_di_gaussian", "slip_mlp",
-                                                                 "batched_slip_mlp"])
+                                                                 "batched_slip_mlp", "cartpole_rmppi"])
     ap.add_argument("--precision", default=None, choices=["bf16", "fp8", "fp32"],
                     help="surrogate workloads: weight precision (default bf16 for slip_mlp, fp8 for batched_slip_mlp)")
     ap.add_argument("--instances", type=int, default=256, help="batched workloads: number of instances")
@@ -145,6 +150,8 @@ def build_workload(name, seed, stream, instances=256, precision=None, params=Non
         return W.batched_di(num_instances=instances, colored=False, **kw)
     if name == "cartpole":
         return W.cartpole(**kw)
+    if name == "cartpole_rmppi":
+        return W.cartpole_rmppi(**kw)
     return W.bicycle(**kw)
 
 
@@ -353,6 +360,47 @@ def cpu_baseline(name, seed, budget_s):
             i += 1
         inst_done = i
         sample = f"{inst_done} of 256 instances (sum K*T = {done_steps}), one iteration each"
+    elif name == "cartpole_rmppi":
+        # one R-MPPI iteration on the host: the candidate evaluation (9 x 64 rollouts), the coupled rollout of both
+        # systems (2 x 2048), weights and the weighted mean of both distributions, and the DDP gains of the
+        # importance-sampler update.  The gains come from the engine's host DDP solver (mppi_ddp_feedback_gains),
+        # the same host code the GPU arm runs between its launches.
+        import ctypes as C
+
+        K, T, N, J = 2048, 100, 9, 64
+        dyn, cost = A.CartpoleParams(1, 1, 1, 9.81), A.CartpoleCostParams(10, 1, 100, 1, 0)
+        sp = A.default_sampling_params(native=False)
+        sp.std_dev[0] = 1.0
+        cc = A.default_constraints(native=False)
+        cc.lower[0], cc.upper[0] = -5.0, 5.0
+        x0 = np.array([0.0, 0.0, 1.0, 0.0], np.float32)
+        u = np.zeros((T, 1), np.float32)
+        xt = np.repeat(x0[None], T, axis=0)
+        cand = np.repeat(x0[None], N, axis=0)
+        strides = np.zeros(N, np.int32)
+        gains = np.zeros(T * 4, np.float32)
+        eye4, eye1 = np.eye(4, dtype=np.float32), np.eye(1, dtype=np.float32)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        lo, hi = np.array([-5.0], np.float32), np.array([5.0], np.float32)
+        while elapsed < budget_s and iters < 200:
+            eps = rng.standard_normal(K * T).astype(np.float32)
+            raw = (eps * np.float32(1.0) + np.tile(u.reshape(-1), K)).astype(np.float32)
+            t0 = time.perf_counter()
+            oracle.rmppi_eval(A.MODEL_CARTPOLE, dyn, cost, cand, strides, J, raw, u, sp, cc, 1.0, 0.0, K, T, 0.02)
+            A.lib().mppi_ddp_feedback_gains(A.MODEL_CARTPOLE, C.cast(C.pointer(dyn), C.c_void_p), C.sizeof(dyn), T,
+                                            0.02, fp(x0), fp(xt), fp(u), fp(eye4), fp(eye4), fp(eye1), 1, fp(lo),
+                                            fp(hi), fp(gains))
+            cn, cr, un, ur = oracle.rmppi_rollout(A.MODEL_CARTPOLE, dyn, cost, x0, x0, raw, raw, u, u,
+                                                  np.tile(gains.reshape(T, 4), 1), sp, cc, 1.0, 0.0, 1000.0, K, T,
+                                                  0.02, threads=threads)
+            for c, smp in ((cn, un), (cr, ur)):
+                w, _, n = oracle.weights(c, lambda_inv=np.float32(1.0))
+                mean, _ = oracle.weighted_mean(w, np.float32(n), smp, K, T, 1)
+            elapsed += time.perf_counter() - t0
+            u = mean.astype(np.float32).reshape(T, 1)
+            done_steps += 2 * K * T + N * J * T
+            iters += 1
+        sample = f"{iters} R-MPPI iterations of K=2048 x 2, T=100, 9 x 64 evaluation rollouts"
     elif name in ("slip_mlp", "batched_slip_mlp"):
         # the surrogate model in FP32 on the host (the oracle's restatement of the GPU rollout), same shapes
         params = surrogate_params()
@@ -598,6 +646,85 @@ def run_gpu(args, ws, rank, local):
         dist.destroy_process_group()
 
 
+def run_rmppi(args, ws, rank, local):
+    """The robust controller's iteration (updateImportanceSamplingControl + computeControl, host buffers) timed end to
+    end, the solve's kernels (sampler, coupled rollout, weights + update) timed with CUDA events on its stream."""
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from mppi_generic_vendor_gb300 import build as B
+
+    B.build()
+    stream = torch.cuda.Stream()
+    wl = build_workload(args.workload, seed=0, stream=stream.cuda_stream)
+    ctrl, x0 = wl.controller, wl.x0
+
+    def iteration():
+        ctrl.updateImportanceSamplingControl(x0, 1)
+        ctrl.computeControl(x0, 1)
+        return ctrl.getControlSeq()
+
+    for _ in range(max(args.warmup, 3)):
+        iteration()
+    if args.steps is None:
+        t0 = time.perf_counter()
+        for _ in range(3):
+            iteration()
+        args.steps = int(min(5000, max(20, np.ceil(1.2 / ((time.perf_counter() - t0) / 3)))))
+        args.steps = int(max_over_ranks(args.steps, dist))
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        u = iteration()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    clk = clocks.stop()
+    steps_per_iter = wl.sample_steps_per_iter
+    e2e = whole_job_rate(steps_per_iter * args.steps, e2e_s, ws)
+    kms = [float(v) for v in ctrl.timeKernels(1, reps=10)]
+    K, T = int(wl.K[0]), int(wl.T[0])
+    S, Cd = wl.state_dim, wl.control_dim
+    # the coupled rollout reads and writes both distributions' samples, writes 2 K costs and reads the gains
+    abytes = 2 * (8 * K * T * Cd) + 8 * K + 4 * T * Cd * S
+    peak, peak_kind = measured_peaks()
+    achieved = abytes / (kms[1] * 1e-3) / 1e9
+    h2d = 4 * (2 * S + 2 * T * Cd + T * Cd * S) + 4 * S
+    d2h = 4 * 2 * T * Cd + 4 * 9 * 64 + u.nbytes
+    line = {
+        "metric": METRIC, "value": e2e, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * e2e_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded; shapes of the benchmark configuration)",
+        "config": config_of(wl, ws), "host_iterated": True,
+        "iters_per_s": args.steps / e2e_s,
+        "kernel_ms": {"sampler": kms[0], "rollout": kms[1], "update": kms[2]},
+        "roofline": {"bound": "hbm", "kernel": "rmppi_rollout_kernel (one thread per sample, latency-bound chain)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes": abytes},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "iters_per_s": ws * args.steps / e2e_s},
+        # the solve's kernels plus the update's sampler, candidate evaluation and counter bump
+        "gpu_launches": (ctrl.kernelsPerCompute() + 3) * args.steps,
+    }
+    if clk:
+        line["clocks"] = clk
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.workload, 0, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctrl.close()
+    if dist:
+        dist.destroy_process_group()
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -631,6 +758,9 @@ def main():
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.workload == "cartpole_rmppi":
+        run_rmppi(args, ws, rank, local)
         return
     run_gpu(args, ws, rank, local)
 

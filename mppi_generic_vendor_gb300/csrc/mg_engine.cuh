@@ -998,6 +998,7 @@ public:
 
   mppi_status launch_rmppi_rollout()
   {
+    MG_CHECK(fb_gains_d_.p != nullptr, "the R-MPPI rollout needs a solve first (mppi_compute_control uploads its gains)");
     RmppiArgs<Model> a{};
     a.inst = inst_d_.p;
     a.samples = samples_d_.p;
@@ -1017,7 +1018,8 @@ public:
     a.use_likelihood = 0;
     for (int c = 0; c < C; ++c)
       if (sp_.control_cost_coeff[c] != 0.0f) a.use_likelihood = 1;
-    rmppi_rollout_kernel<Model><<<(K_[0] + 127) / 128, 128, 0, stream_>>>(a);
+    // two lanes per sample (nominal, real)
+    rmppi_rollout_kernel<Model><<<(2 * K_[0] + 127) / 128, 128, 0, stream_>>>(a);
     MG_CUDA(cudaGetLastError());
     return MPPI_OK;
   }

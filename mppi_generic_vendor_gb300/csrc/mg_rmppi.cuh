@@ -1,8 +1,8 @@
 // mg_rmppi.cuh — the two kernels of the robust controller (R-MPPI):
 //  * rmppi_rollout_kernel: rolloutRMPPIKernel (rmppi_kernels.cu:666-861).  The reference runs the nominal and the real
-//    system of a sample as two threads (threadIdx.z) sharing the nominal state through shared memory; here one thread
-//    runs both in lockstep, so the real system's feedback K_t (x_real - x_nominal) sees the nominal state of the same
-//    step in registers.  Both controls pass through the constraints (deadband, clamp) every step and are written back
+//    system of a sample as two threads (threadIdx.z) sharing the nominal state through shared memory; here they are
+//    two neighbouring lanes of a warp, so the real system's feedback K_t (x_real - x_nominal) reads the nominal state
+//    of the same step by a register shuffle.  Both controls pass through the constraints (deadband, clamp) every step and are written back
 //    as the samples the update averages.  Costs (running cost on the stepped state, likelihood-ratio term, terminal
 //    cost, all divided by T): the real system pays running + likelihood; the nominal one
 //        0.5 J_nom + 0.5 max(min(J_real_fb, threshold), J_nom) + likelihood_nom,
@@ -13,6 +13,8 @@
 //    candidate c from its state with the samples of the nominal distribution read at t + stride_c (held at T-1).
 // Both run the built-in models and a caller's plugin pair (its own step, computeRunningCost with the sample's crash
 // flag, and its own enforceConstraints when it defines one).  One thread per sample, no shared memory and no waits.
+// The evaluation's time loop issues each step's sample load kPrefetch steps ahead into a register ring (the loop runs
+// in unrolled groups of kPrefetch steps so every ring slot is a fixed register).
 #pragma once
 
 #include "mg_kernels.cuh"
@@ -23,6 +25,8 @@ namespace mg
 
 // One increment of a device counter (the Philox noise counter after the candidate evaluation's sampling).
 static __global__ void bump_u32_kernel(unsigned int* p) { *p += 1u; }
+
+constexpr int kPrefetch = 4;  // steps between a load and its use
 
 template <class Model>
 struct RmppiArgs
@@ -101,87 +105,99 @@ __device__ __forceinline__ float feedback_cost(const Args& a, const float* fb)
   return 0.5f * a.lambda * (1.0f - a.alpha) * c;
 }
 
+// Lane 2i of a warp runs sample k's nominal system and lane 2i + 1 its real system (the reference's threadIdx.z = 0
+// and 1): each lane carries one dependent chain of steps, and the real lane reads the nominal state of the same step
+// from its partner by a shuffle.  Pairs past K run sample K - 1 without writing anything, so that every lane of a
+// warp reaches each shuffle.
 template <class Model>
 __global__ void __launch_bounds__(128) rmppi_rollout_kernel(const __grid_constant__ RmppiArgs<Model> a)
 {
   constexpr int S = Model::STATE_DIM, C = Model::CONTROL_DIM, O = Model::OUTPUT_DIM;
+  constexpr unsigned kFull = 0xffffffffu;
   const InstDesc dn = a.inst[0], dr = a.inst[1];
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= dn.K) return;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool real = (threadIdx.x & 1) != 0;
+  const bool active = (g >> 1) < dn.K;
+  const int k = active ? (g >> 1) : dn.K - 1;
+  const int nominal_lane = (threadIdx.x & 31) & ~1;
   const int T = dn.T;
-  const typename Model::DynParams& dp = a.dyn[0];
-  const typename Model::CostParams& cp = a.cost[0];
-  float xn[S], xr[S], yn[O], yr[O];
-  int crash_n = 0, crash_r = 0;  // crash_status of each system (mppi_common.cu:85-86)
+  // the parameter blocks by value: the sample write-backs below cannot alias them
+  const typename Model::DynParams dp = a.dyn[0];
+  const typename Model::CostParams cp = a.cost[0];
+  const InstDesc d = real ? dr : dn;
+  float x[S], y[O];
+  int crash = 0;  // crash_status of this lane's system (mppi_common.cu:85-86)
 #pragma unroll
-  for (int s = 0; s < S; ++s)
-  {
-    xn[s] = a.x0[s];
-    xr[s] = a.x0[S + s];
-  }
-  float* un_row = a.samples + dn.u_off + (long long)k * T * C;
-  float* ur_row = a.samples + dr.u_off + (long long)k * T * C;
-  float run_n = 0.0f, lik_n = 0.0f, run_r = 0.0f, extra_r = 0.0f;
+  for (int s = 0; s < S; ++s) x[s] = a.x0[(real ? S : 0) + s];
+  float* row = a.samples + d.u_off + (long long)k * T * C;
+  // nominal lane: running cost and likelihood apart; real lane: running + likelihood, and running + feedback cost
+  float run = 0.0f, lik = 0.0f, extra = 0.0f;
   for (int t = 0; t < T; ++t)
   {
-    float un[C], ur[C], fb[C], xn2[S], xr2[S];
-    // the nominal system takes its sample, constrained (no feedback on the nominal system)
+    float u[C], fb[C], x2[S], xnom[S];
 #pragma unroll
-    for (int c = 0; c < C; ++c) un[c] = un_row[t * C + c];
-    rmppi_constrain<Model>(a, dp, xn, un);
+    for (int s = 0; s < S; ++s) xnom[s] = __shfl_sync(kFull, x[s], nominal_lane);
 #pragma unroll
-    for (int c = 0; c < C; ++c) un_row[t * C + c] = un[c];
-    // the real system adds the feedback against the nominal state of this step
-    const float* K = a.gains + (size_t)t * C * S;
-#pragma unroll
-    for (int r = 0; r < C; ++r)
+    for (int c = 0; c < C; ++c) u[c] = row[t * C + c];
+    if (real)
     {
-      float acc = 0.0f;
+      // the real system adds the feedback K_t (x_real - x_nominal) of this step
+      const float* K = a.gains + (size_t)t * C * S;
 #pragma unroll
-      for (int c = 0; c < S; ++c) acc += K[r + c * C] * (xr[c] - xn[c]);
-      fb[r] = acc;
+      for (int r = 0; r < C; ++r)
+      {
+        float acc = 0.0f;
+#pragma unroll
+        for (int c = 0; c < S; ++c) acc += K[r + c * C] * (x[c] - xnom[c]);
+        fb[r] = acc;
+      }
+#pragma unroll
+      for (int c = 0; c < C; ++c) u[c] = u[c] + fb[c];
     }
+    rmppi_constrain<Model>(a, dp, x, u);
+    if (active)
 #pragma unroll
-    for (int c = 0; c < C; ++c) ur[c] = ur_row[t * C + c] + fb[c];
-    rmppi_constrain<Model>(a, dp, xr, ur);
-#pragma unroll
-    for (int c = 0; c < C; ++c) ur_row[t * C + c] = ur[c];
-    const float cn = rmppi_step<Model>(a, dp, cp, xn, un, xn2, yn, t, &crash_n);
-    const float cr = rmppi_step<Model>(a, dp, cp, xr, ur, xr2, yr, t, &crash_r);
-    run_n += cn;
-    if (a.use_likelihood)
+      for (int c = 0; c < C; ++c) row[t * C + c] = u[c];
+    const float cs = rmppi_step<Model>(a, dp, cp, x, u, x2, y, t, &crash);
+    if (real)
     {
-      lik_n += likelihood_ratio_cost<C>(a, dn, k, un, t);
-      run_r += cr + likelihood_ratio_cost<C>(a, dr, k, ur, t);
+      if (a.use_likelihood)
+        run += cs + likelihood_ratio_cost<C>(a, d, k, u, t);
+      else
+        run += cs;
+      extra += cs + feedback_cost<C>(a, fb);
     }
     else
     {
-      run_r += cr;
+      run += cs;
+      if (a.use_likelihood) lik += likelihood_ratio_cost<C>(a, d, k, u, t);
     }
-    extra_r += cr + feedback_cost<C>(a, fb);
 #pragma unroll
-    for (int s = 0; s < S; ++s)
-    {
-      xn[s] = xn2[s];
-      xr[s] = xr2[s];
-    }
+    for (int s = 0; s < S; ++s) x[s] = x2[s];
   }
-  run_n += rmppi_terminal<Model>(a, cp, yn);
-  const float term_r = rmppi_terminal<Model>(a, cp, yr);
-  run_r += term_r;
-  extra_r += term_r;
+  const float term = rmppi_terminal<Model>(a, cp, y);
+  run += term;
+  if (real) extra += term;
   const float Tf = (float)T;
-  run_n /= Tf;
-  lik_n /= Tf;
-  run_r /= Tf;
-  extra_r /= Tf;
-  // 0.5 J_nom + 0.5 max(min(J_real_fb, threshold), J_nom), formed in double as the reference's double literals make it
-  float cost_n = (float)(0.5 * (double)run_n + 0.5 * (double)fmaxf(fminf(extra_r, a.value_threshold), run_n));
-  cost_n += lik_n;
-  a.costs[dn.k_off + k] = cost_n;
-  a.costs[dr.k_off + k] = run_r;
-  atomicMin(&a.baseline_bits[0], float_to_ordered(cost_n));
-  atomicMin(&a.baseline_bits[1], float_to_ordered(run_r));
+  run /= Tf;
+  lik /= Tf;
+  extra /= Tf;
+  const float extra_r = __shfl_sync(kFull, extra, nominal_lane + 1);
+  if (!active) return;
+  if (real)
+  {
+    a.costs[dr.k_off + k] = run;
+    atomicMin(&a.baseline_bits[1], float_to_ordered(run));
+  }
+  else
+  {
+    // 0.5 J_nom + 0.5 max(min(J_real_fb, threshold), J_nom), formed in double as the reference's double literals
+    // make it
+    float cost_n = (float)(0.5 * (double)run + 0.5 * (double)fmaxf(fminf(extra_r, a.value_threshold), run));
+    cost_n += lik;
+    a.costs[dn.k_off + k] = cost_n;
+    atomicMin(&a.baseline_bits[0], float_to_ordered(cost_n));
+  }
 }
 
 template <class Model>
@@ -210,20 +226,37 @@ __global__ void __launch_bounds__(64) rmppi_eval_kernel(const __grid_constant__ 
   if (g >= a.num_cand * a.per_cand) return;
   const int cand = g / a.per_cand, j = g - cand * a.per_cand;
   const int T = a.d.T, stride = a.cand_strides[cand];
-  const typename Model::DynParams& dp = a.dyn[0];
-  const typename Model::CostParams& cp = a.cost[0];
+  const typename Model::DynParams dp = a.dyn[0];
+  const typename Model::CostParams cp = a.cost[0];
   const float* row = a.samples + a.d.u_off + (long long)j * T * C;
   float x[S], y[O];
 #pragma unroll
   for (int s = 0; s < S; ++s) x[s] = a.cand_states[cand * S + s];
   float running = 0.0f;
   int crash = 0;
-  for (int t = 0; t < T; ++t)
+  // ring of the next kPrefetch steps' samples (step t reads the sample at min(t + stride, T - 1))
+  float ring[kPrefetch][C];
+#pragma unroll
+  for (int j = 0; j < kPrefetch; ++j)
   {
-    const int tc = min(t + stride, T - 1);
+    const int tc = min(j + stride, T - 1);
+#pragma unroll
+    for (int c = 0; c < C; ++c) ring[j][c] = row[tc * C + c];
+  }
+  for (int t0 = 0; t0 < T; t0 += kPrefetch)
+#pragma unroll
+  for (int j = 0; j < kPrefetch; ++j)
+  {
+    const int t = t0 + j;
+    if (t >= T) break;
     float u[C], xn[S];
 #pragma unroll
-    for (int c = 0; c < C; ++c) u[c] = row[tc * C + c];
+    for (int c = 0; c < C; ++c) u[c] = ring[j][c];
+    {
+      const int tn = min(t + kPrefetch + stride, T - 1);
+#pragma unroll
+      for (int c = 0; c < C; ++c) ring[j][c] = row[tn * C + c];
+    }
     rmppi_constrain<Model>(a, dp, x, u);
     float c = rmppi_step<Model>(a, dp, cp, x, u, xn, y, t, &crash);
     // the likelihood term of sample g (its index among the evaluation rollouts) against the mean at step t

@@ -12,6 +12,9 @@
   costmap of ``bicycle``, sigma (0.5, 0.5), lambda 2.0.
 * ``batched_slip_mlp`` — 128 surrogate instances with K ~ U[2048, 16384] and T ~ U{50, 100, 200}, FP8 E4M3 weights
   with one scale per layer, one shared costmap as in ``bicycle``.
+* ``cartpole_rmppi`` — the robust controller (R-MPPI) on the cart-pole of ``cartpole``: two distributions of K=2048
+  samples, T=100, 9 candidate nominal states with 64 evaluation samples each, value-function threshold 1000, the DDP
+  feedback with identity weights; one iteration = the importance-sampler update + the solve.
 
 There is no public dataset behind these configurations; every input is drawn from a recorded seed.
 """
@@ -23,8 +26,9 @@ import numpy as np
 
 from .controller import (BatchedMPPIController, BicycleDynamics, BicycleSlipMLPDynamics, CartpoleDynamics,
                          CartpoleSwingupCost,
-                         ColoredNoiseDistribution, CostmapCost, DoubleIntegratorDynamics,
-                         DoubleIntegratorObstacleCost, GaussianDistribution, VanillaMPPIController)
+                         ColoredNoiseDistribution, CostmapCost, DDPFeedback, DoubleIntegratorDynamics,
+                         DoubleIntegratorObstacleCost, GaussianDistribution, RobustMPPIController,
+                         VanillaMPPIController)
 
 
 @dataclass
@@ -38,10 +42,11 @@ class Workload:
     control_dim: int
     num_iters: int
     description: dict = field(default_factory=dict)
+    eval_sample_steps: int = 0  # R-MPPI: the candidate evaluation's rollout steps per iteration
 
     @property
     def sample_steps_per_iter(self) -> int:
-        return int(np.sum(self.K.astype(np.int64) * self.T))
+        return int(np.sum(self.K.astype(np.int64) * self.T)) + self.eval_sample_steps
 
     @property
     def control_floats(self) -> int:
@@ -59,6 +64,25 @@ def cartpole(seed: int = 0, K: int = 2048, T: int = 100, stream: int = 0, descri
                    rng.uniform(-0.1, 0.1)], dtype=np.float32)
     return Workload("cartpole_K2048_T100", ctrl, x0, np.array([K]), np.array([T]), 4, 1, 1,
                     dict(model="cartpole", K=K, T=T, sigma=1.0, lam=1.0, dt=0.02, seed=seed))
+
+
+def cartpole_rmppi(seed: int = 0, K: int = 2048, T: int = 100, num_candidates: int = 9, eval_samples: int = 64,
+                   stream: int = 0, describe_only: bool = False) -> Workload:
+    rng = np.random.default_rng(seed)
+    dyn = CartpoleDynamics(1.0, 1.0, 1.0, 9.81)
+    dyn.setControlRanges([(-5.0, 5.0)])
+    cost = CartpoleSwingupCost(10.0, 1.0, 100.0, 1.0, 0.0)
+    ctrl = None
+    if not describe_only:
+        ctrl = RobustMPPIController(dyn, cost, DDPFeedback(dyn, 0.02), GaussianDistribution(std_dev=(1.0,)), 0.02, 1,
+                                    1.0, 0.0, 1000.0, T, K, num_candidate_nominal_states=num_candidates,
+                                    num_eval_samples_per_candidate=eval_samples, stream=stream, seed=seed)
+    x0 = np.array([rng.uniform(-0.1, 0.1), rng.uniform(-0.1, 0.1), rng.uniform(-np.pi, np.pi),
+                   rng.uniform(-0.1, 0.1)], dtype=np.float32)
+    return Workload(f"cartpole_rmppi_K{K}x2_T{T}", ctrl, x0, np.array([K, K]), np.array([T, T]), 4, 1, 1,
+                    dict(model="cartpole", controller="R-MPPI", K=K, T=T, candidates=num_candidates,
+                         eval_samples=eval_samples, threshold=1000.0, sigma=1.0, lam=1.0, dt=0.02, seed=seed),
+                    eval_sample_steps=num_candidates * eval_samples * T)
 
 
 def batched_di_params(seed: int = 0, num_instances: int = 256):

@@ -134,15 +134,18 @@ __global__ void __launch_bounds__(128) rmppi_rollout_kernel(const __grid_constan
   float run = 0.0f, lik = 0.0f, extra = 0.0f;
   for (int t = 0; t < T; ++t)
   {
-    float u[C], fb[C], x2[S], xnom[S];
-#pragma unroll
-    for (int s = 0; s < S; ++s) xnom[s] = __shfl_sync(kFull, x[s], nominal_lane);
+    float u[C], fb[C], x2[S], xnom[S], K[C * S];
+    // this step's loads first (both lanes load the gain, the same for every lane, so that the load is issued before
+    // the shuffles rather than behind the branch)
 #pragma unroll
     for (int c = 0; c < C; ++c) u[c] = row[t * C + c];
+#pragma unroll
+    for (int i = 0; i < C * S; ++i) K[i] = a.gains[(size_t)t * C * S + i];
+#pragma unroll
+    for (int s = 0; s < S; ++s) xnom[s] = __shfl_sync(kFull, x[s], nominal_lane);
     if (real)
     {
       // the real system adds the feedback K_t (x_real - x_nominal) of this step
-      const float* K = a.gains + (size_t)t * C * S;
 #pragma unroll
       for (int r = 0; r < C; ++r)
       {

@@ -14,7 +14,7 @@ A step is one MPPI iteration (sample -> rollout -> weights -> update) over every
 ``--workload cartpole_rmppi`` times the robust controller (R-MPPI), a host-iterated controller: every iteration runs
 the importance-sampler update (candidate evaluation kernel, free energies and the DDP gains on the host) and the solve
 through the public calls, so its line reports the end-to-end rate as `value` too, with the solve's kernel times
-beside it.
+beside it.  ``--workload cartpole_tube`` does the same for Tube-MPPI (solve, feedback gains, one-step slide).
 
 Multi-GPU: the path does not shard across GPUs; ``--gpus N`` under torchrun runs N independent replicas (weak scaling).
 ``--impl reference`` times the reference's CPU path (the oracle port) and prints its own line.
@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched_slip_mlp", choices=["batched_di", "cartpole", "bicycle",
                                                                  "batched_di_gaussian", "slip_mlp",
-                                                                 "batched_slip_mlp", "cartpole_rmppi"])
+                                                                 "batched_slip_mlp", "cartpole_rmppi",
+                                                                 "cartpole_tube"])
     ap.add_argument("--precision", default=None, choices=["bf16", "fp8", "fp32"],
                     help="surrogate workloads: weight precision (default bf16 for slip_mlp, fp8 for batched_slip_mlp)")
     ap.add_argument("--instances", type=int, default=256, help="batched workloads: number of instances")
@@ -152,6 +153,8 @@ def build_workload(name, seed, stream, instances=256, precision=None, params=Non
         return W.cartpole(**kw)
     if name == "cartpole_rmppi":
         return W.cartpole_rmppi(**kw)
+    if name == "cartpole_tube":
+        return W.cartpole_tube(**kw)
     return W.bicycle(**kw)
 
 
@@ -401,6 +404,44 @@ def cpu_baseline(name, seed, budget_s):
             done_steps += 2 * K * T + N * J * T
             iters += 1
         sample = f"{iters} R-MPPI iterations of K=2048 x 2, T=100, 9 x 64 evaluation rollouts"
+    elif name == "cartpole_tube":
+        # one Tube-MPPI iteration on the host: the oracle's iteration over both distributions (rollouts, weights,
+        # updates, the nominal-state decision, smoothing, state trajectories) and the feedback gains around the
+        # nominal trajectory by the engine's host DDP solver, the same host code the GPU arm runs after its solve
+        import ctypes as C
+
+        K, T = 2048, 100
+        dyn, cost = A.CartpoleParams(1, 1, 1, 9.81), A.CartpoleCostParams(10, 1, 100, 1, 0)
+        cp = A.default_controller_params(native=False)
+        cp.dt, cp.lambda_, cp.num_iters = 0.02, 1.0, 1
+        cp.controller, cp.nominal_threshold = A.CONTROLLER_TUBE, 20.0
+        sp = A.default_sampling_params(native=False)
+        sp.std_dev[0] = 1.0
+        cc = A.default_constraints(native=False)
+        cc.lower[0], cc.upper[0] = -5.0, 5.0
+        x0 = np.array([0.0, 0.0, 1.0, 0.0], np.float32)
+        xn = x0.copy()
+        ctl = np.zeros((2, T, 1), np.float32)
+        gains = np.zeros(T * 4, np.float32)
+        eye4, eye1 = np.eye(4, dtype=np.float32), np.eye(1, dtype=np.float32)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        lo, hi = np.array([-5.0], np.float32), np.array([5.0], np.float32)
+        while elapsed < budget_s and iters < 200:
+            e = rng.standard_normal(K * T).astype(np.float32)
+            eps = np.concatenate([e, e])
+            t0 = time.perf_counter()
+            r = oracle.tube_compute_control(A.MODEL_CARTPOLE, dyn, cost, cp, sp, cc, K, T, 1, 4, x0, xn, eps, ctl,
+                                            threads=threads)
+            xt = np.ascontiguousarray(r["state_seq"][1])
+            un = np.ascontiguousarray(r["control"][1])
+            A.lib().mppi_ddp_feedback_gains(A.MODEL_CARTPOLE, C.cast(C.pointer(dyn), C.c_void_p), C.sizeof(dyn), T,
+                                            0.02, fp(x0), fp(xt), fp(un), fp(eye4), fp(eye4), fp(eye1), 1, fp(lo),
+                                            fp(hi), fp(gains))
+            elapsed += time.perf_counter() - t0
+            ctl = r["control"]
+            done_steps += 2 * K * T
+            iters += 1
+        sample = f"{iters} Tube-MPPI iterations of K=2048 x 2, T=100 (sequences not slid)"
     elif name in ("slip_mlp", "batched_slip_mlp"):
         # the surrogate model in FP32 on the host (the oracle's restatement of the GPU rollout), same shapes
         params = surrogate_params()
@@ -646,9 +687,10 @@ def run_gpu(args, ws, rank, local):
         dist.destroy_process_group()
 
 
-def run_rmppi(args, ws, rank, local):
-    """The robust controller's iteration (updateImportanceSamplingControl + computeControl, host buffers) timed end to
-    end, the solve's kernels (sampler, coupled rollout, weights + update) timed with CUDA events on its stream."""
+def run_host_iterated(args, ws, rank, local):
+    """A host-iterated controller's iteration through its public calls with host buffers, timed end to end: R-MPPI
+    (updateImportanceSamplingControl + computeControl) or Tube-MPPI (computeControl + computeFeedback + a one-step
+    slide); the solve's kernels (sampler, rollout, weights + update) timed with CUDA events on its stream."""
     import torch
 
     torch.cuda.set_device(local)
@@ -663,8 +705,16 @@ def run_rmppi(args, ws, rank, local):
     stream = torch.cuda.Stream()
     wl = build_workload(args.workload, seed=0, stream=stream.cuda_stream)
     ctrl, x0 = wl.controller, wl.x0
+    tube = args.workload == "cartpole_tube"
 
     def iteration():
+        if tube:
+            # TubeMPPIController in a receding-horizon loop: solve, feedback gains, slide by one step
+            ctrl.computeControl(x0, 1)
+            ctrl.computeFeedback(x0)
+            u = ctrl.getControlSeq()
+            ctrl.slideControlSequence(1)
+            return u
         ctrl.updateImportanceSamplingControl(x0, 1)
         ctrl.computeControl(x0, 1)
         return ctrl.getControlSeq()
@@ -693,12 +743,20 @@ def run_rmppi(args, ws, rank, local):
     kms = [float(v) for v in ctrl.timeKernels(1, reps=10)]
     K, T = int(wl.K[0]), int(wl.T[0])
     S, Cd = wl.state_dim, wl.control_dim
-    # the coupled rollout reads and writes both distributions' samples, writes 2 K costs and reads the gains
-    abytes = 2 * (8 * K * T * Cd) + 8 * K + 4 * T * Cd * S
+    if tube:
+        # the rollout of both distributions reads their samples and writes 2 K costs
+        abytes = 2 * (4 * K * T * Cd) + 8 * K
+        kname = "rollout of both distributions (one T-step chain per sample)"
+        h2d = 4 * (2 * S + 2 * T * Cd)
+        d2h = 4 * 2 * T * Cd + u.nbytes
+    else:
+        # the coupled rollout reads and writes both distributions' samples, writes 2 K costs and reads the gains
+        abytes = 2 * (8 * K * T * Cd) + 8 * K + 4 * T * Cd * S
+        kname = "rmppi_rollout_kernel (two lanes per sample, latency-bound chain)"
+        h2d = 4 * (2 * S + 2 * T * Cd + T * Cd * S) + 4 * S
+        d2h = 4 * 2 * T * Cd + 4 * 9 * 64 + u.nbytes
     peak, peak_kind = measured_peaks()
     achieved = abytes / (kms[1] * 1e-3) / 1e9
-    h2d = 4 * (2 * S + 2 * T * Cd + T * Cd * S) + 4 * S
-    d2h = 4 * 2 * T * Cd + 4 * 9 * 64 + u.nbytes
     line = {
         "metric": METRIC, "value": e2e, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * e2e_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -706,13 +764,13 @@ def run_rmppi(args, ws, rank, local):
         "config": config_of(wl, ws), "host_iterated": True,
         "iters_per_s": args.steps / e2e_s,
         "kernel_ms": {"sampler": kms[0], "rollout": kms[1], "update": kms[2]},
-        "roofline": {"bound": "hbm", "kernel": "rmppi_rollout_kernel (one thread per sample, latency-bound chain)",
+        "roofline": {"bound": "hbm", "kernel": kname,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes": abytes},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "iters_per_s": ws * args.steps / e2e_s},
-        # the solve's kernels plus the update's sampler, candidate evaluation and counter bump
-        "gpu_launches": (ctrl.kernelsPerCompute() + 3) * args.steps,
+        # the solve's kernels, plus for R-MPPI the update's sampler, candidate evaluation and counter bump
+        "gpu_launches": (ctrl.kernelsPerCompute() + (0 if tube else 3)) * args.steps,
     }
     if clk:
         line["clocks"] = clk
@@ -759,8 +817,8 @@ def main():
     if args.impl == "reference":
         run_reference(args, ws, rank)
         return
-    if args.workload == "cartpole_rmppi":
-        run_rmppi(args, ws, rank, local)
+    if args.workload in ("cartpole_rmppi", "cartpole_tube"):
+        run_host_iterated(args, ws, rank, local)
         return
     run_gpu(args, ws, rank, local)
 

@@ -15,6 +15,8 @@
 * ``cartpole_rmppi`` — the robust controller (R-MPPI) on the cart-pole of ``cartpole``: two distributions of K=2048
   samples, T=100, 9 candidate nominal states with 64 evaluation samples each, value-function threshold 1000, the DDP
   feedback with identity weights; one iteration = the importance-sampler update + the solve.
+* ``cartpole_tube`` — Tube-MPPI on the same cart-pole: two distributions of K=2048 samples, T=100, nominal threshold
+  20, the DDP feedback with identity weights; one iteration = the solve + the feedback gains + a one-step slide.
 
 There is no public dataset behind these configurations; every input is drawn from a recorded seed.
 """
@@ -28,7 +30,7 @@ from .controller import (BatchedMPPIController, BicycleDynamics, BicycleSlipMLPD
                          CartpoleSwingupCost,
                          ColoredNoiseDistribution, CostmapCost, DDPFeedback, DoubleIntegratorDynamics,
                          DoubleIntegratorObstacleCost, GaussianDistribution, RobustMPPIController,
-                         VanillaMPPIController)
+                         TubeMPPIController, VanillaMPPIController)
 
 
 @dataclass
@@ -83,6 +85,23 @@ def cartpole_rmppi(seed: int = 0, K: int = 2048, T: int = 100, num_candidates: i
                     dict(model="cartpole", controller="R-MPPI", K=K, T=T, candidates=num_candidates,
                          eval_samples=eval_samples, threshold=1000.0, sigma=1.0, lam=1.0, dt=0.02, seed=seed),
                     eval_sample_steps=num_candidates * eval_samples * T)
+
+
+def cartpole_tube(seed: int = 0, K: int = 2048, T: int = 100, stream: int = 0,
+                  describe_only: bool = False) -> Workload:
+    rng = np.random.default_rng(seed)
+    dyn = CartpoleDynamics(1.0, 1.0, 1.0, 9.81)
+    dyn.setControlRanges([(-5.0, 5.0)])
+    cost = CartpoleSwingupCost(10.0, 1.0, 100.0, 1.0, 0.0)
+    ctrl = None
+    if not describe_only:
+        ctrl = TubeMPPIController(dyn, cost, DDPFeedback(dyn, 0.02), GaussianDistribution(std_dev=(1.0,)), 0.02, 1,
+                                  1.0, 0.0, T, K, stream=stream, seed=seed, nominal_threshold=20.0)
+    x0 = np.array([rng.uniform(-0.1, 0.1), rng.uniform(-0.1, 0.1), rng.uniform(-np.pi, np.pi),
+                   rng.uniform(-0.1, 0.1)], dtype=np.float32)
+    return Workload(f"cartpole_tube_K{K}x2_T{T}", ctrl, x0, np.array([K, K]), np.array([T, T]), 4, 1, 1,
+                    dict(model="cartpole", controller="Tube-MPPI", K=K, T=T, nominal_threshold=20.0, sigma=1.0,
+                         lam=1.0, dt=0.02, seed=seed))
 
 
 def batched_di_params(seed: int = 0, num_instances: int = 256):

@@ -69,3 +69,24 @@ def test_reference_arm_runs_on_rank_zero_only(capsys):
 
     bench.run_reference(Args, ws=2, rank=1)
     assert capsys.readouterr().out == ""
+
+
+@pytest.mark.parametrize("workload,per_iter", [("cartpole_rmppi", 2 * 2048 * 100 + 9 * 64 * 100),
+                                               ("cartpole_tube", 2 * 2048 * 100)])
+def test_reference_arm_of_the_host_iterated_controllers(capsys, workload, per_iter):
+    """The R-MPPI and Tube-MPPI workloads' reference arm: one line on rank 0 with the workload's config, its sample
+    steps per iteration and a CPU sample of the oracle's iteration."""
+    import json
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    class Args:
+        steps, warmup, cpu_seconds, instances, precision = 1, 0, 0.1, 256, None
+
+    Args.workload = workload
+    bench.run_reference(Args, ws=1, rank=0)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["config"]["workload"].startswith(workload) and line["config"]["sample_steps_per_iter"] == per_iter
+    assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
